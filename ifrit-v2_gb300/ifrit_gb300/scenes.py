@@ -1,0 +1,236 @@
+"""Seeded synthetic scenes and cameras.
+
+The reference's benchmark assets (bunny, sponza, character models) are not shipped with
+it, so every workload here is generated: icospheres with radial jitter, log-normal
+triangle soups, value-noise textures and random cameras, all from numpy's PCG64 so the
+same seed gives the same bytes on x86 and Arm hosts.
+
+Conventions (shared with the renderer): clip = M @ (x, y, z, 1) with M row-major;
+NDC z in [0, 1] (near plane at 0); pixel x = (x_ndc * 0.5 + 0.5) * W and
+pixel y = (y_ndc * 0.5 + 0.5) * H, so NDC y = -1 is image row 0.
+"""
+import math
+
+import numpy as np
+
+# ----------------------------------------------------------------------------- cameras
+
+
+def perspective(fovy_deg, aspect, near, far):
+    """Right-handed perspective projection with a [0, 1] depth range."""
+    f = 1.0 / math.tan(math.radians(fovy_deg) / 2.0)
+    m = np.zeros((4, 4), np.float64)
+    m[0, 0] = f / aspect
+    m[1, 1] = f
+    m[2, 2] = far / (near - far)
+    m[2, 3] = near * far / (near - far)
+    m[3, 2] = -1.0
+    return m
+
+
+def look_at(eye, target, up=(0.0, 1.0, 0.0)):
+    eye, target, up = (np.asarray(a, np.float64) for a in (eye, target, up))
+    f = target - eye
+    f /= np.linalg.norm(f)
+    s = np.cross(f, up)
+    s /= np.linalg.norm(s)
+    u = np.cross(s, f)
+    m = np.eye(4)
+    m[0, :3], m[1, :3], m[2, :3] = s, u, -f
+    m[:3, 3] = -m[:3, :3] @ eye
+    return m
+
+
+def orbit_camera(rng, distance, aspect, fovy=60.0, near=0.1, far=100.0):
+    """Random viewing direction on a sphere of radius `distance` looking at the origin."""
+    v = rng.normal(size=3)
+    v /= np.linalg.norm(v)
+    up = (0.0, 1.0, 0.0) if abs(v[1]) < 0.95 else (1.0, 0.0, 0.0)
+    return (perspective(fovy, aspect, near, far) @ look_at(v * distance, (0, 0, 0), up)).astype(np.float32)
+
+
+def default_mvp(aspect=1.0):
+    """Perspective fov 60 deg, camera at distance 3 on +z looking at the origin."""
+    return (perspective(60.0, aspect, 0.1, 100.0) @ look_at((0, 0, 3), (0, 0, 0))).astype(np.float32)
+
+
+# ----------------------------------------------------------------------------- meshes
+
+
+def icosphere(subdivisions):
+    """Unit icosphere: (vertices (V,3) float64, faces (T,3) int32), outward CCW winding."""
+    t = (1.0 + 5.0 ** 0.5) / 2.0
+    verts = [(-1, t, 0), (1, t, 0), (-1, -t, 0), (1, -t, 0), (0, -1, t), (0, 1, t), (0, -1, -t), (0, 1, -t),
+             (t, 0, -1), (t, 0, 1), (-t, 0, -1), (-t, 0, 1)]
+    faces = [(0, 11, 5), (0, 5, 1), (0, 1, 7), (0, 7, 10), (0, 10, 11), (1, 5, 9), (5, 11, 4), (11, 10, 2),
+             (10, 7, 6), (7, 1, 8), (3, 9, 4), (3, 4, 2), (3, 2, 6), (3, 6, 8), (3, 8, 9), (4, 9, 5), (2, 4, 11),
+             (6, 2, 10), (8, 6, 7), (9, 8, 1)]
+    verts = [np.array(v, np.float64) / np.linalg.norm(v) for v in verts]
+    for _ in range(subdivisions):
+        cache = {}
+        new_faces = []
+
+        def mid(a, b):
+            key = (min(a, b), max(a, b))
+            if key not in cache:
+                m = verts[a] + verts[b]
+                verts.append(m / np.linalg.norm(m))
+                cache[key] = len(verts) - 1
+            return cache[key]
+
+        for a, b, c in faces:
+            ab, bc, ca = mid(a, b), mid(b, c), mid(c, a)
+            new_faces += [(a, ab, ca), (b, bc, ab), (c, ca, bc), (ab, bc, ca)]
+        faces = new_faces
+    v = np.array(verts)
+    f = np.array(faces, np.int32)
+    # enforce outward winding: (b - a) x (c - a) points away from the centre
+    n = np.cross(v[f[:, 1]] - v[f[:, 0]], v[f[:, 2]] - v[f[:, 0]])
+    flip = np.einsum("ij,ij->i", n, v[f].mean(axis=1)) < 0
+    f[flip] = f[flip][:, [0, 2, 1]]
+    return v, f
+
+
+def jittered_icosphere(subdivisions, seed, jitter=0.02):
+    """Icosphere with uniform radial jitter +-jitter and per-vertex RGB in [0, 1].
+
+    Returns (vertices (V,6) float32 [x y z r g b], indices (T,3) int32)."""
+    rng = np.random.default_rng(seed)
+    v, f = icosphere(subdivisions)
+    r = 1.0 + rng.uniform(-jitter, jitter, size=(len(v), 1))
+    col = rng.uniform(0.0, 1.0, size=(len(v), 3))
+    return np.concatenate([v * r, col], axis=1).astype(np.float32), f
+
+
+def geodesic_sphere(frequency, seed, displacement=0.05):
+    """Class-I geodesic icosphere of the given frequency (20 * f^2 triangles), radially
+    displaced by value noise on the sphere.  Returns (positions (V,3), uv (V,2), indices)."""
+    rng = np.random.default_rng(seed)
+    base_v, base_f = icosphere(0)
+    verts = {}
+    out_v = []
+    faces = []
+
+    def vid(key, p):
+        if key not in verts:
+            verts[key] = len(out_v)
+            out_v.append(p)
+        return verts[key]
+
+    n = frequency
+    for a, b, c in base_f:
+        A, B, C = base_v[a], base_v[b], base_v[c]
+        ids = {}
+        for i in range(n + 1):
+            for j in range(n + 1 - i):
+                k = n - i - j
+                p = (A * k + B * i + C * j) / n
+                # canonical key shared along edges between base faces
+                key = tuple(sorted(((a, k), (b, i), (c, j)), key=lambda x: x[0]))
+                key = tuple((vv, w) for vv, w in key if w != 0)
+                ids[(i, j)] = vid(key, p / np.linalg.norm(p))
+        for i in range(n):
+            for j in range(n - i):
+                faces.append((ids[(i, j)], ids[(i + 1, j)], ids[(i, j + 1)]))
+                if j < n - i - 1:
+                    faces.append((ids[(i + 1, j)], ids[(i + 1, j + 1)], ids[(i, j + 1)]))
+    v = np.array(out_v)
+    f = np.array(faces, np.int32)
+    nrm = np.cross(v[f[:, 1]] - v[f[:, 0]], v[f[:, 2]] - v[f[:, 0]])
+    flip = np.einsum("ij,ij->i", nrm, v[f].mean(axis=1)) < 0
+    f[flip] = f[flip][:, [0, 2, 1]]
+    # smooth radial displacement from a few random spherical waves
+    k = rng.normal(size=(6, 3)) * 4.0
+    ph = rng.uniform(0, 2 * np.pi, size=6)
+    disp = np.sin(v @ k.T + ph).mean(axis=1)
+    v = v * (1.0 + displacement * disp)[:, None]
+    uv = np.stack([0.5 + np.arctan2(v[:, 2], v[:, 0]) / (2 * np.pi), 0.5 + np.arcsin(np.clip(v[:, 1] / np.linalg.norm(v, axis=1), -1, 1)) / np.pi], 1)
+    return v.astype(np.float32), uv.astype(np.float32), f
+
+
+def triangle_soup(num_tris, seed, width, height, fovy=60.0, median_px=4.0, sigma=1.0, near=0.5, far=20.0,
+                  area_scale=1.0, uv_density=(0.5, 4.0), max_stretch=8.0):
+    """Unshared random triangles with centres uniform (by volume) in the view frustum and
+    edge lengths log-normal in pixels at the centre's depth.  Each vertex carries a UV from
+    a random anisotropic affine map of its screen position.
+
+    Returns (vertices (3T,5) float32 [x y z u v] in view space, indices (T,3), mvp)."""
+    rng = np.random.default_rng(seed)
+    aspect = width / height
+    th = math.tan(math.radians(fovy) / 2)
+    # depth with pdf ~ d^2 on [near, far]
+    u = rng.uniform(size=num_tris)
+    d = (near ** 3 + u * (far ** 3 - near ** 3)) ** (1.0 / 3.0)
+    xn = rng.uniform(-1, 1, num_tris)
+    yn = rng.uniform(-1, 1, num_tris)
+    centre = np.stack([xn * d * th * aspect, yn * d * th, -d], 1)
+    px_world = 2.0 * d * th / height  # world size of one pixel at depth d
+    L = median_px * np.exp(sigma * rng.normal(size=num_tris)) * area_scale
+    # three vertices around the centre in a random plane roughly facing the camera
+    ang = rng.uniform(0, 2 * np.pi, size=(num_tris, 1)) + np.array([[0.0, 2.0944, 4.18879]]) + \
+        rng.uniform(-0.5, 0.5, size=(num_tris, 3))
+    rad = (L / math.sqrt(3.0))[:, None] * rng.uniform(0.6, 1.2, size=(num_tris, 3))
+    off = np.stack([np.cos(ang) * rad, np.sin(ang) * rad, rng.uniform(-0.3, 0.3, size=(num_tris, 3)) * rad], 2)
+    pos = centre[:, None, :] + off * px_world[:, None, None]
+    # UV: random anisotropic affine map of the in-plane offset (in pixels)
+    dens = np.exp(rng.uniform(np.log(uv_density[0]), np.log(uv_density[1]), num_tris)) / 1024.0
+    stretch = np.exp(rng.uniform(0, np.log(max_stretch), num_tris))
+    rot = rng.uniform(0, np.pi, num_tris)
+    c, s = np.cos(rot), np.sin(rot)
+    m00, m01 = c * dens * stretch, -s * dens
+    m10, m11 = s * dens * stretch, c * dens
+    base = rng.uniform(0, 1, size=(num_tris, 2))
+    ox, oy = off[..., 0], off[..., 1]
+    uu = base[:, 0:1] + m00[:, None] * ox + m01[:, None] * oy
+    vv = base[:, 1:2] + m10[:, None] * ox + m11[:, None] * oy
+    verts = np.concatenate([pos.reshape(-1, 3), np.stack([uu, vv], 2).reshape(-1, 2)], 1).astype(np.float32)
+    idx = np.arange(3 * num_tris, dtype=np.int32).reshape(-1, 3)
+    mvp = perspective(fovy, aspect, 0.1, 100.0).astype(np.float32)
+    return verts, idx, mvp
+
+
+def soup_depth_complexity(verts, idx, mvp, width, height):
+    """Sum of projected triangle areas over the screen area (no culling, no clipping)."""
+    p = verts[:, :3].astype(np.float64)
+    clip = np.concatenate([p, np.ones((len(p), 1))], 1) @ mvp.astype(np.float64).T
+    xy = clip[:, :2] / clip[:, 3:4]
+    sx = (xy[:, 0] * 0.5 + 0.5) * width
+    sy = (xy[:, 1] * 0.5 + 0.5) * height
+    a, b, c = idx[:, 0], idx[:, 1], idx[:, 2]
+    area = 0.5 * np.abs((sx[b] - sx[a]) * (sy[c] - sy[a]) - (sx[c] - sx[a]) * (sy[b] - sy[a]))
+    return float(area.sum() / (width * height))
+
+
+# ----------------------------------------------------------------------------- textures
+
+
+def value_noise_texture(size, seed, octaves=5):
+    """Seeded multi-octave value noise, RGBA8 packed as uint32 (h, w), alpha 255."""
+    rng = np.random.default_rng(seed)
+    img = np.zeros((size, size, 3), np.float64)
+    amp, total = 1.0, 0.0
+    for o in range(octaves):
+        cells = 4 * (2 ** o)
+        lat = rng.uniform(0, 1, size=(cells + 1, cells + 1, 3))
+        lat[-1, :, :] = lat[0, :, :]
+        lat[:, -1, :] = lat[:, 0, :]
+        t = (np.arange(size) + 0.5) / size * cells
+        i0 = np.floor(t).astype(int)
+        f = t - i0
+        f = f * f * (3 - 2 * f)
+        i1 = i0 + 1
+        fy, fx = f[:, None, None], f[None, :, None]
+        v = (lat[i0][:, i0] * (1 - fx) * (1 - fy) + lat[i0][:, i1] * fx * (1 - fy) +
+             lat[i1][:, i0] * (1 - fx) * fy + lat[i1][:, i1] * fx * fy)
+        img += amp * v
+        total += amp
+        amp *= 0.55
+    img = np.clip(np.round(img / total * 255.0), 0, 255).astype(np.uint32)
+    return img[..., 0] | (img[..., 1] << 8) | (img[..., 2] << 16) | (np.uint32(255) << 24)
+
+
+def c1_scene(seed=1):
+    """20,480-triangle icosphere (subdivision 5) with +-2% radial jitter and per-vertex RGB,
+    perspective fov 60 deg at distance 3 (512x512 target in the benchmark)."""
+    v, f = jittered_icosphere(5, seed)
+    return v, f, default_mvp(1.0)
