@@ -1,0 +1,328 @@
+"""Benchmark of the GB300 software rasterizer (one JSON line on rank 0).
+
+Workload (default ``c2``): 1,000,000 unshared random triangles (centres uniform in the view
+frustum, log-normal edges, depth complexity ~6), each vertex with a float32 UV; 1920x1080
+RGBA8 target with 4x MSAA and float32 depth (LEQUAL); shading samples a seeded 1024x1024
+RGBA8 value-noise texture with a full mip chain, trilinear + 8x anisotropic filtering from
+quad derivatives.  ``c1`` is the plain 512x512 Gouraud icosphere frame.
+
+A step is one render pass (binning, raster, shading, resolve) of the whole frame.
+  value      shaded samples/s with geometry and texture resident in HBM; L2 is flushed
+             (256 MB write) before every timed step; per-step device time from CUDA events.
+  e2e        the same metric through the reference-style C-ABI with host buffers: each step
+             uploads the pinned vertex + index buffers (marked rewritten), draws
+             synchronously (iftrDrawLegacy) and reads the resolved colour back to pinned host
+             memory; host wall time.
+  roofline   the tile kernel (the dominant kernel) against measured HBM bandwidth.
+  cpu_baseline  the multithreaded CPU oracle (a port of the reference's CPU pipeline with
+             this path's MSAA and texturing) on one full frame, rank 0 only.
+
+``--impl reference`` times the reference-side CPU implementation of the path on the host
+cores instead (the reference's own CPU renderer has no MSAA or texturing, so the port
+stands in for it on this workload).  Multi-GPU runs render independent replicas (the frame
+does not shard), report ``scaling: weak`` and take the max time over ranks.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+for _p in (ROOT, os.path.join(ROOT, "ifrit-v2_gb300")):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+import numpy as np  # noqa: E402
+
+METRIC = "shaded samples/s"
+L2_FLUSH_BYTES = 256 << 20
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=20)
+    p.add_argument("--warmup", type=int, default=5)
+    p.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    p.add_argument("--workload", default="c2", choices=["c1", "c2"])
+    p.add_argument("--e2e-steps", type=int, default=10)
+    return p.parse_args()
+
+
+def workload(name):
+    from ifrit_gb300 import scenes
+    if name == "c1":
+        v, f, mvp = scenes.c1_scene(1)
+        return dict(name="c1", vertices=v, indices=f, mvp=mvp, W=512, H=512, S=1, attr=3, texture=None,
+                    aniso=1, cull=2, shading=0, depth_func=3,
+                    desc="plain frame: 20,480-triangle icosphere (subdivision 5, +-2% radial jitter, per-vertex "
+                         "RGB), fov 60 at distance 3, 512x512 RGBA8 + D32 LEQUAL, 1x, back-face culling, Gouraud")
+    v, f, mvp = scenes.c2_scene()
+    tex = scenes.value_noise_texture(1024, 2)
+    return dict(name="c2", vertices=v, indices=f, mvp=mvp, W=1920, H=1080, S=4, attr=2, texture=tex, aniso=8,
+                cull=0, shading=1, depth_func=3,
+                desc="1M random triangles (log-normal edges, median 4 px, sigma 1, depth complexity 5.9), "
+                     "1920x1080 RGBA8 + D32 LEQUAL, 4x MSAA, 1024^2 RGBA8 value-noise texture with full mips, "
+                     "trilinear + 8x anisotropic")
+
+
+def algorithmic_bytes(w):
+    """Compulsory bytes of one frame: vertices + indices read once, per-sample depth and
+    resolved colour written once, the texture's full mip chain read once."""
+    P = w["W"] * w["H"]
+    tex = 0
+    if w["texture"] is not None:
+        th, tw = w["texture"].shape
+        total, ww, hh = 0, tw, th
+        while True:
+            total += ww * hh
+            if ww == 1 and hh == 1:
+                break
+            ww, hh = (ww + 1) >> 1, (hh + 1) >> 1
+        tex = total * 4
+    return int(w["vertices"].nbytes + w["indices"].nbytes + P * w["S"] * 4 + P * 4 + tex)
+
+
+def peak_hbm():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def profiled_traffic(name):
+    """dram bytes per tile-kernel launch from the committed ncu summary, if present."""
+    path = os.path.join(ROOT, "profiles", "tile_kernel_%s.txt" % name)
+    try:
+        for line in open(path):
+            if line.startswith("traffic_bytes_per_launch:"):
+                return int(float(line.split(":", 1)[1].strip()))
+    except OSError:
+        pass
+    return None
+
+
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self):
+        self.proc = None
+        self.path = os.path.join("/tmp", "ifrit_clocks_%d.csv" % os.getpid())
+
+    def start(self):
+        try:
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "--query-gpu=" + self.FIELDS, "--format=csv,noheader,nounits",
+                                          "-lms", "200"], stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self, device_index=0):
+        if not self.proc:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.f.close()
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9 or parts[0] != str(device_index):
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax = float(parts[2])
+            except ValueError:
+                continue
+            for n, val in zip(names, parts[5:9]):
+                if val.lower() == "active":
+                    reasons.add(n)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": smax, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_oracle_frame(w, nthreads, frames=1):
+    """Times the multithreaded CPU oracle on full frames; returns (seconds per frame, samples)."""
+    from oracle import oracle as O
+    tex_arg = None
+    if w["texture"] is not None:
+        chain, levels = O.build_mips(w["texture"])
+        tex_arg = (chain, levels, w["texture"].shape[1], w["texture"].shape[0])
+    d = O.make_draw(w["vertices"], w["indices"], w["mvp"], attr_offset=3, attr_count=w["attr"], cull_mode=w["cull"],
+                    depth_func=w["depth_func"], shading=w["shading"], texture=tex_arg,
+                    sampler={"max_aniso": w["aniso"]})
+    times, shaded = [], 0
+    for _ in range(frames):
+        t0 = time.perf_counter()
+        out = O.render([d], w["W"], w["H"], w["S"], nthreads=nthreads)
+        times.append(time.perf_counter() - t0)
+        shaded = int((out["vis"] >= 0).sum())
+    return statistics.median(times), shaded
+
+
+def dist_setup(n):
+    if n <= 1 or int(os.environ.get("WORLD_SIZE", "1")) <= 1:
+        return 0, 1, None
+    import torch
+    import torch.distributed as dist
+    rank, world = int(os.environ["RANK"]), int(os.environ["WORLD_SIZE"])
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    dist.init_process_group("nccl")
+    return rank, world, dist
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    w = workload(args.workload)
+    nthreads = os.cpu_count() or 1
+    for _ in range(args.warmup):
+        cpu_oracle_frame(w, nthreads)
+    times, shaded = [], 0
+    for _ in range(args.steps):
+        t, shaded = cpu_oracle_frame(w, nthreads)
+        times.append(t)
+    ms = 1000.0 * statistics.mean(times)
+    value = shaded / (ms / 1000.0)
+    line = {
+        "metric": METRIC, "value": value, "unit": "samples/s", "impl": "reference", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32+i64", "data": "synthetic (seeded)",
+        "config": {"workload": w["desc"], "width": w["W"], "height": w["H"], "samples": w["S"],
+                   "triangles": int(len(w["indices"]))},
+        "tris_per_s": len(w["indices"]) / (ms / 1000.0),
+        "cpu_baseline": {"value": value, "unit": "samples/s", "cores": nthreads, "kind": "port",
+                         "sample": "one full frame per step (the reference CPU renderer has no MSAA or texturing; "
+                                   "its multithreaded CPU pipeline is run as the oracle port)"},
+        "e2e": {"value": value, "unit": "samples/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args):
+    import torch
+    import ifrit_gb300 as ig
+
+    rank, world, dist = dist_setup(args.gpus)
+    dev = torch.device("cuda", torch.cuda.current_device())
+    w = workload(args.workload)
+    r = ig.Renderer(w["W"], w["H"], w["S"], ig.FORMAT_RGBA8, visibility=True)
+    stream = torch.cuda.current_stream(dev)
+    r.set_stream(stream.cuda_stream)
+    r.set_state(cull=w["cull"], depth_func=w["depth_func"], shading=w["shading"])
+    r.set_mvp(w["mvp"])
+    r.set_geometry(w["vertices"], w["indices"], w["attr"])
+    if w["texture"] is not None:
+        r.set_texture(w["texture"], max_aniso=w["aniso"])
+    # settle scratch capacity and count the shaded samples of this frame
+    r.draw(clear=True)
+    shaded = int((r.visibility() >= 0).sum())
+    r.lib.iftrSetVisibilityOutput(r.h, 0)
+    r.set_stage_timing(True)
+    flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device=dev)
+    for _ in range(args.warmup):
+        flush.fill_(1)
+        r.draw_async(clear=True)
+        r.finish()
+    ev0 = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ev1 = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    tile_ms, bin_ms = [], []
+    clocks = ClockSampler()
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    clocks.start()
+    for i in range(args.steps):
+        flush.fill_(i & 255)
+        ev0[i].record(stream)
+        r.draw_async(clear=True)
+        ev1[i].record(stream)
+        r.finish()
+        st = r.stage_times()
+        bin_ms.append(st[0] + st[1] + st[2])
+        tile_ms.append(st[3])
+    torch.cuda.synchronize()
+    clk = clocks.stop(torch.cuda.current_device())
+    step_ms = [a.elapsed_time(b) for a, b in zip(ev0, ev1)]
+    ms = statistics.mean(step_ms)
+    if dist:
+        t = torch.tensor([ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+
+    # end to end through the C-ABI with host buffers
+    r.set_stage_timing(False)
+    out = torch.empty(w["W"] * w["H"], dtype=torch.int32, pin_memory=True).numpy()
+    e2e_times = []
+    for i in range(args.e2e_steps + 2):
+        t0 = time.perf_counter()
+        r.mark_geometry_dirty()
+        r.draw(clear=True)
+        r.color_into(out)
+        if i >= 2:
+            e2e_times.append(time.perf_counter() - t0)
+    e2e_s = statistics.mean(e2e_times)
+    if dist:
+        t = torch.tensor([e2e_s], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    if rank != 0:
+        dist.barrier()
+        return
+
+    B = algorithmic_bytes(w)
+    peak, peak_kind = peak_hbm()
+    t_tile = statistics.mean(tile_ms) / 1000.0
+    achieved = B / t_tile / 1e9
+    line = {
+        "metric": METRIC, "value": world * shaded / (ms / 1000.0), "unit": "samples/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32+i64", "data": "synthetic (seeded)",
+        "config": {"workload": w["desc"], "width": w["W"], "height": w["H"], "samples": w["S"],
+                   "triangles": int(len(w["indices"])), "shaded_samples_per_frame": shaded,
+                   "l2": "flushed before every timed step (256 MB write)",
+                   "parallelism": "replicas" if world > 1 else "single"},
+        "tris_per_s": world * len(w["indices"]) / (ms / 1000.0),
+        "stage_ms": {"binning": statistics.mean(bin_ms), "tile": statistics.mean(tile_ms)},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": profiled_traffic(w["name"]), "algorithmic_bytes": B, "kernel": "tile_kernel",
+                     "peak_source": peak_kind},
+        "pass_roofline_frac": B / (ms / 1000.0) / 1e9 / peak,
+        "e2e": {"value": world * shaded / e2e_s, "unit": "samples/s",
+                "h2d_bytes_per_step": int(w["vertices"].nbytes + w["indices"].nbytes),
+                "d2h_bytes_per_step": int(out.nbytes), "ms_per_step": 1000.0 * e2e_s},
+        "gpu_launches": 4 * args.steps,
+        "clocks": clk,
+    }
+    nthreads = os.cpu_count() or 1
+    t_cpu, shaded_cpu = cpu_oracle_frame(w, nthreads, frames=2)
+    line["cpu_baseline"] = {"value": shaded_cpu / t_cpu, "unit": "samples/s", "cores": nthreads, "kind": "port",
+                            "sample": "one full frame of the same workload (median of 2)"}
+    print(json.dumps(line), flush=True)
+    if dist:
+        dist.barrier()
+    r.close()
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

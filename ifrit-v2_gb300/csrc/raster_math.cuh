@@ -1,0 +1,520 @@
+// Device arithmetic of the GB300 triangle pipeline.
+//
+// Every function here is the sm_103a form of one stage of the soft renderer
+// (Aeroraven/Ifrit-v2 projects/softgraphics): vertex transform (TileRasterWorker.cpp:432-476),
+// homogeneous clipping (TileRasterWorker.cpp:136-277, TileRasterCoreInvocationCuda.cu:1342-1400),
+// culling and setup (TileRasterWorker.cpp:503-727, TileRasterCoreInvocationCuda.cu:1549-1644),
+// coverage (TileRasterCoreInvocationCuda.cu:891-982), depth (TileRasterWorker.cpp:2244-2386),
+// perspective interpolation with quad derivatives (TileRasterCoreInvocationCuda.cu:2144-2317,
+// ShaderBuiltinCuda.cuh:36-94), texture sampling (ShaderBuiltinCuda.cuh:96-272) and blending
+// (TileRasterWorker.cpp:2346-2373).
+//
+// Bit-exactness contract: coverage is integer (16.8 fixed-point vertices, 64-bit edge
+// functions, top-left fill rule); every float expression is evaluated in one fixed order with
+// IEEE round-to-nearest and no contraction (the library is compiled with --fmad=false, and
+// division/sqrt are the IEEE ones), so the CPU checker reproduces every bit.
+#pragma once
+#include <cstdint>
+
+namespace ifr {
+
+constexpr float kWEps = 1e-5f;
+constexpr int kMaxPoly = 10;
+constexpr float kSnapLimit = 8000000.0f;
+constexpr float kInv255 = 0x1.010102p-8f;
+
+enum { FMT_RGBA8 = 0, FMT_RGBA16F = 1, FMT_RGBA32F = 2, FMT_RGB32F = 3 };
+enum { SHADE_GOURAUD = 0, SHADE_TEXTURED = 1, SHADE_PRIMID = 2 };
+
+struct SamplerDev {
+    int address_u, address_v, filter, border_white, max_aniso;
+    float lod_bias;
+};
+
+// One draw of a render pass, as the kernels see it (device pointers).
+struct DrawDev {
+    const float* vertices;
+    int stride, num_vertices, attr_offset, attr_count;
+    const int* indices;
+    int num_triangles, prim_base;
+    float mvp[16];
+    int cull_mode, front_ccw, depth_func, depth_write;
+    int blend_enable, blend_src_color, blend_dst_color, blend_src_alpha, blend_dst_alpha;
+    int shading;
+    const uint32_t* texels;
+    int tex_w, tex_h, tex_levels;
+    SamplerDev sampler;
+};
+
+// Pass-wide constants.
+struct PassConst {
+    int W, H, S;
+    int tiles_x, tiles_y;
+    int sx[16], sy[16];
+    int smin_x, smax_x, smin_y, smax_y;
+    int shade_x, shade_y;
+    float W256, H256, gx, gy;
+};
+
+struct CVert {
+    float p[4];
+    float b[3];
+};
+
+// A set-up (sub-)triangle: snapped vertices, edge functions, depth plane, pixel bbox.
+struct SubTri {
+    int32_t X[3], Y[3];
+    float z[3], iw[3];
+    float bary[3][3];
+    int32_t A[3], B[3];
+    int64_t C[3], Cb[3];
+    float dzdx, dzdy;
+    int px0, px1, py0, py1;
+};
+
+__device__ __forceinline__ int64_t floordiv256(int64_t a) { return a >= 0 ? a / 256 : -((-a + 255) / 256); }
+__device__ __forceinline__ int64_t ceildiv256(int64_t a) { return -floordiv256(-a); }
+
+__device__ __forceinline__ void xform(const float* m, const float* v, float out[4]) {
+    float x = __ldg(v), y = __ldg(v + 1), z = __ldg(v + 2);
+#pragma unroll
+    for (int r = 0; r < 4; r++) out[r] = m[4 * r + 0] * x + m[4 * r + 1] * y + m[4 * r + 2] * z + m[4 * r + 3];
+}
+
+__device__ __forceinline__ float plane_dist(const PassConst& c, int plane, const float* p) {
+    switch (plane) {
+    case 0: return p[3] - kWEps;
+    case 1: return p[2];
+    case 2: return p[3] - p[2];
+    case 3: return c.gx * p[3] - p[0];
+    case 4: return c.gx * p[3] + p[0];
+    case 5: return c.gy * p[3] - p[1];
+    default: return c.gy * p[3] + p[1];
+    }
+}
+
+// Sutherland-Hodgman against the 7 planes (w >= eps, 0 <= z <= w, x/y guard band) in fixed order.
+static __device__ __noinline__ int clip_polygon(const PassConst& c, CVert* poly) {
+    int n = 3;
+    CVert tmp[kMaxPoly];
+    for (int pl = 0; pl < 7; pl++) {
+        bool all_in = true, all_out = true;
+        for (int i = 0; i < n; i++) {
+            float d = plane_dist(c, pl, poly[i].p);
+            if (d >= 0.0f) all_out = false; else all_in = false;
+        }
+        if (all_out) return 0;
+        if (all_in) continue;
+        int m = 0;
+        for (int i = 0; i < n; i++) {
+            const CVert a = poly[i];
+            const CVert b = poly[(i + 1) % n];
+            float da = plane_dist(c, pl, a.p), db = plane_dist(c, pl, b.p);
+            if (da >= 0.0f) tmp[m++] = a;
+            if ((da >= 0.0f) != (db >= 0.0f)) {
+                float t = da / (da - db);
+                CVert q;
+#pragma unroll
+                for (int k = 0; k < 4; k++) q.p[k] = a.p[k] + t * (b.p[k] - a.p[k]);
+#pragma unroll
+                for (int k = 0; k < 3; k++) q.b[k] = a.b[k] + t * (b.b[k] - a.b[k]);
+                tmp[m++] = q;
+            }
+        }
+        n = m;
+        if (n < 3) return 0;
+        for (int i = 0; i < n; i++) poly[i] = tmp[i];
+    }
+    return n;
+}
+
+// Projection, 16.8 snap, cull, orientation normalisation, edge functions, depth plane and
+// the pixel range that may hold covered samples.  Returns false when nothing can be covered.
+__device__ __forceinline__ bool setup_sub(const PassConst& c, const DrawDev& d, const CVert& v0, const CVert& v1,
+                                          const CVert& v2, SubTri& o) {
+    const CVert* v[3] = {&v0, &v1, &v2};
+#pragma unroll
+    for (int i = 0; i < 3; i++) {
+        float iw = 1.0f / v[i]->p[3];
+        float xn = v[i]->p[0] * iw, yn = v[i]->p[1] * iw, zn = v[i]->p[2] * iw;
+        float fx = (xn * 0.5f + 0.5f) * c.W256;
+        float fy = (yn * 0.5f + 0.5f) * c.H256;
+        fx = fminf(fmaxf(fx, -kSnapLimit), kSnapLimit);
+        fy = fminf(fmaxf(fy, -kSnapLimit), kSnapLimit);
+        o.X[i] = __float2int_rn(fx);
+        o.Y[i] = __float2int_rn(fy);
+        o.z[i] = zn;
+        o.iw[i] = iw;
+#pragma unroll
+        for (int k = 0; k < 3; k++) o.bary[i][k] = v[i]->b[k];
+    }
+    int64_t a2 = (int64_t)(o.X[1] - o.X[0]) * (o.Y[2] - o.Y[0]) - (int64_t)(o.X[2] - o.X[0]) * (o.Y[1] - o.Y[0]);
+    if (a2 == 0) return false;
+    bool front = d.front_ccw ? (a2 > 0) : (a2 < 0);
+    if (d.cull_mode == 3) return false;
+    if (d.cull_mode == 1 && front) return false;
+    if (d.cull_mode == 2 && !front) return false;
+    if (a2 < 0) {
+        int32_t t;
+        float tf;
+        t = o.X[1]; o.X[1] = o.X[2]; o.X[2] = t;
+        t = o.Y[1]; o.Y[1] = o.Y[2]; o.Y[2] = t;
+        tf = o.z[1]; o.z[1] = o.z[2]; o.z[2] = tf;
+        tf = o.iw[1]; o.iw[1] = o.iw[2]; o.iw[2] = tf;
+#pragma unroll
+        for (int k = 0; k < 3; k++) { tf = o.bary[1][k]; o.bary[1][k] = o.bary[2][k]; o.bary[2][k] = tf; }
+        a2 = -a2;
+    }
+    int32_t xmin = min(o.X[0], min(o.X[1], o.X[2])), xmax = max(o.X[0], max(o.X[1], o.X[2]));
+    int32_t ymin = min(o.Y[0], min(o.Y[1], o.Y[2])), ymax = max(o.Y[0], max(o.Y[1], o.Y[2]));
+    int64_t px0 = ceildiv256((int64_t)xmin - c.smax_x), px1 = floordiv256((int64_t)xmax - c.smin_x);
+    int64_t py0 = ceildiv256((int64_t)ymin - c.smax_y), py1 = floordiv256((int64_t)ymax - c.smin_y);
+    if (px0 < 0) px0 = 0;
+    if (py0 < 0) py0 = 0;
+    if (px1 > c.W - 1) px1 = c.W - 1;
+    if (py1 > c.H - 1) py1 = c.H - 1;
+    if (px0 > px1 || py0 > py1) return false;
+    o.px0 = (int)px0; o.px1 = (int)px1; o.py0 = (int)py0; o.py1 = (int)py1;
+#pragma unroll
+    for (int i = 0; i < 3; i++) {
+        int j = (i + 1) % 3, k = (i + 2) % 3;
+        o.A[i] = o.Y[j] - o.Y[k];
+        o.B[i] = o.X[k] - o.X[j];
+        o.C[i] = (int64_t)(o.Y[k] - o.Y[j]) * o.X[j] - (int64_t)(o.X[k] - o.X[j]) * o.Y[j];
+        bool topleft = (o.A[i] > 0) || (o.A[i] == 0 && o.B[i] > 0);
+        o.Cb[i] = o.C[i] - (topleft ? 0 : 1);
+    }
+    float dX1 = (float)(o.X[1] - o.X[0]), dY1 = (float)(o.Y[1] - o.Y[0]);
+    float dX2 = (float)(o.X[2] - o.X[0]), dY2 = (float)(o.Y[2] - o.Y[0]);
+    float dz1 = o.z[1] - o.z[0], dz2 = o.z[2] - o.z[0];
+    float fa = (float)a2;
+    o.dzdx = (dz1 * dY2 - dz2 * dY1) / fa;
+    o.dzdy = (dz2 * dX1 - dz1 * dX2) / fa;
+    return true;
+}
+
+// Fetch + transform the three vertices of triangle t.  Returns false for invalid indices or
+// non-finite clip coordinates.  Sets `inside` when no clip plane cuts the triangle.
+__device__ __forceinline__ bool fetch_triangle(const PassConst& c, const DrawDev& d, int t, CVert* poly,
+                                               bool& inside, bool& rejected) {
+    inside = true;
+    rejected = false;
+#pragma unroll
+    for (int i = 0; i < 3; i++) {
+        int vid = __ldg(d.indices + 3 * (size_t)t + i);
+        if (vid < 0 || vid >= d.num_vertices) return false;
+        xform(d.mvp, d.vertices + (size_t)vid * d.stride, poly[i].p);
+#pragma unroll
+        for (int k = 0; k < 4; k++)
+            if (!isfinite(poly[i].p[k])) return false;
+#pragma unroll
+        for (int k = 0; k < 3; k++) poly[i].b[k] = (k == i) ? 1.0f : 0.0f;
+    }
+    for (int pl = 0; pl < 7; pl++) {
+        int nin = 0;
+#pragma unroll
+        for (int i = 0; i < 3; i++) nin += plane_dist(c, pl, poly[i].p) >= 0.0f;
+        if (nin == 0) { rejected = true; return false; }
+        if (nin != 3) inside = false;
+    }
+    return true;
+}
+
+// Sets up fan triangle `sub` of triangle t (after clipping).  Returns false if it is culled
+// or absent.
+__device__ __forceinline__ bool setup_triangle_sub(const PassConst& c, const DrawDev& d, int t, int sub, SubTri& o) {
+    CVert poly[kMaxPoly];
+    bool inside, rejected;
+    if (!fetch_triangle(c, d, t, poly, inside, rejected)) return false;
+    if (inside) {
+        if (sub != 0) return false;
+        return setup_sub(c, d, poly[0], poly[1], poly[2], o);
+    }
+    int n = clip_polygon(c, poly);
+    if (sub + 2 >= n) return false;
+    return setup_sub(c, d, poly[0], poly[sub + 1], poly[sub + 2], o);
+}
+
+__device__ __forceinline__ bool covered(const int32_t* A, const int32_t* B, const int64_t* Cb, int32_t x, int32_t y) {
+    bool ok = true;
+#pragma unroll
+    for (int i = 0; i < 3; i++) ok &= (Cb[i] + (int64_t)A[i] * x + (int64_t)B[i] * y) >= 0;
+    return ok;
+}
+
+__device__ __forceinline__ float sample_depth(float z0, float dzdx, float dzdy, int32_t X0, int32_t Y0, int32_t x,
+                                              int32_t y) {
+    return (z0 + dzdx * (float)(x - X0)) + dzdy * (float)(y - Y0);
+}
+
+__device__ __forceinline__ bool depth_cmp(int func, float z, float dd) {
+    switch (func) {
+    case 0: return false;
+    case 1: return z < dd;
+    case 2: return z == dd;
+    case 3: return z <= dd;
+    case 4: return z > dd;
+    case 5: return z != dd;
+    case 6: return z >= dd;
+    default: return true;
+    }
+}
+
+// ------------------------------------------------------------------ log2 (own atanh series)
+// ln(m) = 2*atanh(s), s = (m-1)/(m+1) (Abramowitz & Stegun 4.1.27), m in [sqrt(1/2), sqrt(2)).
+__device__ __forceinline__ float log2_series(float x) {
+    if (!(x > 0.0f)) return -__int_as_float(0x7f800000);
+    if (x == __int_as_float(0x7f800000)) return 128.0f;
+    int e = 0;
+    uint32_t b = __float_as_uint(x);
+    if ((b >> 23) == 0) {
+        x = x * 8388608.0f;
+        b = __float_as_uint(x);
+        e = -23;
+    }
+    e += (int)((b >> 23) & 255u) - 127;
+    float m = __uint_as_float((b & 0x7fffffu) | 0x3f800000u);
+    if (m > 0x1.6a09e6p+0f) {
+        m = m * 0.5f;
+        e = e + 1;
+    }
+    float s = (m - 1.0f) / (m + 1.0f);
+    float s2 = s * s;
+    float p = s2 * 0x1.c71c72p-4f + 0x1.24924ap-3f;
+    p = p * s2 + 0x1.99999ap-3f;
+    p = p * s2 + 0x1.555556p-2f;
+    p = p * s2 + 1.0f;
+    float lnm = (2.0f * s) * p;
+    return (float)e + lnm * 0x1.715476p+0f;
+}
+
+// ------------------------------------------------------------------ textures
+__device__ __forceinline__ void unpack_rgba8(uint32_t t, float c[4]) {
+    c[0] = (float)(t & 255u) * kInv255;
+    c[1] = (float)((t >> 8) & 255u) * kInv255;
+    c[2] = (float)((t >> 16) & 255u) * kInv255;
+    c[3] = (float)(t >> 24) * kInv255;
+}
+
+__device__ __forceinline__ float lerpf_(float a, float b, float t) { return a + t * (b - a); }
+
+__device__ __forceinline__ bool tex_address(int mode, float& c, int n) {
+    float nf = (float)n;
+    float v = c;
+    switch (mode) {
+    case 0:
+        v = fmodf(v, nf);
+        if (v < 0.0f) v = v + nf;
+        break;
+    case 1: {
+        float n2 = nf + nf;
+        v = fmodf(v, n2);
+        if (v < 0.0f) v = v + n2;
+        v = fminf(v, n2 - v);
+        break;
+    }
+    case 3:
+        if (v < 0.0f || v >= nf) return false;
+        break;
+    case 4:
+        v = fabsf(v);
+        v = fminf(v, nf - 1.0f);
+        break;
+    default:
+        v = fmaxf(v, 0.0f);
+        v = fminf(v, nf - 1.0f);
+        break;
+    }
+    if (!(v >= 0.0f)) v = 0.0f;
+    c = v;
+    return true;
+}
+
+__device__ __forceinline__ void tex_level_info(const DrawDev& d, int level, int& w, int& h, int& off) {
+    int ww = d.tex_w, hh = d.tex_h, o = 0;
+    for (int i = 0; i < level; i++) {
+        o += ww * hh;
+        ww = (ww + 1) >> 1;
+        hh = (hh + 1) >> 1;
+    }
+    w = ww;
+    h = hh;
+    off = o;
+}
+
+__device__ __forceinline__ void tex_sample_level(const DrawDev& d, int level, float u, float v, float out[4]) {
+    int w, h, off;
+    tex_level_info(d, level, w, h, off);
+    float cx = u * (float)(w - 1);
+    float cy = v * (float)(h - 1);
+    if (!tex_address(d.sampler.address_u, cx, w) || !tex_address(d.sampler.address_v, cy, h)) {
+        float b = d.sampler.border_white ? 1.0f : 0.0f;
+        out[0] = b; out[1] = b; out[2] = b; out[3] = 1.0f;
+        return;
+    }
+    const uint32_t* t = d.texels + off;
+    if (d.sampler.filter == 0) {
+        int x = min((int)(cx + 0.5f), w - 1), y = min((int)(cy + 0.5f), h - 1);
+        unpack_rgba8(__ldg(t + y * w + x), out);
+        return;
+    }
+    int x0 = (int)cx, y0 = (int)cy;
+    float fx = cx - (float)x0, fy = cy - (float)y0;
+    x0 = min(x0, w - 1);
+    y0 = min(y0, h - 1);
+    int x1 = min(x0 + 1, w - 1), y1 = min(y0 + 1, h - 1);
+    float c00[4], c01[4], c10[4], c11[4];
+    unpack_rgba8(__ldg(t + y0 * w + x0), c00);
+    unpack_rgba8(__ldg(t + y0 * w + x1), c01);
+    unpack_rgba8(__ldg(t + y1 * w + x0), c10);
+    unpack_rgba8(__ldg(t + y1 * w + x1), c11);
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+        float top = lerpf_(c00[i], c01[i], fx);
+        float bot = lerpf_(c10[i], c11[i], fx);
+        out[i] = lerpf_(top, bot, fy);
+    }
+}
+
+__device__ __forceinline__ void tex_trilinear(const DrawDev& d, float u, float v, float lam, float out[4]) {
+    float maxl = (float)(d.tex_levels - 1);
+    if (!(lam > 0.0f)) lam = 0.0f;
+    if (lam > maxl) lam = maxl;
+    int lo = (int)floorf(lam);
+    float t = lam - (float)lo;
+    int hi = min(lo + 1, d.tex_levels - 1);
+    tex_sample_level(d, lo, u, v, out);
+    if (hi == lo || t == 0.0f) return;
+    float c1[4];
+    tex_sample_level(d, hi, u, v, c1);
+#pragma unroll
+    for (int i = 0; i < 4; i++) out[i] = lerpf_(out[i], c1[i], t);
+}
+
+__device__ __forceinline__ float finite_or_zero(float x) { return isfinite(x) ? x : 0.0f; }
+
+__device__ __forceinline__ void tex_sample(const DrawDev& d, float u, float v, float dudx, float dvdx, float dudy,
+                                           float dvdy, float out[4]) {
+    u = finite_or_zero(u); v = finite_or_zero(v);
+    dudx = finite_or_zero(dudx); dvdx = finite_or_zero(dvdx);
+    dudy = finite_or_zero(dudy); dvdy = finite_or_zero(dvdy);
+    if (d.sampler.filter == 0) {
+        tex_sample_level(d, 0, u, v, out);
+        return;
+    }
+    float tw = (float)d.tex_w, th = (float)d.tex_h;
+    float xu = dudx * tw, xv = dvdx * th, yu = dudy * tw, yv = dvdy * th;
+    float lx2 = xu * xu + xv * xv;
+    float ly2 = yu * yu + yv * yv;
+    if (d.sampler.max_aniso <= 1) {
+        float lam = 0.5f * log2_series(fmaxf(lx2, ly2)) + d.sampler.lod_bias;
+        tex_trilinear(d, u, v, lam, out);
+        return;
+    }
+    float px = sqrtf(lx2), py = sqrtf(ly2);
+    bool major_x = px >= py;
+    float pmax = major_x ? px : py, pmin = major_x ? py : px;
+    float amax = (float)d.sampler.max_aniso;
+    float ratio = pmin > 0.0f ? pmax / pmin : amax;
+    ratio = fminf(ratio, amax);
+    int n = (int)ceilf(ratio);
+    if (n < 1) n = 1;
+    float lam = log2_series(pmax / (float)n) + d.sampler.lod_bias;
+    float du = major_x ? dudx : dudy, dv = major_x ? dvdx : dvdy;
+    float acc[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+    float inv = (float)(n + 1);
+    for (int i = 0; i < n; i++) {
+        float t = (float)(i + 1) / inv - 0.5f;
+        float cc[4];
+        tex_trilinear(d, u + du * t, v + dv * t, lam, cc);
+#pragma unroll
+        for (int k = 0; k < 4; k++) acc[k] = acc[k] + cc[k];
+    }
+    float fn = (float)n;
+#pragma unroll
+    for (int k = 0; k < 4; k++) out[k] = acc[k] / fn;
+}
+
+// ------------------------------------------------------------------ interpolation + shading
+// Perspective-correct interpolation of the draw's attribute at fixed-point position (x, y).
+__device__ __forceinline__ void interp_attr(const SubTri& s, const DrawDev& d, const float* a0, const float* a1,
+                                            const float* a2, int32_t x, int32_t y, float out[4]) {
+    float p[3];
+#pragma unroll
+    for (int i = 0; i < 3; i++) {
+        float e = (float)(s.C[i] + (int64_t)s.A[i] * x + (int64_t)s.B[i] * y);
+        p[i] = e * s.iw[i];
+    }
+    float sum = (p[0] + p[1]) + p[2];
+    float r = 1.0f / sum;
+    float b0 = p[0] * r, b1 = p[1] * r, b2 = p[2] * r;
+    float W[3];
+#pragma unroll
+    for (int k = 0; k < 3; k++) W[k] = (b0 * s.bary[0][k] + b1 * s.bary[1][k]) + b2 * s.bary[2][k];
+#pragma unroll
+    for (int k = 0; k < 4; k++) out[k] = 0.0f;
+    for (int k = 0; k < d.attr_count; k++)
+        out[k] = (W[0] * __ldg(a0 + k) + W[1] * __ldg(a1 + k)) + W[2] * __ldg(a2 + k);
+}
+
+// Fragment colour of pixel (px, py) for triangle t / sub-triangle s.  Derivatives for texture
+// LOD are the fine 2x2-quad differences: attribute at the quad's right column minus left
+// column (same row) and bottom row minus top row (same column), each evaluated for this
+// primitive exactly as a helper invocation would.
+__device__ __forceinline__ void shade_fragment(const PassConst& c, const DrawDev& d, const SubTri& s, int t, int sub,
+                                               int px, int py, float col[4]) {
+    if (d.shading == SHADE_PRIMID) {
+        col[0] = (float)(d.prim_base + t); col[1] = (float)sub; col[2] = 0.0f; col[3] = 1.0f;
+        return;
+    }
+    const float* a0 = d.vertices + (size_t)__ldg(d.indices + 3 * (size_t)t + 0) * d.stride + d.attr_offset;
+    const float* a1 = d.vertices + (size_t)__ldg(d.indices + 3 * (size_t)t + 1) * d.stride + d.attr_offset;
+    const float* a2 = d.vertices + (size_t)__ldg(d.indices + 3 * (size_t)t + 2) * d.stride + d.attr_offset;
+    int32_t qx = px * 256 + c.shade_x, qy = py * 256 + c.shade_y;
+    float a[4];
+    interp_attr(s, d, a0, a1, a2, qx, qy, a);
+    if (d.shading == SHADE_TEXTURED) {
+        int xl = px & ~1, yt = py & ~1;
+        float al[4], ar[4], at[4], ab[4];
+        interp_attr(s, d, a0, a1, a2, xl * 256 + c.shade_x, qy, al);
+        interp_attr(s, d, a0, a1, a2, (xl + 1) * 256 + c.shade_x, qy, ar);
+        interp_attr(s, d, a0, a1, a2, qx, yt * 256 + c.shade_y, at);
+        interp_attr(s, d, a0, a1, a2, qx, (yt + 1) * 256 + c.shade_y, ab);
+        float dudx = ar[0] - al[0], dvdx = ar[1] - al[1];
+        float dudy = ab[0] - at[0], dvdy = ab[1] - at[1];
+        tex_sample(d, a[0], a[1], dudx, dvdx, dudy, dvdy, col);
+        return;
+    }
+    col[0] = a[0]; col[1] = a[1]; col[2] = a[2];
+    col[3] = d.attr_count >= 4 ? a[3] : 1.0f;
+}
+
+__device__ __forceinline__ float blend_factor(int f, int ch, const float* src, const float* dst) {
+    switch (f) {
+    case 0: return 0.0f;
+    case 1: return 1.0f;
+    case 2: return src[ch];
+    case 3: return 1.0f - src[ch];
+    case 4: return dst[ch];
+    case 5: return 1.0f - dst[ch];
+    case 6: return src[3];
+    case 7: return 1.0f - src[3];
+    case 8: return dst[3];
+    case 9: return 1.0f - dst[3];
+    default: return 0.0f;
+    }
+}
+
+__device__ __forceinline__ void blend_into(const DrawDev& d, const float* src, float* dst) {
+    float out[4];
+#pragma unroll
+    for (int ch = 0; ch < 4; ch++) {
+        int fs = ch < 3 ? d.blend_src_color : d.blend_src_alpha;
+        int fd = ch < 3 ? d.blend_dst_color : d.blend_dst_alpha;
+        out[ch] = dst[ch] * blend_factor(fd, ch, src, dst) + src[ch] * blend_factor(fs, ch, src, dst);
+    }
+#pragma unroll
+    for (int ch = 0; ch < 4; ch++) dst[ch] = out[ch];
+}
+
+}  // namespace ifr

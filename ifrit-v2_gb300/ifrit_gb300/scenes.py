@@ -149,30 +149,41 @@ def geodesic_sphere(frequency, seed, displacement=0.05):
 
 
 def triangle_soup(num_tris, seed, width, height, fovy=60.0, median_px=4.0, sigma=1.0, near=0.5, far=20.0,
-                  area_scale=1.0, uv_density=(0.5, 4.0), max_stretch=8.0):
-    """Unshared random triangles with centres uniform (by volume) in the view frustum and
-    edge lengths log-normal in pixels at the centre's depth.  Each vertex carries a UV from
-    a random anisotropic affine map of its screen position.
+                  apex=0.2, uv_density=(0.5, 4.0), max_stretch=8.0):
+    """Unshared random triangles with centres uniform (by volume) in the view frustum.
+
+    Each triangle has a longest (base) edge whose on-screen length at the centre's depth is
+    log-normal in pixels (median `median_px`, shape `sigma`) and an apex at `apex` x base
+    length (x U[0.5, 1.5]) from the base; `apex` = 0.2 gives a depth complexity of about 6
+    for 1M triangles at 1920x1080.  Each vertex carries a UV from a random anisotropic affine
+    map (texel density log-uniform in `uv_density` texels per pixel of a 1024^2 texture,
+    stretch up to `max_stretch`).
 
     Returns (vertices (3T,5) float32 [x y z u v] in view space, indices (T,3), mvp)."""
     rng = np.random.default_rng(seed)
     aspect = width / height
     th = math.tan(math.radians(fovy) / 2)
-    # depth with pdf ~ d^2 on [near, far]
     u = rng.uniform(size=num_tris)
-    d = (near ** 3 + u * (far ** 3 - near ** 3)) ** (1.0 / 3.0)
+    d = (near ** 3 + u * (far ** 3 - near ** 3)) ** (1.0 / 3.0)  # pdf ~ d^2 on [near, far]
     xn = rng.uniform(-1, 1, num_tris)
     yn = rng.uniform(-1, 1, num_tris)
     centre = np.stack([xn * d * th * aspect, yn * d * th, -d], 1)
     px_world = 2.0 * d * th / height  # world size of one pixel at depth d
-    L = median_px * np.exp(sigma * rng.normal(size=num_tris)) * area_scale
-    # three vertices around the centre in a random plane roughly facing the camera
-    ang = rng.uniform(0, 2 * np.pi, size=(num_tris, 1)) + np.array([[0.0, 2.0944, 4.18879]]) + \
-        rng.uniform(-0.5, 0.5, size=(num_tris, 3))
-    rad = (L / math.sqrt(3.0))[:, None] * rng.uniform(0.6, 1.2, size=(num_tris, 3))
-    off = np.stack([np.cos(ang) * rad, np.sin(ang) * rad, rng.uniform(-0.3, 0.3, size=(num_tris, 3)) * rad], 2)
+    L = median_px * np.exp(sigma * rng.normal(size=num_tris))
+    theta = rng.uniform(0, 2 * np.pi, num_tris)
+    ex = np.stack([np.cos(theta), np.sin(theta)], 1)
+    ey = np.stack([-np.sin(theta), np.cos(theta)], 1)
+    h = apex * L * rng.uniform(0.5, 1.5, num_tris)
+    t = rng.uniform(-0.5, 0.5, num_tris)
+    off2 = np.stack([-0.5 * L[:, None] * ex - h[:, None] * ey / 3,
+                     0.5 * L[:, None] * ex - h[:, None] * ey / 3,
+                     (t * L)[:, None] * ex + (2 * h / 3)[:, None] * ey], 1)  # (T, 3, 2) pixels
+    # counter-clockwise in NDC for half of them, clockwise for the rest
+    flip = rng.uniform(size=num_tris) < 0.5
+    off2[flip] = off2[flip][:, [0, 2, 1]]
+    offz = rng.uniform(-0.3, 0.3, size=(num_tris, 3)) * L[:, None]
+    off = np.concatenate([off2, offz[..., None]], 2)
     pos = centre[:, None, :] + off * px_world[:, None, None]
-    # UV: random anisotropic affine map of the in-plane offset (in pixels)
     dens = np.exp(rng.uniform(np.log(uv_density[0]), np.log(uv_density[1]), num_tris)) / 1024.0
     stretch = np.exp(rng.uniform(0, np.log(max_stretch), num_tris))
     rot = rng.uniform(0, np.pi, num_tris)
@@ -187,6 +198,11 @@ def triangle_soup(num_tris, seed, width, height, fovy=60.0, median_px=4.0, sigma
     idx = np.arange(3 * num_tris, dtype=np.int32).reshape(-1, 3)
     mvp = perspective(fovy, aspect, 0.1, 100.0).astype(np.float32)
     return verts, idx, mvp
+
+
+def c2_scene(seed=2, num_tris=1_000_000, width=1920, height=1080):
+    """1M-triangle textured soup for a 1920x1080 4x MSAA target (depth complexity ~6)."""
+    return triangle_soup(num_tris, seed, width, height)
 
 
 def soup_depth_complexity(verts, idx, mvp, width, height):

@@ -1,0 +1,199 @@
+/*
+ * ifrit_gb300.h -- C-ABI of the GB300 (sm_103a) software triangle rasterizer.
+ *
+ * Drop-in boundary for Ifrit-v2's soft renderer (projects/softgraphics).  Entry points keep
+ * the reference's exported names and argument meaning (iftr*, ifcr*, ifbuf*); every call is
+ * noexcept and returns an int status (IFTR_OK = 0) where the reference returned void.
+ * Objects created here are opaque handles.  Framebuffers, images, vertex buffers and
+ * varying descriptors are caller-owned and bound by pointer (non-owning), as in the
+ * reference (TileRasterContext.h:62-69); the renderer owns its device memory.
+ *
+ * References (Aeroraven/Ifrit-v2):
+ *   TRE = include/ifrit/softgraphics/engine/export/TileRasterRendererExport.h
+ *   ECE = include/ifrit/softgraphics/engine/export/EngineCommonExport.h
+ *   CE  = include/ifrit/softgraphics/core/export/CommonExport.h
+ *   BME = include/ifrit/softgraphics/engine/export/BufferManagerExport.h
+ *   TRC = include/ifrit/softgraphics/engine/tilerastercuda/TileRasterRendererCuda.h
+ */
+#ifndef IFRIT_GB300_H
+#define IFRIT_GB300_H
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#if defined(_WIN32)
+#define IFTR_API __declspec(dllexport)
+#else
+#define IFTR_API __attribute__((visibility("default")))
+#endif
+
+/* ---- status codes */
+enum {
+    IFTR_OK = 0,
+    IFTR_ERR_INVALID_ARG = 1,
+    IFTR_ERR_UNSUPPORTED = 2,   /* e.g. host function-pointer shaders */
+    IFTR_ERR_CUDA = 3,
+    IFTR_ERR_OVERFLOW = 4,      /* a scratch capacity was exceeded; see iftrReserve */
+    IFTR_ERR_NO_DEVICE = 5,
+    IFTR_ERR_STATE = 6          /* missing binding (framebuffer, vertex/index buffer, shader) */
+};
+
+/* ---- enums (same numbering as the reference, base/Constants.h:23-96, TypeDescriptor.h:26-40) */
+enum { IFTP_FLOAT1 = 1, IFTP_FLOAT2 = 2, IFTP_FLOAT3 = 3, IFTP_FLOAT4 = 4 };
+enum { IF_CULL_MODE_NONE = 0, IF_CULL_MODE_FRONT = 1, IF_CULL_MODE_BACK = 2, IF_CULL_MODE_FRONT_AND_BACK = 3 };
+enum {
+    IF_COMPARE_OP_NEVER = 0, IF_COMPARE_OP_LESS = 1, IF_COMPARE_OP_EQUAL = 2, IF_COMPARE_OP_LESS_OR_EQUAL = 3,
+    IF_COMPARE_OP_GREATER = 4, IF_COMPARE_OP_NOT_EQUAL = 5, IF_COMPARE_OP_GREATER_OR_EQUAL = 6,
+    IF_COMPARE_OP_ALWAYS = 7
+};
+enum {
+    IF_BLEND_FACTOR_ZERO = 0, IF_BLEND_FACTOR_ONE = 1, IF_BLEND_FACTOR_SRC_COLOR = 2,
+    IF_BLEND_FACTOR_ONE_MINUS_SRC_COLOR = 3, IF_BLEND_FACTOR_DST_COLOR = 4, IF_BLEND_FACTOR_ONE_MINUS_DST_COLOR = 5,
+    IF_BLEND_FACTOR_SRC_ALPHA = 6, IF_BLEND_FACTOR_ONE_MINUS_SRC_ALPHA = 7, IF_BLEND_FACTOR_DST_ALPHA = 8,
+    IF_BLEND_FACTOR_ONE_MINUS_DST_ALPHA = 9
+};
+enum {
+    IF_SAMPLER_ADDRESS_MODE_REPEAT = 0, IF_SAMPLER_ADDRESS_MODE_MIRRORED_REPEAT = 1,
+    IF_SAMPLER_ADDRESS_MODE_CLAMP_TO_EDGE = 2, IF_SAMPLER_ADDRESS_MODE_CLAMP_TO_BORDER = 3,
+    IF_SAMPLER_ADDRESS_MODE_MIRROR_CLAMP_TO_EDGE = 4
+};
+enum { IF_FILTER_NEAREST = 0, IF_FILTER_LINEAR = 1 };
+/* colour attachment formats held on the device */
+enum { IFTR_FORMAT_RGBA8 = 0, IFTR_FORMAT_RGBA16F = 1, IFTR_FORMAT_RGBA32F = 2, IFTR_FORMAT_RGB32F = 3 };
+/* built-in shading models (device shaders; see iftrBindFragmentShaderBuiltin) */
+enum { IFTR_FS_GOURAUD = 0, IFTR_FS_TEXTURED = 1, IFTR_FS_PRIMITIVE_ID = 2 };
+enum { IFTR_VS_MVP_TRANSFORM = 0 };
+
+/* IfritColorAttachmentBlendState (base/Structures.h:91-98) */
+typedef struct {
+    int blendEnable;
+    int srcColorBlendFactor, dstColorBlendFactor, srcAlphaBlendFactor, dstAlphaBlendFactor;
+} IfritGbBlendState;
+
+/* IfritSamplerT (base/Structures.h:52-61) */
+typedef struct {
+    int filterMode, addressModeU, addressModeV, addressModeW, borderColor;
+    int anisotropyEnable;
+    float maxAnisotropy;
+    float lodBias;
+} IfritGbSampler;
+
+typedef struct {
+    uint64_t triangles_in;        /* triangles submitted in the last pass */
+    uint64_t tile_pairs;          /* (triangle, tile) overlaps binned in the last pass */
+    uint64_t pair_capacity;       /* current scratch capacity in pairs */
+    int retries;                  /* overflow re-runs of the last synchronous draw */
+} IfritGbStats;
+
+typedef struct IfritGbRenderer IfritGbRenderer;
+typedef struct IfritGbFrameBuffer IfritGbFrameBuffer;
+typedef struct IfritGbVertexBuffer IfritGbVertexBuffer;
+typedef struct IfritGbVaryingDescriptor IfritGbVaryingDescriptor;
+typedef struct IfritGbImageF32 IfritGbImageF32;
+
+/* ---- renderer instance (TRE:33-78, TRC:81-115) */
+IFTR_API IfritGbRenderer* iftrCreateInstance(void);                                  /* TRE:33 */
+IFTR_API int iftrDestroyInstance(IfritGbRenderer* h);                                /* TRE:35 */
+IFTR_API int iftrInit(IfritGbRenderer* h);                                           /* TRE:71 */
+IFTR_API int iftrBindFrameBuffer(IfritGbRenderer* h, IfritGbFrameBuffer* fb);        /* TRE:37 */
+IFTR_API int iftrBindVertexBuffer(IfritGbRenderer* h, const IfritGbVertexBuffer* vb); /* TRE:40 */
+IFTR_API int iftrBindIndexBuffer(IfritGbRenderer* h, void* indexBuffer);             /* TRE:43, ifbuf buffer */
+/* Host function-pointer and C++-object shaders cannot execute on the device: these return
+ * IFTR_ERR_UNSUPPORTED (TRE:45, TRE:49, TRE:75, TRE:77).  Use the built-in device shaders. */
+IFTR_API int iftrBindVertexShaderFunc(IfritGbRenderer* h, void* func, IfritGbVaryingDescriptor* vsOut);
+IFTR_API int iftrBindFragmentShaderFunc(IfritGbRenderer* h, void* func);
+IFTR_API int iftrBindVertexShader(IfritGbRenderer* h, void* pVertexShader);
+IFTR_API int iftrBindFragmentShader(IfritGbRenderer* h, void* pFragmentShader);
+/* Built-in device shaders replacing the bound shader objects of TileRasterRenderer::
+ * bindVertexShader / bindFragmentShader (TileRasterRenderer.h:96-99): the vertex shader is
+ * clip = MVP * (attribute 0 xyz, 1) with attribute 1 as the interpolated varying; the MVP is
+ * uniform binding 0, set 0 (16 floats, row-major). */
+IFTR_API int iftrBindVertexShaderBuiltin(IfritGbRenderer* h, int kind, const IfritGbVaryingDescriptor* vsOut);
+IFTR_API int iftrBindFragmentShaderBuiltin(IfritGbRenderer* h, int model);
+IFTR_API int iftrBindUniformBuffer(IfritGbRenderer* h, int binding, int set, void* buffer); /* TileRasterRenderer.h:100 */
+IFTR_API int iftrSetBlendFunc(IfritGbRenderer* h, const IfritGbBlendState* state);   /* TRE:52 */
+IFTR_API int iftrSetDepthFunc(IfritGbRenderer* h, int compareOp);                   /* TRE:55 */
+IFTR_API int iftrOptsetForceDeterministic(IfritGbRenderer* h, int opt);             /* TRE:58; always deterministic */
+IFTR_API int iftrOptSetDepthTestEnable(IfritGbRenderer* h, int opt);                /* TRE:61 */
+IFTR_API int iftrDrawLegacy(IfritGbRenderer* h, int numIndices, int clearFramebuffer); /* TRE:64, synchronous */
+IFTR_API int iftrClear(IfritGbRenderer* h);                                          /* TRE:67 */
+/* CUDA-renderer state (TRC:91-111) */
+IFTR_API int iftrSetCullMode(IfritGbRenderer* h, int cullMode);                      /* TRC:107 */
+IFTR_API int iftrSetFrontFace(IfritGbRenderer* h, int counterClockwise);
+IFTR_API int iftrSetMsaaSamples(IfritGbRenderer* h, int samples);                    /* TRC:103, 1/2/4/8/16 */
+IFTR_API int iftrSetClearValues(IfritGbRenderer* h, const float* rgba, float depth); /* TRC:108 */
+IFTR_API int iftrSetDepthWriteEnable(IfritGbRenderer* h, int enable);
+IFTR_API int iftrCreateTexture(IfritGbRenderer* h, int slot, int width, int height, int mipLevels); /* TRC:91, RGBA8 */
+IFTR_API int iftrCopyHostBufferToImage(IfritGbRenderer* h, const void* rgba8, int slot); /* TRC:96, level 0 */
+IFTR_API int iftrGenerateMipmap(IfritGbRenderer* h, int slot, int filter);           /* TRC:93 */
+IFTR_API int iftrCreateSampler(IfritGbRenderer* h, int slot, const IfritGbSampler* sampler); /* TRC:92 */
+IFTR_API int iftrBindTexture(IfritGbRenderer* h, int textureSlot, int samplerSlot);
+/* ---- device-resident extensions (no host copies) */
+IFTR_API int iftrSetStream(IfritGbRenderer* h, void* cudaStream);
+IFTR_API int iftrDrawAsync(IfritGbRenderer* h, int numIndices, int clearFramebuffer);
+IFTR_API int iftrFinish(IfritGbRenderer* h);
+IFTR_API int iftrBindVertexBufferDevice(IfritGbRenderer* h, const float* vertices, int strideFloats, int numVertices,
+                                        int attrOffsetFloats, int attrCount);
+IFTR_API int iftrBindIndexBufferDevice(IfritGbRenderer* h, const int* indices, int numIndices);
+IFTR_API int iftrSetUniformMatrix(IfritGbRenderer* h, const float* mvpRowMajor);
+IFTR_API int iftrSetVisibilityOutput(IfritGbRenderer* h, int enable);
+IFTR_API int iftrReserve(IfritGbRenderer* h, size_t tilePairs);
+IFTR_API int iftrGetDeviceAttachments(IfritGbRenderer* h, void** color, float** depth, int** visibility);
+IFTR_API int iftrReadbackColor(IfritGbRenderer* h, void* dst, size_t bytes);
+IFTR_API int iftrReadbackDepth(IfritGbRenderer* h, float* dst, size_t count);
+IFTR_API int iftrReadbackVisibility(IfritGbRenderer* h, int* dst, size_t count);
+IFTR_API int iftrGetStats(IfritGbRenderer* h, IfritGbStats* out);
+/* Per-stage device timing of the last pass, from CUDA events on the renderer's stream:
+ * ms[0] counting binner, ms[1] list-offset scan, ms[2] scattering binner, ms[3] tile
+ * raster/shade/resolve kernel.  Enable before the draw; read after iftrFinish/iftrDrawLegacy. */
+IFTR_API int iftrSetStageTiming(IfritGbRenderer* h, int enable);
+IFTR_API int iftrGetStageTimes(IfritGbRenderer* h, float* ms, int n);
+IFTR_API const char* iftrGetErrorString(int status);
+
+/* ---- framebuffers and images (ECE:31-40, CE:25-31) */
+IFTR_API IfritGbFrameBuffer* iftrCreateFrameBuffer(void);                            /* ECE:31 */
+IFTR_API int iftrDestroyFrameBuffer(IfritGbFrameBuffer* fb);                         /* ECE:33 */
+IFTR_API int iftrSetFrameBufferColorAttachmentFP32(IfritGbFrameBuffer* fb, IfritGbImageF32* const* images,
+                                                   size_t nums);                     /* ECE:35 */
+IFTR_API int iftrSetFrameBufferDepthAttachmentFP32(IfritGbFrameBuffer* fb, IfritGbImageF32* image); /* ECE:38 */
+/* Device-format colour attachment of the given size (no host image; read back explicitly). */
+IFTR_API int iftrSetFrameBufferColorAttachmentDevice(IfritGbFrameBuffer* fb, int format, int width, int height);
+IFTR_API IfritGbImageF32* ifcrCreateImageFP32(size_t width, size_t height, size_t channel); /* CE:25 */
+IFTR_API int ifcrDestroyImageFP32(IfritGbImageF32* image);                          /* CE:27 */
+IFTR_API float* ifcrGetImageRawDataFP32(IfritGbImageF32* image);                     /* CE:29 */
+
+/* ---- varying descriptors and vertex buffers (ECE:43-69) */
+IFTR_API IfritGbVaryingDescriptor* iftrCreateVaryingDescriptor(void);                /* ECE:43 */
+IFTR_API int iftrDestroyVaryingDescriptor(IfritGbVaryingDescriptor* vd);             /* ECE:45 */
+IFTR_API int iftrWriteVaryingDescriptor(IfritGbVaryingDescriptor* vd, const int* desc, size_t num); /* ECE:47 */
+IFTR_API IfritGbVertexBuffer* iftrCreateVertexBuffer(void);                          /* ECE:53 */
+IFTR_API int iftrDestroyVertexBuffer(IfritGbVertexBuffer* vb);                       /* ECE:55 */
+IFTR_API int iftrSetVertexBufferLayout(IfritGbVertexBuffer* vb, const int* desc, size_t num); /* ECE:57 */
+IFTR_API int iftrSetVertexBufferSize(IfritGbVertexBuffer* vb, size_t num);           /* ECE:61 */
+IFTR_API int iftrAllocateVertexBuffer(IfritGbVertexBuffer* vb);                      /* ECE:64 */
+IFTR_API int iftrSetVertexBufferValueFloat4(IfritGbVertexBuffer* vb, int index, int attr, void* value); /* ECE:66 */
+IFTR_API int iftrSetVertexBufferData(IfritGbVertexBuffer* vb, const void* src, size_t bytes);
+/* Raw (page-locked when a device is present) storage of the vertex buffer, as
+ * VertexBuffer::GetBufferUnsafe (VertexBuffer.h:75); after writing through it call
+ * iftrSetVertexBufferDirty so the next draw uploads it. */
+IFTR_API void* iftrGetVertexBufferRawData(IfritGbVertexBuffer* vb);
+IFTR_API int iftrSetVertexBufferDirty(IfritGbVertexBuffer* vb);
+
+/* ---- buffer manager (BME:24-35) */
+IFTR_API void* ifbufCreateBufferManager(void);                                       /* BME:24 */
+IFTR_API int ifbufDestroyBufferManager(void* manager);                               /* BME:26 */
+IFTR_API void* ifbufCreateBuffer(void* manager, size_t bufSize);                     /* BME:28 */
+IFTR_API int ifbufDestroyBuffer(void* buffer);                                       /* BME:30 */
+IFTR_API int ifbufBufferData(void* buffer, const void* data, size_t offset, size_t size); /* BME:32 */
+/* Raw storage of a buffer (TrivialBufferManager::mapBufferMemory, BufferManager.h:73) and
+ * its dirty mark for writes made through it. */
+IFTR_API void* ifbufGetBufferRawData(void* buffer);
+IFTR_API int ifbufSetBufferDirty(void* buffer);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* IFRIT_GB300_H */

@@ -1,0 +1,91 @@
+"""C-ABI checks that need no GPU: the library builds and loads, exports every entry point
+include/ifrit_gb300.h declares, and its host-only objects behave (no compute calls)."""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+import ifrit_gb300 as ig
+
+HEADER = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "include", "ifrit_gb300.h")
+
+
+def declared_symbols():
+    text = open(HEADER).read()
+    return sorted(set(re.findall(r"IFTR_API\s+[\w\s\*]+?\b(\w+)\s*\(", text)))
+
+
+@pytest.fixture(scope="module")
+def lib():
+    return ig.load()
+
+
+def test_header_declares_entry_points():
+    syms = declared_symbols()
+    assert len(syms) >= 60
+    assert set(ig.EXPORTED) == set(syms), set(ig.EXPORTED) ^ set(syms)
+
+
+def test_library_exports_every_declared_symbol(lib):
+    missing = [s for s in declared_symbols() if not hasattr(lib, s)]
+    assert not missing, missing
+
+
+def test_error_strings(lib):
+    assert lib.iftrGetErrorString(0) == b"ok"
+    assert lib.iftrGetErrorString(4) == b"scratch capacity exceeded"
+
+
+def test_host_function_shaders_are_unsupported(lib):
+    h = lib.iftrCreateInstance()
+    assert h
+    assert lib.iftrBindVertexShaderFunc(h, None, None) == 2
+    assert lib.iftrBindFragmentShaderFunc(h, None) == 2
+    assert lib.iftrBindVertexShader(h, None) == 2
+    assert lib.iftrBindFragmentShader(h, None) == 2
+    assert lib.iftrBindFragmentShaderBuiltin(h, ig.FS_TEXTURED) == 0
+    assert lib.iftrBindFragmentShaderBuiltin(h, 99) == 1
+    assert lib.iftrSetMsaaSamples(h, 3) == 1
+    assert lib.iftrSetMsaaSamples(h, 8) == 0
+    assert lib.iftrSetDepthFunc(h, 8) == 1
+    assert lib.iftrSetCullMode(h, 4) == 1
+    assert lib.iftrDestroyInstance(h) == 0
+
+
+def test_host_objects(lib):
+    img = lib.ifcrCreateImageFP32(8, 4, 4)
+    data = lib.ifcrGetImageRawDataFP32(img)
+    assert data[0] == 0.0 and data[8 * 4 * 4 - 1] == 0.0
+    fb = lib.iftrCreateFrameBuffer()
+    arr = (ctypes.c_void_p * 1)(img)
+    assert lib.iftrSetFrameBufferColorAttachmentFP32(fb, arr, 1) == 0
+    assert lib.iftrSetFrameBufferColorAttachmentDevice(fb, 7, 8, 8) == 1
+    vb = lib.iftrCreateVertexBuffer()
+    layout = (ctypes.c_int * 2)(ig.IFTP_FLOAT3, ig.IFTP_FLOAT2)
+    assert lib.iftrSetVertexBufferLayout(vb, layout, 2) == 0
+    assert lib.iftrSetVertexBufferSize(vb, 3) == 0
+    assert lib.iftrAllocateVertexBuffer(vb) == 0
+    v = np.array([1, 2, 3, 4], np.float32)
+    assert lib.iftrSetVertexBufferValueFloat4(vb, 2, 1, ctypes.c_void_p(v.ctypes.data)) == 0
+    assert lib.iftrSetVertexBufferValueFloat4(vb, 3, 0, ctypes.c_void_p(v.ctypes.data)) == 1
+    assert lib.iftrSetVertexBufferData(vb, ctypes.c_void_p(v.ctypes.data), 4) == 1  # wrong size
+    bad = (ctypes.c_int * 1)(ig.IFTP_FLOAT2)
+    assert lib.iftrSetVertexBufferLayout(vb, bad, 1) == 2  # position needs >= 3 floats
+    mgr = lib.ifbufCreateBufferManager()
+    buf = lib.ifbufCreateBuffer(mgr, 16)
+    assert lib.ifbufBufferData(buf, ctypes.c_void_p(v.ctypes.data), 0, 16) == 0
+    assert lib.ifbufBufferData(buf, ctypes.c_void_p(v.ctypes.data), 8, 16) == 1
+    vd = lib.iftrCreateVaryingDescriptor()
+    desc = (ctypes.c_int * 1)(ig.IFTP_FLOAT4)
+    assert lib.iftrWriteVaryingDescriptor(vd, desc, 1) == 0
+    for call, obj in ((lib.iftrDestroyVaryingDescriptor, vd), (lib.ifbufDestroyBufferManager, mgr),
+                      (lib.iftrDestroyVertexBuffer, vb), (lib.iftrDestroyFrameBuffer, fb), (lib.ifcrDestroyImageFP32, img)):
+        assert call(obj) == 0
+
+
+def test_null_handles_rejected(lib):
+    assert lib.iftrDrawLegacy(None, 3, 1) == 1
+    assert lib.iftrDestroyInstance(None) == 1
+    assert lib.iftrFinish(None) == 1
