@@ -238,7 +238,7 @@ def run_ours(args):
         r.finish()
     ev0 = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
     ev1 = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
-    tile_ms, bin_ms = [], []
+    tile_ms, bin_ms, raster_ms, shade_ms = [], [], [], []
     clocks = ClockSampler()
     if dist:
         dist.barrier()
@@ -252,7 +252,9 @@ def run_ours(args):
         r.finish()
         st = r.stage_times()
         bin_ms.append(st[0] + st[1] + st[2])
-        tile_ms.append(st[3])
+        raster_ms.append(st[3])
+        shade_ms.append(st[4])
+        tile_ms.append(st[3] + st[4])
     torch.cuda.synchronize()
     clk = clocks.stop(torch.cuda.current_device())
     step_ms = [a.elapsed_time(b) for a, b in zip(ev0, ev1)]
@@ -295,7 +297,8 @@ def run_ours(args):
                    "l2": "flushed before every timed step (256 MB write)",
                    "parallelism": "replicas" if world > 1 else "single"},
         "tris_per_s": world * len(w["indices"]) / (ms / 1000.0),
-        "stage_ms": {"binning": statistics.mean(bin_ms), "tile": statistics.mean(tile_ms)},
+        "stage_ms": {"binning": statistics.mean(bin_ms), "raster": statistics.mean(raster_ms),
+                     "shade": statistics.mean(shade_ms)},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": profiled_traffic(w["name"]), "algorithmic_bytes": B, "kernel": "tile_kernel",
                      "peak_source": peak_kind},

@@ -155,13 +155,13 @@ struct IfritGbRenderer {
     float clear_depth = 1.0f;
     bool vis_output = false;
     // device state
-    DevMem d_vertices, d_indices, d_color, d_depth, d_vis;
+    DevMem d_vertices, d_indices, d_color, d_depth, d_vis, d_entries;
     const void* up_vb_key = nullptr;
     uint64_t up_vb_gen = 0;
     const void* up_ib_key = nullptr;
     uint64_t up_ib_gen = 0;
     int att_w = 0, att_h = 0, att_s = 0, att_fmt = -1;
-    DevMem d_tile_count, d_tile_offset, d_tile_cursor, d_pairs, d_status, d_draws, d_draw_start;
+    DevMem d_tile_count, d_tile_offset, d_tile_cursor, d_pairs, d_status, d_draws, d_draw_start, d_records;
     int tiles_alloc = 0;
     uint32_t pair_capacity = 0;
     uint32_t* h_status = nullptr;  // pinned
@@ -172,8 +172,8 @@ struct IfritGbRenderer {
     int bound_tex = 0, bound_sampler = 0;
     IfritGbStats stats{};
     bool timing = false;
-    cudaEvent_t ev[5] = {};
-    float stage_ms[4] = {0, 0, 0, 0};
+    cudaEvent_t ev[6] = {};
+    float stage_ms[5] = {0, 0, 0, 0, 0};
     std::string last_error;
     int pending = 0;  // an async pass whose status has not been checked
 };
@@ -220,6 +220,7 @@ int ensure_attachments(IfritGbRenderer* h, int W, int H, int S, int fmt) {
     size_t npix = (size_t)W * H;
     IFTR_CUDA(h, h->d_color.reserve(npix * color_bytes(fmt)));
     IFTR_CUDA(h, h->d_depth.reserve(npix * S * sizeof(float)));
+    IFTR_CUDA(h, h->d_entries.reserve(npix * S * sizeof(int)));
     if (h->vis_output) IFTR_CUDA(h, h->d_vis.reserve(npix * S * sizeof(int)));
     bool fresh = !(h->att_w == W && h->att_h == H && h->att_s == S && h->att_fmt == fmt);
     h->att_w = W; h->att_h = H; h->att_s = S; h->att_fmt = fmt;
@@ -326,6 +327,17 @@ void fill_state(IfritGbRenderer* h, DrawDev& d) {
     d.sampler.border_white = s.borderColor;
     d.sampler.max_aniso = s.anisotropyEnable ? std::max(1, (int)s.maxAnisotropy) : 1;
     d.sampler.lod_bias = s.lodBias;
+    int w = t.w, hh = t.h, off = 0;
+    for (int l = 0; l < 16; l++) {
+        d.lvl_off[l] = off;
+        d.lvl_w[l] = w;
+        d.lvl_h[l] = hh;
+        off += w * hh;
+        w = (w + 1) >> 1;
+        hh = (hh + 1) >> 1;
+        if (w < 1) w = 1;
+        if (hh < 1) hh = 1;
+    }
 }
 
 void sample_table(int S, int* xs, int* ys) {
@@ -410,6 +422,7 @@ int enqueue_draw(IfritGbRenderer* h, int numIndices, int clear) {
         rc = ensure_pairs(h, std::max<size_t>(1u << 20, (size_t)d.num_triangles * 4));
         if (rc) return rc;
     }
+    IFTR_CUDA(h, h->d_records.reserve(std::max<size_t>(1, (size_t)d.num_triangles) * sizeof(ifr::TriRecord)));
     IFTR_CUDA(h, cudaMemsetAsync(h->d_status.p, 0, ifr::ST_WORDS * sizeof(uint32_t), h->stream));
     PassArgs a;
     std::memset(&a, 0, sizeof(a));
@@ -422,6 +435,7 @@ int enqueue_draw(IfritGbRenderer* h, int numIndices, int clear) {
     a.color = h->d_color.p;
     a.depth = h->d_depth.as<float>();
     a.vis = h->vis_output ? h->d_vis.as<int>() : nullptr;
+    a.entries = h->d_entries.as<int>();
     a.clear = clear;
     std::memcpy(a.clear_color, h->clear_color, sizeof(a.clear_color));
     a.clear_depth = h->clear_depth;
@@ -431,6 +445,7 @@ int enqueue_draw(IfritGbRenderer* h, int numIndices, int clear) {
     a.tile_offset = h->d_tile_offset.as<uint32_t>();
     a.tile_cursor = h->d_tile_cursor.as<uint32_t>();
     a.pairs = h->d_pairs.as<uint32_t>();
+    a.records = h->d_records.as<ifr::TriRecord>();
     a.pair_capacity = h->pair_capacity;
     a.status = h->d_status.as<uint32_t>();
     IFTR_CUDA(h, ifr::launch_pass(a, h->stream, h->timing ? h->ev : nullptr));
@@ -445,7 +460,7 @@ int check_pending(IfritGbRenderer* h) {
     IFTR_CUDA(h, cudaStreamSynchronize(h->stream));
     h->pending = 0;
     if (h->timing)
-        for (int i = 0; i < 4; i++) cudaEventElapsedTime(&h->stage_ms[i], h->ev[i], h->ev[i + 1]);
+        for (int i = 0; i < 5; i++) cudaEventElapsedTime(&h->stage_ms[i], h->ev[i], h->ev[i + 1]);
     h->stats.tile_pairs = h->h_status[ifr::ST_PAIRS];
     h->stats.pair_capacity = h->pair_capacity;
     if (h->h_status[ifr::ST_OVERFLOW]) {
@@ -493,8 +508,9 @@ IFTR_API int iftrDestroyInstance(IfritGbRenderer* h) {
     if (!h) return IFTR_ERR_INVALID_ARG;
     if (h->inited) {
         cudaStreamSynchronize(h->stream);
-        for (DevMem* m : {&h->d_vertices, &h->d_indices, &h->d_color, &h->d_depth, &h->d_vis, &h->d_tile_count,
-                          &h->d_tile_offset, &h->d_tile_cursor, &h->d_pairs, &h->d_status, &h->d_draws, &h->d_draw_start})
+        for (DevMem* m : {&h->d_vertices, &h->d_indices, &h->d_color, &h->d_depth, &h->d_vis, &h->d_entries, &h->d_tile_count,
+                          &h->d_tile_offset, &h->d_tile_cursor, &h->d_pairs, &h->d_status, &h->d_draws, &h->d_draw_start,
+                          &h->d_records})
             m->release();
         for (auto& t : h->tex) t.mem.release();
         for (cudaEvent_t e : h->ev)
@@ -806,7 +822,7 @@ IFTR_API int iftrSetStageTiming(IfritGbRenderer* h, int enable) {
 
 IFTR_API int iftrGetStageTimes(IfritGbRenderer* h, float* ms, int n) {
     if (!h || !ms || n < 0) return IFTR_ERR_INVALID_ARG;
-    for (int i = 0; i < n && i < 4; i++) ms[i] = h->stage_ms[i];
+    for (int i = 0; i < n && i < 5; i++) ms[i] = h->stage_ms[i];
     return IFTR_OK;
 }
 

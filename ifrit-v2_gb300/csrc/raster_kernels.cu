@@ -32,34 +32,80 @@ __device__ __forceinline__ int find_draw(const PassArgs& a, int g) {
     return lo;
 }
 
-template <bool kScatter>
-__global__ void __launch_bounds__(256) bin_kernel(PassArgs a) {
+__device__ __forceinline__ void bin_sub(const PassArgs& a, const SubTri& s, uint32_t entry, bool scatter) {
+    int tx0 = s.px0 >> kTileShift, tx1 = s.px1 >> kTileShift;
+    int ty0 = s.py0 >> kTileShift, ty1 = s.py1 >> kTileShift;
+    for (int ty = ty0; ty <= ty1; ty++)
+        for (int tx = tx0; tx <= tx1; tx++) {
+            int tile = ty * a.c.tiles_x + tx;
+            if (scatter) {
+                uint32_t pos = atomicAdd(a.tile_cursor + tile, 1u);
+                if (pos < a.pair_capacity) a.pairs[pos] = entry;
+            } else {
+                atomicAdd(a.tile_count + tile, 1u);
+            }
+        }
+}
+
+// Counting pass: full front end per triangle; unclipped triangles leave a compact record.
+__global__ void __launch_bounds__(256) bin_count_kernel(PassArgs a) {
     int g = blockIdx.x * blockDim.x + threadIdx.x;
     if (g >= a.total_tris) return;
-    if (kScatter && a.status[ST_OVERFLOW]) return;
+    int di = find_draw(a, g);
+    const DrawDev& d = a.draws[di];
+    int t = g - __ldg(a.draw_start + di);
+    CVert poly[kMaxPoly];
+    bool inside, rejected;
+    TriRecord* rec = a.records + g;
+    if (!fetch_triangle(a.c, d, t, poly, inside, rejected)) {
+        rec->flags = 0;
+        return;
+    }
+    if (inside) {
+        SubTri s;
+        if (!setup_sub(a.c, d, poly[0], poly[1], poly[2], s)) {
+            rec->flags = 0;
+            return;
+        }
+        TriRecord r;
+        record_from_sub(s, r);
+        const int4* src = reinterpret_cast<const int4*>(&r);
+        int4* dst = reinterpret_cast<int4*>(rec);
+        dst[0] = src[0]; dst[1] = src[1]; dst[2] = src[2]; dst[3] = src[3];
+        bin_sub(a, s, (uint32_t)g << 3, false);
+        return;
+    }
+    rec->flags = REC_CLIPPED;
+    int n = clip_polygon(a.c, poly);
+    for (int i = 1; i + 1 < n; i++) {
+        SubTri s;
+        if (setup_sub(a.c, d, poly[0], poly[i], poly[i + 1], s)) bin_sub(a, s, ((uint32_t)g << 3) | (uint32_t)(i - 1), false);
+    }
+}
+
+// Scattering pass: same overlaps as the counting pass, read back from the records (clipped
+// triangles run the front end again).
+__global__ void __launch_bounds__(256) bin_scatter_kernel(PassArgs a) {
+    int g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= a.total_tris) return;
+    if (a.status[ST_OVERFLOW]) return;
+    const int flags = __ldg(&a.records[g].flags);
+    if (flags & REC_VALID) {
+        SubTri s;
+        if (sub_from_record(a.c, a.records + g, s)) bin_sub(a, s, (uint32_t)g << 3, true);
+        return;
+    }
+    if (!(flags & REC_CLIPPED)) return;
     int di = find_draw(a, g);
     const DrawDev& d = a.draws[di];
     int t = g - __ldg(a.draw_start + di);
     CVert poly[kMaxPoly];
     bool inside, rejected;
     if (!fetch_triangle(a.c, d, t, poly, inside, rejected)) return;
-    int n = inside ? 3 : clip_polygon(a.c, poly);
+    int n = clip_polygon(a.c, poly);
     for (int i = 1; i + 1 < n; i++) {
         SubTri s;
-        if (!setup_sub(a.c, d, poly[0], poly[i], poly[i + 1], s)) continue;
-        int tx0 = s.px0 >> kTileShift, tx1 = s.px1 >> kTileShift;
-        int ty0 = s.py0 >> kTileShift, ty1 = s.py1 >> kTileShift;
-        uint32_t entry = ((uint32_t)g << 3) | (uint32_t)(i - 1);
-        for (int ty = ty0; ty <= ty1; ty++)
-            for (int tx = tx0; tx <= tx1; tx++) {
-                int tile = ty * a.c.tiles_x + tx;
-                if (kScatter) {
-                    uint32_t pos = atomicAdd(a.tile_cursor + tile, 1u);
-                    if (pos < a.pair_capacity) a.pairs[pos] = entry;
-                } else {
-                    atomicAdd(a.tile_count + tile, 1u);
-                }
-            }
+        if (setup_sub(a.c, d, poly[0], poly[i], poly[i + 1], s)) bin_sub(a, s, ((uint32_t)g << 3) | (uint32_t)(i - 1), true);
     }
 }
 
@@ -93,18 +139,9 @@ __global__ void __launch_bounds__(1024) scan_kernel(PassArgs a, int T) {
     }
 }
 
-// Order-independent depth test with API-order tie break (see file comment).
-__device__ __forceinline__ bool depth_key_pass(int func, int write, float z, float dd, int prim, int cur) {
-    if (!write) return depth_cmp(func, z, dd) && prim > cur;
-    switch (func) {
-    case 1: return z < dd || (z == dd && prim < cur);
-    case 2: return z == dd && prim > cur;
-    case 3: return z < dd || (z == dd && prim > cur);
-    case 4: return z > dd || (z == dd && prim < cur);
-    case 6: return z > dd || (z == dd && prim > cur);
-    case 7: return prim > cur;
-    default: return false;
-    }
+// Initial depth of sample k of pixel (x, y) for the explicit-compare key modes.
+__device__ __forceinline__ float d0_of(const PassArgs& a, int x, int y, int k) {
+    return a.clear ? a.clear_depth : a.depth[((size_t)y * a.c.W + x) * a.c.S + k];
 }
 
 __device__ __forceinline__ void decode_color(const PassArgs& a, size_t pix, float c[4]) {
@@ -159,133 +196,450 @@ __device__ __forceinline__ void encode_color(const PassArgs& a, size_t pix, cons
     }
 }
 
+// ---------------------------------------------------------------------------- tile kernel
+// Visibility keys.  Every sample holds one 64-bit key in shared memory; a fragment that
+// passes the depth test lowers it with atomicMin, so the final key is the same whatever the
+// order fragments arrive in:
+//   high word: depth order  (LESS/LEQUAL: z ascending, GREATER/GEQUAL: descending; 0 for the
+//              functions whose pass test is an explicit compare against the initial depth)
+//   low word:  entry order  (entry = global triangle << 3 | fan index; "earliest wins" modes
+//              store entry + 1 with the background at 0, "latest wins" modes store
+//              0xFFFFFFFE - entry with the background at 0xFFFFFFFF)
+// Ties therefore resolve exactly as submission-order processing does: LESS/GREATER keep the
+// earlier primitive, LEQUAL/GEQUAL/EQUAL/ALWAYS (and any test without depth writes) the later.
+enum KeyMode { KM_EARLIEST = 0, KM_LATEST = 1 };
+
+__device__ __forceinline__ uint32_t depth_order(float z) {
+    uint32_t u = __float_as_uint(z);
+    if (u == 0x80000000u) u = 0u;  // -0 and +0 compare equal
+    return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+
+struct KeyRule {
+    int func;       // depth function
+    int write;      // depth writes enabled
+    int explicit_;  // pass decided by compare against the initial depth; depth word = 0
+    int invert;     // GREATER/GEQUAL: descending depth order
+    int mode;       // KM_EARLIEST / KM_LATEST
+};
+
+__device__ __forceinline__ KeyRule key_rule(int func, int write) {
+    KeyRule r;
+    r.func = func;
+    r.write = write;
+    r.explicit_ = !write || func == 2 || func == 7 || func == 0;
+    r.invert = func == 4 || func == 6;
+    r.mode = (write && (func == 1 || func == 4)) ? KM_EARLIEST : KM_LATEST;
+    return r;
+}
+
+__device__ __forceinline__ unsigned long long background_key(const KeyRule& r, float d0) {
+    uint32_t hi = 0u;
+    if (!r.explicit_) hi = r.invert ? ~depth_order(d0) : depth_order(d0);
+    uint32_t lo = r.mode == KM_EARLIEST ? 0u : 0xFFFFFFFFu;
+    return ((unsigned long long)hi << 32) | lo;
+}
+
+__device__ __forceinline__ int key_entry(const KeyRule& r, unsigned long long key) {
+    uint32_t lo = (uint32_t)key;
+    if (r.mode == KM_EARLIEST) return lo == 0u ? -1 : (int)(lo - 1u);
+    return lo == 0xFFFFFFFFu ? -1 : (int)(0xFFFFFFFEu - lo);
+}
+
+struct RecordPlane {
+    float z0, dzdx, dzdy;
+    int32_t X0, Y0;
+};
+
+// Shading of one visible (sub-)triangle at one pixel; out of line so the kernel carries a
+// single copy of the (large) texture-filtering code.
+__device__ __noinline__ void shade_with(const PassArgs& a, int e, const ShadeGeom& g, int px, int py, float* col) {
+    int gi = e >> 3, sub = e & 7;
+    int di = find_draw(a, gi);
+    shade_fragment(a.c, a.draws[di], g, gi - __ldg(a.draw_start + di), sub, px, py, col);
+}
+
+// Set-up of entry e (global triangle << 3 | fan index) for shading: geometry + depth plane.
+__device__ __noinline__ void setup_entry(const PassArgs& a, int e, ShadeGeom* g, RecordPlane* pl) {
+    int gi = e >> 3, sub = e & 7;
+    int di = find_draw(a, gi);
+    SubTri s;
+    setup_entry_sub(a.c, a.draws[di], a.records, gi, gi - __ldg(a.draw_start + di), sub, s);
+    shade_geom_from(s, *g);
+    pl->z0 = s.z[0];
+    pl->dzdx = s.dzdx;
+    pl->dzdy = s.dzdy;
+    pl->X0 = s.X[0];
+    pl->Y0 = s.Y[0];
+}
+
+// Raster set-up of entry e for the batch phase (out of line: one copy of the clip path).
+__device__ __noinline__ bool setup_raster_entry(const PassArgs& a, uint32_t e, SubTri* s) {
+    int g = (int)(e >> 3), sub = (int)(e & 7u);
+    int di = find_draw(a, g);
+    return setup_entry_sub(a.c, a.draws[di], a.records, g, g - __ldg(a.draw_start + di), sub, *s);
+}
+
+constexpr int kShadeCap = 192;   // visible entries per tile set up once in shared memory
+constexpr int kHashSize = 512;   // open-addressing table entry -> shade slot
+
+// Per-tile cache of shading set-ups, overlaid on the raster batch records once rasterisation
+// of the tile is complete.
+struct ShadeRecords {
+    int32_t A[3][kShadeCap], B[3][kShadeCap];
+    long long C[3][kShadeCap];
+    float iw[3][kShadeCap];
+    float bary[9][kShadeCap];
+    float z0[kShadeCap], dzdx[kShadeCap], dzdy[kShadeCap];
+    int32_t X0[kShadeCap], Y0[kShadeCap];
+    int32_t entry[kShadeCap];
+};
+
+__device__ __forceinline__ void load_shade_record(const ShadeRecords& r, int i, ShadeGeom& g, RecordPlane& pl) {
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+        g.A[k] = r.A[k][i];
+        g.B[k] = r.B[k][i];
+        g.C[k] = r.C[k][i];
+        g.iw[k] = r.iw[k][i];
+#pragma unroll
+        for (int j = 0; j < 3; j++) g.bary[k][j] = r.bary[3 * k + j][i];
+    }
+    pl.z0 = r.z0[i];
+    pl.dzdx = r.dzdx[i];
+    pl.dzdy = r.dzdy[i];
+    pl.X0 = r.X0[i];
+    pl.Y0 = r.Y0[i];
+}
+
+__device__ __forceinline__ void store_shade_record(ShadeRecords& r, int i, const ShadeGeom& g, const RecordPlane& pl) {
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+        r.A[k][i] = g.A[k];
+        r.B[k][i] = g.B[k];
+        r.C[k][i] = g.C[k];
+        r.iw[k][i] = g.iw[k];
+#pragma unroll
+        for (int j = 0; j < 3; j++) r.bary[3 * k + j][i] = g.bary[k][j];
+    }
+    r.z0[i] = pl.z0;
+    r.dzdx[i] = pl.dzdx;
+    r.dzdy[i] = pl.dzdy;
+    r.X0[i] = pl.X0;
+    r.Y0[i] = pl.Y0;
+}
+
 struct TileRecords {
     int32_t A[3][kTileThreads], B[3][kTileThreads];
     long long Cb[3][kTileThreads];
     float z0[kTileThreads], dzdx[kTileThreads], dzdy[kTileThreads];
     int32_t X0[kTileThreads], Y0[kTileThreads];
-    int32_t bx[kTileThreads], by[kTileThreads];  // packed px0 | px1 << 16, py0 | py1 << 16
-    int32_t key[kTileThreads];                   // global triangle << 3 | fan index
+    int32_t org[kTileThreads];    // tile-local x0 | y0 << 8 of the clipped bbox
+    int32_t width[kTileThreads];  // clipped bbox width in pixels
+    float rwidth[kTileThreads];   // 1 / width
+    int32_t key[kTileThreads];    // entry
+    uint32_t start[kTileThreads + 1];  // exclusive prefix of pixel counts
 };
 
+
+// Raster stage: one CTA per 16x16 tile.  The tile's list is consumed in batches of up to 256
+// set-ups; every (triangle, pixel) pair of a batch is spread over the CTA, and each covered
+// sample that passes the depth test lowers its key.  The winning entry of every sample
+// (or -1) is written for the shading stage.
 template <int S>
-__global__ void __launch_bounds__(kTileThreads, 2) tile_kernel(PassArgs a) {
-    __shared__ TileRecords rec;
+__global__ void __launch_bounds__(kTileThreads) raster_kernel(PassArgs a) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    TileRecords& rec = *reinterpret_cast<TileRecords*>(smem_raw);
+    unsigned long long* skey = reinterpret_cast<unsigned long long*>(smem_raw + sizeof(TileRecords));
+    __shared__ uint32_t warp_sum[kTileThreads / 32];
+
     const int tile = blockIdx.x;
     const int tx = tile % a.c.tiles_x, ty = tile / a.c.tiles_x;
-    const int tid = threadIdx.x;
-    // 2x2 quads on consecutive lanes; a warp covers a 16x2 pixel strip
+    const int tx0 = tx * kTileSize, ty0 = ty * kTileSize;
+    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
     const int lx = ((tid >> 2) & 7) * 2 + (tid & 1);
     const int ly = (tid >> 5) * 2 + ((tid >> 1) & 1);
-    const int px = tx * kTileSize + lx, py = ty * kTileSize + ly;
+    const int px = tx0 + lx, py = ty0 + ly;
     const bool inpix = px < a.c.W && py < a.c.H;
     const size_t pix = (size_t)py * a.c.W + px;
+    const KeyRule rule = key_rule(a.depth_func, a.depth_write);
 
-    float dep[S];
-    int id[S];
 #pragma unroll
     for (int k = 0; k < S; k++) {
-        dep[k] = a.clear ? a.clear_depth : (inpix ? a.depth[pix * S + k] : 0.0f);
-        id[k] = -1;
+        float d0 = a.clear ? a.clear_depth : (inpix ? a.depth[pix * S + k] : 0.0f);
+        skey[(ly * kTileSize + lx) * S + k] = background_key(rule, d0);
     }
-    const bool has_list = a.total_tris > 0 && a.status[ST_OVERFLOW] == 0;
+    const bool has_list = a.total_tris > 0 && a.status[ST_OVERFLOW] == 0 && rule.func != 0;
     const uint32_t beg = has_list ? a.tile_offset[tile] : 0u;
     const uint32_t end = has_list ? a.tile_offset[tile + 1] : 0u;
-    int sxk[S], syk[S];
-#pragma unroll
-    for (int k = 0; k < S; k++) {
-        sxk[k] = px * 256 + a.c.sx[k];
-        syk[k] = py * 256 + a.c.sy[k];
-    }
+    const int xmax = min(a.c.W, tx0 + kTileSize) - 1, ymax = min(a.c.H, ty0 + kTileSize) - 1;
 
     for (uint32_t base = beg; base < end; base += kTileThreads) {
         const int nb = (int)min((uint32_t)kTileThreads, end - base);
+        uint32_t cnt = 0;
         if (tid < nb) {
             uint32_t e = __ldg(a.pairs + base + tid);
-            int g = (int)(e >> 3), sub = (int)(e & 7u);
-            int di = find_draw(a, g);
             SubTri s;
-            bool ok = setup_triangle_sub(a.c, a.draws[di], g - __ldg(a.draw_start + di), sub, s);
-            if (ok) {
+            if (setup_raster_entry(a, e, &s)) {
+                int x0 = max(s.px0, tx0), x1 = min(s.px1, xmax);
+                int y0 = max(s.py0, ty0), y1 = min(s.py1, ymax);
+                if (x0 <= x1 && y0 <= y1) {
 #pragma unroll
-                for (int i = 0; i < 3; i++) {
-                    rec.A[i][tid] = s.A[i];
-                    rec.B[i][tid] = s.B[i];
-                    rec.Cb[i][tid] = s.Cb[i];
+                    for (int i = 0; i < 3; i++) {
+                        rec.A[i][tid] = s.A[i];
+                        rec.B[i][tid] = s.B[i];
+                        rec.Cb[i][tid] = s.Cb[i];
+                    }
+                    rec.z0[tid] = s.z[0];
+                    rec.dzdx[tid] = s.dzdx;
+                    rec.dzdy[tid] = s.dzdy;
+                    rec.X0[tid] = s.X[0];
+                    rec.Y0[tid] = s.Y[0];
+                    int w = x1 - x0 + 1;
+                    rec.org[tid] = (x0 - tx0) | ((y0 - ty0) << 8);
+                    rec.width[tid] = w;
+                    rec.rwidth[tid] = 1.0f / (float)w;
+                    cnt = (uint32_t)(w * (y1 - y0 + 1));
                 }
-                rec.z0[tid] = s.z[0];
-                rec.dzdx[tid] = s.dzdx;
-                rec.dzdy[tid] = s.dzdy;
-                rec.X0[tid] = s.X[0];
-                rec.Y0[tid] = s.Y[0];
-                rec.bx[tid] = s.px0 | (s.px1 << 16);
-                rec.by[tid] = s.py0 | (s.py1 << 16);
-            } else {
-                rec.bx[tid] = 1;  // empty range: px0 = 1 > px1 = 0
-                rec.by[tid] = 1;
             }
             rec.key[tid] = (int)e;
         }
-        __syncthreads();
-        if (inpix) {
-            for (int r = 0; r < nb; r++) {
-                int bx = rec.bx[r], by = rec.by[r];
-                if (px < (bx & 0xffff) || px > (bx >> 16) || py < (by & 0xffff) || py > (by >> 16)) continue;
-                int32_t A[3] = {rec.A[0][r], rec.A[1][r], rec.A[2][r]};
-                int32_t B[3] = {rec.B[0][r], rec.B[1][r], rec.B[2][r]};
-                int64_t Cb[3] = {rec.Cb[0][r], rec.Cb[1][r], rec.Cb[2][r]};
-                float z0 = rec.z0[r], gx = rec.dzdx[r], gy = rec.dzdy[r];
-                int32_t X0 = rec.X0[r], Y0 = rec.Y0[r];
-                int key = rec.key[r];
-                int prim = key >> 3;
+        // block-wide exclusive scan of the per-record pixel counts
+        uint32_t incl = cnt;
 #pragma unroll
-                for (int k = 0; k < S; k++) {
-                    if (!covered(A, B, Cb, sxk[k], syk[k])) continue;
-                    float z = sample_depth(z0, gx, gy, X0, Y0, sxk[k], syk[k]);
-                    int cur = id[k] < 0 ? -1 : (id[k] >> 3);
-                    if (depth_key_pass(a.depth_func, a.depth_write, z, dep[k], prim, cur)) {
-                        if (a.depth_write) dep[k] = z;
-                        id[k] = key;
-                    }
+        for (int o = 1; o < 32; o <<= 1) {
+            uint32_t v = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += v;
+        }
+        if (lane == 31) warp_sum[wid] = incl;
+        __syncthreads();
+        uint32_t wbase = 0, total = 0;
+#pragma unroll
+        for (int w = 0; w < kTileThreads / 32; w++) {
+            uint32_t v = warp_sum[w];
+            if (w < wid) wbase += v;
+            total += v;
+        }
+        rec.start[tid] = wbase + incl - cnt;
+        if (tid == 0) rec.start[kTileThreads] = total;
+        __syncthreads();
+        for (uint32_t p = tid; p < total; p += kTileThreads) {
+            int lo = 0, hi = nb - 1;
+            while (lo < hi) {  // last record with start <= p
+                int mid = (lo + hi + 1) >> 1;
+                if (rec.start[mid] <= p) lo = mid; else hi = mid - 1;
+            }
+            const int r = lo;
+            const int local = (int)(p - rec.start[r]);
+            const int w = rec.width[r];
+            const int oy = (int)(((float)local + 0.5f) * rec.rwidth[r]);
+            const int ox = local - oy * w;
+            const int org = rec.org[r];
+            const int qx = (org & 255) + ox, qy = (org >> 8) + oy;
+            const int gx = tx0 + qx, gy = ty0 + qy;
+            int32_t A[3] = {rec.A[0][r], rec.A[1][r], rec.A[2][r]};
+            int32_t B[3] = {rec.B[0][r], rec.B[1][r], rec.B[2][r]};
+            int64_t Cb[3] = {rec.Cb[0][r], rec.Cb[1][r], rec.Cb[2][r]};
+            const float z0 = rec.z0[r], gzx = rec.dzdx[r], gzy = rec.dzdy[r];
+            const int32_t X0 = rec.X0[r], Y0 = rec.Y0[r];
+            const uint32_t e = (uint32_t)rec.key[r];
+            const uint32_t lo_word = rule.mode == KM_EARLIEST ? e + 1u : 0xFFFFFFFEu - e;
+            unsigned long long* kp = skey + (qy * kTileSize + qx) * S;
+            // (float)(sx - X0) == fbx + sample offset exactly: every term is an integer below
+            // 2^24 in magnitude (guard-band bound), so no conversion per sample is needed.
+            const float fbx = (float)(gx * 256 - X0), fby = (float)(gy * 256 - Y0);
+#pragma unroll
+            for (int k = 0; k < S; k++) {
+                const int32_t sx = gx * 256 + a.c.sx[k], sy = gy * 256 + a.c.sy[k];
+                if (!covered(A, B, Cb, sx, sy)) continue;
+                const float z = (z0 + gzx * (fbx + (float)a.c.sx[k])) + gzy * (fby + (float)a.c.sy[k]);
+                uint32_t hi_word;
+                if (rule.explicit_) {
+                    if (!depth_cmp(rule.func, z, d0_of(a, gx, gy, k))) continue;
+                    hi_word = 0u;
+                } else {
+                    hi_word = rule.invert ? ~depth_order(z) : depth_order(z);
                 }
+                const unsigned long long kv = ((unsigned long long)hi_word << 32) | lo_word;
+                if (kv < kp[k]) atomicMin(kp + k, kv);
             }
         }
         __syncthreads();
     }
     if (!inpix) return;
+    int out[S];
+#pragma unroll
+    for (int k = 0; k < S; k++) out[k] = key_entry(rule, skey[(ly * kTileSize + lx) * S + k]);
+    int* ep = a.entries + pix * S;
+    if constexpr (S % 4 == 0) {
+#pragma unroll
+        for (int k = 0; k < S; k += 4) reinterpret_cast<int4*>(ep)[k / 4] = make_int4(out[k], out[k + 1], out[k + 2], out[k + 3]);
+    } else {
+#pragma unroll
+        for (int k = 0; k < S; k++) ep[k] = out[k];
+    }
+}
 
-    // ---- deferred shading of the visible primitives + resolve
+// Shading stage: one CTA per tile.  Distinct visible entries of the tile get one shading
+// set-up each (shared memory), then every pixel shades its distinct entries (the warp
+// iterates over list slots together), resolves its samples on chip and stores depth,
+// visibility and the resolved colour once.
+template <int S>
+__global__ void __launch_bounds__(kTileThreads) shade_kernel(PassArgs a) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    ShadeRecords& srec = *reinterpret_cast<ShadeRecords*>(smem_raw);
+    __shared__ int hkey[kHashSize], hslot[kHashSize];
+    __shared__ int nslots;
+
+    const int tile = blockIdx.x;
+    const int tx = tile % a.c.tiles_x, ty = tile / a.c.tiles_x;
+    const int tid = threadIdx.x;
+    const int lx = ((tid >> 2) & 7) * 2 + (tid & 1);
+    const int ly = (tid >> 5) * 2 + ((tid >> 1) & 1);
+    const int px = tx * kTileSize + lx, py = ty * kTileSize + ly;
+    const bool inpix = px < a.c.W && py < a.c.H;
+    const size_t pix = (size_t)py * a.c.W + px;
+    const KeyRule rule = key_rule(a.depth_func, a.depth_write);
+
+    for (int i = tid; i < kHashSize; i += kTileThreads) hkey[i] = -1;
+    if (tid == 0) nslots = 0;
+    int ent[S], hpos[S];
+    if (inpix) {
+        const int* ep = a.entries + pix * S;
+        if constexpr (S % 4 == 0) {
+#pragma unroll
+            for (int k = 0; k < S; k += 4) {
+                int4 v = reinterpret_cast<const int4*>(ep)[k / 4];
+                ent[k] = v.x; ent[k + 1] = v.y; ent[k + 2] = v.z; ent[k + 3] = v.w;
+            }
+        } else {
+#pragma unroll
+            for (int k = 0; k < S; k++) ent[k] = ep[k];
+        }
+    } else {
+#pragma unroll
+        for (int k = 0; k < S; k++) ent[k] = -1;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < S; k++) {
+        hpos[k] = -1;
+        if (ent[k] < 0) continue;
+        if (k > 0 && ent[k] == ent[k - 1]) {
+            hpos[k] = hpos[k - 1];
+            continue;
+        }
+        int h = (int)(((uint32_t)ent[k] * 2654435761u) >> 23) & (kHashSize - 1);
+        for (int probe = 0; probe < kHashSize; probe++) {
+            int prev = atomicCAS(&hkey[h], -1, ent[k]);
+            if (prev == -1) {
+                int slot = atomicAdd(&nslots, 1);
+                hslot[h] = slot;
+                if (slot < kShadeCap) srec.entry[slot] = ent[k];
+                hpos[k] = h;
+                break;
+            }
+            if (prev == ent[k]) {
+                hpos[k] = h;
+                break;
+            }
+            h = (h + 1) & (kHashSize - 1);
+        }
+    }
+    __syncthreads();
+    const int ncached = min(nslots, kShadeCap);
+    for (int i = tid; i < ncached; i += kTileThreads) {
+        ShadeGeom g;
+        RecordPlane pl;
+        setup_entry(a, srec.entry[i], &g, &pl);
+        store_shade_record(srec, i, g, pl);
+    }
+    __syncthreads();
+
     float bg[4];
     if (a.clear) {
         bg[0] = a.clear_color[0]; bg[1] = a.clear_color[1]; bg[2] = a.clear_color[2]; bg[3] = a.clear_color[3];
-    } else {
+    } else if (inpix) {
         decode_color(a, pix, bg);
     }
-    int ckey[2] = {-1, -1};
-    float ccol[2][4];
+    // distinct visible entries of this pixel, in sample order; sample k uses list slot which[k]
+    constexpr int U = S < 4 ? S : 4;  // slots shaded together across the warp
+    int uniq[U], which[S];
+    int nu = 0;
+#pragma unroll
+    for (int k = 0; k < S; k++) {
+        which[k] = -1;
+        if (ent[k] < 0) continue;
+        int found = -1;
+#pragma unroll
+        for (int j = 0; j < k; j++)
+            if (which[j] >= 0 && ent[j] == ent[k]) found = which[j];
+        if (found < 0) {
+            found = nu;
+#pragma unroll
+            for (int j = 0; j < U; j++)
+                if (j == nu) uniq[j] = ent[k];
+            nu++;
+        }
+        which[k] = found;
+    }
+    int nmax = min(nu, U);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) nmax = max(nmax, __shfl_xor_sync(0xffffffffu, nmax, o));
+    float scol[U][4];
+    RecordPlane spl[U];
+    for (int i = 0; i < nmax; i++) {
+        int e = -1;
+#pragma unroll
+        for (int j = 0; j < U; j++)
+            if (j == i) e = uniq[j];
+        float c[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+        RecordPlane pl{};
+        if (i < nu) {
+            int h = -1;
+#pragma unroll
+            for (int k = 0; k < S; k++)
+                if (which[k] == i && h < 0) h = hpos[k];
+            ShadeGeom g;
+            int cs = h >= 0 ? hslot[h] : kShadeCap;
+            if (cs < kShadeCap) load_shade_record(srec, cs, g, pl);
+            else setup_entry(a, e, &g, &pl);
+            shade_with(a, e, g, px, py, c);
+        }
+#pragma unroll
+        for (int j = 0; j < U; j++)
+            if (j == i) {
+                scol[j][0] = c[0]; scol[j][1] = c[1]; scol[j][2] = c[2]; scol[j][3] = c[3];
+                spl[j] = pl;
+            }
+    }
+    if (!inpix) return;
     float acc[4];
+    float dep[S];
 #pragma unroll
     for (int k = 0; k < S; k++) {
         float c[4];
-        if (id[k] < 0) {
+        const float d0 = a.clear ? a.clear_depth : a.depth[pix * S + k];
+        if (which[k] < 0) {
             c[0] = bg[0]; c[1] = bg[1]; c[2] = bg[2]; c[3] = bg[3];
-        } else if (id[k] == ckey[0]) {
-            c[0] = ccol[0][0]; c[1] = ccol[0][1]; c[2] = ccol[0][2]; c[3] = ccol[0][3];
-        } else if (id[k] == ckey[1]) {
-            c[0] = ccol[1][0]; c[1] = ccol[1][1]; c[2] = ccol[1][2]; c[3] = ccol[1][3];
+            dep[k] = d0;
         } else {
-            int g = id[k] >> 3, sub = id[k] & 7;
-            int di = find_draw(a, g);
-            const DrawDev& d = a.draws[di];
-            int t = g - __ldg(a.draw_start + di);
-            SubTri s;
-            setup_triangle_sub(a.c, d, t, sub, s);
-            shade_fragment(a.c, d, s, t, sub, px, py, c);
-            // keep the two most recent distinct primitives
-            ckey[1] = ckey[0];
-            ccol[1][0] = ccol[0][0]; ccol[1][1] = ccol[0][1]; ccol[1][2] = ccol[0][2]; ccol[1][3] = ccol[0][3];
-            ckey[0] = id[k];
-            ccol[0][0] = c[0]; ccol[0][1] = c[1]; ccol[0][2] = c[2]; ccol[0][3] = c[3];
+            RecordPlane pl{};
+            if (which[k] < U) {
+#pragma unroll
+                for (int j = 0; j < U; j++)
+                    if (j == which[k]) {
+                        c[0] = scol[j][0]; c[1] = scol[j][1]; c[2] = scol[j][2]; c[3] = scol[j][3];
+                        pl = spl[j];
+                    }
+            } else {  // more than U distinct primitives in one pixel: shade this one here
+                ShadeGeom g;
+                setup_entry(a, ent[k], &g, &pl);
+                shade_with(a, ent[k], g, px, py, c);
+            }
+            dep[k] = rule.write ? sample_depth(pl.z0, pl.dzdx, pl.dzdy, pl.X0, pl.Y0, px * 256 + a.c.sx[k],
+                                               py * 256 + a.c.sy[k])
+                                : d0;
         }
         if (k == 0) {
             acc[0] = c[0]; acc[1] = c[1]; acc[2] = c[2]; acc[3] = c[3];
@@ -308,9 +662,15 @@ __global__ void __launch_bounds__(kTileThreads, 2) tile_kernel(PassArgs a) {
     if (a.vis) {
         int* vp = a.vis + pix * S;
 #pragma unroll
-        for (int k = 0; k < S; k++) vp[k] = id[k] < 0 ? -1 : (id[k] >> 3);
+        for (int k = 0; k < S; k++) vp[k] = ent[k] < 0 ? -1 : (ent[k] >> 3);
     }
 }
+
+template <int S>
+size_t raster_smem_bytes() {
+    return sizeof(TileRecords) + (size_t)kTileThreads * S * sizeof(unsigned long long);
+}
+
 
 __global__ void mip_kernel(const uint32_t* __restrict__ src, int sw, int sh, uint32_t* __restrict__ dst, int dw, int dh) {
     int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
@@ -333,16 +693,33 @@ cudaError_t launch_mip_level(const uint32_t* src, int sw, int sh, uint32_t* dst,
     return cudaGetLastError();
 }
 
+template <int S>
+cudaError_t launch_tile(const PassArgs& a, int T, cudaStream_t stream, cudaEvent_t mid) {
+    static bool configured = false;
+    const size_t rbytes = raster_smem_bytes<S>(), sbytes = sizeof(ShadeRecords);
+    if (!configured) {
+        cudaError_t e = cudaFuncSetAttribute(raster_kernel<S>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rbytes);
+        if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(shade_kernel<S>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sbytes);
+        if (e != cudaSuccess) return e;
+        configured = true;
+    }
+    raster_kernel<S><<<T, kTileThreads, rbytes, stream>>>(a);
+    if (mid) cudaEventRecord(mid, stream);
+    shade_kernel<S><<<T, kTileThreads, sbytes, stream>>>(a);
+    return cudaSuccess;
+}
+
 cudaError_t launch_pass(const PassArgs& a, cudaStream_t stream, cudaEvent_t* ev) {
     const int T = a.c.tiles_x * a.c.tiles_y;
     if (ev) cudaEventRecord(ev[0], stream);
     if (a.total_tris > 0) {
         int blocks = (a.total_tris + 255) / 256;
-        bin_kernel<false><<<blocks, 256, 0, stream>>>(a);
+        bin_count_kernel<<<blocks, 256, 0, stream>>>(a);
         if (ev) cudaEventRecord(ev[1], stream);
         scan_kernel<<<1, 1024, 0, stream>>>(a, T);
         if (ev) cudaEventRecord(ev[2], stream);
-        bin_kernel<true><<<blocks, 256, 0, stream>>>(a);
+        bin_scatter_kernel<<<blocks, 256, 0, stream>>>(a);
         if (ev) cudaEventRecord(ev[3], stream);
     } else if (ev) {
         cudaEventRecord(ev[1], stream);
@@ -350,15 +727,16 @@ cudaError_t launch_pass(const PassArgs& a, cudaStream_t stream, cudaEvent_t* ev)
         cudaEventRecord(ev[3], stream);
     }
     cudaError_t err = cudaSuccess;
+    cudaEvent_t mid = ev ? ev[4] : nullptr;
     switch (a.c.S) {
-    case 1: tile_kernel<1><<<T, kTileThreads, 0, stream>>>(a); break;
-    case 2: tile_kernel<2><<<T, kTileThreads, 0, stream>>>(a); break;
-    case 4: tile_kernel<4><<<T, kTileThreads, 0, stream>>>(a); break;
-    case 8: tile_kernel<8><<<T, kTileThreads, 0, stream>>>(a); break;
-    case 16: tile_kernel<16><<<T, kTileThreads, 0, stream>>>(a); break;
+    case 1: err = launch_tile<1>(a, T, stream, mid); break;
+    case 2: err = launch_tile<2>(a, T, stream, mid); break;
+    case 4: err = launch_tile<4>(a, T, stream, mid); break;
+    case 8: err = launch_tile<8>(a, T, stream, mid); break;
+    case 16: err = launch_tile<16>(a, T, stream, mid); break;
     default: err = cudaErrorInvalidValue;
     }
-    if (ev) cudaEventRecord(ev[4], stream);
+    if (ev) cudaEventRecord(ev[5], stream);
     return err != cudaSuccess ? err : cudaGetLastError();
 }
 

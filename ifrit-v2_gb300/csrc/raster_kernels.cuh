@@ -23,6 +23,7 @@ struct PassArgs {
     void* color;             // resolved colour (format-dependent)
     float* depth;            // per-sample depth [H][W][S]
     int* vis;                // per-sample primitive id [H][W][S] or nullptr
+    int* entries;            // scratch: per-sample winning entry [H][W][S] (raster -> shade)
     int clear;
     float clear_color[4];
     float clear_depth;
@@ -33,6 +34,7 @@ struct PassArgs {
     uint32_t* tile_offset;   // [T + 1]
     uint32_t* tile_cursor;   // [T]
     uint32_t* pairs;         // (global triangle << 3 | fan index), capacity entries
+    TriRecord* records;      // [total_tris] compact set-ups written by the counting binner
     uint32_t pair_capacity;
     uint32_t* status;        // StatusWord
 };
@@ -41,8 +43,8 @@ struct PassArgs {
 
 // Host-callable launchers (defined in raster_kernels.cu).
 namespace ifr {
-// ev: optional array of 5 events recorded before binning, after counting, after the scan,
-// after scattering and after the tile kernel (per-stage device timing).
+// ev: optional array of 6 events recorded before binning, after counting, after the scan,
+// after scattering, after the raster kernel and after the shade kernel (per-stage timing).
 cudaError_t launch_pass(const PassArgs& a, cudaStream_t stream, cudaEvent_t* ev);
 cudaError_t launch_mip_level(const uint32_t* src, int sw, int sh, uint32_t* dst, int dw, int dh, cudaStream_t stream);
 }  // namespace ifr

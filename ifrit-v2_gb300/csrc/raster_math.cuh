@@ -44,6 +44,7 @@ struct DrawDev {
     const uint32_t* texels;
     int tex_w, tex_h, tex_levels;
     SamplerDev sampler;
+    int lvl_off[16], lvl_w[16], lvl_h[16];  // mip table: texel offset and size of each level
 };
 
 // Pass-wide constants.
@@ -70,7 +71,18 @@ struct SubTri {
     int64_t C[3], Cb[3];
     float dzdx, dzdy;
     int px0, px1, py0, py1;
+    int swapped;  // vertices 1 and 2 were exchanged to make the area positive
 };
+
+// Compact set-up of an unclipped triangle, written once per triangle by the counting binner
+// and reused by the scattering binner and the tile kernel (64 bytes, four 16-byte vectors).
+struct __align__(16) TriRecord {
+    int32_t X0, Y0, X1, Y1;
+    int32_t X2, Y2, flags, pad0;
+    float z0, dzdx, dzdy, iw0;
+    float iw1, iw2, pad1, pad2;
+};
+enum { REC_VALID = 1, REC_SWAPPED = 2, REC_CLIPPED = 4 };
 
 __device__ __forceinline__ int64_t floordiv256(int64_t a) { return a >= 0 ? a / 256 : -((-a + 255) / 256); }
 __device__ __forceinline__ int64_t ceildiv256(int64_t a) { return -floordiv256(-a); }
@@ -128,6 +140,34 @@ static __device__ __noinline__ int clip_polygon(const PassConst& c, CVert* poly)
     return n;
 }
 
+// Pixel range that may hold covered samples (conservative in the sample pattern's extent).
+__device__ __forceinline__ bool sub_bbox(const PassConst& c, SubTri& o) {
+    int32_t xmin = min(o.X[0], min(o.X[1], o.X[2])), xmax = max(o.X[0], max(o.X[1], o.X[2]));
+    int32_t ymin = min(o.Y[0], min(o.Y[1], o.Y[2])), ymax = max(o.Y[0], max(o.Y[1], o.Y[2]));
+    int64_t px0 = ceildiv256((int64_t)xmin - c.smax_x), px1 = floordiv256((int64_t)xmax - c.smin_x);
+    int64_t py0 = ceildiv256((int64_t)ymin - c.smax_y), py1 = floordiv256((int64_t)ymax - c.smin_y);
+    if (px0 < 0) px0 = 0;
+    if (py0 < 0) py0 = 0;
+    if (px1 > c.W - 1) px1 = c.W - 1;
+    if (py1 > c.H - 1) py1 = c.H - 1;
+    if (px0 > px1 || py0 > py1) return false;
+    o.px0 = (int)px0; o.px1 = (int)px1; o.py0 = (int)py0; o.py1 = (int)py1;
+    return true;
+}
+
+// Edge functions E_i = A_i x + B_i y + C_i (positive inside) and their top-left biased form.
+__device__ __forceinline__ void sub_edges(SubTri& o) {
+#pragma unroll
+    for (int i = 0; i < 3; i++) {
+        int j = (i + 1) % 3, k = (i + 2) % 3;
+        o.A[i] = o.Y[j] - o.Y[k];
+        o.B[i] = o.X[k] - o.X[j];
+        o.C[i] = (int64_t)(o.Y[k] - o.Y[j]) * o.X[j] - (int64_t)(o.X[k] - o.X[j]) * o.Y[j];
+        bool topleft = (o.A[i] > 0) || (o.A[i] == 0 && o.B[i] > 0);
+        o.Cb[i] = o.C[i] - (topleft ? 0 : 1);
+    }
+}
+
 // Projection, 16.8 snap, cull, orientation normalisation, edge functions, depth plane and
 // the pixel range that may hold covered samples.  Returns false when nothing can be covered.
 __device__ __forceinline__ bool setup_sub(const PassConst& c, const DrawDev& d, const CVert& v0, const CVert& v1,
@@ -154,7 +194,9 @@ __device__ __forceinline__ bool setup_sub(const PassConst& c, const DrawDev& d, 
     if (d.cull_mode == 3) return false;
     if (d.cull_mode == 1 && front) return false;
     if (d.cull_mode == 2 && !front) return false;
+    o.swapped = 0;
     if (a2 < 0) {
+        o.swapped = 1;
         int32_t t;
         float tf;
         t = o.X[1]; o.X[1] = o.X[2]; o.X[2] = t;
@@ -165,25 +207,8 @@ __device__ __forceinline__ bool setup_sub(const PassConst& c, const DrawDev& d, 
         for (int k = 0; k < 3; k++) { tf = o.bary[1][k]; o.bary[1][k] = o.bary[2][k]; o.bary[2][k] = tf; }
         a2 = -a2;
     }
-    int32_t xmin = min(o.X[0], min(o.X[1], o.X[2])), xmax = max(o.X[0], max(o.X[1], o.X[2]));
-    int32_t ymin = min(o.Y[0], min(o.Y[1], o.Y[2])), ymax = max(o.Y[0], max(o.Y[1], o.Y[2]));
-    int64_t px0 = ceildiv256((int64_t)xmin - c.smax_x), px1 = floordiv256((int64_t)xmax - c.smin_x);
-    int64_t py0 = ceildiv256((int64_t)ymin - c.smax_y), py1 = floordiv256((int64_t)ymax - c.smin_y);
-    if (px0 < 0) px0 = 0;
-    if (py0 < 0) py0 = 0;
-    if (px1 > c.W - 1) px1 = c.W - 1;
-    if (py1 > c.H - 1) py1 = c.H - 1;
-    if (px0 > px1 || py0 > py1) return false;
-    o.px0 = (int)px0; o.px1 = (int)px1; o.py0 = (int)py0; o.py1 = (int)py1;
-#pragma unroll
-    for (int i = 0; i < 3; i++) {
-        int j = (i + 1) % 3, k = (i + 2) % 3;
-        o.A[i] = o.Y[j] - o.Y[k];
-        o.B[i] = o.X[k] - o.X[j];
-        o.C[i] = (int64_t)(o.Y[k] - o.Y[j]) * o.X[j] - (int64_t)(o.X[k] - o.X[j]) * o.Y[j];
-        bool topleft = (o.A[i] > 0) || (o.A[i] == 0 && o.B[i] > 0);
-        o.Cb[i] = o.C[i] - (topleft ? 0 : 1);
-    }
+    if (!sub_bbox(c, o)) return false;
+    sub_edges(o);
     float dX1 = (float)(o.X[1] - o.X[0]), dY1 = (float)(o.Y[1] - o.Y[0]);
     float dX2 = (float)(o.X[2] - o.X[0]), dY2 = (float)(o.Y[2] - o.Y[0]);
     float dz1 = o.z[1] - o.z[0], dz2 = o.z[2] - o.z[0];
@@ -233,6 +258,51 @@ __device__ __forceinline__ bool setup_triangle_sub(const PassConst& c, const Dra
     int n = clip_polygon(c, poly);
     if (sub + 2 >= n) return false;
     return setup_sub(c, d, poly[0], poly[sub + 1], poly[sub + 2], o);
+}
+
+__device__ __forceinline__ void record_from_sub(const SubTri& s, TriRecord& r) {
+    r.X0 = s.X[0]; r.Y0 = s.Y[0]; r.X1 = s.X[1]; r.Y1 = s.Y[1];
+    r.X2 = s.X[2]; r.Y2 = s.Y[2];
+    r.flags = REC_VALID | (s.swapped ? REC_SWAPPED : 0);
+    r.pad0 = 0;
+    r.z0 = s.z[0]; r.dzdx = s.dzdx; r.dzdy = s.dzdy; r.iw0 = s.iw[0];
+    r.iw1 = s.iw[1]; r.iw2 = s.iw[2]; r.pad1 = 0.0f; r.pad2 = 0.0f;
+}
+
+// Rebuilds the set-up of an unclipped triangle from its record; every field equals what
+// setup_sub computed (integers are recomputed exactly, floats are stored values).
+__device__ __forceinline__ bool sub_from_record(const PassConst& c, const TriRecord* rp, SubTri& o) {
+    const int4 q0 = __ldg(reinterpret_cast<const int4*>(rp));
+    const int4 q1 = __ldg(reinterpret_cast<const int4*>(rp) + 1);
+    const float4 q2 = __ldg(reinterpret_cast<const float4*>(rp) + 2);
+    const float4 q3 = __ldg(reinterpret_cast<const float4*>(rp) + 3);
+    o.X[0] = q0.x; o.Y[0] = q0.y; o.X[1] = q0.z; o.Y[1] = q0.w;
+    o.X[2] = q1.x; o.Y[2] = q1.y;
+    const int flags = q1.z;
+    o.swapped = (flags & REC_SWAPPED) != 0;
+    o.z[0] = q2.x; o.dzdx = q2.y; o.dzdy = q2.z;
+    o.iw[0] = q2.w; o.iw[1] = q3.x; o.iw[2] = q3.y;
+#pragma unroll
+    for (int i = 0; i < 3; i++)
+#pragma unroll
+        for (int k = 0; k < 3; k++) o.bary[i][k] = 0.0f;
+    o.bary[0][0] = 1.0f;
+    o.bary[1][o.swapped ? 2 : 1] = 1.0f;
+    o.bary[2][o.swapped ? 1 : 2] = 1.0f;
+    if (!sub_bbox(c, o)) return false;
+    sub_edges(o);
+    return true;
+}
+
+// Set-up of fan triangle `sub` of triangle t, from its record when it is an unclipped one.
+__device__ __forceinline__ bool setup_entry_sub(const PassConst& c, const DrawDev& d, const TriRecord* records, int g,
+                                                int t, int sub, SubTri& o) {
+    if (records && sub == 0) {
+        int flags = __ldg(&records[g].flags);
+        if (flags & REC_VALID) return sub_from_record(c, records + g, o);
+        if (!(flags & REC_CLIPPED)) return false;
+    }
+    return setup_triangle_sub(c, d, t, sub, o);
 }
 
 __device__ __forceinline__ bool covered(const int32_t* A, const int32_t* B, const int64_t* Cb, int32_t x, int32_t y) {
@@ -289,11 +359,15 @@ __device__ __forceinline__ float log2_series(float x) {
 }
 
 // ------------------------------------------------------------------ textures
+// Byte b -> float(b) exactly via the 2^23 bias trick (one logic op and one add, both full
+// rate), then the same scale the conversion instruction path would use.
+__device__ __forceinline__ float byte_to_float(uint32_t b) { return __uint_as_float(0x4B000000u | b) - 8388608.0f; }
+
 __device__ __forceinline__ void unpack_rgba8(uint32_t t, float c[4]) {
-    c[0] = (float)(t & 255u) * kInv255;
-    c[1] = (float)((t >> 8) & 255u) * kInv255;
-    c[2] = (float)((t >> 16) & 255u) * kInv255;
-    c[3] = (float)(t >> 24) * kInv255;
+    c[0] = byte_to_float(t & 255u) * kInv255;
+    c[1] = byte_to_float((t >> 8) & 255u) * kInv255;
+    c[2] = byte_to_float((t >> 16) & 255u) * kInv255;
+    c[3] = byte_to_float(t >> 24) * kInv255;
 }
 
 __device__ __forceinline__ float lerpf_(float a, float b, float t) { return a + t * (b - a); }
@@ -301,15 +375,29 @@ __device__ __forceinline__ float lerpf_(float a, float b, float t) { return a + 
 __device__ __forceinline__ bool tex_address(int mode, float& c, int n) {
     float nf = (float)n;
     float v = c;
+    // fmodf is exact, and so are the shortcuts below on the ranges where they are taken
+    // (Sterbenz: v - n is exact for n <= v <= 2n; for |v| < n fmodf returns v itself).
     switch (mode) {
     case 0:
-        v = fmodf(v, nf);
-        if (v < 0.0f) v = v + nf;
+        if (v >= 0.0f && v < nf) {
+        } else if (v >= nf && v < nf + nf) {
+            v = v - nf;
+        } else if (v < 0.0f && v > -nf) {
+            v = v + nf;
+        } else {
+            v = fmodf(v, nf);
+            if (v < 0.0f) v = v + nf;
+        }
         break;
     case 1: {
         float n2 = nf + nf;
-        v = fmodf(v, n2);
-        if (v < 0.0f) v = v + n2;
+        if (v >= 0.0f && v < n2) {
+        } else if (v < 0.0f && v > -n2) {
+            v = v + n2;
+        } else {
+            v = fmodf(v, n2);
+            if (v < 0.0f) v = v + n2;
+        }
         v = fminf(v, n2 - v);
         break;
     }
@@ -331,15 +419,9 @@ __device__ __forceinline__ bool tex_address(int mode, float& c, int n) {
 }
 
 __device__ __forceinline__ void tex_level_info(const DrawDev& d, int level, int& w, int& h, int& off) {
-    int ww = d.tex_w, hh = d.tex_h, o = 0;
-    for (int i = 0; i < level; i++) {
-        o += ww * hh;
-        ww = (ww + 1) >> 1;
-        hh = (hh + 1) >> 1;
-    }
-    w = ww;
-    h = hh;
-    off = o;
+    w = d.lvl_w[level];
+    h = d.lvl_h[level];
+    off = d.lvl_off[level];
 }
 
 __device__ __forceinline__ void tex_sample_level(const DrawDev& d, int level, float u, float v, float out[4]) {
@@ -376,19 +458,33 @@ __device__ __forceinline__ void tex_sample_level(const DrawDev& d, int level, fl
     }
 }
 
-__device__ __forceinline__ void tex_trilinear(const DrawDev& d, float u, float v, float lam, float out[4]) {
+struct LodPick {
+    int lo, hi;
+    float t;
+};
+
+__device__ __forceinline__ LodPick pick_lod(const DrawDev& d, float lam) {
     float maxl = (float)(d.tex_levels - 1);
     if (!(lam > 0.0f)) lam = 0.0f;
     if (lam > maxl) lam = maxl;
-    int lo = (int)floorf(lam);
-    float t = lam - (float)lo;
-    int hi = min(lo + 1, d.tex_levels - 1);
-    tex_sample_level(d, lo, u, v, out);
-    if (hi == lo || t == 0.0f) return;
+    LodPick p;
+    p.lo = (int)floorf(lam);
+    p.t = lam - (float)p.lo;
+    p.hi = min(p.lo + 1, d.tex_levels - 1);
+    return p;
+}
+
+__device__ __forceinline__ void tex_trilinear_at(const DrawDev& d, const LodPick& p, float u, float v, float out[4]) {
+    tex_sample_level(d, p.lo, u, v, out);
+    if (p.hi == p.lo || p.t == 0.0f) return;
     float c1[4];
-    tex_sample_level(d, hi, u, v, c1);
+    tex_sample_level(d, p.hi, u, v, c1);
 #pragma unroll
-    for (int i = 0; i < 4; i++) out[i] = lerpf_(out[i], c1[i], t);
+    for (int i = 0; i < 4; i++) out[i] = lerpf_(out[i], c1[i], p.t);
+}
+
+__device__ __forceinline__ void tex_trilinear(const DrawDev& d, float u, float v, float lam, float out[4]) {
+    tex_trilinear_at(d, pick_lod(d, lam), u, v, out);
 }
 
 __device__ __forceinline__ float finite_or_zero(float x) { return isfinite(x) ? x : 0.0f; }
@@ -420,13 +516,14 @@ __device__ __forceinline__ void tex_sample(const DrawDev& d, float u, float v, f
     int n = (int)ceilf(ratio);
     if (n < 1) n = 1;
     float lam = log2_series(pmax / (float)n) + d.sampler.lod_bias;
+    const LodPick lp = pick_lod(d, lam);
     float du = major_x ? dudx : dudy, dv = major_x ? dvdx : dvdy;
     float acc[4] = {0.0f, 0.0f, 0.0f, 0.0f};
     float inv = (float)(n + 1);
     for (int i = 0; i < n; i++) {
         float t = (float)(i + 1) / inv - 0.5f;
         float cc[4];
-        tex_trilinear(d, u + du * t, v + dv * t, lam, cc);
+        tex_trilinear_at(d, lp, u + du * t, v + dv * t, cc);
 #pragma unroll
         for (int k = 0; k < 4; k++) acc[k] = acc[k] + cc[k];
     }
@@ -436,8 +533,28 @@ __device__ __forceinline__ void tex_sample(const DrawDev& d, float u, float v, f
 }
 
 // ------------------------------------------------------------------ interpolation + shading
+// What interpolation needs of a (sub-)triangle.
+struct ShadeGeom {
+    int32_t A[3], B[3];
+    int64_t C[3];
+    float iw[3];
+    float bary[3][3];
+};
+
+__device__ __forceinline__ void shade_geom_from(const SubTri& s, ShadeGeom& g) {
+#pragma unroll
+    for (int i = 0; i < 3; i++) {
+        g.A[i] = s.A[i];
+        g.B[i] = s.B[i];
+        g.C[i] = s.C[i];
+        g.iw[i] = s.iw[i];
+#pragma unroll
+        for (int k = 0; k < 3; k++) g.bary[i][k] = s.bary[i][k];
+    }
+}
+
 // Perspective-correct interpolation of the draw's attribute at fixed-point position (x, y).
-__device__ __forceinline__ void interp_attr(const SubTri& s, const DrawDev& d, const float* a0, const float* a1,
+__device__ __forceinline__ void interp_attr(const ShadeGeom& s, int attr_count, const float* a0, const float* a1,
                                             const float* a2, int32_t x, int32_t y, float out[4]) {
     float p[3];
 #pragma unroll
@@ -453,15 +570,15 @@ __device__ __forceinline__ void interp_attr(const SubTri& s, const DrawDev& d, c
     for (int k = 0; k < 3; k++) W[k] = (b0 * s.bary[0][k] + b1 * s.bary[1][k]) + b2 * s.bary[2][k];
 #pragma unroll
     for (int k = 0; k < 4; k++) out[k] = 0.0f;
-    for (int k = 0; k < d.attr_count; k++)
+    for (int k = 0; k < attr_count; k++)
         out[k] = (W[0] * __ldg(a0 + k) + W[1] * __ldg(a1 + k)) + W[2] * __ldg(a2 + k);
 }
 
-// Fragment colour of pixel (px, py) for triangle t / sub-triangle s.  Derivatives for texture
-// LOD are the fine 2x2-quad differences: attribute at the quad's right column minus left
-// column (same row) and bottom row minus top row (same column), each evaluated for this
-// primitive exactly as a helper invocation would.
-__device__ __forceinline__ void shade_fragment(const PassConst& c, const DrawDev& d, const SubTri& s, int t, int sub,
+// Fragment colour of pixel (px, py) for triangle t / fan index `sub` of draw d.  Texture
+// LOD uses fine 2x2-quad derivatives: the attribute at the quad's right column minus the
+// left column (same row) and bottom row minus top row (same column), each evaluated for this
+// primitive exactly as a helper invocation would evaluate it.
+__device__ __forceinline__ void shade_fragment(const PassConst& c, const DrawDev& d, const ShadeGeom& s, int t, int sub,
                                                int px, int py, float col[4]) {
     if (d.shading == SHADE_PRIMID) {
         col[0] = (float)(d.prim_base + t); col[1] = (float)sub; col[2] = 0.0f; col[3] = 1.0f;
@@ -472,16 +589,15 @@ __device__ __forceinline__ void shade_fragment(const PassConst& c, const DrawDev
     const float* a2 = d.vertices + (size_t)__ldg(d.indices + 3 * (size_t)t + 2) * d.stride + d.attr_offset;
     int32_t qx = px * 256 + c.shade_x, qy = py * 256 + c.shade_y;
     float a[4];
-    interp_attr(s, d, a0, a1, a2, qx, qy, a);
+    interp_attr(s, d.attr_count, a0, a1, a2, qx, qy, a);
     if (d.shading == SHADE_TEXTURED) {
-        int xl = px & ~1, yt = py & ~1;
-        float al[4], ar[4], at[4], ab[4];
-        interp_attr(s, d, a0, a1, a2, xl * 256 + c.shade_x, qy, al);
-        interp_attr(s, d, a0, a1, a2, (xl + 1) * 256 + c.shade_x, qy, ar);
-        interp_attr(s, d, a0, a1, a2, qx, yt * 256 + c.shade_y, at);
-        interp_attr(s, d, a0, a1, a2, qx, (yt + 1) * 256 + c.shade_y, ab);
-        float dudx = ar[0] - al[0], dvdx = ar[1] - al[1];
-        float dudy = ab[0] - at[0], dvdy = ab[1] - at[1];
+        float ah[4], av[4];  // horizontal and vertical quad partners
+        interp_attr(s, d.attr_count, a0, a1, a2, (px ^ 1) * 256 + c.shade_x, qy, ah);
+        interp_attr(s, d.attr_count, a0, a1, a2, qx, (py ^ 1) * 256 + c.shade_y, av);
+        float dudx = (px & 1) ? a[0] - ah[0] : ah[0] - a[0];
+        float dvdx = (px & 1) ? a[1] - ah[1] : ah[1] - a[1];
+        float dudy = (py & 1) ? a[0] - av[0] : av[0] - a[0];
+        float dvdy = (py & 1) ? a[1] - av[1] : av[1] - a[1];
         tex_sample(d, a[0], a[1], dudx, dvdx, dudy, dvdy, col);
         return;
     }

@@ -293,8 +293,8 @@ class Renderer:
         check("iftrSetStageTiming", self.lib.iftrSetStageTiming(self.h, int(enable)))
 
     def stage_times(self):
-        ms = (ctypes.c_float * 4)()
-        check("iftrGetStageTimes", self.lib.iftrGetStageTimes(self.h, ms, 4))
+        ms = (ctypes.c_float * 5)()
+        check("iftrGetStageTimes", self.lib.iftrGetStageTimes(self.h, ms, 5))
         return list(ms)
 
     def mark_geometry_dirty(self):

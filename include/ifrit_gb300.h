@@ -147,8 +147,9 @@ IFTR_API int iftrReadbackDepth(IfritGbRenderer* h, float* dst, size_t count);
 IFTR_API int iftrReadbackVisibility(IfritGbRenderer* h, int* dst, size_t count);
 IFTR_API int iftrGetStats(IfritGbRenderer* h, IfritGbStats* out);
 /* Per-stage device timing of the last pass, from CUDA events on the renderer's stream:
- * ms[0] counting binner, ms[1] list-offset scan, ms[2] scattering binner, ms[3] tile
- * raster/shade/resolve kernel.  Enable before the draw; read after iftrFinish/iftrDrawLegacy. */
+ * ms[0] counting binner, ms[1] list-offset scan, ms[2] scattering binner, ms[3] tile raster
+ * (coverage + depth test), ms[4] tile shading + resolve.  Enable before the draw; read after
+ * iftrFinish/iftrDrawLegacy. */
 IFTR_API int iftrSetStageTiming(IfritGbRenderer* h, int enable);
 IFTR_API int iftrGetStageTimes(IfritGbRenderer* h, float* ms, int n);
 IFTR_API const char* iftrGetErrorString(int status);
