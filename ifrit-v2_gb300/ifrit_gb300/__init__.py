@@ -42,7 +42,7 @@ EXPORTED = [
     "iftrAllocateVertexBuffer", "iftrSetVertexBufferValueFloat4", "iftrSetVertexBufferData",
     "ifbufCreateBufferManager", "ifbufDestroyBufferManager", "ifbufCreateBuffer", "ifbufDestroyBuffer",
     "ifbufBufferData", "iftrSetStageTiming", "iftrGetStageTimes", "iftrGetVertexBufferRawData",
-    "iftrSetVertexBufferDirty", "ifbufGetBufferRawData", "ifbufSetBufferDirty",
+    "iftrSetVertexBufferDirty", "ifbufGetBufferRawData", "ifbufSetBufferDirty", "iftrDrawNoAlloc",
 ]
 
 
@@ -56,6 +56,20 @@ class SamplerState(ctypes.Structure):
     _fields_ = [("filterMode", ctypes.c_int), ("addressModeU", ctypes.c_int), ("addressModeV", ctypes.c_int),
                 ("addressModeW", ctypes.c_int), ("borderColor", ctypes.c_int), ("anisotropyEnable", ctypes.c_int),
                 ("maxAnisotropy", ctypes.c_float), ("lodBias", ctypes.c_float)]
+
+
+class NoAllocPass(ctypes.Structure):
+    """IfritGbNoAllocPass (include/ifrit_gb300.h)."""
+    _fields_ = [("vertices", ctypes.c_void_p), ("strideFloats", ctypes.c_int), ("numVertices", ctypes.c_int),
+                ("attrOffsetFloats", ctypes.c_int), ("attrCount", ctypes.c_int), ("indices", ctypes.c_void_p),
+                ("numIndices", ctypes.c_int), ("mvp", ctypes.c_float * 16), ("width", ctypes.c_int),
+                ("height", ctypes.c_int), ("samples", ctypes.c_int), ("colorFormat", ctypes.c_int),
+                ("color", ctypes.c_void_p), ("depth", ctypes.c_void_p), ("visibility", ctypes.c_void_p),
+                ("clear", ctypes.c_int), ("clearColor", ctypes.c_float * 4), ("clearDepth", ctypes.c_float),
+                ("depthFunc", ctypes.c_int), ("depthTest", ctypes.c_int), ("depthWrite", ctypes.c_int),
+                ("cullMode", ctypes.c_int), ("frontCounterClockwise", ctypes.c_int), ("shadingModel", ctypes.c_int),
+                ("texels", ctypes.c_void_p), ("texWidth", ctypes.c_int), ("texHeight", ctypes.c_int),
+                ("texLevels", ctypes.c_int), ("sampler", SamplerState)]
 
 
 class Stats(ctypes.Structure):
@@ -112,7 +126,7 @@ def load(build_if_missing=True):
         "ifbufDestroyBufferManager": [vp], "ifbufCreateBuffer": [vp, sz], "ifbufDestroyBuffer": [vp],
         "ifbufBufferData": [vp, vp, sz, sz], "iftrSetStageTiming": [vp, ip], "iftrGetStageTimes": [vp, fp, ip],
         "iftrGetVertexBufferRawData": [vp], "iftrSetVertexBufferDirty": [vp], "ifbufGetBufferRawData": [vp],
-        "ifbufSetBufferDirty": [vp],
+        "ifbufSetBufferDirty": [vp], "iftrDrawNoAlloc": [ctypes.POINTER(NoAllocPass), vp],
     }
     for name, args in sig.items():
         getattr(lib, name).argtypes = args

@@ -154,6 +154,48 @@ IFTR_API int iftrSetStageTiming(IfritGbRenderer* h, int enable);
 IFTR_API int iftrGetStageTimes(IfritGbRenderer* h, float* ms, int n);
 IFTR_API const char* iftrGetErrorString(int status);
 
+/* ---- allocation-free pass (no counterpart in the reference)
+ * For callers that cannot allocate device memory at draw time: plugins inside a host
+ * application that owns all GPU memory, real-time loops with an allocation budget of zero,
+ * and code that records its work into an already-built memory plan.  iftrDrawNoAlloc renders
+ * one pass from device buffers the caller owns into device outputs the caller owns.  All
+ * intermediate data (binning lists, set-up records, per-sample winners, status words) lives in
+ * one file-scope device array inside the library, of IFTR_NOALLOC_SCRATCH_BYTES, which every
+ * GPU that loads the library holds until the process exits.  The call makes no cudaMalloc,
+ * cudaFree or other allocating call.  Its first call on a device (with that device current)
+ * looks up the array's device address once; make that first call before any stream capture.
+ * The array is shared by every call and keeps the last call's contents: calls that overlap on
+ * the GPU (different streams or threads) race and must be serialised by the caller.  The call
+ * is synchronous on `cudaStream` (it reads a status word back) and returns
+ * IFTR_ERR_INVALID_ARG for sizes above the limits below and IFTR_ERR_OVERFLOW if the scene
+ * produces more (triangle, tile) overlaps than the list capacity. */
+#define IFTR_NOALLOC_MAX_TRIANGLES (1 << 16)   /* numIndices / 3 */
+#define IFTR_NOALLOC_MAX_SAMPLES (1 << 21)     /* width * height * samples */
+#define IFTR_NOALLOC_MAX_TILE_PAIRS (1 << 19)  /* (triangle, 16x16 tile) overlaps */
+#define IFTR_NOALLOC_MAX_TILES 8192            /* ceil(width/16) * ceil(height/16) */
+#define IFTR_NOALLOC_SCRATCH_BYTES (15u << 20)
+typedef struct {
+    const float* vertices;          /* device, AoS floats; position = floats 0..2 */
+    int strideFloats, numVertices, attrOffsetFloats, attrCount;
+    const int* indices;             /* device, 3 per triangle */
+    int numIndices;
+    float mvp[16];                  /* row-major, clip = mvp * (x, y, z, 1) */
+    int width, height, samples;     /* samples: 1, 2, 4, 8 or 16 */
+    int colorFormat;                /* IFTR_FORMAT_* */
+    void* color;                    /* device, resolved colour */
+    float* depth;                   /* device, per-sample depth [H][W][S] */
+    int* visibility;                /* device, per-sample primitive id, or NULL */
+    int clear;
+    float clearColor[4];
+    float clearDepth;
+    int depthFunc, depthTest, depthWrite, cullMode, frontCounterClockwise;
+    int shadingModel;               /* IFTR_FS_* */
+    const uint32_t* texels;         /* device RGBA8 mip chain (IFTR_FS_TEXTURED), level after level */
+    int texWidth, texHeight, texLevels;
+    IfritGbSampler sampler;
+} IfritGbNoAllocPass;
+IFTR_API int iftrDrawNoAlloc(const IfritGbNoAllocPass* pass, void* cudaStream);
+
 /* ---- framebuffers and images (ECE:31-40, CE:25-31) */
 IFTR_API IfritGbFrameBuffer* iftrCreateFrameBuffer(void);                            /* ECE:31 */
 IFTR_API int iftrDestroyFrameBuffer(IfritGbFrameBuffer* fb);                         /* ECE:33 */
