@@ -412,6 +412,7 @@ int enqueue_draw(IfritGbRenderer* h, int numIndices, int clear) {
     }
     fill_state(h, d);
     if (d.shading == IFTR_FS_TEXTURED && (!d.texels || d.tex_levels <= 0)) return IFTR_ERR_STATE;
+
     if (d.blend_enable || (d.depth_write && d.depth_func == IF_COMPARE_OP_NOT_EQUAL)) return IFTR_ERR_UNSUPPORTED;
     h->h_draws[0] = d;
     h->h_draw_start[0] = 0;

@@ -251,9 +251,7 @@ struct RecordPlane {
     int32_t X0, Y0;
 };
 
-// Shading of one visible (sub-)triangle at one pixel; out of line so the kernel carries a
-// single copy of the (large) texture-filtering code.
-__device__ __noinline__ void shade_with(const PassArgs& a, int e, const ShadeGeom& g, int px, int py, float* col) {
+__device__ __forceinline__ void shade_entry_geom(const PassArgs& a, int e, const ShadeGeom& g, int px, int py, float* col) {
     int gi = e >> 3, sub = e & 7;
     int di = find_draw(a, gi);
     shade_fragment(a.c, a.draws[di], g, gi - __ldg(a.draw_start + di), sub, px, py, col);
@@ -280,53 +278,11 @@ __device__ __noinline__ bool setup_raster_entry(const PassArgs& a, uint32_t e, S
     return setup_entry_sub(a.c, a.draws[di], a.records, g, g - __ldg(a.draw_start + di), sub, *s);
 }
 
-constexpr int kShadeCap = 192;   // visible entries per tile set up once in shared memory
-constexpr int kHashSize = 512;   // open-addressing table entry -> shade slot
-
-// Per-tile cache of shading set-ups, overlaid on the raster batch records once rasterisation
-// of the tile is complete.
-struct ShadeRecords {
-    int32_t A[3][kShadeCap], B[3][kShadeCap];
-    long long C[3][kShadeCap];
-    float iw[3][kShadeCap];
-    float bary[9][kShadeCap];
-    float z0[kShadeCap], dzdx[kShadeCap], dzdy[kShadeCap];
-    int32_t X0[kShadeCap], Y0[kShadeCap];
-    int32_t entry[kShadeCap];
-};
-
-__device__ __forceinline__ void load_shade_record(const ShadeRecords& r, int i, ShadeGeom& g, RecordPlane& pl) {
-#pragma unroll
-    for (int k = 0; k < 3; k++) {
-        g.A[k] = r.A[k][i];
-        g.B[k] = r.B[k][i];
-        g.C[k] = r.C[k][i];
-        g.iw[k] = r.iw[k][i];
-#pragma unroll
-        for (int j = 0; j < 3; j++) g.bary[k][j] = r.bary[3 * k + j][i];
-    }
-    pl.z0 = r.z0[i];
-    pl.dzdx = r.dzdx[i];
-    pl.dzdy = r.dzdy[i];
-    pl.X0 = r.X0[i];
-    pl.Y0 = r.Y0[i];
-}
-
-__device__ __forceinline__ void store_shade_record(ShadeRecords& r, int i, const ShadeGeom& g, const RecordPlane& pl) {
-#pragma unroll
-    for (int k = 0; k < 3; k++) {
-        r.A[k][i] = g.A[k];
-        r.B[k][i] = g.B[k];
-        r.C[k][i] = g.C[k];
-        r.iw[k][i] = g.iw[k];
-#pragma unroll
-        for (int j = 0; j < 3; j++) r.bary[3 * k + j][i] = g.bary[k][j];
-    }
-    r.z0[i] = pl.z0;
-    r.dzdx[i] = pl.dzdx;
-    r.dzdy[i] = pl.dzdy;
-    r.X0[i] = pl.X0;
-    r.Y0[i] = pl.Y0;
+// Set-up and shading of an entry that did not fit the tile's set-up cache (rare; out of line).
+__device__ __noinline__ void shade_uncached(const PassArgs& a, int e, int px, int py, float* col, RecordPlane* pl) {
+    ShadeGeom g;
+    setup_entry(a, e, &g, pl);
+    shade_entry_geom(a, e, g, px, py, col);
 }
 
 struct TileRecords {
@@ -480,16 +436,14 @@ __global__ void __launch_bounds__(kTileThreads) raster_kernel(PassArgs a) {
     }
 }
 
-// Shading stage: one CTA per tile.  Distinct visible entries of the tile get one shading
-// set-up each (shared memory), then every pixel shades its distinct entries (the warp
-// iterates over list slots together), resolves its samples on chip and stores depth,
-// visibility and the resolved colour once.
+// Shading stage: one CTA per tile, one thread per pixel.  Each pixel lists its distinct
+// visible entries in sample order; the warp shades list slot i of all its lanes together
+// (set-up straight from the binner's record, quad derivatives, texture filtering), then the
+// samples are resolved on chip and depth, visibility and the resolved colour stored once.
 template <int S>
-__global__ void __launch_bounds__(kTileThreads) shade_kernel(PassArgs a) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    ShadeRecords& srec = *reinterpret_cast<ShadeRecords*>(smem_raw);
-    __shared__ int hkey[kHashSize], hslot[kHashSize];
-    __shared__ int nslots;
+__global__ void __launch_bounds__(kTileThreads, 2) shade_kernel(PassArgs a) {
+    __shared__ DrawDev sdraw;
+    __shared__ float4 scol[4][kTileThreads];  // colours of each thread's (up to 4) distinct entries
 
     const int tile = blockIdx.x;
     const int tx = tile % a.c.tiles_x, ty = tile / a.c.tiles_x;
@@ -500,10 +454,12 @@ __global__ void __launch_bounds__(kTileThreads) shade_kernel(PassArgs a) {
     const bool inpix = px < a.c.W && py < a.c.H;
     const size_t pix = (size_t)py * a.c.W + px;
     const KeyRule rule = key_rule(a.depth_func, a.depth_write);
-
-    for (int i = tid; i < kHashSize; i += kTileThreads) hkey[i] = -1;
-    if (tid == 0) nslots = 0;
-    int ent[S], hpos[S];
+    if (a.ndraws == 1) {  // stage the draw descriptor on chip (read by every shading step)
+        const int* src = reinterpret_cast<const int*>(a.draws);
+        int* dst = reinterpret_cast<int*>(&sdraw);
+        for (int i = tid; i < (int)(sizeof(DrawDev) / 4); i += kTileThreads) dst[i] = src[i];
+    }
+    int ent[S];
     if (inpix) {
         const int* ep = a.entries + pix * S;
         if constexpr (S % 4 == 0) {
@@ -521,47 +477,8 @@ __global__ void __launch_bounds__(kTileThreads) shade_kernel(PassArgs a) {
         for (int k = 0; k < S; k++) ent[k] = -1;
     }
     __syncthreads();
-#pragma unroll
-    for (int k = 0; k < S; k++) {
-        hpos[k] = -1;
-        if (ent[k] < 0) continue;
-        if (k > 0 && ent[k] == ent[k - 1]) {
-            hpos[k] = hpos[k - 1];
-            continue;
-        }
-        int h = (int)(((uint32_t)ent[k] * 2654435761u) >> 23) & (kHashSize - 1);
-        for (int probe = 0; probe < kHashSize; probe++) {
-            int prev = atomicCAS(&hkey[h], -1, ent[k]);
-            if (prev == -1) {
-                int slot = atomicAdd(&nslots, 1);
-                hslot[h] = slot;
-                if (slot < kShadeCap) srec.entry[slot] = ent[k];
-                hpos[k] = h;
-                break;
-            }
-            if (prev == ent[k]) {
-                hpos[k] = h;
-                break;
-            }
-            h = (h + 1) & (kHashSize - 1);
-        }
-    }
-    __syncthreads();
-    const int ncached = min(nslots, kShadeCap);
-    for (int i = tid; i < ncached; i += kTileThreads) {
-        ShadeGeom g;
-        RecordPlane pl;
-        setup_entry(a, srec.entry[i], &g, &pl);
-        store_shade_record(srec, i, g, pl);
-    }
-    __syncthreads();
+    const DrawDev& d0 = a.ndraws == 1 ? sdraw : a.draws[0];
 
-    float bg[4];
-    if (a.clear) {
-        bg[0] = a.clear_color[0]; bg[1] = a.clear_color[1]; bg[2] = a.clear_color[2]; bg[3] = a.clear_color[3];
-    } else if (inpix) {
-        decode_color(a, pix, bg);
-    }
     // distinct visible entries of this pixel, in sample order; sample k uses list slot which[k]
     constexpr int U = S < 4 ? S : 4;  // slots shaded together across the warp
     int uniq[U], which[S];
@@ -586,60 +503,58 @@ __global__ void __launch_bounds__(kTileThreads) shade_kernel(PassArgs a) {
     int nmax = min(nu, U);
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) nmax = max(nmax, __shfl_xor_sync(0xffffffffu, nmax, o));
-    float scol[U][4];
-    RecordPlane spl[U];
+    float dep[S];
+#pragma unroll
+    for (int k = 0; k < S; k++) dep[k] = 0.0f;
     for (int i = 0; i < nmax; i++) {
         int e = -1;
 #pragma unroll
         for (int j = 0; j < U; j++)
             if (j == i) e = uniq[j];
-        float c[4] = {0.0f, 0.0f, 0.0f, 0.0f};
-        RecordPlane pl{};
         if (i < nu) {
-            int h = -1;
+            const int g = e >> 3, sub = e & 7;
+            const int di = a.ndraws == 1 ? 0 : find_draw(a, g);
+            const DrawDev& d = a.ndraws == 1 ? d0 : a.draws[di];
+            const int t = g - (a.ndraws == 1 ? 0 : __ldg(a.draw_start + di));
+            SubTri st;
+            setup_entry_sub(a.c, d, a.records, g, t, sub, st);
+            ShadeGeom geo;
+            shade_geom_from(st, geo);
+            float c[4];
+            shade_fragment(a.c, d, geo, t, sub, px, py, c);
+            scol[i][tid] = make_float4(c[0], c[1], c[2], c[3]);
 #pragma unroll
             for (int k = 0; k < S; k++)
-                if (which[k] == i && h < 0) h = hpos[k];
-            ShadeGeom g;
-            int cs = h >= 0 ? hslot[h] : kShadeCap;
-            if (cs < kShadeCap) load_shade_record(srec, cs, g, pl);
-            else setup_entry(a, e, &g, &pl);
-            shade_with(a, e, g, px, py, c);
+                if (which[k] == i)
+                    dep[k] = sample_depth(st.z[0], st.dzdx, st.dzdy, st.X[0], st.Y[0], px * 256 + a.c.sx[k],
+                                          py * 256 + a.c.sy[k]);
         }
-#pragma unroll
-        for (int j = 0; j < U; j++)
-            if (j == i) {
-                scol[j][0] = c[0]; scol[j][1] = c[1]; scol[j][2] = c[2]; scol[j][3] = c[3];
-                spl[j] = pl;
-            }
     }
     if (!inpix) return;
+    float bg[4];
+    if (a.clear) {
+        bg[0] = a.clear_color[0]; bg[1] = a.clear_color[1]; bg[2] = a.clear_color[2]; bg[3] = a.clear_color[3];
+    } else {
+        decode_color(a, pix, bg);
+    }
     float acc[4];
-    float dep[S];
 #pragma unroll
     for (int k = 0; k < S; k++) {
         float c[4];
-        const float d0 = a.clear ? a.clear_depth : a.depth[pix * S + k];
+        const float d0v = a.clear ? a.clear_depth : a.depth[pix * S + k];
         if (which[k] < 0) {
             c[0] = bg[0]; c[1] = bg[1]; c[2] = bg[2]; c[3] = bg[3];
-            dep[k] = d0;
+            dep[k] = d0v;
         } else {
-            RecordPlane pl{};
             if (which[k] < U) {
-#pragma unroll
-                for (int j = 0; j < U; j++)
-                    if (j == which[k]) {
-                        c[0] = scol[j][0]; c[1] = scol[j][1]; c[2] = scol[j][2]; c[3] = scol[j][3];
-                        pl = spl[j];
-                    }
+                float4 v = scol[which[k]][tid];
+                c[0] = v.x; c[1] = v.y; c[2] = v.z; c[3] = v.w;
             } else {  // more than U distinct primitives in one pixel: shade this one here
-                ShadeGeom g;
-                setup_entry(a, ent[k], &g, &pl);
-                shade_with(a, ent[k], g, px, py, c);
+                RecordPlane pl;
+                shade_uncached(a, ent[k], px, py, c, &pl);
+                dep[k] = sample_depth(pl.z0, pl.dzdx, pl.dzdy, pl.X0, pl.Y0, px * 256 + a.c.sx[k], py * 256 + a.c.sy[k]);
             }
-            dep[k] = rule.write ? sample_depth(pl.z0, pl.dzdx, pl.dzdy, pl.X0, pl.Y0, px * 256 + a.c.sx[k],
-                                               py * 256 + a.c.sy[k])
-                                : d0;
+            if (!rule.write) dep[k] = d0v;
         }
         if (k == 0) {
             acc[0] = c[0]; acc[1] = c[1]; acc[2] = c[2]; acc[3] = c[3];
@@ -696,17 +611,15 @@ cudaError_t launch_mip_level(const uint32_t* src, int sw, int sh, uint32_t* dst,
 template <int S>
 cudaError_t launch_tile(const PassArgs& a, int T, cudaStream_t stream, cudaEvent_t mid) {
     static bool configured = false;
-    const size_t rbytes = raster_smem_bytes<S>(), sbytes = sizeof(ShadeRecords);
+    const size_t rbytes = raster_smem_bytes<S>();
     if (!configured) {
         cudaError_t e = cudaFuncSetAttribute(raster_kernel<S>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rbytes);
-        if (e == cudaSuccess)
-            e = cudaFuncSetAttribute(shade_kernel<S>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sbytes);
         if (e != cudaSuccess) return e;
         configured = true;
     }
     raster_kernel<S><<<T, kTileThreads, rbytes, stream>>>(a);
     if (mid) cudaEventRecord(mid, stream);
-    shade_kernel<S><<<T, kTileThreads, sbytes, stream>>>(a);
+    shade_kernel<S><<<T, kTileThreads, 0, stream>>>(a);
     return cudaSuccess;
 }
 

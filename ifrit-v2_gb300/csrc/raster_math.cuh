@@ -372,11 +372,11 @@ __device__ __forceinline__ void unpack_rgba8(uint32_t t, float c[4]) {
 
 __device__ __forceinline__ float lerpf_(float a, float b, float t) { return a + t * (b - a); }
 
-__device__ __forceinline__ bool tex_address(int mode, float& c, int n) {
-    float nf = (float)n;
+// Texel-space wrapping per address mode; returns false outside a clamp-to-border texture.
+// fmodf is exact, and so are the shortcuts on the ranges where they are taken (Sterbenz:
+// v - n is exact for n <= v <= 2n; for |v| < n fmodf returns v itself).
+__device__ __forceinline__ bool tex_address(int mode, float& c, float nf) {
     float v = c;
-    // fmodf is exact, and so are the shortcuts below on the ranges where they are taken
-    // (Sterbenz: v - n is exact for n <= v <= 2n; for |v| < n fmodf returns v itself).
     switch (mode) {
     case 0:
         if (v >= 0.0f && v < nf) {
@@ -418,38 +418,68 @@ __device__ __forceinline__ bool tex_address(int mode, float& c, int n) {
     return true;
 }
 
-__device__ __forceinline__ void tex_level_info(const DrawDev& d, int level, int& w, int& h, int& off) {
-    w = d.lvl_w[level];
-    h = d.lvl_h[level];
-    off = d.lvl_off[level];
+// One mip level, with the constants every fetch from it needs.
+struct TexLevel {
+    const uint32_t* t;
+    int w, h;
+    float fw, fh;    // size as float (wrap modulus)
+    float fw1, fh1;  // size - 1 as float (texel mapping c = uv * (size - 1))
+};
+
+struct TexState {
+    int addr_u, addr_v, filter, border_white;
+};
+
+__device__ __forceinline__ TexLevel tex_level(const DrawDev& d, int level) {
+    TexLevel L;
+    L.w = d.lvl_w[level];
+    L.h = d.lvl_h[level];
+    L.t = d.texels + d.lvl_off[level];
+    L.fw = (float)L.w;
+    L.fh = (float)L.h;
+    L.fw1 = (float)(L.w - 1);
+    L.fh1 = (float)(L.h - 1);
+    return L;
 }
 
-__device__ __forceinline__ void tex_sample_level(const DrawDev& d, int level, float u, float v, float out[4]) {
-    int w, h, off;
-    tex_level_info(d, level, w, h, off);
-    float cx = u * (float)(w - 1);
-    float cy = v * (float)(h - 1);
-    if (!tex_address(d.sampler.address_u, cx, w) || !tex_address(d.sampler.address_v, cy, h)) {
-        float b = d.sampler.border_white ? 1.0f : 0.0f;
+__device__ __forceinline__ TexState tex_state(const DrawDev& d) {
+    TexState st;
+    st.addr_u = d.sampler.address_u;
+    st.addr_v = d.sampler.address_v;
+    st.filter = d.sampler.filter;
+    st.border_white = d.sampler.border_white;
+    return st;
+}
+
+// Bilinear (or nearest) fetch from one level; texel mapping c = uv * (size - 1) as in
+// ShaderBuiltinCuda.cuh:112-113, neighbours clamped to the last texel (:176-179).
+__device__ __forceinline__ void tex_bilinear(const TexLevel& L, const TexState& st, float u, float v, float out[4]) {
+    float cx = u * L.fw1;
+    float cy = v * L.fh1;
+    if (!tex_address(st.addr_u, cx, L.fw) || !tex_address(st.addr_v, cy, L.fh)) {
+        float b = st.border_white ? 1.0f : 0.0f;
         out[0] = b; out[1] = b; out[2] = b; out[3] = 1.0f;
         return;
     }
-    const uint32_t* t = d.texels + off;
-    if (d.sampler.filter == 0) {
-        int x = min((int)(cx + 0.5f), w - 1), y = min((int)(cy + 0.5f), h - 1);
-        unpack_rgba8(__ldg(t + y * w + x), out);
+    if (st.filter == 0) {
+        int x = min((int)(cx + 0.5f), L.w - 1), y = min((int)(cy + 0.5f), L.h - 1);
+        unpack_rgba8(__ldg(L.t + y * L.w + x), out);
         return;
     }
     int x0 = (int)cx, y0 = (int)cy;
     float fx = cx - (float)x0, fy = cy - (float)y0;
-    x0 = min(x0, w - 1);
-    y0 = min(y0, h - 1);
-    int x1 = min(x0 + 1, w - 1), y1 = min(y0 + 1, h - 1);
+    x0 = min(x0, L.w - 1);
+    y0 = min(y0, L.h - 1);
+    const int x1 = min(x0 + 1, L.w - 1), y1 = min(y0 + 1, L.h - 1);
+    const uint32_t t00 = __ldg(L.t + y0 * L.w + x0);
+    const uint32_t t01 = __ldg(L.t + y0 * L.w + x1);
+    const uint32_t t10 = __ldg(L.t + y1 * L.w + x0);
+    const uint32_t t11 = __ldg(L.t + y1 * L.w + x1);
     float c00[4], c01[4], c10[4], c11[4];
-    unpack_rgba8(__ldg(t + y0 * w + x0), c00);
-    unpack_rgba8(__ldg(t + y0 * w + x1), c01);
-    unpack_rgba8(__ldg(t + y1 * w + x0), c10);
-    unpack_rgba8(__ldg(t + y1 * w + x1), c11);
+    unpack_rgba8(t00, c00);
+    unpack_rgba8(t01, c01);
+    unpack_rgba8(t10, c10);
+    unpack_rgba8(t11, c11);
 #pragma unroll
     for (int i = 0; i < 4; i++) {
         float top = lerpf_(c00[i], c01[i], fx);
@@ -474,56 +504,66 @@ __device__ __forceinline__ LodPick pick_lod(const DrawDev& d, float lam) {
     return p;
 }
 
-__device__ __forceinline__ void tex_trilinear_at(const DrawDev& d, const LodPick& p, float u, float v, float out[4]) {
-    tex_sample_level(d, p.lo, u, v, out);
-    if (p.hi == p.lo || p.t == 0.0f) return;
+// Trilinear fetch between two prepared levels (one level when `two` is false).
+__device__ __forceinline__ void tex_trilinear2(const TexLevel& L0, const TexLevel& L1, const TexState& st, bool two,
+                                               float t, float u, float v, float out[4]) {
+    tex_bilinear(L0, st, u, v, out);
+    if (!two) return;
     float c1[4];
-    tex_sample_level(d, p.hi, u, v, c1);
+    tex_bilinear(L1, st, u, v, c1);
 #pragma unroll
-    for (int i = 0; i < 4; i++) out[i] = lerpf_(out[i], c1[i], p.t);
-}
-
-__device__ __forceinline__ void tex_trilinear(const DrawDev& d, float u, float v, float lam, float out[4]) {
-    tex_trilinear_at(d, pick_lod(d, lam), u, v, out);
+    for (int i = 0; i < 4; i++) out[i] = lerpf_(out[i], c1[i], t);
 }
 
 __device__ __forceinline__ float finite_or_zero(float x) { return isfinite(x) ? x : 0.0f; }
 
+// Texture sampling with LOD from screen-space derivatives (ShaderBuiltinCuda.cuh:225-272).
 __device__ __forceinline__ void tex_sample(const DrawDev& d, float u, float v, float dudx, float dvdx, float dudy,
                                            float dvdy, float out[4]) {
     u = finite_or_zero(u); v = finite_or_zero(v);
     dudx = finite_or_zero(dudx); dvdx = finite_or_zero(dvdx);
     dudy = finite_or_zero(dudy); dvdy = finite_or_zero(dvdy);
-    if (d.sampler.filter == 0) {
-        tex_sample_level(d, 0, u, v, out);
+    const TexState st = tex_state(d);
+    if (st.filter == 0) {
+        tex_bilinear(tex_level(d, 0), st, u, v, out);
         return;
     }
     float tw = (float)d.tex_w, th = (float)d.tex_h;
     float xu = dudx * tw, xv = dvdx * th, yu = dudy * tw, yv = dvdy * th;
     float lx2 = xu * xu + xv * xv;
     float ly2 = yu * yu + yv * yv;
-    if (d.sampler.max_aniso <= 1) {
-        float lam = 0.5f * log2_series(fmaxf(lx2, ly2)) + d.sampler.lod_bias;
-        tex_trilinear(d, u, v, lam, out);
+    const bool aniso = d.sampler.max_aniso > 1;
+    float lam;
+    int n = 1;
+    float du = 0.0f, dv = 0.0f;
+    if (!aniso) {
+        lam = 0.5f * log2_series(fmaxf(lx2, ly2)) + d.sampler.lod_bias;
+    } else {
+        float px = sqrtf(lx2), py = sqrtf(ly2);
+        bool major_x = px >= py;
+        float pmax = major_x ? px : py, pmin = major_x ? py : px;
+        float amax = (float)d.sampler.max_aniso;
+        float ratio = pmin > 0.0f ? pmax / pmin : amax;
+        ratio = fminf(ratio, amax);
+        n = (int)ceilf(ratio);
+        if (n < 1) n = 1;
+        lam = log2_series(pmax / (float)n) + d.sampler.lod_bias;
+        du = major_x ? dudx : dudy;
+        dv = major_x ? dvdx : dvdy;
+    }
+    const LodPick lp = pick_lod(d, lam);
+    const TexLevel L0 = tex_level(d, lp.lo), L1 = tex_level(d, lp.hi);
+    const bool two = !(lp.hi == lp.lo || lp.t == 0.0f);
+    if (!aniso) {
+        tex_trilinear2(L0, L1, st, two, lp.t, u, v, out);
         return;
     }
-    float px = sqrtf(lx2), py = sqrtf(ly2);
-    bool major_x = px >= py;
-    float pmax = major_x ? px : py, pmin = major_x ? py : px;
-    float amax = (float)d.sampler.max_aniso;
-    float ratio = pmin > 0.0f ? pmax / pmin : amax;
-    ratio = fminf(ratio, amax);
-    int n = (int)ceilf(ratio);
-    if (n < 1) n = 1;
-    float lam = log2_series(pmax / (float)n) + d.sampler.lod_bias;
-    const LodPick lp = pick_lod(d, lam);
-    float du = major_x ? dudx : dudy, dv = major_x ? dvdx : dvdy;
     float acc[4] = {0.0f, 0.0f, 0.0f, 0.0f};
     float inv = (float)(n + 1);
     for (int i = 0; i < n; i++) {
         float t = (float)(i + 1) / inv - 0.5f;
         float cc[4];
-        tex_trilinear_at(d, lp, u + du * t, v + dv * t, cc);
+        tex_trilinear2(L0, L1, st, two, lp.t, u + du * t, v + dv * t, cc);
 #pragma unroll
         for (int k = 0; k < 4; k++) acc[k] = acc[k] + cc[k];
     }
@@ -553,9 +593,10 @@ __device__ __forceinline__ void shade_geom_from(const SubTri& s, ShadeGeom& g) {
     }
 }
 
-// Perspective-correct interpolation of the draw's attribute at fixed-point position (x, y).
-__device__ __forceinline__ void interp_attr(const ShadeGeom& s, int attr_count, const float* a0, const float* a1,
-                                            const float* a2, int32_t x, int32_t y, float out[4]) {
+// Perspective-correct interpolation of the draw's attribute at fixed-point position (x, y);
+// va/vb/vc hold the attribute of the triangle's three vertices (unused components zero).
+__device__ __forceinline__ void interp_attr(const ShadeGeom& s, int attr_count, const float* va, const float* vb,
+                                            const float* vc, int32_t x, int32_t y, float out[4]) {
     float p[3];
 #pragma unroll
     for (int i = 0; i < 3; i++) {
@@ -569,9 +610,12 @@ __device__ __forceinline__ void interp_attr(const ShadeGeom& s, int attr_count, 
 #pragma unroll
     for (int k = 0; k < 3; k++) W[k] = (b0 * s.bary[0][k] + b1 * s.bary[1][k]) + b2 * s.bary[2][k];
 #pragma unroll
-    for (int k = 0; k < 4; k++) out[k] = 0.0f;
-    for (int k = 0; k < attr_count; k++)
-        out[k] = (W[0] * __ldg(a0 + k) + W[1] * __ldg(a1 + k)) + W[2] * __ldg(a2 + k);
+    for (int k = 0; k < 4; k++) out[k] = k < attr_count ? (W[0] * va[k] + W[1] * vb[k]) + W[2] * vc[k] : 0.0f;
+}
+
+__device__ __forceinline__ void load_attr(const float* p, int attr_count, float v[4]) {
+#pragma unroll
+    for (int k = 0; k < 4; k++) v[k] = k < attr_count ? __ldg(p + k) : 0.0f;
 }
 
 // Fragment colour of pixel (px, py) for triangle t / fan index `sub` of draw d.  Texture
@@ -584,9 +628,10 @@ __device__ __forceinline__ void shade_fragment(const PassConst& c, const DrawDev
         col[0] = (float)(d.prim_base + t); col[1] = (float)sub; col[2] = 0.0f; col[3] = 1.0f;
         return;
     }
-    const float* a0 = d.vertices + (size_t)__ldg(d.indices + 3 * (size_t)t + 0) * d.stride + d.attr_offset;
-    const float* a1 = d.vertices + (size_t)__ldg(d.indices + 3 * (size_t)t + 1) * d.stride + d.attr_offset;
-    const float* a2 = d.vertices + (size_t)__ldg(d.indices + 3 * (size_t)t + 2) * d.stride + d.attr_offset;
+    float a0[4], a1[4], a2[4];
+    load_attr(d.vertices + (size_t)__ldg(d.indices + 3 * (size_t)t + 0) * d.stride + d.attr_offset, d.attr_count, a0);
+    load_attr(d.vertices + (size_t)__ldg(d.indices + 3 * (size_t)t + 1) * d.stride + d.attr_offset, d.attr_count, a1);
+    load_attr(d.vertices + (size_t)__ldg(d.indices + 3 * (size_t)t + 2) * d.stride + d.attr_offset, d.attr_count, a2);
     int32_t qx = px * 256 + c.shade_x, qy = py * 256 + c.shade_y;
     float a[4];
     interp_attr(s, d.attr_count, a0, a1, a2, qx, qy, a);
