@@ -176,6 +176,9 @@ struct IfritGbRenderer {
     float stage_ms[5] = {0, 0, 0, 0, 0};
     std::string last_error;
     int pending = 0;  // an async pass whose status has not been checked
+    bool in_pass = false;
+    int pass_clear = 0;
+    std::vector<DrawDev> pass_draws;
 };
 
 namespace {
@@ -394,44 +397,63 @@ int ensure_init(IfritGbRenderer* h) {
     return IFTR_OK;
 }
 
-// Enqueues one pass (draw) on the renderer's stream.
-int enqueue_draw(IfritGbRenderer* h, int numIndices, int clear) {
+// Snapshot of the current state as one draw of `numIndices` indices starting at `firstIndex`.
+int prepare_draw(IfritGbRenderer* h, int firstIndex, int numIndices, DrawDev& d) {
+    if (numIndices < 0 || numIndices % 3 != 0 || firstIndex < 0 || firstIndex % 3 != 0) return IFTR_ERR_INVALID_ARG;
+    std::memset(&d, 0, sizeof(d));
+    if (numIndices > 0) {
+        int rc = prepare_geometry(h, firstIndex + numIndices, d);
+        if (rc) return rc;
+        d.indices += firstIndex;
+    }
+    d.num_triangles = numIndices / 3;
+    fill_state(h, d);
+    if (d.shading == IFTR_FS_TEXTURED && (!d.texels || d.tex_levels <= 0)) return IFTR_ERR_STATE;
+    return IFTR_OK;
+}
+
+// Enqueues one pass of draws on the renderer's stream.
+int enqueue_pass(IfritGbRenderer* h, std::vector<DrawDev>& draws, int clear) {
     int rc = ensure_init(h);
     if (rc) return rc;
-    if (numIndices < 0 || numIndices % 3 != 0) return IFTR_ERR_INVALID_ARG;
+    if (draws.empty() || draws.size() > (size_t)ifr::kMaxDraws) return IFTR_ERR_INVALID_ARG;
     int W, H, fmt;
     if (!fb_geometry(h->fb, W, H, fmt)) return IFTR_ERR_STATE;
     if (W > 16384 || H > 16384) return IFTR_ERR_INVALID_ARG;
     int S = h->samples;
     rc = ensure_attachments(h, W, H, S, fmt);
     if (rc) return rc;
-    DrawDev d{};
-    if (numIndices > 0) {
-        rc = prepare_geometry(h, numIndices, d);
-        if (rc) return rc;
+    // global triangle ids: draw i covers [start_i, start_{i+1})
+    int64_t total = 0;
+    bool ordered = false;
+    for (size_t i = 0; i < draws.size(); i++) {
+        DrawDev& d = draws[i];
+        d.prim_base = (int)total;
+        h->h_draw_start[i] = (int)total;
+        total += d.num_triangles;
+        if (d.blend_enable || (d.depth_write && d.depth_func == IF_COMPARE_OP_NOT_EQUAL) ||
+            d.depth_func != draws[0].depth_func || d.depth_write != draws[0].depth_write)
+            ordered = true;
+        h->h_draws[i] = d;
     }
-    fill_state(h, d);
-    if (d.shading == IFTR_FS_TEXTURED && (!d.texels || d.tex_levels <= 0)) return IFTR_ERR_STATE;
-
-    if (d.blend_enable || (d.depth_write && d.depth_func == IF_COMPARE_OP_NOT_EQUAL)) return IFTR_ERR_UNSUPPORTED;
-    h->h_draws[0] = d;
-    h->h_draw_start[0] = 0;
-    h->h_draw_start[1] = d.num_triangles;
-    IFTR_CUDA(h, cudaMemcpyAsync(h->d_draws.p, h->h_draws, sizeof(DrawDev), cudaMemcpyHostToDevice, h->stream));
-    IFTR_CUDA(h, cudaMemcpyAsync(h->d_draw_start.p, h->h_draw_start, 2 * sizeof(int), cudaMemcpyHostToDevice, h->stream));
+    if (total >= (int64_t)1 << 28) return IFTR_ERR_INVALID_ARG;  // entry = triangle << 3 | fan index
+    h->h_draw_start[draws.size()] = (int)total;
+    IFTR_CUDA(h, cudaMemcpyAsync(h->d_draws.p, h->h_draws, draws.size() * sizeof(DrawDev), cudaMemcpyHostToDevice, h->stream));
+    IFTR_CUDA(h, cudaMemcpyAsync(h->d_draw_start.p, h->h_draw_start, (draws.size() + 1) * sizeof(int),
+                                 cudaMemcpyHostToDevice, h->stream));
     if (h->pair_capacity == 0) {
-        rc = ensure_pairs(h, std::max<size_t>(1u << 20, (size_t)d.num_triangles * 4));
+        rc = ensure_pairs(h, std::max<size_t>(1u << 20, (size_t)total * 4));
         if (rc) return rc;
     }
-    IFTR_CUDA(h, h->d_records.reserve(std::max<size_t>(1, (size_t)d.num_triangles) * sizeof(ifr::TriRecord)));
+    IFTR_CUDA(h, h->d_records.reserve(std::max<size_t>(1, (size_t)total) * sizeof(ifr::TriRecord)));
     IFTR_CUDA(h, cudaMemsetAsync(h->d_status.p, 0, ifr::ST_WORDS * sizeof(uint32_t), h->stream));
     PassArgs a;
     std::memset(&a, 0, sizeof(a));
     fill_pass_const(a.c, W, H, S);
     a.draws = h->d_draws.as<DrawDev>();
     a.draw_start = h->d_draw_start.as<int>();
-    a.ndraws = 1;
-    a.total_tris = d.num_triangles;
+    a.ndraws = (int)draws.size();
+    a.total_tris = (int)total;
     a.format = fmt;
     a.color = h->d_color.p;
     a.depth = h->d_depth.as<float>();
@@ -440,8 +462,9 @@ int enqueue_draw(IfritGbRenderer* h, int numIndices, int clear) {
     a.clear = clear;
     std::memcpy(a.clear_color, h->clear_color, sizeof(a.clear_color));
     a.clear_depth = h->clear_depth;
-    a.depth_func = d.depth_func;
-    a.depth_write = d.depth_write;
+    a.depth_func = draws[0].depth_func;
+    a.depth_write = draws[0].depth_write;
+    a.ordered = ordered ? 1 : 0;
     a.tile_count = h->d_tile_count.as<uint32_t>();
     a.tile_offset = h->d_tile_offset.as<uint32_t>();
     a.tile_cursor = h->d_tile_cursor.as<uint32_t>();
@@ -451,9 +474,19 @@ int enqueue_draw(IfritGbRenderer* h, int numIndices, int clear) {
     a.status = h->d_status.as<uint32_t>();
     IFTR_CUDA(h, ifr::launch_pass(a, h->stream, h->timing ? h->ev : nullptr));
     IFTR_CUDA(h, cudaMemcpyAsync(h->h_status, h->d_status.p, ifr::ST_WORDS * sizeof(uint32_t), cudaMemcpyDeviceToHost, h->stream));
-    h->stats.triangles_in = (uint64_t)d.num_triangles;
+    h->stats.triangles_in = (uint64_t)total;
     h->pending = 1;
     return IFTR_OK;
+}
+
+// Enqueues a single-draw pass with the current state.
+int enqueue_draw(IfritGbRenderer* h, int numIndices, int clear) {
+    int rc = ensure_init(h);
+    if (rc) return rc;
+    std::vector<DrawDev> one(1);
+    rc = prepare_draw(h, 0, numIndices, one[0]);
+    if (rc) return rc;
+    return enqueue_pass(h, one, clear);
 }
 
 int check_pending(IfritGbRenderer* h) {
@@ -469,6 +502,7 @@ int check_pending(IfritGbRenderer* h) {
         int rc = ensure_pairs(h, want);
         return rc ? rc : IFTR_ERR_OVERFLOW;
     }
+    if (h->h_status[ifr::ST_ORDERED_LIMIT]) return IFTR_ERR_LIMIT;
     return IFTR_OK;
 }
 
@@ -619,6 +653,7 @@ IFTR_API int iftrFinish(IfritGbRenderer* h) {
 
 IFTR_API int iftrDrawLegacy(IfritGbRenderer* h, int numIndices, int clear) {
     if (!h) return IFTR_ERR_INVALID_ARG;
+    if (h->in_pass) return iftrPassDraw(h, 0, numIndices);
     h->stats.retries = 0;
     for (int attempt = 0; attempt < 4; attempt++) {
         int rc = enqueue_draw(h, numIndices, clear);
@@ -627,6 +662,50 @@ IFTR_API int iftrDrawLegacy(IfritGbRenderer* h, int numIndices, int clear) {
         if (rc == IFTR_ERR_OVERFLOW) {
             h->stats.retries++;
             if (!clear) return rc;  // the pass may have partially updated depth; caller decides
+            continue;
+        }
+        if (rc) return rc;
+        return copy_back_host_images(h);
+    }
+    return IFTR_ERR_OVERFLOW;
+}
+
+IFTR_API int iftrBeginPass(IfritGbRenderer* h, int clear) {
+    if (!h) return IFTR_ERR_INVALID_ARG;
+    if (h->in_pass) return IFTR_ERR_STATE;
+    int rc = ensure_init(h);
+    if (rc) return rc;
+    h->in_pass = true;
+    h->pass_clear = clear;
+    h->pass_draws.clear();
+    return IFTR_OK;
+}
+
+IFTR_API int iftrPassDraw(IfritGbRenderer* h, int firstIndex, int numIndices) {
+    if (!h) return IFTR_ERR_INVALID_ARG;
+    if (!h->in_pass) return IFTR_ERR_STATE;
+    if (h->pass_draws.size() >= (size_t)ifr::kMaxDraws) return IFTR_ERR_INVALID_ARG;
+    DrawDev d;
+    int rc = prepare_draw(h, firstIndex, numIndices, d);
+    if (rc) return rc;
+    h->pass_draws.push_back(d);
+    return IFTR_OK;
+}
+
+IFTR_API int iftrEndPass(IfritGbRenderer* h) {
+    if (!h) return IFTR_ERR_INVALID_ARG;
+    if (!h->in_pass) return IFTR_ERR_STATE;
+    h->in_pass = false;
+    if (h->pass_draws.empty()) return h->pass_clear ? iftrClear(h) : IFTR_OK;
+    h->stats.retries = 0;
+    for (int attempt = 0; attempt < 4; attempt++) {
+        std::vector<DrawDev> draws = h->pass_draws;
+        int rc = enqueue_pass(h, draws, h->pass_clear);
+        if (rc) return rc;
+        rc = check_pending(h);
+        if (rc == IFTR_ERR_OVERFLOW) {
+            h->stats.retries++;
+            if (!h->pass_clear) return rc;
             continue;
         }
         if (rc) return rc;

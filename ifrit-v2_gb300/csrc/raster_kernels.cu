@@ -581,6 +581,186 @@ __global__ void __launch_bounds__(kTileThreads, 2) shade_kernel(PassArgs a) {
     }
 }
 
+// Ordered stage (forward path), one CTA per tile.  Used when results depend on submission
+// order: blending, NOT_EQUAL with depth writes, or draws of one pass with different depth
+// state.  The tile's entries are sorted into API order in shared memory, then every pixel
+// applies them one after another exactly as the reference's ordered CPU path does
+// (TileRasterWorker.cpp:1517-1580): per-sample depth test and write, one shading per pixel
+// and triangle when any sample passes, per-sample blend (TileRasterWorker.cpp:2346-2373,
+// pixelShadingAlphaBlendKernel .cu:1648-1897), then the on-chip resolve.
+struct FwdRecords {
+    int32_t A[3][kTileThreads], B[3][kTileThreads];
+    long long Cb[3][kTileThreads];
+    float z0[kTileThreads], dzdx[kTileThreads], dzdy[kTileThreads];
+    int32_t X0[kTileThreads], Y0[kTileThreads];
+    int32_t bx[kTileThreads], by[kTileThreads];  // px0 | px1 << 16, py0 | py1 << 16
+    int32_t key[kTileThreads];
+    int32_t draw[kTileThreads];
+};
+
+template <int S>
+__global__ void __launch_bounds__(kTileThreads) forward_kernel(PassArgs a) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    FwdRecords& rec = *reinterpret_cast<FwdRecords*>(smem_raw);
+    float4* scol = reinterpret_cast<float4*>(smem_raw + sizeof(FwdRecords));                  // [S][256]
+    uint32_t* list = reinterpret_cast<uint32_t*>(smem_raw + sizeof(FwdRecords) + sizeof(float4) * S * kTileThreads);
+
+    const int tile = blockIdx.x;
+    const int tx = tile % a.c.tiles_x, ty = tile / a.c.tiles_x;
+    const int tid = threadIdx.x;
+    const int lx = ((tid >> 2) & 7) * 2 + (tid & 1);
+    const int ly = (tid >> 5) * 2 + ((tid >> 1) & 1);
+    const int px = tx * kTileSize + lx, py = ty * kTileSize + ly;
+    const bool inpix = px < a.c.W && py < a.c.H;
+    const size_t pix = (size_t)py * a.c.W + px;
+
+    float dep[S];
+    int vid[S];
+    {
+        float bg[4];
+        if (a.clear) {
+            bg[0] = a.clear_color[0]; bg[1] = a.clear_color[1]; bg[2] = a.clear_color[2]; bg[3] = a.clear_color[3];
+        } else if (inpix) {
+            decode_color(a, pix, bg);
+        } else {
+            bg[0] = bg[1] = bg[2] = bg[3] = 0.0f;
+        }
+#pragma unroll
+        for (int k = 0; k < S; k++) {
+            dep[k] = a.clear ? a.clear_depth : (inpix ? a.depth[pix * S + k] : 0.0f);
+            vid[k] = -1;
+            scol[k * kTileThreads + tid] = make_float4(bg[0], bg[1], bg[2], bg[3]);
+        }
+    }
+    const bool has_list = a.total_tris > 0 && a.status[ST_OVERFLOW] == 0;
+    const uint32_t beg = has_list ? a.tile_offset[tile] : 0u;
+    const uint32_t end = has_list ? a.tile_offset[tile + 1] : 0u;
+    int n = (int)(end - beg);
+    if (n > kOrderedCap) {  // cannot order this tile on chip: report and leave it cleared
+        if (tid == 0) atomicOr(a.status + ST_ORDERED_LIMIT, 1u);
+        n = 0;
+    }
+    // load and sort the tile's entries into submission order (bitonic, padded to 2^k)
+    int P = 1;
+    while (P < n) P <<= 1;
+    for (int i = tid; i < P; i += kTileThreads) list[i] = i < n ? __ldg(a.pairs + beg + i) : 0xFFFFFFFFu;
+    __syncthreads();
+    for (int k = 2; k <= P; k <<= 1) {
+        for (int j = k >> 1; j > 0; j >>= 1) {
+            for (int i = tid; i < P; i += kTileThreads) {
+                int ixj = i ^ j;
+                if (ixj > i) {
+                    uint32_t x = list[i], y = list[ixj];
+                    bool up = (i & k) == 0;
+                    if ((x > y) == up) {
+                        list[i] = y;
+                        list[ixj] = x;
+                    }
+                }
+            }
+            __syncthreads();
+        }
+    }
+
+    for (int base = 0; base < n; base += kTileThreads) {
+        const int nb = min(kTileThreads, n - base);
+        if (tid < nb) {
+            uint32_t e = list[base + tid];
+            int g = (int)(e >> 3), sub = (int)(e & 7u);
+            int di = find_draw(a, g);
+            SubTri s;
+            if (setup_entry_sub(a.c, a.draws[di], a.records, g, g - __ldg(a.draw_start + di), sub, s)) {
+#pragma unroll
+                for (int i = 0; i < 3; i++) {
+                    rec.A[i][tid] = s.A[i];
+                    rec.B[i][tid] = s.B[i];
+                    rec.Cb[i][tid] = s.Cb[i];
+                }
+                rec.z0[tid] = s.z[0];
+                rec.dzdx[tid] = s.dzdx;
+                rec.dzdy[tid] = s.dzdy;
+                rec.X0[tid] = s.X[0];
+                rec.Y0[tid] = s.Y[0];
+                rec.bx[tid] = s.px0 | (s.px1 << 16);
+                rec.by[tid] = s.py0 | (s.py1 << 16);
+            } else {
+                rec.bx[tid] = 1;
+                rec.by[tid] = 1;
+            }
+            rec.key[tid] = (int)e;
+            rec.draw[tid] = di;
+        }
+        __syncthreads();
+        if (inpix) {
+            for (int r = 0; r < nb; r++) {
+                const int bx = rec.bx[r], by = rec.by[r];
+                if (px < (bx & 0xffff) || px > (bx >> 16) || py < (by & 0xffff) || py > (by >> 16)) continue;
+                const int32_t A[3] = {rec.A[0][r], rec.A[1][r], rec.A[2][r]};
+                const int32_t B[3] = {rec.B[0][r], rec.B[1][r], rec.B[2][r]};
+                const int64_t Cb[3] = {rec.Cb[0][r], rec.Cb[1][r], rec.Cb[2][r]};
+                const DrawDev& d = a.draws[rec.draw[r]];
+                const int func = d.depth_func, write = d.depth_write;
+                const int e = rec.key[r];
+                unsigned mask = 0;
+#pragma unroll
+                for (int k = 0; k < S; k++) {
+                    const int32_t sx = px * 256 + a.c.sx[k], sy = py * 256 + a.c.sy[k];
+                    if (!covered(A, B, Cb, sx, sy)) continue;
+                    const float z = sample_depth(rec.z0[r], rec.dzdx[r], rec.dzdy[r], rec.X0[r], rec.Y0[r], sx, sy);
+                    if (!depth_cmp(func, z, dep[k])) continue;
+                    if (write) dep[k] = z;
+                    vid[k] = e >> 3;
+                    mask |= 1u << k;
+                }
+                if (!mask) continue;
+                float c[4];
+                RecordPlane pl;
+                shade_uncached(a, e, px, py, c, &pl);
+#pragma unroll
+                for (int k = 0; k < S; k++) {
+                    if (!(mask & (1u << k))) continue;
+                    float4& sc = scol[k * kTileThreads + tid];
+                    if (d.blend_enable) {
+                        float dst[4] = {sc.x, sc.y, sc.z, sc.w};
+                        blend_into(d, c, dst);
+                        sc = make_float4(dst[0], dst[1], dst[2], dst[3]);
+                    } else {
+                        sc = make_float4(c[0], c[1], c[2], c[3]);
+                    }
+                }
+            }
+        }
+        __syncthreads();
+    }
+    if (!inpix) return;
+    float acc[4];
+#pragma unroll
+    for (int k = 0; k < S; k++) {
+        const float4 v = scol[k * kTileThreads + tid];
+        if (k == 0) {
+            acc[0] = v.x; acc[1] = v.y; acc[2] = v.z; acc[3] = v.w;
+        } else {
+            acc[0] = acc[0] + v.x; acc[1] = acc[1] + v.y; acc[2] = acc[2] + v.z; acc[3] = acc[3] + v.w;
+        }
+    }
+    const float invS = 1.0f / (float)S;
+    acc[0] = acc[0] * invS; acc[1] = acc[1] * invS; acc[2] = acc[2] * invS; acc[3] = acc[3] * invS;
+    encode_color(a, pix, acc);
+    float* dp = a.depth + pix * S;
+#pragma unroll
+    for (int k = 0; k < S; k++) dp[k] = dep[k];
+    if (a.vis) {
+        int* vp = a.vis + pix * S;
+#pragma unroll
+        for (int k = 0; k < S; k++) vp[k] = vid[k];
+    }
+}
+
+template <int S>
+size_t forward_smem_bytes() {
+    return sizeof(FwdRecords) + sizeof(float4) * S * kTileThreads + sizeof(uint32_t) * kOrderedCap;
+}
+
 template <int S>
 size_t raster_smem_bytes() {
     return sizeof(TileRecords) + (size_t)kTileThreads * S * sizeof(unsigned long long);
@@ -610,6 +790,18 @@ cudaError_t launch_mip_level(const uint32_t* src, int sw, int sh, uint32_t* dst,
 
 template <int S>
 cudaError_t launch_tile(const PassArgs& a, int T, cudaStream_t stream, cudaEvent_t mid) {
+    if (a.ordered) {
+        static bool fconfigured = false;
+        const size_t fbytes = forward_smem_bytes<S>();
+        if (!fconfigured) {
+            cudaError_t e = cudaFuncSetAttribute(forward_kernel<S>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fbytes);
+            if (e != cudaSuccess) return e;
+            fconfigured = true;
+        }
+        forward_kernel<S><<<T, kTileThreads, fbytes, stream>>>(a);
+        if (mid) cudaEventRecord(mid, stream);
+        return cudaSuccess;
+    }
     static bool configured = false;
     const size_t rbytes = raster_smem_bytes<S>();
     if (!configured) {

@@ -10,7 +10,8 @@ constexpr int kTileSize = 1 << kTileShift;
 constexpr int kTileThreads = kTileSize * kTileSize;
 constexpr int kMaxDraws = 256;
 
-enum StatusWord { ST_OVERFLOW = 0, ST_PAIRS = 1, ST_ERROR = 2, ST_WORDS = 4 };
+enum StatusWord { ST_OVERFLOW = 0, ST_PAIRS = 1, ST_ORDERED_LIMIT = 2, ST_WORDS = 4 };
+constexpr int kOrderedCap = 8192;  // entries per tile an ordered (in-API-order) pass can sort
 
 struct PassArgs {
     PassConst c;
@@ -29,6 +30,8 @@ struct PassArgs {
     float clear_depth;
     int depth_func;          // pass-uniform depth function (deferred path)
     int depth_write;
+    int ordered;             // 1: triangles applied to each sample in API order (blending, NOT_EQUAL,
+                             //    or draws with different depth state)
     // binning
     uint32_t* tile_count;    // [T], zero between passes
     uint32_t* tile_offset;   // [T + 1]

@@ -16,7 +16,7 @@ LIB_PATH = _build.LIB
 
 IFTR_OK = 0
 ERRORS = {1: "invalid argument", 2: "unsupported", 3: "CUDA error", 4: "scratch capacity exceeded",
-          5: "no CUDA device", 6: "missing binding"}
+          5: "no CUDA device", 6: "missing binding", 7: "ordered tile list limit"}
 FORMAT_RGBA8, FORMAT_RGBA16F, FORMAT_RGBA32F, FORMAT_RGB32F = 0, 1, 2, 3
 FS_GOURAUD, FS_TEXTURED, FS_PRIMITIVE_ID = 0, 1, 2
 IFTP_FLOAT1, IFTP_FLOAT2, IFTP_FLOAT3, IFTP_FLOAT4 = 1, 2, 3, 4
@@ -43,6 +43,7 @@ EXPORTED = [
     "ifbufCreateBufferManager", "ifbufDestroyBufferManager", "ifbufCreateBuffer", "ifbufDestroyBuffer",
     "ifbufBufferData", "iftrSetStageTiming", "iftrGetStageTimes", "iftrGetVertexBufferRawData",
     "iftrSetVertexBufferDirty", "ifbufGetBufferRawData", "ifbufSetBufferDirty", "iftrDrawNoAlloc",
+    "iftrBeginPass", "iftrPassDraw", "iftrEndPass",
 ]
 
 
@@ -127,6 +128,7 @@ def load(build_if_missing=True):
         "ifbufBufferData": [vp, vp, sz, sz], "iftrSetStageTiming": [vp, ip], "iftrGetStageTimes": [vp, fp, ip],
         "iftrGetVertexBufferRawData": [vp], "iftrSetVertexBufferDirty": [vp], "ifbufGetBufferRawData": [vp],
         "ifbufSetBufferDirty": [vp], "iftrDrawNoAlloc": [ctypes.POINTER(NoAllocPass), vp],
+        "iftrBeginPass": [vp, ip], "iftrPassDraw": [vp, ip, ip], "iftrEndPass": [vp],
     }
     for name, args in sig.items():
         getattr(lib, name).argtypes = args
@@ -220,6 +222,20 @@ class Renderer:
         s = SamplerState(filter_mode, address, address, address, 0, int(max_aniso > 1), float(max_aniso), lod_bias)
         check("iftrCreateSampler", L.iftrCreateSampler(h, slot, ctypes.byref(s)))
         check("iftrBindTexture", L.iftrBindTexture(h, slot, slot))
+
+    def set_blend(self, enable, src_color=6, dst_color=7, src_alpha=1, dst_alpha=7):
+        """Blend factors use the IfritBlendFactor numbering (6 SRC_ALPHA, 7 ONE_MINUS_SRC_ALPHA)."""
+        s = BlendState(int(enable), src_color, dst_color, src_alpha, dst_alpha)
+        check("iftrSetBlendFunc", self.lib.iftrSetBlendFunc(self.h, ctypes.byref(s)))
+
+    def begin_pass(self, clear=True):
+        check("iftrBeginPass", self.lib.iftrBeginPass(self.h, int(clear)))
+
+    def pass_draw(self, first_index, num_indices):
+        check("iftrPassDraw", self.lib.iftrPassDraw(self.h, first_index, num_indices))
+
+    def end_pass(self):
+        check("iftrEndPass", self.lib.iftrEndPass(self.h))
 
     def set_mvp(self, mvp):
         m = np.ascontiguousarray(mvp, np.float32).reshape(-1)

@@ -38,7 +38,8 @@ enum {
     IFTR_ERR_CUDA = 3,
     IFTR_ERR_OVERFLOW = 4,      /* a scratch capacity was exceeded; see iftrReserve */
     IFTR_ERR_NO_DEVICE = 5,
-    IFTR_ERR_STATE = 6          /* missing binding (framebuffer, vertex/index buffer, shader) */
+    IFTR_ERR_STATE = 6,         /* missing binding (framebuffer, vertex/index buffer, shader) */
+    IFTR_ERR_LIMIT = 7          /* an ordered pass had more than 8192 entries in one 16x16 tile */
 };
 
 /* ---- enums (same numbering as the reference, base/Constants.h:23-96, TypeDescriptor.h:26-40) */
@@ -120,6 +121,15 @@ IFTR_API int iftrOptsetForceDeterministic(IfritGbRenderer* h, int opt);         
 IFTR_API int iftrOptSetDepthTestEnable(IfritGbRenderer* h, int opt);                /* TRE:61 */
 IFTR_API int iftrDrawLegacy(IfritGbRenderer* h, int numIndices, int clearFramebuffer); /* TRE:64, synchronous */
 IFTR_API int iftrClear(IfritGbRenderer* h);                                          /* TRE:67 */
+/* Multi-draw render pass (no counterpart call in the reference, whose drawElements is one draw
+ * per pass): draws recorded between Begin and End snapshot the state current at each
+ * iftrPassDraw (MVP, shading, blend, depth, cull, texture, geometry) and run as one pass, so
+ * MSAA samples of all draws resolve together on chip.  Geometry bound from host objects must
+ * not change inside a pass.  Passes that blend, use NOT_EQUAL with depth writes or mix depth
+ * states run the ordered path (triangles applied per sample in submission order). */
+IFTR_API int iftrBeginPass(IfritGbRenderer* h, int clearFramebuffer);
+IFTR_API int iftrPassDraw(IfritGbRenderer* h, int firstIndex, int numIndices);
+IFTR_API int iftrEndPass(IfritGbRenderer* h);
 /* CUDA-renderer state (TRC:91-111) */
 IFTR_API int iftrSetCullMode(IfritGbRenderer* h, int cullMode);                      /* TRC:107 */
 IFTR_API int iftrSetFrontFace(IfritGbRenderer* h, int counterClockwise);

@@ -149,3 +149,89 @@ def test_full_size_textured_msaa_frame():
                               shading=ig.FS_TEXTURED, texture=tex, max_aniso=8)
     assert_parity(gpu, ref)
     assert (gpu["vis"] >= 0).mean() > 0.95
+
+
+# ---------------------------------------------------------------- multi-draw passes, blending
+def _pass_both(W, H, S, draws, fmt=ig.FORMAT_RGBA8, clear_color=(0.1, 0.2, 0.3, 1.0)):
+    """draws: list of dicts(vertices, indices, mvp, attr, cull, depth_func, depth_write, blend, shading)
+    sharing one vertex/index array each; renders them as one pass on both sides."""
+    from oracle import oracle as O
+    v = draws[0]["vertices"]
+    allf = np.concatenate([d["indices"] for d in draws], 0)
+    r = ig.Renderer(W, H, S, fmt, visibility=True)
+    r.set_geometry(v, allf, draws[0]["attr"])
+    r.set_state(cull=draws[0]["cull"], depth_func=draws[0]["depth_func"], clear_color=clear_color)
+    r.begin_pass(clear=True)
+    first, odraws, base = 0, [], 0
+    for d in draws:
+        r.set_state(cull=d["cull"], depth_func=d["depth_func"], depth_write=d.get("depth_write", True),
+                    shading=d.get("shading", ig.FS_GOURAUD), clear_color=clear_color)
+        r.set_mvp(d["mvp"])
+        blend = d.get("blend")
+        if blend:
+            r.set_blend(True, *blend)
+        else:
+            r.set_blend(False)
+        n = d["indices"].size
+        r.pass_draw(first, n)
+        od, keep = O.make_draw(v, d["indices"], d["mvp"], attr_offset=3, attr_count=d["attr"], cull_mode=d["cull"],
+                               depth_func=d["depth_func"], depth_write=int(d.get("depth_write", True)),
+                               blend=blend, shading=d.get("shading", 0), prim_base=base)
+        odraws.append((od, keep))
+        first += n
+        base += n // 3
+    r.end_pass()
+    gpu = {"color": r.color(), "depth": r.depth(), "vis": r.visibility()}
+    from tests.gpu_harness import FMT_TO_ORACLE
+    ref = O.render(odraws, W, H, S, FMT_TO_ORACLE[fmt], clear=True, clear_color=clear_color, clear_depth=1.0,
+                   nthreads=os.cpu_count() or 1)
+    return gpu, ref
+
+
+def _rgba_soup(n, seed, W, H):
+    v, f, mvp = soup(n, seed, W, H)
+    rng = np.random.default_rng(seed)
+    col = rng.uniform(0, 1, (len(v), 4)).astype(np.float32)
+    col[:, 3] = rng.uniform(0.2, 0.9, len(v))
+    return np.concatenate([v[:, :3], col], 1), f, mvp
+
+
+@pytest.mark.parametrize("S", [1, 4, 8])
+def test_multi_draw_instances_deferred(S):
+    v, f, mvp = _rgba_soup(6000, 31, 160, 128)
+    rng = np.random.default_rng(2)
+    draws = []
+    for i in range(4):
+        m = mvp.copy()
+        m[:, 3] += (rng.normal(size=4) * 0.05).astype(np.float32)
+        draws.append(dict(vertices=v, indices=f[i * 1500:(i + 1) * 1500], mvp=m, attr=4, cull=0, depth_func=ig.LESS))
+    gpu, ref = _pass_both(160, 128, S, draws)
+    assert_parity(gpu, ref)
+
+
+@pytest.mark.parametrize("S", [1, 4])
+def test_alpha_blended_draws_in_order(S):
+    v, f, mvp = _rgba_soup(6000, 32, 160, 128)
+    draws = [dict(vertices=v, indices=f[:3000], mvp=mvp, attr=4, cull=0, depth_func=ig.LESS),
+             dict(vertices=v, indices=f[3000:], mvp=mvp, attr=4, cull=0, depth_func=ig.LESS, depth_write=False,
+                  blend=(6, 7, 1, 7))]
+    gpu, ref = _pass_both(160, 128, S, draws)
+    assert_parity(gpu, ref)
+
+
+@pytest.mark.parametrize("factors", [(1, 1, 1, 1), (2, 3, 8, 9), (4, 5, 0, 1), (8, 9, 6, 7)])
+def test_blend_factors(factors):
+    v, f, mvp = _rgba_soup(3000, 33, 96, 80)
+    draws = [dict(vertices=v, indices=f, mvp=mvp, attr=4, cull=0, depth_func=ig.ALWAYS, blend=factors)]
+    gpu, ref = _pass_both(96, 80, 4, draws, fmt=ig.FORMAT_RGBA32F)
+    assert_parity(gpu, ref, fmt=ig.FORMAT_RGBA32F)
+
+
+def test_not_equal_and_mixed_depth_state_pass():
+    v, f, mvp = _rgba_soup(4000, 34, 128, 96)
+    f = np.concatenate([f, f[::4]], 0)
+    draws = [dict(vertices=v, indices=f[:2000], mvp=mvp, attr=4, cull=0, depth_func=ig.LESS),
+             dict(vertices=v, indices=f[2000:4000], mvp=mvp, attr=4, cull=0, depth_func=ig.NOT_EQUAL),
+             dict(vertices=v, indices=f[4000:], mvp=mvp, attr=4, cull=0, depth_func=ig.GREATER_OR_EQUAL)]
+    gpu, ref = _pass_both(128, 96, 4, draws)
+    assert_parity(gpu, ref)
