@@ -8,6 +8,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstddef>
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
@@ -17,6 +18,7 @@
 #include <vector>
 
 #include "../../include/ifrit_gb300.h"
+#include "pass_plan.h"
 #include "raster_kernels.cuh"
 
 using ifr::DrawDev;
@@ -126,12 +128,56 @@ struct Texture {
 
 uint64_t g_id_counter = 1;
 
+// Device scratch and pinned descriptor staging of a pass.  Buffers grow on demand; each growth
+// bumps `generation`, which invalidates CUDA graphs captured with the old addresses.
+struct PassScratch {
+    DevMem tile_count, tile_offset, tile_cursor, pairs, records, status, draws, draw_start, views, view_tiles, queues,
+        entries;
+    size_t tiles_alloc = 0;
+    uint32_t pair_capacity = 0;
+    uint64_t generation = 1;
+    uint32_t* h_status = nullptr;  // pinned copy of the status words, written by each pass
+    HostBytes staging;             // pinned descriptors: draws | draw starts | views | view tile starts
+    cudaEvent_t staged = nullptr;  // recorded after the last descriptor upload
+    bool staged_pending = false;
+    void release() {
+        for (DevMem* m : {&tile_count, &tile_offset, &tile_cursor, &pairs, &records, &status, &draws, &draw_start, &views,
+                          &view_tiles, &queues, &entries})
+            m->release();
+        if (h_status) cudaFreeHost(h_status);
+        h_status = nullptr;
+        staging.release();
+        if (staged) cudaEventDestroy(staged);
+        staged = nullptr;
+    }
+};
+
+// A batched pass prepared from one description (views + draws), with its captured graph.
+struct BatchState {
+    PassScratch scratch;
+    std::vector<uint8_t> key;  // description bytes and tuning settings of the captured graph
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    uint64_t captured_generation = 0;
+    cudaStream_t capture_stream = nullptr;
+    int autotune = 1, tile_size = 16, ctas_per_sm = 0;  // settings
+    int tuned_tile = 16, tuned_ctas = 0;                // last choice
+    void drop_graph() {
+        if (exec) cudaGraphExecDestroy(exec);
+        if (graph) cudaGraphDestroy(graph);
+        exec = nullptr;
+        graph = nullptr;
+        key.clear();
+    }
+};
+
 }  // namespace
 
 struct IfritGbRenderer {
     bool inited = false;
     cudaStream_t stream = nullptr;
     bool own_stream = false;
+    int sms = 0;
     // bindings
     IfritGbFrameBuffer* fb = nullptr;
     const IfritGbVertexBuffer* vb = nullptr;
@@ -161,12 +207,8 @@ struct IfritGbRenderer {
     const void* up_ib_key = nullptr;
     uint64_t up_ib_gen = 0;
     int att_w = 0, att_h = 0, att_s = 0, att_fmt = -1;
-    DevMem d_tile_count, d_tile_offset, d_tile_cursor, d_pairs, d_status, d_draws, d_draw_start, d_records;
-    int tiles_alloc = 0;
-    uint32_t pair_capacity = 0;
-    uint32_t* h_status = nullptr;  // pinned
-    DrawDev* h_draws = nullptr;    // pinned staging
-    int* h_draw_start = nullptr;   // pinned staging
+    PassScratch pass;  // scratch of the plain (single-view) passes
+    BatchState batch;
     Texture tex[16];
     IfritGbSampler samplers[16];
     int bound_tex = 0, bound_sampler = 0;
@@ -175,7 +217,8 @@ struct IfritGbRenderer {
     cudaEvent_t ev[6] = {};
     float stage_ms[5] = {0, 0, 0, 0, 0};
     std::string last_error;
-    int pending = 0;  // an async pass whose status has not been checked
+    int pending = 0;        // plain passes whose status has not been checked
+    int pending_batch = 0;  // batched passes whose status has not been checked
     bool in_pass = false;
     int pass_clear = 0;
     std::vector<DrawDev> pass_draws;
@@ -229,29 +272,146 @@ int ensure_attachments(IfritGbRenderer* h, int W, int H, int S, int fmt) {
     h->att_w = W; h->att_h = H; h->att_s = S; h->att_fmt = fmt;
     if (fresh) {
         IFTR_CUDA(h, cudaMemsetAsync(h->d_color.p, 0, npix * color_bytes(fmt), h->stream));
-        std::vector<float> init(1, h->clear_depth);
         // depth starts at the clear value
         std::vector<float> dv(npix * S, h->clear_depth);
         IFTR_CUDA(h, cudaMemcpyAsync(h->d_depth.p, dv.data(), dv.size() * sizeof(float), cudaMemcpyHostToDevice, h->stream));
         IFTR_CUDA(h, cudaStreamSynchronize(h->stream));
     }
-    int tx = (W + ifr::kTileSize - 1) / ifr::kTileSize, ty = (H + ifr::kTileSize - 1) / ifr::kTileSize;
-    int T = tx * ty;
-    if (T > h->tiles_alloc) {
-        IFTR_CUDA(h, h->d_tile_count.reserve((size_t)T * 4));
-        IFTR_CUDA(h, h->d_tile_offset.reserve((size_t)(T + 1) * 4));
-        IFTR_CUDA(h, h->d_tile_cursor.reserve((size_t)T * 4));
-        IFTR_CUDA(h, cudaMemsetAsync(h->d_tile_count.p, 0, (size_t)T * 4, h->stream));
-        h->tiles_alloc = T;
-    }
     return IFTR_OK;
 }
 
-int ensure_pairs(IfritGbRenderer* h, size_t want) {
-    if (want <= h->pair_capacity) return IFTR_OK;
+int scratch_init(IfritGbRenderer* h, PassScratch& s) {
+    if (s.h_status) return IFTR_OK;
+    IFTR_CUDA(h, cudaMallocHost(&s.h_status, ifr::ST_WORDS * sizeof(uint32_t)));
+    std::memset(s.h_status, 0, ifr::ST_WORDS * sizeof(uint32_t));
+    IFTR_CUDA(h, s.status.reserve(ifr::ST_WORDS * sizeof(uint32_t)));
+    IFTR_CUDA(h, cudaMemsetAsync(s.status.p, 0, ifr::ST_WORDS * sizeof(uint32_t), h->stream));
+    IFTR_CUDA(h, s.queues.reserve(2 * ifr::kMaxGroups * sizeof(uint32_t)));
+    IFTR_CUDA(h, cudaEventCreateWithFlags(&s.staged, cudaEventDisableTiming));
+    return IFTR_OK;
+}
+
+int ensure_pairs(IfritGbRenderer* h, PassScratch& s, size_t want) {
+    if (want <= s.pair_capacity) return IFTR_OK;
     if (want > 0x7fffffffu) return IFTR_ERR_OVERFLOW;
-    IFTR_CUDA(h, h->d_pairs.reserve(want * 4));
-    h->pair_capacity = (uint32_t)want;
+    IFTR_CUDA(h, s.pairs.reserve(want * 4));
+    s.pair_capacity = (uint32_t)want;
+    s.generation++;
+    return IFTR_OK;
+}
+
+// Grows the scratch of a pass over `tiles` screen tiles and `tris` triangles; `entries` is the
+// per-sample winner scratch in ints (0: the views bring their own).
+int scratch_reserve(IfritGbRenderer* h, PassScratch& s, size_t tiles, size_t tris, size_t ndraws, size_t nviews,
+                    size_t entries) {
+    int rc = scratch_init(h, s);
+    if (rc) return rc;
+    const uint64_t gen0 = s.generation;
+    auto grow = [&](DevMem& m, size_t bytes) -> cudaError_t {
+        if (bytes <= m.bytes) return cudaSuccess;
+        s.generation++;
+        return m.reserve(bytes + bytes / 4);
+    };
+    if (tiles > s.tiles_alloc) {
+        const size_t n = tiles + tiles / 4;
+        IFTR_CUDA(h, s.tile_count.reserve(n * 4));
+        IFTR_CUDA(h, s.tile_offset.reserve((n + 1) * 4));
+        IFTR_CUDA(h, s.tile_cursor.reserve(n * 4));
+        IFTR_CUDA(h, cudaMemsetAsync(s.tile_count.p, 0, n * 4, h->stream));  // counts start at zero
+        s.tiles_alloc = n;
+        s.generation++;
+    }
+    IFTR_CUDA(h, grow(s.records, std::max<size_t>(1, tris) * sizeof(ifr::TriRecord)));
+    IFTR_CUDA(h, grow(s.draws, std::max<size_t>(1, ndraws) * sizeof(DrawDev)));
+    IFTR_CUDA(h, grow(s.draw_start, (ndraws + 1) * sizeof(int)));
+    IFTR_CUDA(h, grow(s.views, std::max<size_t>(1, nviews) * sizeof(ifr::ViewArgs)));
+    IFTR_CUDA(h, grow(s.view_tiles, (nviews + 1) * sizeof(int)));
+    if (entries) IFTR_CUDA(h, grow(s.entries, entries * sizeof(int)));
+    if (s.pair_capacity == 0) {
+        rc = ensure_pairs(h, s, std::max<size_t>(1u << 20, tris * 4));
+        if (rc) return rc;
+    }
+    (void)gen0;
+    return IFTR_OK;
+}
+
+// Copies the pass descriptors to the device through pinned staging (reused once the previous
+// upload has executed).
+int upload_descriptors(IfritGbRenderer* h, PassScratch& s, const std::vector<DrawDev>& draws,
+                       const std::vector<int>& draw_start, const std::vector<ifr::ViewArgs>& views,
+                       const std::vector<int>& view_tiles) {
+    const size_t b0 = draws.size() * sizeof(DrawDev), b1 = draw_start.size() * sizeof(int);
+    const size_t b2 = views.size() * sizeof(ifr::ViewArgs), b3 = view_tiles.size() * sizeof(int);
+    if (s.staged_pending) {
+        IFTR_CUDA(h, cudaEventSynchronize(s.staged));
+        s.staged_pending = false;
+    }
+    if (s.staging.size() < b0 + b1 + b2 + b3 && !s.staging.assign(b0 + b1 + b2 + b3)) return IFTR_ERR_CUDA;
+    uint8_t* p = s.staging.data();
+    std::memcpy(p, draws.data(), b0);
+    std::memcpy(p + b0, draw_start.data(), b1);
+    std::memcpy(p + b0 + b1, views.data(), b2);
+    std::memcpy(p + b0 + b1 + b2, view_tiles.data(), b3);
+    IFTR_CUDA(h, cudaMemcpyAsync(s.draws.p, p, b0, cudaMemcpyHostToDevice, h->stream));
+    IFTR_CUDA(h, cudaMemcpyAsync(s.draw_start.p, p + b0, b1, cudaMemcpyHostToDevice, h->stream));
+    IFTR_CUDA(h, cudaMemcpyAsync(s.views.p, p + b0 + b1, b2, cudaMemcpyHostToDevice, h->stream));
+    IFTR_CUDA(h, cudaMemcpyAsync(s.view_tiles.p, p + b0 + b1 + b2, b3, cudaMemcpyHostToDevice, h->stream));
+    IFTR_CUDA(h, cudaEventRecord(s.staged, h->stream));
+    s.staged_pending = true;
+    return IFTR_OK;
+}
+
+PassArgs make_args(const PassScratch& s, int ndraws, int total_tris, int nviews, int total_tiles) {
+    PassArgs a;
+    std::memset(&a, 0, sizeof(a));
+    a.draws = s.draws.as<DrawDev>();
+    a.draw_start = s.draw_start.as<int>();
+    a.ndraws = ndraws;
+    a.total_tris = total_tris;
+    a.views = s.views.as<ifr::ViewArgs>();
+    a.view_tile_start = s.view_tiles.as<int>();
+    a.nviews = nviews;
+    a.total_tiles = total_tiles;
+    a.tile_count = s.tile_count.as<uint32_t>();
+    a.tile_offset = s.tile_offset.as<uint32_t>();
+    a.tile_cursor = s.tile_cursor.as<uint32_t>();
+    a.pairs = s.pairs.as<uint32_t>();
+    a.records = s.records.as<ifr::TriRecord>();
+    a.pair_capacity = s.pair_capacity;
+    a.status = s.status.as<uint32_t>();
+    a.queues = s.queues.as<uint32_t>();
+    return a;
+}
+
+// Stream work of one pass: clear the per-pass status words, run the pipeline, copy the status
+// back to pinned memory.  Contains no host synchronisation (it is also captured into graphs).
+cudaError_t launch_with_status(PassScratch& s, const PassArgs& a, const ifr::LaunchPlan& plan, cudaStream_t st,
+                               cudaEvent_t* ev) {
+    cudaError_t e = cudaMemsetAsync(s.status.p, 0, ifr::ST_PASS_WORDS * sizeof(uint32_t), st);
+    if (e == cudaSuccess) e = ifr::launch_pass(a, plan, st, ev);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(s.h_status, s.status.p, ifr::ST_WORDS * sizeof(uint32_t), cudaMemcpyDeviceToHost, st);
+    return e;
+}
+
+// Reads the sticky status of a scratch after the stream was synchronised, grows the pair list
+// if a pass overflowed, and clears the sticky words.
+int consume_status(IfritGbRenderer* h, PassScratch& s) {
+    const uint32_t sticky = s.h_status[ifr::ST_STICKY];
+    const uint32_t max_pairs = s.h_status[ifr::ST_MAX_PAIRS];
+    h->stats.tile_pairs = s.h_status[ifr::ST_PAIRS];
+    if (sticky || max_pairs) {
+        IFTR_CUDA(h, cudaMemsetAsync(s.status.as<uint32_t>() + ifr::ST_STICKY, 0,
+                                     (ifr::ST_WORDS - ifr::ST_STICKY) * sizeof(uint32_t), h->stream));
+        s.h_status[ifr::ST_STICKY] = 0;
+        s.h_status[ifr::ST_MAX_PAIRS] = 0;
+    }
+    if (sticky & 1u) {
+        size_t want = (size_t)max_pairs + max_pairs / 4 + 1024;
+        int rc = ensure_pairs(h, s, want);
+        return rc ? rc : IFTR_ERR_OVERFLOW;
+    }
+    if (sticky & 2u) return IFTR_ERR_LIMIT;
     return IFTR_OK;
 }
 
@@ -312,66 +472,10 @@ void fill_state(IfritGbRenderer* h, DrawDev& d) {
     d.front_ccw = h->front_ccw;
     d.depth_func = h->depth_test ? h->depth_func : IF_COMPARE_OP_ALWAYS;
     d.depth_write = h->depth_write;
-    d.blend_enable = h->blend.blendEnable;
-    d.blend_src_color = h->blend.srcColorBlendFactor;
-    d.blend_dst_color = h->blend.dstColorBlendFactor;
-    d.blend_src_alpha = h->blend.srcAlphaBlendFactor;
-    d.blend_dst_alpha = h->blend.dstAlphaBlendFactor;
+    ifr::fill_blend(d, h->blend);
     d.shading = h->fs_model;
     const Texture& t = h->tex[h->bound_tex];
-    d.texels = t.mem.as<uint32_t>();
-    d.tex_w = t.w;
-    d.tex_h = t.h;
-    d.tex_levels = t.levels;
-    const IfritGbSampler& s = h->samplers[h->bound_sampler];
-    d.sampler.address_u = s.addressModeU;
-    d.sampler.address_v = s.addressModeV;
-    d.sampler.filter = s.filterMode;
-    d.sampler.border_white = s.borderColor;
-    d.sampler.max_aniso = s.anisotropyEnable ? std::max(1, (int)s.maxAnisotropy) : 1;
-    d.sampler.lod_bias = s.lodBias;
-    int w = t.w, hh = t.h, off = 0;
-    for (int l = 0; l < 16; l++) {
-        d.lvl_off[l] = off;
-        d.lvl_w[l] = w;
-        d.lvl_h[l] = hh;
-        off += w * hh;
-        w = (w + 1) >> 1;
-        hh = (hh + 1) >> 1;
-        if (w < 1) w = 1;
-        if (hh < 1) hh = 1;
-    }
-}
-
-void sample_table(int S, int* xs, int* ys) {
-    static const int SP1[2] = {128, 128};
-    static const int SP2[4] = {192, 192, 64, 64};
-    static const int SP4[8] = {96, 32, 224, 96, 32, 160, 160, 224};
-    static const int SP8[16] = {144, 80, 112, 176, 208, 144, 80, 48, 48, 208, 16, 112, 176, 240, 240, 16};
-    static const int SP16[32] = {144, 144, 112, 80, 80, 160, 192, 112, 48, 96, 160, 208, 208, 176, 176, 48,
-                                 96, 224, 128, 16, 64, 32, 32, 192, 0, 128, 240, 64, 224, 240, 16, 0};
-    const int* t = S == 1 ? SP1 : S == 2 ? SP2 : S == 4 ? SP4 : S == 8 ? SP8 : SP16;
-    for (int k = 0; k < S; k++) { xs[k] = t[2 * k]; ys[k] = t[2 * k + 1]; }
-}
-
-void fill_pass_const(ifr::PassConst& c, int W, int H, int S) {
-    std::memset(&c, 0, sizeof(c));
-    c.W = W; c.H = H; c.S = S;
-    c.tiles_x = (W + ifr::kTileSize - 1) / ifr::kTileSize;
-    c.tiles_y = (H + ifr::kTileSize - 1) / ifr::kTileSize;
-    sample_table(S, c.sx, c.sy);
-    c.smin_x = c.smax_x = c.sx[0];
-    c.smin_y = c.smax_y = c.sy[0];
-    for (int k = 1; k < S; k++) {
-        c.smin_x = std::min(c.smin_x, c.sx[k]); c.smax_x = std::max(c.smax_x, c.sx[k]);
-        c.smin_y = std::min(c.smin_y, c.sy[k]); c.smax_y = std::max(c.smax_y, c.sy[k]);
-    }
-    c.shade_x = 128;
-    c.shade_y = 128;
-    c.W256 = (float)W * 256.0f;
-    c.H256 = (float)H * 256.0f;
-    c.gx = (float)(1.0 + 2.0 * 8192.0 / (double)W);
-    c.gy = (float)(1.0 + 2.0 * 8192.0 / (double)H);
+    ifr::fill_texture(d, t.mem.as<uint32_t>(), t.w, t.h, t.levels, h->samplers[h->bound_sampler]);
 }
 
 int ensure_init(IfritGbRenderer* h) {
@@ -382,13 +486,11 @@ int ensure_init(IfritGbRenderer* h) {
         IFTR_CUDA(h, cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
         h->own_stream = true;
     }
-    IFTR_CUDA(h, cudaMallocHost(&h->h_status, ifr::ST_WORDS * sizeof(uint32_t)));
-    IFTR_CUDA(h, cudaMallocHost(&h->h_draws, ifr::kMaxDraws * sizeof(DrawDev)));
-    IFTR_CUDA(h, cudaMallocHost(&h->h_draw_start, (ifr::kMaxDraws + 1) * sizeof(int)));
-    IFTR_CUDA(h, h->d_status.reserve(ifr::ST_WORDS * sizeof(uint32_t)));
-    IFTR_CUDA(h, h->d_draws.reserve(ifr::kMaxDraws * sizeof(DrawDev)));
-    IFTR_CUDA(h, h->d_draw_start.reserve((ifr::kMaxDraws + 1) * sizeof(int)));
-    std::memset(h->h_status, 0, ifr::ST_WORDS * sizeof(uint32_t));
+    int dev = 0;
+    IFTR_CUDA(h, cudaGetDevice(&dev));
+    IFTR_CUDA(h, cudaDeviceGetAttribute(&h->sms, cudaDevAttrMultiProcessorCount, dev));
+    int rc = scratch_init(h, h->pass);
+    if (rc) return rc;
     for (auto& s : h->samplers) {
         s = IfritGbSampler{IF_FILTER_LINEAR, IF_SAMPLER_ADDRESS_MODE_REPEAT, IF_SAMPLER_ADDRESS_MODE_REPEAT,
                            IF_SAMPLER_ADDRESS_MODE_REPEAT, 0, 0, 1.0f, 0.0f};
@@ -412,7 +514,7 @@ int prepare_draw(IfritGbRenderer* h, int firstIndex, int numIndices, DrawDev& d)
     return IFTR_OK;
 }
 
-// Enqueues one pass of draws on the renderer's stream.
+// Enqueues one pass of draws into the bound framebuffer on the renderer's stream.
 int enqueue_pass(IfritGbRenderer* h, std::vector<DrawDev>& draws, int clear) {
     int rc = ensure_init(h);
     if (rc) return rc;
@@ -424,56 +526,40 @@ int enqueue_pass(IfritGbRenderer* h, std::vector<DrawDev>& draws, int clear) {
     rc = ensure_attachments(h, W, H, S, fmt);
     if (rc) return rc;
     // global triangle ids: draw i covers [start_i, start_{i+1})
+    std::vector<int> draw_start(draws.size() + 1);
     int64_t total = 0;
-    bool ordered = false;
     for (size_t i = 0; i < draws.size(); i++) {
         DrawDev& d = draws[i];
+        d.view = 0;
         d.prim_base = (int)total;
-        h->h_draw_start[i] = (int)total;
+        draw_start[i] = (int)total;
         total += d.num_triangles;
-        if (d.blend_enable || (d.depth_write && d.depth_func == IF_COMPARE_OP_NOT_EQUAL) ||
-            d.depth_func != draws[0].depth_func || d.depth_write != draws[0].depth_write)
-            ordered = true;
-        h->h_draws[i] = d;
+        if (total >= (int64_t)1 << 28) return IFTR_ERR_INVALID_ARG;  // entry = triangle << 3 | fan index
     }
-    if (total >= (int64_t)1 << 28) return IFTR_ERR_INVALID_ARG;  // entry = triangle << 3 | fan index
-    h->h_draw_start[draws.size()] = (int)total;
-    IFTR_CUDA(h, cudaMemcpyAsync(h->d_draws.p, h->h_draws, draws.size() * sizeof(DrawDev), cudaMemcpyHostToDevice, h->stream));
-    IFTR_CUDA(h, cudaMemcpyAsync(h->d_draw_start.p, h->h_draw_start, (draws.size() + 1) * sizeof(int),
-                                 cudaMemcpyHostToDevice, h->stream));
-    if (h->pair_capacity == 0) {
-        rc = ensure_pairs(h, std::max<size_t>(1u << 20, (size_t)total * 4));
-        if (rc) return rc;
-    }
-    IFTR_CUDA(h, h->d_records.reserve(std::max<size_t>(1, (size_t)total) * sizeof(ifr::TriRecord)));
-    IFTR_CUDA(h, cudaMemsetAsync(h->d_status.p, 0, ifr::ST_WORDS * sizeof(uint32_t), h->stream));
-    PassArgs a;
-    std::memset(&a, 0, sizeof(a));
-    fill_pass_const(a.c, W, H, S);
-    a.draws = h->d_draws.as<DrawDev>();
-    a.draw_start = h->d_draw_start.as<int>();
-    a.ndraws = (int)draws.size();
-    a.total_tris = (int)total;
-    a.format = fmt;
-    a.color = h->d_color.p;
-    a.depth = h->d_depth.as<float>();
-    a.vis = h->vis_output ? h->d_vis.as<int>() : nullptr;
-    a.entries = h->d_entries.as<int>();
-    a.clear = clear;
-    std::memcpy(a.clear_color, h->clear_color, sizeof(a.clear_color));
-    a.clear_depth = h->clear_depth;
-    a.depth_func = draws[0].depth_func;
-    a.depth_write = draws[0].depth_write;
-    a.ordered = ordered ? 1 : 0;
-    a.tile_count = h->d_tile_count.as<uint32_t>();
-    a.tile_offset = h->d_tile_offset.as<uint32_t>();
-    a.tile_cursor = h->d_tile_cursor.as<uint32_t>();
-    a.pairs = h->d_pairs.as<uint32_t>();
-    a.records = h->d_records.as<ifr::TriRecord>();
-    a.pair_capacity = h->pair_capacity;
-    a.status = h->d_status.as<uint32_t>();
-    IFTR_CUDA(h, ifr::launch_pass(a, h->stream, h->timing ? h->ev : nullptr));
-    IFTR_CUDA(h, cudaMemcpyAsync(h->h_status, h->d_status.p, ifr::ST_WORDS * sizeof(uint32_t), cudaMemcpyDeviceToHost, h->stream));
+    draw_start[draws.size()] = (int)total;
+    std::vector<ifr::ViewArgs> views(1);
+    ifr::ViewArgs& v = views[0];
+    std::memset(&v, 0, sizeof(v));
+    ifr::fill_pass_const(v.c, W, H, S, 16);
+    v.format = fmt;
+    v.color = h->d_color.p;
+    v.depth = h->d_depth.as<float>();
+    v.vis = h->vis_output ? h->d_vis.as<int>() : nullptr;
+    v.entries = h->d_entries.as<int>();
+    v.clear = clear;
+    std::memcpy(v.clear_color, h->clear_color, sizeof(v.clear_color));
+    v.clear_depth = h->clear_depth;
+    ifr::set_view_depth_state(v, draws.data(), (int)draws.size());
+    std::vector<int> view_tiles(2);
+    ifr::LaunchPlan plan;
+    int T = 0;
+    if (!ifr::plan_groups(views.data(), 1, view_tiles.data(), h->sms, 0, plan, T)) return IFTR_ERR_INVALID_ARG;
+    rc = scratch_reserve(h, h->pass, (size_t)T, (size_t)total, draws.size(), 1, 0);
+    if (rc) return rc;
+    rc = upload_descriptors(h, h->pass, draws, draw_start, views, view_tiles);
+    if (rc) return rc;
+    PassArgs a = make_args(h->pass, (int)draws.size(), (int)total, 1, T);
+    IFTR_CUDA(h, launch_with_status(h->pass, a, plan, h->stream, h->timing ? h->ev : nullptr));
     h->stats.triangles_in = (uint64_t)total;
     h->pending = 1;
     return IFTR_OK;
@@ -490,20 +576,23 @@ int enqueue_draw(IfritGbRenderer* h, int numIndices, int clear) {
 }
 
 int check_pending(IfritGbRenderer* h) {
-    if (!h->pending) return IFTR_OK;
+    if (!h->pending && !h->pending_batch) return IFTR_OK;
     IFTR_CUDA(h, cudaStreamSynchronize(h->stream));
-    h->pending = 0;
-    if (h->timing)
-        for (int i = 0; i < 5; i++) cudaEventElapsedTime(&h->stage_ms[i], h->ev[i], h->ev[i + 1]);
-    h->stats.tile_pairs = h->h_status[ifr::ST_PAIRS];
-    h->stats.pair_capacity = h->pair_capacity;
-    if (h->h_status[ifr::ST_OVERFLOW]) {
-        size_t want = (size_t)h->h_status[ifr::ST_PAIRS] + h->h_status[ifr::ST_PAIRS] / 4 + 1024;
-        int rc = ensure_pairs(h, want);
-        return rc ? rc : IFTR_ERR_OVERFLOW;
+    int rc = IFTR_OK;
+    if (h->pending) {
+        h->pending = 0;
+        if (h->timing)
+            for (int i = 0; i < 5; i++) cudaEventElapsedTime(&h->stage_ms[i], h->ev[i], h->ev[i + 1]);
+        rc = consume_status(h, h->pass);
+        h->stats.pair_capacity = h->pass.pair_capacity;
     }
-    if (h->h_status[ifr::ST_ORDERED_LIMIT]) return IFTR_ERR_LIMIT;
-    return IFTR_OK;
+    if (h->pending_batch) {
+        h->pending_batch = 0;
+        int rb = consume_status(h, h->batch.scratch);
+        if (rb == IFTR_ERR_OVERFLOW) h->batch.drop_graph();  // re-size and re-capture on the next call
+        if (!rc) rc = rb;
+    }
+    return rc;
 }
 
 int copy_back_host_images(IfritGbRenderer* h) {
@@ -532,6 +621,323 @@ int copy_back_host_images(IfritGbRenderer* h) {
     return IFTR_OK;
 }
 
+// ----------------------------------------------------------------------------- batched views
+int validate_batch(const IfritGbBatchView* views, int nv, const IfritGbBatchDraw* draws, int nd) {
+    if (!views || nv <= 0 || nv > IFTR_MAX_BATCH_VIEWS || nd < 0 || nd > IFTR_MAX_BATCH_DRAWS || (nd > 0 && !draws))
+        return IFTR_ERR_INVALID_ARG;
+    for (int i = 0; i < nv; i++) {
+        const IfritGbBatchView& v = views[i];
+        if (v.width <= 0 || v.height <= 0 || v.width > 16384 || v.height > 16384 || !ifr::valid_samples(v.samples))
+            return IFTR_ERR_INVALID_ARG;
+        if (v.colorFormat < 0 || v.colorFormat > 3 || !v.color || !v.depth) return IFTR_ERR_INVALID_ARG;
+        if (!ifr::targets_aligned(v.color, v.colorFormat, v.depth, v.visibility, v.samples)) return IFTR_ERR_INVALID_ARG;
+    }
+    int64_t total = 0;
+    for (int i = 0; i < nd; i++) {
+        const IfritGbBatchDraw& d = draws[i];
+        if (d.view < 0 || d.view >= nv || d.numIndices < 0 || d.numIndices % 3 != 0) return IFTR_ERR_INVALID_ARG;
+        if (d.numIndices > 0 && (!d.vertices || !d.indices)) return IFTR_ERR_INVALID_ARG;
+        if ((uintptr_t)d.vertices % 4 || (uintptr_t)d.indices % 4 || (uintptr_t)d.texels % 4) return IFTR_ERR_INVALID_ARG;
+        if (d.strideFloats < 3 || d.attrCount < 0 || d.attrCount > 4 || d.attrOffsetFloats < 0 ||
+            d.attrOffsetFloats + d.attrCount > d.strideFloats)
+            return IFTR_ERR_INVALID_ARG;
+        if (d.depthFunc < 0 || d.depthFunc > 7 || d.cullMode < 0 || d.cullMode > 3 || d.shadingModel < IFTR_FS_GOURAUD ||
+            d.shadingModel > IFTR_FS_PRIMITIVE_ID)
+            return IFTR_ERR_INVALID_ARG;
+        for (int f : {d.blend.srcColorBlendFactor, d.blend.dstColorBlendFactor, d.blend.srcAlphaBlendFactor,
+                      d.blend.dstAlphaBlendFactor})
+            if (d.blend.blendEnable && (f < 0 || f > 9)) return IFTR_ERR_INVALID_ARG;
+        if (d.shadingModel == IFTR_FS_TEXTURED &&
+            (!d.texels || d.texWidth <= 0 || d.texHeight <= 0 || d.texLevels <= 0 || d.texLevels > 16))
+            return IFTR_ERR_INVALID_ARG;
+        total += d.numIndices / 3;
+    }
+    if (total >= (int64_t)1 << 28) return IFTR_ERR_INVALID_ARG;  // entry = triangle << 3 | fan index
+    return IFTR_OK;
+}
+
+// Descriptor bytes of a batch call (struct padding left out) plus the tuning settings; a call
+// whose key equals the captured one replays the graph.
+std::vector<uint8_t> batch_key(const BatchState& b, const IfritGbBatchView* views, int nv, const IfritGbBatchDraw* draws,
+                               int nd) {
+    constexpr size_t d0 = offsetof(IfritGbBatchDraw, vertices);
+    constexpr size_t d1 = offsetof(IfritGbBatchDraw, sampler) + sizeof(IfritGbSampler);
+    const int settings[5] = {b.autotune, b.tile_size, b.ctas_per_sm, nv, nd};
+    std::vector<uint8_t> key(sizeof(settings) + (size_t)nv * sizeof(IfritGbBatchView) + (size_t)nd * (4 + d1 - d0));
+    uint8_t* p = key.data();
+    std::memcpy(p, settings, sizeof(settings));
+    p += sizeof(settings);
+    std::memcpy(p, views, (size_t)nv * sizeof(IfritGbBatchView));
+    p += (size_t)nv * sizeof(IfritGbBatchView);
+    for (int i = 0; i < nd; i++) {
+        std::memcpy(p, &draws[i].view, 4);
+        std::memcpy(p + 4, reinterpret_cast<const uint8_t*>(&draws[i]) + d0, d1 - d0);
+        p += 4 + d1 - d0;
+    }
+    return key;
+}
+
+// Host descriptors of a batch for one choice of tile size and persistent CTAs.  Views are
+// reordered so that each launch group is contiguous; the draws of each view follow in array
+// order, so global triangle ids keep every view's submission order.
+struct BatchBuild {
+    std::vector<DrawDev> draws;
+    std::vector<int> draw_start;
+    std::vector<ifr::ViewArgs> views;
+    std::vector<size_t> entry_offset;  // per internal view, ints into the entries scratch
+    std::vector<int> view_tiles;
+    ifr::LaunchPlan plan;
+    int total_tiles = 0;
+    int64_t total_tris = 0;
+    size_t entries = 0;
+};
+
+int build_batch(IfritGbRenderer* h, const IfritGbBatchView* views, int nv, const IfritGbBatchDraw* draws, int nd,
+                int tile_size, int ctas_per_sm, BatchBuild& out) {
+    std::vector<std::vector<int>> per_view(nv);
+    for (int i = 0; i < nd; i++) per_view[draws[i].view].push_back(i);
+    std::vector<DrawDev> dd(nd);
+    for (int i = 0; i < nd; i++) {
+        const IfritGbBatchDraw& s = draws[i];
+        DrawDev& d = dd[i];
+        std::memset(&d, 0, sizeof(d));
+        d.vertices = s.vertices;
+        d.stride = s.strideFloats;
+        d.num_vertices = s.numVertices;
+        d.attr_offset = s.attrOffsetFloats;
+        d.attr_count = s.attrCount;
+        d.indices = s.indices;
+        d.num_triangles = s.numIndices / 3;
+        std::memcpy(d.mvp, s.mvp, sizeof(d.mvp));
+        d.cull_mode = s.cullMode;
+        d.front_ccw = s.frontCounterClockwise != 0;
+        d.depth_func = s.depthTest ? s.depthFunc : IF_COMPARE_OP_ALWAYS;
+        d.depth_write = s.depthWrite != 0;
+        d.shading = s.shadingModel;
+        ifr::fill_blend(d, s.blend);
+        if (s.shadingModel == IFTR_FS_TEXTURED) ifr::fill_texture(d, s.texels, s.texWidth, s.texHeight, s.texLevels, s.sampler);
+    }
+    std::vector<ifr::ViewArgs> uv(nv);
+    std::vector<DrawDev> tmp;
+    for (int i = 0; i < nv; i++) {
+        const IfritGbBatchView& s = views[i];
+        ifr::ViewArgs& v = uv[i];
+        std::memset(&v, 0, sizeof(v));
+        tmp.clear();
+        for (int di : per_view[i]) tmp.push_back(dd[di]);
+        ifr::set_view_depth_state(v, tmp.data(), (int)tmp.size());
+        const int TS = ifr::tile_size_supported(s.samples, tile_size, v.ordered != 0) ? tile_size : 16;
+        ifr::fill_pass_const(v.c, s.width, s.height, s.samples, TS);
+        v.format = s.colorFormat;
+        v.color = s.color;
+        v.depth = s.depth;
+        v.vis = s.visibility;
+        v.clear = s.clear != 0;
+        std::memcpy(v.clear_color, s.clearColor, sizeof(v.clear_color));
+        v.clear_depth = s.clearDepth;
+    }
+    std::vector<int> order(nv);
+    for (int i = 0; i < nv; i++) order[i] = i;
+    std::stable_sort(order.begin(), order.end(),
+                     [&](int x, int y) { return ifr::group_key(uv[x]) < ifr::group_key(uv[y]); });
+    out.draws.clear();
+    out.draw_start.clear();
+    out.views.clear();
+    out.entry_offset.clear();
+    int64_t tri = 0;
+    size_t ent = 0;
+    for (int k = 0; k < nv; k++) {
+        const int vi = order[k];
+        ifr::ViewArgs v = uv[vi];
+        v.first_tri = (int)tri;
+        int prim = 0;
+        for (int di : per_view[vi]) {
+            DrawDev d = dd[di];
+            d.view = k;
+            d.prim_base = prim;
+            out.draw_start.push_back((int)tri);
+            out.draws.push_back(d);
+            prim += d.num_triangles;
+            tri += d.num_triangles;
+        }
+        out.entry_offset.push_back(ent);
+        // each view's winners start on a 256-byte boundary (the tile kernels move them as int4)
+        if (!v.ordered) ent += ((size_t)v.c.W * v.c.H * v.c.S + 63) / 64 * 64;
+        out.views.push_back(v);
+    }
+    out.draw_start.push_back((int)tri);
+    out.total_tris = tri;
+    out.entries = std::max<size_t>(ent, 1);
+    out.view_tiles.assign(nv + 1, 0);
+    if (!ifr::plan_groups(out.views.data(), nv, out.view_tiles.data(), h->sms, ctas_per_sm, out.plan, out.total_tiles))
+        return IFTR_ERR_INVALID_ARG;
+    return IFTR_OK;
+}
+
+// Grows the batch scratch for `bb`, points its views at the entries scratch and uploads the
+// descriptors.
+int stage_batch(IfritGbRenderer* h, BatchBuild& bb) {
+    PassScratch& s = h->batch.scratch;
+    int rc = scratch_reserve(h, s, (size_t)bb.total_tiles, (size_t)bb.total_tris, bb.draws.size(), bb.views.size(), bb.entries);
+    if (rc) return rc;
+    for (size_t k = 0; k < bb.views.size(); k++) bb.views[k].entries = s.entries.as<int>() + bb.entry_offset[k];
+    if (bb.draws.empty()) bb.draws.resize(1);  // keeps the upload well-formed; ndraws stays 0
+    return upload_descriptors(h, s, bb.draws, bb.draw_start, bb.views, bb.view_tiles);
+}
+
+PassArgs batch_args(IfritGbRenderer* h, const BatchBuild& bb, int nd) {
+    return make_args(h->batch.scratch, nd, (int)bb.total_tris, (int)bb.views.size(), bb.total_tiles);
+}
+
+// Saved colour and depth of the views that do not clear, so that sizing and tuning runs (which
+// execute the pass more than once) leave those targets as the one real run sees them.
+struct TargetBackup {
+    DevMem mem;
+    std::vector<std::pair<void*, size_t>> spans;  // (target, bytes), packed in order
+    int save(IfritGbRenderer* h, const IfritGbBatchView* views, int nv) {
+        size_t total = 0;
+        spans.clear();
+        for (int i = 0; i < nv; i++) {
+            if (views[i].clear) continue;
+            const size_t npix = (size_t)views[i].width * views[i].height;
+            spans.push_back({views[i].color, npix * color_bytes(views[i].colorFormat)});
+            spans.push_back({views[i].depth, npix * views[i].samples * sizeof(float)});
+            if (views[i].visibility) spans.push_back({views[i].visibility, npix * views[i].samples * sizeof(int)});
+        }
+        for (auto& sp : spans) total += sp.second;
+        if (!total) return IFTR_OK;
+        IFTR_CUDA(h, mem.reserve(total));
+        size_t off = 0;
+        for (auto& sp : spans) {
+            IFTR_CUDA(h, cudaMemcpyAsync(mem.as<uint8_t>() + off, sp.first, sp.second, cudaMemcpyDeviceToDevice, h->stream));
+            off += sp.second;
+        }
+        return IFTR_OK;
+    }
+    int restore(IfritGbRenderer* h) {
+        size_t off = 0;
+        for (auto& sp : spans) {
+            IFTR_CUDA(h, cudaMemcpyAsync(sp.first, mem.as<uint8_t>() + off, sp.second, cudaMemcpyDeviceToDevice, h->stream));
+            off += sp.second;
+        }
+        return IFTR_OK;
+    }
+};
+
+// Runs the staged batch once, synchronously, growing the pair list until it fits.
+int run_sized(IfritGbRenderer* h, BatchBuild& bb, int nd, TargetBackup& backup, bool& ran) {
+    for (int attempt = 0; attempt < 4; attempt++) {
+        int rc = stage_batch(h, bb);
+        if (rc) return rc;
+        if (ran) {
+            rc = backup.restore(h);
+            if (rc) return rc;
+        }
+        PassArgs a = batch_args(h, bb, nd);
+        IFTR_CUDA(h, launch_with_status(h->batch.scratch, a, bb.plan, h->stream, nullptr));
+        IFTR_CUDA(h, cudaStreamSynchronize(h->stream));
+        ran = true;
+        rc = consume_status(h, h->batch.scratch);
+        if (rc != IFTR_ERR_OVERFLOW) return rc;
+    }
+    return IFTR_ERR_OVERFLOW;
+}
+
+// Sizes the scratch, picks the launch parameters and captures the pass into a graph.
+int prepare_batch(IfritGbRenderer* h, const IfritGbBatchView* views, int nv, const IfritGbBatchDraw* draws, int nd) {
+    BatchState& b = h->batch;
+    b.drop_graph();
+    std::vector<std::pair<int, int>> cands;
+    if (b.autotune) {
+        bool any8 = false;
+        for (int i = 0; i < nv; i++) any8 |= ifr::tile_size_supported(views[i].samples, 8, false);
+        cands = {{16, 0}, {16, -2}};
+        if (any8) {
+            cands.push_back({8, 0});
+            cands.push_back({8, -2});
+        }
+    } else {
+        cands = {{b.tile_size, b.ctas_per_sm}};
+    }
+    TargetBackup backup;
+    int rc = backup.save(h, views, nv);
+    if (rc) return rc;
+    bool ran = false;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    if (cands.size() > 1) {
+        IFTR_CUDA(h, cudaEventCreate(&e0));
+        IFTR_CUDA(h, cudaEventCreate(&e1));
+    }
+    float best_ms = 1e30f;
+    int best = -1;
+    std::vector<ifr::LaunchPlan> seen;
+    for (size_t ci = 0; ci < cands.size() && !rc; ci++) {
+        BatchBuild bb;
+        rc = build_batch(h, views, nv, draws, nd, cands[ci].first, cands[ci].second, bb);
+        if (rc) break;
+        bool dup = false;
+        for (const auto& p : seen) dup |= std::memcmp(&p, &bb.plan, sizeof(p)) == 0;
+        if (dup) continue;
+        seen.push_back(bb.plan);
+        rc = run_sized(h, bb, nd, backup, ran);
+        if (rc) break;
+        if (cands.size() == 1) {
+            best = (int)ci;
+            break;
+        }
+        PassArgs a = batch_args(h, bb, nd);
+        cudaEventRecord(e0, h->stream);
+        for (int r = 0; r < 2 && !rc; r++) rc = cuda_fail(h, launch_with_status(b.scratch, a, bb.plan, h->stream, nullptr));
+        cudaEventRecord(e1, h->stream);
+        if (rc) break;
+        IFTR_CUDA(h, cudaStreamSynchronize(h->stream));
+        float ms = 0.0f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        rc = consume_status(h, b.scratch);
+        if (rc == IFTR_ERR_OVERFLOW) {  // cannot happen after a sized run; skip the candidate
+            rc = IFTR_OK;
+            continue;
+        }
+        if (!rc && ms < best_ms) {
+            best_ms = ms;
+            best = (int)ci;
+        }
+    }
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    if (rc) return rc;
+    if (best < 0) return IFTR_ERR_OVERFLOW;
+    b.tuned_tile = cands[best].first;
+    b.tuned_ctas = cands[best].second;
+    BatchBuild bb;
+    rc = build_batch(h, views, nv, draws, nd, b.tuned_tile, b.tuned_ctas, bb);
+    if (rc) return rc;
+    rc = stage_batch(h, bb);
+    if (rc) return rc;
+    if (ran) {
+        rc = backup.restore(h);
+        if (rc) return rc;
+    }
+    IFTR_CUDA(h, cudaStreamSynchronize(h->stream));
+    backup.mem.release();
+    // capture on the renderer's private stream (the caller's stream may be the legacy stream)
+    if (!b.capture_stream) IFTR_CUDA(h, cudaStreamCreateWithFlags(&b.capture_stream, cudaStreamNonBlocking));
+    PassArgs a = batch_args(h, bb, nd);
+    IFTR_CUDA(h, cudaStreamBeginCapture(b.capture_stream, cudaStreamCaptureModeThreadLocal));
+    cudaError_t e = launch_with_status(b.scratch, a, bb.plan, b.capture_stream, nullptr);
+    cudaGraph_t g = nullptr;
+    cudaError_t e2 = cudaStreamEndCapture(b.capture_stream, &g);
+    if (e != cudaSuccess || e2 != cudaSuccess) {
+        if (g) cudaGraphDestroy(g);
+        return cuda_fail(h, e != cudaSuccess ? e : e2);
+    }
+    b.graph = g;
+    IFTR_CUDA(h, cudaGraphInstantiate(&b.exec, g, 0));
+    b.captured_generation = b.scratch.generation;
+    h->stats.triangles_in = (uint64_t)bb.total_tris;
+    return IFTR_OK;
+}
+
 }  // namespace
 
 // ============================================================================ C-ABI
@@ -543,16 +949,14 @@ IFTR_API int iftrDestroyInstance(IfritGbRenderer* h) {
     if (!h) return IFTR_ERR_INVALID_ARG;
     if (h->inited) {
         cudaStreamSynchronize(h->stream);
-        for (DevMem* m : {&h->d_vertices, &h->d_indices, &h->d_color, &h->d_depth, &h->d_vis, &h->d_entries, &h->d_tile_count,
-                          &h->d_tile_offset, &h->d_tile_cursor, &h->d_pairs, &h->d_status, &h->d_draws, &h->d_draw_start,
-                          &h->d_records})
-            m->release();
+        for (DevMem* m : {&h->d_vertices, &h->d_indices, &h->d_color, &h->d_depth, &h->d_vis, &h->d_entries}) m->release();
+        h->pass.release();
+        h->batch.drop_graph();
+        h->batch.scratch.release();
+        if (h->batch.capture_stream) cudaStreamDestroy(h->batch.capture_stream);
         for (auto& t : h->tex) t.mem.release();
         for (cudaEvent_t e : h->ev)
             if (e) cudaEventDestroy(e);
-        cudaFreeHost(h->h_status);
-        cudaFreeHost(h->h_draws);
-        cudaFreeHost(h->h_draw_start);
         if (h->own_stream) cudaStreamDestroy(h->stream);
     }
     delete h;
@@ -637,6 +1041,44 @@ IFTR_API int iftrOptSetDepthTestEnable(IfritGbRenderer* h, int opt) {
 IFTR_API int iftrSetDepthWriteEnable(IfritGbRenderer* h, int enable) {
     if (!h) return IFTR_ERR_INVALID_ARG;
     h->depth_write = enable != 0;
+    return IFTR_OK;
+}
+
+IFTR_API int iftrDrawBatch(IfritGbRenderer* h, const IfritGbBatchView* views, int numViews, const IfritGbBatchDraw* draws,
+                           int numDraws) {
+    if (!h) return IFTR_ERR_INVALID_ARG;
+    if (h->in_pass) return IFTR_ERR_STATE;
+    int rc = validate_batch(views, numViews, draws, numDraws);
+    if (rc) return rc;
+    rc = ensure_init(h);
+    if (rc) return rc;
+    BatchState& b = h->batch;
+    std::vector<uint8_t> key = batch_key(b, views, numViews, draws, numDraws);
+    if (!(b.exec && b.captured_generation == b.scratch.generation && key == b.key)) {
+        rc = prepare_batch(h, views, numViews, draws, numDraws);
+        if (rc) {
+            b.drop_graph();
+            return rc;
+        }
+        b.key = std::move(key);
+    }
+    IFTR_CUDA(h, cudaGraphLaunch(b.exec, h->stream));
+    h->pending_batch = 1;
+    return IFTR_OK;
+}
+
+IFTR_API int iftrSetBatchTuning(IfritGbRenderer* h, int autotune, int tileSize, int ctasPerSm) {
+    if (!h || (tileSize != 8 && tileSize != 16) || ctasPerSm < -8 || ctasPerSm > 64) return IFTR_ERR_INVALID_ARG;
+    h->batch.autotune = autotune != 0;
+    h->batch.tile_size = tileSize;
+    h->batch.ctas_per_sm = ctasPerSm;
+    return IFTR_OK;
+}
+
+IFTR_API int iftrGetBatchTuning(IfritGbRenderer* h, int* tileSize, int* ctasPerSm) {
+    if (!h) return IFTR_ERR_INVALID_ARG;
+    if (tileSize) *tileSize = h->batch.tuned_tile;
+    if (ctasPerSm) *ctasPerSm = h->batch.tuned_ctas;
     return IFTR_OK;
 }
 
@@ -846,7 +1288,7 @@ IFTR_API int iftrSetVisibilityOutput(IfritGbRenderer* h, int enable) {
 IFTR_API int iftrReserve(IfritGbRenderer* h, size_t pairs) {
     if (!h) return IFTR_ERR_INVALID_ARG;
     int rc = ensure_init(h);
-    return rc ? rc : ensure_pairs(h, pairs);
+    return rc ? rc : ensure_pairs(h, h->pass, pairs);
 }
 
 IFTR_API int iftrGetDeviceAttachments(IfritGbRenderer* h, void** color, float** depth, int** vis) {

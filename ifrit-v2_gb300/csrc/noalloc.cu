@@ -17,6 +17,7 @@
 #include <mutex>
 
 #include "../../include/ifrit_gb300.h"
+#include "pass_plan.h"
 #include "raster_kernels.cuh"
 
 namespace {
@@ -26,7 +27,10 @@ constexpr size_t align256(size_t x) { return (x + 255) / 256 * 256; }
 constexpr size_t kOffStatus = 0;
 constexpr size_t kOffDraw = kOffStatus + align256(ifr::ST_WORDS * sizeof(uint32_t));
 constexpr size_t kOffDrawStart = kOffDraw + align256(sizeof(ifr::DrawDev));
-constexpr size_t kOffTileCount = kOffDrawStart + align256(2 * sizeof(int));
+constexpr size_t kOffView = kOffDrawStart + align256(2 * sizeof(int));
+constexpr size_t kOffViewTiles = kOffView + align256(sizeof(ifr::ViewArgs));
+constexpr size_t kOffQueues = kOffViewTiles + align256(2 * sizeof(int));
+constexpr size_t kOffTileCount = kOffQueues + align256(2 * ifr::kMaxGroups * sizeof(uint32_t));
 constexpr size_t kOffTileOffset = kOffTileCount + align256((size_t)IFTR_NOALLOC_MAX_TILES * 4);
 constexpr size_t kOffTileCursor = kOffTileOffset + align256((size_t)(IFTR_NOALLOC_MAX_TILES + 1) * 4);
 constexpr size_t kOffPairs = kOffTileCursor + align256((size_t)IFTR_NOALLOC_MAX_TILES * 4);
@@ -59,17 +63,6 @@ cudaError_t scratch_address(unsigned char** out) {
     return cudaSuccess;
 }
 
-void sample_pattern(int S, int* xs, int* ys) {
-    static const int P1[2] = {128, 128};
-    static const int P2[4] = {192, 192, 64, 64};
-    static const int P4[8] = {96, 32, 224, 96, 32, 160, 160, 224};
-    static const int P8[16] = {144, 80, 112, 176, 208, 144, 80, 48, 48, 208, 16, 112, 176, 240, 240, 16};
-    static const int P16[32] = {144, 144, 112, 80, 80, 160, 192, 112, 48, 96, 160, 208, 208, 176, 176, 48,
-                                96, 224, 128, 16, 64, 32, 32, 192, 0, 128, 240, 64, 224, 240, 16, 0};
-    const int* t = S == 1 ? P1 : S == 2 ? P2 : S == 4 ? P4 : S == 8 ? P8 : P16;
-    for (int k = 0; k < S; k++) { xs[k] = t[2 * k]; ys[k] = t[2 * k + 1]; }
-}
-
 }  // namespace
 
 extern "C" IFTR_API int iftrDrawNoAlloc(const IfritGbNoAllocPass* p, void* cudaStream) {
@@ -77,13 +70,14 @@ extern "C" IFTR_API int iftrDrawNoAlloc(const IfritGbNoAllocPass* p, void* cudaS
     const int S = p->samples;
     if (!(S == 1 || S == 2 || S == 4 || S == 8 || S == 16)) return IFTR_ERR_INVALID_ARG;
     if (p->width <= 0 || p->height <= 0 || p->numIndices < 0 || p->numIndices % 3 != 0) return IFTR_ERR_INVALID_ARG;
-    const int tiles_x = (p->width + ifr::kTileSize - 1) / ifr::kTileSize;
-    const int tiles_y = (p->height + ifr::kTileSize - 1) / ifr::kTileSize;
-    const size_t T = (size_t)tiles_x * tiles_y;
+    const size_t T = (size_t)ifr::tiles_of(p->width, p->height, 16);
     if ((size_t)p->numIndices / 3 > IFTR_NOALLOC_MAX_TRIANGLES || T > IFTR_NOALLOC_MAX_TILES ||
         (size_t)p->width * p->height * S > IFTR_NOALLOC_MAX_SAMPLES)
         return IFTR_ERR_INVALID_ARG;
     if (!p->color || !p->depth || (p->numIndices > 0 && (!p->vertices || !p->indices))) return IFTR_ERR_INVALID_ARG;
+    if (!ifr::targets_aligned(p->color, p->colorFormat, p->depth, p->visibility, S) || (uintptr_t)p->vertices % 4 ||
+        (uintptr_t)p->indices % 4 || (uintptr_t)p->texels % 4)
+        return IFTR_ERR_INVALID_ARG;
     if (p->colorFormat < 0 || p->colorFormat > 3 || p->shadingModel < 0 || p->shadingModel > 2) return IFTR_ERR_INVALID_ARG;
     if (p->strideFloats < 3 || p->attrCount < 0 || p->attrCount > 4 || p->attrOffsetFloats + p->attrCount > p->strideFloats)
         return IFTR_ERR_INVALID_ARG;
@@ -114,63 +108,39 @@ extern "C" IFTR_API int iftrDrawNoAlloc(const IfritGbNoAllocPass* p, void* cudaS
     d.depth_func = func;
     d.depth_write = p->depthWrite != 0;
     d.shading = p->shadingModel;
-    d.texels = p->texels;
-    d.tex_w = p->texWidth;
-    d.tex_h = p->texHeight;
-    d.tex_levels = p->texLevels;
-    d.sampler.address_u = p->sampler.addressModeU;
-    d.sampler.address_v = p->sampler.addressModeV;
-    d.sampler.filter = p->sampler.filterMode;
-    d.sampler.border_white = p->sampler.borderColor;
-    d.sampler.max_aniso = p->sampler.anisotropyEnable ? (p->sampler.maxAnisotropy >= 1.0f ? (int)p->sampler.maxAnisotropy : 1) : 1;
-    d.sampler.lod_bias = p->sampler.lodBias;
-    int w = p->texWidth, h = p->texHeight, off = 0;
-    for (int l = 0; l < 16; l++) {
-        d.lvl_off[l] = off;
-        d.lvl_w[l] = w;
-        d.lvl_h[l] = h;
-        off += w * h;
-        w = w > 1 ? (w + 1) >> 1 : 1;
-        h = h > 1 ? (h + 1) >> 1 : 1;
-    }
+    if (p->shadingModel == IFTR_FS_TEXTURED) ifr::fill_texture(d, p->texels, p->texWidth, p->texHeight, p->texLevels, p->sampler);
     const int draw_start[2] = {0, d.num_triangles};
+
+    ifr::ViewArgs v;
+    std::memset(&v, 0, sizeof(v));
+    ifr::fill_pass_const(v.c, p->width, p->height, S, 16);
+    v.format = p->colorFormat;
+    v.color = p->color;
+    v.depth = p->depth;
+    v.vis = p->visibility;
+    v.entries = reinterpret_cast<int*>(base + kOffEntries);
+    v.clear = p->clear != 0;
+    std::memcpy(v.clear_color, p->clearColor, sizeof(v.clear_color));
+    v.clear_depth = p->clearDepth;
+    ifr::set_view_depth_state(v, &d, 1);
+    int view_tiles[2] = {0, 0};
+    ifr::LaunchPlan plan;
+    int total_tiles = 0;
+    int dev = 0, sms = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+        return IFTR_ERR_CUDA;
+    if (!ifr::plan_groups(&v, 1, view_tiles, sms, 0, plan, total_tiles)) return IFTR_ERR_INVALID_ARG;
 
     ifr::PassArgs a;
     std::memset(&a, 0, sizeof(a));
-    a.c.W = p->width;
-    a.c.H = p->height;
-    a.c.S = S;
-    a.c.tiles_x = tiles_x;
-    a.c.tiles_y = tiles_y;
-    sample_pattern(S, a.c.sx, a.c.sy);
-    a.c.smin_x = a.c.smax_x = a.c.sx[0];
-    a.c.smin_y = a.c.smax_y = a.c.sy[0];
-    for (int k = 1; k < S; k++) {
-        a.c.smin_x = a.c.sx[k] < a.c.smin_x ? a.c.sx[k] : a.c.smin_x;
-        a.c.smax_x = a.c.sx[k] > a.c.smax_x ? a.c.sx[k] : a.c.smax_x;
-        a.c.smin_y = a.c.sy[k] < a.c.smin_y ? a.c.sy[k] : a.c.smin_y;
-        a.c.smax_y = a.c.sy[k] > a.c.smax_y ? a.c.sy[k] : a.c.smax_y;
-    }
-    a.c.shade_x = 128;
-    a.c.shade_y = 128;
-    a.c.W256 = (float)p->width * 256.0f;
-    a.c.H256 = (float)p->height * 256.0f;
-    a.c.gx = (float)(1.0 + 2.0 * 8192.0 / (double)p->width);
-    a.c.gy = (float)(1.0 + 2.0 * 8192.0 / (double)p->height);
     a.draws = reinterpret_cast<const ifr::DrawDev*>(base + kOffDraw);
     a.draw_start = reinterpret_cast<const int*>(base + kOffDrawStart);
     a.ndraws = 1;
     a.total_tris = d.num_triangles;
-    a.format = p->colorFormat;
-    a.color = p->color;
-    a.depth = p->depth;
-    a.vis = p->visibility;
-    a.entries = reinterpret_cast<int*>(base + kOffEntries);
-    a.clear = p->clear != 0;
-    std::memcpy(a.clear_color, p->clearColor, sizeof(a.clear_color));
-    a.clear_depth = p->clearDepth;
-    a.depth_func = func;
-    a.depth_write = d.depth_write;
+    a.views = reinterpret_cast<const ifr::ViewArgs*>(base + kOffView);
+    a.view_tile_start = reinterpret_cast<const int*>(base + kOffViewTiles);
+    a.nviews = 1;
+    a.total_tiles = total_tiles;
     a.tile_count = reinterpret_cast<uint32_t*>(base + kOffTileCount);
     a.tile_offset = reinterpret_cast<uint32_t*>(base + kOffTileOffset);
     a.tile_cursor = reinterpret_cast<uint32_t*>(base + kOffTileCursor);
@@ -178,15 +148,18 @@ extern "C" IFTR_API int iftrDrawNoAlloc(const IfritGbNoAllocPass* p, void* cudaS
     a.pair_capacity = IFTR_NOALLOC_MAX_TILE_PAIRS;
     a.records = reinterpret_cast<ifr::TriRecord*>(base + kOffRecords);
     a.status = reinterpret_cast<uint32_t*>(base + kOffStatus);
+    a.queues = reinterpret_cast<uint32_t*>(base + kOffQueues);
 
     // zero what the pass expects to start at zero (status words and per-tile counts)
     if (cudaMemsetAsync(base + kOffStatus, 0, ifr::ST_WORDS * sizeof(uint32_t), stream) != cudaSuccess ||
         cudaMemsetAsync(base + kOffTileCount, 0, T * 4, stream) != cudaSuccess ||
         cudaMemcpyAsync(base + kOffDraw, &d, sizeof(d), cudaMemcpyHostToDevice, stream) != cudaSuccess ||
-        cudaMemcpyAsync(base + kOffDrawStart, draw_start, sizeof(draw_start), cudaMemcpyHostToDevice, stream) != cudaSuccess)
+        cudaMemcpyAsync(base + kOffDrawStart, draw_start, sizeof(draw_start), cudaMemcpyHostToDevice, stream) != cudaSuccess ||
+        cudaMemcpyAsync(base + kOffView, &v, sizeof(v), cudaMemcpyHostToDevice, stream) != cudaSuccess ||
+        cudaMemcpyAsync(base + kOffViewTiles, view_tiles, sizeof(view_tiles), cudaMemcpyHostToDevice, stream) != cudaSuccess)
         return IFTR_ERR_CUDA;
-    if (ifr::launch_pass(a, stream, nullptr) != cudaSuccess) return IFTR_ERR_CUDA;
-    uint32_t status[ifr::ST_WORDS] = {0, 0, 0, 0};
+    if (ifr::launch_pass(a, plan, stream, nullptr) != cudaSuccess) return IFTR_ERR_CUDA;
+    uint32_t status[ifr::ST_WORDS] = {};
     if (cudaMemcpyAsync(status, base + kOffStatus, sizeof(status), cudaMemcpyDeviceToHost, stream) != cudaSuccess ||
         cudaStreamSynchronize(stream) != cudaSuccess)
         return IFTR_ERR_CUDA;

@@ -1,0 +1,152 @@
+// Host-side planning of a pass, shared by the renderer runtime (capi.cu) and the
+// allocation-free entry point (noalloc.cu): per-view constants, the tile ranges of the views
+// and the launch groups of the tile stages.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstring>
+
+#include "../../include/ifrit_gb300.h"
+#include "raster_kernels.cuh"
+
+namespace ifr {
+
+inline void fill_blend(DrawDev& d, const IfritGbBlendState& b) {
+    d.blend_enable = b.blendEnable != 0;
+    d.blend_src_color = b.srcColorBlendFactor;
+    d.blend_dst_color = b.dstColorBlendFactor;
+    d.blend_src_alpha = b.srcAlphaBlendFactor;
+    d.blend_dst_alpha = b.dstAlphaBlendFactor;
+}
+
+// Texture and sampler of a draw; the mip chain is stored level after level, each level
+// ((w + 1) >> 1) x ((h + 1) >> 1) of the previous one.
+inline void fill_texture(DrawDev& d, const uint32_t* texels, int w, int h, int levels, const IfritGbSampler& s) {
+    d.texels = texels;
+    d.tex_w = w;
+    d.tex_h = h;
+    d.tex_levels = levels;
+    d.sampler.address_u = s.addressModeU;
+    d.sampler.address_v = s.addressModeV;
+    d.sampler.filter = s.filterMode;
+    d.sampler.border_white = s.borderColor;
+    d.sampler.max_aniso = s.anisotropyEnable ? (s.maxAnisotropy >= 1.0f ? (int)s.maxAnisotropy : 1) : 1;
+    d.sampler.lod_bias = s.lodBias;
+    int off = 0;
+    for (int l = 0; l < 16; l++) {
+        d.lvl_off[l] = off;
+        d.lvl_w[l] = w;
+        d.lvl_h[l] = h;
+        off += w * h;
+        w = w > 1 ? (w + 1) >> 1 : 1;
+        h = h > 1 ? (h + 1) >> 1 : 1;
+    }
+}
+
+// Depth state and path of a view from its draws: the deferred path needs one depth function
+// and write mask for the whole view and no blending or NOT_EQUAL writes; anything else runs the
+// ordered path.
+inline void set_view_depth_state(ViewArgs& v, const DrawDev* draws, int n) {
+    v.depth_func = n > 0 ? draws[0].depth_func : IF_COMPARE_OP_LESS;
+    v.depth_write = n > 0 ? draws[0].depth_write : 1;
+    v.ordered = 0;
+    for (int i = 0; i < n; i++) {
+        const DrawDev& d = draws[i];
+        if (d.blend_enable || (d.depth_write && d.depth_func == IF_COMPARE_OP_NOT_EQUAL) || d.depth_func != v.depth_func ||
+            d.depth_write != v.depth_write)
+            v.ordered = 1;
+    }
+}
+
+inline bool valid_samples(int S) { return S == 1 || S == 2 || S == 4 || S == 8 || S == 16; }
+
+// Screen-tile edges the tile kernels are built for: 16 for every sample count, 8 for 1x and 4x
+// deferred views (the ordered path always runs 16x16 tiles).
+inline bool tile_size_supported(int S, int TS, bool ordered) {
+    if (TS == 16) return true;
+    return TS == 8 && !ordered && (S == 1 || S == 4);
+}
+
+inline int tiles_of(int W, int H, int TS) { return ((W + TS - 1) / TS) * ((H + TS - 1) / TS); }
+
+// Alignment the tile kernels' vector accesses need on a view's targets: 16-byte float4 depth
+// stores when the sample count is a multiple of 4, 8/16-byte colour stores for RGBA16F/RGBA32F.
+inline bool targets_aligned(const void* color, int fmt, const void* depth, const void* vis, int S) {
+    const uintptr_t ca = fmt == IFTR_FORMAT_RGBA32F ? 16 : fmt == IFTR_FORMAT_RGBA16F ? 8 : 4;
+    const uintptr_t da = S % 4 == 0 ? 16 : 4;
+    return (uintptr_t)color % ca == 0 && (uintptr_t)depth % da == 0 && (uintptr_t)vis % 4 == 0;
+}
+
+inline void fill_pass_const(PassConst& c, int W, int H, int S, int TS) {
+    std::memset(&c, 0, sizeof(c));
+    c.W = W;
+    c.H = H;
+    c.S = S;
+    c.tile_shift = TS == 8 ? 3 : 4;
+    c.tiles_x = (W + TS - 1) / TS;
+    c.tiles_y = (H + TS - 1) / TS;
+    c.smin_x = c.smax_x = sample_pos(S, 0, 0);
+    c.smin_y = c.smax_y = sample_pos(S, 0, 1);
+    for (int k = 1; k < S; k++) {
+        c.smin_x = std::min(c.smin_x, sample_pos(S, k, 0));
+        c.smax_x = std::max(c.smax_x, sample_pos(S, k, 0));
+        c.smin_y = std::min(c.smin_y, sample_pos(S, k, 1));
+        c.smax_y = std::max(c.smax_y, sample_pos(S, k, 1));
+    }
+    c.W256 = (float)W * 256.0f;
+    c.H256 = (float)H * 256.0f;
+    // guard band: clip space is clipped to +-(1 + 2 * 8192 / size) so snapped coordinates fit
+    c.gx = (float)(1.0 + 2.0 * 8192.0 / (double)W);
+    c.gy = (float)(1.0 + 2.0 * 8192.0 / (double)H);
+}
+
+// Launch-group key of a view: views of one group share the tile kernels' template arguments.
+inline int group_key(const ViewArgs& v) { return v.c.S * 4 + (v.ordered ? 2 : 0) + (v.c.tile_shift == 3 ? 1 : 0); }
+
+// Assigns each view its tile range and splits the views into launch groups of equal sample
+// count, path and tile size.  `v` must already be ordered so that each group is contiguous.
+// Persistent CTAs per SM: `ctas_per_sm` > 0 as given (at most the occupancy), 0 the kernels'
+// full occupancy, -k the full occupancy divided by k.  Returns false if the views need more
+// launch groups than a plan holds or a view's tile size is not built.
+inline bool plan_groups(ViewArgs* v, int n, int* view_tile_start, int sms, int ctas_per_sm, LaunchPlan& plan,
+                        int& total_tiles) {
+    std::memset(&plan, 0, sizeof(plan));
+    int t = 0;
+    for (int i = 0; i < n; i++) {
+        const int TS = 1 << v[i].c.tile_shift;
+        if (!tile_size_supported(v[i].c.S, TS, v[i].ordered != 0)) return false;
+        v[i].tile_start = t;
+        view_tile_start[i] = t;
+        t += v[i].c.tiles_x * v[i].c.tiles_y;
+        if (i == 0 || group_key(v[i]) != group_key(v[i - 1])) {
+            if (plan.ngroups == kMaxGroups) return false;
+            GroupArgs& g = plan.groups[plan.ngroups];
+            g.view_begin = i;
+            g.tile_begin = v[i].tile_start;
+            g.queue = plan.ngroups;
+            plan.samples[plan.ngroups] = v[i].c.S;
+            plan.tile_size[plan.ngroups] = TS;
+            plan.ordered[plan.ngroups] = v[i].ordered ? 1 : 0;
+            plan.ngroups++;
+        }
+        GroupArgs& g = plan.groups[plan.ngroups - 1];
+        g.view_end = i + 1;
+        g.tile_end = t;
+    }
+    view_tile_start[n] = t;
+    total_tiles = t;
+    for (int k = 0; k < plan.ngroups; k++) {
+        const int tiles = plan.groups[k].tile_end - plan.groups[k].tile_begin;
+        for (int stage = 0; stage < 2; stage++) {
+            const int occ = tile_kernel_occupancy(plan.samples[k], plan.tile_size[k], plan.ordered[k], stage);
+            const int per_sm = ctas_per_sm > 0 ? std::min(ctas_per_sm, occ)
+                               : ctas_per_sm < 0 ? std::max(1, occ / -ctas_per_sm)
+                                                 : occ;
+            (stage == 0 ? plan.ctas : plan.ctas_shade)[k] = std::max(1, std::min(tiles, sms * per_sm));
+        }
+    }
+    return true;
+}
+
+}  // namespace ifr

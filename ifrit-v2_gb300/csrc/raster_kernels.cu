@@ -1,22 +1,26 @@
-// sm_103a kernels of one render pass.
+// sm_103a kernels of one render pass (one or many views).
 //
-//   bin_kernel<false>   per triangle: fetch + transform + clip + set up, count (tile, triangle)
-//                       overlaps per 16x16 tile  (reference: first/second binners,
-//                       TileRasterCoreInvocationCuda.cu:721-1339, CPU executeBinner
-//                       TileRasterWorker.cpp:314-397)
+//   bin_count_kernel    per triangle: fetch + transform + clip + set up, count (tile, triangle)
+//                       overlaps per screen tile of the triangle's view (reference: first and
+//                       second binners, TileRasterCoreInvocationCuda.cu:721-1339; CPU
+//                       executeBinner TileRasterWorker.cpp:314-397); unclipped triangles
+//                       leave a compact 64-byte set-up record
 //   scan_kernel         exclusive scan of the per-tile counts -> list offsets; resets counts
-//   bin_kernel<true>    same front end, scatters (triangle, fan index) into the tile lists
-//   tile_kernel<S>      one CTA per tile, one thread per pixel holding S samples in
-//                       registers: coverage + early depth test for every listed triangle
-//                       (pixelTaggingExecKernel, .cu:1900-2142), then deferred shading of the
-//                       visible primitives with quad derivatives (pixelShadingExecKernel,
-//                       .cu:2144-2317), on-chip MSAA resolve (.cu:2319-2361), and one store of
-//                       depth / visibility / colour per pixel.
+//   bin_scatter_kernel  same overlaps (from the records), scatters entries into tile lists
+//   raster_kernel       persistent CTAs over a tile queue, one CTA per tile at a time: coverage
+//                       + early depth test of every listed triangle with order-independent
+//                       64-bit keys in shared memory (pixelTaggingExecKernel, .cu:1900-2142)
+//   shade_kernel        persistent CTAs: deferred shading of the visible primitives with quad
+//                       derivatives (pixelShadingExecKernel, .cu:2144-2317), on-chip MSAA
+//                       resolve (.cu:2319-2361), one store of depth / visibility / colour
+//   forward_kernel      ordered path: entries sorted into API order, per-sample depth test,
+//                       shading and blend in order (.cu:1648-1897, TileRasterWorker.cpp:1517-1580)
 //
-// Visibility is order independent: a sample keeps the primitive that wins under the pass's
-// depth function with ties broken by API order (earlier wins for LESS/GREATER, later for
-// LEQUAL/GEQUAL/EQUAL/ALWAYS), which is exactly what processing triangles in submission
-// order produces.  So the tile lists need no sorting and the result is deterministic.
+// Visibility in the deferred path is order independent: a sample keeps the primitive that
+// wins under the view's depth function with ties broken by API order (earlier wins for
+// LESS/GREATER, later for LEQUAL/GEQUAL/EQUAL/ALWAYS), which is exactly what processing
+// triangles in submission order produces.  So tile lists need no sorting there and the
+// result is deterministic.
 #include <cuda_runtime.h>
 #include <cuda_fp16.h>
 #include "raster_kernels.cuh"
@@ -32,12 +36,14 @@ __device__ __forceinline__ int find_draw(const PassArgs& a, int g) {
     return lo;
 }
 
-__device__ __forceinline__ void bin_sub(const PassArgs& a, const SubTri& s, uint32_t entry, bool scatter) {
-    int tx0 = s.px0 >> kTileShift, tx1 = s.px1 >> kTileShift;
-    int ty0 = s.py0 >> kTileShift, ty1 = s.py1 >> kTileShift;
+__device__ __forceinline__ void bin_sub(const PassArgs& a, const ViewArgs& v, const SubTri& s, uint32_t entry,
+                                        bool scatter) {
+    const int sh = v.c.tile_shift;
+    int tx0 = s.px0 >> sh, tx1 = s.px1 >> sh;
+    int ty0 = s.py0 >> sh, ty1 = s.py1 >> sh;
     for (int ty = ty0; ty <= ty1; ty++)
         for (int tx = tx0; tx <= tx1; tx++) {
-            int tile = ty * a.c.tiles_x + tx;
+            int tile = v.tile_start + ty * v.c.tiles_x + tx;
             if (scatter) {
                 uint32_t pos = atomicAdd(a.tile_cursor + tile, 1u);
                 if (pos < a.pair_capacity) a.pairs[pos] = entry;
@@ -53,17 +59,18 @@ __global__ void __launch_bounds__(256) bin_count_kernel(PassArgs a) {
     if (g >= a.total_tris) return;
     int di = find_draw(a, g);
     const DrawDev& d = a.draws[di];
+    const ViewArgs& v = a.views[d.view];
     int t = g - __ldg(a.draw_start + di);
     CVert poly[kMaxPoly];
     bool inside, rejected;
     TriRecord* rec = a.records + g;
-    if (!fetch_triangle(a.c, d, t, poly, inside, rejected)) {
+    if (!fetch_triangle(v.c, d, t, poly, inside, rejected)) {
         rec->flags = 0;
         return;
     }
     if (inside) {
         SubTri s;
-        if (!setup_sub(a.c, d, poly[0], poly[1], poly[2], s)) {
+        if (!setup_sub(v.c, d, poly[0], poly[1], poly[2], s)) {
             rec->flags = 0;
             return;
         }
@@ -72,14 +79,14 @@ __global__ void __launch_bounds__(256) bin_count_kernel(PassArgs a) {
         const int4* src = reinterpret_cast<const int4*>(&r);
         int4* dst = reinterpret_cast<int4*>(rec);
         dst[0] = src[0]; dst[1] = src[1]; dst[2] = src[2]; dst[3] = src[3];
-        bin_sub(a, s, (uint32_t)g << 3, false);
+        bin_sub(a, v, s, (uint32_t)g << 3, false);
         return;
     }
     rec->flags = REC_CLIPPED;
-    int n = clip_polygon(a.c, poly);
+    int n = clip_polygon(v.c, poly);
     for (int i = 1; i + 1 < n; i++) {
         SubTri s;
-        if (setup_sub(a.c, d, poly[0], poly[i], poly[i + 1], s)) bin_sub(a, s, ((uint32_t)g << 3) | (uint32_t)(i - 1), false);
+        if (setup_sub(v.c, d, poly[0], poly[i], poly[i + 1], s)) bin_sub(a, v, s, ((uint32_t)g << 3) | (uint32_t)(i - 1), false);
     }
 }
 
@@ -90,22 +97,23 @@ __global__ void __launch_bounds__(256) bin_scatter_kernel(PassArgs a) {
     if (g >= a.total_tris) return;
     if (a.status[ST_OVERFLOW]) return;
     const int flags = __ldg(&a.records[g].flags);
-    if (flags & REC_VALID) {
-        SubTri s;
-        if (sub_from_record(a.c, a.records + g, s)) bin_sub(a, s, (uint32_t)g << 3, true);
-        return;
-    }
-    if (!(flags & REC_CLIPPED)) return;
+    if (!(flags & (REC_VALID | REC_CLIPPED))) return;
     int di = find_draw(a, g);
     const DrawDev& d = a.draws[di];
+    const ViewArgs& v = a.views[d.view];
+    if (flags & REC_VALID) {
+        SubTri s;
+        if (sub_from_record(v.c, a.records + g, s)) bin_sub(a, v, s, (uint32_t)g << 3, true);
+        return;
+    }
     int t = g - __ldg(a.draw_start + di);
     CVert poly[kMaxPoly];
     bool inside, rejected;
-    if (!fetch_triangle(a.c, d, t, poly, inside, rejected)) return;
-    int n = clip_polygon(a.c, poly);
+    if (!fetch_triangle(v.c, d, t, poly, inside, rejected)) return;
+    int n = clip_polygon(v.c, poly);
     for (int i = 1; i + 1 < n; i++) {
         SubTri s;
-        if (setup_sub(a.c, d, poly[0], poly[i], poly[i + 1], s)) bin_sub(a, s, ((uint32_t)g << 3) | (uint32_t)(i - 1), true);
+        if (setup_sub(v.c, d, poly[0], poly[i], poly[i + 1], s)) bin_sub(a, v, s, ((uint32_t)g << 3) | (uint32_t)(i - 1), true);
     }
 }
 
@@ -135,78 +143,80 @@ __global__ void __launch_bounds__(1024) scan_kernel(PassArgs a, int T) {
     if (tid == 1023) {
         a.tile_offset[T] = part[1023];
         a.status[ST_PAIRS] = part[1023];
-        if (part[1023] > a.pair_capacity) a.status[ST_OVERFLOW] = 1u;
+        atomicMax(a.status + ST_MAX_PAIRS, part[1023]);
+        if (part[1023] > a.pair_capacity) {
+            a.status[ST_OVERFLOW] = 1u;
+            atomicOr(a.status + ST_STICKY, 1u);
+        }
     }
 }
 
 // Initial depth of sample k of pixel (x, y) for the explicit-compare key modes.
-__device__ __forceinline__ float d0_of(const PassArgs& a, int x, int y, int k) {
-    return a.clear ? a.clear_depth : a.depth[((size_t)y * a.c.W + x) * a.c.S + k];
+__device__ __forceinline__ float d0_of(const ViewArgs& v, int x, int y, int k) {
+    return v.clear ? v.clear_depth : v.depth[((size_t)y * v.c.W + x) * v.c.S + k];
 }
 
-__device__ __forceinline__ void decode_color(const PassArgs& a, size_t pix, float c[4]) {
-    switch (a.format) {
-    case FMT_RGBA8: unpack_rgba8(static_cast<const uint32_t*>(a.color)[pix], c); break;
+__device__ __forceinline__ void decode_color(const ViewArgs& v, size_t pix, float c[4]) {
+    switch (v.format) {
+    case FMT_RGBA8: unpack_rgba8(static_cast<const uint32_t*>(v.color)[pix], c); break;
     case FMT_RGBA16F: {
-        uint2 v = static_cast<const uint2*>(a.color)[pix];
-        c[0] = __half2float(__ushort_as_half((unsigned short)(v.x & 0xffffu)));
-        c[1] = __half2float(__ushort_as_half((unsigned short)(v.x >> 16)));
-        c[2] = __half2float(__ushort_as_half((unsigned short)(v.y & 0xffffu)));
-        c[3] = __half2float(__ushort_as_half((unsigned short)(v.y >> 16)));
+        uint2 q = static_cast<const uint2*>(v.color)[pix];
+        c[0] = __half2float(__ushort_as_half((unsigned short)(q.x & 0xffffu)));
+        c[1] = __half2float(__ushort_as_half((unsigned short)(q.x >> 16)));
+        c[2] = __half2float(__ushort_as_half((unsigned short)(q.y & 0xffffu)));
+        c[3] = __half2float(__ushort_as_half((unsigned short)(q.y >> 16)));
         break;
     }
     case FMT_RGBA32F: {
-        float4 v = static_cast<const float4*>(a.color)[pix];
-        c[0] = v.x; c[1] = v.y; c[2] = v.z; c[3] = v.w;
+        float4 q = static_cast<const float4*>(v.color)[pix];
+        c[0] = q.x; c[1] = q.y; c[2] = q.z; c[3] = q.w;
         break;
     }
     default: {
-        const float* p = static_cast<const float*>(a.color) + pix * 3;
+        const float* p = static_cast<const float*>(v.color) + pix * 3;
         c[0] = p[0]; c[1] = p[1]; c[2] = p[2]; c[3] = 1.0f;
         break;
     }
     }
 }
 
-__device__ __forceinline__ void encode_color(const PassArgs& a, size_t pix, const float c[4]) {
-    switch (a.format) {
+__device__ __forceinline__ void encode_color(const ViewArgs& v, size_t pix, const float c[4]) {
+    switch (v.format) {
     case FMT_RGBA8: {
-        uint32_t v = 0;
+        uint32_t q = 0;
 #pragma unroll
         for (int i = 0; i < 4; i++) {
             float x = fminf(fmaxf(c[i], 0.0f), 1.0f);
-            v |= __float2uint_rn(x * 255.0f) << (8 * i);
+            q |= __float2uint_rn(x * 255.0f) << (8 * i);
         }
-        static_cast<uint32_t*>(a.color)[pix] = v;
+        static_cast<uint32_t*>(v.color)[pix] = q;
         break;
     }
     case FMT_RGBA16F: {
-        uint2 v;
-        v.x = (uint32_t)__half_as_ushort(__float2half_rn(c[0])) | ((uint32_t)__half_as_ushort(__float2half_rn(c[1])) << 16);
-        v.y = (uint32_t)__half_as_ushort(__float2half_rn(c[2])) | ((uint32_t)__half_as_ushort(__float2half_rn(c[3])) << 16);
-        static_cast<uint2*>(a.color)[pix] = v;
+        uint2 q;
+        q.x = (uint32_t)__half_as_ushort(__float2half_rn(c[0])) | ((uint32_t)__half_as_ushort(__float2half_rn(c[1])) << 16);
+        q.y = (uint32_t)__half_as_ushort(__float2half_rn(c[2])) | ((uint32_t)__half_as_ushort(__float2half_rn(c[3])) << 16);
+        static_cast<uint2*>(v.color)[pix] = q;
         break;
     }
-    case FMT_RGBA32F: static_cast<float4*>(a.color)[pix] = make_float4(c[0], c[1], c[2], c[3]); break;
+    case FMT_RGBA32F: static_cast<float4*>(v.color)[pix] = make_float4(c[0], c[1], c[2], c[3]); break;
     default: {
-        float* p = static_cast<float*>(a.color) + pix * 3;
+        float* p = static_cast<float*>(v.color) + pix * 3;
         p[0] = c[0]; p[1] = c[1]; p[2] = c[2];
         break;
     }
     }
 }
 
-// ---------------------------------------------------------------------------- tile kernel
-// Visibility keys.  Every sample holds one 64-bit key in shared memory; a fragment that
-// passes the depth test lowers it with atomicMin, so the final key is the same whatever the
-// order fragments arrive in:
+// ---------------------------------------------------------------------------- visibility keys
+// Every sample holds one 64-bit key in shared memory; a fragment that passes the depth test
+// lowers it with atomicMin, so the final key is the same whatever the order fragments arrive in:
 //   high word: depth order  (LESS/LEQUAL: z ascending, GREATER/GEQUAL: descending; 0 for the
 //              functions whose pass test is an explicit compare against the initial depth)
 //   low word:  entry order  (entry = global triangle << 3 | fan index; "earliest wins" modes
 //              store entry + 1 with the background at 0, "latest wins" modes store
 //              0xFFFFFFFE - entry with the background at 0xFFFFFFFF)
-// Ties therefore resolve exactly as submission-order processing does: LESS/GREATER keep the
-// earlier primitive, LEQUAL/GEQUAL/EQUAL/ALWAYS (and any test without depth writes) the later.
+// Ties therefore resolve exactly as submission-order processing does.
 enum KeyMode { KM_EARLIEST = 0, KM_LATEST = 1 };
 
 __device__ __forceinline__ uint32_t depth_order(float z) {
@@ -251,18 +261,12 @@ struct RecordPlane {
     int32_t X0, Y0;
 };
 
-__device__ __forceinline__ void shade_entry_geom(const PassArgs& a, int e, const ShadeGeom& g, int px, int py, float* col) {
-    int gi = e >> 3, sub = e & 7;
-    int di = find_draw(a, gi);
-    shade_fragment(a.c, a.draws[di], g, gi - __ldg(a.draw_start + di), sub, px, py, col);
-}
-
 // Set-up of entry e (global triangle << 3 | fan index) for shading: geometry + depth plane.
-__device__ __noinline__ void setup_entry(const PassArgs& a, int e, ShadeGeom* g, RecordPlane* pl) {
+__device__ __noinline__ void setup_entry(const PassArgs& a, const PassConst& c, int e, ShadeGeom* g, RecordPlane* pl) {
     int gi = e >> 3, sub = e & 7;
     int di = find_draw(a, gi);
     SubTri s;
-    setup_entry_sub(a.c, a.draws[di], a.records, gi, gi - __ldg(a.draw_start + di), sub, s);
+    setup_entry_sub(c, a.draws[di], a.records, gi, gi - __ldg(a.draw_start + di), sub, s);
     shade_geom_from(s, *g);
     pl->z0 = s.z[0];
     pl->dzdx = s.dzdx;
@@ -272,71 +276,118 @@ __device__ __noinline__ void setup_entry(const PassArgs& a, int e, ShadeGeom* g,
 }
 
 // Raster set-up of entry e for the batch phase (out of line: one copy of the clip path).
-__device__ __noinline__ bool setup_raster_entry(const PassArgs& a, uint32_t e, SubTri* s) {
+__device__ __noinline__ bool setup_raster_entry(const PassArgs& a, const PassConst& c, uint32_t e, SubTri* s, int* draw) {
     int g = (int)(e >> 3), sub = (int)(e & 7u);
     int di = find_draw(a, g);
-    return setup_entry_sub(a.c, a.draws[di], a.records, g, g - __ldg(a.draw_start + di), sub, *s);
+    *draw = di;
+    return setup_entry_sub(c, a.draws[di], a.records, g, g - __ldg(a.draw_start + di), sub, *s);
 }
 
-// Set-up and shading of an entry that did not fit the tile's set-up cache (rare; out of line).
-__device__ __noinline__ void shade_uncached(const PassArgs& a, int e, int px, int py, float* col, RecordPlane* pl) {
+// Set-up and shading of one entry at one pixel (out of line: the rare paths share one copy).
+__device__ __noinline__ void shade_uncached(const PassArgs& a, const PassConst& c, int e, int px, int py, float* col,
+                                            RecordPlane* pl) {
     ShadeGeom g;
-    setup_entry(a, e, &g, pl);
-    shade_entry_geom(a, e, g, px, py, col);
+    setup_entry(a, c, e, &g, pl);
+    int gi = e >> 3, sub = e & 7;
+    int di = find_draw(a, gi);
+    shade_fragment(c, a.draws[di], g, gi - __ldg(a.draw_start + di), sub, px, py, col);
 }
 
+// ---------------------------------------------------------------------------- persistent tiles
+// Pulls the next tile of the group from its queue and stages its view's arguments in shared
+// memory (the copy is skipped when the view did not change).  Returns false when the queue is
+// empty.  Must be called by the whole CTA.
+template <int NT>
+__device__ __forceinline__ bool next_tile(const PassArgs& a, const GroupArgs& g, int qslot, ViewArgs& sv, int& s_tile,
+                                          int& s_view) {
+    const int tid = threadIdx.x;
+    __syncthreads();  // everyone is done with the previous tile's staged data
+    if (tid == 0) {
+        int t = g.tile_begin + (int)atomicAdd(a.queues + qslot, 1u);
+        int vi = -1;
+        if (t < g.tile_end) {
+            int lo = g.view_begin, hi = g.view_end - 1;
+            while (lo < hi) {
+                int mid = (lo + hi + 1) >> 1;
+                if (__ldg(a.view_tile_start + mid) <= t) lo = mid; else hi = mid - 1;
+            }
+            vi = lo;
+        }
+        s_tile = t;
+        if (vi != s_view) s_view = vi | 0x40000000;  // mark: copy needed
+    }
+    __syncthreads();
+    if (s_tile >= g.tile_end) return false;
+    if (s_view & 0x40000000) {
+        const int vi = s_view & 0x3fffffff;
+        const int* src = reinterpret_cast<const int*>(a.views + vi);
+        int* dst = reinterpret_cast<int*>(&sv);
+        for (int i = tid; i < (int)(sizeof(ViewArgs) / 4); i += NT) dst[i] = src[i];
+        __syncthreads();
+        if (tid == 0) s_view = vi;
+        __syncthreads();
+    }
+    return true;
+}
+
+// Pixel of lane `tid` in a TS x TS tile: 2x2 quads on consecutive lanes, quads row-major.
+template <int TS>
+__device__ __forceinline__ void tile_pixel(int tid, int& lx, int& ly) {
+    constexpr int QR = TS / 2;
+    lx = ((tid >> 2) % QR) * 2 + (tid & 1);
+    ly = ((tid >> 2) / QR) * 2 + ((tid >> 1) & 1);
+}
+
+// ---------------------------------------------------------------------------- raster stage
+template <int NT>
 struct TileRecords {
-    int32_t A[3][kTileThreads], B[3][kTileThreads];
-    long long Cb[3][kTileThreads];
-    float z0[kTileThreads], dzdx[kTileThreads], dzdy[kTileThreads];
-    int32_t X0[kTileThreads], Y0[kTileThreads];
-    int32_t org[kTileThreads];    // tile-local x0 | y0 << 8 of the clipped bbox
-    int32_t width[kTileThreads];  // clipped bbox width in pixels
-    float rwidth[kTileThreads];   // 1 / width
-    int32_t key[kTileThreads];    // entry
-    uint32_t start[kTileThreads + 1];  // exclusive prefix of pixel counts
+    int32_t A[3][NT], B[3][NT];
+    long long Cb[3][NT];
+    float z0[NT], dzdx[NT], dzdy[NT];
+    int32_t X0[NT], Y0[NT];
+    int32_t org[NT];    // tile-local x0 | y0 << 8 of the clipped bbox
+    int32_t width[NT];  // clipped bbox width in pixels
+    float rwidth[NT];   // 1 / width
+    int32_t key[NT];    // entry
+    uint32_t start[NT + 1];  // exclusive prefix of pixel counts
 };
 
-
-// Raster stage: one CTA per 16x16 tile.  The tile's list is consumed in batches of up to 256
-// set-ups; every (triangle, pixel) pair of a batch is spread over the CTA, and each covered
-// sample that passes the depth test lowers its key.  The winning entry of every sample
-// (or -1) is written for the shading stage.
-template <int S>
-__global__ void __launch_bounds__(kTileThreads) raster_kernel(PassArgs a) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    TileRecords& rec = *reinterpret_cast<TileRecords*>(smem_raw);
-    unsigned long long* skey = reinterpret_cast<unsigned long long*>(smem_raw + sizeof(TileRecords));
-    __shared__ uint32_t warp_sum[kTileThreads / 32];
-
-    const int tile = blockIdx.x;
-    const int tx = tile % a.c.tiles_x, ty = tile / a.c.tiles_x;
-    const int tx0 = tx * kTileSize, ty0 = ty * kTileSize;
+// One tile: the tile's list is consumed in batches of up to NT set-ups; every (triangle, pixel)
+// pair of a batch is spread over the CTA, and each covered sample that passes the depth test
+// lowers its key.  The winning entry of every sample (or -1) is written for the shading stage.
+template <int S, int TS>
+__device__ __forceinline__ void raster_tile(const PassArgs& a, const ViewArgs& v, int gtile, TileRecords<TS * TS>& rec,
+                                            unsigned long long* skey, uint32_t* warp_sum) {
+    constexpr int NT = TS * TS;
+    const int ltile = gtile - v.tile_start;
+    const int tx = ltile % v.c.tiles_x, ty = ltile / v.c.tiles_x;
+    const int tx0 = tx * TS, ty0 = ty * TS;
     const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
-    const int lx = ((tid >> 2) & 7) * 2 + (tid & 1);
-    const int ly = (tid >> 5) * 2 + ((tid >> 1) & 1);
+    int lx, ly;
+    tile_pixel<TS>(tid, lx, ly);
     const int px = tx0 + lx, py = ty0 + ly;
-    const bool inpix = px < a.c.W && py < a.c.H;
-    const size_t pix = (size_t)py * a.c.W + px;
-    const KeyRule rule = key_rule(a.depth_func, a.depth_write);
+    const bool inpix = px < v.c.W && py < v.c.H;
+    const size_t pix = (size_t)py * v.c.W + px;
+    const KeyRule rule = key_rule(v.depth_func, v.depth_write);
 
 #pragma unroll
     for (int k = 0; k < S; k++) {
-        float d0 = a.clear ? a.clear_depth : (inpix ? a.depth[pix * S + k] : 0.0f);
-        skey[(ly * kTileSize + lx) * S + k] = background_key(rule, d0);
+        float d0 = v.clear ? v.clear_depth : (inpix ? v.depth[pix * S + k] : 0.0f);
+        skey[(ly * TS + lx) * S + k] = background_key(rule, d0);
     }
     const bool has_list = a.total_tris > 0 && a.status[ST_OVERFLOW] == 0 && rule.func != 0;
-    const uint32_t beg = has_list ? a.tile_offset[tile] : 0u;
-    const uint32_t end = has_list ? a.tile_offset[tile + 1] : 0u;
-    const int xmax = min(a.c.W, tx0 + kTileSize) - 1, ymax = min(a.c.H, ty0 + kTileSize) - 1;
+    const uint32_t beg = has_list ? a.tile_offset[gtile] : 0u;
+    const uint32_t end = has_list ? a.tile_offset[gtile + 1] : 0u;
+    const int xmax = min(v.c.W, tx0 + TS) - 1, ymax = min(v.c.H, ty0 + TS) - 1;
 
-    for (uint32_t base = beg; base < end; base += kTileThreads) {
-        const int nb = (int)min((uint32_t)kTileThreads, end - base);
+    for (uint32_t base = beg; base < end; base += NT) {
+        const int nb = (int)min((uint32_t)NT, end - base);
         uint32_t cnt = 0;
         if (tid < nb) {
             uint32_t e = __ldg(a.pairs + base + tid);
             SubTri s;
-            if (setup_raster_entry(a, e, &s)) {
+            int di;
+            if (setup_raster_entry(a, v.c, e, &s, &di)) {
                 int x0 = max(s.px0, tx0), x1 = min(s.px1, xmax);
                 int y0 = max(s.py0, ty0), y1 = min(s.py1, ymax);
                 if (x0 <= x1 && y0 <= y1) {
@@ -364,22 +415,22 @@ __global__ void __launch_bounds__(kTileThreads) raster_kernel(PassArgs a) {
         uint32_t incl = cnt;
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
-            uint32_t v = __shfl_up_sync(0xffffffffu, incl, o);
-            if (lane >= o) incl += v;
+            uint32_t q = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += q;
         }
         if (lane == 31) warp_sum[wid] = incl;
         __syncthreads();
         uint32_t wbase = 0, total = 0;
 #pragma unroll
-        for (int w = 0; w < kTileThreads / 32; w++) {
-            uint32_t v = warp_sum[w];
-            if (w < wid) wbase += v;
-            total += v;
+        for (int w = 0; w < NT / 32; w++) {
+            uint32_t q = warp_sum[w];
+            if (w < wid) wbase += q;
+            total += q;
         }
         rec.start[tid] = wbase + incl - cnt;
-        if (tid == 0) rec.start[kTileThreads] = total;
+        if (tid == 0) rec.start[NT] = total;
         __syncthreads();
-        for (uint32_t p = tid; p < total; p += kTileThreads) {
+        for (uint32_t p = tid; p < total; p += NT) {
             int lo = 0, hi = nb - 1;
             while (lo < hi) {  // last record with start <= p
                 int mid = (lo + hi + 1) >> 1;
@@ -400,18 +451,18 @@ __global__ void __launch_bounds__(kTileThreads) raster_kernel(PassArgs a) {
             const int32_t X0 = rec.X0[r], Y0 = rec.Y0[r];
             const uint32_t e = (uint32_t)rec.key[r];
             const uint32_t lo_word = rule.mode == KM_EARLIEST ? e + 1u : 0xFFFFFFFEu - e;
-            unsigned long long* kp = skey + (qy * kTileSize + qx) * S;
+            unsigned long long* kp = skey + (qy * TS + qx) * S;
             // (float)(sx - X0) == fbx + sample offset exactly: every term is an integer below
             // 2^24 in magnitude (guard-band bound), so no conversion per sample is needed.
             const float fbx = (float)(gx * 256 - X0), fby = (float)(gy * 256 - Y0);
 #pragma unroll
             for (int k = 0; k < S; k++) {
-                const int32_t sx = gx * 256 + a.c.sx[k], sy = gy * 256 + a.c.sy[k];
+                const int32_t sx = gx * 256 + sample_x<S>(k), sy = gy * 256 + sample_y<S>(k);
                 if (!covered(A, B, Cb, sx, sy)) continue;
-                const float z = (z0 + gzx * (fbx + (float)a.c.sx[k])) + gzy * (fby + (float)a.c.sy[k]);
+                const float z = (z0 + gzx * (fbx + (float)sample_x<S>(k))) + gzy * (fby + (float)sample_y<S>(k));
                 uint32_t hi_word;
                 if (rule.explicit_) {
-                    if (!depth_cmp(rule.func, z, d0_of(a, gx, gy, k))) continue;
+                    if (!depth_cmp(rule.func, z, d0_of(v, gx, gy, k))) continue;
                     hi_word = 0u;
                 } else {
                     hi_word = rule.invert ? ~depth_order(z) : depth_order(z);
@@ -422,11 +473,12 @@ __global__ void __launch_bounds__(kTileThreads) raster_kernel(PassArgs a) {
         }
         __syncthreads();
     }
+    __syncthreads();
     if (!inpix) return;
     int out[S];
 #pragma unroll
-    for (int k = 0; k < S; k++) out[k] = key_entry(rule, skey[(ly * kTileSize + lx) * S + k]);
-    int* ep = a.entries + pix * S;
+    for (int k = 0; k < S; k++) out[k] = key_entry(rule, skey[(ly * TS + lx) * S + k]);
+    int* ep = v.entries + pix * S;
     if constexpr (S % 4 == 0) {
 #pragma unroll
         for (int k = 0; k < S; k += 4) reinterpret_cast<int4*>(ep)[k / 4] = make_int4(out[k], out[k + 1], out[k + 2], out[k + 3]);
@@ -436,37 +488,48 @@ __global__ void __launch_bounds__(kTileThreads) raster_kernel(PassArgs a) {
     }
 }
 
-// Shading stage: one CTA per tile, one thread per pixel.  Each pixel lists its distinct
-// visible entries in sample order; the warp shades list slot i of all its lanes together
-// (set-up straight from the binner's record, quad derivatives, texture filtering), then the
-// samples are resolved on chip and depth, visibility and the resolved colour stored once.
-template <int S>
-__global__ void __launch_bounds__(kTileThreads, 2) shade_kernel(PassArgs a) {
-    __shared__ DrawDev sdraw;
-    __shared__ float4 scol[4][kTileThreads];  // colours of each thread's (up to 4) distinct entries
+template <int S, int TS>
+size_t raster_smem_bytes() {
+    return sizeof(TileRecords<TS * TS>) + (size_t)TS * TS * S * sizeof(unsigned long long);
+}
 
-    const int tile = blockIdx.x;
-    const int tx = tile % a.c.tiles_x, ty = tile / a.c.tiles_x;
+template <int S, int TS>
+__global__ void __launch_bounds__(TS * TS) raster_kernel(PassArgs a, GroupArgs g) {
+    constexpr int NT = TS * TS;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    TileRecords<NT>& rec = *reinterpret_cast<TileRecords<NT>*>(smem_raw);
+    unsigned long long* skey = reinterpret_cast<unsigned long long*>(smem_raw + sizeof(TileRecords<NT>));
+    __shared__ uint32_t warp_sum[NT / 32];
+    __shared__ ViewArgs sv;
+    __shared__ int s_tile, s_view;
+    if (threadIdx.x == 0) s_view = -1;
+    while (next_tile<NT>(a, g, 2 * g.queue, sv, s_tile, s_view)) raster_tile<S, TS>(a, sv, s_tile, rec, skey, warp_sum);
+}
+
+// ---------------------------------------------------------------------------- shade stage
+// One tile, one thread per pixel.  Each pixel lists its distinct visible entries in sample
+// order; the warp shades list slot i of all its lanes together (set-up straight from the
+// binner's record, quad derivatives, texture filtering), then the samples are resolved on chip
+// and depth, visibility and the resolved colour stored once.
+template <int S, int TS>
+__device__ __forceinline__ void shade_tile(const PassArgs& a, const ViewArgs& v, int gtile, float4 (*scol)[TS * TS]) {
+    const int ltile = gtile - v.tile_start;
+    const int tx = ltile % v.c.tiles_x, ty = ltile / v.c.tiles_x;
     const int tid = threadIdx.x;
-    const int lx = ((tid >> 2) & 7) * 2 + (tid & 1);
-    const int ly = (tid >> 5) * 2 + ((tid >> 1) & 1);
-    const int px = tx * kTileSize + lx, py = ty * kTileSize + ly;
-    const bool inpix = px < a.c.W && py < a.c.H;
-    const size_t pix = (size_t)py * a.c.W + px;
-    const KeyRule rule = key_rule(a.depth_func, a.depth_write);
-    if (a.ndraws == 1) {  // stage the draw descriptor on chip (read by every shading step)
-        const int* src = reinterpret_cast<const int*>(a.draws);
-        int* dst = reinterpret_cast<int*>(&sdraw);
-        for (int i = tid; i < (int)(sizeof(DrawDev) / 4); i += kTileThreads) dst[i] = src[i];
-    }
+    int lx, ly;
+    tile_pixel<TS>(tid, lx, ly);
+    const int px = tx * TS + lx, py = ty * TS + ly;
+    const bool inpix = px < v.c.W && py < v.c.H;
+    const size_t pix = (size_t)py * v.c.W + px;
+    const KeyRule rule = key_rule(v.depth_func, v.depth_write);
     int ent[S];
     if (inpix) {
-        const int* ep = a.entries + pix * S;
+        const int* ep = v.entries + pix * S;
         if constexpr (S % 4 == 0) {
 #pragma unroll
             for (int k = 0; k < S; k += 4) {
-                int4 v = reinterpret_cast<const int4*>(ep)[k / 4];
-                ent[k] = v.x; ent[k + 1] = v.y; ent[k + 2] = v.z; ent[k + 3] = v.w;
+                int4 q = reinterpret_cast<const int4*>(ep)[k / 4];
+                ent[k] = q.x; ent[k + 1] = q.y; ent[k + 2] = q.z; ent[k + 3] = q.w;
             }
         } else {
 #pragma unroll
@@ -476,8 +539,6 @@ __global__ void __launch_bounds__(kTileThreads, 2) shade_kernel(PassArgs a) {
 #pragma unroll
         for (int k = 0; k < S; k++) ent[k] = -1;
     }
-    __syncthreads();
-    const DrawDev& d0 = a.ndraws == 1 ? sdraw : a.draws[0];
 
     // distinct visible entries of this pixel, in sample order; sample k uses list slot which[k]
     constexpr int U = S < 4 ? S : 4;  // slots shaded together across the warp
@@ -513,46 +574,47 @@ __global__ void __launch_bounds__(kTileThreads, 2) shade_kernel(PassArgs a) {
             if (j == i) e = uniq[j];
         if (i < nu) {
             const int g = e >> 3, sub = e & 7;
-            const int di = a.ndraws == 1 ? 0 : find_draw(a, g);
-            const DrawDev& d = a.ndraws == 1 ? d0 : a.draws[di];
-            const int t = g - (a.ndraws == 1 ? 0 : __ldg(a.draw_start + di));
+            const int di = find_draw(a, g);
+            const DrawDev& d = a.draws[di];
+            const int t = g - __ldg(a.draw_start + di);
             SubTri st;
-            setup_entry_sub(a.c, d, a.records, g, t, sub, st);
+            setup_entry_sub(v.c, d, a.records, g, t, sub, st);
             ShadeGeom geo;
             shade_geom_from(st, geo);
             float c[4];
-            shade_fragment(a.c, d, geo, t, sub, px, py, c);
+            shade_fragment(v.c, d, geo, t, sub, px, py, c);
             scol[i][tid] = make_float4(c[0], c[1], c[2], c[3]);
 #pragma unroll
             for (int k = 0; k < S; k++)
                 if (which[k] == i)
-                    dep[k] = sample_depth(st.z[0], st.dzdx, st.dzdy, st.X[0], st.Y[0], px * 256 + a.c.sx[k],
-                                          py * 256 + a.c.sy[k]);
+                    dep[k] = sample_depth(st.z[0], st.dzdx, st.dzdy, st.X[0], st.Y[0], px * 256 + sample_x<S>(k),
+                                          py * 256 + sample_y<S>(k));
         }
     }
     if (!inpix) return;
     float bg[4];
-    if (a.clear) {
-        bg[0] = a.clear_color[0]; bg[1] = a.clear_color[1]; bg[2] = a.clear_color[2]; bg[3] = a.clear_color[3];
+    if (v.clear) {
+        bg[0] = v.clear_color[0]; bg[1] = v.clear_color[1]; bg[2] = v.clear_color[2]; bg[3] = v.clear_color[3];
     } else {
-        decode_color(a, pix, bg);
+        decode_color(v, pix, bg);
     }
     float acc[4];
 #pragma unroll
     for (int k = 0; k < S; k++) {
         float c[4];
-        const float d0v = a.clear ? a.clear_depth : a.depth[pix * S + k];
+        const float d0v = v.clear ? v.clear_depth : v.depth[pix * S + k];
         if (which[k] < 0) {
             c[0] = bg[0]; c[1] = bg[1]; c[2] = bg[2]; c[3] = bg[3];
             dep[k] = d0v;
         } else {
             if (which[k] < U) {
-                float4 v = scol[which[k]][tid];
-                c[0] = v.x; c[1] = v.y; c[2] = v.z; c[3] = v.w;
+                float4 q = scol[which[k]][tid];
+                c[0] = q.x; c[1] = q.y; c[2] = q.z; c[3] = q.w;
             } else {  // more than U distinct primitives in one pixel: shade this one here
                 RecordPlane pl;
-                shade_uncached(a, ent[k], px, py, c, &pl);
-                dep[k] = sample_depth(pl.z0, pl.dzdx, pl.dzdy, pl.X0, pl.Y0, px * 256 + a.c.sx[k], py * 256 + a.c.sy[k]);
+                shade_uncached(a, v.c, ent[k], px, py, c, &pl);
+                dep[k] = sample_depth(pl.z0, pl.dzdx, pl.dzdy, pl.X0, pl.Y0, px * 256 + sample_x<S>(k),
+                                      py * 256 + sample_y<S>(k));
             }
             if (!rule.write) dep[k] = d0v;
         }
@@ -564,9 +626,9 @@ __global__ void __launch_bounds__(kTileThreads, 2) shade_kernel(PassArgs a) {
     }
     const float invS = 1.0f / (float)S;
     acc[0] = acc[0] * invS; acc[1] = acc[1] * invS; acc[2] = acc[2] * invS; acc[3] = acc[3] * invS;
-    encode_color(a, pix, acc);
+    encode_color(v, pix, acc);
 
-    float* dp = a.depth + pix * S;
+    float* dp = v.depth + pix * S;
     if constexpr (S % 4 == 0) {
 #pragma unroll
         for (int k = 0; k < S; k += 4) reinterpret_cast<float4*>(dp)[k / 4] = make_float4(dep[k], dep[k + 1], dep[k + 2], dep[k + 3]);
@@ -574,80 +636,93 @@ __global__ void __launch_bounds__(kTileThreads, 2) shade_kernel(PassArgs a) {
 #pragma unroll
         for (int k = 0; k < S; k++) dp[k] = dep[k];
     }
-    if (a.vis) {
-        int* vp = a.vis + pix * S;
+    if (v.vis) {
+        int* vp = v.vis + pix * S;
 #pragma unroll
-        for (int k = 0; k < S; k++) vp[k] = ent[k] < 0 ? -1 : (ent[k] >> 3);
+        for (int k = 0; k < S; k++) vp[k] = ent[k] < 0 ? -1 : (ent[k] >> 3) - v.first_tri;
     }
 }
 
-// Ordered stage (forward path), one CTA per tile.  Used when results depend on submission
-// order: blending, NOT_EQUAL with depth writes, or draws of one pass with different depth
-// state.  The tile's entries are sorted into API order in shared memory, then every pixel
-// applies them one after another exactly as the reference's ordered CPU path does
-// (TileRasterWorker.cpp:1517-1580): per-sample depth test and write, one shading per pixel
-// and triangle when any sample passes, per-sample blend (TileRasterWorker.cpp:2346-2373,
-// pixelShadingAlphaBlendKernel .cu:1648-1897), then the on-chip resolve.
+template <int S, int TS>
+__global__ void __launch_bounds__(TS * TS, 512 / (TS * TS)) shade_kernel(PassArgs a, GroupArgs g) {
+    constexpr int NT = TS * TS;
+    __shared__ float4 scol[4][NT];  // colours of each thread's (up to 4) distinct entries
+    __shared__ ViewArgs sv;
+    __shared__ int s_tile, s_view;
+    if (threadIdx.x == 0) s_view = -1;
+    while (next_tile<NT>(a, g, 2 * g.queue + 1, sv, s_tile, s_view)) shade_tile<S, TS>(a, sv, s_tile, scol);
+}
+
+// ---------------------------------------------------------------------------- ordered stage
+// Used when results depend on submission order: blending, NOT_EQUAL with depth writes, or
+// draws of one view with different depth state.  The tile's entries are sorted into API order
+// in shared memory, then every pixel applies them one after another exactly as the reference's
+// ordered CPU path does (TileRasterWorker.cpp:1517-1580): per-sample depth test and write, one
+// shading per pixel and triangle when any sample passes, per-sample blend
+// (TileRasterWorker.cpp:2346-2373, pixelShadingAlphaBlendKernel .cu:1648-1897), then the
+// on-chip resolve.  16x16 tiles.
+constexpr int kFwdThreads = 256;
+
 struct FwdRecords {
-    int32_t A[3][kTileThreads], B[3][kTileThreads];
-    long long Cb[3][kTileThreads];
-    float z0[kTileThreads], dzdx[kTileThreads], dzdy[kTileThreads];
-    int32_t X0[kTileThreads], Y0[kTileThreads];
-    int32_t bx[kTileThreads], by[kTileThreads];  // px0 | px1 << 16, py0 | py1 << 16
-    int32_t key[kTileThreads];
-    int32_t draw[kTileThreads];
+    int32_t A[3][kFwdThreads], B[3][kFwdThreads];
+    long long Cb[3][kFwdThreads];
+    float z0[kFwdThreads], dzdx[kFwdThreads], dzdy[kFwdThreads];
+    int32_t X0[kFwdThreads], Y0[kFwdThreads];
+    int32_t bx[kFwdThreads], by[kFwdThreads];  // px0 | px1 << 16, py0 | py1 << 16
+    int32_t key[kFwdThreads];
+    int32_t draw[kFwdThreads];
 };
 
 template <int S>
-__global__ void __launch_bounds__(kTileThreads) forward_kernel(PassArgs a) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    FwdRecords& rec = *reinterpret_cast<FwdRecords*>(smem_raw);
-    float4* scol = reinterpret_cast<float4*>(smem_raw + sizeof(FwdRecords));                  // [S][256]
-    uint32_t* list = reinterpret_cast<uint32_t*>(smem_raw + sizeof(FwdRecords) + sizeof(float4) * S * kTileThreads);
-
-    const int tile = blockIdx.x;
-    const int tx = tile % a.c.tiles_x, ty = tile / a.c.tiles_x;
+__device__ __forceinline__ void forward_tile(const PassArgs& a, const ViewArgs& v, int gtile, FwdRecords& rec,
+                                             float4* scol, uint32_t* list) {
+    constexpr int TS = 16, NT = kFwdThreads;
+    const int ltile = gtile - v.tile_start;
+    const int tx = ltile % v.c.tiles_x, ty = ltile / v.c.tiles_x;
     const int tid = threadIdx.x;
-    const int lx = ((tid >> 2) & 7) * 2 + (tid & 1);
-    const int ly = (tid >> 5) * 2 + ((tid >> 1) & 1);
-    const int px = tx * kTileSize + lx, py = ty * kTileSize + ly;
-    const bool inpix = px < a.c.W && py < a.c.H;
-    const size_t pix = (size_t)py * a.c.W + px;
+    int lx, ly;
+    tile_pixel<TS>(tid, lx, ly);
+    const int px = tx * TS + lx, py = ty * TS + ly;
+    const bool inpix = px < v.c.W && py < v.c.H;
+    const size_t pix = (size_t)py * v.c.W + px;
 
     float dep[S];
     int vid[S];
     {
         float bg[4];
-        if (a.clear) {
-            bg[0] = a.clear_color[0]; bg[1] = a.clear_color[1]; bg[2] = a.clear_color[2]; bg[3] = a.clear_color[3];
+        if (v.clear) {
+            bg[0] = v.clear_color[0]; bg[1] = v.clear_color[1]; bg[2] = v.clear_color[2]; bg[3] = v.clear_color[3];
         } else if (inpix) {
-            decode_color(a, pix, bg);
+            decode_color(v, pix, bg);
         } else {
             bg[0] = bg[1] = bg[2] = bg[3] = 0.0f;
         }
 #pragma unroll
         for (int k = 0; k < S; k++) {
-            dep[k] = a.clear ? a.clear_depth : (inpix ? a.depth[pix * S + k] : 0.0f);
+            dep[k] = v.clear ? v.clear_depth : (inpix ? v.depth[pix * S + k] : 0.0f);
             vid[k] = -1;
-            scol[k * kTileThreads + tid] = make_float4(bg[0], bg[1], bg[2], bg[3]);
+            scol[k * NT + tid] = make_float4(bg[0], bg[1], bg[2], bg[3]);
         }
     }
     const bool has_list = a.total_tris > 0 && a.status[ST_OVERFLOW] == 0;
-    const uint32_t beg = has_list ? a.tile_offset[tile] : 0u;
-    const uint32_t end = has_list ? a.tile_offset[tile + 1] : 0u;
+    const uint32_t beg = has_list ? a.tile_offset[gtile] : 0u;
+    const uint32_t end = has_list ? a.tile_offset[gtile + 1] : 0u;
     int n = (int)(end - beg);
     if (n > kOrderedCap) {  // cannot order this tile on chip: report and leave it cleared
-        if (tid == 0) atomicOr(a.status + ST_ORDERED_LIMIT, 1u);
+        if (tid == 0) {
+            atomicOr(a.status + ST_ORDERED_LIMIT, 1u);
+            atomicOr(a.status + ST_STICKY, 2u);
+        }
         n = 0;
     }
     // load and sort the tile's entries into submission order (bitonic, padded to 2^k)
     int P = 1;
     while (P < n) P <<= 1;
-    for (int i = tid; i < P; i += kTileThreads) list[i] = i < n ? __ldg(a.pairs + beg + i) : 0xFFFFFFFFu;
+    for (int i = tid; i < P; i += NT) list[i] = i < n ? __ldg(a.pairs + beg + i) : 0xFFFFFFFFu;
     __syncthreads();
     for (int k = 2; k <= P; k <<= 1) {
         for (int j = k >> 1; j > 0; j >>= 1) {
-            for (int i = tid; i < P; i += kTileThreads) {
+            for (int i = tid; i < P; i += NT) {
                 int ixj = i ^ j;
                 if (ixj > i) {
                     uint32_t x = list[i], y = list[ixj];
@@ -662,14 +737,13 @@ __global__ void __launch_bounds__(kTileThreads) forward_kernel(PassArgs a) {
         }
     }
 
-    for (int base = 0; base < n; base += kTileThreads) {
-        const int nb = min(kTileThreads, n - base);
+    for (int base = 0; base < n; base += NT) {
+        const int nb = min(NT, n - base);
         if (tid < nb) {
             uint32_t e = list[base + tid];
-            int g = (int)(e >> 3), sub = (int)(e & 7u);
-            int di = find_draw(a, g);
             SubTri s;
-            if (setup_entry_sub(a.c, a.draws[di], a.records, g, g - __ldg(a.draw_start + di), sub, s)) {
+            int di;
+            if (setup_raster_entry(a, v.c, e, &s, &di)) {
 #pragma unroll
                 for (int i = 0; i < 3; i++) {
                     rec.A[i][tid] = s.A[i];
@@ -704,22 +778,22 @@ __global__ void __launch_bounds__(kTileThreads) forward_kernel(PassArgs a) {
                 unsigned mask = 0;
 #pragma unroll
                 for (int k = 0; k < S; k++) {
-                    const int32_t sx = px * 256 + a.c.sx[k], sy = py * 256 + a.c.sy[k];
+                    const int32_t sx = px * 256 + sample_x<S>(k), sy = py * 256 + sample_y<S>(k);
                     if (!covered(A, B, Cb, sx, sy)) continue;
                     const float z = sample_depth(rec.z0[r], rec.dzdx[r], rec.dzdy[r], rec.X0[r], rec.Y0[r], sx, sy);
                     if (!depth_cmp(func, z, dep[k])) continue;
                     if (write) dep[k] = z;
-                    vid[k] = e >> 3;
+                    vid[k] = (e >> 3) - v.first_tri;
                     mask |= 1u << k;
                 }
                 if (!mask) continue;
                 float c[4];
                 RecordPlane pl;
-                shade_uncached(a, e, px, py, c, &pl);
+                shade_uncached(a, v.c, e, px, py, c, &pl);
 #pragma unroll
                 for (int k = 0; k < S; k++) {
                     if (!(mask & (1u << k))) continue;
-                    float4& sc = scol[k * kTileThreads + tid];
+                    float4& sc = scol[k * NT + tid];
                     if (d.blend_enable) {
                         float dst[4] = {sc.x, sc.y, sc.z, sc.w};
                         blend_into(d, c, dst);
@@ -736,21 +810,21 @@ __global__ void __launch_bounds__(kTileThreads) forward_kernel(PassArgs a) {
     float acc[4];
 #pragma unroll
     for (int k = 0; k < S; k++) {
-        const float4 v = scol[k * kTileThreads + tid];
+        const float4 q = scol[k * NT + tid];
         if (k == 0) {
-            acc[0] = v.x; acc[1] = v.y; acc[2] = v.z; acc[3] = v.w;
+            acc[0] = q.x; acc[1] = q.y; acc[2] = q.z; acc[3] = q.w;
         } else {
-            acc[0] = acc[0] + v.x; acc[1] = acc[1] + v.y; acc[2] = acc[2] + v.z; acc[3] = acc[3] + v.w;
+            acc[0] = acc[0] + q.x; acc[1] = acc[1] + q.y; acc[2] = acc[2] + q.z; acc[3] = acc[3] + q.w;
         }
     }
     const float invS = 1.0f / (float)S;
     acc[0] = acc[0] * invS; acc[1] = acc[1] * invS; acc[2] = acc[2] * invS; acc[3] = acc[3] * invS;
-    encode_color(a, pix, acc);
-    float* dp = a.depth + pix * S;
+    encode_color(v, pix, acc);
+    float* dp = v.depth + pix * S;
 #pragma unroll
     for (int k = 0; k < S; k++) dp[k] = dep[k];
-    if (a.vis) {
-        int* vp = a.vis + pix * S;
+    if (v.vis) {
+        int* vp = v.vis + pix * S;
 #pragma unroll
         for (int k = 0; k < S; k++) vp[k] = vid[k];
     }
@@ -758,15 +832,22 @@ __global__ void __launch_bounds__(kTileThreads) forward_kernel(PassArgs a) {
 
 template <int S>
 size_t forward_smem_bytes() {
-    return sizeof(FwdRecords) + sizeof(float4) * S * kTileThreads + sizeof(uint32_t) * kOrderedCap;
+    return sizeof(FwdRecords) + sizeof(float4) * S * kFwdThreads + sizeof(uint32_t) * kOrderedCap;
 }
 
 template <int S>
-size_t raster_smem_bytes() {
-    return sizeof(TileRecords) + (size_t)kTileThreads * S * sizeof(unsigned long long);
+__global__ void __launch_bounds__(kFwdThreads) forward_kernel(PassArgs a, GroupArgs g) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    FwdRecords& rec = *reinterpret_cast<FwdRecords*>(smem_raw);
+    float4* scol = reinterpret_cast<float4*>(smem_raw + sizeof(FwdRecords));  // [S][256]
+    uint32_t* list = reinterpret_cast<uint32_t*>(smem_raw + sizeof(FwdRecords) + sizeof(float4) * S * kFwdThreads);
+    __shared__ ViewArgs sv;
+    __shared__ int s_tile, s_view;
+    if (threadIdx.x == 0) s_view = -1;
+    while (next_tile<kFwdThreads>(a, g, 2 * g.queue, sv, s_tile, s_view)) forward_tile<S>(a, sv, s_tile, rec, scol, list);
 }
 
-
+// ---------------------------------------------------------------------------- mips
 __global__ void mip_kernel(const uint32_t* __restrict__ src, int sw, int sh, uint32_t* __restrict__ dst, int dw, int dh) {
     int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
     if (x >= dw || y >= dh) return;
@@ -788,36 +869,121 @@ cudaError_t launch_mip_level(const uint32_t* src, int sw, int sh, uint32_t* dst,
     return cudaGetLastError();
 }
 
+// ---------------------------------------------------------------------------- launches
+template <int S, int TS>
+cudaError_t configure_deferred() {
+    static bool done = false;
+    if (done) return cudaSuccess;
+    cudaError_t e = cudaFuncSetAttribute(raster_kernel<S, TS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)raster_smem_bytes<S, TS>());
+    if (e == cudaSuccess) done = true;
+    return e;
+}
+
 template <int S>
-cudaError_t launch_tile(const PassArgs& a, int T, cudaStream_t stream, cudaEvent_t mid) {
-    if (a.ordered) {
-        static bool fconfigured = false;
-        const size_t fbytes = forward_smem_bytes<S>();
-        if (!fconfigured) {
-            cudaError_t e = cudaFuncSetAttribute(forward_kernel<S>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fbytes);
-            if (e != cudaSuccess) return e;
-            fconfigured = true;
-        }
-        forward_kernel<S><<<T, kTileThreads, fbytes, stream>>>(a);
-        if (mid) cudaEventRecord(mid, stream);
-        return cudaSuccess;
-    }
-    static bool configured = false;
-    const size_t rbytes = raster_smem_bytes<S>();
-    if (!configured) {
-        cudaError_t e = cudaFuncSetAttribute(raster_kernel<S>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rbytes);
-        if (e != cudaSuccess) return e;
-        configured = true;
-    }
-    raster_kernel<S><<<T, kTileThreads, rbytes, stream>>>(a);
-    if (mid) cudaEventRecord(mid, stream);
-    shade_kernel<S><<<T, kTileThreads, 0, stream>>>(a);
+cudaError_t configure_forward() {
+    static bool done = false;
+    if (done) return cudaSuccess;
+    cudaError_t e = cudaFuncSetAttribute(forward_kernel<S>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)forward_smem_bytes<S>());
+    if (e == cudaSuccess) done = true;
+    return e;
+}
+
+template <int S, int TS>
+cudaError_t launch_deferred(const PassArgs& a, const GroupArgs& g, int ctas, cudaStream_t stream, bool shade) {
+    cudaError_t e = configure_deferred<S, TS>();
+    if (e != cudaSuccess) return e;
+    if (!shade) raster_kernel<S, TS><<<ctas, TS * TS, raster_smem_bytes<S, TS>(), stream>>>(a, g);
+    else shade_kernel<S, TS><<<ctas, TS * TS, 0, stream>>>(a, g);
     return cudaSuccess;
 }
 
-cudaError_t launch_pass(const PassArgs& a, cudaStream_t stream, cudaEvent_t* ev) {
-    const int T = a.c.tiles_x * a.c.tiles_y;
+template <int S>
+cudaError_t launch_forward(const PassArgs& a, const GroupArgs& g, int ctas, cudaStream_t stream) {
+    cudaError_t e = configure_forward<S>();
+    if (e != cudaSuccess) return e;
+    forward_kernel<S><<<ctas, kFwdThreads, forward_smem_bytes<S>(), stream>>>(a, g);
+    return cudaSuccess;
+}
+
+// One tile stage (raster or shade) of a deferred group.
+cudaError_t launch_group_stage(const PassArgs& a, const GroupArgs& g, int S, int TS, int ctas, cudaStream_t stream,
+                               bool shade) {
+    if (TS == 8) {
+        switch (S) {
+        case 1: return launch_deferred<1, 8>(a, g, ctas, stream, shade);
+        case 4: return launch_deferred<4, 8>(a, g, ctas, stream, shade);
+        default: break;
+        }
+    }
+    switch (S) {
+    case 1: return launch_deferred<1, 16>(a, g, ctas, stream, shade);
+    case 2: return launch_deferred<2, 16>(a, g, ctas, stream, shade);
+    case 4: return launch_deferred<4, 16>(a, g, ctas, stream, shade);
+    case 8: return launch_deferred<8, 16>(a, g, ctas, stream, shade);
+    case 16: return launch_deferred<16, 16>(a, g, ctas, stream, shade);
+    default: return cudaErrorInvalidValue;
+    }
+}
+
+cudaError_t launch_group_forward(const PassArgs& a, const GroupArgs& g, int S, int ctas, cudaStream_t stream) {
+    switch (S) {
+    case 1: return launch_forward<1>(a, g, ctas, stream);
+    case 2: return launch_forward<2>(a, g, ctas, stream);
+    case 4: return launch_forward<4>(a, g, ctas, stream);
+    case 8: return launch_forward<8>(a, g, ctas, stream);
+    case 16: return launch_forward<16>(a, g, ctas, stream);
+    default: return cudaErrorInvalidValue;
+    }
+}
+
+template <class K>
+int occupancy_of(K kernel, int threads, size_t smem) {
+    int n = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kernel, threads, smem) != cudaSuccess) return 1;
+    return n > 0 ? n : 1;
+}
+
+template <int S, int TS>
+int deferred_occupancy(int stage) {
+    configure_deferred<S, TS>();
+    return stage == 0 ? occupancy_of(raster_kernel<S, TS>, TS * TS, raster_smem_bytes<S, TS>())
+                      : occupancy_of(shade_kernel<S, TS>, TS * TS, 0);
+}
+
+template <int S>
+int forward_occupancy() {
+    configure_forward<S>();
+    return occupancy_of(forward_kernel<S>, kFwdThreads, forward_smem_bytes<S>());
+}
+
+int tile_kernel_occupancy(int S, int TS, int ordered, int stage) {
+    if (ordered) {
+        switch (S) {
+        case 1: return forward_occupancy<1>();
+        case 2: return forward_occupancy<2>();
+        case 4: return forward_occupancy<4>();
+        case 8: return forward_occupancy<8>();
+        default: return forward_occupancy<16>();
+        }
+    }
+    if (TS == 8 && S == 1) return deferred_occupancy<1, 8>(stage);
+    if (TS == 8 && S == 4) return deferred_occupancy<4, 8>(stage);
+    switch (S) {
+    case 1: return deferred_occupancy<1, 16>(stage);
+    case 2: return deferred_occupancy<2, 16>(stage);
+    case 4: return deferred_occupancy<4, 16>(stage);
+    case 8: return deferred_occupancy<8, 16>(stage);
+    default: return deferred_occupancy<16, 16>(stage);
+    }
+}
+
+cudaError_t launch_pass(const PassArgs& a, const LaunchPlan& plan, cudaStream_t stream, cudaEvent_t* ev) {
+    const int T = a.total_tiles;
     if (ev) cudaEventRecord(ev[0], stream);
+    cudaError_t err = cudaMemsetAsync(a.queues, 0, sizeof(uint32_t) * 2 * plan.ngroups, stream);
+    if (err != cudaSuccess) return err;
     if (a.total_tris > 0) {
         int blocks = (a.total_tris + 255) / 256;
         bin_count_kernel<<<blocks, 256, 0, stream>>>(a);
@@ -831,16 +997,15 @@ cudaError_t launch_pass(const PassArgs& a, cudaStream_t stream, cudaEvent_t* ev)
         cudaEventRecord(ev[2], stream);
         cudaEventRecord(ev[3], stream);
     }
-    cudaError_t err = cudaSuccess;
-    cudaEvent_t mid = ev ? ev[4] : nullptr;
-    switch (a.c.S) {
-    case 1: err = launch_tile<1>(a, T, stream, mid); break;
-    case 2: err = launch_tile<2>(a, T, stream, mid); break;
-    case 4: err = launch_tile<4>(a, T, stream, mid); break;
-    case 8: err = launch_tile<8>(a, T, stream, mid); break;
-    case 16: err = launch_tile<16>(a, T, stream, mid); break;
-    default: err = cudaErrorInvalidValue;
+    // raster stages of all groups, then shade stages (the ordered stage counts as raster)
+    for (int i = 0; i < plan.ngroups && err == cudaSuccess; i++) {
+        if (plan.ordered[i]) err = launch_group_forward(a, plan.groups[i], plan.samples[i], plan.ctas[i], stream);
+        else err = launch_group_stage(a, plan.groups[i], plan.samples[i], plan.tile_size[i], plan.ctas[i], stream, false);
     }
+    if (ev) cudaEventRecord(ev[4], stream);
+    for (int i = 0; i < plan.ngroups && err == cudaSuccess; i++)
+        if (!plan.ordered[i])
+            err = launch_group_stage(a, plan.groups[i], plan.samples[i], plan.tile_size[i], plan.ctas_shade[i], stream, true);
     if (ev) cudaEventRecord(ev[5], stream);
     return err != cudaSuccess ? err : cudaGetLastError();
 }

@@ -1,25 +1,37 @@
 // Kernel-side pass description shared by raster_kernels.cu and the host runtime.
+//
+// A pass renders one or more views (each its own target, size and sample count); a single
+// frame is a pass with one view.  Triangles of all views are binned together into the
+// concatenation of every view's screen tiles; the tile stages then run as persistent CTAs
+// that pull tiles from a queue per launch group (views of equal sample count and path).
 #pragma once
 #include <cstdint>
 #include "raster_math.cuh"
 
 namespace ifr {
 
-constexpr int kTileShift = 4;  // 16x16-pixel screen tiles
-constexpr int kTileSize = 1 << kTileShift;
-constexpr int kTileThreads = kTileSize * kTileSize;
 constexpr int kMaxDraws = 256;
+constexpr int kMaxViews = 4096;
 
-enum StatusWord { ST_OVERFLOW = 0, ST_PAIRS = 1, ST_ORDERED_LIMIT = 2, ST_WORDS = 4 };
+// Status words of a pass.  Words below ST_PASS_WORDS describe the latest pass and are cleared
+// when it starts; ST_STICKY (bit 0: some pass overflowed its pair list, bit 1: some ordered tile
+// exceeded kOrderedCap) and ST_MAX_PAIRS accumulate until the host reads and clears them.
+enum StatusWord {
+    ST_OVERFLOW = 0,
+    ST_PAIRS = 1,
+    ST_ORDERED_LIMIT = 2,
+    ST_PASS_WORDS = 4,
+    ST_STICKY = 4,
+    ST_MAX_PAIRS = 5,
+    ST_WORDS = 8
+};
 constexpr int kOrderedCap = 8192;  // entries per tile an ordered (in-API-order) pass can sort
 
-struct PassArgs {
+// One view (render target) of a pass.
+struct ViewArgs {
     PassConst c;
-    const DrawDev* draws;    // device array [ndraws]
-    const int* draw_start;   // device array [ndraws + 1], prefix of triangle counts
-    int ndraws;
-    int total_tris;
-    // targets
+    int tile_start;          // global index of the view's first tile
+    int first_tri;           // global index of the view's first triangle (its primitive id 0)
     int format;
     void* color;             // resolved colour (format-dependent)
     float* depth;            // per-sample depth [H][W][S]
@@ -28,18 +40,50 @@ struct PassArgs {
     int clear;
     float clear_color[4];
     float clear_depth;
-    int depth_func;          // pass-uniform depth function (deferred path)
+    int depth_func;          // view-uniform depth function (deferred path)
     int depth_write;
     int ordered;             // 1: triangles applied to each sample in API order (blending, NOT_EQUAL,
                              //    or draws with different depth state)
+};
+
+struct PassArgs {
+    const DrawDev* draws;    // device array [ndraws]
+    const int* draw_start;   // device array [ndraws + 1], prefix of triangle counts
+    int ndraws;
+    int total_tris;
+    const ViewArgs* views;   // device array [nviews]
+    const int* view_tile_start;  // device array [nviews + 1]
+    int nviews;
+    int total_tiles;
     // binning
-    uint32_t* tile_count;    // [T], zero between passes
-    uint32_t* tile_offset;   // [T + 1]
-    uint32_t* tile_cursor;   // [T]
+    uint32_t* tile_count;    // [total_tiles], zero between passes
+    uint32_t* tile_offset;   // [total_tiles + 1]
+    uint32_t* tile_cursor;   // [total_tiles]
     uint32_t* pairs;         // (global triangle << 3 | fan index), capacity entries
     TriRecord* records;      // [total_tris] compact set-ups written by the counting binner
     uint32_t pair_capacity;
     uint32_t* status;        // StatusWord
+    uint32_t* queues;        // persistent tile counters, 2 per launch group (raster, shade)
+};
+
+constexpr int kMaxGroups = 16;  // launch groups of a pass: (samples, path, tile size) combinations
+
+// A contiguous range of views sharing sample count and path, with its tiles.
+struct GroupArgs {
+    int view_begin, view_end;
+    int tile_begin, tile_end;
+    int queue;               // index of the group's counters in PassArgs::queues
+};
+
+// Launch plan of a pass (host side).
+struct LaunchPlan {
+    int ngroups;
+    GroupArgs groups[kMaxGroups];
+    int samples[kMaxGroups];
+    int tile_size[kMaxGroups];  // 8 or 16
+    int ordered[kMaxGroups];
+    int ctas[kMaxGroups];       // persistent CTAs of the group's raster (or ordered) stage
+    int ctas_shade[kMaxGroups]; // persistent CTAs of the group's shade stage
 };
 
 }  // namespace ifr
@@ -47,7 +91,10 @@ struct PassArgs {
 // Host-callable launchers (defined in raster_kernels.cu).
 namespace ifr {
 // ev: optional array of 6 events recorded before binning, after counting, after the scan,
-// after scattering, after the raster kernel and after the shade kernel (per-stage timing).
-cudaError_t launch_pass(const PassArgs& a, cudaStream_t stream, cudaEvent_t* ev);
+// after scattering, after the raster stage and after the shade stage (per-stage timing).
+cudaError_t launch_pass(const PassArgs& a, const LaunchPlan& plan, cudaStream_t stream, cudaEvent_t* ev);
 cudaError_t launch_mip_level(const uint32_t* src, int sw, int sh, uint32_t* dst, int dw, int dh, cudaStream_t stream);
+// Maximum resident CTAs per SM of a tile kernel for (samples, tile size, ordered); stage 0 is
+// the raster (or ordered) kernel, stage 1 the shade kernel.
+int tile_kernel_occupancy(int samples, int tile_size, int ordered, int stage);
 }  // namespace ifr

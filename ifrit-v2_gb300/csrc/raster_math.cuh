@@ -33,6 +33,7 @@ struct SamplerDev {
 
 // One draw of a render pass, as the kernels see it (device pointers).
 struct DrawDev {
+    int view;  // index of the view (target) this draw renders into
     const float* vertices;
     int stride, num_vertices, attr_offset, attr_count;
     const int* indices;
@@ -47,13 +48,33 @@ struct DrawDev {
     int lvl_off[16], lvl_w[16], lvl_h[16];  // mip table: texel offset and size of each level
 };
 
-// Pass-wide constants.
+// Standard sample positions in 1/256 pixel (the D3D 1/2/4/8/16x patterns): (x, y) of sample k
+// of an S-sample pixel.  With S and k compile-time constants (templated sample counts, unrolled
+// sample loops) these fold to immediates.
+__host__ __device__ __forceinline__ int sample_pos(int S, int k, int axis) {
+    const int p1[2] = {128, 128};
+    const int p2[4] = {192, 192, 64, 64};
+    const int p4[8] = {96, 32, 224, 96, 32, 160, 160, 224};
+    const int p8[16] = {144, 80, 112, 176, 208, 144, 80, 48, 48, 208, 16, 112, 176, 240, 240, 16};
+    const int p16[32] = {144, 144, 112, 80, 80, 160, 192, 112, 48, 96, 160, 208, 208, 176, 176, 48,
+                         96, 224, 128, 16, 64, 32, 32, 192, 0, 128, 240, 64, 224, 240, 16, 0};
+    const int i = 2 * k + axis;
+    return S == 1 ? p1[i] : S == 2 ? p2[i] : S == 4 ? p4[i] : S == 8 ? p8[i] : p16[i];
+}
+template <int S>
+__device__ __forceinline__ int sample_x(int k) { return sample_pos(S, k, 0); }
+template <int S>
+__device__ __forceinline__ int sample_y(int k) { return sample_pos(S, k, 1); }
+
+// Attributes are evaluated at the pixel centre (1/256-pixel units).
+constexpr int kShadeOffset = 128;
+
+// Per-view constants of a pass.
 struct PassConst {
     int W, H, S;
+    int tile_shift;  // log2 of the screen-tile edge (3: 8x8, 4: 16x16)
     int tiles_x, tiles_y;
-    int sx[16], sy[16];
-    int smin_x, smax_x, smin_y, smax_y;
-    int shade_x, shade_y;
+    int smin_x, smax_x, smin_y, smax_y;  // bounds of the sample positions
     float W256, H256, gx, gy;
 };
 
@@ -632,13 +653,13 @@ __device__ __forceinline__ void shade_fragment(const PassConst& c, const DrawDev
     load_attr(d.vertices + (size_t)__ldg(d.indices + 3 * (size_t)t + 0) * d.stride + d.attr_offset, d.attr_count, a0);
     load_attr(d.vertices + (size_t)__ldg(d.indices + 3 * (size_t)t + 1) * d.stride + d.attr_offset, d.attr_count, a1);
     load_attr(d.vertices + (size_t)__ldg(d.indices + 3 * (size_t)t + 2) * d.stride + d.attr_offset, d.attr_count, a2);
-    int32_t qx = px * 256 + c.shade_x, qy = py * 256 + c.shade_y;
+    int32_t qx = px * 256 + kShadeOffset, qy = py * 256 + kShadeOffset;
     float a[4];
     interp_attr(s, d.attr_count, a0, a1, a2, qx, qy, a);
     if (d.shading == SHADE_TEXTURED) {
         float ah[4], av[4];  // horizontal and vertical quad partners
-        interp_attr(s, d.attr_count, a0, a1, a2, (px ^ 1) * 256 + c.shade_x, qy, ah);
-        interp_attr(s, d.attr_count, a0, a1, a2, qx, (py ^ 1) * 256 + c.shade_y, av);
+        interp_attr(s, d.attr_count, a0, a1, a2, (px ^ 1) * 256 + kShadeOffset, qy, ah);
+        interp_attr(s, d.attr_count, a0, a1, a2, qx, (py ^ 1) * 256 + kShadeOffset, av);
         float dudx = (px & 1) ? a[0] - ah[0] : ah[0] - a[0];
         float dvdx = (px & 1) ? a[1] - ah[1] : ah[1] - a[1];
         float dudy = (py & 1) ? a[0] - av[0] : av[0] - a[0];

@@ -43,7 +43,7 @@ EXPORTED = [
     "ifbufCreateBufferManager", "ifbufDestroyBufferManager", "ifbufCreateBuffer", "ifbufDestroyBuffer",
     "ifbufBufferData", "iftrSetStageTiming", "iftrGetStageTimes", "iftrGetVertexBufferRawData",
     "iftrSetVertexBufferDirty", "ifbufGetBufferRawData", "ifbufSetBufferDirty", "iftrDrawNoAlloc",
-    "iftrBeginPass", "iftrPassDraw", "iftrEndPass",
+    "iftrBeginPass", "iftrPassDraw", "iftrEndPass", "iftrDrawBatch", "iftrSetBatchTuning", "iftrGetBatchTuning",
 ]
 
 
@@ -71,6 +71,25 @@ class NoAllocPass(ctypes.Structure):
                 ("cullMode", ctypes.c_int), ("frontCounterClockwise", ctypes.c_int), ("shadingModel", ctypes.c_int),
                 ("texels", ctypes.c_void_p), ("texWidth", ctypes.c_int), ("texHeight", ctypes.c_int),
                 ("texLevels", ctypes.c_int), ("sampler", SamplerState)]
+
+
+class BatchView(ctypes.Structure):
+    """IfritGbBatchView (include/ifrit_gb300.h)."""
+    _fields_ = [("width", ctypes.c_int), ("height", ctypes.c_int), ("samples", ctypes.c_int),
+                ("colorFormat", ctypes.c_int), ("color", ctypes.c_void_p), ("depth", ctypes.c_void_p),
+                ("visibility", ctypes.c_void_p), ("clear", ctypes.c_int), ("clearColor", ctypes.c_float * 4),
+                ("clearDepth", ctypes.c_float)]
+
+
+class BatchDraw(ctypes.Structure):
+    """IfritGbBatchDraw (include/ifrit_gb300.h)."""
+    _fields_ = [("view", ctypes.c_int), ("vertices", ctypes.c_void_p), ("strideFloats", ctypes.c_int),
+                ("numVertices", ctypes.c_int), ("attrOffsetFloats", ctypes.c_int), ("attrCount", ctypes.c_int),
+                ("indices", ctypes.c_void_p), ("numIndices", ctypes.c_int), ("mvp", ctypes.c_float * 16),
+                ("depthFunc", ctypes.c_int), ("depthTest", ctypes.c_int), ("depthWrite", ctypes.c_int),
+                ("cullMode", ctypes.c_int), ("frontCounterClockwise", ctypes.c_int), ("shadingModel", ctypes.c_int),
+                ("blend", BlendState), ("texels", ctypes.c_void_p), ("texWidth", ctypes.c_int),
+                ("texHeight", ctypes.c_int), ("texLevels", ctypes.c_int), ("sampler", SamplerState)]
 
 
 class Stats(ctypes.Structure):
@@ -129,6 +148,9 @@ def load(build_if_missing=True):
         "iftrGetVertexBufferRawData": [vp], "iftrSetVertexBufferDirty": [vp], "ifbufGetBufferRawData": [vp],
         "ifbufSetBufferDirty": [vp], "iftrDrawNoAlloc": [ctypes.POINTER(NoAllocPass), vp],
         "iftrBeginPass": [vp, ip], "iftrPassDraw": [vp, ip, ip], "iftrEndPass": [vp],
+        "iftrDrawBatch": [vp, ctypes.POINTER(BatchView), ip, ctypes.POINTER(BatchDraw), ip],
+        "iftrSetBatchTuning": [vp, ip, ip, ip],
+        "iftrGetBatchTuning": [vp, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)],
     }
     for name, args in sig.items():
         getattr(lib, name).argtypes = args

@@ -206,6 +206,53 @@ typedef struct {
 } IfritGbNoAllocPass;
 IFTR_API int iftrDrawNoAlloc(const IfritGbNoAllocPass* pass, void* cudaStream);
 
+/* ---- batched views (no counterpart in the reference, which renders one view per drawElements)
+ * Many independent views of uneven size, sample count and triangle count rendered as one pass:
+ * one binning launch over all views' triangles and one persistent launch per tile stage and
+ * (samples, path, tile size) group, pulling tiles from per-group work queues.  Inputs and
+ * outputs are caller-owned device buffers; each view has its own target and clear values, each
+ * draw names its view and carries its own state.  Within a view, draws keep their array order
+ * (it decides depth ties and blending order).  The first call with a given description sizes
+ * the scratch (synchronously), optionally autotunes the launch parameters, and captures the
+ * pass into a CUDA graph; later calls with a byte-identical description replay that graph
+ * asynchronously on the renderer's stream.  iftrFinish returns the status (IFTR_ERR_OVERFLOW or
+ * IFTR_ERR_LIMIT if a replay exceeded the sized scratch, after growing it; the next call then
+ * re-sizes and re-captures). */
+typedef struct {
+    int width, height, samples;     /* samples: 1, 2, 4, 8 or 16 */
+    int colorFormat;                /* IFTR_FORMAT_* */
+    void* color;                    /* device, resolved colour */
+    float* depth;                   /* device, per-sample depth [H][W][S] */
+    int* visibility;                /* device, per-sample primitive id, or NULL */
+    int clear;
+    float clearColor[4];
+    float clearDepth;
+} IfritGbBatchView;
+typedef struct {
+    int view;                       /* index into the view array */
+    const float* vertices;          /* device, AoS floats; position = floats 0..2 */
+    int strideFloats, numVertices, attrOffsetFloats, attrCount;
+    const int* indices;             /* device, 3 per triangle */
+    int numIndices;
+    float mvp[16];                  /* row-major */
+    int depthFunc, depthTest, depthWrite, cullMode, frontCounterClockwise;
+    int shadingModel;               /* IFTR_FS_* */
+    IfritGbBlendState blend;
+    const uint32_t* texels;         /* device RGBA8 mip chain (IFTR_FS_TEXTURED) */
+    int texWidth, texHeight, texLevels;
+    IfritGbSampler sampler;
+} IfritGbBatchDraw;
+#define IFTR_MAX_BATCH_VIEWS 4096
+#define IFTR_MAX_BATCH_DRAWS 65536
+IFTR_API int iftrDrawBatch(IfritGbRenderer* h, const IfritGbBatchView* views, int numViews,
+                           const IfritGbBatchDraw* draws, int numDraws);
+/* Launch parameters of batched passes.  autotune = 1 (default): the first call of a new batch
+ * description times each candidate (tile edge 8 or 16 for 1x/4x views, persistent CTAs per SM
+ * at full or half occupancy) and keeps the fastest; autotune = 0 uses tileSize (8 or 16; views
+ * whose sample count has no 8x8 kernels use 16) and ctasPerSm (0: full occupancy). */
+IFTR_API int iftrSetBatchTuning(IfritGbRenderer* h, int autotune, int tileSize, int ctasPerSm);
+IFTR_API int iftrGetBatchTuning(IfritGbRenderer* h, int* tileSize, int* ctasPerSm);
+
 /* ---- framebuffers and images (ECE:31-40, CE:25-31) */
 IFTR_API IfritGbFrameBuffer* iftrCreateFrameBuffer(void);                            /* ECE:31 */
 IFTR_API int iftrDestroyFrameBuffer(IfritGbFrameBuffer* fb);                         /* ECE:33 */
