@@ -28,6 +28,7 @@ import os
 import statistics
 import subprocess
 import sys
+import tempfile
 import time
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
@@ -38,6 +39,7 @@ for _p in (ROOT, os.path.join(ROOT, "ifrit-v2_gb300")):
 import numpy as np  # noqa: E402
 
 METRIC = "shaded samples/s"
+KERNELS_PER_PASS = 5  # counting binner, scan, scattering binner, raster, shade (one launch group)
 L2_FLUSH_BYTES = 256 << 20
 
 
@@ -47,8 +49,9 @@ def parse():
     p.add_argument("--steps", type=int, default=20)
     p.add_argument("--warmup", type=int, default=5)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    p.add_argument("--workload", default="c2", choices=["c1", "c2"])
+    p.add_argument("--workload", default="c2", choices=["c1", "c2", "c3"])
     p.add_argument("--e2e-steps", type=int, default=10)
+    p.add_argument("--no-batch", action="store_true", help="leave the batched (c3) summary out of the c2 line")
     return p.parse_args()
 
 
@@ -114,7 +117,7 @@ class ClockSampler:
 
     def __init__(self):
         self.proc = None
-        self.path = os.path.join("/tmp", "ifrit_clocks_%d.csv" % os.getpid())
+        self.path = os.path.join(tempfile.gettempdir(), "ifrit_clocks_%d.csv" % os.getpid())
 
     def start(self):
         try:
@@ -211,6 +214,177 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def c3_algorithmic_bytes(views):
+    """Compulsory bytes of the batch: per view, its vertices and indices read once, per-sample
+    depth and resolved RGBA8 colour written once."""
+    return int(sum(v["vertices"].nbytes + v["indices"].nbytes + v["width"] * v["height"] * (4 * v["samples"] + 4)
+                   for v in views))
+
+
+def run_c3(args, steps, warmup, e2e_steps, with_cpu=True):
+    """Batched workload: 256 views (edges U{128,256,512,1024}, 1x/4x, 1k-200k triangles
+    log-uniform, icospheres or soups, Gouraud).  Returns a dict of measurements."""
+    import torch
+    import ifrit_gb300 as ig
+    from ifrit_gb300 import scenes
+    from ifrit_gb300.batch import BatchRenderer
+
+    dev = torch.device("cuda", torch.cuda.current_device())
+    stream = torch.cuda.current_stream(dev)
+    views = scenes.c3_batch()
+    T = sum(len(v["indices"]) for v in views)
+
+    def build(subset, vis):
+        br = BatchRenderer()
+        for k, i in enumerate(subset):
+            v = views[i]
+            br.add_view(v["width"], v["height"], v["samples"], ig.FORMAT_RGBA8, visibility=vis)
+            br.add_mesh(k, v["vertices"], v["indices"], v["mvp"], attr_count=v["vertices"].shape[1] - 3, cull=v["cull"])
+        return br
+
+    def time_batch(br, n, w):
+        for _ in range(w):
+            br.draw()
+        br.finish()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for _ in range(n):
+            br.draw()
+        e1.record(stream)
+        br.finish()
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / n
+
+    everything = list(range(len(views)))
+    small = [i for i, v in enumerate(views) if v["width"] == 128]
+    # shaded samples per view, from one run with visibility output
+    br = build(everything, True)
+    br.draw()
+    br.finish()
+    shaded = [int((br.target(k)["vis"] >= 0).sum().item()) for k in range(len(views))]
+    br.close()
+    del br
+    torch.cuda.empty_cache()
+    clocks = ClockSampler()
+    br = build(everything, False)
+    br.draw()  # sizes, tunes, captures
+    br.finish()
+    clocks.start()
+    ms = time_batch(br, steps, warmup)
+    clk = clocks.stop(torch.cuda.current_device())
+    tuning = br.tuning()
+    # end to end: pinned host geometry uploaded every step, colours read back every step
+    host_in = [(torch.from_numpy(v["vertices"]).pin_memory(), torch.from_numpy(v["indices"].reshape(-1)).pin_memory())
+               for v in views]
+    host_out = [torch.empty(br.target(k)["color"].shape, dtype=torch.int32, pin_memory=True) for k in everything]
+    h2d = sum(a.numel() * 4 + b.numel() * 4 for a, b in host_in)
+    d2h = sum(o.numel() * 4 for o in host_out)
+    e2e = []
+    for it in range(max(1, e2e_steps) + 1):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for k, (a, b) in enumerate(host_in):
+            br.keep[k][0].copy_(a, non_blocking=True)
+            br.keep[k][1].copy_(b, non_blocking=True)
+        br.draw()
+        for k in everything:
+            host_out[k].copy_(br.target(k)["color"], non_blocking=True)
+        br.finish()
+        torch.cuda.synchronize()
+        if it:
+            e2e.append(time.perf_counter() - t0)
+    br.close()
+    del br
+    torch.cuda.empty_cache()
+    # small views: batched (only the 128^2 views) against the plain one-pass-per-frame path
+    brs = build(small, False)
+    brs.draw()
+    brs.finish()
+    ms_small = time_batch(brs, steps, warmup)
+    brs.close()
+    del brs
+    plain = []
+    for i in everything:
+        v = views[i]
+        r = ig.Renderer(v["width"], v["height"], v["samples"], ig.FORMAT_RGBA8, visibility=False)
+        r.set_stream(stream.cuda_stream)
+        r.set_state(cull=v["cull"], depth_func=ig.LESS_OR_EQUAL, shading=ig.FS_GOURAUD)
+        r.set_mvp(v["mvp"])
+        dv = torch.from_numpy(v["vertices"]).to(dev)
+        di = torch.from_numpy(v["indices"].reshape(-1)).to(dev)
+        stride = v["vertices"].shape[1]
+        r.bind_device_geometry(dv.data_ptr(), stride, len(v["vertices"]), 3, stride - 3, di.data_ptr(), di.numel())
+        r.draw_async()
+        r.finish()  # settles scratch
+        ts = []
+        for _ in range(3):
+            t0 = time.perf_counter()
+            r.draw_async()
+            r.finish()
+            ts.append(time.perf_counter() - t0)
+        plain.append(statistics.median(ts))
+        r.close()
+    plain_all = sum(shaded) / sum(plain)
+    plain_small = sum(shaded[i] for i in small) / sum(plain[i] for i in small)
+    batched_small = sum(shaded[i] for i in small) / (ms_small / 1000.0)
+    B = c3_algorithmic_bytes(views)
+    peak, peak_kind = peak_hbm()
+    out = {
+        "value": sum(shaded) / (ms / 1000.0), "ms_per_step": ms, "tris_per_s": T / (ms / 1000.0),
+        # per pass: three binning kernels plus raster and shade per launch group (1x and 4x views)
+        "kernels_per_step": 3 + 2 * len(set(v["samples"] for v in views)),
+        "views": len(views), "triangles": T, "shaded_samples_per_step": sum(shaded),
+        "pixels": int(sum(v["width"] * v["height"] for v in views)),
+        "tuning": {"tile_size": tuning[0], "ctas_per_sm": tuning[1]},
+        "plain": {"value": plain_all, "ms_per_step": 1000.0 * sum(plain),
+                  "how": "one iftrDrawAsync + iftrFinish per view, device-resident geometry, host wall time"},
+        "small_views": {"views": len(small), "size": 128, "batched": batched_small, "plain": plain_small,
+                        "ratio": batched_small / plain_small},
+        "roofline": {"bound": "hbm", "achieved": B / (ms / 1000.0) / 1e9, "peak": peak, "unit": "GB/s",
+                     "frac": B / (ms / 1000.0) / 1e9 / peak, "traffic": None, "algorithmic_bytes": B,
+                     "kernel": "whole batched pass", "peak_source": peak_kind},
+        "e2e": {"value": sum(shaded) / statistics.mean(e2e), "unit": "samples/s", "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": int(d2h), "ms_per_step": 1000.0 * statistics.mean(e2e)},
+        "clocks": clk,
+    }
+    if with_cpu:
+        # bounded CPU sample: the oracle on views in order until ~10 s of CPU work
+        from oracle import oracle as O
+        nthreads = os.cpu_count() or 1
+        spent, done = 0.0, 0
+        for i in everything:
+            v = views[i]
+            d = O.make_draw(v["vertices"], v["indices"], v["mvp"], attr_offset=3, attr_count=v["vertices"].shape[1] - 3,
+                            cull_mode=v["cull"], depth_func=3)
+            t0 = time.perf_counter()
+            res = O.render([d], v["width"], v["height"], v["samples"], nthreads=nthreads)
+            spent += time.perf_counter() - t0
+            done += int((res["vis"] >= 0).sum())
+            if spent > 10.0:
+                break
+        out["cpu_baseline"] = {"value": done / spent, "unit": "samples/s", "cores": nthreads, "kind": "port",
+                               "sample": "oracle on the batch's views in order until 10 s of work (%d samples)" % done}
+    return out
+
+
+def run_ours_c3(args):
+    rank, world, dist = dist_setup(args.gpus)
+    res = run_c3(args, args.steps, args.warmup, args.e2e_steps)
+    if rank != 0:
+        return
+    line = {"metric": METRIC, "value": world * res["value"], "unit": "samples/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": res["ms_per_step"], "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32+i64", "data": "synthetic (seeded)",
+            "config": {"workload": "batched: %d views (edges U{128,256,512,1024}, 1x/4x MSAA 50/50, RGBA8 + D32), "
+                                   "%d triangles (1k-200k per view, log-uniform; geodesic icospheres or random soups), "
+                                   "Gouraud, one persistent pass replayed from a CUDA graph" % (res["views"], res["triangles"]),
+                       "l2": "inputs larger than L2 (no flush)", "parallelism": "single"},
+            "tris_per_s": world * res["tris_per_s"], "gpu_launches": res["kernels_per_step"] * args.steps}
+    line.update({k: res[k] for k in ("roofline", "e2e", "clocks", "plain", "small_views", "tuning", "cpu_baseline")})
+    print(json.dumps(line), flush=True)
+
+
 def run_ours(args):
     import torch
     import ifrit_gb300 as ig
@@ -268,7 +442,7 @@ def run_ours(args):
     r.set_stage_timing(False)
     out = torch.empty(w["W"] * w["H"], dtype=torch.int32, pin_memory=True).numpy()
     e2e_times = []
-    for i in range(args.e2e_steps + 2):
+    for i in range(max(1, args.e2e_steps) + 2):
         t0 = time.perf_counter()
         r.mark_geometry_dirty()
         r.draw(clear=True)
@@ -306,13 +480,18 @@ def run_ours(args):
         "e2e": {"value": world * shaded / e2e_s, "unit": "samples/s",
                 "h2d_bytes_per_step": int(w["vertices"].nbytes + w["indices"].nbytes),
                 "d2h_bytes_per_step": int(out.nbytes), "ms_per_step": 1000.0 * e2e_s},
-        "gpu_launches": 4 * args.steps,
+        "gpu_launches": KERNELS_PER_PASS * args.steps,
         "clocks": clk,
     }
     nthreads = os.cpu_count() or 1
     t_cpu, shaded_cpu = cpu_oracle_frame(w, nthreads, frames=2)
     line["cpu_baseline"] = {"value": shaded_cpu / t_cpu, "unit": "samples/s", "cores": nthreads, "kind": "port",
                             "sample": "one full frame of the same workload (median of 2)"}
+    if args.workload == "c2" and not args.no_batch and world == 1:
+        r.close()
+        res = run_c3(args, 5, 3, 3, with_cpu=False)
+        line["batched_c3"] = {k: res[k] for k in ("value", "ms_per_step", "tris_per_s", "views", "triangles", "tuning",
+                                                   "plain", "small_views", "roofline", "e2e")}
     print(json.dumps(line), flush=True)
     if dist:
         dist.barrier()
@@ -323,6 +502,8 @@ def main():
     args = parse()
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload == "c3":
+        run_ours_c3(args)
     else:
         run_ours(args)
 

@@ -131,8 +131,8 @@ uint64_t g_id_counter = 1;
 // Device scratch and pinned descriptor staging of a pass.  Buffers grow on demand; each growth
 // bumps `generation`, which invalidates CUDA graphs captured with the old addresses.
 struct PassScratch {
-    DevMem tile_count, tile_offset, tile_cursor, pairs, records, status, draws, draw_start, views, view_tiles, queues,
-        entries;
+    DevMem tile_count, tile_offset, tile_cursor, block_sums, pairs, records, status, draws, draw_start, views, view_tiles,
+        queues, entries;
     size_t tiles_alloc = 0;
     uint32_t pair_capacity = 0;
     uint64_t generation = 1;
@@ -141,8 +141,8 @@ struct PassScratch {
     cudaEvent_t staged = nullptr;  // recorded after the last descriptor upload
     bool staged_pending = false;
     void release() {
-        for (DevMem* m : {&tile_count, &tile_offset, &tile_cursor, &pairs, &records, &status, &draws, &draw_start, &views,
-                          &view_tiles, &queues, &entries})
+        for (DevMem* m : {&tile_count, &tile_offset, &tile_cursor, &block_sums, &pairs, &records, &status, &draws,
+                          &draw_start, &views, &view_tiles, &queues, &entries})
             m->release();
         if (h_status) cudaFreeHost(h_status);
         h_status = nullptr;
@@ -317,6 +317,7 @@ int scratch_reserve(IfritGbRenderer* h, PassScratch& s, size_t tiles, size_t tri
         IFTR_CUDA(h, s.tile_count.reserve(n * 4));
         IFTR_CUDA(h, s.tile_offset.reserve((n + 1) * 4));
         IFTR_CUDA(h, s.tile_cursor.reserve(n * 4));
+        IFTR_CUDA(h, s.block_sums.reserve((size_t)ifr::scan_blocks((int)n) * 4));
         IFTR_CUDA(h, cudaMemsetAsync(s.tile_count.p, 0, n * 4, h->stream));  // counts start at zero
         s.tiles_alloc = n;
         s.generation++;
@@ -375,6 +376,7 @@ PassArgs make_args(const PassScratch& s, int ndraws, int total_tris, int nviews,
     a.tile_count = s.tile_count.as<uint32_t>();
     a.tile_offset = s.tile_offset.as<uint32_t>();
     a.tile_cursor = s.tile_cursor.as<uint32_t>();
+    a.block_sums = s.block_sums.as<uint32_t>();
     a.pairs = s.pairs.as<uint32_t>();
     a.records = s.records.as<ifr::TriRecord>();
     a.pair_capacity = s.pair_capacity;

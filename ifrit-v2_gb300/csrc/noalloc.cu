@@ -33,7 +33,8 @@ constexpr size_t kOffQueues = kOffViewTiles + align256(2 * sizeof(int));
 constexpr size_t kOffTileCount = kOffQueues + align256(2 * ifr::kMaxGroups * sizeof(uint32_t));
 constexpr size_t kOffTileOffset = kOffTileCount + align256((size_t)IFTR_NOALLOC_MAX_TILES * 4);
 constexpr size_t kOffTileCursor = kOffTileOffset + align256((size_t)(IFTR_NOALLOC_MAX_TILES + 1) * 4);
-constexpr size_t kOffPairs = kOffTileCursor + align256((size_t)IFTR_NOALLOC_MAX_TILES * 4);
+constexpr size_t kOffBlockSums = kOffTileCursor + align256((size_t)IFTR_NOALLOC_MAX_TILES * 4);
+constexpr size_t kOffPairs = kOffBlockSums + align256((size_t)ifr::scan_blocks(IFTR_NOALLOC_MAX_TILES) * 4);
 constexpr size_t kOffRecords = kOffPairs + align256((size_t)IFTR_NOALLOC_MAX_TILE_PAIRS * 4);
 constexpr size_t kOffEntries = kOffRecords + align256((size_t)IFTR_NOALLOC_MAX_TRIANGLES * sizeof(ifr::TriRecord));
 constexpr size_t kScratchEnd = kOffEntries + align256((size_t)IFTR_NOALLOC_MAX_SAMPLES * 4);
@@ -144,6 +145,7 @@ extern "C" IFTR_API int iftrDrawNoAlloc(const IfritGbNoAllocPass* p, void* cudaS
     a.tile_count = reinterpret_cast<uint32_t*>(base + kOffTileCount);
     a.tile_offset = reinterpret_cast<uint32_t*>(base + kOffTileOffset);
     a.tile_cursor = reinterpret_cast<uint32_t*>(base + kOffTileCursor);
+    a.block_sums = reinterpret_cast<uint32_t*>(base + kOffBlockSums);
     a.pairs = reinterpret_cast<uint32_t*>(base + kOffPairs);
     a.pair_capacity = IFTR_NOALLOC_MAX_TILE_PAIRS;
     a.records = reinterpret_cast<ifr::TriRecord*>(base + kOffRecords);

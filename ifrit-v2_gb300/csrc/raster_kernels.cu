@@ -5,7 +5,7 @@
 //                       second binners, TileRasterCoreInvocationCuda.cu:721-1339; CPU
 //                       executeBinner TileRasterWorker.cpp:314-397); unclipped triangles
 //                       leave a compact 64-byte set-up record
-//   scan_kernel         exclusive scan of the per-tile counts -> list offsets; resets counts
+//   scan_*_kernel       exclusive scan of the per-tile counts -> list offsets; resets counts
 //   bin_scatter_kernel  same overlaps (from the records), scatters entries into tile lists
 //   raster_kernel       persistent CTAs over a tile queue, one CTA per tile at a time: coverage
 //                       + early depth test of every listed triangle with order-independent
@@ -36,6 +36,18 @@ __device__ __forceinline__ int find_draw(const PassArgs& a, int g) {
     return lo;
 }
 
+// Draw of triangle g for a full warp of consecutive triangles: lane 0 searches, and lanes past
+// the end of its draw search on their own.
+__device__ __forceinline__ int find_draw_warp(const PassArgs& a, int g) {
+    int lead = 0;
+    if ((threadIdx.x & 31) == 0) lead = find_draw(a, g);
+    lead = __shfl_sync(0xffffffffu, lead, 0);
+    return (g >= __ldg(a.draw_start + lead) && g < __ldg(a.draw_start + lead + 1)) ? lead : find_draw(a, g);
+}
+
+// Draw of a binned triangle (its record holds it).
+__device__ __forceinline__ int record_draw(const PassArgs& a, int g) { return __ldg(&a.records[g].draw); }
+
 __device__ __forceinline__ void bin_sub(const PassArgs& a, const ViewArgs& v, const SubTri& s, uint32_t entry,
                                         bool scatter) {
     const int sh = v.c.tile_shift;
@@ -55,9 +67,9 @@ __device__ __forceinline__ void bin_sub(const PassArgs& a, const ViewArgs& v, co
 
 // Counting pass: full front end per triangle; unclipped triangles leave a compact record.
 __global__ void __launch_bounds__(256) bin_count_kernel(PassArgs a) {
-    int g = blockIdx.x * blockDim.x + threadIdx.x;
+    const int g = blockIdx.x * blockDim.x + threadIdx.x;
+    const int di = find_draw_warp(a, min(g, a.total_tris - 1));
     if (g >= a.total_tris) return;
-    int di = find_draw(a, g);
     const DrawDev& d = a.draws[di];
     const ViewArgs& v = a.views[d.view];
     int t = g - __ldg(a.draw_start + di);
@@ -76,6 +88,7 @@ __global__ void __launch_bounds__(256) bin_count_kernel(PassArgs a) {
         }
         TriRecord r;
         record_from_sub(s, r);
+        r.draw = di;
         const int4* src = reinterpret_cast<const int4*>(&r);
         int4* dst = reinterpret_cast<int4*>(rec);
         dst[0] = src[0]; dst[1] = src[1]; dst[2] = src[2]; dst[3] = src[3];
@@ -83,6 +96,7 @@ __global__ void __launch_bounds__(256) bin_count_kernel(PassArgs a) {
         return;
     }
     rec->flags = REC_CLIPPED;
+    rec->draw = di;
     int n = clip_polygon(v.c, poly);
     for (int i = 1; i + 1 < n; i++) {
         SubTri s;
@@ -98,7 +112,7 @@ __global__ void __launch_bounds__(256) bin_scatter_kernel(PassArgs a) {
     if (a.status[ST_OVERFLOW]) return;
     const int flags = __ldg(&a.records[g].flags);
     if (!(flags & (REC_VALID | REC_CLIPPED))) return;
-    int di = find_draw(a, g);
+    const int di = record_draw(a, g);
     const DrawDev& d = a.draws[di];
     const ViewArgs& v = a.views[d.view];
     if (flags & REC_VALID) {
@@ -117,36 +131,89 @@ __global__ void __launch_bounds__(256) bin_scatter_kernel(PassArgs a) {
     }
 }
 
-__global__ void __launch_bounds__(1024) scan_kernel(PassArgs a, int T) {
-    __shared__ uint32_t part[1024];
-    int tid = threadIdx.x;
-    int per = (T + 1023) / 1024;
-    int b = min(tid * per, T), e = min(b + per, T);
-    uint32_t sum = 0;
-    for (int i = b; i < e; i++) sum += a.tile_count[i];
-    part[tid] = sum;
+// List offsets: exclusive scan of the per-tile counts in three launches (per-CTA scans of
+// kScanTile tiles, a scan of the CTA totals, then the CTA offsets added back).  Also sets the
+// scatter cursors, clears the counts for the next pass and checks the list capacity.
+constexpr int kScanThreads = 1024;
+constexpr int kScanTile = 4 * kScanThreads;
+
+__device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t x, uint32_t* wsum, uint32_t& total) {
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    uint32_t incl = x;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        uint32_t q = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += q;
+    }
+    if (lane == 31) wsum[wid] = incl;
     __syncthreads();
-    for (int off = 1; off < 1024; off <<= 1) {
-        uint32_t v = tid >= off ? part[tid - off] : 0u;
-        __syncthreads();
-        part[tid] += v;
-        __syncthreads();
+    if (wid == 0) {
+        uint32_t w = wsum[lane];
+        uint32_t wi = w;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            uint32_t q = __shfl_up_sync(0xffffffffu, wi, o);
+            if (lane >= o) wi += q;
+        }
+        wsum[lane] = wi - w;  // exclusive prefix of the warp totals
+        if (lane == 31) wsum[32] = wi;
     }
-    uint32_t run = part[tid] - sum;
+    __syncthreads();
+    total = wsum[32];
+    return wsum[wid] + incl - x;
+}
+
+__global__ void __launch_bounds__(kScanThreads) scan_local_kernel(PassArgs a, int T) {
+    __shared__ uint32_t wsum[33];
+    const int base = blockIdx.x * kScanTile + threadIdx.x * 4;
+    uint32_t c[4];
+#pragma unroll
+    for (int i = 0; i < 4; i++) c[i] = base + i < T ? a.tile_count[base + i] : 0u;
+    uint32_t total;
+    uint32_t run = block_exclusive_scan(c[0] + c[1] + c[2] + c[3], wsum, total);
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+        if (base + i < T) a.tile_offset[base + i] = run;
+        run += c[i];
+    }
+    if (threadIdx.x == 0) a.block_sums[blockIdx.x] = total;
+}
+
+__global__ void __launch_bounds__(kScanThreads) scan_blocks_kernel(PassArgs a, int T, int nb) {
+    __shared__ uint32_t wsum[33];
+    const int per = (nb + kScanThreads - 1) / kScanThreads;
+    const int b = min((int)threadIdx.x * per, nb), e = min(b + per, nb);
+    uint32_t sum = 0;
+    for (int i = b; i < e; i++) sum += a.block_sums[i];
+    uint32_t total;
+    uint32_t run = block_exclusive_scan(sum, wsum, total);
     for (int i = b; i < e; i++) {
-        uint32_t c = a.tile_count[i];
-        a.tile_offset[i] = run;
-        a.tile_cursor[i] = run;
-        a.tile_count[i] = 0u;
-        run += c;
+        const uint32_t x = a.block_sums[i];
+        a.block_sums[i] = run;
+        run += x;
     }
-    if (tid == 1023) {
-        a.tile_offset[T] = part[1023];
-        a.status[ST_PAIRS] = part[1023];
-        atomicMax(a.status + ST_MAX_PAIRS, part[1023]);
-        if (part[1023] > a.pair_capacity) {
+    if (threadIdx.x == 0) {
+        a.tile_offset[T] = total;
+        a.status[ST_PAIRS] = total;
+        atomicMax(a.status + ST_MAX_PAIRS, total);
+        if (total > a.pair_capacity) {
             a.status[ST_OVERFLOW] = 1u;
             atomicOr(a.status + ST_STICKY, 1u);
+        }
+    }
+}
+
+__global__ void __launch_bounds__(kScanThreads) scan_apply_kernel(PassArgs a, int T) {
+    const uint32_t add = a.block_sums[blockIdx.x];
+    const int base = blockIdx.x * kScanTile + threadIdx.x * 4;
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+        const int t = base + i;
+        if (t < T) {
+            const uint32_t off = a.tile_offset[t] + add;
+            a.tile_offset[t] = off;
+            a.tile_cursor[t] = off;
+            a.tile_count[t] = 0u;
         }
     }
 }
@@ -264,7 +331,7 @@ struct RecordPlane {
 // Set-up of entry e (global triangle << 3 | fan index) for shading: geometry + depth plane.
 __device__ __noinline__ void setup_entry(const PassArgs& a, const PassConst& c, int e, ShadeGeom* g, RecordPlane* pl) {
     int gi = e >> 3, sub = e & 7;
-    int di = find_draw(a, gi);
+    int di = record_draw(a, gi);
     SubTri s;
     setup_entry_sub(c, a.draws[di], a.records, gi, gi - __ldg(a.draw_start + di), sub, s);
     shade_geom_from(s, *g);
@@ -278,7 +345,7 @@ __device__ __noinline__ void setup_entry(const PassArgs& a, const PassConst& c, 
 // Raster set-up of entry e for the batch phase (out of line: one copy of the clip path).
 __device__ __noinline__ bool setup_raster_entry(const PassArgs& a, const PassConst& c, uint32_t e, SubTri* s, int* draw) {
     int g = (int)(e >> 3), sub = (int)(e & 7u);
-    int di = find_draw(a, g);
+    int di = record_draw(a, g);
     *draw = di;
     return setup_entry_sub(c, a.draws[di], a.records, g, g - __ldg(a.draw_start + di), sub, *s);
 }
@@ -289,7 +356,7 @@ __device__ __noinline__ void shade_uncached(const PassArgs& a, const PassConst& 
     ShadeGeom g;
     setup_entry(a, c, e, &g, pl);
     int gi = e >> 3, sub = e & 7;
-    int di = find_draw(a, gi);
+    int di = record_draw(a, gi);
     shade_fragment(c, a.draws[di], g, gi - __ldg(a.draw_start + di), sub, px, py, col);
 }
 
@@ -512,12 +579,13 @@ __global__ void __launch_bounds__(TS * TS) raster_kernel(PassArgs a, GroupArgs g
 // binner's record, quad derivatives, texture filtering), then the samples are resolved on chip
 // and depth, visibility and the resolved colour stored once.
 template <int S, int TS>
-__device__ __forceinline__ void shade_tile(const PassArgs& a, const ViewArgs& v, int gtile, float4 (*scol)[TS * TS]) {
+__device__ __forceinline__ void shade_tile(const PassArgs& a, const ViewArgs& v, int gtile, int part,
+                                           float4 (*scol)[TS * TS]) {
     const int ltile = gtile - v.tile_start;
     const int tx = ltile % v.c.tiles_x, ty = ltile / v.c.tiles_x;
     const int tid = threadIdx.x;
     int lx, ly;
-    tile_pixel<TS>(tid, lx, ly);
+    tile_pixel<TS>(part * 32 + (tid & 31), lx, ly);
     const int px = tx * TS + lx, py = ty * TS + ly;
     const bool inpix = px < v.c.W && py < v.c.H;
     const size_t pix = (size_t)py * v.c.W + px;
@@ -574,7 +642,7 @@ __device__ __forceinline__ void shade_tile(const PassArgs& a, const ViewArgs& v,
             if (j == i) e = uniq[j];
         if (i < nu) {
             const int g = e >> 3, sub = e & 7;
-            const int di = find_draw(a, g);
+            const int di = record_draw(a, g);
             const DrawDev& d = a.draws[di];
             const int t = g - __ldg(a.draw_start + di);
             SubTri st;
@@ -643,14 +711,35 @@ __device__ __forceinline__ void shade_tile(const PassArgs& a, const ViewArgs& v,
     }
 }
 
+// Persistent warps: each warp pulls 32-pixel tasks (8 quads of one tile) from the group's
+// queue on its own, so a warp that finishes early starts its next task instead of waiting at a
+// tile barrier.  View arguments are read through L1 from the descriptor array.
 template <int S, int TS>
 __global__ void __launch_bounds__(TS * TS, 512 / (TS * TS)) shade_kernel(PassArgs a, GroupArgs g) {
     constexpr int NT = TS * TS;
+    constexpr int kTasksPerTile = NT / 32;
     __shared__ float4 scol[4][NT];  // colours of each thread's (up to 4) distinct entries
-    __shared__ ViewArgs sv;
-    __shared__ int s_tile, s_view;
-    if (threadIdx.x == 0) s_view = -1;
-    while (next_tile<NT>(a, g, 2 * g.queue + 1, sv, s_tile, s_view)) shade_tile<S, TS>(a, sv, s_tile, scol);
+    const int lane = threadIdx.x & 31;
+    const int ntasks = (g.tile_end - g.tile_begin) * kTasksPerTile;
+    for (;;) {
+        int task = 0, vi = 0;
+        if (lane == 0) {
+            task = (int)atomicAdd(a.queues + 2 * g.queue + 1, 1u);
+            if (task < ntasks) {
+                const int t = g.tile_begin + task / kTasksPerTile;
+                int lo = g.view_begin, hi = g.view_end - 1;
+                while (lo < hi) {
+                    int mid = (lo + hi + 1) >> 1;
+                    if (__ldg(a.view_tile_start + mid) <= t) lo = mid; else hi = mid - 1;
+                }
+                vi = lo;
+            }
+        }
+        task = __shfl_sync(0xffffffffu, task, 0);
+        if (task >= ntasks) break;
+        vi = __shfl_sync(0xffffffffu, vi, 0);
+        shade_tile<S, TS>(a, a.views[vi], g.tile_begin + task / kTasksPerTile, task % kTasksPerTile, scol);
+    }
 }
 
 // ---------------------------------------------------------------------------- ordered stage
@@ -988,7 +1077,10 @@ cudaError_t launch_pass(const PassArgs& a, const LaunchPlan& plan, cudaStream_t 
         int blocks = (a.total_tris + 255) / 256;
         bin_count_kernel<<<blocks, 256, 0, stream>>>(a);
         if (ev) cudaEventRecord(ev[1], stream);
-        scan_kernel<<<1, 1024, 0, stream>>>(a, T);
+        const int nb = (T + kScanTile - 1) / kScanTile;
+        scan_local_kernel<<<nb, kScanThreads, 0, stream>>>(a, T);
+        scan_blocks_kernel<<<1, kScanThreads, 0, stream>>>(a, T, nb);
+        scan_apply_kernel<<<nb, kScanThreads, 0, stream>>>(a, T);
         if (ev) cudaEventRecord(ev[2], stream);
         bin_scatter_kernel<<<blocks, 256, 0, stream>>>(a);
         if (ev) cudaEventRecord(ev[3], stream);

@@ -59,6 +59,7 @@ struct PassArgs {
     uint32_t* tile_count;    // [total_tiles], zero between passes
     uint32_t* tile_offset;   // [total_tiles + 1]
     uint32_t* tile_cursor;   // [total_tiles]
+    uint32_t* block_sums;    // [scan_blocks(total_tiles)] scan partials
     uint32_t* pairs;         // (global triangle << 3 | fan index), capacity entries
     TriRecord* records;      // [total_tris] compact set-ups written by the counting binner
     uint32_t pair_capacity;
@@ -90,6 +91,8 @@ struct LaunchPlan {
 
 // Host-callable launchers (defined in raster_kernels.cu).
 namespace ifr {
+// Entries of PassArgs::block_sums a pass over `tiles` tiles needs.
+constexpr int scan_blocks(int tiles) { return (tiles + 4095) / 4096 + 1; }
 // ev: optional array of 6 events recorded before binning, after counting, after the scan,
 // after scattering, after the raster stage and after the shade stage (per-stage timing).
 cudaError_t launch_pass(const PassArgs& a, const LaunchPlan& plan, cudaStream_t stream, cudaEvent_t* ev);

@@ -97,9 +97,10 @@ struct SubTri {
 
 // Compact set-up of an unclipped triangle, written once per triangle by the counting binner
 // and reused by the scattering binner and the tile kernel (64 bytes, four 16-byte vectors).
+// Clipped triangles keep only `flags` and `draw` (their sub-triangles are set up again).
 struct __align__(16) TriRecord {
     int32_t X0, Y0, X1, Y1;
-    int32_t X2, Y2, flags, pad0;
+    int32_t X2, Y2, flags, draw;  // draw: index of the draw the triangle belongs to
     float z0, dzdx, dzdy, iw0;
     float iw1, iw2, pad1, pad2;
 };
@@ -285,7 +286,6 @@ __device__ __forceinline__ void record_from_sub(const SubTri& s, TriRecord& r) {
     r.X0 = s.X[0]; r.Y0 = s.Y[0]; r.X1 = s.X[1]; r.Y1 = s.Y[1];
     r.X2 = s.X[2]; r.Y2 = s.Y[2];
     r.flags = REC_VALID | (s.swapped ? REC_SWAPPED : 0);
-    r.pad0 = 0;
     r.z0 = s.z[0]; r.dzdx = s.dzdx; r.dzdy = s.dzdy; r.iw0 = s.iw[0];
     r.iw1 = s.iw[1]; r.iw2 = s.iw[2]; r.pad1 = 0.0f; r.pad2 = 0.0f;
 }

@@ -102,49 +102,52 @@ def jittered_icosphere(subdivisions, seed, jitter=0.02):
     return np.concatenate([v * r, col], axis=1).astype(np.float32), f
 
 
-def geodesic_sphere(frequency, seed, displacement=0.05):
-    """Class-I geodesic icosphere of the given frequency (20 * f^2 triangles), radially
-    displaced by value noise on the sphere.  Returns (positions (V,3), uv (V,2), indices)."""
-    rng = np.random.default_rng(seed)
+def geodesic_mesh(frequency):
+    """Class-I geodesic subdivision of the icosahedron: every base face is split into
+    frequency^2 triangles and the points are pushed onto the unit sphere (20 f^2 triangles,
+    10 f^2 + 2 vertices).  Points shared by neighbouring base faces are merged."""
+    n = int(frequency)
     base_v, base_f = icosphere(0)
-    verts = {}
-    out_v = []
-    faces = []
-
-    def vid(key, p):
-        if key not in verts:
-            verts[key] = len(out_v)
-            out_v.append(p)
-        return verts[key]
-
-    n = frequency
-    for a, b, c in base_f:
-        A, B, C = base_v[a], base_v[b], base_v[c]
-        ids = {}
-        for i in range(n + 1):
-            for j in range(n + 1 - i):
-                k = n - i - j
-                p = (A * k + B * i + C * j) / n
-                # canonical key shared along edges between base faces
-                key = tuple(sorted(((a, k), (b, i), (c, j)), key=lambda x: x[0]))
-                key = tuple((vv, w) for vv, w in key if w != 0)
-                ids[(i, j)] = vid(key, p / np.linalg.norm(p))
-        for i in range(n):
-            for j in range(n - i):
-                faces.append((ids[(i, j)], ids[(i + 1, j)], ids[(i, j + 1)]))
-                if j < n - i - 1:
-                    faces.append((ids[(i + 1, j)], ids[(i + 1, j + 1)], ids[(i, j + 1)]))
-    v = np.array(out_v)
-    f = np.array(faces, np.int32)
+    ii, jj = np.meshgrid(np.arange(n + 1), np.arange(n + 1), indexing="ij")
+    keep = ii + jj <= n
+    ii, jj = ii[keep], jj[keep]
+    kk = n - ii - jj
+    local = {(a, b): t for t, (a, b) in enumerate(zip(ii.tolist(), jj.tolist()))}
+    # triangles of one face in local point numbering
+    tri = []
+    for i in range(n):
+        for j in range(n - i):
+            tri.append((local[(i, j)], local[(i + 1, j)], local[(i, j + 1)]))
+            if j < n - i - 1:
+                tri.append((local[(i + 1, j)], local[(i + 1, j + 1)], local[(i, j + 1)]))
+    tri = np.asarray(tri, np.int64)
+    A, B, C = base_v[base_f[:, 0]], base_v[base_f[:, 1]], base_v[base_f[:, 2]]
+    pts = (A[:, None, :] * kk[None, :, None] + B[:, None, :] * ii[None, :, None] + C[:, None, :] * jj[None, :, None]) / n
+    pts = pts / np.linalg.norm(pts, axis=2, keepdims=True)
+    npt = pts.shape[1]
+    allp = pts.reshape(-1, 3)
+    key = np.round(allp * (1 << 20)).astype(np.int64)
+    _, first, inv = np.unique(key, axis=0, return_index=True, return_inverse=True)
+    v = allp[first]
+    f = inv.reshape(-1)[(tri[None, :, :] + (np.arange(len(base_f)) * npt)[:, None, None]).reshape(-1, 3)]
+    f = f.astype(np.int32)
     nrm = np.cross(v[f[:, 1]] - v[f[:, 0]], v[f[:, 2]] - v[f[:, 0]])
     flip = np.einsum("ij,ij->i", nrm, v[f].mean(axis=1)) < 0
     f[flip] = f[flip][:, [0, 2, 1]]
-    # smooth radial displacement from a few random spherical waves
+    return v, f
+
+
+def geodesic_sphere(frequency, seed, displacement=0.05):
+    """Geodesic icosphere of the given frequency (20 * f^2 triangles), radially displaced by a
+    sum of random spherical waves.  Returns (positions (V,3), uv (V,2), indices)."""
+    rng = np.random.default_rng(seed)
+    v, f = geodesic_mesh(frequency)
     k = rng.normal(size=(6, 3)) * 4.0
     ph = rng.uniform(0, 2 * np.pi, size=6)
     disp = np.sin(v @ k.T + ph).mean(axis=1)
     v = v * (1.0 + displacement * disp)[:, None]
-    uv = np.stack([0.5 + np.arctan2(v[:, 2], v[:, 0]) / (2 * np.pi), 0.5 + np.arcsin(np.clip(v[:, 1] / np.linalg.norm(v, axis=1), -1, 1)) / np.pi], 1)
+    uv = np.stack([0.5 + np.arctan2(v[:, 2], v[:, 0]) / (2 * np.pi),
+                   0.5 + np.arcsin(np.clip(v[:, 1] / np.linalg.norm(v, axis=1), -1, 1)) / np.pi], 1)
     return v.astype(np.float32), uv.astype(np.float32), f
 
 
@@ -250,3 +253,31 @@ def c1_scene(seed=1):
     perspective fov 60 deg at distance 3 (512x512 target in the benchmark)."""
     v, f = jittered_icosphere(5, seed)
     return v, f, default_mvp(1.0)
+
+
+def c3_batch(seed=3, num_views=256, sizes=(128, 256, 512, 1024), tri_range=(1000, 200_000)):
+    """Batched workload: `num_views` independent square views with edge uniform in `sizes`,
+    each with one mesh of T triangles, T log-uniform in `tri_range`: a displaced geodesic
+    icosphere with per-vertex RGB (20 f^2 triangles for the f closest to T) seen from a random
+    camera, or a random-triangle soup (per-vertex UV as colour), 50/50; 1x or 4x MSAA (50/50).
+
+    Returns a list of dicts(width, height, samples, kind, vertices, indices, mvp, cull)."""
+    rng = np.random.default_rng(seed)
+    views = []
+    for i in range(num_views):
+        size = int(rng.choice(sizes))
+        S = int(rng.choice([1, 4]))
+        T = int(np.exp(rng.uniform(np.log(tri_range[0]), np.log(tri_range[1]))))
+        if rng.uniform() < 0.5:
+            f_ = max(1, int(round(math.sqrt(T / 20.0))))
+            pos, _uv, idx = geodesic_sphere(f_, 1000 + i)
+            col = rng.uniform(0, 1, size=(len(pos), 3)).astype(np.float32)
+            verts = np.concatenate([pos, col], 1).astype(np.float32)
+            mvp = orbit_camera(rng, rng.uniform(2.2, 4.0), 1.0)
+            views.append(dict(width=size, height=size, samples=S, kind="ico", vertices=verts, indices=idx, mvp=mvp,
+                              cull=2))
+        else:
+            verts, idx, mvp = triangle_soup(T, 2000 + i, size, size)
+            views.append(dict(width=size, height=size, samples=S, kind="soup", vertices=verts, indices=idx, mvp=mvp,
+                              cull=0))
+    return views
