@@ -49,7 +49,7 @@ def parse():
     p.add_argument("--steps", type=int, default=20)
     p.add_argument("--warmup", type=int, default=5)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    p.add_argument("--workload", default="c2", choices=["c1", "c2", "c3"])
+    p.add_argument("--workload", default="c2", choices=["c1", "c2", "c3", "c4"])
     p.add_argument("--e2e-steps", type=int, default=10)
     p.add_argument("--no-batch", action="store_true", help="leave the batched (c3) summary out of the c2 line")
     return p.parse_args()
@@ -368,6 +368,121 @@ def run_c3(args, steps, warmup, e2e_steps, with_cpu=True):
     return out
 
 
+def run_c4(steps, warmup, with_cpu=True):
+    """Differentiable workload: 64 views at 256x256 float32 RGB of a 20,480-triangle icosphere
+    (per-vertex colours, UVs, positions with noise std 0.05), 256x256 float32 texture, L2 loss
+    against images of the clean positions.  Times the forward (visibility + shading +
+    antialiasing) and forward + backward per step with CUDA events, L2 flushed before each."""
+    import torch
+    from ifrit_gb300 import scenes
+    from ifrit_gb300.diff import DiffRenderer
+
+    dev = torch.device("cuda", torch.cuda.current_device())
+    stream = torch.cuda.current_stream(dev)
+    sc = scenes.c4_scene()
+    dr = DiffRenderer(sc["faces"], len(sc["clean"]), sc["width"], sc["height"], sc["mvps"], sc["texture"])
+    t = {k: torch.from_numpy(sc[k]).to(dev) for k in ("clean", "noisy", "colors", "uvs")}
+    with torch.no_grad():
+        target = dr.forward(t["clean"], t["colors"], t["uvs"])[0]
+    pos = t["noisy"].clone().requires_grad_(True)
+    col = t["colors"].clone().requires_grad_(True)
+    uv = t["uvs"].clone().requires_grad_(True)
+    flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device=dev)
+
+    def fwd():
+        with torch.no_grad():
+            return dr.render(pos, col, uv)
+
+    def fwd_bwd():
+        pos.grad = col.grad = uv.grad = None
+        loss = ((dr.render(pos, col, uv) - target) ** 2).sum()
+        loss.backward()
+        return loss
+
+    def timed(fn):
+        for _ in range(warmup):
+            fn()
+        torch.cuda.synchronize()
+        ms = []
+        for i in range(steps):
+            flush.fill_(i & 255)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            fn()
+            e1.record(stream)
+            torch.cuda.synchronize()
+            ms.append(e0.elapsed_time(e1))
+        return statistics.mean(ms)
+
+    clocks = ClockSampler()
+    clocks.start()
+    ms_f = timed(fwd)
+    ms_fb = timed(fwd_bwd)
+    clk = clocks.stop(torch.cuda.current_device())
+    vis = dr.forward(t["noisy"], t["colors"], t["uvs"])[2]
+    covered = int((vis >= 0).sum().item())
+    N, H, W = dr.N, dr.H, dr.W
+    out = {"views": N, "width": W, "height": H, "triangles": dr.T, "ms_forward": ms_f, "ms_forward_backward": ms_fb,
+           "ratio": ms_fb / ms_f, "covered_pixels": covered, "value": covered / (ms_fb / 1000.0),
+           "forward_samples_per_s": covered / (ms_f / 1000.0), "clocks": clk,
+           # per step: rasterizer (3 binning + raster + shade), diff shade + antialias, adjoint
+           "kernels_forward": 7, "kernels_forward_backward": 8}
+    dr.close()
+    if with_cpu:
+        # the FP64 CPU restatement (forward + adjoint) on 4 of the views, and the GPU gradients
+        # of the same 4 views against it
+        from oracle import diff_oracle as D
+        nv = 4
+        sub = DiffRenderer(sc["faces"], len(sc["clean"]), W, H, sc["mvps"][:nv], sc["texture"])
+        with torch.no_grad():
+            tg = sub.forward(t["clean"], t["colors"], t["uvs"])[0]
+        p2, c2, u2 = (x.clone().requires_grad_(True) for x in (t["noisy"], t["colors"], t["uvs"]))
+        ((sub.render(p2, c2, u2) - tg) ** 2).sum().backward()
+        _, _, vis4, codes4 = sub.forward(t["noisy"], t["colors"], t["uvs"])
+        args = (sc["noisy"], sc["colors"], sc["uvs"], sc["texture"], sc["faces"], sc["mvps"][:nv], vis4.cpu().numpy(),
+                codes4.cpu().numpy())
+        t0 = time.perf_counter()
+        _, gp, gc, gu, _ = D.loss_and_grads(*args, tg.cpu().numpy())
+        cpu_s = time.perf_counter() - t0
+        with torch.no_grad():
+            upstream = (2 * (sub.forward(t["noisy"], t["colors"], t["uvs"])[0] - tg)).cpu().numpy()
+        ap, ac, au = D.adjoint(*args, upstream)
+        err = lambda g, r: float(np.abs(g.grad.cpu().numpy() - r).max() / max(np.abs(r).max(), 1e-30))
+        out["grad_error_vs_fp64"] = {
+            "adjoint": {"positions": err(p2, ap), "colors": err(c2, ac), "uvs": err(u2, au)},
+            "end_to_end": {"positions": err(p2, gp), "colors": err(c2, gc), "uvs": err(u2, gu)},
+            "views": nv, "metric": "max |g_gpu - g_fp64| / max |g_fp64|; adjoint: same dL/dimage on both sides, "
+                                   "end_to_end: each side from its own forward"}
+        cov4 = int((vis4 >= 0).sum().item())
+        out["cpu_baseline"] = {"value": cov4 / cpu_s, "unit": "samples/s", "cores": torch.get_num_threads(),
+                               "kind": "port", "sample": "FP64 forward + adjoint (torch CPU) of 4 of the 64 views"}
+        sub.close()
+    return out
+
+
+def run_ours_c4(args):
+    rank, world, dist = dist_setup(args.gpus)
+    res = run_c4(args.steps, args.warmup)
+    if rank != 0:
+        return
+    line = {"metric": "covered samples/s through forward + backward", "value": world * res["value"],
+            "unit": "samples/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": res["ms_forward_backward"], "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
+            "config": {"workload": "differentiable: %d views %dx%d float32 RGB, %d-triangle icosphere (colours, UVs, "
+                                   "positions with noise std 0.05), 256^2 float32 texture, L2 loss; forward = visibility "
+                                   "+ shading + silhouette antialiasing, backward = hand-written adjoint"
+                                   % (res["views"], res["width"], res["height"], res["triangles"]),
+                       "l2": "flushed before every timed step (256 MB write)", "parallelism": "single"},
+            "ms_forward": res["ms_forward"], "fwd_bwd_over_fwd": res["ratio"],
+            "gpu_launches": res["kernels_forward_backward"] * args.steps, "clocks": res["clocks"],
+            "e2e": None}
+    for k in ("grad_error_vs_fp64", "cpu_baseline"):
+        if k in res:
+            line[k] = res[k]
+    print(json.dumps(line), flush=True)
+
+
 def run_ours_c3(args):
     rank, world, dist = dist_setup(args.gpus)
     res = run_c3(args, args.steps, args.warmup, args.e2e_steps)
@@ -492,6 +607,9 @@ def run_ours(args):
         res = run_c3(args, 5, 3, 3, with_cpu=False)
         line["batched_c3"] = {k: res[k] for k in ("value", "ms_per_step", "tris_per_s", "views", "triangles", "tuning",
                                                    "plain", "small_views", "roofline", "e2e")}
+        res4 = run_c4(5, 3, with_cpu=False)
+        line["differentiable_c4"] = {k: res4[k] for k in ("views", "width", "height", "triangles", "ms_forward",
+                                                          "ms_forward_backward", "ratio", "value")}
     print(json.dumps(line), flush=True)
     if dist:
         dist.barrier()
@@ -504,6 +622,8 @@ def main():
         run_reference(args)
     elif args.workload == "c3":
         run_ours_c3(args)
+    elif args.workload == "c4":
+        run_ours_c4(args)
     else:
         run_ours(args)
 

@@ -44,6 +44,7 @@ EXPORTED = [
     "ifbufBufferData", "iftrSetStageTiming", "iftrGetStageTimes", "iftrGetVertexBufferRawData",
     "iftrSetVertexBufferDirty", "ifbufGetBufferRawData", "ifbufSetBufferDirty", "iftrDrawNoAlloc",
     "iftrBeginPass", "iftrPassDraw", "iftrEndPass", "iftrDrawBatch", "iftrSetBatchTuning", "iftrGetBatchTuning",
+    "iftrDiffForward", "iftrDiffBackward",
 ]
 
 
@@ -90,6 +91,18 @@ class BatchDraw(ctypes.Structure):
                 ("cullMode", ctypes.c_int), ("frontCounterClockwise", ctypes.c_int), ("shadingModel", ctypes.c_int),
                 ("blend", BlendState), ("texels", ctypes.c_void_p), ("texWidth", ctypes.c_int),
                 ("texHeight", ctypes.c_int), ("texLevels", ctypes.c_int), ("sampler", SamplerState)]
+
+
+class DiffPass(ctypes.Structure):
+    """IfritGbDiffPass (include/ifrit_gb300.h)."""
+    _fields_ = [("numViews", ctypes.c_int), ("width", ctypes.c_int), ("height", ctypes.c_int),
+                ("mvp", ctypes.c_void_p), ("positions", ctypes.c_void_p), ("colors", ctypes.c_void_p),
+                ("uvs", ctypes.c_void_p), ("faces", ctypes.c_void_p), ("neighbors", ctypes.c_void_p),
+                ("numVertices", ctypes.c_int), ("numTriangles", ctypes.c_int), ("texture", ctypes.c_void_p),
+                ("texWidth", ctypes.c_int), ("texHeight", ctypes.c_int), ("visibility", ctypes.c_void_p),
+                ("shaded", ctypes.c_void_p), ("image", ctypes.c_void_p), ("aaCodes", ctypes.c_void_p),
+                ("gradImage", ctypes.c_void_p), ("gradPositions", ctypes.c_void_p), ("gradColors", ctypes.c_void_p),
+                ("gradUvs", ctypes.c_void_p)]
 
 
 class Stats(ctypes.Structure):
@@ -151,6 +164,7 @@ def load(build_if_missing=True):
         "iftrDrawBatch": [vp, ctypes.POINTER(BatchView), ip, ctypes.POINTER(BatchDraw), ip],
         "iftrSetBatchTuning": [vp, ip, ip, ip],
         "iftrGetBatchTuning": [vp, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)],
+        "iftrDiffForward": [ctypes.POINTER(DiffPass), vp], "iftrDiffBackward": [ctypes.POINTER(DiffPass), vp],
     }
     for name, args in sig.items():
         getattr(lib, name).argtypes = args

@@ -57,12 +57,19 @@ class BatchRenderer:
 
     # ---- description
     def add_view(self, width, height, samples=1, fmt=FORMAT_RGBA8, visibility=False, clear=True,
-                 clear_color=(0.0, 0.0, 0.0, 0.0), clear_depth=1.0):
+                 clear_color=(0.0, 0.0, 0.0, 0.0), clear_depth=1.0, targets=None):
+        """targets: optional dict of caller-owned CUDA tensors (color, depth, vis) to render into."""
         torch = self.torch
         shape, dt = _color_shape(fmt, height, width)
-        t = {"color": torch.zeros(shape, dtype=dt, device=self.device),
-             "depth": torch.full((height, width, samples), float(clear_depth), dtype=torch.float32, device=self.device),
-             "vis": torch.full((height, width, samples), -1, dtype=torch.int32, device=self.device) if visibility else None}
+        if targets is not None:
+            t = dict(targets)
+            visibility = t.get("vis") is not None
+        else:
+            t = {"color": torch.zeros(shape, dtype=dt, device=self.device),
+                 "depth": torch.full((height, width, samples), float(clear_depth), dtype=torch.float32,
+                                     device=self.device),
+                 "vis": torch.full((height, width, samples), -1, dtype=torch.int32, device=self.device)
+                 if visibility else None}
         v = BatchView()
         v.width, v.height, v.samples, v.colorFormat = width, height, samples, fmt
         v.color, v.depth = t["color"].data_ptr(), t["depth"].data_ptr()

@@ -13,8 +13,8 @@ ROOT = os.path.dirname(PKG)
 CSRC = os.path.join(ROOT, "csrc")
 BUILD = os.path.join(ROOT, "_build")
 LIB = os.path.join(PKG, "libifrit_gb300.so")
-SOURCES = ["raster_kernels.cu", "capi.cu", "noalloc.cu"]
-HEADERS = ["raster_math.cuh", "raster_kernels.cuh", os.path.join("..", "..", "include", "ifrit_gb300.h")]
+SOURCES = ["raster_kernels.cu", "capi.cu", "noalloc.cu", "diff_kernels.cu"]
+HEADERS = ["raster_math.cuh", "raster_kernels.cuh", "pass_plan.h", os.path.join("..", "..", "include", "ifrit_gb300.h")]
 NVCC = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc")
 FLAGS = ["-std=c++17", "-O3", "-gencode", "arch=compute_103a,code=sm_103a", "-lineinfo", "--fmad=false",
          "-Xcompiler", "-fPIC,-fvisibility=hidden", "-Xptxas", "-v"]

@@ -281,3 +281,24 @@ def c3_batch(seed=3, num_views=256, sizes=(128, 256, 512, 1024), tri_range=(1000
             views.append(dict(width=size, height=size, samples=S, kind="soup", vertices=verts, indices=idx, mvp=mvp,
                               cull=0))
     return views
+
+
+def c4_scene(seed=4, num_views=64, size=256, subdivisions=5, noise=0.05, tex_size=256):
+    """Differentiable workload: an icosphere (subdivision 5: 20,480 triangles) with per-vertex
+    RGB colours U[0, 1] and spherical UVs, seen by `num_views` random cameras at distance 3;
+    `clean` positions render the target images, `noisy` positions (Gaussian noise of std
+    `noise`) are the parameters; float32 RGB value-noise texture of `tex_size`^2.
+
+    Returns dict(clean, noisy, colors, uvs, faces, texture, mvps, width, height)."""
+    rng = np.random.default_rng(seed)
+    v, f = icosphere(subdivisions)
+    clean = v.astype(np.float32)
+    noisy = (v + noise * rng.normal(size=v.shape)).astype(np.float32)
+    colors = rng.uniform(0.0, 1.0, size=(len(v), 3)).astype(np.float32)
+    uvs = np.stack([0.5 + np.arctan2(v[:, 2], v[:, 0]) / (2 * np.pi),
+                    0.5 + np.arcsin(np.clip(v[:, 1], -1, 1)) / np.pi], 1).astype(np.float32)
+    t8 = value_noise_texture(tex_size, seed)
+    texture = np.stack([(t8 >> (8 * c)) & 255 for c in range(3)], -1).astype(np.float32) / 255.0
+    mvps = np.stack([orbit_camera(rng, 3.0, 1.0) for _ in range(num_views)]).astype(np.float32)
+    return dict(clean=clean, noisy=noisy, colors=colors, uvs=uvs, faces=f.astype(np.int32), texture=texture,
+                mvps=mvps, width=size, height=size)

@@ -253,6 +253,38 @@ IFTR_API int iftrDrawBatch(IfritGbRenderer* h, const IfritGbBatchView* views, in
 IFTR_API int iftrSetBatchTuning(IfritGbRenderer* h, int autotune, int tileSize, int ctasPerSm);
 IFTR_API int iftrGetBatchTuning(IfritGbRenderer* h, int* tileSize, int* ctasPerSm);
 
+/* ---- differentiable shading (no counterpart in the reference)
+ * Shading and silhouette antialiasing of many views of one triangle mesh over visibility
+ * buffers produced by iftrDrawBatch (1x, one triangle id per pixel), and the adjoint of both.
+ * Forward: perspective-correct barycentrics from the triangle id, colour * bilinear texture(uv)
+ * per pixel (`shaded`), then every horizontally or vertically adjacent pixel pair across a
+ * silhouette edge of the nearer triangle is blended by how far the edge reaches past the pixel
+ * boundary (`image`; decisions in `aaCodes`).  Backward: gradients of a loss with respect to
+ * per-vertex positions, colours and UVs, given dL/dimage; they are added to the gradient
+ * buffers (zero them first).  Both calls are asynchronous on `cudaStream`. */
+typedef struct {
+    int numViews, width, height;
+    const float* mvp;               /* device [numViews][16], row-major */
+    const float* positions;         /* device [numVertices][3] */
+    const float* colors;            /* device [numVertices][3] */
+    const float* uvs;               /* device [numVertices][2] */
+    const int* faces;               /* device [numTriangles][3] */
+    const int* neighbors;           /* device [numTriangles][3]: triangle across the edge opposite vertex k, or -1 */
+    int numVertices, numTriangles;
+    const float* texture;           /* device [texHeight][texWidth][3], repeat addressing, bilinear */
+    int texWidth, texHeight;
+    const int* visibility;          /* device [numViews][height][width]: triangle id or -1 */
+    float* shaded;                  /* device [numViews][height][width][3], before antialiasing */
+    float* image;                   /* device [numViews][height][width][3], forward output */
+    signed char* aaCodes;           /* device [numViews][height][width][2], antialiasing decisions */
+    const float* gradImage;         /* device [numViews][height][width][3], dL/dimage (backward) */
+    float* gradPositions;           /* device [numVertices][3] (backward, accumulated) */
+    float* gradColors;              /* device [numVertices][3] (backward, accumulated) */
+    float* gradUvs;                 /* device [numVertices][2] (backward, accumulated) */
+} IfritGbDiffPass;
+IFTR_API int iftrDiffForward(const IfritGbDiffPass* pass, void* cudaStream);
+IFTR_API int iftrDiffBackward(const IfritGbDiffPass* pass, void* cudaStream);
+
 /* ---- framebuffers and images (ECE:31-40, CE:25-31) */
 IFTR_API IfritGbFrameBuffer* iftrCreateFrameBuffer(void);                            /* ECE:31 */
 IFTR_API int iftrDestroyFrameBuffer(IfritGbFrameBuffer* fb);                         /* ECE:33 */
