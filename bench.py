@@ -49,7 +49,7 @@ def parse():
     p.add_argument("--steps", type=int, default=20)
     p.add_argument("--warmup", type=int, default=5)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    p.add_argument("--workload", default="c2", choices=["c1", "c2", "c3", "c4"])
+    p.add_argument("--workload", default="c2", choices=["c1", "c2", "c3", "c4", "c5"])
     p.add_argument("--e2e-steps", type=int, default=10)
     p.add_argument("--no-batch", action="store_true", help="leave the batched (c3) summary out of the c2 line")
     return p.parse_args()
@@ -483,6 +483,116 @@ def run_ours_c4(args):
     print(json.dumps(line), flush=True)
 
 
+def c5_pass(r, sc, ig):
+    """Records and runs the stress pass: opaque instances, then the blended ones back to front."""
+    r.begin_pass(clear=True)
+    for d in sc["draws"]:
+        r.set_state(cull=ig.CULL_BACK, depth_func=ig.LESS_OR_EQUAL, depth_write=not d["blend"], shading=ig.FS_TEXTURED)
+        r.set_blend(d["blend"], 6, 7, 1, 7)  # SRC_ALPHA, ONE_MINUS_SRC_ALPHA; alpha ONE, ONE_MINUS_SRC_ALPHA
+        r.set_mvp(d["mvp"])
+        r.pass_draw(d["first"], d["count"])
+    r.end_pass()
+
+
+def c5_algorithmic_bytes(sc):
+    """Vertices and indices read once, per-sample depth (8x) and resolved RGBA16F written once,
+    the texture's mip chain read once, and the resolved colour of the blended instances' pixels
+    read back once (counted as the whole target)."""
+    P = sc["width"] * sc["height"]
+    n, total = sc["texture"].shape[0], 0
+    while True:
+        total += n * n
+        if n == 1:
+            break
+        n = (n + 1) >> 1
+    return int(sc["vertices"].nbytes + sc["indices"].nbytes + P * 8 * 4 + P * 8 + total * 4 + P * 8)
+
+
+def run_ours_c5(args):
+    import torch
+    import ifrit_gb300 as ig
+    from ifrit_gb300 import scenes
+
+    rank, world, dist = dist_setup(args.gpus)
+    dev = torch.device("cuda", torch.cuda.current_device())
+    stream = torch.cuda.current_stream(dev)
+    sc = scenes.c5_scene()
+    W, H = sc["width"], sc["height"]
+    r = ig.Renderer(W, H, 8, ig.FORMAT_RGBA16F, visibility=True)
+    r.set_stream(stream.cuda_stream)
+    r.set_geometry(sc["vertices"], sc["indices"], 2)
+    r.set_texture(sc["texture"], max_aniso=16)
+    c5_pass(r, sc, ig)
+    shaded = int((r.visibility() >= 0).sum())
+    r.lib.iftrSetVisibilityOutput(r.h, 0)
+    r.set_stage_timing(True)
+    for _ in range(args.warmup):
+        c5_pass(r, sc, ig)
+    clocks = ClockSampler()
+    clocks.start()
+    ms, stages = [], []
+    for _ in range(args.steps):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        c5_pass(r, sc, ig)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms.append(e0.elapsed_time(e1))
+        stages.append(r.stage_times())
+    clk = clocks.stop(torch.cuda.current_device())
+    r.set_stage_timing(False)
+    out = torch.empty((H, W), dtype=torch.int64, pin_memory=True).numpy()
+    e2e = []
+    for i in range(max(1, args.e2e_steps) + 1):
+        t0 = time.perf_counter()
+        r.mark_geometry_dirty()
+        c5_pass(r, sc, ig)
+        r.color_into(out)
+        if i:
+            e2e.append(time.perf_counter() - t0)
+    m = statistics.mean(ms)
+    B = c5_algorithmic_bytes(sc)
+    peak, peak_kind = peak_hbm()
+    st = [statistics.mean(x[i] for x in stages) for i in range(5)]
+    T = len(sc["indices"])
+    line = {"metric": METRIC, "value": world * shaded / (m / 1000.0), "unit": "samples/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": m, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32+i64", "data": "synthetic (seeded)",
+            "config": {"workload": "stress: 3840x2160 RGBA16F + D32 LEQUAL, 8x MSAA, %d triangles from 40 displaced "
+                                   "geodesic icospheres (frequency 112) with random transforms, depth complexity ~8, "
+                                   "4096^2 RGBA8 texture with full mips, 16x anisotropic, 4 of 40 instances "
+                                   "alpha-blended back to front (one ordered pass)" % T,
+                       "width": W, "height": H, "samples": 8, "triangles": T, "shaded_samples_per_frame": shaded,
+                       "l2": "inputs larger than L2 (no flush)", "parallelism": "single"},
+            "tris_per_s": T / (m / 1000.0),
+            "stage_ms": {"binning": st[0] + st[1] + st[2], "ordered_tiles": st[3]},
+            "roofline": {"bound": "hbm", "achieved": B / (m / 1000.0) / 1e9, "peak": peak, "unit": "GB/s",
+                         "frac": B / (m / 1000.0) / 1e9 / peak, "traffic": None, "algorithmic_bytes": B,
+                         "kernel": "whole pass", "peak_source": peak_kind},
+            "e2e": {"value": shaded / statistics.mean(e2e), "unit": "samples/s",
+                    "h2d_bytes_per_step": int(sc["vertices"].nbytes + sc["indices"].nbytes),
+                    "d2h_bytes_per_step": int(out.nbytes), "ms_per_step": 1000.0 * statistics.mean(e2e)},
+            "gpu_launches": 4 * args.steps, "clocks": clk}
+    r.close()
+    # CPU oracle on a bounded sample: the first two instances of the pass at full resolution
+    from oracle import oracle as O
+    chain, levels = O.build_mips(sc["texture"])
+    tex = (chain, levels, sc["texture"].shape[1], sc["texture"].shape[0])
+    draws = []
+    for d in sc["draws"][:2]:
+        f = sc["indices"][d["first"] // 3:(d["first"] + d["count"]) // 3]
+        draws.append(O.make_draw(sc["vertices"], f, d["mvp"], attr_offset=3, attr_count=2, cull_mode=2, depth_func=3,
+                                 depth_write=int(not d["blend"]), blend=(6, 7, 1, 7) if d["blend"] else None,
+                                 shading=O.SHADE_TEXTURED, texture=tex, sampler={"max_aniso": 16}))
+    nthreads = os.cpu_count() or 1
+    t0 = time.perf_counter()
+    res = O.render(draws, W, H, 8, O.FMT_RGBA16F, nthreads=nthreads)
+    dt = time.perf_counter() - t0
+    line["cpu_baseline"] = {"value": int((res["vis"] >= 0).sum()) / dt, "unit": "samples/s", "cores": nthreads,
+                            "kind": "port", "sample": "oracle on the first 2 of the 40 instances at full resolution"}
+    print(json.dumps(line), flush=True)
+
+
 def run_ours_c3(args):
     rank, world, dist = dist_setup(args.gpus)
     res = run_c3(args, args.steps, args.warmup, args.e2e_steps)
@@ -624,6 +734,8 @@ def main():
         run_ours_c3(args)
     elif args.workload == "c4":
         run_ours_c4(args)
+    elif args.workload == "c5":
+        run_ours_c5(args)
     else:
         run_ours(args)
 

@@ -132,7 +132,7 @@ uint64_t g_id_counter = 1;
 // bumps `generation`, which invalidates CUDA graphs captured with the old addresses.
 struct PassScratch {
     DevMem tile_count, tile_offset, tile_cursor, block_sums, pairs, records, status, draws, draw_start, views, view_tiles,
-        queues, entries;
+        queues, entries, sample_colors;
     size_t tiles_alloc = 0;
     uint32_t pair_capacity = 0;
     uint64_t generation = 1;
@@ -142,7 +142,7 @@ struct PassScratch {
     bool staged_pending = false;
     void release() {
         for (DevMem* m : {&tile_count, &tile_offset, &tile_cursor, &block_sums, &pairs, &records, &status, &draws,
-                          &draw_start, &views, &view_tiles, &queues, &entries})
+                          &draw_start, &views, &view_tiles, &queues, &entries, &sample_colors})
             m->release();
         if (h_status) cudaFreeHost(h_status);
         h_status = nullptr;
@@ -201,7 +201,7 @@ struct IfritGbRenderer {
     float clear_depth = 1.0f;
     bool vis_output = false;
     // device state
-    DevMem d_vertices, d_indices, d_color, d_depth, d_vis, d_entries;
+    DevMem d_vertices, d_indices, d_color, d_depth, d_vis, d_entries, d_sample_colors;
     const void* up_vb_key = nullptr;
     uint64_t up_vb_gen = 0;
     const void* up_ib_key = nullptr;
@@ -286,7 +286,7 @@ int scratch_init(IfritGbRenderer* h, PassScratch& s) {
     std::memset(s.h_status, 0, ifr::ST_WORDS * sizeof(uint32_t));
     IFTR_CUDA(h, s.status.reserve(ifr::ST_WORDS * sizeof(uint32_t)));
     IFTR_CUDA(h, cudaMemsetAsync(s.status.p, 0, ifr::ST_WORDS * sizeof(uint32_t), h->stream));
-    IFTR_CUDA(h, s.queues.reserve(2 * ifr::kMaxGroups * sizeof(uint32_t)));
+    IFTR_CUDA(h, s.queues.reserve(3 * ifr::kMaxGroups * sizeof(uint32_t)));
     IFTR_CUDA(h, cudaEventCreateWithFlags(&s.staged, cudaEventDisableTiming));
     return IFTR_OK;
 }
@@ -552,6 +552,10 @@ int enqueue_pass(IfritGbRenderer* h, std::vector<DrawDev>& draws, int clear) {
     std::memcpy(v.clear_color, h->clear_color, sizeof(v.clear_color));
     v.clear_depth = h->clear_depth;
     ifr::set_view_depth_state(v, draws.data(), (int)draws.size());
+    if (v.ordered) {  // per-sample colours handed from the shade stage to the ordered stage
+        IFTR_CUDA(h, h->d_sample_colors.reserve((size_t)W * H * S * sizeof(float4)));
+        v.sample_colors = h->d_sample_colors.as<float4>();
+    }
     std::vector<int> view_tiles(2);
     ifr::LaunchPlan plan;
     int T = 0;
@@ -687,6 +691,8 @@ struct BatchBuild {
     std::vector<int> draw_start;
     std::vector<ifr::ViewArgs> views;
     std::vector<size_t> entry_offset;  // per internal view, ints into the entries scratch
+    std::vector<size_t> color_offset;  // per internal view, float4s into the sample colour scratch (or ~0)
+    size_t sample_colors = 0;
     std::vector<int> view_tiles;
     ifr::LaunchPlan plan;
     int total_tiles = 0;
@@ -746,8 +752,9 @@ int build_batch(IfritGbRenderer* h, const IfritGbBatchView* views, int nv, const
     out.draw_start.clear();
     out.views.clear();
     out.entry_offset.clear();
+    out.color_offset.clear();
     int64_t tri = 0;
-    size_t ent = 0;
+    size_t ent = 0, cols = 0;
     for (int k = 0; k < nv; k++) {
         const int vi = order[k];
         ifr::ViewArgs v = uv[vi];
@@ -763,13 +770,17 @@ int build_batch(IfritGbRenderer* h, const IfritGbBatchView* views, int nv, const
             tri += d.num_triangles;
         }
         out.entry_offset.push_back(ent);
-        // each view's winners start on a 256-byte boundary (the tile kernels move them as int4)
-        if (!v.ordered) ent += ((size_t)v.c.W * v.c.H * v.c.S + 63) / 64 * 64;
+        // every view gets winner scratch (a launch group that runs the raster stage writes it for
+        // all its views), each starting on a 256-byte boundary (the tile kernels move it as int4)
+        ent += ((size_t)v.c.W * v.c.H * v.c.S + 63) / 64 * 64;
+        out.color_offset.push_back(v.ordered ? cols : ~(size_t)0);
+        if (v.ordered) cols += (size_t)v.c.W * v.c.H * v.c.S;
         out.views.push_back(v);
     }
     out.draw_start.push_back((int)tri);
     out.total_tris = tri;
     out.entries = std::max<size_t>(ent, 1);
+    out.sample_colors = cols;
     out.view_tiles.assign(nv + 1, 0);
     if (!ifr::plan_groups(out.views.data(), nv, out.view_tiles.data(), h->sms, ctas_per_sm, out.plan, out.total_tiles))
         return IFTR_ERR_INVALID_ARG;
@@ -782,7 +793,15 @@ int stage_batch(IfritGbRenderer* h, BatchBuild& bb) {
     PassScratch& s = h->batch.scratch;
     int rc = scratch_reserve(h, s, (size_t)bb.total_tiles, (size_t)bb.total_tris, bb.draws.size(), bb.views.size(), bb.entries);
     if (rc) return rc;
-    for (size_t k = 0; k < bb.views.size(); k++) bb.views[k].entries = s.entries.as<int>() + bb.entry_offset[k];
+    if (bb.sample_colors * sizeof(float4) > s.sample_colors.bytes) {
+        s.generation++;  // captured graphs hold the old address
+        IFTR_CUDA(h, s.sample_colors.reserve(bb.sample_colors * sizeof(float4)));
+    }
+    for (size_t k = 0; k < bb.views.size(); k++) {
+        bb.views[k].entries = s.entries.as<int>() + bb.entry_offset[k];
+        bb.views[k].sample_colors =
+            bb.color_offset[k] == ~(size_t)0 ? nullptr : s.sample_colors.as<float4>() + bb.color_offset[k];
+    }
     if (bb.draws.empty()) bb.draws.resize(1);  // keeps the upload well-formed; ndraws stays 0
     return upload_descriptors(h, s, bb.draws, bb.draw_start, bb.views, bb.view_tiles);
 }
@@ -951,7 +970,9 @@ IFTR_API int iftrDestroyInstance(IfritGbRenderer* h) {
     if (!h) return IFTR_ERR_INVALID_ARG;
     if (h->inited) {
         cudaStreamSynchronize(h->stream);
-        for (DevMem* m : {&h->d_vertices, &h->d_indices, &h->d_color, &h->d_depth, &h->d_vis, &h->d_entries}) m->release();
+        for (DevMem* m : {&h->d_vertices, &h->d_indices, &h->d_color, &h->d_depth, &h->d_vis, &h->d_entries,
+                          &h->d_sample_colors})
+            m->release();
         h->pass.release();
         h->batch.drop_graph();
         h->batch.scratch.release();

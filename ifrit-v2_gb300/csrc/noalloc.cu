@@ -30,7 +30,7 @@ constexpr size_t kOffDrawStart = kOffDraw + align256(sizeof(ifr::DrawDev));
 constexpr size_t kOffView = kOffDrawStart + align256(2 * sizeof(int));
 constexpr size_t kOffViewTiles = kOffView + align256(sizeof(ifr::ViewArgs));
 constexpr size_t kOffQueues = kOffViewTiles + align256(2 * sizeof(int));
-constexpr size_t kOffTileCount = kOffQueues + align256(2 * ifr::kMaxGroups * sizeof(uint32_t));
+constexpr size_t kOffTileCount = kOffQueues + align256(3 * ifr::kMaxGroups * sizeof(uint32_t));
 constexpr size_t kOffTileOffset = kOffTileCount + align256((size_t)IFTR_NOALLOC_MAX_TILES * 4);
 constexpr size_t kOffTileCursor = kOffTileOffset + align256((size_t)(IFTR_NOALLOC_MAX_TILES + 1) * 4);
 constexpr size_t kOffBlockSums = kOffTileCursor + align256((size_t)IFTR_NOALLOC_MAX_TILES * 4);

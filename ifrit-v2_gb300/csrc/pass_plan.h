@@ -46,17 +46,21 @@ inline void fill_texture(DrawDev& d, const uint32_t* texels, int w, int h, int l
 
 // Depth state and path of a view from its draws: the deferred path needs one depth function
 // and write mask for the whole view and no blending or NOT_EQUAL writes; anything else runs the
-// ordered path.
+// ordered path, whose leading draws that satisfy those conditions (the order-independent prefix)
+// still go through the deferred raster stage.
+inline bool order_independent(const DrawDev& d, const DrawDev& first) {
+    return !d.blend_enable && !(d.depth_write && d.depth_func == IF_COMPARE_OP_NOT_EQUAL) &&
+           d.depth_func == first.depth_func && d.depth_write == first.depth_write;
+}
+
 inline void set_view_depth_state(ViewArgs& v, const DrawDev* draws, int n) {
     v.depth_func = n > 0 ? draws[0].depth_func : IF_COMPARE_OP_LESS;
     v.depth_write = n > 0 ? draws[0].depth_write : 1;
     v.ordered = 0;
-    for (int i = 0; i < n; i++) {
-        const DrawDev& d = draws[i];
-        if (d.blend_enable || (d.depth_write && d.depth_func == IF_COMPARE_OP_NOT_EQUAL) || d.depth_func != v.depth_func ||
-            d.depth_write != v.depth_write)
-            v.ordered = 1;
-    }
+    v.ordered_prefix = 0;
+    int i = 0;
+    while (i < n && order_independent(draws[i], draws[0])) v.ordered_prefix += draws[i++].num_triangles;
+    if (i < n) v.ordered = 1;
 }
 
 inline bool valid_samples(int S) { return S == 1 || S == 2 || S == 4 || S == 8 || S == 16; }
@@ -130,6 +134,7 @@ inline bool plan_groups(ViewArgs* v, int n, int* view_tile_start, int sms, int c
             plan.ordered[plan.ngroups] = v[i].ordered ? 1 : 0;
             plan.ngroups++;
         }
+        if (v[i].ordered && v[i].ordered_prefix > 0) plan.hybrid[plan.ngroups - 1] = 1;
         GroupArgs& g = plan.groups[plan.ngroups - 1];
         g.view_end = i + 1;
         g.tile_end = t;
@@ -138,12 +143,17 @@ inline bool plan_groups(ViewArgs* v, int n, int* view_tile_start, int sms, int c
     total_tiles = t;
     for (int k = 0; k < plan.ngroups; k++) {
         const int tiles = plan.groups[k].tile_end - plan.groups[k].tile_begin;
-        for (int stage = 0; stage < 2; stage++) {
-            const int occ = tile_kernel_occupancy(plan.samples[k], plan.tile_size[k], plan.ordered[k], stage);
-            const int per_sm = ctas_per_sm > 0 ? std::min(ctas_per_sm, occ)
-                               : ctas_per_sm < 0 ? std::max(1, occ / -ctas_per_sm)
-                                                 : occ;
-            (stage == 0 ? plan.ctas : plan.ctas_shade)[k] = std::max(1, std::min(tiles, sms * per_sm));
+        const int S = plan.samples[k], TS = plan.tile_size[k];
+        // stage kernels: raster, shade (deferred); raster, shade, ordered (hybrid); ordered (ordered)
+        const int occ_raster = tile_kernel_occupancy(S, TS, 0, 0), occ_shade = tile_kernel_occupancy(S, TS, 0, 1);
+        const int occ_ordered = plan.ordered[k] ? tile_kernel_occupancy(S, TS, 1, 0) : 1;
+        const int occ[3] = {plan.ordered[k] && !plan.hybrid[k] ? occ_ordered : occ_raster, occ_shade, occ_ordered};
+        int* out[3] = {plan.ctas, plan.ctas_shade, plan.ctas_fwd};
+        for (int stage = 0; stage < 3; stage++) {
+            const int per_sm = ctas_per_sm > 0 ? std::min(ctas_per_sm, occ[stage])
+                               : ctas_per_sm < 0 ? std::max(1, occ[stage] / -ctas_per_sm)
+                                                 : occ[stage];
+            out[stage][k] = std::max(1, std::min(tiles, sms * per_sm));
         }
     }
     return true;

@@ -446,6 +446,7 @@ __device__ __forceinline__ void raster_tile(const PassArgs& a, const ViewArgs& v
     const uint32_t beg = has_list ? a.tile_offset[gtile] : 0u;
     const uint32_t end = has_list ? a.tile_offset[gtile + 1] : 0u;
     const int xmax = min(v.c.W, tx0 + TS) - 1, ymax = min(v.c.H, ty0 + TS) - 1;
+    uint32_t ordered_left = 0;  // ordered views: entries of the tile left for the ordered stage
 
     for (uint32_t base = beg; base < end; base += NT) {
         const int nb = (int)min((uint32_t)NT, end - base);
@@ -454,7 +455,10 @@ __device__ __forceinline__ void raster_tile(const PassArgs& a, const ViewArgs& v
             uint32_t e = __ldg(a.pairs + base + tid);
             SubTri s;
             int di;
-            if (setup_raster_entry(a, v.c, e, &s, &di)) {
+            // ordered views: only the order-independent prefix is resolved here
+            const bool in_stage = !v.ordered || (int)(e >> 3) < v.first_tri + v.ordered_prefix;
+            ordered_left += in_stage ? 0u : 1u;
+            if (in_stage && setup_raster_entry(a, v.c, e, &s, &di)) {
                 int x0 = max(s.px0, tx0), x1 = min(s.px1, xmax);
                 int y0 = max(s.py0, ty0), y1 = min(s.py1, ymax);
                 if (x0 <= x1 && y0 <= y1) {
@@ -541,6 +545,19 @@ __device__ __forceinline__ void raster_tile(const PassArgs& a, const ViewArgs& v
         __syncthreads();
     }
     __syncthreads();
+    if (v.ordered) {
+        // tiles without ordered entries are finished by the shade stage; the scatter cursors are
+        // free after binning and carry the per-tile count to the later stages
+        ordered_left = __reduce_add_sync(0xffffffffu, ordered_left);
+        if (lane == 0) warp_sum[wid] = ordered_left;
+        __syncthreads();
+        if (tid == 0) {
+            uint32_t sum = 0;
+#pragma unroll
+            for (int w = 0; w < NT / 32; w++) sum += warp_sum[w];
+            a.tile_cursor[gtile] = sum;
+        }
+    }
     if (!inpix) return;
     int out[S];
 #pragma unroll
@@ -570,7 +587,7 @@ __global__ void __launch_bounds__(TS * TS) raster_kernel(PassArgs a, GroupArgs g
     __shared__ ViewArgs sv;
     __shared__ int s_tile, s_view;
     if (threadIdx.x == 0) s_view = -1;
-    while (next_tile<NT>(a, g, 2 * g.queue, sv, s_tile, s_view)) raster_tile<S, TS>(a, sv, s_tile, rec, skey, warp_sum);
+    while (next_tile<NT>(a, g, 3 * g.queue, sv, s_tile, s_view)) raster_tile<S, TS>(a, sv, s_tile, rec, skey, warp_sum);
 }
 
 // ---------------------------------------------------------------------------- shade stage
@@ -580,7 +597,7 @@ __global__ void __launch_bounds__(TS * TS) raster_kernel(PassArgs a, GroupArgs g
 // and depth, visibility and the resolved colour stored once.
 template <int S, int TS>
 __device__ __forceinline__ void shade_tile(const PassArgs& a, const ViewArgs& v, int gtile, int part,
-                                           float4 (*scol)[TS * TS]) {
+                                           float4 (*scol)[TS * TS], bool keep_samples) {
     const int ltile = gtile - v.tile_start;
     const int tx = ltile % v.c.tiles_x, ty = ltile / v.c.tiles_x;
     const int tid = threadIdx.x;
@@ -686,15 +703,18 @@ __device__ __forceinline__ void shade_tile(const PassArgs& a, const ViewArgs& v,
             }
             if (!rule.write) dep[k] = d0v;
         }
+        if (keep_samples) v.sample_colors[pix * S + k] = make_float4(c[0], c[1], c[2], c[3]);
         if (k == 0) {
             acc[0] = c[0]; acc[1] = c[1]; acc[2] = c[2]; acc[3] = c[3];
         } else {
             acc[0] = acc[0] + c[0]; acc[1] = acc[1] + c[1]; acc[2] = acc[2] + c[2]; acc[3] = acc[3] + c[3];
         }
     }
-    const float invS = 1.0f / (float)S;
-    acc[0] = acc[0] * invS; acc[1] = acc[1] * invS; acc[2] = acc[2] * invS; acc[3] = acc[3] * invS;
-    encode_color(v, pix, acc);
+    if (!keep_samples) {  // a tile with ordered entries is resolved by the ordered stage
+        const float invS = 1.0f / (float)S;
+        acc[0] = acc[0] * invS; acc[1] = acc[1] * invS; acc[2] = acc[2] * invS; acc[3] = acc[3] * invS;
+        encode_color(v, pix, acc);
+    }
 
     float* dp = v.depth + pix * S;
     if constexpr (S % 4 == 0) {
@@ -724,7 +744,7 @@ __global__ void __launch_bounds__(TS * TS, 512 / (TS * TS)) shade_kernel(PassArg
     for (;;) {
         int task = 0, vi = 0;
         if (lane == 0) {
-            task = (int)atomicAdd(a.queues + 2 * g.queue + 1, 1u);
+            task = (int)atomicAdd(a.queues + 3 * g.queue + 1, 1u);
             if (task < ntasks) {
                 const int t = g.tile_begin + task / kTasksPerTile;
                 int lo = g.view_begin, hi = g.view_end - 1;
@@ -738,7 +758,11 @@ __global__ void __launch_bounds__(TS * TS, 512 / (TS * TS)) shade_kernel(PassArg
         task = __shfl_sync(0xffffffffu, task, 0);
         if (task >= ntasks) break;
         vi = __shfl_sync(0xffffffffu, vi, 0);
-        shade_tile<S, TS>(a, a.views[vi], g.tile_begin + task / kTasksPerTile, task % kTasksPerTile, scol);
+        const int gtile = g.tile_begin + task / kTasksPerTile;
+        // tiles of ordered views with entries left for the ordered stage keep their per-sample
+        // colours for it instead of resolving
+        const bool keep = a.views[vi].ordered && __ldg(a.tile_cursor + gtile) != 0u;
+        shade_tile<S, TS>(a, a.views[vi], gtile, task % kTasksPerTile, scol, keep);
     }
 }
 
@@ -764,8 +788,11 @@ struct FwdRecords {
 
 template <int S>
 __device__ __forceinline__ void forward_tile(const PassArgs& a, const ViewArgs& v, int gtile, FwdRecords& rec,
-                                             float4* scol, uint32_t* list) {
+                                             float4* scol, uint32_t* list, bool after_raster) {
     constexpr int TS = 16, NT = kFwdThreads;
+    // after the raster and shade stages the shade stage has finished the tiles without ordered
+    // entries (uniform over the CTA)
+    if (after_raster && a.tile_cursor[gtile] == 0u) return;
     const int ltile = gtile - v.tile_start;
     const int tx = ltile % v.c.tiles_x, ty = ltile / v.c.tiles_x;
     const int tid = threadIdx.x;
@@ -788,26 +815,49 @@ __device__ __forceinline__ void forward_tile(const PassArgs& a, const ViewArgs& 
         }
 #pragma unroll
         for (int k = 0; k < S; k++) {
-            dep[k] = v.clear ? v.clear_depth : (inpix ? v.depth[pix * S + k] : 0.0f);
-            vid[k] = -1;
-            scol[k * NT + tid] = make_float4(bg[0], bg[1], bg[2], bg[3]);
+            if (after_raster) {
+                // the prefix's per-sample state as the shade stage left it: colour in the
+                // per-sample scratch, depth and primitive id in the outputs
+                const int ent = inpix ? v.entries[pix * S + k] : -1;
+                dep[k] = inpix ? v.depth[pix * S + k] : 0.0f;
+                vid[k] = ent < 0 ? -1 : (ent >> 3) - v.first_tri;
+                scol[k * NT + tid] = inpix ? v.sample_colors[pix * S + k] : make_float4(bg[0], bg[1], bg[2], bg[3]);
+            } else {
+                dep[k] = v.clear ? v.clear_depth : (inpix ? v.depth[pix * S + k] : 0.0f);
+                vid[k] = -1;
+                scol[k * NT + tid] = make_float4(bg[0], bg[1], bg[2], bg[3]);
+            }
         }
     }
     const bool has_list = a.total_tris > 0 && a.status[ST_OVERFLOW] == 0;
     const uint32_t beg = has_list ? a.tile_offset[gtile] : 0u;
     const uint32_t end = has_list ? a.tile_offset[gtile + 1] : 0u;
-    int n = (int)(end - beg);
-    if (n > kOrderedCap) {  // cannot order this tile on chip: report and leave it cleared
+    const int total = (int)(end - beg);
+    // gather the entries still to apply in order (the prefix was resolved by the raster stage)
+    const uint32_t first_ordered = (uint32_t)(v.first_tri + v.ordered_prefix);
+    __shared__ int s_count;
+    if (tid == 0) s_count = 0;
+    __syncthreads();
+    for (int i = tid; i < total; i += NT) {
+        const uint32_t e = __ldg(a.pairs + beg + i);
+        if ((e >> 3) >= first_ordered) {
+            const int at = atomicAdd(&s_count, 1);
+            if (at < kOrderedCap) list[at] = e;
+        }
+    }
+    __syncthreads();
+    int n = s_count;
+    if (n > kOrderedCap) {  // cannot order this tile on chip: report and leave it as the prefix left it
         if (tid == 0) {
             atomicOr(a.status + ST_ORDERED_LIMIT, 1u);
             atomicOr(a.status + ST_STICKY, 2u);
         }
         n = 0;
     }
-    // load and sort the tile's entries into submission order (bitonic, padded to 2^k)
+    // sort them into submission order (bitonic, padded to 2^k)
     int P = 1;
     while (P < n) P <<= 1;
-    for (int i = tid; i < P; i += NT) list[i] = i < n ? __ldg(a.pairs + beg + i) : 0xFFFFFFFFu;
+    for (int i = n + tid; i < P; i += NT) list[i] = 0xFFFFFFFFu;
     __syncthreads();
     for (int k = 2; k <= P; k <<= 1) {
         for (int j = k >> 1; j > 0; j >>= 1) {
@@ -925,7 +975,7 @@ size_t forward_smem_bytes() {
 }
 
 template <int S>
-__global__ void __launch_bounds__(kFwdThreads) forward_kernel(PassArgs a, GroupArgs g) {
+__global__ void __launch_bounds__(kFwdThreads) forward_kernel(PassArgs a, GroupArgs g, int qslot, int after_raster) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     FwdRecords& rec = *reinterpret_cast<FwdRecords*>(smem_raw);
     float4* scol = reinterpret_cast<float4*>(smem_raw + sizeof(FwdRecords));  // [S][256]
@@ -933,7 +983,8 @@ __global__ void __launch_bounds__(kFwdThreads) forward_kernel(PassArgs a, GroupA
     __shared__ ViewArgs sv;
     __shared__ int s_tile, s_view;
     if (threadIdx.x == 0) s_view = -1;
-    while (next_tile<kFwdThreads>(a, g, 2 * g.queue, sv, s_tile, s_view)) forward_tile<S>(a, sv, s_tile, rec, scol, list);
+    while (next_tile<kFwdThreads>(a, g, qslot, sv, s_tile, s_view))
+        forward_tile<S>(a, sv, s_tile, rec, scol, list, after_raster != 0);
 }
 
 // ---------------------------------------------------------------------------- mips
@@ -989,10 +1040,10 @@ cudaError_t launch_deferred(const PassArgs& a, const GroupArgs& g, int ctas, cud
 }
 
 template <int S>
-cudaError_t launch_forward(const PassArgs& a, const GroupArgs& g, int ctas, cudaStream_t stream) {
+cudaError_t launch_forward(const PassArgs& a, const GroupArgs& g, int ctas, cudaStream_t stream, int qslot) {
     cudaError_t e = configure_forward<S>();
     if (e != cudaSuccess) return e;
-    forward_kernel<S><<<ctas, kFwdThreads, forward_smem_bytes<S>(), stream>>>(a, g);
+    forward_kernel<S><<<ctas, kFwdThreads, forward_smem_bytes<S>(), stream>>>(a, g, qslot, qslot % 3 == 2);
     return cudaSuccess;
 }
 
@@ -1016,13 +1067,17 @@ cudaError_t launch_group_stage(const PassArgs& a, const GroupArgs& g, int S, int
     }
 }
 
-cudaError_t launch_group_forward(const PassArgs& a, const GroupArgs& g, int S, int ctas, cudaStream_t stream) {
+// The ordered stage of a group; `second` when it follows the group's raster stage (its queue
+// counter is then the group's second one).
+cudaError_t launch_group_forward(const PassArgs& a, const GroupArgs& g, int S, int ctas, cudaStream_t stream,
+                                 bool second) {
+    const int q = 3 * g.queue + (second ? 2 : 0);
     switch (S) {
-    case 1: return launch_forward<1>(a, g, ctas, stream);
-    case 2: return launch_forward<2>(a, g, ctas, stream);
-    case 4: return launch_forward<4>(a, g, ctas, stream);
-    case 8: return launch_forward<8>(a, g, ctas, stream);
-    case 16: return launch_forward<16>(a, g, ctas, stream);
+    case 1: return launch_forward<1>(a, g, ctas, stream, q);
+    case 2: return launch_forward<2>(a, g, ctas, stream, q);
+    case 4: return launch_forward<4>(a, g, ctas, stream, q);
+    case 8: return launch_forward<8>(a, g, ctas, stream, q);
+    case 16: return launch_forward<16>(a, g, ctas, stream, q);
     default: return cudaErrorInvalidValue;
     }
 }
@@ -1071,7 +1126,7 @@ int tile_kernel_occupancy(int S, int TS, int ordered, int stage) {
 cudaError_t launch_pass(const PassArgs& a, const LaunchPlan& plan, cudaStream_t stream, cudaEvent_t* ev) {
     const int T = a.total_tiles;
     if (ev) cudaEventRecord(ev[0], stream);
-    cudaError_t err = cudaMemsetAsync(a.queues, 0, sizeof(uint32_t) * 2 * plan.ngroups, stream);
+    cudaError_t err = cudaMemsetAsync(a.queues, 0, sizeof(uint32_t) * 3 * plan.ngroups, stream);
     if (err != cudaSuccess) return err;
     if (a.total_tris > 0) {
         int blocks = (a.total_tris + 255) / 256;
@@ -1089,15 +1144,20 @@ cudaError_t launch_pass(const PassArgs& a, const LaunchPlan& plan, cudaStream_t 
         cudaEventRecord(ev[2], stream);
         cudaEventRecord(ev[3], stream);
     }
-    // raster stages of all groups, then shade stages (the ordered stage counts as raster)
+    // first stages of all groups (raster; ordered for ordered groups without a prefix), then the
+    // second stages (shade; ordered on top of the prefix for hybrid groups)
     for (int i = 0; i < plan.ngroups && err == cudaSuccess; i++) {
-        if (plan.ordered[i]) err = launch_group_forward(a, plan.groups[i], plan.samples[i], plan.ctas[i], stream);
-        else err = launch_group_stage(a, plan.groups[i], plan.samples[i], plan.tile_size[i], plan.ctas[i], stream, false);
+        if (plan.ordered[i] && !plan.hybrid[i])
+            err = launch_group_forward(a, plan.groups[i], plan.samples[i], plan.ctas[i], stream, false);
+        else
+            err = launch_group_stage(a, plan.groups[i], plan.samples[i], plan.tile_size[i], plan.ctas[i], stream, false);
     }
     if (ev) cudaEventRecord(ev[4], stream);
     for (int i = 0; i < plan.ngroups && err == cudaSuccess; i++)
-        if (!plan.ordered[i])
+        if (!plan.ordered[i] || plan.hybrid[i])
             err = launch_group_stage(a, plan.groups[i], plan.samples[i], plan.tile_size[i], plan.ctas_shade[i], stream, true);
+    for (int i = 0; i < plan.ngroups && err == cudaSuccess; i++)
+        if (plan.hybrid[i]) err = launch_group_forward(a, plan.groups[i], plan.samples[i], plan.ctas_fwd[i], stream, true);
     if (ev) cudaEventRecord(ev[5], stream);
     return err != cudaSuccess ? err : cudaGetLastError();
 }

@@ -44,6 +44,11 @@ struct ViewArgs {
     int depth_write;
     int ordered;             // 1: triangles applied to each sample in API order (blending, NOT_EQUAL,
                              //    or draws with different depth state)
+    int ordered_prefix;      // ordered views: triangles of the leading draws that need no ordering
+                             //    (opaque, the first draw's depth state); they go through the
+                             //    order-independent raster stage and the rest is applied on top
+    float4* sample_colors;   // views with an ordered prefix: per-sample colour [H][W][S] of the
+                             //    prefix, handed from the shade stage to the ordered stage
 };
 
 struct PassArgs {
@@ -64,7 +69,7 @@ struct PassArgs {
     TriRecord* records;      // [total_tris] compact set-ups written by the counting binner
     uint32_t pair_capacity;
     uint32_t* status;        // StatusWord
-    uint32_t* queues;        // persistent tile counters, 2 per launch group (raster, shade)
+    uint32_t* queues;        // persistent tile counters, 3 per launch group (raster, shade, ordered)
 };
 
 constexpr int kMaxGroups = 16;  // launch groups of a pass: (samples, path, tile size) combinations
@@ -83,8 +88,10 @@ struct LaunchPlan {
     int samples[kMaxGroups];
     int tile_size[kMaxGroups];  // 8 or 16
     int ordered[kMaxGroups];
-    int ctas[kMaxGroups];       // persistent CTAs of the group's raster (or ordered) stage
+    int hybrid[kMaxGroups];     // ordered group with an order-independent prefix: raster, then ordered
+    int ctas[kMaxGroups];       // persistent CTAs of the group's first stage (raster or ordered)
     int ctas_shade[kMaxGroups]; // persistent CTAs of the group's shade stage
+    int ctas_fwd[kMaxGroups];   // hybrid groups: persistent CTAs of the ordered stage after shading
 };
 
 }  // namespace ifr

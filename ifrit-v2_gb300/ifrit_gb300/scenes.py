@@ -302,3 +302,104 @@ def c4_scene(seed=4, num_views=64, size=256, subdivisions=5, noise=0.05, tex_siz
     mvps = np.stack([orbit_camera(rng, 3.0, 1.0) for _ in range(num_views)]).astype(np.float32)
     return dict(clean=clean, noisy=noisy, colors=colors, uvs=uvs, faces=f.astype(np.int32), texture=texture,
                 mvps=mvps, width=size, height=size)
+
+
+def value_noise_rgba(size, seed, octaves=5, alpha=(0.35, 0.85)):
+    """Seeded multi-octave value noise with a noise alpha channel in `alpha`, RGBA8 packed as
+    uint32 (size, size).  Each octave's bilinear lattice interpolation (smoothstep weights) is
+    separable and evaluated as two matrix products, so large textures are cheap to make."""
+    rng = np.random.default_rng(seed)
+    acc = np.zeros((4, size, size), np.float32)
+    amp, total = 1.0, 0.0
+    t = (np.arange(size) + 0.5) / size
+    for o in range(octaves):
+        cells = 4 * (2 ** o)
+        x = t * cells
+        i0 = np.floor(x).astype(int)
+        f = x - i0
+        f = f * f * (3 - 2 * f)
+        Wm = np.zeros((size, cells + 1), np.float32)
+        Wm[np.arange(size), i0] = 1 - f
+        Wm[np.arange(size), i0 + 1] += f
+        lat = rng.uniform(0, 1, size=(4, cells + 1, cells + 1)).astype(np.float32)
+        lat[:, -1, :] = lat[:, 0, :]
+        lat[:, :, -1] = lat[:, :, 0]
+        for c in range(4):
+            acc[c] += amp * (Wm @ lat[c] @ Wm.T)
+        total += amp
+        amp *= 0.55
+    acc /= total
+    acc[3] = alpha[0] + (alpha[1] - alpha[0]) * acc[3]
+    b = np.clip(np.round(acc * 255.0), 0, 255).astype(np.uint32)
+    return b[0] | (b[1] << 8) | (b[2] << 16) | (b[3] << 24)
+
+
+def c5_scene(seed=5, instances=40, frequency=112, width=3840, height=2160, blended=0.1, tex_size=4096,
+             target_complexity=7.0):
+    """Stress workload: `instances` displaced geodesic icospheres of `frequency` (20 f^2 =
+    250,880 triangles each at f = 112: 10,035,200 in total) with spherical UVs, random
+    positions, orientations and sizes chosen for a front-face depth complexity of about
+    `target_complexity` on a `width` x `height` target; a fraction `blended` of the instances are
+    alpha-blended and drawn last, back to front.  One shared vertex / index buffer.
+
+    Returns dict(vertices (V,5) [x y z u v], indices (T,3), draws: list of dict(first, count,
+    mvp, blend, depth), texture (RGBA8 uint32 with noise alpha), width, height)."""
+    rng = np.random.default_rng(seed)
+    base_v, base_f = geodesic_mesh(frequency)
+    aspect = width / height
+    proj = perspective(60.0, aspect, 0.1, 100.0)
+    view = look_at((0.0, 0.0, 0.0), (0.0, 0.0, -1.0))
+    th = math.tan(math.radians(30.0))
+    verts, idx, placed = [], [], []
+    off = 0
+    for i in range(instances):
+        k = rng.normal(size=(6, 3)) * 4.0
+        ph = rng.uniform(0, 2 * np.pi, size=6)
+        disp = np.sin(base_v @ k.T + ph).mean(axis=1)
+        v = base_v * (1.0 + 0.05 * disp)[:, None]
+        uv = np.stack([0.5 + np.arctan2(v[:, 2], v[:, 0]) / (2 * np.pi),
+                       0.5 + np.arcsin(np.clip(v[:, 1] / np.linalg.norm(v, axis=1), -1, 1)) / np.pi], 1)
+        verts.append(np.concatenate([v, uv], 1))
+        idx.append(base_f + off)
+        off += len(v)
+        d = rng.uniform(6.0, 14.0)
+        placed.append((d, rng.uniform(-0.8, 0.8) * d * th * aspect, rng.uniform(-0.8, 0.8) * d * th))
+    scales = rng.uniform(0.8, 1.2, size=instances)
+
+    def complexity(r):  # mean number of projected discs over a grid of screen points
+        ys, xs = np.mgrid[-1:1:108j, -1:1:192j]
+        cnt = np.zeros_like(xs)
+        for (d, x, y), sc in zip(placed, scales):
+            rr = min(r * sc * 1.05, 0.95 * d)  # displaced radius; silhouette half-angle asin(rr / d)
+            t_half = rr / math.sqrt(d * d - rr * rr)
+            rx, ry = t_half / (th * aspect), t_half / th
+            cnt += ((xs - x / (d * th * aspect)) / rx) ** 2 + ((ys - y / (d * th)) / ry) ** 2 <= 1.0
+        return cnt.mean()
+
+    lo, hi = 0.1, 20.0  # sphere radius for the target depth complexity (bisection)
+    for _ in range(40):
+        mid = 0.5 * (lo + hi)
+        lo, hi = (mid, hi) if complexity(mid) < target_complexity else (lo, mid)
+    radius = 0.5 * (lo + hi)
+    draws = []
+    for i, (d, x, y) in enumerate(placed):
+        q = rng.normal(size=4)
+        q /= np.linalg.norm(q)
+        a, b, c, w = q
+        R = np.array([[1 - 2 * (b * b + c * c), 2 * (a * b - c * w), 2 * (a * c + b * w)],
+                      [2 * (a * b + c * w), 1 - 2 * (a * a + c * c), 2 * (b * c - a * w)],
+                      [2 * (a * c - b * w), 2 * (b * c + a * w), 1 - 2 * (a * a + b * b)]])
+        M = np.eye(4)
+        M[:3, :3] = R * radius * scales[i]
+        M[:3, 3] = (x, y, -d)
+        draws.append(dict(first=3 * i * len(base_f), count=3 * len(base_f),
+                          mvp=(proj @ view @ M).astype(np.float32), blend=False, depth=d))
+    nblend = int(round(blended * instances))
+    order = list(rng.permutation(instances))
+    opaque, trans = order[nblend:], order[:nblend]
+    trans.sort(key=lambda i: -draws[i]["depth"])  # back to front
+    for i in trans:
+        draws[i]["blend"] = True
+    return dict(vertices=np.concatenate(verts).astype(np.float32), indices=np.concatenate(idx).astype(np.int32),
+                draws=[draws[i] for i in opaque + trans], texture=value_noise_rgba(tex_size, seed),
+                width=width, height=height, radius=radius)

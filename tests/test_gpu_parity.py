@@ -235,3 +235,37 @@ def test_not_equal_and_mixed_depth_state_pass():
              dict(vertices=v, indices=f[4000:], mvp=mvp, attr=4, cull=0, depth_func=ig.GREATER_OR_EQUAL)]
     gpu, ref = _pass_both(128, 96, 4, draws)
     assert_parity(gpu, ref)
+
+
+def test_stress_style_pass_small():
+    """Every feature of the 4K stress configuration in one pass, at a size the oracle renders in
+    seconds: RGBA16F, 8x MSAA, displaced geodesic instances with random transforms, 16x
+    anisotropic texturing with a noise alpha, blended instances drawn last back to front."""
+    from oracle import oracle as O
+    sc = scenes.c5_scene(seed=9, instances=6, frequency=12, width=320, height=180, blended=0.34, tex_size=256,
+                         target_complexity=2.0)
+    W, H = sc["width"], sc["height"]
+    assert sum(d["blend"] for d in sc["draws"]) == 2
+    r = ig.Renderer(W, H, 8, ig.FORMAT_RGBA16F, visibility=True)
+    r.set_geometry(sc["vertices"], sc["indices"], 2)
+    r.set_texture(sc["texture"], max_aniso=16)
+    r.begin_pass(clear=True)
+    chain, levels = O.build_mips(sc["texture"])
+    tex = (chain, levels, sc["texture"].shape[1], sc["texture"].shape[0])
+    odraws, base = [], 0
+    for d in sc["draws"]:
+        r.set_state(cull=ig.CULL_BACK, depth_func=ig.LESS_OR_EQUAL, depth_write=not d["blend"], shading=ig.FS_TEXTURED)
+        r.set_blend(d["blend"], 6, 7, 1, 7)
+        r.set_mvp(d["mvp"])
+        r.pass_draw(d["first"], d["count"])
+        f = sc["indices"][d["first"] // 3:(d["first"] + d["count"]) // 3]
+        odraws.append(O.make_draw(sc["vertices"], f, d["mvp"], attr_offset=3, attr_count=2, cull_mode=2, depth_func=3,
+                                  depth_write=int(not d["blend"]), blend=(6, 7, 1, 7) if d["blend"] else None,
+                                  shading=O.SHADE_TEXTURED, texture=tex, sampler={"max_aniso": 16}, prim_base=base))
+        base += len(f)
+    r.end_pass()
+    gpu = {"color": r.color(), "depth": r.depth(), "vis": r.visibility()}
+    ref = O.render(odraws, W, H, 8, O.FMT_RGBA16F, clear=True, nthreads=os.cpu_count() or 1)
+    assert_parity(gpu, ref, fmt=ig.FORMAT_RGBA16F)
+    assert (gpu["vis"] >= 0).mean() > 0.5
+    r.close()
