@@ -553,7 +553,7 @@ def run_ours_c5(args):
     m = statistics.mean(ms)
     B = c5_algorithmic_bytes(sc)
     peak, peak_kind = peak_hbm()
-    st = [statistics.mean(x[i] for x in stages) for i in range(5)]
+    st = [statistics.mean(x[i] for x in stages) for i in range(6)]
     T = len(sc["indices"])
     line = {"metric": METRIC, "value": world * shaded / (m / 1000.0), "unit": "samples/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": m, "higher_is_better": True, "scaling": "weak",
@@ -565,7 +565,7 @@ def run_ours_c5(args):
                        "width": W, "height": H, "samples": 8, "triangles": T, "shaded_samples_per_frame": shaded,
                        "l2": "inputs larger than L2 (no flush)", "parallelism": "single"},
             "tris_per_s": T / (m / 1000.0),
-            "stage_ms": {"binning": st[0] + st[1] + st[2], "ordered_tiles": st[3]},
+            "stage_ms": {"binning": st[0] + st[1] + st[2], "raster": st[3], "shade": st[4], "ordered": st[5]},
             "roofline": {"bound": "hbm", "achieved": B / (m / 1000.0) / 1e9, "peak": peak, "unit": "GB/s",
                          "frac": B / (m / 1000.0) / 1e9 / peak, "traffic": None, "algorithmic_bytes": B,
                          "kernel": "whole pass", "peak_source": peak_kind},

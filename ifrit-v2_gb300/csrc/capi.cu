@@ -214,8 +214,8 @@ struct IfritGbRenderer {
     int bound_tex = 0, bound_sampler = 0;
     IfritGbStats stats{};
     bool timing = false;
-    cudaEvent_t ev[6] = {};
-    float stage_ms[5] = {0, 0, 0, 0, 0};
+    cudaEvent_t ev[ifr::kStageEvents] = {};
+    float stage_ms[ifr::kStageEvents - 1] = {};
     std::string last_error;
     int pending = 0;        // plain passes whose status has not been checked
     int pending_batch = 0;  // batched passes whose status has not been checked
@@ -553,7 +553,7 @@ int enqueue_pass(IfritGbRenderer* h, std::vector<DrawDev>& draws, int clear) {
     v.clear_depth = h->clear_depth;
     ifr::set_view_depth_state(v, draws.data(), (int)draws.size());
     if (v.ordered) {  // per-sample colours handed from the shade stage to the ordered stage
-        IFTR_CUDA(h, h->d_sample_colors.reserve((size_t)W * H * S * sizeof(float4)));
+        IFTR_CUDA(h, h->d_sample_colors.reserve((size_t)ifr::tiles_of(W, H, 16) * 256 * S * sizeof(float4)));
         v.sample_colors = h->d_sample_colors.as<float4>();
     }
     std::vector<int> view_tiles(2);
@@ -588,7 +588,7 @@ int check_pending(IfritGbRenderer* h) {
     if (h->pending) {
         h->pending = 0;
         if (h->timing)
-            for (int i = 0; i < 5; i++) cudaEventElapsedTime(&h->stage_ms[i], h->ev[i], h->ev[i + 1]);
+            for (int i = 0; i + 1 < ifr::kStageEvents; i++) cudaEventElapsedTime(&h->stage_ms[i], h->ev[i], h->ev[i + 1]);
         rc = consume_status(h, h->pass);
         h->stats.pair_capacity = h->pass.pair_capacity;
     }
@@ -774,7 +774,7 @@ int build_batch(IfritGbRenderer* h, const IfritGbBatchView* views, int nv, const
         // all its views), each starting on a 256-byte boundary (the tile kernels move it as int4)
         ent += ((size_t)v.c.W * v.c.H * v.c.S + 63) / 64 * 64;
         out.color_offset.push_back(v.ordered ? cols : ~(size_t)0);
-        if (v.ordered) cols += (size_t)v.c.W * v.c.H * v.c.S;
+        if (v.ordered) cols += (size_t)v.c.tiles_x * v.c.tiles_y * 256 * v.c.S;  // ordered views use 16x16 tiles
         out.views.push_back(v);
     }
     out.draw_start.push_back((int)tri);
@@ -1367,7 +1367,7 @@ IFTR_API int iftrSetStageTiming(IfritGbRenderer* h, int enable) {
 
 IFTR_API int iftrGetStageTimes(IfritGbRenderer* h, float* ms, int n) {
     if (!h || !ms || n < 0) return IFTR_ERR_INVALID_ARG;
-    for (int i = 0; i < n && i < 5; i++) ms[i] = h->stage_ms[i];
+    for (int i = 0; i < n && i + 1 < ifr::kStageEvents; i++) ms[i] = h->stage_ms[i];
     return IFTR_OK;
 }
 

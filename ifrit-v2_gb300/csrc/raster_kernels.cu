@@ -703,7 +703,8 @@ __device__ __forceinline__ void shade_tile(const PassArgs& a, const ViewArgs& v,
             }
             if (!rule.write) dep[k] = d0v;
         }
-        if (keep_samples) v.sample_colors[pix * S + k] = make_float4(c[0], c[1], c[2], c[3]);
+        if (keep_samples)  // tile-major hand-off: [tile][sample][lane], coalesced on both sides
+            v.sample_colors[((size_t)ltile * S + k) * (TS * TS) + part * 32 + (tid & 31)] = make_float4(c[0], c[1], c[2], c[3]);
         if (k == 0) {
             acc[0] = c[0]; acc[1] = c[1]; acc[2] = c[2]; acc[3] = c[3];
         } else {
@@ -786,9 +787,42 @@ struct FwdRecords {
     int32_t draw[kFwdThreads];
 };
 
+constexpr int kFwdFrags = 8;  // fragments a pixel holds before they are shaded
+
+// Shades fragment f = (entry, sample mask) at pixel (px, py) and writes or blends it into the
+// per-sample colours of the calling thread.
+template <int S>
+__device__ __forceinline__ void apply_fragment(const PassArgs& a, const ViewArgs& v, int px, int py, float4* scol,
+                                               int2 f) {
+    constexpr int NT = kFwdThreads;
+    float c[4];
+    RecordPlane pl;
+    shade_uncached(a, v.c, f.x, px, py, c, &pl);
+    const DrawDev& d = a.draws[record_draw(a, f.x >> 3)];
+    const unsigned mask = (unsigned)f.y;
+#pragma unroll
+    for (int k = 0; k < S; k++) {
+        if (!(mask & (1u << k))) continue;
+        float4& sc = scol[k * NT + threadIdx.x];
+        if (d.blend_enable) {
+            float dst[4] = {sc.x, sc.y, sc.z, sc.w};
+            blend_into(d, c, dst);
+            sc = make_float4(dst[0], dst[1], dst[2], dst[3]);
+        } else {
+            sc = make_float4(c[0], c[1], c[2], c[3]);
+        }
+    }
+}
+
+template <int S>
+__device__ __noinline__ void apply_fragments(const PassArgs& a, const ViewArgs& v, int px, int py, float4* scol,
+                                             const int2* frags, int n) {
+    for (int i = 0; i < n; i++) apply_fragment<S>(a, v, px, py, scol, frags[i * kFwdThreads + threadIdx.x]);
+}
+
 template <int S>
 __device__ __forceinline__ void forward_tile(const PassArgs& a, const ViewArgs& v, int gtile, FwdRecords& rec,
-                                             float4* scol, uint32_t* list, bool after_raster) {
+                                             float4* scol, uint32_t* list, int2* frags, bool after_raster) {
     constexpr int TS = 16, NT = kFwdThreads;
     // after the raster and shade stages the shade stage has finished the tiles without ordered
     // entries (uniform over the CTA)
@@ -821,7 +855,8 @@ __device__ __forceinline__ void forward_tile(const PassArgs& a, const ViewArgs& 
                 const int ent = inpix ? v.entries[pix * S + k] : -1;
                 dep[k] = inpix ? v.depth[pix * S + k] : 0.0f;
                 vid[k] = ent < 0 ? -1 : (ent >> 3) - v.first_tri;
-                scol[k * NT + tid] = inpix ? v.sample_colors[pix * S + k] : make_float4(bg[0], bg[1], bg[2], bg[3]);
+                scol[k * NT + tid] = inpix ? v.sample_colors[((size_t)ltile * S + k) * NT + tid]
+                                           : make_float4(bg[0], bg[1], bg[2], bg[3]);
             } else {
                 dep[k] = v.clear ? v.clear_depth : (inpix ? v.depth[pix * S + k] : 0.0f);
                 vid[k] = -1;
@@ -876,6 +911,7 @@ __device__ __forceinline__ void forward_tile(const PassArgs& a, const ViewArgs& 
         }
     }
 
+    int nfrag = 0;  // fragments recorded for this thread's pixel, not yet shaded
     for (int base = 0; base < n; base += NT) {
         const int nb = min(NT, n - base);
         if (tid < nb) {
@@ -926,25 +962,22 @@ __device__ __forceinline__ void forward_tile(const PassArgs& a, const ViewArgs& 
                     mask |= 1u << k;
                 }
                 if (!mask) continue;
-                float c[4];
-                RecordPlane pl;
-                shade_uncached(a, v.c, e, px, py, c, &pl);
-#pragma unroll
-                for (int k = 0; k < S; k++) {
-                    if (!(mask & (1u << k))) continue;
-                    float4& sc = scol[k * NT + tid];
-                    if (d.blend_enable) {
-                        float dst[4] = {sc.x, sc.y, sc.z, sc.w};
-                        blend_into(d, c, dst);
-                        sc = make_float4(dst[0], dst[1], dst[2], dst[3]);
-                    } else {
-                        sc = make_float4(c[0], c[1], c[2], c[3]);
-                    }
+                // colours never change depth: record the fragment now, shade it later
+                if (nfrag == kFwdFrags) {  // a full list is applied on the spot (rare)
+                    apply_fragments<S>(a, v, px, py, scol, frags, nfrag);
+                    nfrag = 0;
                 }
+                frags[nfrag * NT + tid] = make_int2(e, (int)mask);
+                nfrag++;
             }
         }
         __syncthreads();
     }
+    // shade the recorded fragments with the warp converged on fragment slot i of every lane, and
+    // apply each one in submission order to its samples
+    const int maxn = __reduce_max_sync(0xffffffffu, nfrag);
+    for (int i = 0; i < maxn; i++)
+        if (i < nfrag) apply_fragment<S>(a, v, px, py, scol, frags[i * NT + tid]);
     if (!inpix) return;
     float acc[4];
 #pragma unroll
@@ -971,7 +1004,8 @@ __device__ __forceinline__ void forward_tile(const PassArgs& a, const ViewArgs& 
 
 template <int S>
 size_t forward_smem_bytes() {
-    return sizeof(FwdRecords) + sizeof(float4) * S * kFwdThreads + sizeof(uint32_t) * kOrderedCap;
+    return sizeof(FwdRecords) + sizeof(float4) * S * kFwdThreads + sizeof(uint32_t) * kOrderedCap +
+           sizeof(int2) * kFwdFrags * kFwdThreads;
 }
 
 template <int S>
@@ -980,11 +1014,12 @@ __global__ void __launch_bounds__(kFwdThreads) forward_kernel(PassArgs a, GroupA
     FwdRecords& rec = *reinterpret_cast<FwdRecords*>(smem_raw);
     float4* scol = reinterpret_cast<float4*>(smem_raw + sizeof(FwdRecords));  // [S][256]
     uint32_t* list = reinterpret_cast<uint32_t*>(smem_raw + sizeof(FwdRecords) + sizeof(float4) * S * kFwdThreads);
+    int2* frags = reinterpret_cast<int2*>(list + kOrderedCap);  // [kFwdFrags][256]
     __shared__ ViewArgs sv;
     __shared__ int s_tile, s_view;
     if (threadIdx.x == 0) s_view = -1;
     while (next_tile<kFwdThreads>(a, g, qslot, sv, s_tile, s_view))
-        forward_tile<S>(a, sv, s_tile, rec, scol, list, after_raster != 0);
+        forward_tile<S>(a, sv, s_tile, rec, scol, list, frags, after_raster != 0);
 }
 
 // ---------------------------------------------------------------------------- mips
@@ -1156,9 +1191,10 @@ cudaError_t launch_pass(const PassArgs& a, const LaunchPlan& plan, cudaStream_t 
     for (int i = 0; i < plan.ngroups && err == cudaSuccess; i++)
         if (!plan.ordered[i] || plan.hybrid[i])
             err = launch_group_stage(a, plan.groups[i], plan.samples[i], plan.tile_size[i], plan.ctas_shade[i], stream, true);
+    if (ev) cudaEventRecord(ev[5], stream);
     for (int i = 0; i < plan.ngroups && err == cudaSuccess; i++)
         if (plan.hybrid[i]) err = launch_group_forward(a, plan.groups[i], plan.samples[i], plan.ctas_fwd[i], stream, true);
-    if (ev) cudaEventRecord(ev[5], stream);
+    if (ev) cudaEventRecord(ev[6], stream);
     return err != cudaSuccess ? err : cudaGetLastError();
 }
 

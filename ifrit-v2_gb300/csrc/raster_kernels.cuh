@@ -47,8 +47,9 @@ struct ViewArgs {
     int ordered_prefix;      // ordered views: triangles of the leading draws that need no ordering
                              //    (opaque, the first draw's depth state); they go through the
                              //    order-independent raster stage and the rest is applied on top
-    float4* sample_colors;   // views with an ordered prefix: per-sample colour [H][W][S] of the
-                             //    prefix, handed from the shade stage to the ordered stage
+    float4* sample_colors;   // ordered views: per-sample colour of the order-independent prefix,
+                             //    handed from the shade stage to the ordered stage, tile-major
+                             //    [tiles][S][256] (16x16 tiles, lanes in tile_pixel order)
 };
 
 struct PassArgs {
@@ -100,8 +101,10 @@ struct LaunchPlan {
 namespace ifr {
 // Entries of PassArgs::block_sums a pass over `tiles` tiles needs.
 constexpr int scan_blocks(int tiles) { return (tiles + 4095) / 4096 + 1; }
-// ev: optional array of 6 events recorded before binning, after counting, after the scan,
-// after scattering, after the raster stage and after the shade stage (per-stage timing).
+// ev: optional array of kStageEvents events recorded before binning, after counting, after the
+// scan, after scattering, after the raster stage, after the shade stage and after the ordered
+// stage (per-stage timing).
+constexpr int kStageEvents = 7;
 cudaError_t launch_pass(const PassArgs& a, const LaunchPlan& plan, cudaStream_t stream, cudaEvent_t* ev);
 cudaError_t launch_mip_level(const uint32_t* src, int sw, int sh, uint32_t* dst, int dw, int dh, cudaStream_t stream);
 // Maximum resident CTAs per SM of a tile kernel for (samples, tile size, ordered); stage 0 is

@@ -359,8 +359,9 @@ class Renderer:
         check("iftrSetStageTiming", self.lib.iftrSetStageTiming(self.h, int(enable)))
 
     def stage_times(self):
-        ms = (ctypes.c_float * 5)()
-        check("iftrGetStageTimes", self.lib.iftrGetStageTimes(self.h, ms, 5))
+        """[count, scan, scatter, raster, shade, ordered] device milliseconds of the last pass."""
+        ms = (ctypes.c_float * 6)()
+        check("iftrGetStageTimes", self.lib.iftrGetStageTimes(self.h, ms, 6))
         return list(ms)
 
     def mark_geometry_dirty(self):

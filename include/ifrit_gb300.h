@@ -158,8 +158,9 @@ IFTR_API int iftrReadbackVisibility(IfritGbRenderer* h, int* dst, size_t count);
 IFTR_API int iftrGetStats(IfritGbRenderer* h, IfritGbStats* out);
 /* Per-stage device timing of the last pass, from CUDA events on the renderer's stream:
  * ms[0] counting binner, ms[1] list-offset scan, ms[2] scattering binner, ms[3] tile raster
- * (coverage + depth test), ms[4] tile shading + resolve.  Enable before the draw; read after
- * iftrFinish/iftrDrawLegacy. */
+ * (coverage + depth test; passes without an order-independent part: the in-order stage),
+ * ms[4] tile shading + resolve, ms[5] in-order stage after shading (blended passes).  Enable
+ * before the draw; read after iftrFinish/iftrDrawLegacy. */
 IFTR_API int iftrSetStageTiming(IfritGbRenderer* h, int enable);
 IFTR_API int iftrGetStageTimes(IfritGbRenderer* h, float* ms, int n);
 IFTR_API const char* iftrGetErrorString(int status);
