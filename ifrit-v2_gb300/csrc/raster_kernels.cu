@@ -406,13 +406,21 @@ __device__ __forceinline__ void tile_pixel(int tid, int& lx, int& ly) {
 }
 
 // ---------------------------------------------------------------------------- raster stage
+// A record whose snapped vertices span less than 32 pixels in x and in y has every edge function
+// value at its bbox samples below 2^28 in magnitude (|A|, |B| < 8192 and sample offsets from a
+// vertex below 8704 in 1/256 pixel), so coverage is evaluated exactly in 32-bit arithmetic
+// relative to the clipped bbox origin.  Larger ones keep the 64-bit edge functions.
+constexpr int kLargeRecord = 1 << 16;
+constexpr int32_t kSmallSpan = 32 * 256;
+
 template <int NT>
 struct TileRecords {
     int32_t A[3][NT], B[3][NT];
     long long Cb[3][NT];
+    int32_t E[3][NT];   // small triangles: biased edge functions at the clipped bbox origin corner
     float z0[NT], dzdx[NT], dzdy[NT];
     int32_t X0[NT], Y0[NT];
-    int32_t org[NT];    // tile-local x0 | y0 << 8 of the clipped bbox
+    int32_t org[NT];    // tile-local x0 | y0 << 8 of the clipped bbox, | kLargeRecord
     int32_t width[NT];  // clipped bbox width in pixels
     float rwidth[NT];   // 1 / width
     int32_t key[NT];    // entry
@@ -474,7 +482,15 @@ __device__ __forceinline__ void raster_tile(const PassArgs& a, const ViewArgs& v
                     rec.X0[tid] = s.X[0];
                     rec.Y0[tid] = s.Y[0];
                     int w = x1 - x0 + 1;
-                    rec.org[tid] = (x0 - tx0) | ((y0 - ty0) << 8);
+                    const int32_t xmn = min(s.X[0], min(s.X[1], s.X[2])), xmx = max(s.X[0], max(s.X[1], s.X[2]));
+                    const int32_t ymn = min(s.Y[0], min(s.Y[1], s.Y[2])), ymx = max(s.Y[0], max(s.Y[1], s.Y[2]));
+                    const bool small = xmx - xmn < kSmallSpan && ymx - ymn < kSmallSpan;
+                    if (small) {
+#pragma unroll
+                        for (int i = 0; i < 3; i++)
+                            rec.E[i][tid] = (int32_t)(s.Cb[i] + (int64_t)s.A[i] * (x0 * 256) + (int64_t)s.B[i] * (y0 * 256));
+                    }
+                    rec.org[tid] = (x0 - tx0) | ((y0 - ty0) << 8) | (small ? 0 : kLargeRecord);
                     rec.width[tid] = w;
                     rec.rwidth[tid] = 1.0f / (float)w;
                     cnt = (uint32_t)(w * (y1 - y0 + 1));
@@ -513,11 +529,29 @@ __device__ __forceinline__ void raster_tile(const PassArgs& a, const ViewArgs& v
             const int oy = (int)(((float)local + 0.5f) * rec.rwidth[r]);
             const int ox = local - oy * w;
             const int org = rec.org[r];
-            const int qx = (org & 255) + ox, qy = (org >> 8) + oy;
+            const int qx = (org & 255) + ox, qy = ((org >> 8) & 255) + oy;
             const int gx = tx0 + qx, gy = ty0 + qy;
-            int32_t A[3] = {rec.A[0][r], rec.A[1][r], rec.A[2][r]};
-            int32_t B[3] = {rec.B[0][r], rec.B[1][r], rec.B[2][r]};
-            int64_t Cb[3] = {rec.Cb[0][r], rec.Cb[1][r], rec.Cb[2][r]};
+            const int32_t A[3] = {rec.A[0][r], rec.A[1][r], rec.A[2][r]};
+            const int32_t B[3] = {rec.B[0][r], rec.B[1][r], rec.B[2][r]};
+            unsigned cov = 0;  // covered samples of this pixel
+            if (!(org & kLargeRecord)) {
+                int32_t e0[3];
+#pragma unroll
+                for (int i = 0; i < 3; i++) e0[i] = rec.E[i][r] + A[i] * (ox * 256) + B[i] * (oy * 256);
+#pragma unroll
+                for (int k = 0; k < S; k++) {
+                    const int32_t c0 = e0[0] + A[0] * sample_x<S>(k) + B[0] * sample_y<S>(k);
+                    const int32_t c1 = e0[1] + A[1] * sample_x<S>(k) + B[1] * sample_y<S>(k);
+                    const int32_t c2 = e0[2] + A[2] * sample_x<S>(k) + B[2] * sample_y<S>(k);
+                    cov |= ((c0 | c1 | c2) >= 0 ? 1u : 0u) << k;
+                }
+            } else {
+                const int64_t Cb[3] = {rec.Cb[0][r], rec.Cb[1][r], rec.Cb[2][r]};
+#pragma unroll
+                for (int k = 0; k < S; k++)
+                    cov |= (covered(A, B, Cb, gx * 256 + sample_x<S>(k), gy * 256 + sample_y<S>(k)) ? 1u : 0u) << k;
+            }
+            if (!cov) continue;
             const float z0 = rec.z0[r], gzx = rec.dzdx[r], gzy = rec.dzdy[r];
             const int32_t X0 = rec.X0[r], Y0 = rec.Y0[r];
             const uint32_t e = (uint32_t)rec.key[r];
@@ -528,8 +562,7 @@ __device__ __forceinline__ void raster_tile(const PassArgs& a, const ViewArgs& v
             const float fbx = (float)(gx * 256 - X0), fby = (float)(gy * 256 - Y0);
 #pragma unroll
             for (int k = 0; k < S; k++) {
-                const int32_t sx = gx * 256 + sample_x<S>(k), sy = gy * 256 + sample_y<S>(k);
-                if (!covered(A, B, Cb, sx, sy)) continue;
+                if (!(cov & (1u << k))) continue;
                 const float z = (z0 + gzx * (fbx + (float)sample_x<S>(k))) + gzy * (fby + (float)sample_y<S>(k));
                 uint32_t hi_word;
                 if (rule.explicit_) {
@@ -578,7 +611,7 @@ size_t raster_smem_bytes() {
 }
 
 template <int S, int TS>
-__global__ void __launch_bounds__(TS * TS) raster_kernel(PassArgs a, GroupArgs g) {
+__global__ void __launch_bounds__(TS * TS, 1024 / (TS * TS)) raster_kernel(PassArgs a, GroupArgs g) {
     constexpr int NT = TS * TS;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     TileRecords<NT>& rec = *reinterpret_cast<TileRecords<NT>*>(smem_raw);
