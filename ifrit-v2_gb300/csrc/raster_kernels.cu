@@ -630,7 +630,8 @@ __global__ void __launch_bounds__(TS * TS, 1024 / (TS * TS)) raster_kernel(PassA
 // and depth, visibility and the resolved colour stored once.
 template <int S, int TS>
 __device__ __forceinline__ void shade_tile(const PassArgs& a, const ViewArgs& v, int gtile, int part,
-                                           float4 (*scol)[TS * TS], bool keep_samples) {
+                                           float4 (*scol)[TS * TS], float4 (*splane)[TS * TS], int (*splane_y)[TS * TS],
+                                           int2* witems, bool keep_samples) {
     const int ltile = gtile - v.tile_start;
     const int tx = ltile % v.c.tiles_x, ty = ltile / v.c.tiles_x;
     const int tid = threadIdx.x;
@@ -679,34 +680,53 @@ __device__ __forceinline__ void shade_tile(const PassArgs& a, const ViewArgs& v,
         }
         which[k] = found;
     }
-    int nmax = min(nu, U);
+    // The warp's (pixel, entry) shading items, compacted: item i of the warp goes to lane i % 32,
+    // whatever pixel it belongs to (quad derivatives are evaluated analytically at the owner's
+    // pixel, so no item depends on another lane).  Results land in the owner's slot.
+    const int lane = tid & 31, wbase = tid & ~31;
+    const int nc = min(nu, U);
+    int incl = nc;
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) nmax = max(nmax, __shfl_xor_sync(0xffffffffu, nmax, o));
+    for (int o = 1; o < 32; o <<= 1) {
+        const int q = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += q;
+    }
+    const int total = __shfl_sync(0xffffffffu, incl, 31);
+    int2* items = witems + (tid >> 5) * (32 * U);
+#pragma unroll
+    for (int j = 0; j < U; j++)
+        if (j < nc) items[incl - nc + j] = make_int2(uniq[j], lane | (j << 5));
+    __syncwarp();
+    for (int b = lane; b < total; b += 32) {
+        const int2 it = items[b];
+        const int owner = it.y & 31, slot = it.y >> 5;
+        int olx, oly;
+        tile_pixel<TS>(part * 32 + owner, olx, oly);
+        const int opx = tx * TS + olx, opy = ty * TS + oly;
+        const int g = it.x >> 3, sub = it.x & 7;
+        const int di = record_draw(a, g);
+        const DrawDev& d = a.draws[di];
+        const int t = g - __ldg(a.draw_start + di);
+        SubTri st;
+        setup_entry_sub(v.c, d, a.records, g, t, sub, st);
+        ShadeGeom geo;
+        shade_geom_from(st, geo);
+        float c[4];
+        shade_fragment(v.c, d, geo, t, sub, opx, opy, c);
+        scol[slot][wbase + owner] = make_float4(c[0], c[1], c[2], c[3]);
+        splane[slot][wbase + owner] = make_float4(st.z[0], st.dzdx, st.dzdy, __int_as_float(st.X[0]));
+        splane_y[slot][wbase + owner] = st.Y[0];
+    }
+    __syncwarp();
     float dep[S];
 #pragma unroll
-    for (int k = 0; k < S; k++) dep[k] = 0.0f;
-    for (int i = 0; i < nmax; i++) {
-        int e = -1;
-#pragma unroll
-        for (int j = 0; j < U; j++)
-            if (j == i) e = uniq[j];
-        if (i < nu) {
-            const int g = e >> 3, sub = e & 7;
-            const int di = record_draw(a, g);
-            const DrawDev& d = a.draws[di];
-            const int t = g - __ldg(a.draw_start + di);
-            SubTri st;
-            setup_entry_sub(v.c, d, a.records, g, t, sub, st);
-            ShadeGeom geo;
-            shade_geom_from(st, geo);
-            float c[4];
-            shade_fragment(v.c, d, geo, t, sub, px, py, c);
-            scol[i][tid] = make_float4(c[0], c[1], c[2], c[3]);
-#pragma unroll
-            for (int k = 0; k < S; k++)
-                if (which[k] == i)
-                    dep[k] = sample_depth(st.z[0], st.dzdx, st.dzdy, st.X[0], st.Y[0], px * 256 + sample_x<S>(k),
-                                          py * 256 + sample_y<S>(k));
+    for (int k = 0; k < S; k++) {
+        dep[k] = 0.0f;
+        const int i = which[k];
+        if (i >= 0 && i < U) {
+            const float4 pl = splane[i][tid];
+            dep[k] = sample_depth(pl.x, pl.y, pl.z, __float_as_int(pl.w), splane_y[i][tid], px * 256 + sample_x<S>(k),
+                                  py * 256 + sample_y<S>(k));
         }
     }
     if (!inpix) return;
@@ -772,7 +792,11 @@ template <int S, int TS>
 __global__ void __launch_bounds__(TS * TS, 512 / (TS * TS)) shade_kernel(PassArgs a, GroupArgs g) {
     constexpr int NT = TS * TS;
     constexpr int kTasksPerTile = NT / 32;
-    __shared__ float4 scol[4][NT];  // colours of each thread's (up to 4) distinct entries
+    constexpr int U = S < 4 ? S : 4;
+    __shared__ float4 scol[4][NT];    // colours of each thread's (up to 4) distinct entries
+    __shared__ float4 splane[4][NT];  // their depth planes: z0, dz/dx, dz/dy, X0 (bits)
+    __shared__ int splane_y[4][NT];   // and Y0
+    __shared__ int2 witems[NT / 32 * 32 * U];  // per warp: compacted (entry, lane | slot << 5) items
     const int lane = threadIdx.x & 31;
     const int ntasks = (g.tile_end - g.tile_begin) * kTasksPerTile;
     for (;;) {
@@ -796,7 +820,7 @@ __global__ void __launch_bounds__(TS * TS, 512 / (TS * TS)) shade_kernel(PassArg
         // tiles of ordered views with entries left for the ordered stage keep their per-sample
         // colours for it instead of resolving
         const bool keep = a.views[vi].ordered && __ldg(a.tile_cursor + gtile) != 0u;
-        shade_tile<S, TS>(a, a.views[vi], gtile, task % kTasksPerTile, scol, keep);
+        shade_tile<S, TS>(a, a.views[vi], gtile, task % kTasksPerTile, scol, splane, splane_y, witems, keep);
     }
 }
 
