@@ -789,7 +789,7 @@ __device__ __forceinline__ void shade_tile(const PassArgs& a, const ViewArgs& v,
 // queue on its own, so a warp that finishes early starts its next task instead of waiting at a
 // tile barrier.  View arguments are read through L1 from the descriptor array.
 template <int S, int TS>
-__global__ void __launch_bounds__(TS * TS, 512 / (TS * TS)) shade_kernel(PassArgs a, GroupArgs g) {
+__global__ void __launch_bounds__(TS * TS, 1024 / (TS * TS)) shade_kernel(PassArgs a, GroupArgs g) {
     constexpr int NT = TS * TS;
     constexpr int kTasksPerTile = NT / 32;
     constexpr int U = S < 4 ? S : 4;
