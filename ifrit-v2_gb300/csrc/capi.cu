@@ -131,8 +131,8 @@ uint64_t g_id_counter = 1;
 // Device scratch and pinned descriptor staging of a pass.  Buffers grow on demand; each growth
 // bumps `generation`, which invalidates CUDA graphs captured with the old addresses.
 struct PassScratch {
-    DevMem tile_count, tile_offset, tile_cursor, block_sums, pairs, records, status, draws, draw_start, views, view_tiles,
-        queues, entries, sample_colors;
+    DevMem tile_count, tile_offset, tile_cursor, block_sums, pairs, records, attrs, status, draws, draw_start, views,
+        view_tiles, queues, entries, sample_colors;
     size_t tiles_alloc = 0;
     uint32_t pair_capacity = 0;
     uint64_t generation = 1;
@@ -141,7 +141,7 @@ struct PassScratch {
     cudaEvent_t staged = nullptr;  // recorded after the last descriptor upload
     bool staged_pending = false;
     void release() {
-        for (DevMem* m : {&tile_count, &tile_offset, &tile_cursor, &block_sums, &pairs, &records, &status, &draws,
+        for (DevMem* m : {&tile_count, &tile_offset, &tile_cursor, &block_sums, &pairs, &records, &attrs, &status, &draws,
                           &draw_start, &views, &view_tiles, &queues, &entries, &sample_colors})
             m->release();
         if (h_status) cudaFreeHost(h_status);
@@ -323,6 +323,7 @@ int scratch_reserve(IfritGbRenderer* h, PassScratch& s, size_t tiles, size_t tri
         s.generation++;
     }
     IFTR_CUDA(h, grow(s.records, std::max<size_t>(1, tris) * sizeof(ifr::TriRecord)));
+    IFTR_CUDA(h, grow(s.attrs, std::max<size_t>(1, tris) * sizeof(ifr::TriAttr)));
     IFTR_CUDA(h, grow(s.draws, std::max<size_t>(1, ndraws) * sizeof(DrawDev)));
     IFTR_CUDA(h, grow(s.draw_start, (ndraws + 1) * sizeof(int)));
     IFTR_CUDA(h, grow(s.views, std::max<size_t>(1, nviews) * sizeof(ifr::ViewArgs)));
@@ -379,6 +380,7 @@ PassArgs make_args(const PassScratch& s, int ndraws, int total_tris, int nviews,
     a.block_sums = s.block_sums.as<uint32_t>();
     a.pairs = s.pairs.as<uint32_t>();
     a.records = s.records.as<ifr::TriRecord>();
+    a.attrs = s.attrs.as<ifr::TriAttr>();
     a.pair_capacity = s.pair_capacity;
     a.status = s.status.as<uint32_t>();
     a.queues = s.queues.as<uint32_t>();

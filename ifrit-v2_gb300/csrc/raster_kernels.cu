@@ -89,6 +89,14 @@ __global__ void __launch_bounds__(256) bin_count_kernel(PassArgs a) {
         TriRecord r;
         record_from_sub(s, r);
         r.draw = di;
+        if (a.attrs && d.shading != SHADE_PRIMID && d.attr_count > 0) {
+            float a0[4], a1[4], a2[4];
+            fetch_attrs(d, t, a0, a1, a2);
+            float4* dst = a.attrs[g].a;
+            dst[0] = make_float4(a0[0], a0[1], a0[2], a0[3]);
+            dst[1] = make_float4(a1[0], a1[1], a1[2], a1[3]);
+            dst[2] = make_float4(a2[0], a2[1], a2[2], a2[3]);
+        }
         const int4* src = reinterpret_cast<const int4*>(&r);
         int4* dst = reinterpret_cast<int4*>(rec);
         dst[0] = src[0]; dst[1] = src[1]; dst[2] = src[2]; dst[3] = src[3];
@@ -708,11 +716,19 @@ __device__ __forceinline__ void shade_tile(const PassArgs& a, const ViewArgs& v,
         const DrawDev& d = a.draws[di];
         const int t = g - __ldg(a.draw_start + di);
         SubTri st;
-        setup_entry_sub(v.c, d, a.records, g, t, sub, st);
+        const bool from_record = setup_entry_sub(v.c, d, a.records, g, t, sub, st) && sub == 0 &&
+                                 (__ldg(&a.records[g].flags) & REC_VALID);
         ShadeGeom geo;
         shade_geom_from(st, geo);
         float c[4];
-        shade_fragment(v.c, d, geo, t, sub, opx, opy, c);
+        if (from_record && a.attrs && d.shading != SHADE_PRIMID && d.attr_count > 0) {
+            const float4 q0 = __ldg(&a.attrs[g].a[0]), q1 = __ldg(&a.attrs[g].a[1]), q2 = __ldg(&a.attrs[g].a[2]);
+            const float a0[4] = {q0.x, q0.y, q0.z, q0.w}, a1[4] = {q1.x, q1.y, q1.z, q1.w};
+            const float a2[4] = {q2.x, q2.y, q2.z, q2.w};
+            shade_fragment_attrs(v.c, d, geo, t, sub, opx, opy, a0, a1, a2, c);
+        } else {
+            shade_fragment(v.c, d, geo, t, sub, opx, opy, c);
+        }
         scol[slot][wbase + owner] = make_float4(c[0], c[1], c[2], c[3]);
         splane[slot][wbase + owner] = make_float4(st.z[0], st.dzdx, st.dzdy, __int_as_float(st.X[0]));
         splane_y[slot][wbase + owner] = st.Y[0];

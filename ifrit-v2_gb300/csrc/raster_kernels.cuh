@@ -68,6 +68,7 @@ struct PassArgs {
     uint32_t* block_sums;    // [scan_blocks(total_tiles)] scan partials
     uint32_t* pairs;         // (global triangle << 3 | fan index), capacity entries
     TriRecord* records;      // [total_tris] compact set-ups written by the counting binner
+    TriAttr* attrs;          // [total_tris] vertex attributes of unclipped triangles, or nullptr
     uint32_t pair_capacity;
     uint32_t* status;        // StatusWord
     uint32_t* queues;        // persistent tile counters, 3 per launch group (raster, shade, ordered)

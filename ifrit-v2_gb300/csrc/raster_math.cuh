@@ -643,16 +643,44 @@ __device__ __forceinline__ void load_attr(const float* p, int attr_count, float 
 // LOD uses fine 2x2-quad derivatives: the attribute at the quad's right column minus the
 // left column (same row) and bottom row minus top row (same column), each evaluated for this
 // primitive exactly as a helper invocation would evaluate it.
+// Attributes of the three vertices of triangle t (original vertex order).
+__device__ __forceinline__ void fetch_attrs(const DrawDev& d, int t, float a0[4], float a1[4], float a2[4]) {
+    load_attr(d.vertices + (size_t)__ldg(d.indices + 3 * (size_t)t + 0) * d.stride + d.attr_offset, d.attr_count, a0);
+    load_attr(d.vertices + (size_t)__ldg(d.indices + 3 * (size_t)t + 1) * d.stride + d.attr_offset, d.attr_count, a1);
+    load_attr(d.vertices + (size_t)__ldg(d.indices + 3 * (size_t)t + 2) * d.stride + d.attr_offset, d.attr_count, a2);
+}
+
+// Vertex attributes of an unclipped triangle stored by the counting binner next to its set-up
+// record, so shading does not chase indices and vertex rows (48 bytes: 3 vertices x 4 floats).
+struct __align__(16) TriAttr {
+    float4 a[3];
+};
+
+__device__ __forceinline__ void shade_fragment_attrs(const PassConst& c, const DrawDev& d, const ShadeGeom& s, int t,
+                                                     int sub, int px, int py, const float a0[4], const float a1[4],
+                                                     const float a2[4], float col[4]);
+
 __device__ __forceinline__ void shade_fragment(const PassConst& c, const DrawDev& d, const ShadeGeom& s, int t, int sub,
                                                int px, int py, float col[4]) {
+    float a0[4], a1[4], a2[4];
+    if (d.shading == SHADE_PRIMID) {
+        a0[0] = a0[1] = a0[2] = a0[3] = 0.0f;
+        a1[0] = a1[1] = a1[2] = a1[3] = 0.0f;
+        a2[0] = a2[1] = a2[2] = a2[3] = 0.0f;
+    } else {
+        fetch_attrs(d, t, a0, a1, a2);
+    }
+    shade_fragment_attrs(c, d, s, t, sub, px, py, a0, a1, a2, col);
+}
+
+// Fragment colour from the triangle's vertex attributes.
+__device__ __forceinline__ void shade_fragment_attrs(const PassConst& c, const DrawDev& d, const ShadeGeom& s, int t,
+                                                     int sub, int px, int py, const float a0[4], const float a1[4],
+                                                     const float a2[4], float col[4]) {
     if (d.shading == SHADE_PRIMID) {
         col[0] = (float)(d.prim_base + t); col[1] = (float)sub; col[2] = 0.0f; col[3] = 1.0f;
         return;
     }
-    float a0[4], a1[4], a2[4];
-    load_attr(d.vertices + (size_t)__ldg(d.indices + 3 * (size_t)t + 0) * d.stride + d.attr_offset, d.attr_count, a0);
-    load_attr(d.vertices + (size_t)__ldg(d.indices + 3 * (size_t)t + 1) * d.stride + d.attr_offset, d.attr_count, a1);
-    load_attr(d.vertices + (size_t)__ldg(d.indices + 3 * (size_t)t + 2) * d.stride + d.attr_offset, d.attr_count, a2);
     int32_t qx = px * 256 + kShadeOffset, qy = py * 256 + kShadeOffset;
     float a[4];
     interp_attr(s, d.attr_count, a0, a1, a2, qx, qy, a);
