@@ -200,6 +200,8 @@ struct IfritGbRenderer {
     float clear_color[4] = {0, 0, 0, 0};
     float clear_depth = 1.0f;
     bool vis_output = false;
+    bool scissor_enable = false;
+    std::vector<float> scissors;  // (x, y, w, h) per rectangle, at most 16
     // device state
     DevMem d_vertices, d_indices, d_color, d_depth, d_vis, d_entries, d_sample_colors;
     const void* up_vb_key = nullptr;
@@ -478,6 +480,7 @@ void fill_state(IfritGbRenderer* h, DrawDev& d) {
     d.depth_write = h->depth_write;
     ifr::fill_blend(d, h->blend);
     d.shading = h->fs_model;
+    ifr::fill_scissor(d, h->scissor_enable, h->scissors.data(), (int)h->scissors.size() / 4);
     const Texture& t = h->tex[h->bound_tex];
     ifr::fill_texture(d, t.mem.as<uint32_t>(), t.w, t.h, t.levels, h->samplers[h->bound_sampler]);
 }
@@ -1187,6 +1190,18 @@ IFTR_API int iftrClear(IfritGbRenderer* h) {
     if (rc) return rc;
     rc = check_pending(h);
     return rc ? rc : copy_back_host_images(h);
+}
+
+IFTR_API int iftrSetScissors(IfritGbRenderer* h, const float* rects, int count) {
+    if (!h || count < 0 || count > 16 || (count > 0 && !rects)) return IFTR_ERR_INVALID_ARG;
+    h->scissors.assign(rects, rects + 4 * count);
+    return IFTR_OK;
+}
+
+IFTR_API int iftrSetScissorTestEnable(IfritGbRenderer* h, int enable) {
+    if (!h) return IFTR_ERR_INVALID_ARG;
+    h->scissor_enable = enable != 0;
+    return IFTR_OK;
 }
 
 IFTR_API int iftrSetCullMode(IfritGbRenderer* h, int m) {

@@ -5,6 +5,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cmath>
 #include <cstring>
 
 #include "../../include/ifrit_gb300.h"
@@ -18,6 +19,31 @@ inline void fill_blend(DrawDev& d, const IfritGbBlendState& b) {
     d.blend_dst_color = b.dstColorBlendFactor;
     d.blend_src_alpha = b.srcAlphaBlendFactor;
     d.blend_dst_alpha = b.dstAlphaBlendFactor;
+}
+
+// Scissor rectangles (x, y, w, h) of a draw as inclusive pixel bounds: pixel x passes the
+// reference's test x >= sx && x <= sx + sw (float compares, TileRasterCoreInvocationCuda.cu:1950-1962)
+// exactly when ceil(sx) <= x <= floor(sx + sw).  Disabled, or enabled with no rectangle: no test.
+inline int clamp_pixel_bound(float v) { return v < -1.0e9f ? -1000000000 : v > 1.0e9f ? 1000000000 : (int)v; }
+
+inline void fill_scissor(DrawDev& d, bool enable, const float* rects, int count) {
+    d.scissor_count = enable ? std::min(count, 16) : 0;
+    int box[4] = {1000000000, 1000000000, -1000000000, -1000000000};
+    for (int i = 0; i < d.scissor_count; i++) {
+        const float* r = rects + 4 * i;
+        const float x1 = r[0] + r[2], y1 = r[1] + r[3];
+        int* q = d.scissor[i];
+        q[0] = clamp_pixel_bound(std::ceil(r[0]));
+        q[1] = clamp_pixel_bound(std::ceil(r[1]));
+        q[2] = clamp_pixel_bound(std::floor(x1));
+        q[3] = clamp_pixel_bound(std::floor(y1));
+        if (q[0] > q[2] || q[1] > q[3]) continue;  // passes no pixel
+        box[0] = std::min(box[0], q[0]);
+        box[1] = std::min(box[1], q[1]);
+        box[2] = std::max(box[2], q[2]);
+        box[3] = std::max(box[3], q[3]);
+    }
+    for (int k = 0; k < 4; k++) d.scissor_box[k] = box[k];
 }
 
 // Texture and sampler of a draw; the mip chain is stored level after level, each level

@@ -48,8 +48,9 @@ __device__ __forceinline__ int find_draw_warp(const PassArgs& a, int g) {
 // Draw of a binned triangle (its record holds it).
 __device__ __forceinline__ int record_draw(const PassArgs& a, int g) { return __ldg(&a.records[g].draw); }
 
-__device__ __forceinline__ void bin_sub(const PassArgs& a, const ViewArgs& v, const SubTri& s, uint32_t entry,
-                                        bool scatter) {
+__device__ __forceinline__ void bin_sub(const PassArgs& a, const ViewArgs& v, const DrawDev& d, SubTri s,
+                                        uint32_t entry, bool scatter) {
+    if (!scissor_clamp(d, s)) return;
     const int sh = v.c.tile_shift;
     int tx0 = s.px0 >> sh, tx1 = s.px1 >> sh;
     int ty0 = s.py0 >> sh, ty1 = s.py1 >> sh;
@@ -100,7 +101,7 @@ __global__ void __launch_bounds__(256) bin_count_kernel(PassArgs a) {
         const int4* src = reinterpret_cast<const int4*>(&r);
         int4* dst = reinterpret_cast<int4*>(rec);
         dst[0] = src[0]; dst[1] = src[1]; dst[2] = src[2]; dst[3] = src[3];
-        bin_sub(a, v, s, (uint32_t)g << 3, false);
+        bin_sub(a, v, d, s, (uint32_t)g << 3, false);
         return;
     }
     rec->flags = REC_CLIPPED;
@@ -108,7 +109,7 @@ __global__ void __launch_bounds__(256) bin_count_kernel(PassArgs a) {
     int n = clip_polygon(v.c, poly);
     for (int i = 1; i + 1 < n; i++) {
         SubTri s;
-        if (setup_sub(v.c, d, poly[0], poly[i], poly[i + 1], s)) bin_sub(a, v, s, ((uint32_t)g << 3) | (uint32_t)(i - 1), false);
+        if (setup_sub(v.c, d, poly[0], poly[i], poly[i + 1], s)) bin_sub(a, v, d, s, ((uint32_t)g << 3) | (uint32_t)(i - 1), false);
     }
 }
 
@@ -125,7 +126,7 @@ __global__ void __launch_bounds__(256) bin_scatter_kernel(PassArgs a) {
     const ViewArgs& v = a.views[d.view];
     if (flags & REC_VALID) {
         SubTri s;
-        if (sub_from_record(v.c, a.records + g, s)) bin_sub(a, v, s, (uint32_t)g << 3, true);
+        if (sub_from_record(v.c, a.records + g, s)) bin_sub(a, v, d, s, (uint32_t)g << 3, true);
         return;
     }
     int t = g - __ldg(a.draw_start + di);
@@ -135,7 +136,7 @@ __global__ void __launch_bounds__(256) bin_scatter_kernel(PassArgs a) {
     int n = clip_polygon(v.c, poly);
     for (int i = 1; i + 1 < n; i++) {
         SubTri s;
-        if (setup_sub(v.c, d, poly[0], poly[i], poly[i + 1], s)) bin_sub(a, v, s, ((uint32_t)g << 3) | (uint32_t)(i - 1), true);
+        if (setup_sub(v.c, d, poly[0], poly[i], poly[i + 1], s)) bin_sub(a, v, d, s, ((uint32_t)g << 3) | (uint32_t)(i - 1), true);
     }
 }
 
@@ -355,7 +356,8 @@ __device__ __noinline__ bool setup_raster_entry(const PassArgs& a, const PassCon
     int g = (int)(e >> 3), sub = (int)(e & 7u);
     int di = record_draw(a, g);
     *draw = di;
-    return setup_entry_sub(c, a.draws[di], a.records, g, g - __ldg(a.draw_start + di), sub, *s);
+    const DrawDev& d = a.draws[di];
+    return setup_entry_sub(c, d, a.records, g, g - __ldg(a.draw_start + di), sub, *s) && scissor_clamp(d, *s);
 }
 
 // Set-up and shading of one entry at one pixel (out of line: the rare paths share one copy).
@@ -432,6 +434,7 @@ struct TileRecords {
     int32_t width[NT];  // clipped bbox width in pixels
     float rwidth[NT];   // 1 / width
     int32_t key[NT];    // entry
+    int32_t sc[NT];     // draw with a scissor test, or -1
     uint32_t start[NT + 1];  // exclusive prefix of pixel counts
 };
 
@@ -499,6 +502,7 @@ __device__ __forceinline__ void raster_tile(const PassArgs& a, const ViewArgs& v
                             rec.E[i][tid] = (int32_t)(s.Cb[i] + (int64_t)s.A[i] * (x0 * 256) + (int64_t)s.B[i] * (y0 * 256));
                     }
                     rec.org[tid] = (x0 - tx0) | ((y0 - ty0) << 8) | (small ? 0 : kLargeRecord);
+                    rec.sc[tid] = a.draws[di].scissor_count ? di : -1;
                     rec.width[tid] = w;
                     rec.rwidth[tid] = 1.0f / (float)w;
                     cnt = (uint32_t)(w * (y1 - y0 + 1));
@@ -539,6 +543,8 @@ __device__ __forceinline__ void raster_tile(const PassArgs& a, const ViewArgs& v
             const int org = rec.org[r];
             const int qx = (org & 255) + ox, qy = ((org >> 8) & 255) + oy;
             const int gx = tx0 + qx, gy = ty0 + qy;
+            const int scd = rec.sc[r];
+            if (scd >= 0 && !scissor_pass(a.draws[scd], gx, gy)) continue;
             const int32_t A[3] = {rec.A[0][r], rec.A[1][r], rec.A[2][r]};
             const int32_t B[3] = {rec.B[0][r], rec.B[1][r], rec.B[2][r]};
             unsigned cov = 0;  // covered samples of this pixel
@@ -1021,6 +1027,7 @@ __device__ __forceinline__ void forward_tile(const PassArgs& a, const ViewArgs& 
                 const int32_t B[3] = {rec.B[0][r], rec.B[1][r], rec.B[2][r]};
                 const int64_t Cb[3] = {rec.Cb[0][r], rec.Cb[1][r], rec.Cb[2][r]};
                 const DrawDev& d = a.draws[rec.draw[r]];
+                if (!scissor_pass(d, px, py)) continue;
                 const int func = d.depth_func, write = d.depth_write;
                 const int e = rec.key[r];
                 unsigned mask = 0;

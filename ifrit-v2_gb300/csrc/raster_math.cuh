@@ -46,7 +46,18 @@ struct DrawDev {
     int tex_w, tex_h, tex_levels;
     SamplerDev sampler;
     int lvl_off[16], lvl_w[16], lvl_h[16];  // mip table: texel offset and size of each level
+    // scissor test: with scissor_count > 0 a pixel is kept iff it lies in one of the rectangles
+    // (inclusive pixel bounds x0, y0, x1, y1); scissor_box is their union's bounds
+    int scissor_count;
+    int scissor_box[4];
+    int scissor[16][4];
 };
+
+__device__ __forceinline__ bool scissor_pass(const DrawDev& d, int x, int y) {
+    for (int i = 0; i < d.scissor_count; i++)
+        if (x >= d.scissor[i][0] && x <= d.scissor[i][2] && y >= d.scissor[i][1] && y <= d.scissor[i][3]) return true;
+    return d.scissor_count == 0;
+}
 
 // Standard sample positions in 1/256 pixel (the D3D 1/2/4/8/16x patterns): (x, y) of sample k
 // of an S-sample pixel.  With S and k compile-time constants (templated sample counts, unrolled
@@ -178,6 +189,17 @@ __device__ __forceinline__ bool sub_bbox(const PassConst& c, SubTri& o) {
 }
 
 // Edge functions E_i = A_i x + B_i y + C_i (positive inside) and their top-left biased form.
+// Clamps the pixel range of a set-up triangle to the draw's scissor rectangles' union; false when
+// nothing is left.
+__device__ __forceinline__ bool scissor_clamp(const DrawDev& d, SubTri& s) {
+    if (d.scissor_count == 0) return true;
+    s.px0 = max(s.px0, d.scissor_box[0]);
+    s.py0 = max(s.py0, d.scissor_box[1]);
+    s.px1 = min(s.px1, d.scissor_box[2]);
+    s.py1 = min(s.py1, d.scissor_box[3]);
+    return s.px0 <= s.px1 && s.py0 <= s.py1;
+}
+
 __device__ __forceinline__ void sub_edges(SubTri& o) {
 #pragma unroll
     for (int i = 0; i < 3; i++) {

@@ -44,7 +44,7 @@ EXPORTED = [
     "ifbufBufferData", "iftrSetStageTiming", "iftrGetStageTimes", "iftrGetVertexBufferRawData",
     "iftrSetVertexBufferDirty", "ifbufGetBufferRawData", "ifbufSetBufferDirty", "iftrDrawNoAlloc",
     "iftrBeginPass", "iftrPassDraw", "iftrEndPass", "iftrDrawBatch", "iftrSetBatchTuning", "iftrGetBatchTuning",
-    "iftrDiffForward", "iftrDiffBackward",
+    "iftrDiffForward", "iftrDiffBackward", "iftrSetScissors", "iftrSetScissorTestEnable",
 ]
 
 
@@ -165,6 +165,7 @@ def load(build_if_missing=True):
         "iftrSetBatchTuning": [vp, ip, ip, ip],
         "iftrGetBatchTuning": [vp, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)],
         "iftrDiffForward": [ctypes.POINTER(DiffPass), vp], "iftrDiffBackward": [ctypes.POINTER(DiffPass), vp],
+        "iftrSetScissors": [vp, fp, ip], "iftrSetScissorTestEnable": [vp, ip],
     }
     for name, args in sig.items():
         getattr(lib, name).argtypes = args
@@ -263,6 +264,12 @@ class Renderer:
         """Blend factors use the IfritBlendFactor numbering (6 SRC_ALPHA, 7 ONE_MINUS_SRC_ALPHA)."""
         s = BlendState(int(enable), src_color, dst_color, src_alpha, dst_alpha)
         check("iftrSetBlendFunc", self.lib.iftrSetBlendFunc(self.h, ctypes.byref(s)))
+
+    def set_scissors(self, rects, enable=True):
+        """rects: list of (x, y, w, h); enable False switches the test off."""
+        arr = (ctypes.c_float * (4 * max(1, len(rects))))(*[float(x) for r in rects for x in r])
+        check("iftrSetScissors", self.lib.iftrSetScissors(self.h, arr, len(rects)))
+        check("iftrSetScissorTestEnable", self.lib.iftrSetScissorTestEnable(self.h, int(enable)))
 
     def begin_pass(self, clear=True):
         check("iftrBeginPass", self.lib.iftrBeginPass(self.h, int(clear)))

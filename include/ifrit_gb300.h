@@ -136,6 +136,11 @@ IFTR_API int iftrSetFrontFace(IfritGbRenderer* h, int counterClockwise);
 IFTR_API int iftrSetMsaaSamples(IfritGbRenderer* h, int samples);                    /* TRC:103, 1/2/4/8/16 */
 IFTR_API int iftrSetClearValues(IfritGbRenderer* h, const float* rgba, float depth); /* TRC:108 */
 IFTR_API int iftrSetDepthWriteEnable(IfritGbRenderer* h, int enable);
+/* Scissor rectangles (x, y, w, h), at most 16, and the scissor test switch (TRC:101-102): with the
+ * test on and at least one rectangle, a pixel (x, y) is drawn iff x >= rx, x <= rx + rw, y >= ry
+ * and y <= ry + rh for one rectangle (bounds inclusive, as the reference's test). */
+IFTR_API int iftrSetScissors(IfritGbRenderer* h, const float* rects, int count);
+IFTR_API int iftrSetScissorTestEnable(IfritGbRenderer* h, int enable);
 IFTR_API int iftrCreateTexture(IfritGbRenderer* h, int slot, int width, int height, int mipLevels); /* TRC:91, RGBA8 */
 IFTR_API int iftrCopyHostBufferToImage(IfritGbRenderer* h, const void* rgba8, int slot); /* TRC:96, level 0 */
 IFTR_API int iftrGenerateMipmap(IfritGbRenderer* h, int slot, int filter);           /* TRC:93 */

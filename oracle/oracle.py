@@ -48,7 +48,9 @@ class Draw(ctypes.Structure):
                 ("depth_func", ctypes.c_int), ("depth_write", ctypes.c_int), ("blend_enable", ctypes.c_int),
                 ("blend_src_color", ctypes.c_int), ("blend_dst_color", ctypes.c_int),
                 ("blend_src_alpha", ctypes.c_int), ("blend_dst_alpha", ctypes.c_int),
-                ("shading", ctypes.c_int), ("tex", Texture), ("sampler", Sampler)]
+                ("shading", ctypes.c_int), ("tex", Texture), ("sampler", Sampler),
+                ("scissor_enable", ctypes.c_int), ("scissor_count", ctypes.c_int),
+                ("scissor", (ctypes.c_float * 4) * 16)]
 
 
 class Target(ctypes.Structure):
@@ -98,7 +100,7 @@ def build_mips(level0):
 
 def make_draw(vertices, indices, mvp, *, attr_offset=3, attr_count=3, prim_base=0, cull_mode=2,
               front_ccw=1, depth_test=1, depth_func=3, depth_write=1, blend=None, shading=SHADE_GOURAUD,
-              texture=None, sampler=None):
+              texture=None, sampler=None, scissor=None):
     """Returns (Draw, keepalive) for numpy vertices (V, stride) float32 and indices (T, 3) int32."""
     vertices = np.ascontiguousarray(vertices, np.float32)
     indices = np.ascontiguousarray(indices, np.int32).reshape(-1)
@@ -133,6 +135,12 @@ def make_draw(vertices, indices, mvp, *, attr_offset=3, attr_count=3, prim_base=
     d.sampler.border_white = s.get("border_white", 0)
     d.sampler.max_aniso = s.get("max_aniso", 1)
     d.sampler.lod_bias = s.get("lod_bias", 0.0)
+    if scissor is not None:  # list of (x, y, w, h) rectangles; [] = enabled with none (passes all)
+        d.scissor_enable = 1
+        d.scissor_count = min(len(scissor), 16)
+        for i, r in enumerate(scissor[:16]):
+            for k in range(4):
+                d.scissor[i][k] = float(r[k])
     return d, keep
 
 

@@ -588,6 +588,17 @@ typedef struct {
     int y0, y1;
 } band_job;
 
+/* Scissor test of pixel (x, y) for draw d (TileRasterCoreInvocationCuda.cu:1950-1962). */
+static int scissor_pass(const ofx_draw* d, int x, int y) {
+    if (!d->scissor_enable || d->scissor_count <= 0) return 1;
+    for (int i = 0; i < d->scissor_count && i < 16; i++) {
+        const float* r = d->scissor[i];
+        const float fx = (float)x, fy = (float)y;
+        if (fx >= r[0] && fx <= r[0] + r[2] && fy >= r[1] && fy <= r[1] + r[3]) return 1;
+    }
+    return 0;
+}
+
 static void* run_band(void* arg) {
     band_job* j = (band_job*)arg;
     const pass_ctx* c = j->c;
@@ -604,6 +615,7 @@ static void* run_band(void* arg) {
                 int ya = imax_(s->py0, j->y0), yb = imin_(s->py1, j->y1 - 1);
                 for (int py = ya; py <= yb; py++) {
                     for (int px = s->px0; px <= s->px1; px++) {
+                        if (!scissor_pass(d, px, py)) continue;
                         size_t base = ((size_t)py * c->W + px) * S;
                         unsigned passmask = 0;
                         for (int k = 0; k < S; k++) {

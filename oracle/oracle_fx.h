@@ -55,6 +55,12 @@ typedef struct {
     int shading;                /* OFX_SHADE_* */
     ofx_texture tex;
     ofx_sampler sampler;
+    /* scissor test (TileRasterRendererCuda.h:101-102, TileRasterCoreInvocationCuda.cu:1950-1962):
+     * with scissor_enable and scissor_count > 0 a pixel (x, y) is kept iff for one rectangle
+     * (sx, sy, sw, sh): x >= sx, x <= sx + sw, y >= sy, y <= sy + sh (float compares) */
+    int scissor_enable;
+    int scissor_count;
+    float scissor[16][4];       /* x, y, w, h */
 } ofx_draw;
 
 typedef struct {

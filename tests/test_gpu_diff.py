@@ -77,8 +77,8 @@ def test_gradients_match_fp64_adjoint():
     e2e = {"positions": _norm_err(pos.grad.cpu().numpy(), gp), "colors": _norm_err(col.grad.cpu().numpy(), gc),
            "uvs": _norm_err(uv.grad.cpu().numpy(), gu)}
     print("loss gpu %.6f fp64 %.6f; max normalised gradient error vs the fp64 adjoint: %s; end to end: %s"
-          % (float(loss), L64, adj, e2e))
-    assert abs(float(loss) - L64) <= 1e-4 * L64
+          % (float(loss.detach()), L64, adj, e2e))
+    assert abs(float(loss.detach()) - L64) <= 1e-4 * L64
     for k in adj:
         assert adj[k] <= 1e-3 and e2e[k] <= 1e-3, (k, adj[k], e2e[k])
     dr.close()

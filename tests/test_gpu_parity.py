@@ -269,3 +269,54 @@ def test_stress_style_pass_small():
     assert_parity(gpu, ref, fmt=ig.FORMAT_RGBA16F)
     assert (gpu["vis"] >= 0).mean() > 0.5
     r.close()
+
+
+def test_scissor_rectangles_single_and_multi_draw():
+    """Scissor test per draw: a soup under two rectangles at 4x; then a pass whose draws carry
+    different scissor state, one of them blended (in-order stage)."""
+    from oracle import oracle as O
+    W, H = 200, 150
+    v, f, mvp = soup(8000, 31, W, H)
+    rects = [(13.5, 20.0, 60.25, 40.0), (90.0, 70.5, 70.0, 60.0)]
+    r = ig.Renderer(W, H, 4, ig.FORMAT_RGBA8, visibility=True)
+    r.set_state(cull=ig.CULL_NONE, depth_func=ig.LESS_OR_EQUAL)
+    r.set_mvp(mvp)
+    r.set_geometry(v, f, 2)
+    r.set_scissors(rects)
+    r.draw(clear=True)
+    gpu = {"color": r.color(), "depth": r.depth(), "vis": r.visibility()}
+    d = O.make_draw(v, f, mvp, attr_offset=3, attr_count=2, cull_mode=0, depth_func=3, scissor=rects)
+    ref = O.render([d], W, H, 4, clear=True, nthreads=os.cpu_count() or 1)
+    assert_parity(gpu, ref)
+    inside = np.zeros((H, W), bool)
+    inside[20:61, 14:74] = True
+    inside[71:131, 90:161] = True
+    assert not (gpu["vis"][~inside] >= 0).any() and (gpu["vis"][inside] >= 0).mean() > 0.5
+    r.close()
+    # multi-draw pass: opaque draw under one rectangle, opaque draw without scissor, blended draw
+    # under another rectangle
+    vr, fr, mvpr = _rgba_soup(6000, 32, W, H)
+    half = len(fr) // 3
+    r = ig.Renderer(W, H, 4, ig.FORMAT_RGBA8, visibility=True)
+    r.set_geometry(vr, fr, 4)
+    r.set_mvp(mvpr)
+    r.begin_pass(clear=True)
+    plan = [((0, 3 * half), [(10.0, 10.0, 100.0, 80.0)], None),
+            ((3 * half, 3 * half), None, None),
+            ((6 * half, 3 * (len(fr) - 2 * half)), [(50.0, 40.0, 120.0, 100.0)], (6, 7, 1, 7))]
+    odraws, base = [], 0
+    for (first, count), sc, blend in plan:
+        r.set_state(cull=ig.CULL_NONE, depth_func=ig.LESS_OR_EQUAL, depth_write=blend is None,
+                    clear_color=(0.1, 0.2, 0.3, 1.0))
+        r.set_blend(blend is not None, *(blend or (6, 7, 1, 7)))
+        r.set_scissors(sc or [], enable=sc is not None)
+        r.pass_draw(first, count)
+        sub = fr[first // 3:(first + count) // 3]
+        odraws.append(O.make_draw(vr, sub, mvpr, attr_offset=3, attr_count=4, cull_mode=0, depth_func=3,
+                                  depth_write=int(blend is None), blend=blend, scissor=sc, prim_base=base))
+        base += len(sub)
+    r.end_pass()
+    gpu = {"color": r.color(), "depth": r.depth(), "vis": r.visibility()}
+    ref = O.render(odraws, W, H, 4, clear=True, clear_color=(0.1, 0.2, 0.3, 1.0), nthreads=os.cpu_count() or 1)
+    assert_parity(gpu, ref)
+    r.close()

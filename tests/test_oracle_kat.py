@@ -182,3 +182,22 @@ def test_texture_constant_and_lod():
         out = (ctypes.c_float * 4)()
         O.lib().ofx_sample_texture(ctypes.byref(tex), ctypes.byref(s), 0.3, 0.7, 0.05, 0.0, 0.0, 0.004, out)
         assert np.allclose(list(out), [0x99 / 255, 0x66 / 255, 0x33 / 255, 1.0], atol=1e-6)
+
+
+def test_scissor_rectangles_inclusive_bounds():
+    # full-screen quad; scissor (2.5, 1, 3, 2): pixels with 2.5 <= x <= 5.5 and 1 <= y <= 3, i.e.
+    # x in 3..5 and y in 1..3 (the reference's inclusive float test); a second rectangle adds
+    # pixel column 7; enabled with no rectangle keeps everything
+    v = tri_vertices([[-1, -1, 0.5], [1, -1, 0.5], [1, 1, 0.5], [-1, 1, 0.5]])
+    f = np.array([[0, 1, 2], [0, 2, 3]], np.int32)
+    d = O.make_draw(v, f, EYE, depth_func=7, cull_mode=0, scissor=[(2.5, 1.0, 3.0, 2.0)])
+    vis = O.render([d], 8, 6, 1)["vis"][..., 0] >= 0
+    want = np.zeros((6, 8), bool)
+    want[1:4, 3:6] = True
+    assert (vis == want).all()
+    d = O.make_draw(v, f, EYE, depth_func=7, cull_mode=0, scissor=[(2.5, 1.0, 3.0, 2.0), (7.0, 0.0, 0.0, 5.0)])
+    vis = O.render([d], 8, 6, 4)["vis"] >= 0
+    want[0:6, 7] = True
+    assert (vis == want[..., None]).all()
+    d = O.make_draw(v, f, EYE, depth_func=7, cull_mode=0, scissor=[])
+    assert (O.render([d], 8, 6, 1)["vis"] >= 0).all()
