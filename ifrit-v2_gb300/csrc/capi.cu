@@ -200,6 +200,7 @@ struct IfritGbRenderer {
     float clear_color[4] = {0, 0, 0, 0};
     float clear_depth = 1.0f;
     bool vis_output = false;
+    int polygon_mode = 0;  // IF_POLYGON_MODE_*
     bool scissor_enable = false;
     std::vector<float> scissors;  // (x, y, w, h) per rectangle, at most 16
     // device state
@@ -481,6 +482,7 @@ void fill_state(IfritGbRenderer* h, DrawDev& d) {
     ifr::fill_blend(d, h->blend);
     d.shading = h->fs_model;
     ifr::fill_scissor(d, h->scissor_enable, h->scissors.data(), (int)h->scissors.size() / 4);
+    d.polygon_mode = h->polygon_mode;
     const Texture& t = h->tex[h->bound_tex];
     ifr::fill_texture(d, t.mem.as<uint32_t>(), t.w, t.h, t.levels, h->samplers[h->bound_sampler]);
 }
@@ -1195,6 +1197,12 @@ IFTR_API int iftrClear(IfritGbRenderer* h) {
 IFTR_API int iftrSetScissors(IfritGbRenderer* h, const float* rects, int count) {
     if (!h || count < 0 || count > 16 || (count > 0 && !rects)) return IFTR_ERR_INVALID_ARG;
     h->scissors.assign(rects, rects + 4 * count);
+    return IFTR_OK;
+}
+
+IFTR_API int iftrSetRasterizerPolygonMode(IfritGbRenderer* h, int mode) {
+    if (!h || mode < IF_POLYGON_MODE_FILL || mode > IF_POLYGON_MODE_POINT) return IFTR_ERR_INVALID_ARG;
+    h->polygon_mode = mode;
     return IFTR_OK;
 }
 

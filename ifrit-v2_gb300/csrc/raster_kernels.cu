@@ -81,6 +81,32 @@ __global__ void __launch_bounds__(256) bin_count_kernel(PassArgs a) {
         rec->flags = 0;
         return;
     }
+    if (d.polygon_mode != POLY_FILL) {  // LINE / POINT: record the projected triangle, bin its parts
+        SubTri tri;
+        if (!inside || !project_oriented(v.c, d, poly, tri)) {
+            rec->flags = 0;
+            return;
+        }
+        TriRecord r;
+        mode_record_from_tri(tri, r);
+        r.draw = di;
+        if (a.attrs && d.shading != SHADE_PRIMID && d.attr_count > 0) {
+            float a0[4], a1[4], a2[4];
+            fetch_attrs(d, t, a0, a1, a2);
+            float4* dst = a.attrs[g].a;
+            dst[0] = make_float4(a0[0], a0[1], a0[2], a0[3]);
+            dst[1] = make_float4(a1[0], a1[1], a1[2], a1[3]);
+            dst[2] = make_float4(a2[0], a2[1], a2[2], a2[3]);
+        }
+        const int4* src = reinterpret_cast<const int4*>(&r);
+        int4* dst = reinterpret_cast<int4*>(rec);
+        dst[0] = src[0]; dst[1] = src[1]; dst[2] = src[2]; dst[3] = src[3];
+        for (int sub = 0; sub < 6; sub++) {
+            SubTri s;
+            if (mode_sub(v.c, d.polygon_mode, tri, sub, s)) bin_sub(a, v, d, s, ((uint32_t)g << 3) | (uint32_t)sub, false);
+        }
+        return;
+    }
     if (inside) {
         SubTri s;
         if (!setup_sub(v.c, d, poly[0], poly[1], poly[2], s)) {
@@ -124,6 +150,15 @@ __global__ void __launch_bounds__(256) bin_scatter_kernel(PassArgs a) {
     const int di = record_draw(a, g);
     const DrawDev& d = a.draws[di];
     const ViewArgs& v = a.views[d.view];
+    if (d.polygon_mode != POLY_FILL) {
+        SubTri tri;
+        tri_from_mode_record(a.records + g, tri);
+        for (int sub = 0; sub < 6; sub++) {
+            SubTri s;
+            if (mode_sub(v.c, d.polygon_mode, tri, sub, s)) bin_sub(a, v, d, s, ((uint32_t)g << 3) | (uint32_t)sub, true);
+        }
+        return;
+    }
     if (flags & REC_VALID) {
         SubTri s;
         if (sub_from_record(v.c, a.records + g, s)) bin_sub(a, v, d, s, (uint32_t)g << 3, true);

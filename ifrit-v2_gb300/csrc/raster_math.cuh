@@ -51,7 +51,15 @@ struct DrawDev {
     int scissor_count;
     int scissor_box[4];
     int scissor[16][4];
+    int polygon_mode;  // POLY_FILL / POLY_LINE / POLY_POINT
 };
+
+// Polygon modes (IfritPolygonMode, base/Constants.h:23-28).  LINE: each edge of the culled,
+// orientation-normalised triangle is a 1-pixel-wide parallelogram offset +-1/2 pixel along the
+// minor axis; POINT: each vertex is a 1-pixel square.  Each part is two sub-triangles
+// (sub = 2 * part + half) rasterised with the fill rules; triangles that need clipping are
+// dropped in these modes.
+enum { POLY_FILL = 0, POLY_LINE = 1, POLY_POINT = 2 };
 
 __device__ __forceinline__ bool scissor_pass(const DrawDev& d, int x, int y) {
     for (int i = 0; i < d.scissor_count; i++)
@@ -338,8 +346,148 @@ __device__ __forceinline__ bool sub_from_record(const PassConst& c, const TriRec
 }
 
 // Set-up of fan triangle `sub` of triangle t, from its record when it is an unclipped one.
+// Completes a sub-triangle whose X, Y, z, iw and bary are set: orientation, pixel range, edge
+// functions and depth plane (no culling).
+__device__ __forceinline__ bool finish_sub(const PassConst& c, SubTri& o) {
+    int64_t a2 = (int64_t)(o.X[1] - o.X[0]) * (o.Y[2] - o.Y[0]) - (int64_t)(o.X[2] - o.X[0]) * (o.Y[1] - o.Y[0]);
+    if (a2 == 0) return false;
+    o.swapped = 0;
+    if (a2 < 0) {
+        o.swapped = 1;
+        int32_t t;
+        float tf;
+        t = o.X[1]; o.X[1] = o.X[2]; o.X[2] = t;
+        t = o.Y[1]; o.Y[1] = o.Y[2]; o.Y[2] = t;
+        tf = o.z[1]; o.z[1] = o.z[2]; o.z[2] = tf;
+        tf = o.iw[1]; o.iw[1] = o.iw[2]; o.iw[2] = tf;
+#pragma unroll
+        for (int k = 0; k < 3; k++) { tf = o.bary[1][k]; o.bary[1][k] = o.bary[2][k]; o.bary[2][k] = tf; }
+        a2 = -a2;
+    }
+    if (!sub_bbox(c, o)) return false;
+    sub_edges(o);
+    float dX1 = (float)(o.X[1] - o.X[0]), dY1 = (float)(o.Y[1] - o.Y[0]);
+    float dX2 = (float)(o.X[2] - o.X[0]), dY2 = (float)(o.Y[2] - o.Y[0]);
+    float dz1 = o.z[1] - o.z[0], dz2 = o.z[2] - o.z[0];
+    float fa = (float)a2;
+    o.dzdx = (dz1 * dY2 - dz2 * dY1) / fa;
+    o.dzdy = (dz2 * dX1 - dz1 * dX2) / fa;
+    return true;
+}
+
+// Projection, 16.8 snap, cull and orientation normalisation of a whole unclipped triangle, without
+// a pixel range: the base of the LINE / POINT modes.
+__device__ __forceinline__ bool project_oriented(const PassConst& c, const DrawDev& d, const CVert* v, SubTri& o) {
+#pragma unroll
+    for (int i = 0; i < 3; i++) {
+        float iw = 1.0f / v[i].p[3];
+        float xn = v[i].p[0] * iw, yn = v[i].p[1] * iw, zn = v[i].p[2] * iw;
+        float fx = fminf(fmaxf((xn * 0.5f + 0.5f) * c.W256, -kSnapLimit), kSnapLimit);
+        float fy = fminf(fmaxf((yn * 0.5f + 0.5f) * c.H256, -kSnapLimit), kSnapLimit);
+        o.X[i] = __float2int_rn(fx);
+        o.Y[i] = __float2int_rn(fy);
+        o.z[i] = zn;
+        o.iw[i] = iw;
+#pragma unroll
+        for (int k = 0; k < 3; k++) o.bary[i][k] = v[i].b[k];
+    }
+    int64_t a2 = (int64_t)(o.X[1] - o.X[0]) * (o.Y[2] - o.Y[0]) - (int64_t)(o.X[2] - o.X[0]) * (o.Y[1] - o.Y[0]);
+    if (a2 == 0) return false;
+    const bool front = d.front_ccw ? (a2 > 0) : (a2 < 0);
+    if (d.cull_mode == 3 || (d.cull_mode == 1 && front) || (d.cull_mode == 2 && !front)) return false;
+    o.swapped = 0;
+    if (a2 < 0) {
+        o.swapped = 1;
+        int32_t t;
+        float tf;
+        t = o.X[1]; o.X[1] = o.X[2]; o.X[2] = t;
+        t = o.Y[1]; o.Y[1] = o.Y[2]; o.Y[2] = t;
+        tf = o.z[1]; o.z[1] = o.z[2]; o.z[2] = tf;
+        tf = o.iw[1]; o.iw[1] = o.iw[2]; o.iw[2] = tf;
+#pragma unroll
+        for (int k = 0; k < 3; k++) { tf = o.bary[1][k]; o.bary[1][k] = o.bary[2][k]; o.bary[2][k] = tf; }
+    }
+    return true;
+}
+
+// Sub-triangle `sub` of a LINE / POINT mode triangle (t: the oriented projected triangle).
+__device__ __forceinline__ bool mode_sub(const PassConst& c, int mode, const SubTri& t, int sub, SubTri& o) {
+    const int part = sub >> 1, half = sub & 1;
+    int32_t cx[4], cy[4];
+    int src[4];
+    if (mode == POLY_LINE) {
+        const int p = part, q = part == 2 ? 0 : part + 1;
+        const int32_t dx = t.X[q] - t.X[p], dy = t.Y[q] - t.Y[p];
+        if (dx == 0 && dy == 0) return false;
+        const bool xmajor = abs(dx) >= abs(dy);
+        const int32_t ox = xmajor ? 0 : 128, oy = xmajor ? 128 : 0;
+        cx[0] = t.X[p] - ox; cy[0] = t.Y[p] - oy; src[0] = p;
+        cx[1] = t.X[q] - ox; cy[1] = t.Y[q] - oy; src[1] = q;
+        cx[2] = t.X[q] + ox; cy[2] = t.Y[q] + oy; src[2] = q;
+        cx[3] = t.X[p] + ox; cy[3] = t.Y[p] + oy; src[3] = p;
+    } else {
+        const int p = part;
+        cx[0] = t.X[p] - 128; cy[0] = t.Y[p] - 128;
+        cx[1] = t.X[p] + 128; cy[1] = t.Y[p] - 128;
+        cx[2] = t.X[p] + 128; cy[2] = t.Y[p] + 128;
+        cx[3] = t.X[p] - 128; cy[3] = t.Y[p] + 128;
+        src[0] = src[1] = src[2] = src[3] = p;
+    }
+#pragma unroll
+    for (int i = 0; i < 3; i++) {
+        const int k = i == 0 ? 0 : (half == 0 ? i : i + 1);  // halves (0, 1, 2) and (0, 2, 3)
+        o.X[i] = cx[k];
+        o.Y[i] = cy[k];
+        o.z[i] = t.z[src[k]];
+        o.iw[i] = t.iw[src[k]];
+#pragma unroll
+        for (int m = 0; m < 3; m++) o.bary[i][m] = t.bary[src[k]][m];
+    }
+    return finish_sub(c, o);
+}
+
+// The oriented projected triangle of a LINE / POINT mode record (its depth-plane fields hold the
+// second and third vertices' depths).
+__device__ __forceinline__ void tri_from_mode_record(const TriRecord* rp, SubTri& o) {
+    const int4 q0 = __ldg(reinterpret_cast<const int4*>(rp));
+    const int4 q1 = __ldg(reinterpret_cast<const int4*>(rp) + 1);
+    const float4 q2 = __ldg(reinterpret_cast<const float4*>(rp) + 2);
+    const float4 q3 = __ldg(reinterpret_cast<const float4*>(rp) + 3);
+    o.X[0] = q0.x; o.Y[0] = q0.y; o.X[1] = q0.z; o.Y[1] = q0.w;
+    o.X[2] = q1.x; o.Y[2] = q1.y;
+    o.swapped = (q1.z & REC_SWAPPED) != 0;
+    o.z[0] = q2.x; o.z[1] = q2.y; o.z[2] = q2.z;
+    o.iw[0] = q2.w; o.iw[1] = q3.x; o.iw[2] = q3.y;
+#pragma unroll
+    for (int i = 0; i < 3; i++)
+#pragma unroll
+        for (int k = 0; k < 3; k++) o.bary[i][k] = 0.0f;
+    o.bary[0][0] = 1.0f;
+    o.bary[1][o.swapped ? 2 : 1] = 1.0f;
+    o.bary[2][o.swapped ? 1 : 2] = 1.0f;
+}
+
+__device__ __forceinline__ void mode_record_from_tri(const SubTri& t, TriRecord& r) {
+    r.X0 = t.X[0]; r.Y0 = t.Y[0]; r.X1 = t.X[1]; r.Y1 = t.Y[1];
+    r.X2 = t.X[2]; r.Y2 = t.Y[2];
+    r.flags = REC_VALID | (t.swapped ? REC_SWAPPED : 0);
+    r.z0 = t.z[0]; r.dzdx = t.z[1]; r.dzdy = t.z[2];
+    r.iw0 = t.iw[0]; r.iw1 = t.iw[1]; r.iw2 = t.iw[2]; r.pad1 = 0.0f; r.pad2 = 0.0f;
+}
+
+// Set-up of LINE / POINT sub-triangle `sub` of binned triangle g (every such triangle has a
+// record).  Out of line: keeps the fill path's frame small.
+static __device__ __noinline__ bool setup_mode_entry(const PassConst& c, int mode, const TriRecord* records, int g,
+                                                     int sub, SubTri* o) {
+    if (!(__ldg(&records[g].flags) & REC_VALID)) return false;
+    SubTri tri;
+    tri_from_mode_record(records + g, tri);
+    return mode_sub(c, mode, tri, sub, *o);
+}
+
 __device__ __forceinline__ bool setup_entry_sub(const PassConst& c, const DrawDev& d, const TriRecord* records, int g,
                                                 int t, int sub, SubTri& o) {
+    if (d.polygon_mode != POLY_FILL) return setup_mode_entry(c, d.polygon_mode, records, g, sub, &o);
     if (records && sub == 0) {
         int flags = __ldg(&records[g].flags);
         if (flags & REC_VALID) return sub_from_record(c, records + g, o);

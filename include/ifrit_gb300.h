@@ -43,6 +43,7 @@ enum {
 };
 
 /* ---- enums (same numbering as the reference, base/Constants.h:23-96, TypeDescriptor.h:26-40) */
+enum { IF_POLYGON_MODE_FILL = 0, IF_POLYGON_MODE_LINE = 1, IF_POLYGON_MODE_POINT = 2 };
 enum { IFTP_FLOAT1 = 1, IFTP_FLOAT2 = 2, IFTP_FLOAT3 = 3, IFTP_FLOAT4 = 4 };
 enum { IF_CULL_MODE_NONE = 0, IF_CULL_MODE_FRONT = 1, IF_CULL_MODE_BACK = 2, IF_CULL_MODE_FRONT_AND_BACK = 3 };
 enum {
@@ -140,6 +141,11 @@ IFTR_API int iftrSetDepthWriteEnable(IfritGbRenderer* h, int enable);
  * test on and at least one rectangle, a pixel (x, y) is drawn iff x >= rx, x <= rx + rw, y >= ry
  * and y <= ry + rh for one rectangle (bounds inclusive, as the reference's test). */
 IFTR_API int iftrSetScissors(IfritGbRenderer* h, const float* rects, int count);
+/* Polygon mode (TRC:106 setRasterizerPolygonMode): FILL; LINE draws each edge of a (culled)
+ * triangle as a 1-pixel-wide parallelogram offset +-1/2 pixel along the edge's minor axis; POINT
+ * draws each vertex as a 1-pixel square.  Both go through the fill rules (MSAA, depth, shading);
+ * triangles that need clipping are dropped in these modes. */
+IFTR_API int iftrSetRasterizerPolygonMode(IfritGbRenderer* h, int mode);
 IFTR_API int iftrSetScissorTestEnable(IfritGbRenderer* h, int enable);
 IFTR_API int iftrCreateTexture(IfritGbRenderer* h, int slot, int width, int height, int mipLevels); /* TRC:91, RGBA8 */
 IFTR_API int iftrCopyHostBufferToImage(IfritGbRenderer* h, const void* rgba8, int slot); /* TRC:96, level 0 */

@@ -15,6 +15,7 @@ LIB_PATH = os.path.join(HERE, "liboracle_fx.so")
 
 FMT_RGBA8, FMT_RGBA16F, FMT_RGBA32F, FMT_RGB32F = 0, 1, 2, 3
 SHADE_GOURAUD, SHADE_TEXTURED, SHADE_PRIMID = 0, 1, 2
+POLY_FILL, POLY_LINE, POLY_POINT = 0, 1, 2
 
 
 def build(force=False):
@@ -50,7 +51,7 @@ class Draw(ctypes.Structure):
                 ("blend_src_alpha", ctypes.c_int), ("blend_dst_alpha", ctypes.c_int),
                 ("shading", ctypes.c_int), ("tex", Texture), ("sampler", Sampler),
                 ("scissor_enable", ctypes.c_int), ("scissor_count", ctypes.c_int),
-                ("scissor", (ctypes.c_float * 4) * 16)]
+                ("scissor", (ctypes.c_float * 4) * 16), ("polygon_mode", ctypes.c_int)]
 
 
 class Target(ctypes.Structure):
@@ -100,7 +101,7 @@ def build_mips(level0):
 
 def make_draw(vertices, indices, mvp, *, attr_offset=3, attr_count=3, prim_base=0, cull_mode=2,
               front_ccw=1, depth_test=1, depth_func=3, depth_write=1, blend=None, shading=SHADE_GOURAUD,
-              texture=None, sampler=None, scissor=None):
+              texture=None, sampler=None, scissor=None, polygon_mode=0):
     """Returns (Draw, keepalive) for numpy vertices (V, stride) float32 and indices (T, 3) int32."""
     vertices = np.ascontiguousarray(vertices, np.float32)
     indices = np.ascontiguousarray(indices, np.int32).reshape(-1)
@@ -135,6 +136,7 @@ def make_draw(vertices, indices, mvp, *, attr_offset=3, attr_count=3, prim_base=
     d.sampler.border_white = s.get("border_white", 0)
     d.sampler.max_aniso = s.get("max_aniso", 1)
     d.sampler.lod_bias = s.get("lod_bias", 0.0)
+    d.polygon_mode = polygon_mode
     if scissor is not None:  # list of (x, y, w, h) rectangles; [] = enabled with none (passes all)
         d.scissor_enable = 1
         d.scissor_count = min(len(scissor), 16)

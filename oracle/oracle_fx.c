@@ -469,6 +469,113 @@ static int setup_sub(const pass_ctx* c, const ofx_draw* d, const cvert* v0, cons
 }
 
 /* Full per-triangle front end: fetch, transform, clip, fan; returns sub-triangle count. */
+/* Completes a sub-triangle whose X, Y, z, iw and bary are set: orientation, pixel range, edge
+ * functions and depth plane (no culling). */
+static int finish_sub(const pass_ctx* c, int prim, int sub, ofx_sub* o) {
+    int64_t a2 = (int64_t)(o->X[1] - o->X[0]) * (o->Y[2] - o->Y[0]) - (int64_t)(o->X[2] - o->X[0]) * (o->Y[1] - o->Y[0]);
+    if (a2 == 0) return 0;
+    if (a2 < 0) {
+        int32_t t32;
+        float tf;
+        t32 = o->X[1]; o->X[1] = o->X[2]; o->X[2] = t32;
+        t32 = o->Y[1]; o->Y[1] = o->Y[2]; o->Y[2] = t32;
+        tf = o->z[1]; o->z[1] = o->z[2]; o->z[2] = tf;
+        tf = o->iw[1]; o->iw[1] = o->iw[2]; o->iw[2] = tf;
+        for (int k = 0; k < 3; k++) { tf = o->bary[1][k]; o->bary[1][k] = o->bary[2][k]; o->bary[2][k] = tf; }
+        a2 = -a2;
+    }
+    int32_t xmin = imin_(o->X[0], imin_(o->X[1], o->X[2])), xmax = imax_(o->X[0], imax_(o->X[1], o->X[2]));
+    int32_t ymin = imin_(o->Y[0], imin_(o->Y[1], o->Y[2])), ymax = imax_(o->Y[0], imax_(o->Y[1], o->Y[2]));
+    int64_t px0 = ceildiv256((int64_t)xmin - c->smax_x), px1 = floordiv256((int64_t)xmax - c->smin_x);
+    int64_t py0 = ceildiv256((int64_t)ymin - c->smax_y), py1 = floordiv256((int64_t)ymax - c->smin_y);
+    if (px0 < 0) px0 = 0;
+    if (py0 < 0) py0 = 0;
+    if (px1 > c->W - 1) px1 = c->W - 1;
+    if (py1 > c->H - 1) py1 = c->H - 1;
+    if (px0 > px1 || py0 > py1) return 0;
+    o->px0 = (int)px0; o->px1 = (int)px1; o->py0 = (int)py0; o->py1 = (int)py1;
+    for (int i = 0; i < 3; i++) {
+        int j = (i + 1) % 3, k = (i + 2) % 3;
+        o->A[i] = o->Y[j] - o->Y[k];
+        o->B[i] = o->X[k] - o->X[j];
+        o->C[i] = (int64_t)(o->Y[k] - o->Y[j]) * o->X[j] - (int64_t)(o->X[k] - o->X[j]) * o->Y[j];
+        int topleft = (o->A[i] > 0) || (o->A[i] == 0 && o->B[i] > 0);
+        o->Cb[i] = o->C[i] - (topleft ? 0 : 1);
+    }
+    float dX1 = (float)(o->X[1] - o->X[0]), dY1 = (float)(o->Y[1] - o->Y[0]);
+    float dX2 = (float)(o->X[2] - o->X[0]), dY2 = (float)(o->Y[2] - o->Y[0]);
+    float dz1 = o->z[1] - o->z[0], dz2 = o->z[2] - o->z[0];
+    float fa = (float)a2;
+    o->dzdx = (dz1 * dY2 - dz2 * dY1) / fa;
+    o->dzdy = (dz2 * dX1 - dz1 * dX2) / fa;
+    o->prim = prim;
+    o->sub = sub;
+    return 1;
+}
+
+/* Line / point polygon modes: the sub-triangles of triangle t (see ofx_draw::polygon_mode). */
+static int mode_subs(const pass_ctx* c, const ofx_draw* d, int t, const cvert* poly, ofx_sub* subs) {
+    for (int pl = 0; pl < 7; pl++)
+        for (int i = 0; i < 3; i++)
+            if (plane_dist(c, pl, poly[i].p) < 0.0f) return 0; /* needs clipping: dropped */
+    /* projection, snap, cull and orientation of the whole triangle */
+    ofx_sub tri;
+    for (int i = 0; i < 3; i++) {
+        float iw = 1.0f / poly[i].p[3];
+        float xn = poly[i].p[0] * iw, yn = poly[i].p[1] * iw, zn = poly[i].p[2] * iw;
+        float fx = fmin_(fmax_((xn * 0.5f + 0.5f) * c->W256, -OFX_SNAP_LIMIT), OFX_SNAP_LIMIT);
+        float fy = fmin_(fmax_((yn * 0.5f + 0.5f) * c->H256, -OFX_SNAP_LIMIT), OFX_SNAP_LIMIT);
+        tri.X[i] = (int32_t)rintf(fx);
+        tri.Y[i] = (int32_t)rintf(fy);
+        tri.z[i] = zn;
+        tri.iw[i] = iw;
+        for (int k = 0; k < 3; k++) tri.bary[i][k] = poly[i].b[k];
+    }
+    int64_t a2 = (int64_t)(tri.X[1] - tri.X[0]) * (tri.Y[2] - tri.Y[0]) - (int64_t)(tri.X[2] - tri.X[0]) * (tri.Y[1] - tri.Y[0]);
+    if (a2 == 0) return 0;
+    int front = d->front_ccw ? (a2 > 0) : (a2 < 0);
+    if (d->cull_mode == 3 || (d->cull_mode == 1 && front) || (d->cull_mode == 2 && !front)) return 0;
+    int ord[3] = {0, 1, 2};
+    if (a2 < 0) { ord[1] = 2; ord[2] = 1; }
+    int cnt = 0;
+    for (int part = 0; part < 3; part++) {
+        int32_t cx[4], cy[4];
+        int src[4];
+        if (d->polygon_mode == 1) { /* edge part -> part + 1 of the oriented triangle */
+            int p = ord[part], q = ord[(part + 1) % 3];
+            int32_t dx = tri.X[q] - tri.X[p], dy = tri.Y[q] - tri.Y[p];
+            if (dx == 0 && dy == 0) continue;
+            int xmajor = (dx < 0 ? -dx : dx) >= (dy < 0 ? -dy : dy);
+            int32_t ox = xmajor ? 0 : 128, oy = xmajor ? 128 : 0;
+            cx[0] = tri.X[p] - ox; cy[0] = tri.Y[p] - oy; src[0] = p;
+            cx[1] = tri.X[q] - ox; cy[1] = tri.Y[q] - oy; src[1] = q;
+            cx[2] = tri.X[q] + ox; cy[2] = tri.Y[q] + oy; src[2] = q;
+            cx[3] = tri.X[p] + ox; cy[3] = tri.Y[p] + oy; src[3] = p;
+        } else { /* vertex part of the oriented triangle */
+            int p = ord[part];
+            cx[0] = tri.X[p] - 128; cy[0] = tri.Y[p] - 128;
+            cx[1] = tri.X[p] + 128; cy[1] = tri.Y[p] - 128;
+            cx[2] = tri.X[p] + 128; cy[2] = tri.Y[p] + 128;
+            cx[3] = tri.X[p] - 128; cy[3] = tri.Y[p] + 128;
+            src[0] = src[1] = src[2] = src[3] = p;
+        }
+        static const int halves[2][3] = {{0, 1, 2}, {0, 2, 3}};
+        for (int h = 0; h < 2; h++) {
+            ofx_sub* o = &subs[cnt];
+            for (int i = 0; i < 3; i++) {
+                int k = halves[h][i];
+                o->X[i] = cx[k];
+                o->Y[i] = cy[k];
+                o->z[i] = tri.z[src[k]];
+                o->iw[i] = tri.iw[src[k]];
+                for (int m = 0; m < 3; m++) o->bary[i][m] = tri.bary[src[k]][m];
+            }
+            if (finish_sub(c, d->prim_base + t, 2 * part + h, o)) cnt++;
+        }
+    }
+    return cnt;
+}
+
 static int triangle_subs(const pass_ctx* c, const ofx_draw* d, int t, ofx_sub* subs) {
     cvert poly[OFX_MAX_POLY];
     for (int i = 0; i < 3; i++) {
@@ -479,6 +586,7 @@ static int triangle_subs(const pass_ctx* c, const ofx_draw* d, int t, ofx_sub* s
             if (!isfinite(poly[i].p[k])) return 0;
         for (int k = 0; k < 3; k++) poly[i].b[k] = (k == i) ? 1.0f : 0.0f;
     }
+    if (d->polygon_mode != 0) return mode_subs(c, d, t, poly, subs);
     int n = clip_polygon(c, poly);
     int cnt = 0;
     for (int i = 1; i + 1 < n; i++)

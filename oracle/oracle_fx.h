@@ -61,6 +61,12 @@ typedef struct {
     int scissor_enable;
     int scissor_count;
     float scissor[16][4];       /* x, y, w, h */
+    /* polygon mode (IfritPolygonMode, base/Constants.h:23-28): 0 fill, 1 line, 2 point.  Line:
+     * each edge of the (culled, orientation-normalised) triangle is a 1-pixel-wide parallelogram,
+     * offset +-1/2 pixel along the minor axis; point: each vertex is a 1-pixel square.  Each is
+     * two sub-triangles (sub = 2 * edge or vertex + half) through the fill-mode rules; triangles
+     * that need clipping are dropped in these modes. */
+    int polygon_mode;
 } ofx_draw;
 
 typedef struct {

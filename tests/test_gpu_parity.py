@@ -320,3 +320,51 @@ def test_scissor_rectangles_single_and_multi_draw():
     ref = O.render(odraws, W, H, 4, clear=True, clear_color=(0.1, 0.2, 0.3, 1.0), nthreads=os.cpu_count() or 1)
     assert_parity(gpu, ref)
     r.close()
+
+
+@pytest.mark.parametrize("mode,S", [(ig.POLYGON_LINE, 1), (ig.POLYGON_LINE, 4), (ig.POLYGON_POINT, 1), (ig.POLYGON_POINT, 8)])
+def test_polygon_modes_soup(mode, S):
+    from oracle import oracle as O
+    W, H = 160, 120
+    v, f, mvp = soup(2000, 40 + S, W, H, median_px=12.0)
+    r = ig.Renderer(W, H, S, ig.FORMAT_RGBA8, visibility=True)
+    r.set_state(cull=ig.CULL_NONE, depth_func=ig.LESS_OR_EQUAL)
+    r.set_polygon_mode(mode)
+    r.set_mvp(mvp)
+    r.set_geometry(v, f, 2)
+    r.draw(clear=True)
+    gpu = {"color": r.color(), "depth": r.depth(), "vis": r.visibility()}
+    d = O.make_draw(v, f, mvp, attr_offset=3, attr_count=2, cull_mode=0, depth_func=3, polygon_mode=mode)
+    ref = O.render([d], W, H, S, clear=True, nthreads=os.cpu_count() or 1)
+    assert_parity(gpu, ref)
+    # something is drawn, and the 1-pixel points cover fewer samples than the filled triangles
+    fill = O.render([O.make_draw(v, f, mvp, attr_offset=3, attr_count=2, cull_mode=0, depth_func=3)], W, H, S,
+                    clear=True, nthreads=os.cpu_count() or 1)
+    n_mode, n_fill = int((gpu["vis"] >= 0).sum()), int((fill["vis"] >= 0).sum())
+    assert n_mode > 0 and (mode == ig.POLYGON_LINE or n_mode < n_fill)
+    r.close()
+
+
+def test_line_mode_icosphere_culled_and_textured():
+    from oracle import oracle as O
+    v, f = scenes.jittered_icosphere(3, 4)
+    uv = np.stack([0.5 + np.arctan2(v[:, 2], v[:, 0]) / (2 * np.pi), 0.5 + v[:, 1] / 2], 1).astype(np.float32)
+    vt = np.concatenate([v[:, :3], uv], 1)
+    mvp = scenes.default_mvp(4 / 3)
+    tex = scenes.value_noise_texture(128, 3)
+    W, H = 256, 192
+    r = ig.Renderer(W, H, 4, ig.FORMAT_RGBA8, visibility=True)
+    r.set_state(cull=ig.CULL_BACK, depth_func=ig.LESS_OR_EQUAL, shading=ig.FS_TEXTURED)
+    r.set_polygon_mode(ig.POLYGON_LINE)
+    r.set_mvp(mvp)
+    r.set_geometry(vt, f, 2)
+    r.set_texture(tex, max_aniso=4)
+    r.draw(clear=True)
+    gpu = {"color": r.color(), "depth": r.depth(), "vis": r.visibility()}
+    chain, levels = O.build_mips(tex)
+    d = O.make_draw(vt, f, mvp, attr_offset=3, attr_count=2, cull_mode=2, depth_func=3, polygon_mode=O.POLY_LINE,
+                    shading=O.SHADE_TEXTURED, texture=(chain, levels, 128, 128), sampler={"max_aniso": 4})
+    ref = O.render([d], W, H, 4, clear=True, nthreads=os.cpu_count() or 1)
+    assert_parity(gpu, ref)
+    assert (gpu["vis"] >= 0).any()
+    r.close()

@@ -201,3 +201,35 @@ def test_scissor_rectangles_inclusive_bounds():
     assert (vis == want[..., None]).all()
     d = O.make_draw(v, f, EYE, depth_func=7, cull_mode=0, scissor=[])
     assert (O.render([d], 8, 6, 1)["vis"] >= 0).all()
+
+
+def _px_to_ndc(pts, W, H):
+    return [[(x / W) * 2 - 1, (y / H) * 2 - 1, 0.5] for x, y in pts]
+
+
+def test_point_mode_covers_the_pixel_of_each_vertex():
+    W, H = 16, 12
+    pts = [(2.3, 3.6), (12.7, 2.2), (6.4, 9.8)]
+    v = tri_vertices(_px_to_ndc(pts, W, H))
+    d = O.make_draw(v, np.array([[0, 1, 2]], np.int32), EYE, depth_func=7, cull_mode=0, polygon_mode=O.POLY_POINT)
+    vis = O.render([d], W, H, 1)["vis"][..., 0] >= 0
+    want = np.zeros((H, W), bool)
+    for x, y in pts:
+        want[int(y), int(x)] = True
+    assert (vis == want).all()
+
+
+def test_line_mode_one_pixel_per_column_along_an_x_major_edge():
+    W, H = 32, 24
+    pts = [(2.3, 5.6), (20.7, 7.1), (11.0, 22.0)]
+    v = tri_vertices(_px_to_ndc(pts, W, H))
+    d = O.make_draw(v, np.array([[0, 1, 2]], np.int32), EYE, depth_func=7, cull_mode=0, polygon_mode=O.POLY_LINE)
+    vis = O.render([d], W, H, 1)["vis"][..., 0] >= 0
+    # rows 0..9 near the top edge only hold that edge between columns 5 and 17
+    col = vis[:10, 5:18].sum(0)
+    assert (col == 1).all(), col
+    # the interior of the triangle is not filled
+    assert not vis[14, 10:13].any()
+    # and the lines are there at 4x too, with every pixel they touch holding at least one sample
+    vis4 = O.render([d], W, H, 4)["vis"] >= 0
+    assert vis4[:10, 5:18].any(axis=2).sum(0).min() >= 1
