@@ -201,10 +201,11 @@ struct IfritGbRenderer {
     float clear_depth = 1.0f;
     bool vis_output = false;
     int polygon_mode = 0;  // IF_POLYGON_MODE_*
+    int raster_path = IFTR_RASTER_TILED;
     bool scissor_enable = false;
     std::vector<float> scissors;  // (x, y, w, h) per rectangle, at most 16
     // device state
-    DevMem d_vertices, d_indices, d_color, d_depth, d_vis, d_entries, d_sample_colors;
+    DevMem d_vertices, d_indices, d_color, d_depth, d_vis, d_entries, d_sample_colors, d_keys;
     const void* up_vb_key = nullptr;
     uint64_t up_vb_gen = 0;
     const void* up_ib_key = nullptr;
@@ -563,10 +564,18 @@ int enqueue_pass(IfritGbRenderer* h, std::vector<DrawDev>& draws, int clear) {
         IFTR_CUDA(h, h->d_sample_colors.reserve((size_t)ifr::tiles_of(W, H, 16) * 256 * S * sizeof(float4)));
         v.sample_colors = h->d_sample_colors.as<float4>();
     }
+    if (h->raster_path == IFTR_RASTER_ATOMIC && !v.ordered) {  // per-sample keys in global memory
+        IFTR_CUDA(h, h->d_keys.reserve((size_t)W * H * S * sizeof(unsigned long long)));
+        v.keys = h->d_keys.as<unsigned long long>();
+    }
     std::vector<int> view_tiles(2);
     ifr::LaunchPlan plan;
     int T = 0;
     if (!ifr::plan_groups(views.data(), 1, view_tiles.data(), h->sms, 0, plan, T)) return IFTR_ERR_INVALID_ARG;
+    if (v.keys) {
+        plan.atomic = 1;
+        plan.atomic_pixels = W * H;
+    }
     rc = scratch_reserve(h, h->pass, (size_t)T, (size_t)total, draws.size(), 1, 0);
     if (rc) return rc;
     rc = upload_descriptors(h, h->pass, draws, draw_start, views, view_tiles);
@@ -978,7 +987,7 @@ IFTR_API int iftrDestroyInstance(IfritGbRenderer* h) {
     if (h->inited) {
         cudaStreamSynchronize(h->stream);
         for (DevMem* m : {&h->d_vertices, &h->d_indices, &h->d_color, &h->d_depth, &h->d_vis, &h->d_entries,
-                          &h->d_sample_colors})
+                          &h->d_sample_colors, &h->d_keys})
             m->release();
         h->pass.release();
         h->batch.drop_graph();
@@ -1197,6 +1206,12 @@ IFTR_API int iftrClear(IfritGbRenderer* h) {
 IFTR_API int iftrSetScissors(IfritGbRenderer* h, const float* rects, int count) {
     if (!h || count < 0 || count > 16 || (count > 0 && !rects)) return IFTR_ERR_INVALID_ARG;
     h->scissors.assign(rects, rects + 4 * count);
+    return IFTR_OK;
+}
+
+IFTR_API int iftrSetRasterPath(IfritGbRenderer* h, int path) {
+    if (!h || (path != IFTR_RASTER_TILED && path != IFTR_RASTER_ATOMIC)) return IFTR_ERR_INVALID_ARG;
+    h->raster_path = path;
     return IFTR_OK;
 }
 

@@ -66,11 +66,11 @@ __device__ __forceinline__ void bin_sub(const PassArgs& a, const ViewArgs& v, co
         }
 }
 
-// Counting pass: full front end per triangle; unclipped triangles leave a compact record.
-__global__ void __launch_bounds__(256) bin_count_kernel(PassArgs a) {
-    const int g = blockIdx.x * blockDim.x + threadIdx.x;
-    const int di = find_draw_warp(a, min(g, a.total_tris - 1));
-    if (g >= a.total_tris) return;
+// Front end of triangle g (draw di), shared by the counting binner and the atomic visibility
+// path: fetch, transform, clip and set-up; writes the triangle's record (and vertex attributes)
+// and hands every visible (sub-)triangle to emit(view, draw, sub-triangle, entry).
+template <class Emit>
+__device__ __forceinline__ void front_end(const PassArgs& a, int g, int di, const Emit& emit) {
     const DrawDev& d = a.draws[di];
     const ViewArgs& v = a.views[d.view];
     int t = g - __ldg(a.draw_start + di);
@@ -81,7 +81,7 @@ __global__ void __launch_bounds__(256) bin_count_kernel(PassArgs a) {
         rec->flags = 0;
         return;
     }
-    if (d.polygon_mode != POLY_FILL) {  // LINE / POINT: record the projected triangle, bin its parts
+    if (d.polygon_mode != POLY_FILL) {  // LINE / POINT: record the projected triangle, emit its parts
         SubTri tri;
         if (!inside || !project_oriented(v.c, d, poly, tri)) {
             rec->flags = 0;
@@ -103,7 +103,7 @@ __global__ void __launch_bounds__(256) bin_count_kernel(PassArgs a) {
         dst[0] = src[0]; dst[1] = src[1]; dst[2] = src[2]; dst[3] = src[3];
         for (int sub = 0; sub < 6; sub++) {
             SubTri s;
-            if (mode_sub(v.c, d.polygon_mode, tri, sub, s)) bin_sub(a, v, d, s, ((uint32_t)g << 3) | (uint32_t)sub, false);
+            if (mode_sub(v.c, d.polygon_mode, tri, sub, s)) emit(v, d, s, ((uint32_t)g << 3) | (uint32_t)sub);
         }
         return;
     }
@@ -127,7 +127,7 @@ __global__ void __launch_bounds__(256) bin_count_kernel(PassArgs a) {
         const int4* src = reinterpret_cast<const int4*>(&r);
         int4* dst = reinterpret_cast<int4*>(rec);
         dst[0] = src[0]; dst[1] = src[1]; dst[2] = src[2]; dst[3] = src[3];
-        bin_sub(a, v, d, s, (uint32_t)g << 3, false);
+        emit(v, d, s, (uint32_t)g << 3);
         return;
     }
     rec->flags = REC_CLIPPED;
@@ -135,8 +135,23 @@ __global__ void __launch_bounds__(256) bin_count_kernel(PassArgs a) {
     int n = clip_polygon(v.c, poly);
     for (int i = 1; i + 1 < n; i++) {
         SubTri s;
-        if (setup_sub(v.c, d, poly[0], poly[i], poly[i + 1], s)) bin_sub(a, v, d, s, ((uint32_t)g << 3) | (uint32_t)(i - 1), false);
+        if (setup_sub(v.c, d, poly[0], poly[i], poly[i + 1], s)) emit(v, d, s, ((uint32_t)g << 3) | (uint32_t)(i - 1));
     }
+}
+
+struct CountEmit {
+    const PassArgs& a;
+    __device__ void operator()(const ViewArgs& v, const DrawDev& d, const SubTri& s, uint32_t entry) const {
+        bin_sub(a, v, d, s, entry, false);
+    }
+};
+
+// Counting pass: full front end per triangle; unclipped triangles leave a compact record.
+__global__ void __launch_bounds__(256) bin_count_kernel(PassArgs a) {
+    const int g = blockIdx.x * blockDim.x + threadIdx.x;
+    const int di = find_draw_warp(a, min(g, a.total_tris - 1));
+    if (g >= a.total_tris) return;
+    front_end(a, g, di, CountEmit{a});
 }
 
 // Scattering pass: same overlaps as the counting pass, read back from the records (clipped
@@ -371,6 +386,65 @@ struct RecordPlane {
     float z0, dzdx, dzdy;
     int32_t X0, Y0;
 };
+
+// ---------------------------------------------------------------------------- atomic visibility
+// Alternative to binning + the tile raster stage for deferred views: the thread of each triangle
+// resolves its own samples straight into per-sample 64-bit keys in global memory with atomicMin
+// (the tile stage's keys, so the winners are the same); the shade stage then reads the keys.
+// Suited to views of small triangles, where binning and per-tile set-up dominate.
+template <int S>
+__global__ void __launch_bounds__(256) init_keys_kernel(PassArgs a, int npix) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= npix) return;
+    const ViewArgs& v = a.views[0];
+    const KeyRule rule = key_rule(v.depth_func, v.depth_write);
+#pragma unroll
+    for (int k = 0; k < S; k++) {
+        const float d0 = v.clear ? v.clear_depth : v.depth[(size_t)p * S + k];
+        v.keys[(size_t)p * S + k] = background_key(rule, d0);
+    }
+}
+
+template <int S>
+struct GlobalRasterEmit {
+    __device__ void operator()(const ViewArgs& v, const DrawDev& d, SubTri s, uint32_t entry) const {
+        if (!scissor_clamp(d, s)) return;
+        const KeyRule rule = key_rule(v.depth_func, v.depth_write);
+        if (rule.func == 0) return;  // NEVER
+        const uint32_t lo_word = rule.mode == KM_EARLIEST ? entry + 1u : 0xFFFFFFFEu - entry;
+        for (int py = s.py0; py <= s.py1; py++) {
+            for (int px = s.px0; px <= s.px1; px++) {
+                if (d.scissor_count && !scissor_pass(d, px, py)) continue;
+                const size_t pix = (size_t)py * v.c.W + px;
+                // the tile stage's depth expression (see raster_tile)
+                const float fbx = (float)(px * 256 - s.X[0]), fby = (float)(py * 256 - s.Y[0]);
+#pragma unroll
+                for (int k = 0; k < S; k++) {
+                    if (!covered(s.A, s.B, s.Cb, px * 256 + sample_x<S>(k), py * 256 + sample_y<S>(k))) continue;
+                    const float z = (s.z[0] + s.dzdx * (fbx + (float)sample_x<S>(k))) + s.dzdy * (fby + (float)sample_y<S>(k));
+                    uint32_t hi_word;
+                    if (rule.explicit_) {
+                        if (!depth_cmp(rule.func, z, d0_of(v, px, py, k))) continue;
+                        hi_word = 0u;
+                    } else {
+                        hi_word = rule.invert ? ~depth_order(z) : depth_order(z);
+                    }
+                    const unsigned long long kv = ((unsigned long long)hi_word << 32) | lo_word;
+                    unsigned long long* kp = v.keys + pix * S + k;
+                    if (kv < *kp) atomicMin(kp, kv);  // keys only fall: a stale read only costs an atomic
+                }
+            }
+        }
+    }
+};
+
+template <int S>
+__global__ void __launch_bounds__(256) atomic_front_kernel(PassArgs a) {
+    const int g = blockIdx.x * blockDim.x + threadIdx.x;
+    const int di = find_draw_warp(a, min(g, a.total_tris - 1));
+    if (g >= a.total_tris) return;
+    front_end(a, g, di, GlobalRasterEmit<S>{});
+}
 
 // Set-up of entry e (global triangle << 3 | fan index) for shading: geometry + depth plane.
 __device__ __noinline__ void setup_entry(const PassArgs& a, const PassConst& c, int e, ShadeGeom* g, RecordPlane* pl) {
@@ -691,7 +765,10 @@ __device__ __forceinline__ void shade_tile(const PassArgs& a, const ViewArgs& v,
     const size_t pix = (size_t)py * v.c.W + px;
     const KeyRule rule = key_rule(v.depth_func, v.depth_write);
     int ent[S];
-    if (inpix) {
+    if (inpix && v.keys) {  // atomic visibility path
+#pragma unroll
+        for (int k = 0; k < S; k++) ent[k] = key_entry(rule, v.keys[pix * S + k]);
+    } else if (inpix) {
         const int* ep = v.entries + pix * S;
         if constexpr (S % 4 == 0) {
 #pragma unroll
@@ -1273,11 +1350,40 @@ int tile_kernel_occupancy(int S, int TS, int ordered, int stage) {
     }
 }
 
+template <int S>
+void launch_atomic_front(const PassArgs& a, int npix, cudaStream_t stream, cudaEvent_t* ev) {
+    init_keys_kernel<S><<<(npix + 255) / 256, 256, 0, stream>>>(a, npix);
+    if (ev) {
+        cudaEventRecord(ev[1], stream);
+        cudaEventRecord(ev[2], stream);
+    }
+    if (a.total_tris > 0) atomic_front_kernel<S><<<(a.total_tris + 255) / 256, 256, 0, stream>>>(a);
+    if (ev) {
+        cudaEventRecord(ev[3], stream);
+        cudaEventRecord(ev[4], stream);
+    }
+}
+
 cudaError_t launch_pass(const PassArgs& a, const LaunchPlan& plan, cudaStream_t stream, cudaEvent_t* ev) {
     const int T = a.total_tiles;
     if (ev) cudaEventRecord(ev[0], stream);
     cudaError_t err = cudaMemsetAsync(a.queues, 0, sizeof(uint32_t) * 3 * plan.ngroups, stream);
     if (err != cudaSuccess) return err;
+    if (plan.atomic) {  // one deferred view: keys by atomics, then the shade stage
+        switch (plan.samples[0]) {
+        case 1: launch_atomic_front<1>(a, plan.atomic_pixels, stream, ev); break;
+        case 2: launch_atomic_front<2>(a, plan.atomic_pixels, stream, ev); break;
+        case 4: launch_atomic_front<4>(a, plan.atomic_pixels, stream, ev); break;
+        case 8: launch_atomic_front<8>(a, plan.atomic_pixels, stream, ev); break;
+        default: launch_atomic_front<16>(a, plan.atomic_pixels, stream, ev); break;
+        }
+        err = launch_group_stage(a, plan.groups[0], plan.samples[0], plan.tile_size[0], plan.ctas_shade[0], stream, true);
+        if (ev) {
+            cudaEventRecord(ev[5], stream);
+            cudaEventRecord(ev[6], stream);
+        }
+        return err != cudaSuccess ? err : cudaGetLastError();
+    }
     if (a.total_tris > 0) {
         int blocks = (a.total_tris + 255) / 256;
         bin_count_kernel<<<blocks, 256, 0, stream>>>(a);

@@ -47,6 +47,7 @@ struct ViewArgs {
     int ordered_prefix;      // ordered views: triangles of the leading draws that need no ordering
                              //    (opaque, the first draw's depth state); they go through the
                              //    order-independent raster stage and the rest is applied on top
+    unsigned long long* keys;  // atomic visibility path: per-sample 64-bit keys [H][W][S], else nullptr
     float4* sample_colors;   // ordered views: per-sample colour of the order-independent prefix,
                              //    handed from the shade stage to the ordered stage, tile-major
                              //    [tiles][S][256] (16x16 tiles, lanes in tile_pixel order)
@@ -94,6 +95,8 @@ struct LaunchPlan {
     int ctas[kMaxGroups];       // persistent CTAs of the group's first stage (raster or ordered)
     int ctas_shade[kMaxGroups]; // persistent CTAs of the group's shade stage
     int ctas_fwd[kMaxGroups];   // hybrid groups: persistent CTAs of the ordered stage after shading
+    int atomic;                 // one deferred view resolved by the atomic visibility path (no binning)
+    int atomic_pixels;          // its W * H
 };
 
 }  // namespace ifr

@@ -23,6 +23,7 @@ IFTP_FLOAT1, IFTP_FLOAT2, IFTP_FLOAT3, IFTP_FLOAT4 = 1, 2, 3, 4
 CULL_NONE, CULL_FRONT, CULL_BACK, CULL_FRONT_AND_BACK = 0, 1, 2, 3
 NEVER, LESS, EQUAL, LESS_OR_EQUAL, GREATER, NOT_EQUAL, GREATER_OR_EQUAL, ALWAYS = range(8)
 POLYGON_FILL, POLYGON_LINE, POLYGON_POINT = 0, 1, 2
+RASTER_TILED, RASTER_ATOMIC = 0, 1
 
 EXPORTED = [
     "iftrCreateInstance", "iftrDestroyInstance", "iftrInit", "iftrBindFrameBuffer", "iftrBindVertexBuffer",
@@ -46,7 +47,7 @@ EXPORTED = [
     "iftrSetVertexBufferDirty", "ifbufGetBufferRawData", "ifbufSetBufferDirty", "iftrDrawNoAlloc",
     "iftrBeginPass", "iftrPassDraw", "iftrEndPass", "iftrDrawBatch", "iftrSetBatchTuning", "iftrGetBatchTuning",
     "iftrDiffForward", "iftrDiffBackward", "iftrSetScissors", "iftrSetScissorTestEnable",
-    "iftrSetRasterizerPolygonMode",
+    "iftrSetRasterizerPolygonMode", "iftrSetRasterPath",
 ]
 
 
@@ -168,7 +169,7 @@ def load(build_if_missing=True):
         "iftrGetBatchTuning": [vp, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)],
         "iftrDiffForward": [ctypes.POINTER(DiffPass), vp], "iftrDiffBackward": [ctypes.POINTER(DiffPass), vp],
         "iftrSetScissors": [vp, fp, ip], "iftrSetScissorTestEnable": [vp, ip],
-        "iftrSetRasterizerPolygonMode": [vp, ip],
+        "iftrSetRasterizerPolygonMode": [vp, ip], "iftrSetRasterPath": [vp, ip],
     }
     for name, args in sig.items():
         getattr(lib, name).argtypes = args
@@ -267,6 +268,9 @@ class Renderer:
         """Blend factors use the IfritBlendFactor numbering (6 SRC_ALPHA, 7 ONE_MINUS_SRC_ALPHA)."""
         s = BlendState(int(enable), src_color, dst_color, src_alpha, dst_alpha)
         check("iftrSetBlendFunc", self.lib.iftrSetBlendFunc(self.h, ctypes.byref(s)))
+
+    def set_raster_path(self, path):
+        check("iftrSetRasterPath", self.lib.iftrSetRasterPath(self.h, path))
 
     def set_polygon_mode(self, mode):
         check("iftrSetRasterizerPolygonMode", self.lib.iftrSetRasterizerPolygonMode(self.h, mode))

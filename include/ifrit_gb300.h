@@ -146,6 +146,13 @@ IFTR_API int iftrSetScissors(IfritGbRenderer* h, const float* rects, int count);
  * draws each vertex as a 1-pixel square.  Both go through the fill rules (MSAA, depth, shading);
  * triangles that need clipping are dropped in these modes. */
 IFTR_API int iftrSetRasterizerPolygonMode(IfritGbRenderer* h, int mode);
+/* Raster path of order-independent passes (no counterpart in the reference).  TILED (default):
+ * triangles binned into 16x16 tiles, resolved per tile in shared memory.  ATOMIC: no binning;
+ * each triangle's thread resolves its samples into per-sample 64-bit (depth, primitive) keys in
+ * device memory with atomicMin (the same keys, so the same image), then the shade stage runs;
+ * suited to many small triangles.  Passes that need submission order always use the tiles. */
+enum { IFTR_RASTER_TILED = 0, IFTR_RASTER_ATOMIC = 1 };
+IFTR_API int iftrSetRasterPath(IfritGbRenderer* h, int path);
 IFTR_API int iftrSetScissorTestEnable(IfritGbRenderer* h, int enable);
 IFTR_API int iftrCreateTexture(IfritGbRenderer* h, int slot, int width, int height, int mipLevels); /* TRC:91, RGBA8 */
 IFTR_API int iftrCopyHostBufferToImage(IfritGbRenderer* h, const void* rgba8, int slot); /* TRC:96, level 0 */

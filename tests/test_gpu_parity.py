@@ -368,3 +368,52 @@ def test_line_mode_icosphere_culled_and_textured():
     assert_parity(gpu, ref)
     assert (gpu["vis"] >= 0).any()
     r.close()
+
+
+@pytest.mark.parametrize("case", ["soup1", "soup4", "soup8", "greater", "always", "textured", "icosphere",
+                                  "scissor_lines"])
+def test_atomic_visibility_path_matches_oracle(case):
+    """The atomics-only raster path (no binning; per-triangle threads resolve global 64-bit keys)
+    gives the tile path's image: visibility and depth bit-exact against the oracle."""
+    from oracle import oracle as O
+    W, H = 192, 144
+    S, func, shading, tex, attr, cull, mode, sc = 4, ig.LESS_OR_EQUAL, ig.FS_GOURAUD, None, 2, ig.CULL_NONE, 0, None
+    v, f, mvp = soup(15000, 50, W, H)
+    if case == "soup1":
+        S = 1
+    elif case == "soup8":
+        S = 8
+    elif case == "greater":
+        func = ig.GREATER
+    elif case == "always":
+        f = np.concatenate([f, f[::2]], 0)
+        func = ig.ALWAYS
+    elif case == "textured":
+        shading, tex = ig.FS_TEXTURED, scenes.value_noise_texture(128, 9)
+    elif case == "icosphere":
+        v, f, mvp = scenes.c1_scene(2)
+        attr, cull = 3, ig.CULL_BACK
+    elif case == "scissor_lines":
+        mode, sc = ig.POLYGON_LINE, [(20.5, 10.0, 90.0, 70.0)]
+    r = ig.Renderer(W, H, S, ig.FORMAT_RGBA8, visibility=True)
+    r.set_raster_path(ig.RASTER_ATOMIC)
+    r.set_state(cull=cull, depth_func=func, shading=shading, clear_depth=0.0 if func == ig.GREATER else 1.0)
+    r.set_polygon_mode(mode)
+    if sc:
+        r.set_scissors(sc)
+    r.set_mvp(mvp)
+    r.set_geometry(v, f, attr)
+    tex_arg = None
+    if tex is not None:
+        r.set_texture(tex, max_aniso=8)
+        chain, levels = O.build_mips(tex)
+        tex_arg = (chain, levels, 128, 128)
+    r.draw(clear=True)
+    gpu = {"color": r.color(), "depth": r.depth(), "vis": r.visibility()}
+    d = O.make_draw(v, f, mvp, attr_offset=3, attr_count=attr, cull_mode=cull, depth_func=func, shading=shading,
+                    texture=tex_arg, sampler={"max_aniso": 8}, polygon_mode=mode, scissor=sc)
+    ref = O.render([d], W, H, S, clear=True, clear_depth=0.0 if func == ig.GREATER else 1.0,
+                   nthreads=os.cpu_count() or 1)
+    assert_parity(gpu, ref)
+    assert (gpu["vis"] >= 0).any()
+    r.close()
