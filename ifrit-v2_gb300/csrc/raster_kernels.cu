@@ -525,35 +525,91 @@ __device__ __forceinline__ void tile_pixel(int tid, int& lx, int& ly) {
 }
 
 // ---------------------------------------------------------------------------- raster stage
-// A record whose snapped vertices span less than 32 pixels in x and in y has every edge function
-// value at its bbox samples below 2^28 in magnitude (|A|, |B| < 8192 and sample offsets from a
-// vertex below 8704 in 1/256 pixel), so coverage is evaluated exactly in 32-bit arithmetic
-// relative to the clipped bbox origin.  Larger ones keep the 64-bit edge functions.
-constexpr int kLargeRecord = 1 << 16;
+// Edge functions are kept relative to the tile origin.  A record whose snapped vertices span
+// less than 32 pixels in x and in y has |A|, |B| < 8192 (1/256 pixel units) and every sample of
+// a 16x16 tile overlapping its bbox lies within 48 pixels (12288 units) of vertex 0, so each edge
+// function there is below 2^28 in magnitude and coverage is evaluated exactly in 32-bit
+// arithmetic.  Larger records keep the 64-bit edge functions.
+constexpr int kLargeRecord = 1;
 constexpr int32_t kSmallSpan = 32 * 256;
+
+// Spans of one batch: a span is one tile row of one record's conservative column range.
+template <int NT>
+__host__ __device__ constexpr int span_capacity() { return NT >= 256 ? 2048 : 8 * NT; }
 
 template <int NT>
 struct TileRecords {
     int32_t A[3][NT], B[3][NT];
-    long long Cb[3][NT];
-    int32_t E[3][NT];   // small triangles: biased edge functions at the clipped bbox origin corner
+    long long Et[3][NT];  // biased edge functions at the tile origin
     float z0[NT], dzdx[NT], dzdy[NT];
     int32_t X0[NT], Y0[NT];
-    int32_t org[NT];    // tile-local x0 | y0 << 8 of the clipped bbox, | kLargeRecord
-    int32_t width[NT];  // clipped bbox width in pixels
-    float rwidth[NT];   // 1 / width
-    int32_t key[NT];    // entry
-    int32_t sc[NT];     // draw with a scissor test, or -1
-    uint32_t start[NT + 1];  // exclusive prefix of pixel counts
+    int32_t meta[NT];     // kLargeRecord | (draw + 1) << 1 when the draw has a scissor test
+    int32_t key[NT];      // entry
+    // pixel offset of the span in the batch (16 bits) | record << 16 | row << 24 | first column << 28
+    uint32_t span[span_capacity<NT>()];
 };
 
-// One tile: the tile's list is consumed in batches of up to NT set-ups; every (triangle, pixel)
-// pair of a batch is spread over the CTA, and each covered sample that passes the depth test
-// lowers its key.  The winning entry of every sample (or -1) is written for the shading stage.
+// Conservative covered columns of every tile row of a record: for each edge the largest value
+// over a pixel's sample pattern, A·(256c + sx) + B·(256r + sy) + E, must be >= 0 at some sample
+// of the pixel, which bounds column c from one side per edge with A != 0 (the crossing column is
+// computed in float from the exact integer and widened to the next integer, which absorbs the
+// relative error of the three roundings, ~2^-22 of at most TS + 2 columns); an edge with A == 0
+// empties the row when its largest value is negative.  Row r's range is packed as lo | hi << 4
+// into bits 8(r mod 4) of word r / 4; an empty row is 0x0f.
+template <int TS>
+struct RowSpans {
+    uint32_t w[TS / 4];
+    int nspan, npix;
+};
+
+template <int TS>
+__device__ __forceinline__ void row_spans(const PassConst& c, const int32_t A[3], const int32_t B[3],
+                                          const long long Et[3], int cx0, int cx1, int ry0, int ry1,
+                                          RowSpans<TS>& o) {
+    long long base0[3];
+    float rcp[3];
+#pragma unroll
+    for (int i = 0; i < 3; i++) {
+        const long long mA = (long long)A[i] * (A[i] > 0 ? c.smax_x : c.smin_x);
+        const long long mB = (long long)B[i] * (B[i] > 0 ? c.smax_y : c.smin_y);
+        base0[i] = Et[i] + mA + mB;
+        rcp[i] = A[i] != 0 ? -1.0f / (256.0f * (float)A[i]) : 0.0f;
+    }
+    o.nspan = 0;
+    o.npix = 0;
+    uint32_t w[TS / 4] = {};
+#pragma unroll
+    for (int r = 0; r < TS; r++) {
+        int lo = cx0, hi = cx1;
+        bool empty = r < ry0 || r > ry1;
+#pragma unroll
+        for (int i = 0; i < 3; i++) {
+            const long long b = base0[i] + (long long)B[i] * (256 * r);
+            const float t = fminf(fmaxf((float)b * rcp[i], -2.0f), (float)TS + 1.0f);
+            if (A[i] > 0) lo = max(lo, (int)floorf(t));
+            else if (A[i] < 0) hi = min(hi, (int)ceilf(t));
+            else empty |= b < 0;
+        }
+        empty |= lo > hi;
+        w[r / 4] |= (empty ? 0x0fu : (uint32_t)(lo | (hi << 4))) << ((r % 4) * 8);
+        o.nspan += empty ? 0 : 1;
+        o.npix += empty ? 0 : hi - lo + 1;
+    }
+#pragma unroll
+    for (int q = 0; q < TS / 4; q++) o.w[q] = w[q];
+}
+
+// One tile: the tile's list is consumed in batches of up to NT set-ups.  Every record's clipped
+// bbox is cut into conservative row spans; the batch's spans are laid end to end and every pixel
+// of them is visited by one lane (each warp walks a contiguous range, finding the span of each of
+// its 32 pixels from a window of the next 32 span starts).  Each covered sample that passes the
+// depth test lowers its key.  A batch holds at most span_capacity spans; records beyond that go to
+// the next batch.  The winning entry of every sample (or -1) is written for the shading stage.
 template <int S, int TS>
 __device__ __forceinline__ void raster_tile(const PassArgs& a, const ViewArgs& v, int gtile, TileRecords<TS * TS>& rec,
                                             unsigned long long* skey, uint32_t* warp_sum) {
-    constexpr int NT = TS * TS;
+    constexpr int NT = TS * TS, NW = NT / 32, CAP = span_capacity<NT>();
+    __shared__ uint32_t s_total[2];
     const int ltile = gtile - v.tile_start;
     const int tx = ltile % v.c.tiles_x, ty = ltile / v.c.tiles_x;
     const int tx0 = tx * TS, ty0 = ty * TS;
@@ -576,50 +632,48 @@ __device__ __forceinline__ void raster_tile(const PassArgs& a, const ViewArgs& v
     const int xmax = min(v.c.W, tx0 + TS) - 1, ymax = min(v.c.H, ty0 + TS) - 1;
     uint32_t ordered_left = 0;  // ordered views: entries of the tile left for the ordered stage
 
-    for (uint32_t base = beg; base < end; base += NT) {
+    for (uint32_t base = beg; base < end;) {
         const int nb = (int)min((uint32_t)NT, end - base);
-        uint32_t cnt = 0;
+        RowSpans<TS> rs;  // every row empty unless the record is set up below
+        rs.nspan = 0;
+        rs.npix = 0;
+#pragma unroll
+        for (int q = 0; q < TS / 4; q++) rs.w[q] = 0x0f0f0f0fu;
+        bool in_stage = true;
         if (tid < nb) {
             uint32_t e = __ldg(a.pairs + base + tid);
             SubTri s;
             int di;
             // ordered views: only the order-independent prefix is resolved here
-            const bool in_stage = !v.ordered || (int)(e >> 3) < v.first_tri + v.ordered_prefix;
-            ordered_left += in_stage ? 0u : 1u;
+            in_stage = !v.ordered || (int)(e >> 3) < v.first_tri + v.ordered_prefix;
             if (in_stage && setup_raster_entry(a, v.c, e, &s, &di)) {
-                int x0 = max(s.px0, tx0), x1 = min(s.px1, xmax);
-                int y0 = max(s.py0, ty0), y1 = min(s.py1, ymax);
+                const int x0 = max(s.px0, tx0), x1 = min(s.px1, xmax);
+                const int y0 = max(s.py0, ty0), y1 = min(s.py1, ymax);
                 if (x0 <= x1 && y0 <= y1) {
+                    long long Et[3];
 #pragma unroll
                     for (int i = 0; i < 3; i++) {
+                        Et[i] = s.Cb[i] + (long long)s.A[i] * (tx0 * 256) + (long long)s.B[i] * (ty0 * 256);
                         rec.A[i][tid] = s.A[i];
                         rec.B[i][tid] = s.B[i];
-                        rec.Cb[i][tid] = s.Cb[i];
+                        rec.Et[i][tid] = Et[i];
                     }
                     rec.z0[tid] = s.z[0];
                     rec.dzdx[tid] = s.dzdx;
                     rec.dzdy[tid] = s.dzdy;
                     rec.X0[tid] = s.X[0];
                     rec.Y0[tid] = s.Y[0];
-                    int w = x1 - x0 + 1;
                     const int32_t xmn = min(s.X[0], min(s.X[1], s.X[2])), xmx = max(s.X[0], max(s.X[1], s.X[2]));
                     const int32_t ymn = min(s.Y[0], min(s.Y[1], s.Y[2])), ymx = max(s.Y[0], max(s.Y[1], s.Y[2]));
                     const bool small = xmx - xmn < kSmallSpan && ymx - ymn < kSmallSpan;
-                    if (small) {
-#pragma unroll
-                        for (int i = 0; i < 3; i++)
-                            rec.E[i][tid] = (int32_t)(s.Cb[i] + (int64_t)s.A[i] * (x0 * 256) + (int64_t)s.B[i] * (y0 * 256));
-                    }
-                    rec.org[tid] = (x0 - tx0) | ((y0 - ty0) << 8) | (small ? 0 : kLargeRecord);
-                    rec.sc[tid] = a.draws[di].scissor_count ? di : -1;
-                    rec.width[tid] = w;
-                    rec.rwidth[tid] = 1.0f / (float)w;
-                    cnt = (uint32_t)(w * (y1 - y0 + 1));
+                    rec.meta[tid] = (small ? 0 : kLargeRecord) | (a.draws[di].scissor_count ? (di + 1) << 1 : 0);
+                    row_spans<TS>(v.c, s.A, s.B, Et, x0 - tx0, x1 - tx0, y0 - ty0, y1 - ty0, rs);
                 }
             }
             rec.key[tid] = (int)e;
         }
-        // block-wide exclusive scan of the per-record pixel counts
+        // block-wide exclusive scan of (pixels | spans << 17) per record
+        const uint32_t cnt = (uint32_t)rs.npix | ((uint32_t)rs.nspan << 17);
         uint32_t incl = cnt;
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
@@ -628,74 +682,109 @@ __device__ __forceinline__ void raster_tile(const PassArgs& a, const ViewArgs& v
         }
         if (lane == 31) warp_sum[wid] = incl;
         __syncthreads();
-        uint32_t wbase = 0, total = 0;
+        uint32_t wbase = 0;
 #pragma unroll
-        for (int w = 0; w < NT / 32; w++) {
-            uint32_t q = warp_sum[w];
-            if (w < wid) wbase += q;
-            total += q;
-        }
-        rec.start[tid] = wbase + incl - cnt;
-        if (tid == 0) rec.start[NT] = total;
-        __syncthreads();
-        for (uint32_t p = tid; p < total; p += NT) {
-            int lo = 0, hi = nb - 1;
-            while (lo < hi) {  // last record with start <= p
-                int mid = (lo + hi + 1) >> 1;
-                if (rec.start[mid] <= p) lo = mid; else hi = mid - 1;
+        for (int w = 0; w < NW; w++) wbase += w < wid ? warp_sum[w] : 0u;
+        const uint32_t first = wbase + incl - cnt;
+        const uint32_t pix0 = first & 0x1ffffu, span0 = first >> 17;
+        const bool fits = tid < nb && span0 + (uint32_t)rs.nspan <= (uint32_t)CAP;
+        const int consumed = __syncthreads_count(fits);
+        if (fits) {
+            ordered_left += in_stage ? 0u : 1u;
+            uint32_t sp = span0, p = pix0;
+            const uint32_t span_end = span0 + (uint32_t)rs.nspan;
+#pragma unroll
+            for (int r = 0; r < TS; r++) {
+                const uint32_t code = (rs.w[r / 4] >> ((r % 4) * 8)) & 0xffu;
+                const uint32_t lo = code & 15u, hi = code >> 4;
+                if (lo <= hi && sp < span_end) {
+                    rec.span[sp++] = p | ((uint32_t)tid << 16) | ((uint32_t)r << 24) | (lo << 28);
+                    p += hi - lo + 1;
+                }
             }
-            const int r = lo;
-            const int local = (int)(p - rec.start[r]);
-            const int w = rec.width[r];
-            const int oy = (int)(((float)local + 0.5f) * rec.rwidth[r]);
-            const int ox = local - oy * w;
-            const int org = rec.org[r];
-            const int qx = (org & 255) + ox, qy = ((org >> 8) & 255) + oy;
-            const int gx = tx0 + qx, gy = ty0 + qy;
-            const int scd = rec.sc[r];
-            if (scd >= 0 && !scissor_pass(a.draws[scd], gx, gy)) continue;
-            const int32_t A[3] = {rec.A[0][r], rec.A[1][r], rec.A[2][r]};
-            const int32_t B[3] = {rec.B[0][r], rec.B[1][r], rec.B[2][r]};
-            unsigned cov = 0;  // covered samples of this pixel
-            if (!(org & kLargeRecord)) {
-                int32_t e0[3];
+            if (tid == consumed - 1) {
+                s_total[0] = p;
+                s_total[1] = sp;
+            }
+        }
+        __syncthreads();
+        base += (uint32_t)consumed;
+        const uint32_t P = s_total[0];
+        const int NSP = (int)s_total[1];
+        const uint32_t per = (P + NT - 1) / NT * 32;  // per-warp pixel range, a multiple of 32
+        const uint32_t pb = (uint32_t)wid * per, pe = min(P, pb + per);
+        if (pb < pe) {
+            int s0 = 0;
+            {
+                int hi = NSP - 1;
+                while (s0 < hi) {  // last span starting at or before pb
+                    const int mid = (s0 + hi + 1) >> 1;
+                    if ((rec.span[mid] & 0xffffu) <= pb) s0 = mid; else hi = mid - 1;
+                }
+            }
+            uint32_t w0 = rec.span[s0];
+            for (uint32_t p0 = pb; p0 < pe; p0 += 32) {
+                const int si = s0 + 1 + lane;
+                const uint32_t wl = si < NSP ? rec.span[si] : 0u;
+                const uint32_t d = si < NSP ? (wl & 0xffffu) - p0 : 0xffffffffu;  // >= 1
+                const unsigned M = __reduce_or_sync(0xffffffffu, d < 32u ? 1u << d : 0u);
+                const int rank = __popc(M & ((2u << lane) - 1u));
+                uint32_t sw = __shfl_sync(0xffffffffu, wl, max(rank - 1, 0));
+                if (rank == 0) sw = w0;
+                const int adv = __popc(__ballot_sync(0xffffffffu, d <= 32u));
+                if (adv) w0 = __shfl_sync(0xffffffffu, wl, adv - 1);
+                s0 += adv;
+                const uint32_t p = p0 + lane;
+                if (p >= pe) continue;
+                const int r = (int)((sw >> 16) & 0xffu);
+                const int qy = (int)((sw >> 24) & 15u);
+                const int qx = (int)(sw >> 28) + (int)(p - (sw & 0xffffu));
+                const int gx = tx0 + qx, gy = ty0 + qy;
+                const int meta = rec.meta[r];
+                if (meta >> 1 && !scissor_pass(a.draws[(meta >> 1) - 1], gx, gy)) continue;
+                const int32_t A[3] = {rec.A[0][r], rec.A[1][r], rec.A[2][r]};
+                const int32_t B[3] = {rec.B[0][r], rec.B[1][r], rec.B[2][r]};
+                unsigned cov = 0;  // covered samples of this pixel
+                if (!(meta & kLargeRecord)) {
+                    int32_t e0[3];
 #pragma unroll
-                for (int i = 0; i < 3; i++) e0[i] = rec.E[i][r] + A[i] * (ox * 256) + B[i] * (oy * 256);
+                    for (int i = 0; i < 3; i++) e0[i] = (int32_t)rec.Et[i][r] + A[i] * (qx * 256) + B[i] * (qy * 256);
+#pragma unroll
+                    for (int k = 0; k < S; k++) {
+                        const int32_t c0 = e0[0] + A[0] * sample_x<S>(k) + B[0] * sample_y<S>(k);
+                        const int32_t c1 = e0[1] + A[1] * sample_x<S>(k) + B[1] * sample_y<S>(k);
+                        const int32_t c2 = e0[2] + A[2] * sample_x<S>(k) + B[2] * sample_y<S>(k);
+                        cov |= ((c0 | c1 | c2) >= 0 ? 1u : 0u) << k;
+                    }
+                } else {
+                    const int64_t Et[3] = {rec.Et[0][r], rec.Et[1][r], rec.Et[2][r]};
+#pragma unroll
+                    for (int k = 0; k < S; k++)
+                        cov |= (covered(A, B, Et, qx * 256 + sample_x<S>(k), qy * 256 + sample_y<S>(k)) ? 1u : 0u) << k;
+                }
+                if (!cov) continue;
+                const float z0 = rec.z0[r], gzx = rec.dzdx[r], gzy = rec.dzdy[r];
+                const int32_t X0 = rec.X0[r], Y0 = rec.Y0[r];
+                const uint32_t e = (uint32_t)rec.key[r];
+                const uint32_t lo_word = rule.mode == KM_EARLIEST ? e + 1u : 0xFFFFFFFEu - e;
+                unsigned long long* kp = skey + (qy * TS + qx) * S;
+                // (float)(sx - X0) == fbx + sample offset exactly: every term is an integer below
+                // 2^24 in magnitude (guard-band bound), so no conversion per sample is needed.
+                const float fbx = (float)(gx * 256 - X0), fby = (float)(gy * 256 - Y0);
 #pragma unroll
                 for (int k = 0; k < S; k++) {
-                    const int32_t c0 = e0[0] + A[0] * sample_x<S>(k) + B[0] * sample_y<S>(k);
-                    const int32_t c1 = e0[1] + A[1] * sample_x<S>(k) + B[1] * sample_y<S>(k);
-                    const int32_t c2 = e0[2] + A[2] * sample_x<S>(k) + B[2] * sample_y<S>(k);
-                    cov |= ((c0 | c1 | c2) >= 0 ? 1u : 0u) << k;
+                    if (!(cov & (1u << k))) continue;
+                    const float z = (z0 + gzx * (fbx + (float)sample_x<S>(k))) + gzy * (fby + (float)sample_y<S>(k));
+                    uint32_t hi_word;
+                    if (rule.explicit_) {
+                        if (!depth_cmp(rule.func, z, d0_of(v, gx, gy, k))) continue;
+                        hi_word = 0u;
+                    } else {
+                        hi_word = rule.invert ? ~depth_order(z) : depth_order(z);
+                    }
+                    const unsigned long long kv = ((unsigned long long)hi_word << 32) | lo_word;
+                    if (kv < kp[k]) atomicMin(kp + k, kv);
                 }
-            } else {
-                const int64_t Cb[3] = {rec.Cb[0][r], rec.Cb[1][r], rec.Cb[2][r]};
-#pragma unroll
-                for (int k = 0; k < S; k++)
-                    cov |= (covered(A, B, Cb, gx * 256 + sample_x<S>(k), gy * 256 + sample_y<S>(k)) ? 1u : 0u) << k;
-            }
-            if (!cov) continue;
-            const float z0 = rec.z0[r], gzx = rec.dzdx[r], gzy = rec.dzdy[r];
-            const int32_t X0 = rec.X0[r], Y0 = rec.Y0[r];
-            const uint32_t e = (uint32_t)rec.key[r];
-            const uint32_t lo_word = rule.mode == KM_EARLIEST ? e + 1u : 0xFFFFFFFEu - e;
-            unsigned long long* kp = skey + (qy * TS + qx) * S;
-            // (float)(sx - X0) == fbx + sample offset exactly: every term is an integer below
-            // 2^24 in magnitude (guard-band bound), so no conversion per sample is needed.
-            const float fbx = (float)(gx * 256 - X0), fby = (float)(gy * 256 - Y0);
-#pragma unroll
-            for (int k = 0; k < S; k++) {
-                if (!(cov & (1u << k))) continue;
-                const float z = (z0 + gzx * (fbx + (float)sample_x<S>(k))) + gzy * (fby + (float)sample_y<S>(k));
-                uint32_t hi_word;
-                if (rule.explicit_) {
-                    if (!depth_cmp(rule.func, z, d0_of(v, gx, gy, k))) continue;
-                    hi_word = 0u;
-                } else {
-                    hi_word = rule.invert ? ~depth_order(z) : depth_order(z);
-                }
-                const unsigned long long kv = ((unsigned long long)hi_word << 32) | lo_word;
-                if (kv < kp[k]) atomicMin(kp + k, kv);
             }
         }
         __syncthreads();
@@ -710,7 +799,7 @@ __device__ __forceinline__ void raster_tile(const PassArgs& a, const ViewArgs& v
         if (tid == 0) {
             uint32_t sum = 0;
 #pragma unroll
-            for (int w = 0; w < NT / 32; w++) sum += warp_sum[w];
+            for (int w = 0; w < NW; w++) sum += warp_sum[w];
             a.tile_cursor[gtile] = sum;
         }
     }
