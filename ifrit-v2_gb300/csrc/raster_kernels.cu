@@ -562,17 +562,18 @@ struct RowSpans {
     int nspan, npix;
 };
 
-template <int TS>
+// T = int32_t for small records (every value below 2^30), long long otherwise.
+template <int TS, class T>
 __device__ __forceinline__ void row_spans(const PassConst& c, const int32_t A[3], const int32_t B[3],
                                           const long long Et[3], int cx0, int cx1, int ry0, int ry1,
                                           RowSpans<TS>& o) {
-    long long base0[3];
+    T base0[3];
     float rcp[3];
 #pragma unroll
     for (int i = 0; i < 3; i++) {
-        const long long mA = (long long)A[i] * (A[i] > 0 ? c.smax_x : c.smin_x);
-        const long long mB = (long long)B[i] * (B[i] > 0 ? c.smax_y : c.smin_y);
-        base0[i] = Et[i] + mA + mB;
+        const T mA = (T)A[i] * (T)(A[i] > 0 ? c.smax_x : c.smin_x);
+        const T mB = (T)B[i] * (T)(B[i] > 0 ? c.smax_y : c.smin_y);
+        base0[i] = (T)Et[i] + mA + mB;
         rcp[i] = A[i] != 0 ? -1.0f / (256.0f * (float)A[i]) : 0.0f;
     }
     o.nspan = 0;
@@ -584,7 +585,7 @@ __device__ __forceinline__ void row_spans(const PassConst& c, const int32_t A[3]
         bool empty = r < ry0 || r > ry1;
 #pragma unroll
         for (int i = 0; i < 3; i++) {
-            const long long b = base0[i] + (long long)B[i] * (256 * r);
+            const T b = base0[i] + (T)B[i] * (T)(256 * r);
             const float t = fminf(fmaxf((float)b * rcp[i], -2.0f), (float)TS + 1.0f);
             if (A[i] > 0) lo = max(lo, (int)floorf(t));
             else if (A[i] < 0) hi = min(hi, (int)ceilf(t));
@@ -599,6 +600,111 @@ __device__ __forceinline__ void row_spans(const PassConst& c, const int32_t A[3]
     for (int q = 0; q < TS / 4; q++) o.w[q] = w[q];
 }
 
+// Raster set-up of one binned entry, clipped to the tile, in registers.
+struct RasterRec {
+    int32_t A[3], B[3];
+    long long Et[3];  // biased edge functions at the tile origin
+    float z0, dzdx, dzdy;
+    int32_t X0, Y0;
+    int x0, x1, y0, y1;  // covered pixel range within the tile (absolute pixels)
+    bool small;
+};
+
+// Unclipped fill-mode triangles are set up straight from their record: the same integers and
+// stored floats as the general set-up (sub_from_record, sub_bbox, sub_edges, scissor_clamp), with
+// the edge constants of small records formed in 32 bits at the tile origin.  Everything else
+// (clipped fan triangles, LINE / POINT parts) goes through the general set-up.
+__device__ __forceinline__ bool raster_entry(const PassArgs& a, const PassConst& c, uint32_t e, int tx0, int ty0,
+                                             int xmax, int ymax, RasterRec& o, int& di) {
+    const int g = (int)(e >> 3), sub = (int)(e & 7u);
+    const TriRecord* rp = a.records + g;
+    const int4 q1 = __ldg(reinterpret_cast<const int4*>(rp) + 1);
+    di = q1.w;
+    const DrawDev& d = a.draws[di];
+    int32_t X[3], Y[3];
+    int px0, px1, py0, py1;
+    if (sub == 0 && (q1.z & REC_VALID) && d.polygon_mode == POLY_FILL) {
+        const int4 q0 = __ldg(reinterpret_cast<const int4*>(rp));
+        const float4 q2 = __ldg(reinterpret_cast<const float4*>(rp) + 2);
+        X[0] = q0.x; Y[0] = q0.y; X[1] = q0.z; Y[1] = q0.w; X[2] = q1.x; Y[2] = q1.y;
+        o.z0 = q2.x; o.dzdx = q2.y; o.dzdy = q2.z;
+        const int32_t xmn = min(X[0], min(X[1], X[2])), xmx = max(X[0], max(X[1], X[2]));
+        const int32_t ymn = min(Y[0], min(Y[1], Y[2])), ymx = max(Y[0], max(Y[1], Y[2]));
+        // snapped coordinates are within the guard band (|X|, |Y| < 2^24): floor division by 256
+        // is an arithmetic shift
+        px0 = max(-((c.smax_x - xmn) >> 8), 0);
+        px1 = min((xmx - c.smin_x) >> 8, c.W - 1);
+        py0 = max(-((c.smax_y - ymn) >> 8), 0);
+        py1 = min((ymx - c.smin_y) >> 8, c.H - 1);
+        if (d.scissor_count) {
+            px0 = max(px0, d.scissor_box[0]);
+            py0 = max(py0, d.scissor_box[1]);
+            px1 = min(px1, d.scissor_box[2]);
+            py1 = min(py1, d.scissor_box[3]);
+        }
+        o.small = xmx - xmn < kSmallSpan && ymx - ymn < kSmallSpan;
+    } else {
+        SubTri s;
+        if (!setup_raster_entry(a, c, e, &s, &di)) return false;
+#pragma unroll
+        for (int i = 0; i < 3; i++) { X[i] = s.X[i]; Y[i] = s.Y[i]; }
+        o.z0 = s.z[0]; o.dzdx = s.dzdx; o.dzdy = s.dzdy;
+        px0 = s.px0; px1 = s.px1; py0 = s.py0; py1 = s.py1;
+        const int32_t xmn = min(X[0], min(X[1], X[2])), xmx = max(X[0], max(X[1], X[2]));
+        const int32_t ymn = min(Y[0], min(Y[1], Y[2])), ymx = max(Y[0], max(Y[1], Y[2]));
+        o.small = xmx - xmn < kSmallSpan && ymx - ymn < kSmallSpan;
+    }
+    o.x0 = max(px0, tx0); o.x1 = min(px1, xmax);
+    o.y0 = max(py0, ty0); o.y1 = min(py1, ymax);
+    if (o.x0 > o.x1 || o.y0 > o.y1) return false;
+    o.X0 = X[0];
+    o.Y0 = Y[0];
+#pragma unroll
+    for (int i = 0; i < 3; i++) {
+        const int j = (i + 1) % 3, k = (i + 2) % 3;
+        o.A[i] = Y[j] - Y[k];
+        o.B[i] = X[k] - X[j];
+        const int bias = (o.A[i] > 0) || (o.A[i] == 0 && o.B[i] > 0) ? 0 : 1;
+        // E_i(x, y) = A (x - X_j) + B (y - Y_j) - bias
+        if (o.small)
+            o.Et[i] = (long long)(o.A[i] * (tx0 * 256 - X[j]) + o.B[i] * (ty0 * 256 - Y[j]) - bias);
+        else
+            o.Et[i] = (long long)o.A[i] * (tx0 * 256 - X[j]) + (long long)o.B[i] * (ty0 * 256 - Y[j]) - bias;
+    }
+    return true;
+}
+
+// Depth test of the covered samples of one queued pixel: record | x << 8 | y << 12 | samples << 16.
+template <int S, int TS>
+__device__ __forceinline__ void raster_depth(const ViewArgs& v, const KeyRule& rule, const TileRecords<TS * TS>& rec,
+                                             unsigned long long* skey, int tx0, int ty0, uint32_t item) {
+    const int r = (int)(item & 0xffu), qx = (int)((item >> 8) & 15u), qy = (int)((item >> 12) & 15u);
+    const unsigned cov = item >> 16;
+    const int gx = tx0 + qx, gy = ty0 + qy;
+    const float z0 = rec.z0[r], gzx = rec.dzdx[r], gzy = rec.dzdy[r];
+    const int32_t X0 = rec.X0[r], Y0 = rec.Y0[r];
+    const uint32_t e = (uint32_t)rec.key[r];
+    const uint32_t lo_word = rule.mode == KM_EARLIEST ? e + 1u : 0xFFFFFFFEu - e;
+    unsigned long long* kp = skey + (qy * TS + qx) * S;
+    // (float)(sx - X0) == fbx + sample offset exactly: every term is an integer below
+    // 2^24 in magnitude (guard-band bound), so no conversion per sample is needed.
+    const float fbx = (float)(gx * 256 - X0), fby = (float)(gy * 256 - Y0);
+#pragma unroll
+    for (int k = 0; k < S; k++) {
+        if (!(cov & (1u << k))) continue;
+        const float z = (z0 + gzx * (fbx + (float)sample_x<S>(k))) + gzy * (fby + (float)sample_y<S>(k));
+        uint32_t hi_word;
+        if (rule.explicit_) {
+            if (!depth_cmp(rule.func, z, d0_of(v, gx, gy, k))) continue;
+            hi_word = 0u;
+        } else {
+            hi_word = rule.invert ? ~depth_order(z) : depth_order(z);
+        }
+        const unsigned long long kv = ((unsigned long long)hi_word << 32) | lo_word;
+        if (kv < kp[k]) atomicMin(kp + k, kv);
+    }
+}
+
 // One tile: the tile's list is consumed in batches of up to NT set-ups.  Every record's clipped
 // bbox is cut into conservative row spans; the batch's spans are laid end to end and every pixel
 // of them is visited by one lane (each warp walks a contiguous range, finding the span of each of
@@ -610,6 +716,8 @@ __device__ __forceinline__ void raster_tile(const PassArgs& a, const ViewArgs& v
                                             unsigned long long* skey, uint32_t* warp_sum) {
     constexpr int NT = TS * TS, NW = NT / 32, CAP = span_capacity<NT>();
     __shared__ uint32_t s_total[2];
+    __shared__ uint32_t s_queue[NW * 64];
+    uint32_t* wq = s_queue + (threadIdx.x >> 5) * 64;
     const int ltile = gtile - v.tile_start;
     const int tx = ltile % v.c.tiles_x, ty = ltile / v.c.tiles_x;
     const int tx0 = tx * TS, ty0 = ty * TS;
@@ -642,33 +750,24 @@ __device__ __forceinline__ void raster_tile(const PassArgs& a, const ViewArgs& v
         bool in_stage = true;
         if (tid < nb) {
             uint32_t e = __ldg(a.pairs + base + tid);
-            SubTri s;
+            RasterRec s;
             int di;
             // ordered views: only the order-independent prefix is resolved here
             in_stage = !v.ordered || (int)(e >> 3) < v.first_tri + v.ordered_prefix;
-            if (in_stage && setup_raster_entry(a, v.c, e, &s, &di)) {
-                const int x0 = max(s.px0, tx0), x1 = min(s.px1, xmax);
-                const int y0 = max(s.py0, ty0), y1 = min(s.py1, ymax);
-                if (x0 <= x1 && y0 <= y1) {
-                    long long Et[3];
+            if (in_stage && raster_entry(a, v.c, e, tx0, ty0, xmax, ymax, s, di)) {
 #pragma unroll
-                    for (int i = 0; i < 3; i++) {
-                        Et[i] = s.Cb[i] + (long long)s.A[i] * (tx0 * 256) + (long long)s.B[i] * (ty0 * 256);
-                        rec.A[i][tid] = s.A[i];
-                        rec.B[i][tid] = s.B[i];
-                        rec.Et[i][tid] = Et[i];
-                    }
-                    rec.z0[tid] = s.z[0];
-                    rec.dzdx[tid] = s.dzdx;
-                    rec.dzdy[tid] = s.dzdy;
-                    rec.X0[tid] = s.X[0];
-                    rec.Y0[tid] = s.Y[0];
-                    const int32_t xmn = min(s.X[0], min(s.X[1], s.X[2])), xmx = max(s.X[0], max(s.X[1], s.X[2]));
-                    const int32_t ymn = min(s.Y[0], min(s.Y[1], s.Y[2])), ymx = max(s.Y[0], max(s.Y[1], s.Y[2]));
-                    const bool small = xmx - xmn < kSmallSpan && ymx - ymn < kSmallSpan;
-                    rec.meta[tid] = (small ? 0 : kLargeRecord) | (a.draws[di].scissor_count ? (di + 1) << 1 : 0);
-                    row_spans<TS>(v.c, s.A, s.B, Et, x0 - tx0, x1 - tx0, y0 - ty0, y1 - ty0, rs);
+                for (int i = 0; i < 3; i++) {
+                    rec.A[i][tid] = s.A[i];
+                    rec.B[i][tid] = s.B[i];
+                    rec.Et[i][tid] = s.Et[i];
                 }
+                rec.z0[tid] = s.z0;
+                rec.dzdx[tid] = s.dzdx;
+                rec.dzdy[tid] = s.dzdy;
+                rec.X0[tid] = s.X0;
+                rec.Y0[tid] = s.Y0;
+                rec.meta[tid] = (s.small ? 0 : kLargeRecord) | (a.draws[di].scissor_count ? (di + 1) << 1 : 0);
+                row_spans<TS, long long>(v.c, s.A, s.B, s.Et, s.x0 - tx0, s.x1 - tx0, s.y0 - ty0, s.y1 - ty0, rs);
             }
             rec.key[tid] = (int)e;
         }
@@ -723,6 +822,7 @@ __device__ __forceinline__ void raster_tile(const PassArgs& a, const ViewArgs& v
                 }
             }
             uint32_t w0 = rec.span[s0];
+            int qh = 0, qn = 0;  // the warp's ring of covered pixels: head, count
             for (uint32_t p0 = pb; p0 < pe; p0 += 32) {
                 const int si = s0 + 1 + lane;
                 const uint32_t wl = si < NSP ? rec.span[si] : 0u;
@@ -735,57 +835,53 @@ __device__ __forceinline__ void raster_tile(const PassArgs& a, const ViewArgs& v
                 if (adv) w0 = __shfl_sync(0xffffffffu, wl, adv - 1);
                 s0 += adv;
                 const uint32_t p = p0 + lane;
-                if (p >= pe) continue;
                 const int r = (int)((sw >> 16) & 0xffu);
                 const int qy = (int)((sw >> 24) & 15u);
                 const int qx = (int)(sw >> 28) + (int)(p - (sw & 0xffffu));
-                const int gx = tx0 + qx, gy = ty0 + qy;
-                const int meta = rec.meta[r];
-                if (meta >> 1 && !scissor_pass(a.draws[(meta >> 1) - 1], gx, gy)) continue;
-                const int32_t A[3] = {rec.A[0][r], rec.A[1][r], rec.A[2][r]};
-                const int32_t B[3] = {rec.B[0][r], rec.B[1][r], rec.B[2][r]};
                 unsigned cov = 0;  // covered samples of this pixel
-                if (!(meta & kLargeRecord)) {
-                    int32_t e0[3];
+                if (p < pe) {
+                    const int meta = rec.meta[r];
+                    if (!(meta >> 1) || scissor_pass(a.draws[(meta >> 1) - 1], tx0 + qx, ty0 + qy)) {
+                        const int32_t A[3] = {rec.A[0][r], rec.A[1][r], rec.A[2][r]};
+                        const int32_t B[3] = {rec.B[0][r], rec.B[1][r], rec.B[2][r]};
+                        if (!(meta & kLargeRecord)) {
+                            int32_t e0[3];
 #pragma unroll
-                    for (int i = 0; i < 3; i++) e0[i] = (int32_t)rec.Et[i][r] + A[i] * (qx * 256) + B[i] * (qy * 256);
+                            for (int i = 0; i < 3; i++)
+                                e0[i] = (int32_t)rec.Et[i][r] + A[i] * (qx * 256) + B[i] * (qy * 256);
 #pragma unroll
-                    for (int k = 0; k < S; k++) {
-                        const int32_t c0 = e0[0] + A[0] * sample_x<S>(k) + B[0] * sample_y<S>(k);
-                        const int32_t c1 = e0[1] + A[1] * sample_x<S>(k) + B[1] * sample_y<S>(k);
-                        const int32_t c2 = e0[2] + A[2] * sample_x<S>(k) + B[2] * sample_y<S>(k);
-                        cov |= ((c0 | c1 | c2) >= 0 ? 1u : 0u) << k;
+                            for (int k = 0; k < S; k++) {
+                                const int32_t c0 = e0[0] + A[0] * sample_x<S>(k) + B[0] * sample_y<S>(k);
+                                const int32_t c1 = e0[1] + A[1] * sample_x<S>(k) + B[1] * sample_y<S>(k);
+                                const int32_t c2 = e0[2] + A[2] * sample_x<S>(k) + B[2] * sample_y<S>(k);
+                                cov |= ((c0 | c1 | c2) >= 0 ? 1u : 0u) << k;
+                            }
+                        } else {
+                            const int64_t Et[3] = {rec.Et[0][r], rec.Et[1][r], rec.Et[2][r]};
+#pragma unroll
+                            for (int k = 0; k < S; k++)
+                                cov |= (covered(A, B, Et, qx * 256 + sample_x<S>(k), qy * 256 + sample_y<S>(k)) ? 1u : 0u)
+                                       << k;
+                        }
                     }
-                } else {
-                    const int64_t Et[3] = {rec.Et[0][r], rec.Et[1][r], rec.Et[2][r]};
-#pragma unroll
-                    for (int k = 0; k < S; k++)
-                        cov |= (covered(A, B, Et, qx * 256 + sample_x<S>(k), qy * 256 + sample_y<S>(k)) ? 1u : 0u) << k;
                 }
-                if (!cov) continue;
-                const float z0 = rec.z0[r], gzx = rec.dzdx[r], gzy = rec.dzdy[r];
-                const int32_t X0 = rec.X0[r], Y0 = rec.Y0[r];
-                const uint32_t e = (uint32_t)rec.key[r];
-                const uint32_t lo_word = rule.mode == KM_EARLIEST ? e + 1u : 0xFFFFFFFEu - e;
-                unsigned long long* kp = skey + (qy * TS + qx) * S;
-                // (float)(sx - X0) == fbx + sample offset exactly: every term is an integer below
-                // 2^24 in magnitude (guard-band bound), so no conversion per sample is needed.
-                const float fbx = (float)(gx * 256 - X0), fby = (float)(gy * 256 - Y0);
-#pragma unroll
-                for (int k = 0; k < S; k++) {
-                    if (!(cov & (1u << k))) continue;
-                    const float z = (z0 + gzx * (fbx + (float)sample_x<S>(k))) + gzy * (fby + (float)sample_y<S>(k));
-                    uint32_t hi_word;
-                    if (rule.explicit_) {
-                        if (!depth_cmp(rule.func, z, d0_of(v, gx, gy, k))) continue;
-                        hi_word = 0u;
-                    } else {
-                        hi_word = rule.invert ? ~depth_order(z) : depth_order(z);
-                    }
-                    const unsigned long long kv = ((unsigned long long)hi_word << 32) | lo_word;
-                    if (kv < kp[k]) atomicMin(kp + k, kv);
+                // covered pixels are queued so that the depth tests run on full warps
+                const unsigned bal = __ballot_sync(0xffffffffu, cov != 0u);
+                if (cov)
+                    wq[(qh + qn + __popc(bal & ((1u << lane) - 1u))) & 63] =
+                        (uint32_t)r | ((uint32_t)qx << 8) | ((uint32_t)qy << 12) | (cov << 16);
+                qn += __popc(bal);
+                if (qn >= 32) {
+                    __syncwarp();
+                    const uint32_t item = wq[(qh + lane) & 63];
+                    __syncwarp();
+                    qh = (qh + 32) & 63;
+                    qn -= 32;
+                    raster_depth<S, TS>(v, rule, rec, skey, tx0, ty0, item);
                 }
             }
+            __syncwarp();
+            if (lane < qn) raster_depth<S, TS>(v, rule, rec, skey, tx0, ty0, wq[(qh + lane) & 63]);
         }
         __syncthreads();
     }
