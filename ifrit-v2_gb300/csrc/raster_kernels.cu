@@ -549,31 +549,34 @@ struct TileRecords {
     uint32_t span[span_capacity<NT>()];
 };
 
-// Conservative covered columns of every tile row of a record: for each edge the largest value
-// over a pixel's sample pattern, A·(256c + sx) + B·(256r + sy) + E, must be >= 0 at some sample
-// of the pixel, which bounds column c from one side per edge with A != 0 (the crossing column is
-// computed in float from the exact integer and widened to the next integer, which absorbs the
-// relative error of the three roundings, ~2^-22 of at most TS + 2 columns); an edge with A == 0
-// empties the row when its largest value is negative.  Row r's range is packed as lo | hi << 4
-// into bits 8(r mod 4) of word r / 4; an empty row is 0x0f.
+// Conservative covered columns of every tile row of a record.  A pixel (c, r) of the tile can
+// hold a covered sample only if, for every edge, E(256c, 256r) + max_k (A sx_k + B sy_k) >= 0
+// (the largest value of the edge over the pixel's sample pattern).  Each edge with A != 0 bounds c
+// from one side at the crossing column t = -(E(0, 256r) + max_k(..)) / (256 A), computed in float
+// from the exact integer with a relative error below 2^-21 (three roundings), i.e. below 10^-5
+// columns where it matters (|t| <= TS + 2); rounding t -+ 2^-10 up / down keeps the bound
+// conservative without widening it by a column.  An edge with A == 0 empties the row when its
+// largest value is negative.  Row r's range is packed as lo | hi << 4 into bits 8(r mod 4) of
+// word r / 4; an empty row is 0x0f.
 template <int TS>
 struct RowSpans {
     uint32_t w[TS / 4];
     int nspan, npix;
+    bool large;  // the record needs the 64-bit coverage test
 };
 
-// T = int32_t for small records (every value below 2^30), long long otherwise.
-template <int TS, class T>
-__device__ __forceinline__ void row_spans(const PassConst& c, const int32_t A[3], const int32_t B[3],
-                                          const long long Et[3], int cx0, int cx1, int ry0, int ry1,
-                                          RowSpans<TS>& o) {
-    T base0[3];
+template <int S, int TS>
+__device__ __forceinline__ void row_spans(const int32_t A[3], const int32_t B[3], const long long Et[3], int cx0,
+                                          int cx1, int ry0, int ry1, RowSpans<TS>& o) {
+    constexpr float kEps = 1.0f / 1024.0f;
+    long long base0[3];
     float rcp[3];
 #pragma unroll
     for (int i = 0; i < 3; i++) {
-        const T mA = (T)A[i] * (T)(A[i] > 0 ? c.smax_x : c.smin_x);
-        const T mB = (T)B[i] * (T)(B[i] > 0 ? c.smax_y : c.smin_y);
-        base0[i] = (T)Et[i] + mA + mB;
+        long long m = (long long)A[i] * sample_x<S>(0) + (long long)B[i] * sample_y<S>(0);
+#pragma unroll
+        for (int k = 1; k < S; k++) m = max(m, (long long)A[i] * sample_x<S>(k) + (long long)B[i] * sample_y<S>(k));
+        base0[i] = Et[i] + m;
         rcp[i] = A[i] != 0 ? -1.0f / (256.0f * (float)A[i]) : 0.0f;
     }
     o.nspan = 0;
@@ -585,10 +588,10 @@ __device__ __forceinline__ void row_spans(const PassConst& c, const int32_t A[3]
         bool empty = r < ry0 || r > ry1;
 #pragma unroll
         for (int i = 0; i < 3; i++) {
-            const T b = base0[i] + (T)B[i] * (T)(256 * r);
+            const long long b = base0[i] + (long long)B[i] * (256 * r);
             const float t = fminf(fmaxf((float)b * rcp[i], -2.0f), (float)TS + 1.0f);
-            if (A[i] > 0) lo = max(lo, (int)floorf(t));
-            else if (A[i] < 0) hi = min(hi, (int)ceilf(t));
+            if (A[i] > 0) lo = max(lo, (int)ceilf(t - kEps));
+            else if (A[i] < 0) hi = min(hi, (int)floorf(t + kEps));
             else empty |= b < 0;
         }
         empty |= lo > hi;
@@ -715,7 +718,7 @@ template <int S, int TS>
 __device__ __forceinline__ void raster_tile(const PassArgs& a, const ViewArgs& v, int gtile, TileRecords<TS * TS>& rec,
                                             unsigned long long* skey, uint32_t* warp_sum) {
     constexpr int NT = TS * TS, NW = NT / 32, CAP = span_capacity<NT>();
-    __shared__ uint32_t s_total[2];
+    __shared__ uint32_t s_total[4];
     __shared__ uint32_t s_queue[NW * 64];
     uint32_t* wq = s_queue + (threadIdx.x >> 5) * 64;
     const int ltile = gtile - v.tile_start;
@@ -745,6 +748,7 @@ __device__ __forceinline__ void raster_tile(const PassArgs& a, const ViewArgs& v
         RowSpans<TS> rs;  // every row empty unless the record is set up below
         rs.nspan = 0;
         rs.npix = 0;
+        rs.large = false;
 #pragma unroll
         for (int q = 0; q < TS / 4; q++) rs.w[q] = 0x0f0f0f0fu;
         bool in_stage = true;
@@ -767,31 +771,53 @@ __device__ __forceinline__ void raster_tile(const PassArgs& a, const ViewArgs& v
                 rec.X0[tid] = s.X0;
                 rec.Y0[tid] = s.Y0;
                 rec.meta[tid] = (s.small ? 0 : kLargeRecord) | (a.draws[di].scissor_count ? (di + 1) << 1 : 0);
-                row_spans<TS, long long>(v.c, s.A, s.B, s.Et, s.x0 - tx0, s.x1 - tx0, s.y0 - ty0, s.y1 - ty0, rs);
+                row_spans<S, TS>(s.A, s.B, s.Et, s.x0 - tx0, s.x1 - tx0, s.y0 - ty0, s.y1 - ty0, rs);
+                rs.large = !s.small;
             }
             rec.key[tid] = (int)e;
         }
-        // block-wide exclusive scan of (pixels | spans << 17) per record
+        // block-wide exclusive scan of (pixels | spans << 17) per record, small and large records
+        // counted apart: the spans of large records (64-bit coverage tests) follow those of the
+        // small ones, so that warps rarely mix the two tests
         const uint32_t cnt = (uint32_t)rs.npix | ((uint32_t)rs.nspan << 17);
-        uint32_t incl = cnt;
+        const bool large = rs.large;
+        uint32_t incl_s = large ? 0u : cnt, incl_l = large ? cnt : 0u;
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
-            uint32_t q = __shfl_up_sync(0xffffffffu, incl, o);
-            if (lane >= o) incl += q;
+            const uint32_t qs = __shfl_up_sync(0xffffffffu, incl_s, o);
+            const uint32_t ql = __shfl_up_sync(0xffffffffu, incl_l, o);
+            if (lane >= o) {
+                incl_s += qs;
+                incl_l += ql;
+            }
         }
-        if (lane == 31) warp_sum[wid] = incl;
+        if (lane == 31) {
+            warp_sum[wid] = incl_s;
+            warp_sum[NW + wid] = incl_l;
+        }
         __syncthreads();
-        uint32_t wbase = 0;
 #pragma unroll
-        for (int w = 0; w < NW; w++) wbase += w < wid ? warp_sum[w] : 0u;
-        const uint32_t first = wbase + incl - cnt;
-        const uint32_t pix0 = first & 0x1ffffu, span0 = first >> 17;
-        const bool fits = tid < nb && span0 + (uint32_t)rs.nspan <= (uint32_t)CAP;
+        for (int w = 0; w < NW; w++) {
+            incl_s += w < wid ? warp_sum[w] : 0u;
+            incl_l += w < wid ? warp_sum[NW + w] : 0u;
+        }
+        const bool fits = tid < nb && (incl_s >> 17) + (incl_l >> 17) <= (uint32_t)CAP;
         const int consumed = __syncthreads_count(fits);
+        if (tid == consumed - 1) {
+            s_total[0] = incl_s & 0x1ffffu;  // pixels and spans of the small records
+            s_total[1] = incl_s >> 17;
+            s_total[2] = incl_l & 0x1ffffu;  // pixels and spans of the large records
+            s_total[3] = incl_l >> 17;
+        }
+        __syncthreads();
+        const uint32_t Ps = s_total[0], Ns = s_total[1];
+        const uint32_t P = Ps + s_total[2];
+        const int NSP = (int)(Ns + s_total[3]);
         if (fits) {
             ordered_left += in_stage ? 0u : 1u;
-            uint32_t sp = span0, p = pix0;
-            const uint32_t span_end = span0 + (uint32_t)rs.nspan;
+            const uint32_t first = (large ? incl_l : incl_s) - cnt;
+            uint32_t sp = (first >> 17) + (large ? Ns : 0u), p = (first & 0x1ffffu) + (large ? Ps : 0u);
+            const uint32_t span_end = sp + (uint32_t)rs.nspan;
 #pragma unroll
             for (int r = 0; r < TS; r++) {
                 const uint32_t code = (rs.w[r / 4] >> ((r % 4) * 8)) & 0xffu;
@@ -801,15 +827,9 @@ __device__ __forceinline__ void raster_tile(const PassArgs& a, const ViewArgs& v
                     p += hi - lo + 1;
                 }
             }
-            if (tid == consumed - 1) {
-                s_total[0] = p;
-                s_total[1] = sp;
-            }
         }
         __syncthreads();
         base += (uint32_t)consumed;
-        const uint32_t P = s_total[0];
-        const int NSP = (int)s_total[1];
         const uint32_t per = (P + NT - 1) / NT * 32;  // per-warp pixel range, a multiple of 32
         const uint32_t pb = (uint32_t)wid * per, pe = min(P, pb + per);
         if (pb < pe) {
@@ -924,7 +944,7 @@ __global__ void __launch_bounds__(TS * TS, 1024 / (TS * TS)) raster_kernel(PassA
     extern __shared__ __align__(16) unsigned char smem_raw[];
     TileRecords<NT>& rec = *reinterpret_cast<TileRecords<NT>*>(smem_raw);
     unsigned long long* skey = reinterpret_cast<unsigned long long*>(smem_raw + sizeof(TileRecords<NT>));
-    __shared__ uint32_t warp_sum[NT / 32];
+    __shared__ uint32_t warp_sum[2 * (NT / 32)];
     __shared__ ViewArgs sv;
     __shared__ int s_tile, s_view;
     if (threadIdx.x == 0) s_view = -1;
