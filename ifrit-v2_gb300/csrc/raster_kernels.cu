@@ -959,7 +959,7 @@ __global__ void __launch_bounds__(TS * TS, 1024 / (TS * TS)) raster_kernel(PassA
 template <int S, int TS>
 __device__ __forceinline__ void shade_tile(const PassArgs& a, const ViewArgs& v, int gtile, int part,
                                            float4 (*scol)[TS * TS], float4 (*splane)[TS * TS], int (*splane_y)[TS * TS],
-                                           int2* witems, bool keep_samples) {
+                                           int2* witems, float4* wres, bool keep_samples) {
     const int ltile = gtile - v.tile_start;
     const int tx = ltile % v.c.tiles_x, ty = ltile / v.c.tiles_x;
     const int tid = threadIdx.x;
@@ -1028,33 +1028,93 @@ __device__ __forceinline__ void shade_tile(const PassArgs& a, const ViewArgs& v,
     for (int j = 0; j < U; j++)
         if (j < nc) items[incl - nc + j] = make_int2(uniq[j], lane | (j << 5));
     __syncwarp();
-    for (int b = lane; b < total; b += 32) {
-        const int2 it = items[b];
-        const int owner = it.y & 31, slot = it.y >> 5;
-        int olx, oly;
-        tile_pixel<TS>(part * 32 + owner, olx, oly);
-        const int opx = tx * TS + olx, opy = ty * TS + oly;
-        const int g = it.x >> 3, sub = it.x & 7;
-        const int di = record_draw(a, g);
-        const DrawDev& d = a.draws[di];
-        const int t = g - __ldg(a.draw_start + di);
-        SubTri st;
-        const bool from_record = setup_entry_sub(v.c, d, a.records, g, t, sub, st) && sub == 0 &&
-                                 (__ldg(&a.records[g].flags) & REC_VALID);
-        ShadeGeom geo;
-        shade_geom_from(st, geo);
-        float c[4];
-        if (from_record && a.attrs && d.shading != SHADE_PRIMID && d.attr_count > 0) {
-            const float4 q0 = __ldg(&a.attrs[g].a[0]), q1 = __ldg(&a.attrs[g].a[1]), q2 = __ldg(&a.attrs[g].a[2]);
-            const float a0[4] = {q0.x, q0.y, q0.z, q0.w}, a1[4] = {q1.x, q1.y, q1.z, q1.w};
-            const float a2[4] = {q2.x, q2.y, q2.z, q2.w};
-            shade_fragment_attrs(v.c, d, geo, t, sub, opx, opy, a0, a1, a2, c);
-        } else {
-            shade_fragment(v.c, d, geo, t, sub, opx, opy, c);
+    for (int r0 = 0; r0 < total; r0 += 32) {
+        const int b = r0 + lane;
+        int owner = 0, slot = 0, di = 0, n = 0;  // n: texture probes of this lane's item
+        float c[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+        TexProbe tp;
+        tp.u = tp.v = tp.du = tp.dv = tp.t = 0.0f;
+        tp.lo = tp.hi = tp.n = 0;
+        tp.two = tp.aniso = false;
+        if (b < total) {
+            const int2 it = items[b];
+            owner = it.y & 31;
+            slot = it.y >> 5;
+            int olx, oly;
+            tile_pixel<TS>(part * 32 + owner, olx, oly);
+            const int opx = tx * TS + olx, opy = ty * TS + oly;
+            const int g = it.x >> 3, sub = it.x & 7;
+            di = record_draw(a, g);
+            const DrawDev& d = a.draws[di];
+            const int t = g - __ldg(a.draw_start + di);
+            SubTri st;
+            const bool from_record = setup_entry_sub(v.c, d, a.records, g, t, sub, st) && sub == 0 &&
+                                     (__ldg(&a.records[g].flags) & REC_VALID);
+            ShadeGeom geo;
+            shade_geom_from(st, geo);
+            float a0[4], a1[4], a2[4];
+            if (from_record && a.attrs && d.shading != SHADE_PRIMID && d.attr_count > 0) {
+                const float4 q0 = __ldg(&a.attrs[g].a[0]), q1 = __ldg(&a.attrs[g].a[1]), q2 = __ldg(&a.attrs[g].a[2]);
+                a0[0] = q0.x; a0[1] = q0.y; a0[2] = q0.z; a0[3] = q0.w;
+                a1[0] = q1.x; a1[1] = q1.y; a1[2] = q1.z; a1[3] = q1.w;
+                a2[0] = q2.x; a2[1] = q2.y; a2[2] = q2.z; a2[3] = q2.w;
+            } else if (d.shading != SHADE_PRIMID) {
+                fetch_attrs(d, t, a0, a1, a2);
+            } else {
+#pragma unroll
+                for (int k = 0; k < 4; k++) a0[k] = a1[k] = a2[k] = 0.0f;
+            }
+            if (shade_prepare_attrs(v.c, d, geo, t, sub, opx, opy, a0, a1, a2, c, tp)) n = tp.n;
+            splane[slot][wbase + owner] = make_float4(st.z[0], st.dzdx, st.dzdy, __int_as_float(st.X[0]));
+            splane_y[slot][wbase + owner] = st.Y[0];
         }
-        scol[slot][wbase + owner] = make_float4(c[0], c[1], c[2], c[3]);
-        splane[slot][wbase + owner] = make_float4(st.z[0], st.dzdx, st.dzdy, __int_as_float(st.X[0]));
-        splane_y[slot][wbase + owner] = st.Y[0];
+        // The round's texture probes are spread over the lanes (anisotropic lookups take 1 to
+        // max_aniso probes each); every item then adds its probes' results in probe order.
+        int incl = n;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int q = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += q;
+        }
+        const int T = __shfl_sync(0xffffffffu, incl, 31);
+        if (T > 0) {
+            const int pre = incl - n;
+            const int packed = tp.lo | (tp.hi << 8) | (tp.n << 16) | (tp.two ? 1 << 24 : 0) | (tp.aniso ? 1 << 25 : 0);
+            float acc[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+            for (int c0 = 0; c0 < T; c0 += 32) {
+                const int j = c0 + lane;
+                int k = 0;  // the item of probe j: the last lane whose first probe is at or before j
+#pragma unroll
+                for (int step = 16; step > 0; step >>= 1)
+                    if (__shfl_sync(0xffffffffu, pre, k + step) <= j) k += step;
+                TexProbe q;
+                q.u = __shfl_sync(0xffffffffu, tp.u, k);
+                q.v = __shfl_sync(0xffffffffu, tp.v, k);
+                q.du = __shfl_sync(0xffffffffu, tp.du, k);
+                q.dv = __shfl_sync(0xffffffffu, tp.dv, k);
+                q.t = __shfl_sync(0xffffffffu, tp.t, k);
+                const int qp = __shfl_sync(0xffffffffu, packed, k);
+                const int qd = __shfl_sync(0xffffffffu, di, k);
+                const int i = j - __shfl_sync(0xffffffffu, pre, k);
+                q.lo = qp & 255;
+                q.hi = (qp >> 8) & 255;
+                q.n = (qp >> 16) & 255;
+                q.two = (qp >> 24) & 1;
+                q.aniso = (qp >> 25) & 1;
+                float r[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+                if (j < T) tex_probe(a.draws[qd], q, i, r);
+                wres[lane] = make_float4(r[0], r[1], r[2], r[3]);
+                __syncwarp();
+                const int qa = max(pre, c0), qb = min(pre + n, c0 + 32);
+                for (int m = qa; m < qb; m++) {
+                    const float4 x = wres[m - c0];
+                    acc[0] = acc[0] + x.x; acc[1] = acc[1] + x.y; acc[2] = acc[2] + x.z; acc[3] = acc[3] + x.w;
+                }
+                __syncwarp();
+            }
+            if (n > 0) tex_finish(tp, acc, c);
+        }
+        if (b < total) scol[slot][wbase + owner] = make_float4(c[0], c[1], c[2], c[3]);
     }
     __syncwarp();
     float dep[S];
@@ -1136,6 +1196,7 @@ __global__ void __launch_bounds__(TS * TS, 1024 / (TS * TS)) shade_kernel(PassAr
     __shared__ float4 splane[4][NT];  // their depth planes: z0, dz/dx, dz/dy, X0 (bits)
     __shared__ int splane_y[4][NT];   // and Y0
     __shared__ int2 witems[NT / 32 * 32 * U];  // per warp: compacted (entry, lane | slot << 5) items
+    __shared__ float4 sres[NT];                // per warp: results of one round of texture probes
     const int lane = threadIdx.x & 31;
     const int ntasks = (g.tile_end - g.tile_begin) * kTasksPerTile;
     for (;;) {
@@ -1159,7 +1220,8 @@ __global__ void __launch_bounds__(TS * TS, 1024 / (TS * TS)) shade_kernel(PassAr
         // tiles of ordered views with entries left for the ordered stage keep their per-sample
         // colours for it instead of resolving
         const bool keep = a.views[vi].ordered && __ldg(a.tile_cursor + gtile) != 0u;
-        shade_tile<S, TS>(a, a.views[vi], gtile, task % kTasksPerTile, scol, splane, splane_y, witems, keep);
+        shade_tile<S, TS>(a, a.views[vi], gtile, task % kTasksPerTile, scol, splane, splane_y, witems,
+                          sres + (threadIdx.x & ~31), keep);
     }
 }
 

@@ -708,15 +708,29 @@ __device__ __forceinline__ void tex_trilinear2(const TexLevel& L0, const TexLeve
 
 __device__ __forceinline__ float finite_or_zero(float x) { return isfinite(x) ? x : 0.0f; }
 
-// Texture sampling with LOD from screen-space derivatives (ShaderBuiltinCuda.cuh:225-272).
-__device__ __forceinline__ void tex_sample(const DrawDev& d, float u, float v, float dudx, float dvdx, float dudy,
-                                           float dvdy, float out[4]) {
+// A texture lookup reduced to its probes: n trilinear fetches between levels lo and hi (weight
+// t, `two` when the second level contributes) at (u, v) or, anisotropic, along (du, dv); the
+// result is the fetch itself (isotropic) or the probes' in-order sum divided by n.
+struct TexProbe {
+    float u, v, du, dv, t;
+    int lo, hi, n;
+    bool two, aniso;
+};
+
+// Texture sampling with LOD from screen-space derivatives (ShaderBuiltinCuda.cuh:225-272),
+// up to the probe loop.
+__device__ __forceinline__ void tex_prepare(const DrawDev& d, float u, float v, float dudx, float dvdx, float dudy,
+                                            float dvdy, TexProbe& p) {
     u = finite_or_zero(u); v = finite_or_zero(v);
     dudx = finite_or_zero(dudx); dvdx = finite_or_zero(dvdx);
     dudy = finite_or_zero(dudy); dvdy = finite_or_zero(dvdy);
-    const TexState st = tex_state(d);
-    if (st.filter == 0) {
-        tex_bilinear(tex_level(d, 0), st, u, v, out);
+    p.u = u; p.v = v; p.du = 0.0f; p.dv = 0.0f;
+    p.n = 1;
+    p.aniso = false;
+    if (d.sampler.filter == 0) {  // nearest from level 0
+        p.lo = p.hi = 0;
+        p.t = 0.0f;
+        p.two = false;
         return;
     }
     float tw = (float)d.tex_w, th = (float)d.tex_h;
@@ -725,8 +739,6 @@ __device__ __forceinline__ void tex_sample(const DrawDev& d, float u, float v, f
     float ly2 = yu * yu + yv * yv;
     const bool aniso = d.sampler.max_aniso > 1;
     float lam;
-    int n = 1;
-    float du = 0.0f, dv = 0.0f;
     if (!aniso) {
         lam = 0.5f * log2_series(fmaxf(lx2, ly2)) + d.sampler.lod_bias;
     } else {
@@ -736,31 +748,57 @@ __device__ __forceinline__ void tex_sample(const DrawDev& d, float u, float v, f
         float amax = (float)d.sampler.max_aniso;
         float ratio = pmin > 0.0f ? pmax / pmin : amax;
         ratio = fminf(ratio, amax);
-        n = (int)ceilf(ratio);
+        int n = (int)ceilf(ratio);
         if (n < 1) n = 1;
+        p.n = n;
+        p.aniso = true;
         lam = log2_series(pmax / (float)n) + d.sampler.lod_bias;
-        du = major_x ? dudx : dudy;
-        dv = major_x ? dvdx : dvdy;
+        p.du = major_x ? dudx : dudy;
+        p.dv = major_x ? dvdx : dvdy;
     }
     const LodPick lp = pick_lod(d, lam);
-    const TexLevel L0 = tex_level(d, lp.lo), L1 = tex_level(d, lp.hi);
-    const bool two = !(lp.hi == lp.lo || lp.t == 0.0f);
-    if (!aniso) {
-        tex_trilinear2(L0, L1, st, two, lp.t, u, v, out);
+    p.lo = lp.lo;
+    p.hi = lp.hi;
+    p.t = lp.t;
+    p.two = !(lp.hi == lp.lo || lp.t == 0.0f);
+}
+
+// Probe i of a prepared lookup.
+__device__ __forceinline__ void tex_probe(const DrawDev& d, const TexProbe& p, int i, float out[4]) {
+    const TexState st = tex_state(d);
+    const TexLevel L0 = tex_level(d, p.lo), L1 = tex_level(d, p.hi);
+    float u = p.u, v = p.v;
+    if (p.aniso) {
+        const float t = (float)(i + 1) / (float)(p.n + 1) - 0.5f;
+        u = u + p.du * t;
+        v = v + p.dv * t;
+    }
+    tex_trilinear2(L0, L1, st, p.two, p.t, u, v, out);
+}
+
+// The lookup's result from its probes' in-order sum (isotropic: the single fetch).
+__device__ __forceinline__ void tex_finish(const TexProbe& p, const float acc[4], float out[4]) {
+    const float fn = (float)p.n;
+#pragma unroll
+    for (int k = 0; k < 4; k++) out[k] = p.aniso ? acc[k] / fn : acc[k];
+}
+
+__device__ __forceinline__ void tex_sample(const DrawDev& d, float u, float v, float dudx, float dvdx, float dudy,
+                                           float dvdy, float out[4]) {
+    TexProbe p;
+    tex_prepare(d, u, v, dudx, dvdx, dudy, dvdy, p);
+    if (!p.aniso) {
+        tex_probe(d, p, 0, out);
         return;
     }
     float acc[4] = {0.0f, 0.0f, 0.0f, 0.0f};
-    float inv = (float)(n + 1);
-    for (int i = 0; i < n; i++) {
-        float t = (float)(i + 1) / inv - 0.5f;
+    for (int i = 0; i < p.n; i++) {
         float cc[4];
-        tex_trilinear2(L0, L1, st, two, lp.t, u + du * t, v + dv * t, cc);
+        tex_probe(d, p, i, cc);
 #pragma unroll
         for (int k = 0; k < 4; k++) acc[k] = acc[k] + cc[k];
     }
-    float fn = (float)n;
-#pragma unroll
-    for (int k = 0; k < 4; k++) out[k] = acc[k] / fn;
+    tex_finish(p, acc, out);
 }
 
 // ------------------------------------------------------------------ interpolation + shading
@@ -867,6 +905,34 @@ __device__ __forceinline__ void shade_fragment_attrs(const PassConst& c, const D
     }
     col[0] = a[0]; col[1] = a[1]; col[2] = a[2];
     col[3] = d.attr_count >= 4 ? a[3] : 1.0f;
+}
+
+// As shade_fragment_attrs, with a textured fragment's lookup returned unevaluated in `tp` (the
+// result is then true and `col` is not set).
+__device__ __forceinline__ bool shade_prepare_attrs(const PassConst& c, const DrawDev& d, const ShadeGeom& s, int t,
+                                                    int sub, int px, int py, const float a0[4], const float a1[4],
+                                                    const float a2[4], float col[4], TexProbe& tp) {
+    if (d.shading == SHADE_PRIMID) {
+        col[0] = (float)(d.prim_base + t); col[1] = (float)sub; col[2] = 0.0f; col[3] = 1.0f;
+        return false;
+    }
+    int32_t qx = px * 256 + kShadeOffset, qy = py * 256 + kShadeOffset;
+    float a[4];
+    interp_attr(s, d.attr_count, a0, a1, a2, qx, qy, a);
+    if (d.shading == SHADE_TEXTURED) {
+        float ah[4], av[4];  // horizontal and vertical quad partners
+        interp_attr(s, d.attr_count, a0, a1, a2, (px ^ 1) * 256 + kShadeOffset, qy, ah);
+        interp_attr(s, d.attr_count, a0, a1, a2, qx, (py ^ 1) * 256 + kShadeOffset, av);
+        float dudx = (px & 1) ? a[0] - ah[0] : ah[0] - a[0];
+        float dvdx = (px & 1) ? a[1] - ah[1] : ah[1] - a[1];
+        float dudy = (py & 1) ? a[0] - av[0] : av[0] - a[0];
+        float dvdy = (py & 1) ? a[1] - av[1] : av[1] - a[1];
+        tex_prepare(d, a[0], a[1], dudx, dvdx, dudy, dvdy, tp);
+        return true;
+    }
+    col[0] = a[0]; col[1] = a[1]; col[2] = a[2];
+    col[3] = d.attr_count >= 4 ? a[3] : 1.0f;
+    return false;
 }
 
 __device__ __forceinline__ float blend_factor(int f, int ch, const float* src, const float* dst) {
