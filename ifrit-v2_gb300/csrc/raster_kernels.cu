@@ -952,6 +952,46 @@ __global__ void __launch_bounds__(TS * TS, 1024 / (TS * TS)) raster_kernel(PassA
 }
 
 // ---------------------------------------------------------------------------- shade stage
+// Interpolation set-up of an unclipped fill-mode triangle straight from its record, in registers:
+// the same values as sub_from_record + shade_geom_from (edges from the snapped vertices, stored
+// 1/w, the vertex order permutation of an oriented triangle).  plane = (z0, dz/dx, dz/dy, X0 bits),
+// plane_y = Y0.
+__device__ __forceinline__ void shade_geom_record(const TriRecord* rp, const int4 q1, ShadeGeom& g, float4& plane,
+                                                  int& plane_y) {
+    const int4 q0 = __ldg(reinterpret_cast<const int4*>(rp));
+    const float4 q2 = __ldg(reinterpret_cast<const float4*>(rp) + 2);
+    const float4 q3 = __ldg(reinterpret_cast<const float4*>(rp) + 3);
+    const int32_t X[3] = {q0.x, q0.z, q1.x}, Y[3] = {q0.y, q0.w, q1.y};
+    const bool swapped = (q1.z & REC_SWAPPED) != 0;
+#pragma unroll
+    for (int i = 0; i < 3; i++) {
+        const int j = (i + 1) % 3, k = (i + 2) % 3;
+        g.A[i] = Y[j] - Y[k];
+        g.B[i] = X[k] - X[j];
+        g.C[i] = (int64_t)(Y[k] - Y[j]) * X[j] - (int64_t)(X[k] - X[j]) * Y[j];
+#pragma unroll
+        for (int m = 0; m < 3; m++) g.bary[i][m] = 0.0f;
+    }
+    g.iw[0] = q2.w; g.iw[1] = q3.x; g.iw[2] = q3.y;
+    g.bary[0][0] = 1.0f;
+    g.bary[1][swapped ? 2 : 1] = 1.0f;
+    g.bary[2][swapped ? 1 : 2] = 1.0f;
+    plane = make_float4(q2.x, q2.y, q2.z, __int_as_float(X[0]));
+    plane_y = Y[0];
+}
+
+// Every other entry (clipped fan triangles, LINE / POINT parts): the general set-up, out of line so
+// that its arrays stay out of the shading loop's frame.
+static __device__ __noinline__ void shade_geom_general(const PassConst& c, const DrawDev& d, const TriRecord* records,
+                                                       int g, int t, int sub, ShadeGeom* geo, float4* plane,
+                                                       int* plane_y) {
+    SubTri st;
+    setup_entry_sub(c, d, records, g, t, sub, st);
+    shade_geom_from(st, *geo);
+    *plane = make_float4(st.z[0], st.dzdx, st.dzdy, __int_as_float(st.X[0]));
+    *plane_y = st.Y[0];
+}
+
 // One tile, one thread per pixel.  Each pixel lists its distinct visible entries in sample
 // order; the warp shades list slot i of all its lanes together (set-up straight from the
 // binner's record, quad derivatives, texture filtering), then the samples are resolved on chip
@@ -1044,14 +1084,26 @@ __device__ __forceinline__ void shade_tile(const PassArgs& a, const ViewArgs& v,
             tile_pixel<TS>(part * 32 + owner, olx, oly);
             const int opx = tx * TS + olx, opy = ty * TS + oly;
             const int g = it.x >> 3, sub = it.x & 7;
-            di = record_draw(a, g);
+            const TriRecord* rp = a.records + g;
+            const int4 q1 = __ldg(reinterpret_cast<const int4*>(rp) + 1);  // X2, Y2, flags, draw
+            di = q1.w;
             const DrawDev& d = a.draws[di];
             const int t = g - __ldg(a.draw_start + di);
-            SubTri st;
-            const bool from_record = setup_entry_sub(v.c, d, a.records, g, t, sub, st) && sub == 0 &&
-                                     (__ldg(&a.records[g].flags) & REC_VALID);
+            const bool from_record = sub == 0 && (q1.z & REC_VALID);
             ShadeGeom geo;
-            shade_geom_from(st, geo);
+            float4 plane;
+            int plane_y;
+            if (from_record && d.polygon_mode == POLY_FILL) {
+                shade_geom_record(rp, q1, geo, plane, plane_y);
+            } else {  // through memory on this rare path only
+                ShadeGeom tg;
+                float4 tpl;
+                int tpy;
+                shade_geom_general(v.c, d, a.records, g, t, sub, &tg, &tpl, &tpy);
+                geo = tg;
+                plane = tpl;
+                plane_y = tpy;
+            }
             float a0[4], a1[4], a2[4];
             if (from_record && a.attrs && d.shading != SHADE_PRIMID && d.attr_count > 0) {
                 const float4 q0 = __ldg(&a.attrs[g].a[0]), q1 = __ldg(&a.attrs[g].a[1]), q2 = __ldg(&a.attrs[g].a[2]);
@@ -1065,8 +1117,8 @@ __device__ __forceinline__ void shade_tile(const PassArgs& a, const ViewArgs& v,
                 for (int k = 0; k < 4; k++) a0[k] = a1[k] = a2[k] = 0.0f;
             }
             if (shade_prepare_attrs(v.c, d, geo, t, sub, opx, opy, a0, a1, a2, c, tp)) n = tp.n;
-            splane[slot][wbase + owner] = make_float4(st.z[0], st.dzdx, st.dzdy, __int_as_float(st.X[0]));
-            splane_y[slot][wbase + owner] = st.Y[0];
+            splane[slot][wbase + owner] = plane;
+            splane_y[slot][wbase + owner] = plane_y;
         }
         // The round's texture probes are spread over the lanes (anisotropic lookups take 1 to
         // max_aniso probes each); every item then adds its probes' results in probe order.
