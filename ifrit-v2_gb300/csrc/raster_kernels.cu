@@ -648,7 +648,9 @@ __device__ __forceinline__ bool raster_entry(const PassArgs& a, const PassConst&
         o.small = xmx - xmn < kSmallSpan && ymx - ymn < kSmallSpan;
     } else {
         SubTri s;
-        if (!setup_raster_entry(a, c, e, &s, &di)) return false;
+        int sdi;
+        if (!setup_raster_entry(a, c, e, &s, &sdi)) return false;
+        di = sdi;
 #pragma unroll
         for (int i = 0; i < 3; i++) { X[i] = s.X[i]; Y[i] = s.Y[i]; }
         o.z0 = s.z[0]; o.dzdx = s.dzdx; o.dzdy = s.dzdy;
@@ -1201,7 +1203,9 @@ __device__ __forceinline__ void shade_tile(const PassArgs& a, const ViewArgs& v,
                 c[0] = q.x; c[1] = q.y; c[2] = q.z; c[3] = q.w;
             } else {  // more than U distinct primitives in one pixel: shade this one here
                 RecordPlane pl;
-                shade_uncached(a, v.c, ent[k], px, py, c, &pl);
+                float uc[4];  // through memory on this rare path only
+                shade_uncached(a, v.c, ent[k], px, py, uc, &pl);
+                c[0] = uc[0]; c[1] = uc[1]; c[2] = uc[2]; c[3] = uc[3];
                 dep[k] = sample_depth(pl.z0, pl.dzdx, pl.dzdy, pl.X0, pl.Y0, px * 256 + sample_x<S>(k),
                                       py * 256 + sample_y<S>(k));
             }
