@@ -552,7 +552,7 @@ __device__ __forceinline__ float log2_series(float x) {
 // ------------------------------------------------------------------ textures
 // Byte b -> float(b) exactly via the 2^23 bias trick (one logic op and one add, both full
 // rate), then the same scale the conversion instruction path would use.
-__device__ __forceinline__ float byte_to_float(uint32_t b) { return __uint_as_float(0x4B000000u | b) - 8388608.0f; }
+__device__ __forceinline__ float byte_to_float(uint32_t b) { return (float)b; }  // exact for b < 2^24
 
 __device__ __forceinline__ void unpack_rgba8(uint32_t t, float c[4]) {
     c[0] = byte_to_float(t & 255u) * kInv255;
