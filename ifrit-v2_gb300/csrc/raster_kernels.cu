@@ -155,38 +155,78 @@ __global__ void __launch_bounds__(256) bin_count_kernel(PassArgs a) {
 }
 
 // Scattering pass: same overlaps as the counting pass, read back from the records (clipped
-// triangles run the front end again).
+// triangles run the front end again).  Every list slot comes from an atomicAdd whose result the
+// store waits for, so a triangle over many tiles would serialise hundreds of round trips in one
+// thread: the tile ranges of unclipped triangles over more than kWarpTiles tiles are walked by the
+// whole warp instead.
+constexpr int kWarpTiles = 4;
+
 __global__ void __launch_bounds__(256) bin_scatter_kernel(PassArgs a) {
-    int g = blockIdx.x * blockDim.x + threadIdx.x;
-    if (g >= a.total_tris) return;
-    if (a.status[ST_OVERFLOW]) return;
-    const int flags = __ldg(&a.records[g].flags);
-    if (!(flags & (REC_VALID | REC_CLIPPED))) return;
-    const int di = record_draw(a, g);
-    const DrawDev& d = a.draws[di];
-    const ViewArgs& v = a.views[d.view];
-    if (d.polygon_mode != POLY_FILL) {
-        SubTri tri;
-        tri_from_mode_record(a.records + g, tri);
-        for (int sub = 0; sub < 6; sub++) {
-            SubTri s;
-            if (mode_sub(v.c, d.polygon_mode, tri, sub, s)) bin_sub(a, v, d, s, ((uint32_t)g << 3) | (uint32_t)sub, true);
+    const int g = blockIdx.x * blockDim.x + threadIdx.x;
+    const int lane = threadIdx.x & 31;
+    bool big = false;
+    int tx0 = 0, tx1 = -1, ty0 = 0, ty1 = -1, tbase = 0, tiles_x = 0;
+    if (g < a.total_tris && !a.status[ST_OVERFLOW]) {
+        const int flags = __ldg(&a.records[g].flags);
+        if (flags & (REC_VALID | REC_CLIPPED)) {
+            const int di = record_draw(a, g);
+            const DrawDev& d = a.draws[di];
+            const ViewArgs& v = a.views[d.view];
+            if (d.polygon_mode != POLY_FILL) {
+                SubTri tri;
+                tri_from_mode_record(a.records + g, tri);
+                for (int sub = 0; sub < 6; sub++) {
+                    SubTri s;
+                    if (mode_sub(v.c, d.polygon_mode, tri, sub, s))
+                        bin_sub(a, v, d, s, ((uint32_t)g << 3) | (uint32_t)sub, true);
+                }
+            } else if (flags & REC_VALID) {
+                SubTri s;
+                if (sub_from_record(v.c, a.records + g, s) && scissor_clamp(d, s)) {
+                    const int sh = v.c.tile_shift;
+                    tx0 = s.px0 >> sh; tx1 = s.px1 >> sh;
+                    ty0 = s.py0 >> sh; ty1 = s.py1 >> sh;
+                    tbase = v.tile_start;
+                    tiles_x = v.c.tiles_x;
+                    big = (tx1 - tx0 + 1) * (ty1 - ty0 + 1) > kWarpTiles;
+                    if (!big) {
+                        for (int ty = ty0; ty <= ty1; ty++)
+                            for (int tx = tx0; tx <= tx1; tx++) {
+                                const uint32_t pos = atomicAdd(a.tile_cursor + tbase + ty * tiles_x + tx, 1u);
+                                if (pos < a.pair_capacity) a.pairs[pos] = (uint32_t)g << 3;
+                            }
+                    }
+                }
+            } else {
+                const int t = g - __ldg(a.draw_start + di);
+                CVert poly[kMaxPoly];
+                bool inside, rejected;
+                if (fetch_triangle(v.c, d, t, poly, inside, rejected)) {
+                    const int n = clip_polygon(v.c, poly);
+                    for (int i = 1; i + 1 < n; i++) {
+                        SubTri s;
+                        if (setup_sub(v.c, d, poly[0], poly[i], poly[i + 1], s))
+                            bin_sub(a, v, d, s, ((uint32_t)g << 3) | (uint32_t)(i - 1), true);
+                    }
+                }
+            }
         }
-        return;
     }
-    if (flags & REC_VALID) {
-        SubTri s;
-        if (sub_from_record(v.c, a.records + g, s)) bin_sub(a, v, d, s, (uint32_t)g << 3, true);
-        return;
-    }
-    int t = g - __ldg(a.draw_start + di);
-    CVert poly[kMaxPoly];
-    bool inside, rejected;
-    if (!fetch_triangle(v.c, d, t, poly, inside, rejected)) return;
-    int n = clip_polygon(v.c, poly);
-    for (int i = 1; i + 1 < n; i++) {
-        SubTri s;
-        if (setup_sub(v.c, d, poly[0], poly[i], poly[i + 1], s)) bin_sub(a, v, d, s, ((uint32_t)g << 3) | (uint32_t)(i - 1), true);
+    // the warp walks the large triangles' tile ranges one triangle at a time
+    unsigned m = __ballot_sync(0xffffffffu, big);
+    while (m) {
+        const int src = __ffs(m) - 1;
+        m &= m - 1;
+        const int sx0 = __shfl_sync(0xffffffffu, tx0, src), sx1 = __shfl_sync(0xffffffffu, tx1, src);
+        const int sy0 = __shfl_sync(0xffffffffu, ty0, src), sy1 = __shfl_sync(0xffffffffu, ty1, src);
+        const int sbase = __shfl_sync(0xffffffffu, tbase, src), stx = __shfl_sync(0xffffffffu, tiles_x, src);
+        const uint32_t entry = (uint32_t)(g - lane + src) << 3;
+        const int w = sx1 - sx0 + 1, n = w * (sy1 - sy0 + 1);
+        for (int i = lane; i < n; i += 32) {
+            const int ty = sy0 + i / w, tx = sx0 + i % w;
+            const uint32_t pos = atomicAdd(a.tile_cursor + sbase + ty * stx + tx, 1u);
+            if (pos < a.pair_capacity) a.pairs[pos] = entry;
+        }
     }
 }
 
