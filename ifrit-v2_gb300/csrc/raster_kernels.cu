@@ -139,19 +139,66 @@ __device__ __forceinline__ void front_end(const PassArgs& a, int g, int di, cons
     }
 }
 
+// Tile range of a (sub-)triangle over more than kWarpTiles tiles, left for the whole warp.
+constexpr int kWarpTiles = 4;
+struct WarpTiles {
+    bool big;
+    int tx0, tx1, ty0, ty1, tbase, tiles_x;
+};
+
 struct CountEmit {
     const PassArgs& a;
+    WarpTiles& w;
     __device__ void operator()(const ViewArgs& v, const DrawDev& d, const SubTri& s, uint32_t entry) const {
+        SubTri c = s;
+        if (!w.big && scissor_clamp(d, c)) {
+            const int sh = v.c.tile_shift;
+            const int tx0 = c.px0 >> sh, tx1 = c.px1 >> sh, ty0 = c.py0 >> sh, ty1 = c.py1 >> sh;
+            if ((tx1 - tx0 + 1) * (ty1 - ty0 + 1) > kWarpTiles) {
+                w.big = true;
+                w.tx0 = tx0; w.tx1 = tx1; w.ty0 = ty0; w.ty1 = ty1;
+                w.tbase = v.tile_start;
+                w.tiles_x = v.c.tiles_x;
+                return;
+            }
+        }
         bin_sub(a, v, d, s, entry, false);
     }
 };
+
+// The warp adds the counts (or, scattering, takes the list slots) of its lanes' large tile ranges,
+// one range at a time.
+__device__ __forceinline__ void warp_tiles(const PassArgs& a, const WarpTiles& w, int g, bool scatter) {
+    const int lane = threadIdx.x & 31;
+    unsigned m = __ballot_sync(0xffffffffu, w.big);
+    while (m) {
+        const int src = __ffs(m) - 1;
+        m &= m - 1;
+        const int sx0 = __shfl_sync(0xffffffffu, w.tx0, src), sx1 = __shfl_sync(0xffffffffu, w.tx1, src);
+        const int sy0 = __shfl_sync(0xffffffffu, w.ty0, src), sy1 = __shfl_sync(0xffffffffu, w.ty1, src);
+        const int sbase = __shfl_sync(0xffffffffu, w.tbase, src), stx = __shfl_sync(0xffffffffu, w.tiles_x, src);
+        const uint32_t entry = (uint32_t)(g - lane + src) << 3;
+        const int wd = sx1 - sx0 + 1, n = wd * (sy1 - sy0 + 1);
+        for (int i = lane; i < n; i += 32) {
+            const int tile = sbase + (sy0 + i / wd) * stx + sx0 + i % wd;
+            if (scatter) {
+                const uint32_t pos = atomicAdd(a.tile_cursor + tile, 1u);
+                if (pos < a.pair_capacity) a.pairs[pos] = entry;
+            } else {
+                atomicAdd(a.tile_count + tile, 1u);
+            }
+        }
+    }
+}
 
 // Counting pass: full front end per triangle; unclipped triangles leave a compact record.
 __global__ void __launch_bounds__(256) bin_count_kernel(PassArgs a) {
     const int g = blockIdx.x * blockDim.x + threadIdx.x;
     const int di = find_draw_warp(a, min(g, a.total_tris - 1));
-    if (g >= a.total_tris) return;
-    front_end(a, g, di, CountEmit{a});
+    WarpTiles w;
+    w.big = false;
+    if (g < a.total_tris) front_end(a, g, di, CountEmit{a, w});
+    warp_tiles(a, w, g, false);
 }
 
 // Scattering pass: same overlaps as the counting pass, read back from the records (clipped
@@ -159,13 +206,10 @@ __global__ void __launch_bounds__(256) bin_count_kernel(PassArgs a) {
 // store waits for, so a triangle over many tiles would serialise hundreds of round trips in one
 // thread: the tile ranges of unclipped triangles over more than kWarpTiles tiles are walked by the
 // whole warp instead.
-constexpr int kWarpTiles = 4;
-
 __global__ void __launch_bounds__(256) bin_scatter_kernel(PassArgs a) {
     const int g = blockIdx.x * blockDim.x + threadIdx.x;
-    const int lane = threadIdx.x & 31;
-    bool big = false;
-    int tx0 = 0, tx1 = -1, ty0 = 0, ty1 = -1, tbase = 0, tiles_x = 0;
+    WarpTiles w;
+    w.big = false;
     if (g < a.total_tris && !a.status[ST_OVERFLOW]) {
         const int flags = __ldg(&a.records[g].flags);
         if (flags & (REC_VALID | REC_CLIPPED)) {
@@ -184,15 +228,15 @@ __global__ void __launch_bounds__(256) bin_scatter_kernel(PassArgs a) {
                 SubTri s;
                 if (sub_from_record(v.c, a.records + g, s) && scissor_clamp(d, s)) {
                     const int sh = v.c.tile_shift;
-                    tx0 = s.px0 >> sh; tx1 = s.px1 >> sh;
-                    ty0 = s.py0 >> sh; ty1 = s.py1 >> sh;
-                    tbase = v.tile_start;
-                    tiles_x = v.c.tiles_x;
-                    big = (tx1 - tx0 + 1) * (ty1 - ty0 + 1) > kWarpTiles;
-                    if (!big) {
-                        for (int ty = ty0; ty <= ty1; ty++)
-                            for (int tx = tx0; tx <= tx1; tx++) {
-                                const uint32_t pos = atomicAdd(a.tile_cursor + tbase + ty * tiles_x + tx, 1u);
+                    w.tx0 = s.px0 >> sh; w.tx1 = s.px1 >> sh;
+                    w.ty0 = s.py0 >> sh; w.ty1 = s.py1 >> sh;
+                    w.tbase = v.tile_start;
+                    w.tiles_x = v.c.tiles_x;
+                    w.big = (w.tx1 - w.tx0 + 1) * (w.ty1 - w.ty0 + 1) > kWarpTiles;
+                    if (!w.big) {
+                        for (int ty = w.ty0; ty <= w.ty1; ty++)
+                            for (int tx = w.tx0; tx <= w.tx1; tx++) {
+                                const uint32_t pos = atomicAdd(a.tile_cursor + w.tbase + ty * w.tiles_x + tx, 1u);
                                 if (pos < a.pair_capacity) a.pairs[pos] = (uint32_t)g << 3;
                             }
                     }
@@ -212,22 +256,7 @@ __global__ void __launch_bounds__(256) bin_scatter_kernel(PassArgs a) {
             }
         }
     }
-    // the warp walks the large triangles' tile ranges one triangle at a time
-    unsigned m = __ballot_sync(0xffffffffu, big);
-    while (m) {
-        const int src = __ffs(m) - 1;
-        m &= m - 1;
-        const int sx0 = __shfl_sync(0xffffffffu, tx0, src), sx1 = __shfl_sync(0xffffffffu, tx1, src);
-        const int sy0 = __shfl_sync(0xffffffffu, ty0, src), sy1 = __shfl_sync(0xffffffffu, ty1, src);
-        const int sbase = __shfl_sync(0xffffffffu, tbase, src), stx = __shfl_sync(0xffffffffu, tiles_x, src);
-        const uint32_t entry = (uint32_t)(g - lane + src) << 3;
-        const int w = sx1 - sx0 + 1, n = w * (sy1 - sy0 + 1);
-        for (int i = lane; i < n; i += 32) {
-            const int ty = sy0 + i / w, tx = sx0 + i % w;
-            const uint32_t pos = atomicAdd(a.tile_cursor + sbase + ty * stx + tx, 1u);
-            if (pos < a.pair_capacity) a.pairs[pos] = entry;
-        }
-    }
+    warp_tiles(a, w, g, true);
 }
 
 // List offsets: exclusive scan of the per-tile counts in three launches (per-CTA scans of
