@@ -331,6 +331,42 @@ __global__ void __launch_bounds__(kScanThreads) scan_blocks_kernel(PassArgs a, i
     }
 }
 
+// Up to kScanSingle tiles: the whole scan in one launch (each thread a run of consecutive tiles).
+constexpr int kScanSingle = 16 * kScanThreads;
+
+__global__ void __launch_bounds__(kScanThreads) scan_single_kernel(PassArgs a, int T) {
+    constexpr int R = kScanSingle / kScanThreads;
+    __shared__ uint32_t wsum[33];
+    const int per = (T + kScanThreads - 1) / kScanThreads;
+    const int b = min((int)threadIdx.x * per, T), e = min(b + per, T);
+    uint32_t c[R];  // the thread's run, all loads in flight together
+#pragma unroll
+    for (int i = 0; i < R; i++) c[i] = b + i < e ? a.tile_count[b + i] : 0u;
+    uint32_t sum = 0;
+#pragma unroll
+    for (int i = 0; i < R; i++) sum += c[i];
+    uint32_t total;
+    uint32_t run = block_exclusive_scan(sum, wsum, total);
+#pragma unroll
+    for (int i = 0; i < R; i++) {
+        if (b + i < e) {
+            a.tile_offset[b + i] = run;
+            a.tile_cursor[b + i] = run;
+            a.tile_count[b + i] = 0u;
+        }
+        run += c[i];
+    }
+    if (threadIdx.x == 0) {
+        a.tile_offset[T] = total;
+        a.status[ST_PAIRS] = total;
+        atomicMax(a.status + ST_MAX_PAIRS, total);
+        if (total > a.pair_capacity) {
+            a.status[ST_OVERFLOW] = 1u;
+            atomicOr(a.status + ST_STICKY, 1u);
+        }
+    }
+}
+
 __global__ void __launch_bounds__(kScanThreads) scan_apply_kernel(PassArgs a, int T) {
     const uint32_t add = a.block_sums[blockIdx.x];
     const int base = blockIdx.x * kScanTile + threadIdx.x * 4;
@@ -775,7 +811,7 @@ __device__ __forceinline__ void raster_depth(const ViewArgs& v, const KeyRule& r
             hi_word = rule.invert ? ~depth_order(z) : depth_order(z);
         }
         const unsigned long long kv = ((unsigned long long)hi_word << 32) | lo_word;
-        if (kv < kp[k]) atomicMin(kp + k, kv);
+        atomicMin(kp + k, kv);
     }
 }
 
@@ -1780,10 +1816,14 @@ cudaError_t launch_pass(const PassArgs& a, const LaunchPlan& plan, cudaStream_t 
         int blocks = (a.total_tris + 255) / 256;
         bin_count_kernel<<<blocks, 256, 0, stream>>>(a);
         if (ev) cudaEventRecord(ev[1], stream);
-        const int nb = (T + kScanTile - 1) / kScanTile;
-        scan_local_kernel<<<nb, kScanThreads, 0, stream>>>(a, T);
-        scan_blocks_kernel<<<1, kScanThreads, 0, stream>>>(a, T, nb);
-        scan_apply_kernel<<<nb, kScanThreads, 0, stream>>>(a, T);
+        if (T <= kScanSingle) {
+            scan_single_kernel<<<1, kScanThreads, 0, stream>>>(a, T);
+        } else {
+            const int nb = (T + kScanTile - 1) / kScanTile;
+            scan_local_kernel<<<nb, kScanThreads, 0, stream>>>(a, T);
+            scan_blocks_kernel<<<1, kScanThreads, 0, stream>>>(a, T, nb);
+            scan_apply_kernel<<<nb, kScanThreads, 0, stream>>>(a, T);
+        }
         if (ev) cudaEventRecord(ev[2], stream);
         bin_scatter_kernel<<<blocks, 256, 0, stream>>>(a);
         if (ev) cudaEventRecord(ev[3], stream);
