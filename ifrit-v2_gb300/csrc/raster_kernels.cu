@@ -661,8 +661,8 @@ struct TileRecords {
 // from the exact integer with a relative error below 2^-21 (three roundings), i.e. below 10^-5
 // columns where it matters (|t| <= TS + 2); rounding t -+ 2^-10 up / down keeps the bound
 // conservative without widening it by a column.  An edge with A == 0 empties the row when its
-// largest value is negative.  Row r's range is packed as lo | hi << 4 into bits 8(r mod 4) of
-// word r / 4; an empty row is 0x0f.
+// largest value is negative.  A record's rows are packed as lo | hi << 4 per row, row r in bits
+// 8(r mod 4) of word r / 4; an empty row is 0x0f.
 template <int TS>
 struct RowSpans {
     uint32_t w[TS / 4];
@@ -670,42 +670,46 @@ struct RowSpans {
     bool large;  // the record needs the 64-bit coverage test
 };
 
-template <int S, int TS>
-__device__ __forceinline__ void row_spans(const int32_t A[3], const int32_t B[3], const long long Et[3], int cx0,
-                                          int cx1, int ry0, int ry1, RowSpans<TS>& o) {
-    constexpr float kEps = 1.0f / 1024.0f;
+// What a row job needs of its record: the largest value of each edge over the pixel's sample
+// pattern at tile column 0, row 0 (exact), -1 / (256 A) (0 for A == 0), B, and the record's
+// clipped column range and first row.
+struct SpanEdges {
     long long base0[3];
     float rcp[3];
+    int32_t B[3];
+    int box;  // cx0 | cx1 << 4 | ry0 << 8
+};
+
+template <int S>
+__device__ __forceinline__ void span_edges(const int32_t A[3], const int32_t B[3], const long long Et[3], int cx0,
+                                           int cx1, int ry0, SpanEdges& o) {
 #pragma unroll
     for (int i = 0; i < 3; i++) {
         long long m = (long long)A[i] * sample_x<S>(0) + (long long)B[i] * sample_y<S>(0);
 #pragma unroll
         for (int k = 1; k < S; k++) m = max(m, (long long)A[i] * sample_x<S>(k) + (long long)B[i] * sample_y<S>(k));
-        base0[i] = Et[i] + m;
-        rcp[i] = A[i] != 0 ? -1.0f / (256.0f * (float)A[i]) : 0.0f;
+        o.base0[i] = Et[i] + m;
+        o.rcp[i] = A[i] != 0 ? -1.0f / (256.0f * (float)A[i]) : 0.0f;
+        o.B[i] = B[i];
     }
-    o.nspan = 0;
-    o.npix = 0;
-    uint32_t w[TS / 4] = {};
+    o.box = cx0 | (cx1 << 4) | (ry0 << 8);
+}
+
+// Span code of tile row r of a record (lo | hi << 4, or 0x0f when empty).
+template <int TS>
+__device__ __forceinline__ uint32_t span_code(const SpanEdges& q, int r) {
+    constexpr float kEps = 1.0f / 1024.0f;
+    int lo = q.box & 15, hi = (q.box >> 4) & 15;
+    bool empty = false;
 #pragma unroll
-    for (int r = 0; r < TS; r++) {
-        int lo = cx0, hi = cx1;
-        bool empty = r < ry0 || r > ry1;
-#pragma unroll
-        for (int i = 0; i < 3; i++) {
-            const long long b = base0[i] + (long long)B[i] * (256 * r);
-            const float t = fminf(fmaxf((float)b * rcp[i], -2.0f), (float)TS + 1.0f);
-            if (A[i] > 0) lo = max(lo, (int)ceilf(t - kEps));
-            else if (A[i] < 0) hi = min(hi, (int)floorf(t + kEps));
-            else empty |= b < 0;
-        }
-        empty |= lo > hi;
-        w[r / 4] |= (empty ? 0x0fu : (uint32_t)(lo | (hi << 4))) << ((r % 4) * 8);
-        o.nspan += empty ? 0 : 1;
-        o.npix += empty ? 0 : hi - lo + 1;
+    for (int i = 0; i < 3; i++) {
+        const long long b = q.base0[i] + (long long)q.B[i] * (256 * r);
+        const float t = fminf(fmaxf((float)b * q.rcp[i], -2.0f), (float)TS + 1.0f);
+        if (q.rcp[i] < 0.0f) lo = max(lo, (int)ceilf(t - kEps));        // A > 0
+        else if (q.rcp[i] > 0.0f) hi = min(hi, (int)floorf(t + kEps));  // A < 0
+        else empty |= b < 0;
     }
-#pragma unroll
-    for (int q = 0; q < TS / 4; q++) o.w[q] = w[q];
+    return empty || lo > hi ? 0x0fu : (uint32_t)(lo | (hi << 4));
 }
 
 // Raster set-up of one binned entry, clipped to the tile, in registers.
@@ -859,6 +863,15 @@ __device__ __forceinline__ void raster_tile(const PassArgs& a, const ViewArgs& v
 #pragma unroll
         for (int q = 0; q < TS / 4; q++) rs.w[q] = 0x0f0f0f0fu;
         bool in_stage = true;
+        SpanEdges se;  // the record's row-span inputs (rows = 0: no spans)
+        se.box = 0;
+#pragma unroll
+        for (int i = 0; i < 3; i++) {
+            se.base0[i] = 0;
+            se.rcp[i] = 0.0f;
+            se.B[i] = 0;
+        }
+        int rows = 0;
         if (tid < nb) {
             uint32_t e = __ldg(a.pairs + base + tid);
             RasterRec s;
@@ -878,10 +891,60 @@ __device__ __forceinline__ void raster_tile(const PassArgs& a, const ViewArgs& v
                 rec.X0[tid] = s.X0;
                 rec.Y0[tid] = s.Y0;
                 rec.meta[tid] = (s.small ? 0 : kLargeRecord) | (a.draws[di].scissor_count ? (di + 1) << 1 : 0);
-                row_spans<S, TS>(s.A, s.B, s.Et, s.x0 - tx0, s.x1 - tx0, s.y0 - ty0, s.y1 - ty0, rs);
+                span_edges<S>(s.A, s.B, s.Et, s.x0 - tx0, s.x1 - tx0, s.y0 - ty0, se);
+                rows = s.y1 - s.y0 + 1;
                 rs.large = !s.small;
             }
             rec.key[tid] = (int)e;
+        }
+        // Row spans of the warp's records: their (record, row) jobs, rows of one record consecutive,
+        // are spread over the lanes; each job's code goes to the record's bytes in the warp's
+        // row-code scratch, which aliases the span list (written only after the block scan below).
+        {
+            uint8_t* rcode = reinterpret_cast<uint8_t*>(rec.span) + wid * 32 * TS;
+            uint32_t* mine = reinterpret_cast<uint32_t*>(rcode + lane * TS);
+#pragma unroll
+            for (int q = 0; q < TS / 4; q++) mine[q] = 0x0f0f0f0fu;
+            int jincl = rows;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int q = __shfl_up_sync(0xffffffffu, jincl, o);
+                if (lane >= o) jincl += q;
+            }
+            const int J = __shfl_sync(0xffffffffu, jincl, 31), jpre = jincl - rows;
+            __syncwarp();
+            for (int c0 = 0; c0 < J; c0 += 32) {
+                const int j = c0 + lane;
+                int k = 0;  // the record of job j: the last lane whose first job is at or before j
+#pragma unroll
+                for (int step = 16; step > 0; step >>= 1)
+                    if (__shfl_sync(0xffffffffu, jpre, k + step) <= j) k += step;
+                SpanEdges q;
+#pragma unroll
+                for (int i = 0; i < 3; i++) {
+                    q.base0[i] = __shfl_sync(0xffffffffu, se.base0[i], k);
+                    q.rcp[i] = __shfl_sync(0xffffffffu, se.rcp[i], k);
+                    q.B[i] = __shfl_sync(0xffffffffu, se.B[i], k);
+                }
+                q.box = __shfl_sync(0xffffffffu, se.box, k);
+                const int kpre = __shfl_sync(0xffffffffu, jpre, k);
+                if (j < J) {
+                    const int r = ((q.box >> 8) & 15) + (j - kpre);
+                    rcode[k * TS + r] = (uint8_t)span_code<TS>(q, r);
+                }
+            }
+            __syncwarp();
+#pragma unroll
+            for (int q = 0; q < TS / 4; q++) {
+                const uint32_t w = mine[q];
+                rs.w[q] = w;
+#pragma unroll
+                for (int b = 0; b < 4; b++) {
+                    const uint32_t lo = (w >> (8 * b)) & 15u, hi = (w >> (8 * b + 4)) & 15u;
+                    rs.nspan += lo <= hi ? 1 : 0;
+                    rs.npix += lo <= hi ? (int)(hi - lo + 1) : 0;
+                }
+            }
         }
         // block-wide exclusive scan of (pixels | spans << 17) per record, small and large records
         // counted apart: the spans of large records (64-bit coverage tests) follow those of the
