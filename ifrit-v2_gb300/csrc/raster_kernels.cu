@@ -331,30 +331,58 @@ __global__ void __launch_bounds__(kScanThreads) scan_blocks_kernel(PassArgs a, i
     }
 }
 
-// Up to kScanSingle tiles: the whole scan in one launch (each thread a run of consecutive tiles).
-constexpr int kScanSingle = 16 * kScanThreads;
+// Up to kScanSingle tiles: the whole scan in one launch.  Warp w owns tiles [512 w, 512 w + 512),
+// read and written coalesced as 16 rows of 32 (tile 512 w + 32 i + lane in row i); rows are
+// scanned across the lanes in order, then the warp totals across the block.
+constexpr int kScanRows = 16;
+constexpr int kScanSingle = kScanRows * kScanThreads;
 
 __global__ void __launch_bounds__(kScanThreads) scan_single_kernel(PassArgs a, int T) {
-    constexpr int R = kScanSingle / kScanThreads;
     __shared__ uint32_t wsum[33];
-    const int per = (T + kScanThreads - 1) / kScanThreads;
-    const int b = min((int)threadIdx.x * per, T), e = min(b + per, T);
-    uint32_t c[R];  // the thread's run, all loads in flight together
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const int first = wid * 32 * kScanRows + lane;
+    uint32_t ex[kScanRows];
+    uint32_t run = 0;
 #pragma unroll
-    for (int i = 0; i < R; i++) c[i] = b + i < e ? a.tile_count[b + i] : 0u;
-    uint32_t sum = 0;
+    for (int i = 0; i < kScanRows; i++) {
+        const int t = first + 32 * i;
+        ex[i] = t < T ? a.tile_count[t] : 0u;
+    }
 #pragma unroll
-    for (int i = 0; i < R; i++) sum += c[i];
-    uint32_t total;
-    uint32_t run = block_exclusive_scan(sum, wsum, total);
+    for (int i = 0; i < kScanRows; i++) {
+        const uint32_t x = ex[i];
+        uint32_t incl = x;
 #pragma unroll
-    for (int i = 0; i < R; i++) {
-        if (b + i < e) {
-            a.tile_offset[b + i] = run;
-            a.tile_cursor[b + i] = run;
-            a.tile_count[b + i] = 0u;
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t q = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += q;
         }
-        run += c[i];
+        ex[i] = run + incl - x;
+        run += __shfl_sync(0xffffffffu, incl, 31);
+    }
+    if (lane == 0) wsum[wid] = run;
+    __syncthreads();
+    if (wid == 0) {
+        const uint32_t w = wsum[lane];
+        uint32_t wi = w;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t q = __shfl_up_sync(0xffffffffu, wi, o);
+            if (lane >= o) wi += q;
+        }
+        wsum[lane] = wi - w;
+        if (lane == 31) wsum[32] = wi;
+    }
+    __syncthreads();
+    const uint32_t add = wsum[wid], total = wsum[32];
+#pragma unroll
+    for (int i = 0; i < kScanRows; i++) {
+        const int t = first + 32 * i;
+        if (t < T) {
+            a.tile_offset[t] = add + ex[i];
+            a.tile_cursor[t] = add + ex[i];
+            a.tile_count[t] = 0u;
+        }
     }
     if (threadIdx.x == 0) {
         a.tile_offset[T] = total;
