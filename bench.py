@@ -615,7 +615,9 @@ def run_ours_c5(args):
             "e2e": {"value": shaded / statistics.mean(e2e), "unit": "samples/s",
                     "h2d_bytes_per_step": int(sc["vertices"].nbytes + sc["indices"].nbytes),
                     "d2h_bytes_per_step": int(out.nbytes), "ms_per_step": 1000.0 * statistics.mean(e2e)},
-            "gpu_launches": 4 * args.steps, "clocks": clk}
+            # count, scan, scatter, raster, shade, ordered (one launch group; 4K = 32,400 tiles,
+            # one scan launch)
+            "gpu_launches": 6 * args.steps, "clocks": clk}
     r.close()
     # CPU oracle on a bounded sample: the first two instances of the pass at full resolution
     from oracle import oracle as O

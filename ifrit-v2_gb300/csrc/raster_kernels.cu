@@ -331,10 +331,10 @@ __global__ void __launch_bounds__(kScanThreads) scan_blocks_kernel(PassArgs a, i
     }
 }
 
-// Up to kScanSingle tiles: the whole scan in one launch.  Warp w owns tiles [512 w, 512 w + 512),
-// read and written coalesced as 16 rows of 32 (tile 512 w + 32 i + lane in row i); rows are
+// Up to kScanSingle tiles: the whole scan in one launch.  Warp w owns tiles [1024 w, 1024 w + 1024),
+// read and written coalesced as 32 rows of 32 (tile 1024 w + 32 i + lane in row i); rows are
 // scanned across the lanes in order, then the warp totals across the block.
-constexpr int kScanRows = 16;
+constexpr int kScanRows = 32;
 constexpr int kScanSingle = kScanRows * kScanThreads;
 
 __global__ void __launch_bounds__(kScanThreads) scan_single_kernel(PassArgs a, int T) {
