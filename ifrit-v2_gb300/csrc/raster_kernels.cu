@@ -74,7 +74,7 @@ __device__ __forceinline__ void front_end(const PassArgs& a, int g, int di, cons
     const DrawDev& d = a.draws[di];
     const ViewArgs& v = a.views[d.view];
     int t = g - __ldg(a.draw_start + di);
-    CVert poly[kMaxPoly];
+    CVert poly[3];  // registers: only the rare clipping path below goes through memory
     bool inside, rejected;
     TriRecord* rec = a.records + g;
     if (!fetch_triangle(v.c, d, t, poly, inside, rejected)) {
@@ -132,10 +132,14 @@ __device__ __forceinline__ void front_end(const PassArgs& a, int g, int di, cons
     }
     rec->flags = REC_CLIPPED;
     rec->draw = di;
-    int n = clip_polygon(v.c, poly);
+    CVert clip[kMaxPoly];
+    clip[0] = poly[0];
+    clip[1] = poly[1];
+    clip[2] = poly[2];
+    int n = clip_polygon(v.c, clip);
     for (int i = 1; i + 1 < n; i++) {
         SubTri s;
-        if (setup_sub(v.c, d, poly[0], poly[i], poly[i + 1], s)) emit(v, d, s, ((uint32_t)g << 3) | (uint32_t)(i - 1));
+        if (setup_sub(v.c, d, clip[0], clip[i], clip[i + 1], s)) emit(v, d, s, ((uint32_t)g << 3) | (uint32_t)(i - 1));
     }
 }
 
