@@ -417,3 +417,23 @@ def test_atomic_visibility_path_matches_oracle(case):
     assert_parity(gpu, ref)
     assert (gpu["vis"] >= 0).any()
     r.close()
+
+
+@pytest.mark.parametrize("S", [4, 16])
+def test_dense_large_triangles_defer_span_batches(S):
+    """Hundreds of large overlapping triangles per tile: a batch of up to 256 records then holds
+    more row spans than one batch takes (2,048), so records are deferred to further batches, and
+    most records need the 64-bit coverage test (vertex spans of 32 pixels and more)."""
+    rng = np.random.default_rng(77)
+    n = 700
+    c = rng.uniform(-0.6, 0.6, (n, 1, 2))
+    p = c + rng.normal(size=(n, 3, 2)) * rng.uniform(0.3, 1.2, (n, 1, 1))
+    z = rng.uniform(-6.0, -2.0, (n, 1, 1)) + rng.normal(size=(n, 3, 1)) * 0.2
+    pos = np.concatenate([p * -z, z], 2).reshape(-1, 3)
+    col = rng.uniform(0, 1, (3 * n, 3))
+    v = np.concatenate([pos, col], 1).astype(np.float32)
+    f = np.arange(3 * n, dtype=np.int32).reshape(-1, 3)
+    mvp = scenes.perspective(60.0, 1.0, 0.1, 100.0).astype(np.float32)
+    gpu, ref, _ = render_both(v, f, mvp, 96, 96, S=S, cull=ig.CULL_NONE, depth_func=ig.LESS)
+    assert_parity(gpu, ref)
+    assert (gpu["vis"] >= 0).mean() > 0.9
