@@ -1194,14 +1194,20 @@ static __device__ __noinline__ void shade_geom_general(const PassConst& c, const
     *plane_y = st.Y[0];
 }
 
+// Shade stage CTAs: warps are independent (each pulls its own 32-pixel tasks); a CTA only holds the
+// warps' shared-memory slices.
+constexpr int kShadeThreads = 256;
+constexpr int kShadeBlocks = 4;
+
 // One tile, one thread per pixel.  Each pixel lists its distinct visible entries in sample
 // order; the warp shades list slot i of all its lanes together (set-up straight from the
 // binner's record, quad derivatives, texture filtering), then the samples are resolved on chip
 // and depth, visibility and the resolved colour stored once.
 template <int S, int TS>
 __device__ __forceinline__ void shade_tile(const PassArgs& a, const ViewArgs& v, int gtile, int part,
-                                           float4 (*scol)[TS * TS], float4 (*splane)[TS * TS], int (*splane_y)[TS * TS],
-                                           int2* witems, float4* wres, bool keep_samples) {
+                                           float4 (*scol)[kShadeThreads], float4 (*splane)[kShadeThreads],
+                                           int (*splane_y)[kShadeThreads], int2* witems, float4* wres,
+                                           bool keep_samples) {
     const int ltile = gtile - v.tile_start;
     const int tx = ltile % v.c.tiles_x, ty = ltile / v.c.tiles_x;
     const int tid = threadIdx.x;
@@ -1444,15 +1450,15 @@ __device__ __forceinline__ void shade_tile(const PassArgs& a, const ViewArgs& v,
 // queue on its own, so a warp that finishes early starts its next task instead of waiting at a
 // tile barrier.  View arguments are read through L1 from the descriptor array.
 template <int S, int TS>
-__global__ void __launch_bounds__(TS * TS, 1024 / (TS * TS)) shade_kernel(PassArgs a, GroupArgs g) {
-    constexpr int NT = TS * TS;
+__global__ void __launch_bounds__(kShadeThreads, kShadeBlocks) shade_kernel(PassArgs a, GroupArgs g) {
+    constexpr int NT = TS * TS, CT = kShadeThreads;
     constexpr int kTasksPerTile = NT / 32;
     constexpr int U = S < 4 ? S : 4;
-    __shared__ float4 scol[4][NT];    // colours of each thread's (up to 4) distinct entries
-    __shared__ float4 splane[4][NT];  // their depth planes: z0, dz/dx, dz/dy, X0 (bits)
-    __shared__ int splane_y[4][NT];   // and Y0
-    __shared__ int2 witems[NT / 32 * 32 * U];  // per warp: compacted (entry, lane | slot << 5) items
-    __shared__ float4 sres[NT];                // per warp: results of one round of texture probes
+    __shared__ float4 scol[4][CT];    // colours of each thread's (up to 4) distinct entries
+    __shared__ float4 splane[4][CT];  // their depth planes: z0, dz/dx, dz/dy, X0 (bits)
+    __shared__ int splane_y[4][CT];   // and Y0
+    __shared__ int2 witems[CT / 32 * 32 * U];  // per warp: compacted (entry, lane | slot << 5) items
+    __shared__ float4 sres[CT];                // per warp: results of one round of texture probes
     const int lane = threadIdx.x & 31;
     const int ntasks = (g.tile_end - g.tile_begin) * kTasksPerTile;
     for (;;) {
@@ -1785,7 +1791,7 @@ cudaError_t launch_deferred(const PassArgs& a, const GroupArgs& g, int ctas, cud
     cudaError_t e = configure_deferred<S, TS>();
     if (e != cudaSuccess) return e;
     if (!shade) raster_kernel<S, TS><<<ctas, TS * TS, raster_smem_bytes<S, TS>(), stream>>>(a, g);
-    else shade_kernel<S, TS><<<ctas, TS * TS, 0, stream>>>(a, g);
+    else shade_kernel<S, TS><<<ctas, kShadeThreads, 0, stream>>>(a, g);
     return cudaSuccess;
 }
 
@@ -1843,7 +1849,7 @@ template <int S, int TS>
 int deferred_occupancy(int stage) {
     configure_deferred<S, TS>();
     return stage == 0 ? occupancy_of(raster_kernel<S, TS>, TS * TS, raster_smem_bytes<S, TS>())
-                      : occupancy_of(shade_kernel<S, TS>, TS * TS, 0);
+                      : occupancy_of(shade_kernel<S, TS>, kShadeThreads, 0);
 }
 
 template <int S>
