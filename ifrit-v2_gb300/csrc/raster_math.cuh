@@ -125,7 +125,8 @@ struct __align__(16) TriRecord {
 };
 enum { REC_VALID = 1, REC_SWAPPED = 2, REC_CLIPPED = 4 };
 
-__device__ __forceinline__ int64_t floordiv256(int64_t a) { return a >= 0 ? a / 256 : -((-a + 255) / 256); }
+// floor(a / 256): an arithmetic right shift (two's complement)
+__device__ __forceinline__ int64_t floordiv256(int64_t a) { return a >> 8; }
 __device__ __forceinline__ int64_t ceildiv256(int64_t a) { return -floordiv256(-a); }
 
 __device__ __forceinline__ void xform(const float* m, const float* v, float out[4]) {
@@ -287,6 +288,7 @@ __device__ __forceinline__ bool fetch_triangle(const PassConst& c, const DrawDev
 #pragma unroll
         for (int k = 0; k < 3; k++) poly[i].b[k] = (k == i) ? 1.0f : 0.0f;
     }
+#pragma unroll
     for (int pl = 0; pl < 7; pl++) {
         int nin = 0;
 #pragma unroll
