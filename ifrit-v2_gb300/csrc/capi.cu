@@ -206,6 +206,7 @@ struct IfritGbRenderer {
     std::vector<float> scissors;  // (x, y, w, h) per rectangle, at most 16
     // device state
     DevMem d_vertices, d_indices, d_color, d_depth, d_vis, d_entries, d_sample_colors, d_keys;
+    DevMem d_mesh_meta, d_mesh_vertices, d_mesh_indices;  // compacted mesh-stage outputs
     const void* up_vb_key = nullptr;
     uint64_t up_vb_gen = 0;
     const void* up_ib_key = nullptr;
@@ -987,7 +988,7 @@ IFTR_API int iftrDestroyInstance(IfritGbRenderer* h) {
     if (h->inited) {
         cudaStreamSynchronize(h->stream);
         for (DevMem* m : {&h->d_vertices, &h->d_indices, &h->d_color, &h->d_depth, &h->d_vis, &h->d_entries,
-                          &h->d_sample_colors, &h->d_keys})
+                          &h->d_sample_colors, &h->d_keys, &h->d_mesh_meta, &h->d_mesh_vertices, &h->d_mesh_indices})
             m->release();
         h->pass.release();
         h->batch.drop_graph();
@@ -1132,12 +1133,12 @@ IFTR_API int iftrFinish(IfritGbRenderer* h) {
     return check_pending(h);
 }
 
-IFTR_API int iftrDrawLegacy(IfritGbRenderer* h, int numIndices, int clear) {
-    if (!h) return IFTR_ERR_INVALID_ARG;
-    if (h->in_pass) return iftrPassDraw(h, 0, numIndices);
+// Renders one prepared pass synchronously; a pass whose tile lists overflowed is drawn again with
+// the grown scratch (clearing passes only).
+int draw_sync(IfritGbRenderer* h, std::vector<DrawDev>& draws, int clear) {
     h->stats.retries = 0;
     for (int attempt = 0; attempt < 4; attempt++) {
-        int rc = enqueue_draw(h, numIndices, clear);
+        int rc = enqueue_pass(h, draws, clear);
         if (rc) return rc;
         rc = check_pending(h);
         if (rc == IFTR_ERR_OVERFLOW) {
@@ -1149,6 +1150,60 @@ IFTR_API int iftrDrawLegacy(IfritGbRenderer* h, int numIndices, int clear) {
         return copy_back_host_images(h);
     }
     return IFTR_ERR_OVERFLOW;
+}
+
+IFTR_API int iftrDrawLegacy(IfritGbRenderer* h, int numIndices, int clear) {
+    if (!h) return IFTR_ERR_INVALID_ARG;
+    if (h->in_pass) return iftrPassDraw(h, 0, numIndices);
+    int rc = ensure_init(h);
+    if (rc) return rc;
+    std::vector<DrawDev> one(1);
+    rc = prepare_draw(h, 0, numIndices, one[0]);
+    if (rc) return rc;
+    return draw_sync(h, one, clear);
+}
+
+IFTR_API int iftrDrawMeshOutputs(IfritGbRenderer* h, int numGroups, const float* positions, const float* attributes,
+                                 int attrCount, const int* indices, const int* numVertices, const int* numIndices,
+                                 int maxVertices, int maxIndices, int clear) {
+    if (!h || numGroups < 0 || maxVertices <= 0 || maxIndices <= 0 || attrCount < 0 || attrCount > 4 ||
+        (numGroups > 0 && (!positions || !indices || !numVertices || !numIndices)) || (attrCount > 0 && !attributes))
+        return IFTR_ERR_INVALID_ARG;
+    if (h->in_pass) return IFTR_ERR_STATE;
+    int rc = ensure_init(h);
+    if (rc) return rc;
+    long long totals[3] = {0, 0, 0};
+    if (numGroups > 0) {
+        const size_t meta = ((size_t)2 * numGroups * sizeof(int) + 15) / 16 * 16;
+        IFTR_CUDA(h, h->d_mesh_meta.reserve(meta + 3 * sizeof(long long)));
+        int* off_v = h->d_mesh_meta.as<int>();
+        int* off_i = off_v + numGroups;
+        long long* d_totals = reinterpret_cast<long long*>(h->d_mesh_meta.as<uint8_t>() + meta);
+        IFTR_CUDA(h, ifr::launch_mesh_offsets(numVertices, numIndices, numGroups, maxVertices, maxIndices, off_v, off_i,
+                                              d_totals, h->stream));
+        IFTR_CUDA(h, cudaMemcpyAsync(totals, d_totals, sizeof(totals), cudaMemcpyDeviceToHost, h->stream));
+        IFTR_CUDA(h, cudaStreamSynchronize(h->stream));
+        if (totals[2] || totals[0] > (1 << 27) || totals[1] > (1LL << 30)) return IFTR_ERR_INVALID_ARG;
+        IFTR_CUDA(h, h->d_mesh_vertices.reserve(std::max<size_t>(16, (size_t)totals[0] * 8 * sizeof(float))));
+        IFTR_CUDA(h, h->d_mesh_indices.reserve(std::max<size_t>(16, (size_t)totals[1] * sizeof(int))));
+        IFTR_CUDA(h, ifr::launch_mesh_compact(positions, attrCount > 0 ? attributes : nullptr, indices, numVertices,
+                                              numIndices, off_v, off_i, numGroups, maxVertices, maxIndices,
+                                              h->d_mesh_vertices.as<float>(), h->d_mesh_indices.as<int>(), h->stream));
+    }
+    std::vector<DrawDev> one(1);
+    DrawDev& d = one[0];
+    std::memset(&d, 0, sizeof(d));
+    d.vertices = h->d_mesh_vertices.as<float>();
+    d.stride = 8;
+    d.num_vertices = (int)totals[0];
+    d.attr_offset = 4;
+    d.attr_count = attrCount;
+    d.indices = h->d_mesh_indices.as<int>();
+    d.num_triangles = (int)(totals[1] / 3);
+    fill_state(h, d);
+    d.clip_input = 1;
+    if (d.shading == IFTR_FS_TEXTURED && (!d.texels || d.tex_levels <= 0)) return IFTR_ERR_STATE;
+    return draw_sync(h, one, clear);
 }
 
 IFTR_API int iftrBeginPass(IfritGbRenderer* h, int clear) {

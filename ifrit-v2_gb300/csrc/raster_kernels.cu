@@ -1743,6 +1743,99 @@ __global__ void __launch_bounds__(kFwdThreads) forward_kernel(PassArgs a, GroupA
         forward_tile<S>(a, sv, s_tile, rec, scol, list, frags, after_raster != 0);
 }
 
+// ---------------------------------------------------------------------------- mesh-stage outputs
+// Compaction of per-work-group mesh (or geometry) stage outputs into one indexed clip-space mesh,
+// in work-group order (TileRasterCoreInvocationCuda.cu:384-402 compacts in atomic arrival order).
+// Offsets: one CTA, each thread a run of consecutive work groups; counts above the per-group
+// maxima, negative counts or index counts that are not a multiple of 3 set totals[2].
+__global__ void __launch_bounds__(1024) mesh_offsets_kernel(const int* __restrict__ nv, const int* __restrict__ ni,
+                                                            int groups, int max_v, int max_i, int* off_v, int* off_i,
+                                                            long long* totals) {
+    __shared__ long long ws[2][33];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const int per = (groups + 1023) / 1024;
+    const int b = min((int)threadIdx.x * per, groups), e = min(b + per, groups);
+    long long sv = 0, si = 0;
+    int bad = 0;
+    for (int g = b; g < e; g++) {
+        const int v = nv[g], i = ni[g];
+        bad |= v < 0 || v > max_v || i < 0 || i > max_i || i % 3 != 0;
+        sv += v < 0 ? 0 : min(v, max_v);
+        si += i < 0 ? 0 : min(i, max_i) / 3 * 3;
+    }
+    long long iv = sv, ii = si;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const long long qv = __shfl_up_sync(0xffffffffu, iv, o), qi = __shfl_up_sync(0xffffffffu, ii, o);
+        if (lane >= o) { iv += qv; ii += qi; }
+    }
+    if (lane == 31) { ws[0][wid] = iv; ws[1][wid] = ii; }
+    bad = __syncthreads_or(bad);
+    if (wid == 0) {
+        long long a = ws[0][lane], c = ws[1][lane], ai = a, ci = c;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const long long qa = __shfl_up_sync(0xffffffffu, ai, o), qc = __shfl_up_sync(0xffffffffu, ci, o);
+            if (lane >= o) { ai += qa; ci += qc; }
+        }
+        ws[0][lane] = ai - a;
+        ws[1][lane] = ci - c;
+        if (lane == 31) { ws[0][32] = ai; ws[1][32] = ci; }
+    }
+    __syncthreads();
+    long long rv = ws[0][wid] + iv - sv, ri = ws[1][wid] + ii - si;
+    for (int g = b; g < e; g++) {
+        const int v = nv[g], i = ni[g];
+        off_v[g] = (int)min(rv, (long long)INT32_MAX);
+        off_i[g] = (int)min(ri, (long long)INT32_MAX);
+        rv += v < 0 ? 0 : min(v, max_v);
+        ri += i < 0 ? 0 : min(i, max_i) / 3 * 3;
+    }
+    if (threadIdx.x == 0) {
+        totals[0] = ws[0][32];
+        totals[1] = ws[1][32];
+        totals[2] = bad;
+    }
+}
+
+// Work group g (one CTA): its vertices become rows [x y z w a0 a1 a2 a3] of the compacted vertex
+// array, its indices are rebased by the group's first vertex.
+__global__ void __launch_bounds__(128) mesh_compact_kernel(const float4* __restrict__ pos, const float4* __restrict__ attr,
+                                                           const int* __restrict__ idx, const int* __restrict__ nv,
+                                                           const int* __restrict__ ni, const int* __restrict__ off_v,
+                                                           const int* __restrict__ off_i, int max_v, int max_i,
+                                                           float4* __restrict__ out_v, int* __restrict__ out_i) {
+    const int g = blockIdx.x;
+    const int v = min(max(nv[g], 0), max_v), n = min(max(ni[g], 0), max_i) / 3 * 3;
+    const int ov = off_v[g], oi = off_i[g];
+    for (int k = threadIdx.x; k < v; k += blockDim.x) {
+        const size_t src = (size_t)g * max_v + k;
+        out_v[2 * ((size_t)ov + k)] = pos[src];
+        out_v[2 * ((size_t)ov + k) + 1] = attr ? attr[src] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    }
+    for (int k = threadIdx.x; k < n; k += blockDim.x) {
+        const int l = idx[(size_t)g * max_i + k];
+        // an index outside the group's vertices becomes -1, which the front end rejects
+        out_i[(size_t)oi + k] = l >= 0 && l < v ? ov + l : -1;
+    }
+}
+
+cudaError_t launch_mesh_offsets(const int* nv, const int* ni, int groups, int max_v, int max_i, int* off_v, int* off_i,
+                                long long* totals, cudaStream_t stream) {
+    mesh_offsets_kernel<<<1, 1024, 0, stream>>>(nv, ni, groups, max_v, max_i, off_v, off_i, totals);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_mesh_compact(const float* pos, const float* attr, const int* idx, const int* nv, const int* ni,
+                                const int* off_v, const int* off_i, int groups, int max_v, int max_i, float* out_v,
+                                int* out_i, cudaStream_t stream) {
+    if (groups > 0)
+        mesh_compact_kernel<<<groups, 128, 0, stream>>>(reinterpret_cast<const float4*>(pos),
+                                                        reinterpret_cast<const float4*>(attr), idx, nv, ni, off_v,
+                                                        off_i, max_v, max_i, reinterpret_cast<float4*>(out_v), out_i);
+    return cudaGetLastError();
+}
+
 // ---------------------------------------------------------------------------- mips
 __global__ void mip_kernel(const uint32_t* __restrict__ src, int sw, int sh, uint32_t* __restrict__ dst, int dw, int dh) {
     int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;

@@ -111,6 +111,13 @@ constexpr int scan_blocks(int tiles) { return (tiles + 4095) / 4096 + 1; }
 constexpr int kStageEvents = 7;
 cudaError_t launch_pass(const PassArgs& a, const LaunchPlan& plan, cudaStream_t stream, cudaEvent_t* ev);
 cudaError_t launch_mip_level(const uint32_t* src, int sw, int sh, uint32_t* dst, int dw, int dh, cudaStream_t stream);
+// Mesh-stage outputs: per-group vertex / index offsets (totals: vertices, indices, bad-count flag),
+// then the compaction into [x y z w a0 a1 a2 a3] rows and rebased indices.
+cudaError_t launch_mesh_offsets(const int* nv, const int* ni, int groups, int max_v, int max_i, int* off_v, int* off_i,
+                                long long* totals, cudaStream_t stream);
+cudaError_t launch_mesh_compact(const float* pos, const float* attr, const int* idx, const int* nv, const int* ni,
+                                const int* off_v, const int* off_i, int groups, int max_v, int max_i, float* out_v,
+                                int* out_i, cudaStream_t stream);
 // Maximum resident CTAs per SM of a tile kernel for (samples, tile size, ordered); stage 0 is
 // the raster (or ordered) kernel, stage 1 the shade kernel.
 int tile_kernel_occupancy(int samples, int tile_size, int ordered, int stage);

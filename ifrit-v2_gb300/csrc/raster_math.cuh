@@ -52,6 +52,7 @@ struct DrawDev {
     int scissor_box[4];
     int scissor[16][4];
     int polygon_mode;  // POLY_FILL / POLY_LINE / POLY_POINT
+    int clip_input;    // 1: vertex positions are 4 clip-space floats (a mesh / geometry stage's output), no MVP
 };
 
 // Polygon modes (IfritPolygonMode, base/Constants.h:23-28).  LINE: each edge of the culled,
@@ -281,7 +282,13 @@ __device__ __forceinline__ bool fetch_triangle(const PassConst& c, const DrawDev
     for (int i = 0; i < 3; i++) {
         int vid = __ldg(d.indices + 3 * (size_t)t + i);
         if (vid < 0 || vid >= d.num_vertices) return false;
-        xform(d.mvp, d.vertices + (size_t)vid * d.stride, poly[i].p);
+        const float* vp = d.vertices + (size_t)vid * d.stride;
+        if (d.clip_input) {
+#pragma unroll
+            for (int k = 0; k < 4; k++) poly[i].p[k] = __ldg(vp + k);
+        } else {
+            xform(d.mvp, vp, poly[i].p);
+        }
 #pragma unroll
         for (int k = 0; k < 4; k++)
             if (!isfinite(poly[i].p[k])) return false;

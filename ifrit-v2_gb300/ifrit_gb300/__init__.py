@@ -47,7 +47,7 @@ EXPORTED = [
     "iftrSetVertexBufferDirty", "ifbufGetBufferRawData", "ifbufSetBufferDirty", "iftrDrawNoAlloc",
     "iftrBeginPass", "iftrPassDraw", "iftrEndPass", "iftrDrawBatch", "iftrSetBatchTuning", "iftrGetBatchTuning",
     "iftrDiffForward", "iftrDiffBackward", "iftrSetScissors", "iftrSetScissorTestEnable",
-    "iftrSetRasterizerPolygonMode", "iftrSetRasterPath",
+    "iftrSetRasterizerPolygonMode", "iftrSetRasterPath", "iftrDrawMeshOutputs",
 ]
 
 
@@ -170,6 +170,7 @@ def load(build_if_missing=True):
         "iftrDiffForward": [ctypes.POINTER(DiffPass), vp], "iftrDiffBackward": [ctypes.POINTER(DiffPass), vp],
         "iftrSetScissors": [vp, fp, ip], "iftrSetScissorTestEnable": [vp, ip],
         "iftrSetRasterizerPolygonMode": [vp, ip], "iftrSetRasterPath": [vp, ip],
+        "iftrDrawMeshOutputs": [vp, ip, vp, vp, ip, vp, vp, vp, ip, ip, ip],
     }
     for name, args in sig.items():
         getattr(lib, name).argtypes = args
@@ -268,6 +269,20 @@ class Renderer:
         """Blend factors use the IfritBlendFactor numbering (6 SRC_ALPHA, 7 ONE_MINUS_SRC_ALPHA)."""
         s = BlendState(int(enable), src_color, dst_color, src_alpha, dst_alpha)
         check("iftrSetBlendFunc", self.lib.iftrSetBlendFunc(self.h, ctypes.byref(s)))
+
+    def draw_mesh_outputs(self, positions, indices, num_vertices, num_indices, attributes=None, attr_count=0,
+                          clear=True):
+        """Draws a mesh (or geometry) stage's per-work-group outputs (iftrDrawMeshOutputs): CUDA
+        tensors positions (G, maxV, 4) float32 clip space, attributes (G, maxV, 4) float32 or None,
+        indices (G, maxI) int32 group-local, num_vertices / num_indices (G,) int32."""
+        G, max_v = int(positions.shape[0]), int(positions.shape[1])
+        max_i = int(indices.shape[1])
+        for t in (positions, indices, num_vertices, num_indices) + ((attributes,) if attributes is not None else ()):
+            if not (t.is_cuda and t.is_contiguous()):
+                raise ValueError("mesh outputs must be contiguous CUDA tensors")
+        check("iftrDrawMeshOutputs", self.lib.iftrDrawMeshOutputs(
+            self.h, G, positions.data_ptr(), attributes.data_ptr() if attributes is not None else None, attr_count,
+            indices.data_ptr(), num_vertices.data_ptr(), num_indices.data_ptr(), max_v, max_i, int(clear)))
 
     def set_raster_path(self, path):
         check("iftrSetRasterPath", self.lib.iftrSetRasterPath(self.h, path))

@@ -156,6 +156,20 @@ IFTR_API int iftrSetRasterizerPolygonMode(IfritGbRenderer* h, int mode);
 enum { IFTR_RASTER_TILED = 0, IFTR_RASTER_ATOMIC = 1 };
 IFTR_API int iftrSetRasterPath(IfritGbRenderer* h, int path);
 IFTR_API int iftrSetScissorTestEnable(IfritGbRenderer* h, int enable);
+/* Outputs of a mesh (or geometry) shading stage drawn as one pass (the boundary of the reference's
+ * MeshShadingStage / GeneralGeometryStage, TileRasterCoreInvocationCuda.cu:355-561, whose shader
+ * objects produce per-work-group vertices and triangle lists that are compacted and fed to
+ * triangle set-up).  Device arrays: work group g holds numVertices[g] <= maxVertices vertices at
+ * positions[(g * maxVertices + i) * 4] (clip-space x, y, z, w; no MVP is applied) with one float4
+ * varying at attributes[(g * maxVertices + i) * 4] (attrCount components used, NULL when 0), and
+ * numIndices[g] <= maxIndices (a multiple of 3) group-local vertex indices at
+ * indices[g * maxIndices + k].  Groups are compacted in group order (triangle ids follow it) and
+ * drawn with the current state, synchronously like iftrDrawLegacy.  A geometry stage's output is
+ * the same with one group per input primitive.  Counts out of range return
+ * IFTR_ERR_INVALID_ARG; an index outside its group's vertices drops the triangle. */
+IFTR_API int iftrDrawMeshOutputs(IfritGbRenderer* h, int numGroups, const float* positions, const float* attributes,
+                                 int attrCount, const int* indices, const int* numVertices, const int* numIndices,
+                                 int maxVertices, int maxIndices, int clear);
 IFTR_API int iftrCreateTexture(IfritGbRenderer* h, int slot, int width, int height, int mipLevels); /* TRC:91, RGBA8 */
 IFTR_API int iftrCopyHostBufferToImage(IfritGbRenderer* h, const void* rgba8, int slot); /* TRC:96, level 0 */
 IFTR_API int iftrGenerateMipmap(IfritGbRenderer* h, int slot, int filter);           /* TRC:93 */
