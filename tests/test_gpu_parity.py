@@ -109,6 +109,24 @@ def test_textured_trilinear_anisotropic(aniso, address):
     assert_parity(gpu, ref)
 
 
+@pytest.mark.parametrize("aniso", [1, 8])
+def test_textured_clipped_triangles(aniso):
+    """Camera inside a textured sphere: the triangles crossing the near plane (95 of 1,280) are
+    clipped into fan triangles whose set-up and vertex attributes take the general path in every
+    stage (no triangle record), with anisotropic texture lookups on them."""
+    v, f = scenes.jittered_icosphere(3, 9, jitter=0.1)
+    v = v.copy()
+    v[:, :3] *= 3.0
+    uv = np.stack([0.5 + np.arctan2(v[:, 2], v[:, 0]) / (2 * np.pi), 0.5 + v[:, 1] / 6.0], 1).astype(np.float32)
+    vt = np.concatenate([v[:, :3], uv * 4.0], 1)
+    mvp = (scenes.perspective(70.0, 1.25, 0.1, 50.0) @ scenes.look_at((0.3, 0.2, 0.1), (0, 0, -1))).astype(np.float32)
+    tex = scenes.value_noise_texture(256, 5)
+    gpu, ref, _ = render_both(vt, f, mvp, 160, 128, S=4, attr=2, cull=ig.CULL_NONE, depth_func=ig.LESS,
+                              shading=ig.FS_TEXTURED, texture=tex, max_aniso=aniso, address=0)
+    assert_parity(gpu, ref)
+    assert (gpu["vis"] >= 0).mean() > 0.9
+
+
 def test_overflow_retry_gives_same_image():
     v, f, mvp = soup(20000, 13, 256, 160)
     v6 = np.concatenate([v[:, :3], np.abs(v[:, 3:5]) % 1.0, np.full((len(v), 1), 0.5, np.float32)], 1)
