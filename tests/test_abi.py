@@ -89,3 +89,21 @@ def test_null_handles_rejected(lib):
     assert lib.iftrDrawLegacy(None, 3, 1) == 1
     assert lib.iftrDestroyInstance(None) == 1
     assert lib.iftrFinish(None) == 1
+
+
+def test_mesh_outputs_argument_checks(lib):
+    """iftrDrawMeshOutputs validates its arguments before any device work."""
+    h = lib.iftrCreateInstance()
+    assert h
+    buf = (ctypes.c_float * 16)()
+    ib = (ctypes.c_int * 8)()
+    p = ctypes.cast(buf, ctypes.c_void_p)
+    q = ctypes.cast(ib, ctypes.c_void_p)
+    # negative group count, attribute count above 4, varyings requested without an array, bad maxima
+    assert lib.iftrDrawMeshOutputs(h, -1, p, None, 0, q, q, q, 4, 3, 1) == 1
+    assert lib.iftrDrawMeshOutputs(h, 1, p, p, 5, q, q, q, 4, 3, 1) == 1
+    assert lib.iftrDrawMeshOutputs(h, 1, p, None, 3, q, q, q, 4, 3, 1) == 1
+    assert lib.iftrDrawMeshOutputs(h, 1, p, None, 0, q, q, q, 0, 3, 1) == 1
+    assert lib.iftrDrawMeshOutputs(h, 1, None, None, 0, q, q, q, 4, 3, 1) == 1
+    assert lib.iftrDrawMeshOutputs(None, 0, None, None, 0, None, None, None, 4, 3, 1) == 1
+    assert lib.iftrDestroyInstance(h) == 0
