@@ -831,7 +831,8 @@ __device__ __forceinline__ void raster_depth(const ViewArgs& v, const KeyRule& r
     const int32_t X0 = rec.X0[r], Y0 = rec.Y0[r];
     const uint32_t e = (uint32_t)rec.key[r];
     const uint32_t lo_word = rule.mode == KM_EARLIEST ? e + 1u : 0xFFFFFFFEu - e;
-    unsigned long long* kp = skey + (qy * TS + qx) * S;
+    // sample-major keys ([sample][pixel]): lanes on different pixels spread over the banks
+    unsigned long long* kp = skey + qy * TS + qx;
     // (float)(sx - X0) == fbx + sample offset exactly: every term is an integer below
     // 2^24 in magnitude (guard-band bound), so no conversion per sample is needed.
     const float fbx = (float)(gx * 256 - X0), fby = (float)(gy * 256 - Y0);
@@ -847,7 +848,7 @@ __device__ __forceinline__ void raster_depth(const ViewArgs& v, const KeyRule& r
             hi_word = rule.invert ? ~depth_order(z) : depth_order(z);
         }
         const unsigned long long kv = ((unsigned long long)hi_word << 32) | lo_word;
-        atomicMin(kp + k, kv);
+        atomicMin(kp + k * (TS * TS), kv);
     }
 }
 
@@ -878,7 +879,7 @@ __device__ __forceinline__ void raster_tile(const PassArgs& a, const ViewArgs& v
 #pragma unroll
     for (int k = 0; k < S; k++) {
         float d0 = v.clear ? v.clear_depth : (inpix ? v.depth[pix * S + k] : 0.0f);
-        skey[(ly * TS + lx) * S + k] = background_key(rule, d0);
+        skey[k * (TS * TS) + ly * TS + lx] = background_key(rule, d0);
     }
     const bool has_list = a.total_tris > 0 && a.status[ST_OVERFLOW] == 0 && rule.func != 0;
     const uint32_t beg = has_list ? a.tile_offset[gtile] : 0u;
@@ -1124,7 +1125,7 @@ __device__ __forceinline__ void raster_tile(const PassArgs& a, const ViewArgs& v
     if (!inpix) return;
     int out[S];
 #pragma unroll
-    for (int k = 0; k < S; k++) out[k] = key_entry(rule, skey[(ly * TS + lx) * S + k]);
+    for (int k = 0; k < S; k++) out[k] = key_entry(rule, skey[k * (TS * TS) + ly * TS + lx]);
     int* ep = v.entries + pix * S;
     if constexpr (S % 4 == 0) {
 #pragma unroll
