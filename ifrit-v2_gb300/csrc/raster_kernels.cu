@@ -1141,8 +1141,16 @@ size_t raster_smem_bytes() {
     return sizeof(TileRecords<TS * TS>) + (size_t)TS * TS * S * sizeof(unsigned long long);
 }
 
+// Resident raster CTAs per SM the register budget is sized for: 16x16 tiles at up to 4x fit five
+// in shared memory (measured best: five beat four by ~2 %, six spill too much); 8x and 16x keys
+// leave room for four and three.
 template <int S, int TS>
-__global__ void __launch_bounds__(TS * TS, 1024 / (TS * TS)) raster_kernel(PassArgs a, GroupArgs g) {
+__host__ __device__ constexpr int raster_min_blocks() {
+    return TS == 16 ? (S <= 4 ? 5 : (S == 8 ? 4 : 3)) : 1024 / (TS * TS);
+}
+
+template <int S, int TS>
+__global__ void __launch_bounds__(TS * TS, raster_min_blocks<S, TS>()) raster_kernel(PassArgs a, GroupArgs g) {
     constexpr int NT = TS * TS;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     TileRecords<NT>& rec = *reinterpret_cast<TileRecords<NT>*>(smem_raw);
