@@ -14,7 +14,6 @@
 #include <cuda_runtime.h>
 
 #include <cstring>
-#include <mutex>
 
 #include "../../include/ifrit_gb300.h"
 #include "pass_plan.h"
@@ -42,25 +41,15 @@ static_assert(kScratchEnd <= IFTR_NOALLOC_SCRATCH_BYTES, "scratch layout exceeds
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[IFTR_NOALLOC_SCRATCH_BYTES];
 
-constexpr int kMaxDevices = 64;
-std::mutex g_mutex;
-unsigned char* g_scratch_ptr[kMaxDevices] = {};
-
-// Device address of the scratch array on the current device (looked up once per device; the
-// array's host-side name is only a stand-in and must never be passed to a kernel).
+// Device address of the scratch array on the current device.  The array's host-side name is
+// only a stand-in and must never be passed to a kernel.  The address is looked up on every call
+// (the lookup allocates nothing), so it stays right if the context is torn down and the module
+// reloaded at another address.
 cudaError_t scratch_address(unsigned char** out) {
-    int dev = 0;
-    cudaError_t e = cudaGetDevice(&dev);
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
     if (e != cudaSuccess) return e;
-    if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
-    std::lock_guard<std::mutex> lock(g_mutex);
-    if (!g_scratch_ptr[dev]) {
-        void* p = nullptr;
-        e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-        if (e != cudaSuccess) return e;
-        g_scratch_ptr[dev] = static_cast<unsigned char*>(p);
-    }
-    *out = g_scratch_ptr[dev];
+    *out = static_cast<unsigned char*>(p);
     return cudaSuccess;
 }
 
@@ -70,7 +59,9 @@ extern "C" IFTR_API int iftrDrawNoAlloc(const IfritGbNoAllocPass* p, void* cudaS
     if (!p) return IFTR_ERR_INVALID_ARG;
     const int S = p->samples;
     if (!(S == 1 || S == 2 || S == 4 || S == 8 || S == 16)) return IFTR_ERR_INVALID_ARG;
-    if (p->width <= 0 || p->height <= 0 || p->numIndices < 0 || p->numIndices % 3 != 0) return IFTR_ERR_INVALID_ARG;
+    if (p->width <= 0 || p->height <= 0 || p->width > 16384 || p->height > 16384 || p->numIndices < 0 ||
+        p->numIndices % 3 != 0)
+        return IFTR_ERR_INVALID_ARG;
     const size_t T = (size_t)ifr::tiles_of(p->width, p->height, 16);
     if ((size_t)p->numIndices / 3 > IFTR_NOALLOC_MAX_TRIANGLES || T > IFTR_NOALLOC_MAX_TILES ||
         (size_t)p->width * p->height * S > IFTR_NOALLOC_MAX_SAMPLES)

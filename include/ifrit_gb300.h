@@ -207,13 +207,17 @@ IFTR_API const char* iftrGetErrorString(int status);
  * intermediate data (binning lists, set-up records, per-sample winners, status words) lives in
  * one file-scope device array inside the library, of IFTR_NOALLOC_SCRATCH_BYTES, which every
  * GPU that loads the library holds until the process exits.  The call makes no cudaMalloc,
- * cudaFree or other allocating call.  Its first call on a device (with that device current)
- * looks up the array's device address once; make that first call before any stream capture.
+ * cudaFree or other allocating call.  Every call looks up the array's device address on the
+ * current device (a lookup that allocates nothing); the first call on a device may also load the
+ * library's device code there, so make it before any stream capture.
  * The array is shared by every call and keeps the last call's contents: calls that overlap on
  * the GPU (different streams or threads) race and must be serialised by the caller.  The call
  * is synchronous on `cudaStream` (it reads a status word back) and returns
- * IFTR_ERR_INVALID_ARG for sizes above the limits below and IFTR_ERR_OVERFLOW if the scene
- * produces more (triangle, tile) overlaps than the list capacity. */
+ * IFTR_ERR_INVALID_ARG for sizes above the limits below (and for a width or height above
+ * 16384, as every other entry point) and IFTR_ERR_OVERFLOW if the scene produces more
+ * (triangle, tile) overlaps than the list capacity.  After IFTR_ERR_OVERFLOW the colour, depth
+ * and visibility outputs are undefined (the pass has cleared and partly written them); the
+ * next call starts afresh. */
 #define IFTR_NOALLOC_MAX_TRIANGLES (1 << 16)   /* numIndices / 3 */
 #define IFTR_NOALLOC_MAX_SAMPLES (1 << 21)     /* width * height * samples */
 #define IFTR_NOALLOC_MAX_TILE_PAIRS (1 << 19)  /* (triangle, 16x16 tile) overlaps */

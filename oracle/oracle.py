@@ -32,7 +32,8 @@ def build(force=False):
 
 class Sampler(ctypes.Structure):
     _fields_ = [("address_u", ctypes.c_int), ("address_v", ctypes.c_int), ("filter", ctypes.c_int),
-                ("border_white", ctypes.c_int), ("max_aniso", ctypes.c_int), ("lod_bias", ctypes.c_float)]
+                ("border_white", ctypes.c_int), ("max_aniso", ctypes.c_int), ("lod_bias", ctypes.c_float),
+                ("compat", ctypes.c_int)]
 
 
 class Texture(ctypes.Structure):
@@ -51,7 +52,8 @@ class Draw(ctypes.Structure):
                 ("blend_src_alpha", ctypes.c_int), ("blend_dst_alpha", ctypes.c_int),
                 ("shading", ctypes.c_int), ("tex", Texture), ("sampler", Sampler),
                 ("scissor_enable", ctypes.c_int), ("scissor_count", ctypes.c_int),
-                ("scissor", (ctypes.c_float * 4) * 16), ("polygon_mode", ctypes.c_int)]
+                ("scissor", (ctypes.c_float * 4) * 16), ("polygon_mode", ctypes.c_int),
+                ("blend_compat", ctypes.c_int)]
 
 
 class Target(ctypes.Structure):
@@ -101,8 +103,10 @@ def build_mips(level0):
 
 def make_draw(vertices, indices, mvp, *, attr_offset=3, attr_count=3, prim_base=0, cull_mode=2,
               front_ccw=1, depth_test=1, depth_func=3, depth_write=1, blend=None, shading=SHADE_GOURAUD,
-              texture=None, sampler=None, scissor=None, polygon_mode=0):
-    """Returns (Draw, keepalive) for numpy vertices (V, stride) float32 and indices (T, 3) int32."""
+              texture=None, sampler=None, scissor=None, polygon_mode=0, blend_compat=0):
+    """Returns (Draw, keepalive) for numpy vertices (V, stride) float32 and indices (T, 3) int32.
+    blend_compat / sampler["compat"] select the reference's blend table and sampler as written
+    (pinning only; see oracle_fx.h)."""
     vertices = np.ascontiguousarray(vertices, np.float32)
     indices = np.ascontiguousarray(indices, np.int32).reshape(-1)
     d = Draw()
@@ -136,7 +140,9 @@ def make_draw(vertices, indices, mvp, *, attr_offset=3, attr_count=3, prim_base=
     d.sampler.border_white = s.get("border_white", 0)
     d.sampler.max_aniso = s.get("max_aniso", 1)
     d.sampler.lod_bias = s.get("lod_bias", 0.0)
+    d.sampler.compat = int(s.get("compat", 0))
     d.polygon_mode = polygon_mode
+    d.blend_compat = int(blend_compat)
     if scissor is not None:  # list of (x, y, w, h) rectangles; [] = enabled with none (passes all)
         d.scissor_enable = 1
         d.scissor_count = min(len(scissor), 16)

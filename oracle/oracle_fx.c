@@ -29,6 +29,7 @@
  * Every floating-point expression is written in the exact evaluation order the device
  * code uses and the file is compiled with -ffp-contract=off, so results are bit-identical.
  */
+#define _POSIX_C_SOURCE 200809L /* pthread barriers under -std=c11 */
 #include "oracle_fx.h"
 #include <math.h>
 #include <pthread.h>
@@ -289,9 +290,140 @@ static void sample_trilinear(const ofx_texture* tex, const ofx_sampler* s, float
 
 static inline float finite_or_zero(float x) { return isfinite(x) ? x : 0.0f; }
 
+/* ---------------------------------------------------------------- reference-compatible sampling
+ * The reference's sampler as written (ShaderBuiltinCuda.cuh:106-272), with the quirks that the
+ * default path above fixes.  It exists only to pin this restatement against the reference's own
+ * sampler compiled on the host; the GPU path implements the default path.  Differences from the
+ * default path, each reproduced here:
+ *   - address modes (:117-157): repeat / mirrored repeat add one period to a negative coordinate
+ *     before fmodf; mirror-clamp-to-edge maps c >= size-1 to 0 and c <= 0 to size-1;
+ *   - nearest filtering rounds half away from zero and wraps modulo the level size (:159-165),
+ *     and is still blended between two levels by the LOD fraction (:214-218);
+ *   - the level pair (floor(lod), floor(lod)+1) is not clamped to the chain (:214-217); callers
+ *     keep the LOD inside the chain or pad it (texels past the chain read as the last level);
+ *   - isotropic LOD: the y footprint uses (du/dy, dv/dx) (the `dx.y` typo, :237), and
+ *     lod = max(0, 0.5 log2(max) + bias) (:240);
+ *   - anisotropic (:244-272): the footprint axes are the gradients of u and of v,
+ *     px = |(du/dx, du/dy)| * width and py = |(dv/dx, dv/dy)| * height (the parameter names there
+ *     swap du/dy and dv/dx), the probe direction is (du/dx, du/dy) if px > py else (dv/dx, dv/dy),
+ *     n = clamp(ceil(pmax/pmin), 1, maxAniso), lambda = max(0, log2(pmax/n)) before the bias,
+ *     and probe i (0-based) sits at i/(n+1) - 1/2 (not centred);
+ *   - log2 is the C library's log2f (the reference calls log2). */
+static inline float compat_clamp(float x, float mi, float ma) { return (x >= ma) ? ma : ((x <= mi) ? mi : x); }
+static inline float compat_mirrorclamp(float x, float mi, float ma) { return (x >= ma) ? mi : ((x <= mi) ? ma : x); }
+
+static int compat_address(int mode, float* c, int n) {
+    float v = *c;
+    switch (mode) {
+    case 0:
+        if (v < 0.0f) v = v + (float)n;
+        v = fmodf(v, (float)n);
+        break;
+    case 1:
+        if (v < 0.0f) v = v + (float)(2 * n);
+        v = fmodf(v, (float)(2 * n));
+        v = fmin_(v, (float)(2 * n) - v);
+        break;
+    case 2: v = compat_clamp(v, 0.0f, (float)n - 1.0f); break;
+    case 3:
+        if (v >= (float)n || v < 0.0f) return 0;
+        break;
+    case 4: v = compat_mirrorclamp(v, 0.0f, (float)n - 1.0f); break;
+    default: break;
+    }
+    *c = v;
+    return 1;
+}
+
+/* One level lookup (textureImplLegacy, :106-182); level sizes continue as 1x1 past the chain. */
+static void compat_level(const ofx_texture* tex, const ofx_sampler* s, int level, float u, float v, float out[4]) {
+    int w = tex->width, h = tex->height, off = 0;
+    for (int i = 0; i < level; i++) {
+        off += w * h;
+        w = (w + 1) >> 1;
+        h = (h + 1) >> 1;
+    }
+    float cx = u * (float)(w - 1), cy = v * (float)(h - 1);
+    if (!compat_address(s->address_u, &cx, w) || !compat_address(s->address_v, &cy, h)) {
+        float b = s->border_white ? 1.0f : 0.0f;
+        out[0] = b; out[1] = b; out[2] = b; out[3] = 1.0f;
+        return;
+    }
+    const uint32_t* t = tex->texels;
+    int last = ofx_mip_chain_texels(tex->width, tex->height, NULL) - 1;
+    /* indices outside the chain are out-of-range reads in the reference (a coordinate below
+     * one period before 0 in repeat modes, levels past the chain): clamped here */
+#define COMPAT_TEXEL(i, dst) unpack_rgba8(t[imax_(0, imin_((i), last))], dst)
+    if (s->filter == 0) {
+        int x = (int)roundf(cx) % w, y = (int)roundf(cy) % h;
+        COMPAT_TEXEL(off + y * w + x, out);
+        return;
+    }
+    int x0 = (int)cx, y0 = (int)cy;
+    float fx = cx - (float)x0, fy = cy - (float)y0;
+    int x1 = imin_(x0 + 1, w - 1), y1 = imin_(y0 + 1, h - 1);
+    float c00[4], c01[4], c10[4], c11[4];
+    COMPAT_TEXEL(off + y0 * w + x0, c00);
+    COMPAT_TEXEL(off + y0 * w + x1, c01);
+    COMPAT_TEXEL(off + y1 * w + x0, c10);
+    COMPAT_TEXEL(off + y1 * w + x1, c11);
+#undef COMPAT_TEXEL
+    for (int i = 0; i < 4; i++) {
+        float top = lerpf_(c00[i], c01[i], fx);
+        float bot = lerpf_(c10[i], c11[i], fx);
+        out[i] = lerpf_(top, bot, fy);
+    }
+}
+
+/* textureImplLod (:210-218): two levels blended by the LOD fraction, unclamped. */
+static void compat_lod(const ofx_texture* tex, const ofx_sampler* s, float u, float v, float lod, float out[4]) {
+    int lo = (int)floorf(lod);
+    float t = lod - (float)lo;
+    float c1[4];
+    compat_level(tex, s, lo, u, v, out);
+    compat_level(tex, s, lo + 1, u, v, c1);
+    for (int i = 0; i < 4; i++) out[i] = lerpf_(out[i], c1[i], t);
+}
+
+static void sample_compat(const ofx_texture* tex, const ofx_sampler* s, float u, float v, float dudx, float dvdx,
+                          float dudy, float dvdy, float out[4]) {
+    const float W = (float)tex->width, H = (float)tex->height;
+    if (s->max_aniso <= 1) { /* textureImplAdaptiveLod (:233-243) */
+        float xx = dudx * W, xy = dvdx * H, yx = dudy * W, yy = dvdx * H;
+        float dx2 = xx * xx + xy * xy, dy2 = yx * yx + yy * yy;
+        float d = fmax_(dx2, dy2);
+        float lod = fmax_(0.0f, 0.5f * log2f(d) + s->lod_bias);
+        compat_lod(tex, s, u, v, lod, out);
+        return;
+    }
+    /* textureImplAnisotropicFilter (:244-272) */
+    float px = sqrtf(dudx * dudx + dudy * dudy) * W;
+    float py = sqrtf(dvdx * dvdx + dvdy * dvdy) * H;
+    float pmax = fmax_(px, py), pmin = fmin_(px, py);
+    double r = (double)ceilf(pmax / pmin) + 1e-3;
+    double lim = (double)s->max_aniso + 1e-3;
+    double m = fmin(r, lim);
+    int n = (int)fmax(1.0, m);
+    float lambda = fmax_(0.0f, log2f(pmax / (float)n));
+    float ddu = px > py ? dudx : dvdx;
+    float ddv = px > py ? dudy : dvdy;
+    float acc[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+    for (int i = 0; i < n; i++) {
+        float t = (1.0f * (float)i) / (float)(n + 1) - 0.5f;
+        float c[4];
+        compat_lod(tex, s, u + ddu * t, v + ddv * t, lambda + s->lod_bias, c);
+        for (int k = 0; k < 4; k++) acc[k] = acc[k] + c[k];
+    }
+    for (int k = 0; k < 4; k++) out[k] = acc[k] / (float)n;
+}
+
 /* Texture sampling with LOD from screen-space derivatives (ShaderBuiltinCuda.cuh:225-272). */
 void ofx_sample_texture(const ofx_texture* tex, const ofx_sampler* s, float u, float v,
                         float dudx, float dvdx, float dudy, float dvdy, float out[4]) {
+    if (s->compat) {
+        sample_compat(tex, s, u, v, dudx, dvdx, dudy, dvdy, out);
+        return;
+    }
     u = finite_or_zero(u); v = finite_or_zero(v);
     dudx = finite_or_zero(dudx); dvdx = finite_or_zero(dvdx);
     dudy = finite_or_zero(dudy); dvdy = finite_or_zero(dvdy);
@@ -676,8 +808,35 @@ static inline float blend_factor(int f, int ch, const float* src, const float* d
     }
 }
 
+/* The reference's coefficient vector per factor (TileRasterRenderer.cpp:212-333). */
+static void compat_coefs(int f, float k[4]) {
+    k[0] = k[1] = k[2] = k[3] = 0.0f;
+    switch (f) {
+    case 1: k[0] = 1.0f; break;                   /* ONE */
+    case 8: k[2] = 1.0f; break;                   /* DST_ALPHA */
+    case 6: k[1] = 1.0f; break;                   /* SRC_ALPHA */
+    case 9: k[0] = 1.0f; k[2] = -1.0f; break;     /* ONE_MINUS_DST_ALPHA */
+    case 7: k[0] = 1.0f; k[1] = -1.0f; break;     /* ONE_MINUS_SRC_ALPHA */
+    default: k[3] = 1.0f; break;                  /* ZERO (and unsupported factors) */
+    }
+}
+
+static inline float compat_factor(int f, const float* src, const float* dst) {
+    float k[4];
+    compat_coefs(f, k);
+    return (k[0] + k[1] * (1.0f - src[3]) + k[2] * (1.0f - dst[3])) * (1.0f - k[3]);
+}
+
 static void blend(const ofx_draw* d, const float* src, float* dst) {
     float out[4];
+    if (d->blend_compat) { /* TileRasterWorker.cpp:2350-2366 */
+        float sx = compat_factor(d->blend_src_color, src, dst), dx = compat_factor(d->blend_dst_color, src, dst);
+        float sa = compat_factor(d->blend_src_alpha, src, dst), da = compat_factor(d->blend_dst_alpha, src, dst);
+        for (int ch = 0; ch < 3; ch++) out[ch] = dst[ch] * dx + src[ch] * sx;
+        out[3] = dst[3] * da + src[3] * sa;
+        for (int ch = 0; ch < 4; ch++) dst[ch] = out[ch];
+        return;
+    }
     for (int ch = 0; ch < 4; ch++) {
         int fs = ch < 3 ? d->blend_src_color : d->blend_src_alpha;
         int fd = ch < 3 ? d->blend_dst_color : d->blend_dst_alpha;
@@ -686,15 +845,35 @@ static void blend(const ofx_draw* d, const float* src, float* dst) {
     for (int ch = 0; ch < 4; ch++) dst[ch] = out[ch];
 }
 
-/* ---------------------------------------------------------------- pass */
+/* ---------------------------------------------------------------- pass
+ * Two phases per chunk of OFX_CHUNK triangles (in submission order): every thread sets up its
+ * slice of the chunk once (clip, snap, cull, edge functions), then every thread rasterises the
+ * whole chunk's sub-triangles, in submission order, into its own band of rows (depth test and
+ * write immediately, as the reference's in-order path).  Passes without blending are shaded
+ * deferred, as the reference's tag-buffer path (TileRasterWorker.cpp:1932-2121): each sample
+ * remembers the last fragment that passed it, and each (pixel, fragment) pair that survives is
+ * shaded once at the end -- the same colour forward shading leaves there, since unblended
+ * fragments overwrite.  Passes with blending shade every passing fragment in order. */
+#define OFX_CHUNK 16384
+
+typedef struct {
+    ofx_sub s;
+    int draw, tri, slot; /* slot: index of s in triangle_subs()'s output */
+} setup_rec;
+
 typedef struct {
     const ofx_draw* draws;
     int ndraws;
     ofx_target* t;
     const pass_ctx* c;
-    float* scol; /* per-sample colour for the whole frame */
-    int y0, y1;
-} band_job;
+    float* scol;        /* per-sample colour for the whole frame */
+    int64_t* win;       /* deferred passes: per-sample last passing fragment, -1 = none */
+    int id, nthreads;
+    int y0, y1;         /* this thread's band of rows */
+    pthread_barrier_t* bar;
+    setup_rec** lists;  /* per-thread set-up records of the current chunk */
+    int* counts;
+} pass_job;
 
 /* Scissor test of pixel (x, y) for draw d (TileRasterCoreInvocationCuda.cu:1950-1962). */
 static int scissor_pass(const ofx_draw* d, int x, int y) {
@@ -707,48 +886,113 @@ static int scissor_pass(const ofx_draw* d, int x, int y) {
     return 0;
 }
 
-static void* run_band(void* arg) {
-    band_job* j = (band_job*)arg;
+static inline int64_t pack_frag(int draw, int tri, int slot) {
+    return ((int64_t)draw << 36) | ((int64_t)tri << 4) | (int64_t)slot;
+}
+
+static void raster_rec(pass_job* j, const setup_rec* r) {
     const pass_ctx* c = j->c;
     ofx_target* tg = j->t;
-    int S = c->S;
+    const ofx_draw* d = &j->draws[r->draw];
+    const ofx_sub* s = &r->s;
+    const int S = c->S;
+    const int func = d->depth_test ? d->depth_func : 7;
+    const int ya = imax_(s->py0, j->y0), yb = imin_(s->py1, j->y1 - 1);
+    for (int py = ya; py <= yb; py++) {
+        for (int px = s->px0; px <= s->px1; px++) {
+            if (!scissor_pass(d, px, py)) continue;
+            size_t base = ((size_t)py * c->W + px) * S;
+            unsigned passmask = 0;
+            for (int k = 0; k < S; k++) {
+                int32_t sx = px * 256 + c->sx[k], sy = py * 256 + c->sy[k];
+                if (!covered(s, sx, sy)) continue;
+                float z = sample_depth(s, sx, sy);
+                if (!depth_cmp(func, z, tg->depth[base + k])) continue;
+                if (d->depth_write) tg->depth[base + k] = z;
+                if (tg->vis) tg->vis[base + k] = s->prim;
+                passmask |= 1u << k;
+            }
+            if (!passmask) continue;
+            if (j->win) {
+                int64_t f = pack_frag(r->draw, r->tri, r->slot);
+                for (int k = 0; k < S; k++)
+                    if (passmask & (1u << k)) j->win[base + k] = f;
+                continue;
+            }
+            float col[4];
+            shade(c, d, s, r->tri, px, py, col);
+            for (int k = 0; k < S; k++) {
+                if (!(passmask & (1u << k))) continue;
+                float* dst = j->scol + (base + k) * 4;
+                if (d->blend_enable) blend(d, col, dst);
+                else memcpy(dst, col, sizeof(float) * 4);
+            }
+        }
+    }
+}
+
+/* Deferred shading of this thread's band: one shade per (pixel, surviving fragment). */
+static void shade_band(pass_job* j) {
+    const pass_ctx* c = j->c;
+    const int S = c->S;
     ofx_sub subs[OFX_MAX_SUB];
-    for (int di = 0; di < j->ndraws; di++) {
-        const ofx_draw* d = &j->draws[di];
-        int func = d->depth_test ? d->depth_func : 7;
-        for (int t = 0; t < d->num_triangles; t++) {
-            int ns = triangle_subs(c, d, t, subs);
-            for (int si = 0; si < ns; si++) {
-                const ofx_sub* s = &subs[si];
-                int ya = imax_(s->py0, j->y0), yb = imin_(s->py1, j->y1 - 1);
-                for (int py = ya; py <= yb; py++) {
-                    for (int px = s->px0; px <= s->px1; px++) {
-                        if (!scissor_pass(d, px, py)) continue;
-                        size_t base = ((size_t)py * c->W + px) * S;
-                        unsigned passmask = 0;
-                        for (int k = 0; k < S; k++) {
-                            int32_t sx = px * 256 + c->sx[k], sy = py * 256 + c->sy[k];
-                            if (!covered(s, sx, sy)) continue;
-                            float z = sample_depth(s, sx, sy);
-                            if (!depth_cmp(func, z, tg->depth[base + k])) continue;
-                            if (d->depth_write) tg->depth[base + k] = z;
-                            if (tg->vis) tg->vis[base + k] = s->prim;
-                            passmask |= 1u << k;
-                        }
-                        if (!passmask) continue;
-                        float col[4];
-                        shade(c, d, s, t, px, py, col);
-                        for (int k = 0; k < S; k++) {
-                            if (!(passmask & (1u << k))) continue;
-                            float* dst = j->scol + (base + k) * 4;
-                            if (d->blend_enable) blend(d, col, dst);
-                            else memcpy(dst, col, sizeof(float) * 4);
-                        }
-                    }
+    int64_t cached = -1;
+    int ncached = 0;
+    for (int py = j->y0; py < j->y1; py++) {
+        for (int px = 0; px < c->W; px++) {
+            size_t base = ((size_t)py * c->W + px) * S;
+            unsigned done = 0;
+            for (int k = 0; k < S; k++) {
+                int64_t f = j->win[base + k];
+                if (f < 0 || (done & (1u << k))) continue;
+                int draw = (int)(f >> 36), tri = (int)((f >> 4) & 0xffffffffll), slot = (int)(f & 15);
+                const ofx_draw* d = &j->draws[draw];
+                if ((f & ~(int64_t)15) != cached) {
+                    ncached = triangle_subs(c, d, tri, subs);
+                    cached = f & ~(int64_t)15;
+                }
+                if (slot >= ncached) continue; /* cannot happen: set-up is deterministic */
+                float col[4];
+                shade(c, d, &subs[slot], tri, px, py, col);
+                for (int q = k; q < S; q++) {
+                    if (j->win[base + q] != f) continue;
+                    memcpy(j->scol + (base + q) * 4, col, sizeof(float) * 4);
+                    done |= 1u << q;
                 }
             }
         }
     }
+}
+
+static void* run_pass(void* arg) {
+    pass_job* j = (pass_job*)arg;
+    ofx_sub subs[OFX_MAX_SUB];
+    for (int di = 0; di < j->ndraws; di++) {
+        const ofx_draw* d = &j->draws[di];
+        for (int t0 = 0; t0 < d->num_triangles; t0 += OFX_CHUNK) {
+            int t1 = imin_(t0 + OFX_CHUNK, d->num_triangles);
+            int a = t0 + (int)((int64_t)(t1 - t0) * j->id / j->nthreads);
+            int b = t0 + (int)((int64_t)(t1 - t0) * (j->id + 1) / j->nthreads);
+            setup_rec* out = j->lists[j->id];
+            int n = 0;
+            for (int t = a; t < b; t++) {
+                int ns = triangle_subs(j->c, d, t, subs);
+                for (int si = 0; si < ns; si++) {
+                    out[n].s = subs[si];
+                    out[n].draw = di;
+                    out[n].tri = t;
+                    out[n].slot = si;
+                    n++;
+                }
+            }
+            j->counts[j->id] = n;
+            pthread_barrier_wait(j->bar);
+            for (int th = 0; th < j->nthreads; th++)
+                for (int i = 0; i < j->counts[th]; i++) raster_rec(j, &j->lists[th][i]);
+            pthread_barrier_wait(j->bar);
+        }
+    }
+    if (j->win) shade_band(j);
     return NULL;
 }
 
@@ -826,19 +1070,46 @@ int ofx_render_pass(const ofx_draw* draws, int ndraws, ofx_target* t, int clear,
     }
     if (nthreads < 1) nthreads = 1;
     if (nthreads > c.H) nthreads = c.H;
-    band_job jobs[256];
-    pthread_t th[256];
     if (nthreads > 256) nthreads = 256;
+    int deferred = 1;
+    for (int i = 0; i < ndraws; i++)
+        if (draws[i].blend_enable) deferred = 0;
+    int64_t* win = NULL;
+    if (deferred) {
+        win = (int64_t*)malloc(npix * S * sizeof(int64_t));
+        if (!win) { free(scol); return 3; }
+        for (size_t i = 0; i < npix * S; i++) win[i] = -1;
+    }
+    pass_job jobs[256];
+    pthread_t th[256];
+    setup_rec* lists[256];
+    int counts[256];
+    const int per_thread = (OFX_CHUNK + nthreads - 1) / nthreads * OFX_MAX_SUB;
+    int rc = 0;
     for (int i = 0; i < nthreads; i++) {
-        jobs[i].draws = draws; jobs[i].ndraws = ndraws; jobs[i].t = t; jobs[i].c = &c; jobs[i].scol = scol;
-        jobs[i].y0 = (int)((int64_t)c.H * i / nthreads);
-        jobs[i].y1 = (int)((int64_t)c.H * (i + 1) / nthreads);
+        lists[i] = (setup_rec*)malloc(sizeof(setup_rec) * (size_t)per_thread);
+        if (!lists[i]) rc = 3;
     }
-    if (nthreads == 1) run_band(&jobs[0]);
-    else {
-        for (int i = 0; i < nthreads; i++) pthread_create(&th[i], NULL, run_band, &jobs[i]);
-        for (int i = 0; i < nthreads; i++) pthread_join(th[i], NULL);
+    pthread_barrier_t bar;
+    if (!rc && pthread_barrier_init(&bar, NULL, (unsigned)nthreads) != 0) rc = 3;
+    if (!rc) {
+        for (int i = 0; i < nthreads; i++) {
+            jobs[i].draws = draws; jobs[i].ndraws = ndraws; jobs[i].t = t; jobs[i].c = &c; jobs[i].scol = scol;
+            jobs[i].win = win; jobs[i].id = i; jobs[i].nthreads = nthreads; jobs[i].bar = &bar;
+            jobs[i].lists = lists; jobs[i].counts = counts;
+            jobs[i].y0 = (int)((int64_t)c.H * i / nthreads);
+            jobs[i].y1 = (int)((int64_t)c.H * (i + 1) / nthreads);
+        }
+        if (nthreads == 1) run_pass(&jobs[0]);
+        else {
+            for (int i = 0; i < nthreads; i++) pthread_create(&th[i], NULL, run_pass, &jobs[i]);
+            for (int i = 0; i < nthreads; i++) pthread_join(th[i], NULL);
+        }
+        pthread_barrier_destroy(&bar);
     }
+    for (int i = 0; i < nthreads; i++) free(lists[i]);
+    free(win);
+    if (rc) { free(scol); return rc; }
     float invS = 1.0f / (float)S;
     for (size_t p = 0; p < npix; p++) {
         float acc[4];

@@ -26,6 +26,7 @@ typedef struct {
     int border_white;
     int max_aniso;              /* 1 disables anisotropic filtering */
     float lod_bias;
+    int compat;                 /* 1: the reference's sampler as written (pinning only; see oracle_fx.c) */
 } ofx_sampler;
 
 typedef struct {
@@ -67,6 +68,13 @@ typedef struct {
      * two sub-triangles (sub = 2 * edge or vertex + half) through the fill-mode rules; triangles
      * that need clipping are dropped in these modes. */
     int polygon_mode;
+    /* 1: blend factors from the reference's coefficient table as written
+     * (TileRasterRenderer.cpp:212-333, applied as TileRasterWorker.cpp:2346-2366): a factor is
+     * (k0 + k1 (1 - src.a) + k2 (1 - dst.a)) (1 - k3), which swaps SRC_ALPHA with
+     * ONE_MINUS_SRC_ALPHA and DST_ALPHA with ONE_MINUS_DST_ALPHA; only the six factors the
+     * reference supports (ZERO, ONE, SRC_ALPHA, ONE_MINUS_SRC_ALPHA, DST_ALPHA,
+     * ONE_MINUS_DST_ALPHA).  Pinning only; the GPU path blends by the factors' names. */
+    int blend_compat;
 } ofx_draw;
 
 typedef struct {

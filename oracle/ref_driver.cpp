@@ -58,9 +58,12 @@ extern "C" {
 // reference's ordered (optForceDeterministic) path.  Outputs: rgba (W*H*4 floats, row-major)
 // and depth (W*H floats).  Returns the median wall time of `timed` frames in milliseconds
 // after `warm` untimed frames (one frame when both are zero).
-double ref_render(const float* verts, int nverts, const int* indices, int ntris, const float* mvp,
-                  int W, int H, int depth_func, int deterministic, float* rgba, float* depth,
-                  int warm, int timed) {
+// blend: NULL, or 5 ints {enable, srcColor, dstColor, srcAlpha, dstAlpha} (IfritBlendFactor
+// numbering), set through TileRasterRenderer::setBlendFunc (TileRasterRenderer.cpp:212-333); a
+// blended draw takes the reference's in-order path (TileRasterWorker.cpp:410).
+double ref_render_ex(const float* verts, int nverts, const int* indices, int ntris, const float* mvp,
+                     int W, int H, int depth_func, int deterministic, const int* blend, float* rgba, float* depth,
+                     int warm, int timed) {
     auto renderer = std::make_shared<TileRasterRenderer>();
     renderer->Init();
 
@@ -99,6 +102,15 @@ double ref_render(const float* verts, int nverts, const int* indices, int ntris,
     renderer->bindFragmentShader(fs);
     renderer->SetDepthFunc((IfritCompareOp)depth_func);
     renderer->optsetForceDeterministic(deterministic != 0);
+    if (blend) {
+        IfritColorAttachmentBlendState bs;
+        bs.blendEnable = blend[0] != 0;
+        bs.srcColorBlendFactor = (IfritBlendFactor)blend[1];
+        bs.dstColorBlendFactor = (IfritBlendFactor)blend[2];
+        bs.srcAlphaBlendFactor = (IfritBlendFactor)blend[3];
+        bs.dstAlphaBlendFactor = (IfritBlendFactor)blend[4];
+        renderer->setBlendFunc(bs);
+    }
 
     std::vector<double> times;
     int total = warm + timed;
@@ -113,6 +125,13 @@ double ref_render(const float* verts, int nverts, const int* indices, int ntris,
     std::memcpy(depth, depthImg.getData(), sizeof(float) * (size_t)W * H);
     std::sort(times.begin(), times.end());
     return times.empty() ? 0.0 : times[times.size() / 2];
+}
+
+double ref_render(const float* verts, int nverts, const int* indices, int ntris, const float* mvp,
+                  int W, int H, int depth_func, int deterministic, float* rgba, float* depth,
+                  int warm, int timed) {
+    return ref_render_ex(verts, nverts, indices, ntris, mvp, W, H, depth_func, deterministic, nullptr, rgba, depth,
+                         warm, timed);
 }
 
 int ref_num_threads() { return TileRasterContext::numThreads; }

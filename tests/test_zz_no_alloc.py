@@ -36,7 +36,7 @@ def reference_render(v, f, mvp, W, H, S, attr, cull, depth_func, shading, textur
     return out
 
 
-def no_alloc_render(torch, v, f, mvp, W, H, S, attr, cull, depth_func, shading, texture=None, aniso=1):
+def no_alloc_render(torch, v, f, mvp, W, H, S, attr, cull, depth_func, shading, texture=None, aniso=1, expect=0):
     dev = torch.device("cuda")
     dv = torch.from_numpy(np.ascontiguousarray(v, np.float32)).to(dev)
     di = torch.from_numpy(np.ascontiguousarray(f, np.int32).reshape(-1)).to(dev)
@@ -63,7 +63,7 @@ def no_alloc_render(torch, v, f, mvp, W, H, S, attr, cull, depth_func, shading, 
         p.sampler = ig.SamplerState(1, 0, 0, 0, 0, int(aniso > 1), float(aniso), 0.0)
     stream = torch.cuda.current_stream(dev)
     rc = ig.load().iftrDrawNoAlloc(ctypes.byref(p), ctypes.c_void_p(stream.cuda_stream))
-    assert rc == 0, ig.load().iftrGetErrorString(rc)
+    assert rc == expect, ig.load().iftrGetErrorString(rc)
     torch.cuda.synchronize()
     return {"color": color.cpu().numpy().view(np.uint32), "depth": depth.cpu().numpy(), "vis": vis.cpu().numpy()}
 
@@ -92,8 +92,38 @@ def test_no_alloc_matches_renderer_on_two_calls_in_a_row():
     assert (second["vis"] >= 0).sum() > 50000
 
 
+def test_no_alloc_matches_the_oracle():
+    torch = pytest.importorskip("torch")
+    v, f, mvp = scenes.triangle_soup(6000, 33, 192, 128)
+    got = no_alloc_render(torch, v, f, mvp, 192, 128, 8, 2, ig.CULL_NONE, ig.LESS, ig.FS_GOURAUD)
+    d = O.make_draw(v, f, mvp, attr_offset=3, attr_count=2, cull_mode=0, depth_func=ig.LESS)
+    assert_same(got, O.render([d], 192, 128, 8))
+
+
+def test_no_alloc_overflow_then_next_call_is_correct():
+    """More (triangle, tile) overlaps than IFTR_NOALLOC_MAX_TILE_PAIRS: the call reports
+    IFTR_ERR_OVERFLOW (its outputs are undefined), and the next call on the same scratch is right."""
+    torch = pytest.importorskip("torch")
+    W, H = 2048, 1024  # 8,192 tiles and 2,097,152 samples: both at their limits
+    n = 100  # each triangle covers every tile: 819,200 overlaps > 524,288
+    z = np.linspace(0.2, 0.8, n, dtype=np.float32)
+    v = np.zeros((3 * n, 6), np.float32)
+    for i in range(n):
+        v[3 * i:3 * i + 3, 0:3] = [[-1, -1, z[i]], [3, -1, z[i]], [-1, 3, z[i]]]
+        v[3 * i:3 * i + 3, 3:6] = (i % 7) / 7.0
+    f = np.arange(3 * n, dtype=np.int32).reshape(-1, 3)
+    no_alloc_render(torch, v, f, np.eye(4, dtype=np.float32), W, H, 1, 3, ig.CULL_NONE, ig.LESS_OR_EQUAL,
+                    ig.FS_GOURAUD, expect=4)
+    v2, f2, mvp2 = scenes.triangle_soup(3000, 8, 256, 128)
+    args = (v2, f2, mvp2, 256, 128, 4, 2, ig.CULL_NONE, ig.LESS_OR_EQUAL, ig.FS_GOURAUD)
+    assert_same(no_alloc_render(torch, *args), reference_render(*args))
+
+
 def test_no_alloc_rejects_sizes_over_its_limits():
     p = ig.NoAllocPass()
     p.width, p.height, p.samples = 4096, 4096, 4  # far above IFTR_NOALLOC_MAX_SAMPLES
     p.strideFloats, p.color, p.depth = 3, 1, 1
+    assert ig.load().iftrDrawNoAlloc(ctypes.byref(p), None) == 1
+    # within the sample and tile limits, but wider than the 16384-pixel cap of every entry point
+    p.width, p.height, p.samples = 40000, 48, 1
     assert ig.load().iftrDrawNoAlloc(ctypes.byref(p), None) == 1
