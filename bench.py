@@ -1,26 +1,36 @@
 """Benchmark of the GB300 software rasterizer (one JSON line on rank 0).
 
-Workload (default ``c2``): 1,000,000 unshared random triangles (centres uniform in the view
-frustum, log-normal edges, depth complexity ~6), each vertex with a float32 UV; 1920x1080
-RGBA8 target with 4x MSAA and float32 depth (LEQUAL); shading samples a seeded 1024x1024
-RGBA8 value-noise texture with a full mip chain, trilinear + 8x anisotropic filtering from
-quad derivatives.  ``c1`` is the plain 512x512 Gouraud icosphere frame.
+Workload (default ``c5``, the largest single-GPU configuration): the stress frame, 3840x2160
+RGBA16F with 8x MSAA and float32 depth (LEQUAL), 10,035,200 triangles from 40 displaced geodesic
+icospheres with random transforms (depth complexity ~8), a 4096x4096 RGBA8 texture with full
+mips and 16x anisotropic filtering, 4 of the 40 instances alpha-blended back to front in one
+ordered pass.  The same line carries the other configurations as sub-keys: ``plain_c2`` (1M
+random triangles, 1920x1080 RGBA8 4x MSAA, 1024^2 texture, 8x anisotropic), ``batched_c3`` (256
+views in one persistent pass replayed from a CUDA graph) and ``differentiable_c4`` (64 views at
+256^2, forward + backward).  ``--workload c1|c2|c3|c4`` prints that configuration's own line.
 
-A step is one render pass (binning, raster, shading, resolve) of the whole frame.
-  value      shaded samples/s with geometry and texture resident in HBM; L2 is flushed
-             (256 MB write) before every timed step; per-step device time from CUDA events.
+A step is one render pass (binning, raster, shading, ordered stage, resolve) of the whole frame.
+  value      shaded samples/s with geometry and texture resident in HBM (inputs larger than L2;
+             C2 flushes L2 with a 256 MB write before every timed step); per-step device time
+             from CUDA events on the renderer's stream.
   e2e        the same metric through the reference-style C-ABI with host buffers: each step
-             uploads the pinned vertex + index buffers (marked rewritten), draws
-             synchronously (iftrDrawLegacy) and reads the resolved colour back to pinned host
-             memory; host wall time.
-  roofline   the tile kernel (the dominant kernel) against measured HBM bandwidth.
-  cpu_baseline  the multithreaded CPU oracle (a port of the reference's CPU pipeline with
-             this path's MSAA and texturing) on one full frame, rank 0 only.
+             uploads the pinned vertex + index buffers (marked rewritten), draws and reads the
+             resolved colour back to pinned host memory; host wall time.
+  roofline   the tile stage (raster + shade + ordered kernels, which produce every output byte)
+             against measured HBM bandwidth.
+  cpu_baseline  the CPU oracle (a restatement of the reference's CPU pipeline with this path's
+             MSAA and texturing, one set-up per triangle, deferred shading of unblended passes)
+             on a bounded sample of the same frame, rank 0 only.
+  cpu_baseline_reference  the reference's own CPU renderer (TileRasterRenderer::drawElements,
+             built by oracle/build_ref.py from the staged reference tree; AVX2 on x86, its scalar
+             build elsewhere) on the plain 512x512 icosphere frame, the one configuration it
+             supports (no MSAA, no texturing), with the core count it used.
 
-``--impl reference`` times the reference-side CPU implementation of the path on the host
-cores instead (the reference's own CPU renderer has no MSAA or texturing, so the port
-stands in for it on this workload).  Multi-GPU runs render independent replicas (the frame
-does not shard), report ``scaling: weak`` and take the max time over ranks.
+``--impl reference`` times the reference-side CPU implementation on the host cores instead: the
+oracle on a bounded sample of the same stress frame per step (the reference renderer has no
+MSAA or texturing), plus the reference renderer's own plain-frame time.  Multi-GPU runs render
+independent replicas of the single frame (it does not shard), report ``scaling: weak`` and take
+the max time over ranks.
 """
 import argparse
 import json
@@ -49,9 +59,12 @@ def parse():
     p.add_argument("--steps", type=int, default=20)
     p.add_argument("--warmup", type=int, default=5)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    p.add_argument("--workload", default="c2", choices=["c1", "c2", "c3", "c4", "c5"])
+    p.add_argument("--workload", default="c5", choices=["c1", "c2", "c3", "c4", "c5"])
     p.add_argument("--e2e-steps", type=int, default=10)
-    p.add_argument("--no-batch", action="store_true", help="leave the batched (c3) summary out of the c2 line")
+    p.add_argument("--no-extras", action="store_true", help="leave the c2/c3/c4 summaries out of the c5 line")
+    p.add_argument("--reduced", action="store_true",
+                   help="profiling case of the stress frame: 1920x1080, 40 instances of frequency 56 (2,508,800 "
+                        "triangles), 2048^2 texture; not a bench configuration")
     return p.parse_args()
 
 
@@ -174,42 +187,80 @@ def cpu_oracle_frame(w, nthreads, frames=1):
     return statistics.median(times), shaded
 
 
+def spawn_ranks_if_needed(n):
+    """`--gpus N` (N > 1) started without a launcher re-runs this script under
+    torch.distributed.run with N ranks on 127.0.0.1 and exits with its status; started by a
+    launcher with a different world size, it stops with an error."""
+    world = int(os.environ.get("WORLD_SIZE", "0"))
+    if n <= 1 and world <= 1:
+        return
+    if world == 0:
+        import socket
+        with socket.socket() as sk:
+            sk.bind(("127.0.0.1", 0))
+            port = sk.getsockname()[1]
+        cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", "--nproc-per-node", str(n),
+               "--master-addr", "127.0.0.1", "--master-port", str(port)] + sys.argv
+        sys.exit(subprocess.call(cmd))
+    if world != n:
+        raise SystemExit("bench.py: --gpus %d but the launcher started %d ranks" % (n, world))
+
+
 def dist_setup(n):
-    if n <= 1 or int(os.environ.get("WORLD_SIZE", "1")) <= 1:
+    if n <= 1 and int(os.environ.get("WORLD_SIZE", "1")) <= 1:
         return 0, 1, None
     import torch
     import torch.distributed as dist
     rank, world = int(os.environ["RANK"]), int(os.environ["WORLD_SIZE"])
+    if world != n:
+        raise SystemExit("bench.py: --gpus %d but WORLD_SIZE is %d" % (n, world))
     torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
     dist.init_process_group("nccl")
     return rank, world, dist
 
 
 def run_reference(args):
+    """Reference arm: the CPU implementation of the path on the host cores, rank 0 only.  The
+    stress frame (default) runs the oracle on a bounded sample per step (C5_SAMPLE); c1/c2 run
+    one full frame of the oracle per step.  The reference renderer's own plain-frame time is
+    added as cpu_baseline_reference."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
-    w = workload(args.workload)
     nthreads = os.cpu_count() or 1
+    if args.workload == "c5":
+        from ifrit_gb300 import scenes
+        sc = scenes.c5_scene()
+        step = lambda: c5_oracle_sample(sc, nthreads)  # noqa: E731
+        cfg = {"workload": "stress: 3840x2160 RGBA16F + D32 LEQUAL, 8x MSAA, %d triangles from 40 displaced "
+                           "geodesic icospheres (frequency 112) with random transforms, depth complexity ~8, "
+                           "4096^2 RGBA8 texture with full mips, 16x anisotropic, 4 of 40 instances "
+                           "alpha-blended back to front (one ordered pass)" % len(sc["indices"]),
+               "width": sc["width"], "height": sc["height"], "samples": 8, "triangles": int(len(sc["indices"]))}
+        sample = C5_SAMPLE
+    else:
+        w = workload(args.workload)
+        step = lambda: cpu_oracle_frame(w, nthreads)  # noqa: E731
+        cfg = {"workload": w["desc"], "width": w["W"], "height": w["H"], "samples": w["S"],
+               "triangles": int(len(w["indices"]))}
+        sample = "one full frame of the same workload per step"
     for _ in range(args.warmup):
-        cpu_oracle_frame(w, nthreads)
+        step()
     times, shaded = [], 0
     for _ in range(args.steps):
-        t, shaded = cpu_oracle_frame(w, nthreads)
+        t, shaded = step()
         times.append(t)
     ms = 1000.0 * statistics.mean(times)
     value = shaded / (ms / 1000.0)
     line = {
         "metric": METRIC, "value": value, "unit": "samples/s", "impl": "reference", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f32+i64", "data": "synthetic (seeded)",
-        "config": {"workload": w["desc"], "width": w["W"], "height": w["H"], "samples": w["S"],
-                   "triangles": int(len(w["indices"]))},
-        "tris_per_s": len(w["indices"]) / (ms / 1000.0),
+        "vs_baseline": None, "dtype": "f32+i64", "data": "synthetic (seeded)", "config": cfg,
         "cpu_baseline": {"value": value, "unit": "samples/s", "cores": nthreads, "kind": "port",
-                         "sample": "one full frame per step (the reference CPU renderer has no MSAA or texturing; "
-                                   "its multithreaded CPU pipeline is run as the oracle port)"},
+                         "sample": sample + " (the reference's CPU renderer has no MSAA or texturing, so the "
+                                            "oracle, a restatement of its pipeline with this path's features, runs)"},
         "e2e": {"value": value, "unit": "samples/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "cpu_baseline_reference": reference_c1_baseline(),
     }
     print(json.dumps(line), flush=True)
 
@@ -221,17 +272,22 @@ def c3_algorithmic_bytes(views):
                    for v in views))
 
 
-def run_c3(args, steps, warmup, e2e_steps, with_cpu=True):
+def run_c3(args, steps, warmup, e2e_steps, with_cpu=True, rank=0, world=1, dist=None):
     """Batched workload: 256 views (edges U{128,256,512,1024}, 1x/4x, 1k-200k triangles
-    log-uniform, icospheres or soups, Gouraud).  Returns a dict of measurements."""
+    log-uniform, icospheres or soups, Gouraud).  With several ranks every rank renders its
+    contiguous share of the views (ifrit_gb300.sharding.view_range; no exchange on the data path)
+    and the result sums the ranks' samples over the slowest rank's time.  Returns a dict."""
     import torch
     import ifrit_gb300 as ig
     from ifrit_gb300 import scenes
     from ifrit_gb300.batch import BatchRenderer
+    from ifrit_gb300.sharding import view_range
 
     dev = torch.device("cuda", torch.cuda.current_device())
     stream = torch.cuda.current_stream(dev)
     views = scenes.c3_batch()
+    vb, ve = view_range(len(views), rank, world)
+    views = views[vb:ve]
     T = sum(len(v["indices"]) for v in views)
 
     def build(subset, vis):
@@ -271,9 +327,23 @@ def run_c3(args, steps, warmup, e2e_steps, with_cpu=True):
     br.draw()  # sizes, tunes, captures
     br.finish()
     clocks.start()
+    if dist:
+        dist.barrier()
     ms = time_batch(br, steps, warmup)
     clk = clocks.stop(torch.cuda.current_device())
     tuning = br.tuning()
+    if world > 1:  # sharded batch: total samples over the slowest rank's time
+        tot = torch.tensor([float(sum(shaded)), float(T)], dtype=torch.float64, device=dev)
+        dist.all_reduce(tot, op=dist.ReduceOp.SUM)
+        mx = torch.tensor([ms], device=dev)
+        dist.all_reduce(mx, op=dist.ReduceOp.MAX)
+        br.close()
+        ms = float(mx.item())
+        return {"value": float(tot[0]) / (ms / 1000.0), "ms_per_step": ms, "tris_per_s": float(tot[1]) / (ms / 1000.0),
+                "kernels_per_step": 3 + 2 * len(set(v["samples"] for v in views)), "views": 256,
+                "views_per_rank": len(views), "triangles": int(tot[1]), "tuning": {"tile_size": tuning[0],
+                                                                                   "ctas_per_sm": tuning[1]},
+                "clocks": clk, "sharding": "views %d-%d on rank %d of %d" % (vb, ve, rank, world)}
     # end to end: pinned host geometry uploaded every step, colours read back every step
     host_in = [(torch.from_numpy(v["vertices"]).pin_memory(), torch.from_numpy(v["indices"].reshape(-1)).pin_memory())
                for v in views]
@@ -411,19 +481,23 @@ def run_c3(args, steps, warmup, e2e_steps, with_cpu=True):
     return out
 
 
-def run_c4(steps, warmup, with_cpu=True):
+def run_c4(steps, warmup, with_cpu=True, rank=0, world=1, dist=None):
     """Differentiable workload: 64 views at 256x256 float32 RGB of a 20,480-triangle icosphere
     (per-vertex colours, UVs, positions with noise std 0.05), 256x256 float32 texture, L2 loss
     against images of the clean positions.  Times the forward (visibility + shading +
-    antialiasing) and forward + backward per step with CUDA events, L2 flushed before each."""
+    antialiasing) and forward + backward per step with CUDA events, L2 flushed before each.
+    With several ranks every rank renders its contiguous share of the views and the step ends
+    with the sum of the mesh gradients over the ranks (ifrit_gb300.sharding)."""
     import torch
     from ifrit_gb300 import scenes
     from ifrit_gb300.diff import DiffRenderer
+    from ifrit_gb300.sharding import allreduce_gradients, view_range
 
     dev = torch.device("cuda", torch.cuda.current_device())
     stream = torch.cuda.current_stream(dev)
     sc = scenes.c4_scene()
-    dr = DiffRenderer(sc["faces"], len(sc["clean"]), sc["width"], sc["height"], sc["mvps"], sc["texture"])
+    vb, ve = view_range(len(sc["mvps"]), rank, world)
+    dr = DiffRenderer(sc["faces"], len(sc["clean"]), sc["width"], sc["height"], sc["mvps"][vb:ve], sc["texture"])
     t = {k: torch.from_numpy(sc[k]).to(dev) for k in ("clean", "noisy", "colors", "uvs")}
     with torch.no_grad():
         target = dr.forward(t["clean"], t["colors"], t["uvs"])[0]
@@ -440,6 +514,8 @@ def run_c4(steps, warmup, with_cpu=True):
         pos.grad = col.grad = uv.grad = None
         loss = ((dr.render(pos, col, uv) - target) ** 2).sum()
         loss.backward()
+        if world > 1:
+            allreduce_gradients([pos.grad, col.grad, uv.grad])
         return loss
 
     def timed(fn):
@@ -465,6 +541,14 @@ def run_c4(steps, warmup, with_cpu=True):
     vis = dr.forward(t["noisy"], t["colors"], t["uvs"])[2]
     covered = int((vis >= 0).sum().item())
     N, H, W = dr.N, dr.H, dr.W
+    if world > 1:  # all ranks' covered samples over the slowest rank's time
+        tot = torch.tensor([float(covered), float(N)], dtype=torch.float64, device=dev)
+        dist.all_reduce(tot, op=dist.ReduceOp.SUM)
+        mx = torch.tensor([ms_f, ms_fb], device=dev)
+        dist.all_reduce(mx, op=dist.ReduceOp.MAX)
+        covered, N = int(tot[0]), int(tot[1])
+        ms_f, ms_fb = float(mx[0]), float(mx[1])
+        with_cpu = False
     out = {"views": N, "width": W, "height": H, "triangles": dr.T, "ms_forward": ms_f, "ms_forward_backward": ms_fb,
            "ratio": ms_fb / ms_f, "covered_pixels": covered, "value": covered / (ms_fb / 1000.0),
            "forward_samples_per_s": covered / (ms_f / 1000.0), "clocks": clk,
@@ -505,18 +589,21 @@ def run_c4(steps, warmup, with_cpu=True):
 
 def run_ours_c4(args):
     rank, world, dist = dist_setup(args.gpus)
-    res = run_c4(args.steps, args.warmup)
+    res = run_c4(args.steps, args.warmup, with_cpu=(world == 1), rank=rank, world=world, dist=dist)
     if rank != 0:
         return
-    line = {"metric": "covered samples/s through forward + backward", "value": world * res["value"],
+    line = {"metric": "covered samples/s through forward + backward", "value": res["value"],
             "unit": "samples/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
-            "ms_per_step": res["ms_forward_backward"], "higher_is_better": True, "scaling": "weak",
+            "ms_per_step": res["ms_forward_backward"], "higher_is_better": True,
+            "scaling": "strong" if world > 1 else "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
             "config": {"workload": "differentiable: %d views %dx%d float32 RGB, %d-triangle icosphere (colours, UVs, "
                                    "positions with noise std 0.05), 256^2 float32 texture, L2 loss; forward = visibility "
                                    "+ shading + silhouette antialiasing, backward = hand-written adjoint"
                                    % (res["views"], res["width"], res["height"], res["triangles"]),
-                       "l2": "flushed before every timed step (256 MB write)", "parallelism": "single"},
+                       "l2": "flushed before every timed step (256 MB write)",
+                       "parallelism": "views sharded over %d ranks, gradient all-reduce" % world if world > 1
+                       else "single"},
             "ms_forward": res["ms_forward"], "fwd_bwd_over_fwd": res["ratio"],
             "gpu_launches": res["kernels_forward_backward"] * args.steps, "clocks": res["clocks"],
             "e2e": None}
@@ -551,6 +638,53 @@ def c5_algorithmic_bytes(sc):
     return int(sc["vertices"].nbytes + sc["indices"].nbytes + P * 8 * 4 + P * 8 + total * 4 + P * 8)
 
 
+C5_REDUCED = dict(width=1920, height=1080, frequency=56, tex_size=2048)
+
+
+def c5_oracle_sample(sc, nthreads):
+    """The CPU oracle on a bounded sample of the stress frame at full resolution: the first two
+    (opaque) instances and the first blended one, in pass order.  Returns (seconds, shaded)."""
+    from oracle import oracle as O
+    chain, levels = O.build_mips(sc["texture"])
+    tex = (chain, levels, sc["texture"].shape[1], sc["texture"].shape[0])
+    picked = sc["draws"][:2] + [d for d in sc["draws"] if d["blend"]][:1]
+    draws = []
+    for d in picked:
+        f = sc["indices"][d["first"] // 3:(d["first"] + d["count"]) // 3]
+        draws.append(O.make_draw(sc["vertices"], f, d["mvp"], attr_offset=3, attr_count=2, cull_mode=2, depth_func=3,
+                                 depth_write=int(not d["blend"]), blend=(6, 7, 1, 7) if d["blend"] else None,
+                                 shading=O.SHADE_TEXTURED, texture=tex, sampler={"max_aniso": 16}))
+    t0 = time.perf_counter()
+    res = O.render(draws, sc["width"], sc["height"], 8, O.FMT_RGBA16F, nthreads=nthreads)
+    return time.perf_counter() - t0, int((res["vis"] >= 0).sum())
+
+
+C5_SAMPLE = ("oracle on 3 of the 40 instances (the first two opaque ones and the first blended one) at full "
+             "3840x2160 8x resolution per step; samples/s of that sub-frame")
+
+
+def reference_c1_baseline(frames=20, warm=3):
+    """The reference's own CPU renderer (TileRasterRenderer::drawElements) on the plain 512x512
+    icosphere frame: default (tag-buffer) path and in-order (deterministic) path, depth LESS."""
+    from oracle import ref_renderer as R
+    lib, kind = R.load()
+    if lib is None:
+        return {"unavailable": kind}
+    w = workload("c1")
+    _, depth, ms = R.render(lib, w["vertices"], w["indices"], w["mvp"], w["W"], w["H"], depth_func=1,
+                            deterministic=False, warm=warm, timed=frames)
+    covered = int((depth < 1e30).sum())
+    _, _, ms_det = R.render(lib, w["vertices"], w["indices"], w["mvp"], w["W"], w["H"], depth_func=1,
+                            deterministic=True, warm=warm, timed=frames)
+    threads = R.num_threads(lib)
+    return {"value": covered / (ms / 1000.0), "unit": "samples/s", "cores": threads + 1, "kind": "reference",
+            "sample": "reference CPU renderer (%s, %d worker threads + the calling thread) on the plain 512x512 "
+                      "Gouraud icosphere frame, 20,480 triangles, 1x, depth LESS: median of %d frames after %d "
+                      "warm-up; its only supported configuration (no MSAA or texturing)" % (kind, threads, frames, warm),
+            "workload": "c1", "ms_per_frame": ms, "tris_per_s": len(w["indices"]) / (ms / 1000.0),
+            "ms_per_frame_in_order_path": ms_det, "covered_pixels": covered}
+
+
 def run_ours_c5(args):
     import torch
     import ifrit_gb300 as ig
@@ -559,7 +693,7 @@ def run_ours_c5(args):
     rank, world, dist = dist_setup(args.gpus)
     dev = torch.device("cuda", torch.cuda.current_device())
     stream = torch.cuda.current_stream(dev)
-    sc = scenes.c5_scene()
+    sc = scenes.c5_scene(**C5_REDUCED) if args.reduced else scenes.c5_scene()
     W, H = sc["width"], sc["height"]
     r = ig.Renderer(W, H, 8, ig.FORMAT_RGBA16F, visibility=True)
     r.set_stream(stream.cuda_stream)
@@ -574,6 +708,9 @@ def run_ours_c5(args):
     clocks = ClockSampler()
     clocks.start()
     ms, stages = [], []
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
     for _ in range(args.steps):
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(stream)
@@ -584,6 +721,11 @@ def run_ours_c5(args):
         stages.append(r.stage_times())
     clk = clocks.stop(torch.cuda.current_device())
     r.set_stage_timing(False)
+    m = statistics.mean(ms)
+    if dist:
+        t = torch.tensor([m], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        m = float(t.item())
     out = torch.empty((H, W), dtype=torch.int64, pin_memory=True).numpy()
     e2e = []
     for i in range(max(1, args.e2e_steps) + 1):
@@ -593,10 +735,21 @@ def run_ours_c5(args):
         r.color_into(out)
         if i:
             e2e.append(time.perf_counter() - t0)
-    m = statistics.mean(ms)
+    e2e_s = statistics.mean(e2e)
+    if dist:
+        t = torch.tensor([e2e_s], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    r.close()
+    del r
+    torch.cuda.empty_cache()
+    if rank != 0:
+        dist.barrier()
+        return
     B = c5_algorithmic_bytes(sc)
     peak, peak_kind = peak_hbm()
     st = [statistics.mean(x[i] for x in stages) for i in range(6)]
+    t_tile = (st[3] + st[4] + st[5]) / 1000.0
     T = len(sc["indices"])
     line = {"metric": METRIC, "value": world * shaded / (m / 1000.0), "unit": "samples/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": m, "higher_is_better": True, "scaling": "weak",
@@ -606,63 +759,80 @@ def run_ours_c5(args):
                                    "4096^2 RGBA8 texture with full mips, 16x anisotropic, 4 of 40 instances "
                                    "alpha-blended back to front (one ordered pass)" % T,
                        "width": W, "height": H, "samples": 8, "triangles": T, "shaded_samples_per_frame": shaded,
-                       "l2": "inputs larger than L2 (no flush)", "parallelism": "single"},
-            "tris_per_s": T / (m / 1000.0),
+                       "l2": "inputs larger than L2 (no flush)", "parallelism": "replicas" if world > 1 else "single"},
+            "tris_per_s": world * T / (m / 1000.0),
             "stage_ms": {"binning": st[0] + st[1] + st[2], "raster": st[3], "shade": st[4], "ordered": st[5]},
-            "roofline": {"bound": "hbm", "achieved": B / (m / 1000.0) / 1e9, "peak": peak, "unit": "GB/s",
-                         "frac": B / (m / 1000.0) / 1e9 / peak, "traffic": None, "algorithmic_bytes": B,
-                         "kernel": "whole pass", "peak_source": peak_kind},
-            "e2e": {"value": shaded / statistics.mean(e2e), "unit": "samples/s",
+            "roofline": {"bound": "hbm", "achieved": B / t_tile / 1e9, "peak": peak, "unit": "GB/s",
+                         "frac": B / t_tile / 1e9 / peak, "traffic": profiled_traffic("c5"), "algorithmic_bytes": B,
+                         "kernel": "tile stage (raster + shade + ordered kernels)", "peak_source": peak_kind},
+            "pass_roofline_frac": B / (m / 1000.0) / 1e9 / peak,
+            "e2e": {"value": world * shaded / e2e_s, "unit": "samples/s",
                     "h2d_bytes_per_step": int(sc["vertices"].nbytes + sc["indices"].nbytes),
-                    "d2h_bytes_per_step": int(out.nbytes), "ms_per_step": 1000.0 * statistics.mean(e2e)},
+                    "d2h_bytes_per_step": int(out.nbytes), "ms_per_step": 1000.0 * e2e_s},
             # count, scan, scatter, raster, shade, ordered (one launch group; 4K = 32,400 tiles,
             # one scan launch)
             "gpu_launches": 6 * args.steps, "clocks": clk}
-    r.close()
-    # CPU oracle on a bounded sample: the first two instances of the pass at full resolution
-    from oracle import oracle as O
-    chain, levels = O.build_mips(sc["texture"])
-    tex = (chain, levels, sc["texture"].shape[1], sc["texture"].shape[0])
-    draws = []
-    for d in sc["draws"][:2]:
-        f = sc["indices"][d["first"] // 3:(d["first"] + d["count"]) // 3]
-        draws.append(O.make_draw(sc["vertices"], f, d["mvp"], attr_offset=3, attr_count=2, cull_mode=2, depth_func=3,
-                                 depth_write=int(not d["blend"]), blend=(6, 7, 1, 7) if d["blend"] else None,
-                                 shading=O.SHADE_TEXTURED, texture=tex, sampler={"max_aniso": 16}))
+    if args.reduced:
+        line["config"]["workload"] = "profiling case (not the bench configuration): stress frame at %dx%d, %d " \
+                                     "triangles, 2048^2 texture" % (W, H, T)
+        print(json.dumps(line), flush=True)
+        return
     nthreads = os.cpu_count() or 1
-    t0 = time.perf_counter()
-    res = O.render(draws, W, H, 8, O.FMT_RGBA16F, nthreads=nthreads)
-    dt = time.perf_counter() - t0
-    line["cpu_baseline"] = {"value": int((res["vis"] >= 0).sum()) / dt, "unit": "samples/s", "cores": nthreads,
-                            "kind": "port", "sample": "oracle on the first 2 of the 40 instances at full resolution"}
+    dt, done = c5_oracle_sample(sc, nthreads)
+    line["cpu_baseline"] = {"value": done / dt, "unit": "samples/s", "cores": nthreads, "kind": "port",
+                            "sample": C5_SAMPLE}
+    if not args.no_extras and world == 1:
+        del sc
+        res2 = measure_frame(workload("c2"), 10, 3, 3)
+        line["plain_c2"] = {k: res2[k] for k in ("value", "ms_per_step", "tris_per_s", "stage_ms", "roofline",
+                                                 "pass_roofline_frac", "e2e")}
+        line["plain_c2"]["workload"] = workload("c2")["desc"]
+        res1 = measure_frame(workload("c1"), 20, 3, 3)
+        line["plain_c1"] = {k: res1[k] for k in ("value", "ms_per_step", "tris_per_s", "e2e")}
+        torch.cuda.empty_cache()
+        res3 = run_c3(args, 5, 3, 3, with_cpu=False)
+        line["batched_c3"] = {k: res3[k] for k in ("value", "ms_per_step", "tris_per_s", "views", "triangles", "tuning",
+                                                    "plain", "small_views", "overhead_bound_small_views", "roofline",
+                                                    "e2e")}
+        torch.cuda.empty_cache()
+        res4 = run_c4(5, 3, with_cpu=False)
+        line["differentiable_c4"] = {k: res4[k] for k in ("views", "width", "height", "triangles", "ms_forward",
+                                                          "ms_forward_backward", "ratio", "value")}
+    line["cpu_baseline_reference"] = reference_c1_baseline()
     print(json.dumps(line), flush=True)
+    if dist:
+        dist.barrier()
 
 
 def run_ours_c3(args):
     rank, world, dist = dist_setup(args.gpus)
-    res = run_c3(args, args.steps, args.warmup, args.e2e_steps)
+    res = run_c3(args, args.steps, args.warmup, args.e2e_steps, with_cpu=(world == 1), rank=rank, world=world,
+                 dist=dist)
     if rank != 0:
         return
-    line = {"metric": METRIC, "value": world * res["value"], "unit": "samples/s", "n_gpus": world,
+    line = {"metric": METRIC, "value": res["value"], "unit": "samples/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": res["ms_per_step"], "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f32+i64", "data": "synthetic (seeded)",
+            "scaling": "strong" if world > 1 else "weak", "vs_baseline": None, "dtype": "f32+i64",
+            "data": "synthetic (seeded)",
             "config": {"workload": "batched: %d views (edges U{128,256,512,1024}, 1x/4x MSAA 50/50, RGBA8 + D32), "
                                    "%d triangles (1k-200k per view, log-uniform; geodesic icospheres or random soups), "
                                    "Gouraud, one persistent pass replayed from a CUDA graph" % (res["views"], res["triangles"]),
-                       "l2": "inputs larger than L2 (no flush)", "parallelism": "single"},
-            "tris_per_s": world * res["tris_per_s"], "gpu_launches": res["kernels_per_step"] * args.steps}
+                       "l2": "inputs larger than L2 (no flush)",
+                       "parallelism": "views sharded over %d ranks" % world if world > 1 else "single"},
+            "tris_per_s": res["tris_per_s"], "gpu_launches": res["kernels_per_step"] * args.steps}
     line.update({k: res[k] for k in ("roofline", "e2e", "clocks", "plain", "small_views", "overhead_bound_small_views",
-                                     "tuning", "cpu_baseline")})
+                                     "tuning", "cpu_baseline", "sharding") if k in res})
+    if "e2e" not in line:
+        line["e2e"] = None
     print(json.dumps(line), flush=True)
 
 
-def run_ours(args):
+def measure_frame(w, steps, warmup, e2e_steps, dist=None, world=1):
+    """Plain one-pass-per-frame measurement of a c1/c2 workload.  Returns a dict."""
     import torch
     import ifrit_gb300 as ig
 
-    rank, world, dist = dist_setup(args.gpus)
     dev = torch.device("cuda", torch.cuda.current_device())
-    w = workload(args.workload)
     r = ig.Renderer(w["W"], w["H"], w["S"], ig.FORMAT_RGBA8, visibility=True)
     stream = torch.cuda.current_stream(dev)
     r.set_stream(stream.cuda_stream)
@@ -677,19 +847,19 @@ def run_ours(args):
     r.lib.iftrSetVisibilityOutput(r.h, 0)
     r.set_stage_timing(True)
     flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device=dev)
-    for _ in range(args.warmup):
+    for _ in range(warmup):
         flush.fill_(1)
         r.draw_async(clear=True)
         r.finish()
-    ev0 = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
-    ev1 = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ev0 = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+    ev1 = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
     tile_ms, bin_ms, raster_ms, shade_ms = [], [], [], []
     clocks = ClockSampler()
+    clocks.start()
     if dist:
         dist.barrier()
     torch.cuda.synchronize()
-    clocks.start()
-    for i in range(args.steps):
+    for i in range(steps):
         flush.fill_(i & 255)
         ev0[i].record(stream)
         r.draw_async(clear=True)
@@ -702,18 +872,16 @@ def run_ours(args):
         tile_ms.append(st[3] + st[4])
     torch.cuda.synchronize()
     clk = clocks.stop(torch.cuda.current_device())
-    step_ms = [a.elapsed_time(b) for a, b in zip(ev0, ev1)]
-    ms = statistics.mean(step_ms)
+    ms = statistics.mean(a.elapsed_time(b) for a, b in zip(ev0, ev1))
     if dist:
         t = torch.tensor([ms], device=dev)
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         ms = float(t.item())
-
     # end to end through the C-ABI with host buffers
     r.set_stage_timing(False)
     out = torch.empty(w["W"] * w["H"], dtype=torch.int32, pin_memory=True).numpy()
     e2e_times = []
-    for i in range(max(1, args.e2e_steps) + 2):
+    for i in range(max(1, e2e_steps) + 2):
         t0 = time.perf_counter()
         r.mark_geometry_dirty()
         r.draw(clear=True)
@@ -725,56 +893,60 @@ def run_ours(args):
         t = torch.tensor([e2e_s], device=dev)
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         e2e_s = float(t.item())
-    if rank != 0:
-        dist.barrier()
-        return
-
+    r.close()
     B = algorithmic_bytes(w)
     peak, peak_kind = peak_hbm()
     t_tile = statistics.mean(tile_ms) / 1000.0
     achieved = B / t_tile / 1e9
-    line = {
-        "metric": METRIC, "value": world * shaded / (ms / 1000.0), "unit": "samples/s", "n_gpus": world,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f32+i64", "data": "synthetic (seeded)",
-        "config": {"workload": w["desc"], "width": w["W"], "height": w["H"], "samples": w["S"],
-                   "triangles": int(len(w["indices"])), "shaded_samples_per_frame": shaded,
-                   "l2": "flushed before every timed step (256 MB write)",
-                   "parallelism": "replicas" if world > 1 else "single"},
+    return {
+        "value": world * shaded / (ms / 1000.0), "ms_per_step": ms, "shaded": shaded,
         "tris_per_s": world * len(w["indices"]) / (ms / 1000.0),
         "stage_ms": {"binning": statistics.mean(bin_ms), "raster": statistics.mean(raster_ms),
                      "shade": statistics.mean(shade_ms)},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "traffic": profiled_traffic(w["name"]), "algorithmic_bytes": B, "kernel": "tile_kernel",
-                     "peak_source": peak_kind},
+                     "traffic": profiled_traffic(w["name"]), "algorithmic_bytes": B,
+                     "kernel": "tile stage (raster + shade kernels)", "peak_source": peak_kind},
         "pass_roofline_frac": B / (ms / 1000.0) / 1e9 / peak,
         "e2e": {"value": world * shaded / e2e_s, "unit": "samples/s",
                 "h2d_bytes_per_step": int(w["vertices"].nbytes + w["indices"].nbytes),
                 "d2h_bytes_per_step": int(out.nbytes), "ms_per_step": 1000.0 * e2e_s},
-        "gpu_launches": KERNELS_PER_PASS * args.steps,
-        "clocks": clk,
+        "gpu_launches": KERNELS_PER_PASS * steps, "clocks": clk,
     }
+
+
+def run_ours(args):
+    rank, world, dist = dist_setup(args.gpus)
+    w = workload(args.workload)
+    res = measure_frame(w, args.steps, args.warmup, args.e2e_steps, dist, world)
+    if rank != 0:
+        dist.barrier()
+        return
+    line = {
+        "metric": METRIC, "value": res["value"], "unit": "samples/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": res["ms_per_step"], "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32+i64", "data": "synthetic (seeded)",
+        "config": {"workload": w["desc"], "width": w["W"], "height": w["H"], "samples": w["S"],
+                   "triangles": int(len(w["indices"])), "shaded_samples_per_frame": res["shaded"],
+                   "l2": "flushed before every timed step (256 MB write)",
+                   "parallelism": "replicas" if world > 1 else "single"},
+    }
+    for k in ("tris_per_s", "stage_ms", "roofline", "pass_roofline_frac", "e2e", "gpu_launches", "clocks"):
+        line[k] = res[k]
     nthreads = os.cpu_count() or 1
     t_cpu, shaded_cpu = cpu_oracle_frame(w, nthreads, frames=2)
     line["cpu_baseline"] = {"value": shaded_cpu / t_cpu, "unit": "samples/s", "cores": nthreads, "kind": "port",
                             "sample": "one full frame of the same workload (median of 2)"}
-    if args.workload == "c2" and not args.no_batch and world == 1:
-        r.close()
-        res = run_c3(args, 5, 3, 3, with_cpu=False)
-        line["batched_c3"] = {k: res[k] for k in ("value", "ms_per_step", "tris_per_s", "views", "triangles", "tuning",
-                                                   "plain", "small_views", "overhead_bound_small_views", "roofline",
-                                                   "e2e")}
-        res4 = run_c4(5, 3, with_cpu=False)
-        line["differentiable_c4"] = {k: res4[k] for k in ("views", "width", "height", "triangles", "ms_forward",
-                                                          "ms_forward_backward", "ratio", "value")}
+    ref = reference_c1_baseline()
+    if ref:
+        line["cpu_baseline_reference"] = ref
     print(json.dumps(line), flush=True)
     if dist:
         dist.barrier()
-    r.close()
 
 
 def main():
     args = parse()
+    spawn_ranks_if_needed(args.gpus)
     if args.impl == "reference":
         run_reference(args)
     elif args.workload == "c3":

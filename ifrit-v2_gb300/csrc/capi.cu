@@ -201,6 +201,7 @@ struct IfritGbRenderer {
     float clear_depth = 1.0f;
     bool vis_output = false;
     int polygon_mode = 0;  // IF_POLYGON_MODE_*
+    int polygon_rules = IFTR_POLYGON_RULES_FILL_PARTS;
     int raster_path = IFTR_RASTER_TILED;
     bool scissor_enable = false;
     std::vector<float> scissors;  // (x, y, w, h) per rectangle, at most 16
@@ -558,6 +559,25 @@ int enqueue_pass(IfritGbRenderer* h, std::vector<DrawDev>& draws, int clear) {
     v.vis = h->vis_output ? h->d_vis.as<int>() : nullptr;
     v.entries = h->d_entries.as<int>();
     v.clear = clear;
+    bool reference_rules = false;
+    for (const DrawDev& d : draws)
+        if (d.polygon_mode != IF_POLYGON_MODE_FILL && h->polygon_rules == IFTR_POLYGON_RULES_REFERENCE)
+            reference_rules = true;
+    if (reference_rules) {  // the reference's own line / point pipelines: a separate path
+        const DrawDev& d = draws[0];
+        if (draws.size() != 1 || S != 1 || (d.shading != IFTR_FS_GOURAUD && d.shading != IFTR_FS_PRIMITIVE_ID))
+            return IFTR_ERR_UNSUPPORTED;
+        std::memcpy(v.clear_color, h->clear_color, sizeof(v.clear_color));
+        v.clear_depth = h->clear_depth;
+        IFTR_CUDA(h, h->d_keys.reserve((size_t)W * H * sizeof(unsigned long long)));
+        IFTR_CUDA(h, cudaMemsetAsync(h->pass.status.p, 0, ifr::ST_PASS_WORDS * sizeof(uint32_t), h->stream));
+        IFTR_CUDA(h, ifr::launch_reference_rules(d, v, h->d_keys.as<unsigned long long>(), h->stream));
+        IFTR_CUDA(h, cudaMemcpyAsync(h->pass.h_status, h->pass.status.p, ifr::ST_WORDS * sizeof(uint32_t),
+                                     cudaMemcpyDeviceToHost, h->stream));
+        h->stats.triangles_in = (uint64_t)total;
+        h->pending = 1;
+        return IFTR_OK;
+    }
     std::memcpy(v.clear_color, h->clear_color, sizeof(v.clear_color));
     v.clear_depth = h->clear_depth;
     ifr::set_view_depth_state(v, draws.data(), (int)draws.size());
@@ -1273,6 +1293,13 @@ IFTR_API int iftrSetRasterPath(IfritGbRenderer* h, int path) {
 IFTR_API int iftrSetRasterizerPolygonMode(IfritGbRenderer* h, int mode) {
     if (!h || mode < IF_POLYGON_MODE_FILL || mode > IF_POLYGON_MODE_POINT) return IFTR_ERR_INVALID_ARG;
     h->polygon_mode = mode;
+    return IFTR_OK;
+}
+
+IFTR_API int iftrSetPolygonRules(IfritGbRenderer* h, int rules) {
+    if (!h || (rules != IFTR_POLYGON_RULES_FILL_PARTS && rules != IFTR_POLYGON_RULES_REFERENCE))
+        return IFTR_ERR_INVALID_ARG;
+    h->polygon_rules = rules;
     return IFTR_OK;
 }
 

@@ -23,6 +23,9 @@
 // result is deterministic.
 #include <cuda_runtime.h>
 #include <cuda_fp16.h>
+
+#include <algorithm>
+
 #include "raster_kernels.cuh"
 
 namespace ifr {
@@ -143,11 +146,13 @@ __device__ __forceinline__ void front_end(const PassArgs& a, int g, int di, cons
     }
 }
 
-// Tile range of a (sub-)triangle over more than kWarpTiles tiles, left for the whole warp.
+// The tile range a lane hands to its warp: ranges over more than kWarpTiles tiles are walked by
+// the whole warp one at a time (big); smaller ones (small) go through warp-aggregated atomics.
 constexpr int kWarpTiles = 4;
 struct WarpTiles {
-    bool big;
+    bool big, small;
     int tx0, tx1, ty0, ty1, tbase, tiles_x;
+    uint32_t entry;  // list entry of a small range
 };
 
 struct CountEmit {
@@ -155,20 +160,48 @@ struct CountEmit {
     WarpTiles& w;
     __device__ void operator()(const ViewArgs& v, const DrawDev& d, const SubTri& s, uint32_t entry) const {
         SubTri c = s;
-        if (!w.big && scissor_clamp(d, c)) {
-            const int sh = v.c.tile_shift;
-            const int tx0 = c.px0 >> sh, tx1 = c.px1 >> sh, ty0 = c.py0 >> sh, ty1 = c.py1 >> sh;
-            if ((tx1 - tx0 + 1) * (ty1 - ty0 + 1) > kWarpTiles) {
-                w.big = true;
-                w.tx0 = tx0; w.tx1 = tx1; w.ty0 = ty0; w.ty1 = ty1;
-                w.tbase = v.tile_start;
-                w.tiles_x = v.c.tiles_x;
-                return;
-            }
+        if (w.big || w.small) {  // a second fan triangle of a clipped triangle (rare): direct atomics
+            bin_sub(a, v, d, s, entry, false);
+            return;
         }
-        bin_sub(a, v, d, s, entry, false);
+        if (!scissor_clamp(d, c)) return;
+        const int sh = v.c.tile_shift;
+        w.tx0 = c.px0 >> sh; w.tx1 = c.px1 >> sh;
+        w.ty0 = c.py0 >> sh; w.ty1 = c.py1 >> sh;
+        w.tbase = v.tile_start;
+        w.tiles_x = v.c.tiles_x;
+        w.entry = entry;
+        if ((w.tx1 - w.tx0 + 1) * (w.ty1 - w.ty0 + 1) > kWarpTiles) w.big = true;
+        else w.small = true;
     }
 };
+
+// Warp-aggregated list updates of the lanes' small tile ranges: for every tile slot k of the
+// ranges, the lanes naming the same tile (__match_any_sync) make one atomicAdd of their count,
+// issued by the lowest of them; scattering, each lane's list slot is the returned base plus its
+// rank among those lanes.  Lanes of a warp hold consecutive triangles, which in a mesh are
+// neighbours and mostly share tiles.  List order within a tile carries no meaning (the
+// order-independent stages key by entry, the ordered stage sorts).
+__device__ __forceinline__ void warp_small_tiles(const PassArgs& a, const WarpTiles& w, bool scatter) {
+    const unsigned lane = threadIdx.x & 31u;
+    const int wd = w.small ? w.tx1 - w.tx0 + 1 : 1;
+    const int n = w.small ? wd * (w.ty1 - w.ty0 + 1) : 0;
+    const int nmax = __reduce_max_sync(0xffffffffu, n);
+    for (int k = 0; k < nmax; k++) {
+        const bool has = k < n;
+        const uint32_t tile = has ? (uint32_t)(w.tbase + (w.ty0 + k / wd) * w.tiles_x + w.tx0 + k % wd) : 0xffffffffu;
+        const unsigned peers = __match_any_sync(0xffffffffu, tile);
+        if (!has) continue;
+        const int leader = __ffs(peers) - 1;
+        uint32_t base = 0;
+        if ((int)lane == leader) base = atomicAdd((scatter ? a.tile_cursor : a.tile_count) + tile, (uint32_t)__popc(peers));
+        if (scatter) {
+            base = __shfl_sync(peers, base, leader);
+            const uint32_t pos = base + (uint32_t)__popc(peers & ((1u << lane) - 1u));
+            if (pos < a.pair_capacity) a.pairs[pos] = w.entry;
+        }
+    }
+}
 
 // The warp adds the counts (or, scattering, takes the list slots) of its lanes' large tile ranges,
 // one range at a time.
@@ -200,8 +233,9 @@ __global__ void __launch_bounds__(256) bin_count_kernel(PassArgs a) {
     const int g = blockIdx.x * blockDim.x + threadIdx.x;
     const int di = find_draw_warp(a, min(g, a.total_tris - 1));
     WarpTiles w;
-    w.big = false;
+    w.big = w.small = false;
     if (g < a.total_tris) front_end(a, g, di, CountEmit{a, w});
+    warp_small_tiles(a, w, false);
     warp_tiles(a, w, g, false);
 }
 
@@ -209,11 +243,11 @@ __global__ void __launch_bounds__(256) bin_count_kernel(PassArgs a) {
 // triangles run the front end again).  Every list slot comes from an atomicAdd whose result the
 // store waits for, so a triangle over many tiles would serialise hundreds of round trips in one
 // thread: the tile ranges of unclipped triangles over more than kWarpTiles tiles are walked by the
-// whole warp instead.
+// whole warp instead, and the smaller ones take their slots through warp-aggregated atomics.
 __global__ void __launch_bounds__(256) bin_scatter_kernel(PassArgs a) {
     const int g = blockIdx.x * blockDim.x + threadIdx.x;
     WarpTiles w;
-    w.big = false;
+    w.big = w.small = false;
     if (g < a.total_tris && !a.status[ST_OVERFLOW]) {
         const int flags = __ldg(&a.records[g].flags);
         if (flags & (REC_VALID | REC_CLIPPED)) {
@@ -236,14 +270,9 @@ __global__ void __launch_bounds__(256) bin_scatter_kernel(PassArgs a) {
                     w.ty0 = s.py0 >> sh; w.ty1 = s.py1 >> sh;
                     w.tbase = v.tile_start;
                     w.tiles_x = v.c.tiles_x;
+                    w.entry = (uint32_t)g << 3;
                     w.big = (w.tx1 - w.tx0 + 1) * (w.ty1 - w.ty0 + 1) > kWarpTiles;
-                    if (!w.big) {
-                        for (int ty = w.ty0; ty <= w.ty1; ty++)
-                            for (int tx = w.tx0; tx <= w.tx1; tx++) {
-                                const uint32_t pos = atomicAdd(a.tile_cursor + w.tbase + ty * w.tiles_x + tx, 1u);
-                                if (pos < a.pair_capacity) a.pairs[pos] = (uint32_t)g << 3;
-                            }
-                    }
+                    w.small = !w.big;
                 }
             } else {
                 const int t = g - __ldg(a.draw_start + di);
@@ -260,6 +289,7 @@ __global__ void __launch_bounds__(256) bin_scatter_kernel(PassArgs a) {
             }
         }
     }
+    warp_small_tiles(a, w, true);
     warp_tiles(a, w, g, true);
 }
 
@@ -1750,6 +1780,208 @@ __global__ void __launch_bounds__(kFwdThreads) forward_kernel(PassArgs a, GroupA
     if (threadIdx.x == 0) s_view = -1;
     while (next_tile<kFwdThreads>(a, g, qslot, sv, s_tile, s_view))
         forward_tile<S>(a, sv, s_tile, rec, scol, list, frags, after_raster != 0);
+}
+
+// ---------------------------------------------------------------------------- reference line / point rules
+// The reference CUDA renderer's own line and point pipelines (TileRasterCoreInvocationCuda.cu:
+// 2780-3334), selected by iftrSetPolygonRules for LINE / POINT polygon modes: points are the
+// draw's indices truncated to pixels (:2782-2822), lines are the triangles' three edges walked by
+// Bresenham between truncated endpoints (:2974-3115), and every pixel keeps its nearest candidate
+// (:2855-2920, 3167-3280).  The reference leaves depth ties to atomic arrival order; here each
+// candidate is a 64-bit key (ordered depth bits, submission order) lowered with atomicMin, so the
+// earliest candidate wins ties and the image is deterministic.  One thread per index (points) or
+// per triangle (lines, three edges each); a resolve pass per pixel applies the depth test against
+// the buffer (strict less, as the reference) and shades the winner.  Single-sample targets.
+__device__ __forceinline__ unsigned long long ref_key(float z, uint32_t order) {
+    uint32_t u = __float_as_uint(z + 0.0f);
+    u = (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+    return ((unsigned long long)u << 32) | order;
+}
+
+__device__ __forceinline__ float ref_key_depth(unsigned long long k) {
+    uint32_t u = (uint32_t)(k >> 32);
+    u = (u & 0x80000000u) ? (u & 0x7fffffffu) : ~u;
+    return __uint_as_float(u);
+}
+
+__device__ __forceinline__ void ref_offer(unsigned long long* keys, const PassConst& c, int px, int py, float z,
+                                          uint32_t order) {
+    if (px < 0 || py < 0 || px >= c.W || py >= c.H || z != z) return;
+    atomicMin(keys + (size_t)py * c.W + px, ref_key(z, order));
+}
+
+// Edge e of triangle t after the w < 0 clip (moved to w = 1) and the NDC mapping; false when dropped.
+__device__ __forceinline__ bool ref_edge(const DrawDev& d, int t, int e, float* p1, float* p2) {
+    const int ia = __ldg(d.indices + 3 * (size_t)t + e), ib = __ldg(d.indices + 3 * (size_t)t + (e + 1) % 3);
+    if (ia < 0 || ia >= d.num_vertices || ib < 0 || ib >= d.num_vertices) return false;
+    float v1[4], v2[4];
+    xform(d.mvp, d.vertices + (size_t)ia * d.stride, v1);
+    xform(d.mvp, d.vertices + (size_t)ib * d.stride, v2);
+    if (v1[3] < 0.0f && v2[3] < 0.0f) return false;
+    if (v1[3] < 0.0f) {
+        const float t1 = __fdiv_rn(-1.0f + v2[3], v2[3] - v1[3]);
+#pragma unroll
+        for (int k = 0; k < 4; k++) v1[k] = v2[k] + (v1[k] - v2[k]) * t1;
+    }
+    if (v2[3] < 0.0f) {
+        const float t2 = __fdiv_rn(-1.0f + v1[3], v1[3] - v2[3]);
+#pragma unroll
+        for (int k = 0; k < 4; k++) v2[k] = v1[k] + (v2[k] - v1[k]) * t2;
+    }
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+        v1[k] = __fdiv_rn(v1[k], v1[3]);
+        v2[k] = __fdiv_rn(v2[k], v2[3]);
+    }
+    v1[0] = v1[0] * 0.5f + 0.5f;
+    v1[1] = v1[1] * 0.5f + 0.5f;
+    v2[0] = v2[0] * 0.5f + 0.5f;
+    v2[1] = v2[1] * 0.5f + 0.5f;
+    if (v1[0] < 0.0f || v1[1] < 0.0f || v1[0] > 1.0f || v1[1] > 1.0f) return false;
+    if (v2[0] < 0.0f || v2[1] < 0.0f) return false;
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+        p1[k] = v1[k];
+        p2[k] = v2[k];
+    }
+    return true;
+}
+
+// Fraction of pixel (px, py) along the edge, on its major axis in pixel units.
+__device__ __forceinline__ float ref_percent(const PassConst& c, const float* p1, const float* p2, int px, int py) {
+    const float ax = p1[0] * (float)c.W, ay = p1[1] * (float)c.H, bx = p2[0] * (float)c.W, by = p2[1] * (float)c.H;
+    if (fabsf(bx - ax) >= fabsf(by - ay)) return __fdiv_rn((float)px - ax, bx - ax);
+    return __fdiv_rn((float)py - ay, by - ay);
+}
+
+__global__ void __launch_bounds__(256) ref_keys_init_kernel(unsigned long long* keys, size_t n) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+        keys[i] = ~0ull;
+}
+
+__global__ void __launch_bounds__(256) ref_point_kernel(DrawDev d, PassConst c, unsigned long long* keys) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= 3 * d.num_triangles) return;
+    const int vid = __ldg(d.indices + i);
+    if (vid < 0 || vid >= d.num_vertices) return;
+    float v[4];
+    xform(d.mvp, d.vertices + (size_t)vid * d.stride, v);
+    if (v[3] < 1e-8f) return;
+    float x = __fdiv_rn(v[0], v[3]), y = __fdiv_rn(v[1], v[3]);
+    const float z = __fdiv_rn(v[2], v[3]);
+    x = x * 0.5f + 0.5f;
+    y = y * 0.5f + 0.5f;
+    if (x < 0.0f || x > 1.0f || y < 0.0f || y > 1.0f) return;
+    ref_offer(keys, c, (int)(x * (float)(c.W - 1)), (int)(y * (float)(c.H - 1)), z, (uint32_t)i);
+}
+
+__global__ void __launch_bounds__(256) ref_line_kernel(DrawDev d, PassConst c, unsigned long long* keys) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= d.num_triangles) return;
+    for (int e = 0; e < 3; e++) {
+        float p1[4], p2[4];
+        if (!ref_edge(d, t, e, p1, p2)) continue;
+        const uint32_t order = (uint32_t)(3 * t + e);
+        int x1 = (int)(p1[0] * (float)(c.W - 1)), y1 = (int)(p1[1] * (float)(c.H - 1));
+        int x2 = (int)(p2[0] * (float)(c.W - 1)), y2 = (int)(p2[1] * (float)(c.H - 1));
+        const bool xmajor = abs(x1 - x2) > abs(y1 - y2);
+        if (xmajor ? x2 < x1 : y2 < y1) {
+            int q = x1; x1 = x2; x2 = q;
+            q = y1; y1 = y2; y2 = q;
+        }
+        // Bresenham with a float error term (:3076-3112): the major coordinate advances by one,
+        // the minor one when the accumulated slope passes 1/2
+        const int len = xmajor ? x2 - x1 : y2 - y1;
+        const float slope = xmajor ? fabsf(__fdiv_rn(1.0f * (float)(y2 - y1), (float)(x2 - x1)))
+                                   : fabsf(__fdiv_rn(1.0f * (float)(x2 - x1), (float)(y2 - y1)));
+        const int step = xmajor ? ((y2 - y1) > 0 ? 1 : -1) : ((x2 - x1) > 0 ? 1 : -1);
+        float err = 0.0f;
+        int cx = x1, cy = y1;
+        for (int i = 0; i <= len; i++) {
+            if (cx < c.W && cy < c.H) {
+                const float f = ref_percent(c, p1, p2, cx, cy);
+                ref_offer(keys, c, cx, cy, p1[2] + (p2[2] - p1[2]) * f, order);
+            }
+            err = err + slope;
+            if (err > 0.5f) {
+                if (xmajor) cy += step; else cx += step;
+                err = err - 1.0f;
+            }
+            if (xmajor) cx++; else cy++;
+        }
+    }
+}
+
+__device__ __forceinline__ void ref_attr(const DrawDev& d, int vid, float out[4]) {
+    const float* a = d.vertices + (size_t)vid * d.stride + d.attr_offset;
+#pragma unroll
+    for (int k = 0; k < 4; k++) out[k] = k < d.attr_count ? __ldg(a + k) : 0.0f;
+}
+
+__global__ void __launch_bounds__(256) ref_resolve_kernel(DrawDev d, ViewArgs v, const unsigned long long* keys) {
+    const int W = v.c.W, H = v.c.H;
+    const size_t npix = (size_t)W * H;
+    for (size_t pix = blockIdx.x * (size_t)blockDim.x + threadIdx.x; pix < npix; pix += (size_t)gridDim.x * blockDim.x) {
+        const int px = (int)(pix % W), py = (int)(pix / W);
+        float depth = v.clear ? v.clear_depth : v.depth[pix];
+        bool write = v.clear;
+        float col[4] = {v.clear_color[0], v.clear_color[1], v.clear_color[2], v.clear_color[3]};
+        int vis = -1;
+        const unsigned long long k = keys[pix];
+        if (k != ~0ull) {
+            const float z = ref_key_depth(k);
+            if (z < depth) {
+                const uint32_t order = (uint32_t)k;
+                const int t = (int)(order / 3u), e = (int)(order % 3u);
+                if (d.shading == SHADE_PRIMID) {
+                    col[0] = (float)(d.prim_base + t); col[1] = (float)e; col[2] = 0.0f; col[3] = 1.0f;
+                } else if (d.polygon_mode == POLY_POINT) {
+                    ref_attr(d, __ldg(d.indices + order), col);
+                    if (d.attr_count < 4) col[3] = 1.0f;
+                } else {
+                    float p1[4], p2[4], a1[4], a2[4];
+                    ref_edge(d, t, e, p1, p2);
+                    const float f = ref_percent(v.c, p1, p2, px, py);
+                    const float z1 = p1[3], z2 = p2[3];
+                    const float zt = __fdiv_rn(z1 * z2, z2 + f * (z1 - z2));
+                    ref_attr(d, __ldg(d.indices + 3 * (size_t)t + e), a1);
+                    ref_attr(d, __ldg(d.indices + 3 * (size_t)t + (e + 1) % 3), a2);
+#pragma unroll
+                    for (int q = 0; q < 4; q++) {
+                        const float u1 = __fdiv_rn(a1[q], z1), u2 = __fdiv_rn(a2[q], z2);
+                        col[q] = (f * (u2 - u1) + u1) * zt;
+                    }
+                    if (d.attr_count < 4) col[3] = 1.0f;
+                }
+                depth = z;
+                vis = d.prim_base + t;
+                write = true;
+            } else if (!v.clear) {
+                continue;
+            }
+        } else if (!v.clear) {
+            continue;
+        }
+        if (write) {
+            encode_color(v, pix, col);
+            v.depth[pix] = depth;
+            if (v.vis) v.vis[pix] = vis;
+        }
+    }
+}
+
+cudaError_t launch_reference_rules(const DrawDev& d, const ViewArgs& v, unsigned long long* keys, cudaStream_t stream) {
+    const size_t npix = (size_t)v.c.W * v.c.H;
+    const int fill_blocks = (int)std::min<size_t>((npix + 255) / 256, 4096);
+    ref_keys_init_kernel<<<fill_blocks, 256, 0, stream>>>(keys, npix);
+    if (d.num_triangles > 0) {
+        if (d.polygon_mode == POLY_POINT)
+            ref_point_kernel<<<(3 * d.num_triangles + 255) / 256, 256, 0, stream>>>(d, v.c, keys);
+        else
+            ref_line_kernel<<<(d.num_triangles + 255) / 256, 256, 0, stream>>>(d, v.c, keys);
+    }
+    ref_resolve_kernel<<<fill_blocks, 256, 0, stream>>>(d, v, keys);
+    return cudaGetLastError();
 }
 
 // ---------------------------------------------------------------------------- mesh-stage outputs

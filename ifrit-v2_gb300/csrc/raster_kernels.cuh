@@ -110,6 +110,9 @@ constexpr int scan_blocks(int tiles) { return (tiles + 4095) / 4096 + 1; }
 // stage (per-stage timing).
 constexpr int kStageEvents = 7;
 cudaError_t launch_pass(const PassArgs& a, const LaunchPlan& plan, cudaStream_t stream, cudaEvent_t* ev);
+// Reference line / point rules (iftrSetPolygonRules): one single-sample draw; `keys` holds W*H
+// 64-bit entries of scratch.
+cudaError_t launch_reference_rules(const DrawDev& d, const ViewArgs& v, unsigned long long* keys, cudaStream_t stream);
 cudaError_t launch_mip_level(const uint32_t* src, int sw, int sh, uint32_t* dst, int dw, int dh, cudaStream_t stream);
 // Mesh-stage outputs: per-group vertex / index offsets (totals: vertices, indices, bad-count flag),
 // then the compaction into [x y z w a0 a1 a2 a3] rows and rebased indices.

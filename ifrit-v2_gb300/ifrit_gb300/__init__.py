@@ -23,6 +23,7 @@ IFTP_FLOAT1, IFTP_FLOAT2, IFTP_FLOAT3, IFTP_FLOAT4 = 1, 2, 3, 4
 CULL_NONE, CULL_FRONT, CULL_BACK, CULL_FRONT_AND_BACK = 0, 1, 2, 3
 NEVER, LESS, EQUAL, LESS_OR_EQUAL, GREATER, NOT_EQUAL, GREATER_OR_EQUAL, ALWAYS = range(8)
 POLYGON_FILL, POLYGON_LINE, POLYGON_POINT = 0, 1, 2
+POLYGON_RULES_FILL_PARTS, POLYGON_RULES_REFERENCE = 0, 1
 RASTER_TILED, RASTER_ATOMIC = 0, 1
 
 EXPORTED = [
@@ -47,7 +48,7 @@ EXPORTED = [
     "iftrSetVertexBufferDirty", "ifbufGetBufferRawData", "ifbufSetBufferDirty", "iftrDrawNoAlloc",
     "iftrBeginPass", "iftrPassDraw", "iftrEndPass", "iftrDrawBatch", "iftrSetBatchTuning", "iftrGetBatchTuning",
     "iftrDiffForward", "iftrDiffBackward", "iftrSetScissors", "iftrSetScissorTestEnable",
-    "iftrSetRasterizerPolygonMode", "iftrSetRasterPath", "iftrDrawMeshOutputs",
+    "iftrSetRasterizerPolygonMode", "iftrSetRasterPath", "iftrDrawMeshOutputs", "iftrSetPolygonRules",
 ]
 
 
@@ -287,8 +288,11 @@ class Renderer:
     def set_raster_path(self, path):
         check("iftrSetRasterPath", self.lib.iftrSetRasterPath(self.h, path))
 
-    def set_polygon_mode(self, mode):
+    def set_polygon_mode(self, mode, rules=None):
+        """rules: POLYGON_RULES_FILL_PARTS or POLYGON_RULES_REFERENCE (iftrSetPolygonRules)."""
         check("iftrSetRasterizerPolygonMode", self.lib.iftrSetRasterizerPolygonMode(self.h, mode))
+        if rules is not None:
+            check("iftrSetPolygonRules", self.lib.iftrSetPolygonRules(self.h, rules))
 
     def set_scissors(self, rects, enable=True):
         """rects: list of (x, y, w, h); enable False switches the test off."""

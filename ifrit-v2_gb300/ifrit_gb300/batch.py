@@ -168,35 +168,3 @@ class BatchRenderer:
 
     def visibility(self, view):
         return self.views[view][1]["vis"].cpu().numpy()
-
-
-def main(argv=None):
-    """Renders the 256-view batched benchmark scene a few times (a fixed description, so the
-    first call prepares and the rest replay the captured graph)."""
-    import argparse
-    import torch
-    from . import scenes
-    p = argparse.ArgumentParser(prog="python -m ifrit_gb300.batch")
-    p.add_argument("--draws", type=int, default=3)
-    p.add_argument("--tile-size", type=int, default=16)
-    p.add_argument("--ctas-per-sm", type=int, default=0)
-    p.add_argument("--autotune", action="store_true")
-    p.add_argument("--views", type=int, default=256)
-    a = p.parse_args(argv)
-    views = scenes.c3_batch(num_views=a.views)
-    br = BatchRenderer()
-    br.set_tuning(a.autotune, a.tile_size, a.ctas_per_sm)
-    for k, v in enumerate(views):
-        br.add_view(v["width"], v["height"], v["samples"], FORMAT_RGBA8)
-        br.add_mesh(k, v["vertices"], v["indices"], v["mvp"], attr_count=v["vertices"].shape[1] - 3, cull=v["cull"])
-    for _ in range(a.draws):
-        br.draw()
-    br.finish()
-    torch.cuda.synchronize()
-    print("rendered %d views, %d triangles, %d times; tuning %s" %
-          (len(views), sum(len(v["indices"]) for v in views), a.draws, br.tuning()))
-    br.close()
-
-
-if __name__ == "__main__":
-    main()

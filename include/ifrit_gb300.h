@@ -146,6 +146,21 @@ IFTR_API int iftrSetScissors(IfritGbRenderer* h, const float* rects, int count);
  * draws each vertex as a 1-pixel square.  Both go through the fill rules (MSAA, depth, shading);
  * triangles that need clipping are dropped in these modes. */
 IFTR_API int iftrSetRasterizerPolygonMode(IfritGbRenderer* h, int mode);
+/* Rules of the LINE and POINT polygon modes (no entry point in the reference; its CUDA renderer
+ * has only these rules for those modes, TileRasterCoreInvocationCuda.cu:2780-3334).
+ * FILL_PARTS (default): the parallelograms / squares above.  REFERENCE: the reference's own line
+ * and point pipelines: POINT draws every index of the draw as the pixel (int)(x (W-1)),
+ * (int)(y (H-1)) of its NDC position mapped to [0, 1] (w < 1e-8 and positions outside [0, 1]
+ * skipped); LINE draws the three edges of every triangle (no culling) with Bresenham between
+ * truncated endpoints after moving an endpoint with w < 0 to w = 1; per pixel the nearest candidate
+ * wins (ties: the earlier point or edge in submission order) and is kept if its depth is below the
+ * buffer's (strict, whatever the depth function); colour is the point's vertex attribute or the
+ * edge's endpoint attributes interpolated perspective-correctly.  REFERENCE needs a single-sample
+ * target, GOURAUD or PRIMITIVE_ID shading and a single-draw pass (iftrDrawLegacy / iftrDrawAsync);
+ * otherwise the draw returns IFTR_ERR_UNSUPPORTED.  Visibility holds the triangle the point or edge
+ * belongs to. */
+enum { IFTR_POLYGON_RULES_FILL_PARTS = 0, IFTR_POLYGON_RULES_REFERENCE = 1 };
+IFTR_API int iftrSetPolygonRules(IfritGbRenderer* h, int rules);
 /* Raster path of order-independent passes (no counterpart in the reference).  TILED (default):
  * triangles binned into 16x16 tiles, resolved per tile in shared memory.  ATOMIC: no binning;
  * each triangle's thread resolves its samples into per-sample 64-bit (depth, primitive) keys in

@@ -23,6 +23,8 @@ never into the repository's history).  Overlays:
   constant, 16 in the reference, TileRasterContext.h:52) becomes ``IFRIT_REF_NUM_THREADS``, set
   at compile time to the host's core count minus one, because the reference's spin barriers
   degrade sharply when oversubscribed.
+* ``ifrit/core/platform/ApiConv.h``: the 64-bit platform test (``ApiConv.h:69``) knows x86-64
+  and ppc64 only and fails a ``static_assert`` elsewhere; the overlay adds aarch64.
 * Scalar build (``simd=False``, the only build on a non-x86 host): the three x86 intrinsic sites
   that the reference uses even with its SIMD switches off are put under the switches:
   ``Image.h:110-113`` (``fillPixelRGBA128ps``, only called from SIMD-128 code) and the
@@ -89,6 +91,10 @@ def _overlay(rel, text):
         text, n = re.subn(r"(IF_CONSTEXPR static int numThreads\s*=\s*)16;", r"\g<1>IFRIT_REF_NUM_THREADS;", text)
         if n != 1:
             raise RuntimeError("TileRasterContext.h overlay pattern not found")
+    elif rel == "include/ifrit/core/platform/ApiConv.h":
+        text, n = re.subn(r"#if __x86_64__ \|\| __ppc64__", "#if __x86_64__ || __ppc64__ || __aarch64__", text)
+        if n != 1:
+            raise RuntimeError("ApiConv.h overlay pattern not found")
     elif rel == "include/ifrit/softgraphics/core/data/Image.h":
         pat = re.compile(r"(\n[ \t]*inline void fillPixelRGBA128ps\(size_t x, size_t y, const __m128& ps\)\s*"
                          r"\{[^{}]*\})")

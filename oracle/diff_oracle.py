@@ -162,6 +162,51 @@ def antialias(s, pos, faces, mvps, vis, codes):
     return (flat + delta).reshape(N, H, W, 3)
 
 
+def kink_signature(pos, uv, tex, faces, mvps, vis, codes):
+    """Where the forward (for fixed visibility and decisions) sits relative to its
+    non-differentiable points: the bilinear texel cell of every shaded pixel's UV (floor in
+    _bilinear) and, for every blended pixel pair, whether the edge crossing t is below 1/2 (the
+    |t - 1/2| kink), below 0 or above 1 (the clamp).  Central differences whose stencil keeps
+    visibility, decisions and this signature measure a smooth function of the parameter."""
+    pos = torch.as_tensor(np.asarray(pos, np.float64))
+    uv = torch.as_tensor(np.asarray(uv, np.float64))
+    faces = torch.as_tensor(np.asarray(faces)).long()
+    mvps = torch.as_tensor(np.asarray(mvps, np.float64)).reshape(-1, 4, 4)
+    vis = torch.as_tensor(np.asarray(vis))
+    codes = torch.as_tensor(np.asarray(codes))
+    N, H, W = vis.shape
+    th, tw = tex.shape[:2]
+    out = []
+    with torch.no_grad():
+        clip = _clip(pos, mvps)
+        n, y, x = torch.nonzero(vis >= 0, as_tuple=True)
+        vtx = faces[vis[n, y, x].long()]
+        px, py = _ndc(x, y, W, H)
+        lam = _bary(clip[n[:, None], vtx], px, py)
+        uvi = (lam[..., None] * uv[vtx]).sum(1)
+        out += [torch.floor(uvi[:, 0] * tw - 0.5).long(), torch.floor(uvi[:, 1] * th - 0.5).long()]
+        for direction in (0, 1):
+            n, y, x, x2, y2 = _pairs(vis, direction)
+            code = codes[n, y, x, direction].long()
+            keep = code >= 0
+            n, y, x, x2, y2, code = n[keep], y[keep], x[keep], x2[keep], y2[keep], code[keep]
+            if len(n) == 0:
+                continue
+            a_is_q = code >= 3
+            k = code % 3
+            axp, ayp = torch.where(a_is_q, x2, x), torch.where(a_is_q, y2, y)
+            bxp, byp = torch.where(a_is_q, x, x2), torch.where(a_is_q, y, y2)
+            c = clip[n[:, None], faces[vis[n, ayp, axp].long()]]
+            X, Y, area = _project(c)
+            sgn = torch.sign(area)
+            ax, ay = _ndc(axp, ayp, W, H)
+            bx, by = _ndc(bxp, byp, W, H)
+            ea, eb = _edge(X, Y, sgn, k, ax, ay), _edge(X, Y, sgn, k, bx, by)
+            t = ea / (ea - eb)
+            out += [(t >= 0.5).long(), (t < 0).long(), (t > 1).long()]
+    return torch.cat(out).numpy()
+
+
 def decisions(pos, faces, nbrs, mvps, vis):
     """The antialiasing decisions computed independently in float64: codes (N, H, W, 2)."""
     pos = torch.as_tensor(pos, dtype=F64)

@@ -53,13 +53,14 @@ class Draw(ctypes.Structure):
                 ("shading", ctypes.c_int), ("tex", Texture), ("sampler", Sampler),
                 ("scissor_enable", ctypes.c_int), ("scissor_count", ctypes.c_int),
                 ("scissor", (ctypes.c_float * 4) * 16), ("polygon_mode", ctypes.c_int),
-                ("blend_compat", ctypes.c_int)]
+                ("blend_compat", ctypes.c_int), ("polygon_rules", ctypes.c_int)]
 
 
 class Target(ctypes.Structure):
     _fields_ = [("width", ctypes.c_int), ("height", ctypes.c_int), ("samples", ctypes.c_int),
                 ("format", ctypes.c_int), ("sample_compat", ctypes.c_int), ("color", ctypes.c_void_p),
-                ("depth", ctypes.POINTER(ctypes.c_float)), ("vis", ctypes.POINTER(ctypes.c_int))]
+                ("depth", ctypes.POINTER(ctypes.c_float)), ("vis", ctypes.POINTER(ctypes.c_int)),
+                ("row0", ctypes.c_int), ("rows", ctypes.c_int)]
 
 
 _lib = None
@@ -103,7 +104,7 @@ def build_mips(level0):
 
 def make_draw(vertices, indices, mvp, *, attr_offset=3, attr_count=3, prim_base=0, cull_mode=2,
               front_ccw=1, depth_test=1, depth_func=3, depth_write=1, blend=None, shading=SHADE_GOURAUD,
-              texture=None, sampler=None, scissor=None, polygon_mode=0, blend_compat=0):
+              texture=None, sampler=None, scissor=None, polygon_mode=0, blend_compat=0, polygon_rules=0):
     """Returns (Draw, keepalive) for numpy vertices (V, stride) float32 and indices (T, 3) int32.
     blend_compat / sampler["compat"] select the reference's blend table and sampler as written
     (pinning only; see oracle_fx.h)."""
@@ -143,6 +144,7 @@ def make_draw(vertices, indices, mvp, *, attr_offset=3, attr_count=3, prim_base=
     d.sampler.compat = int(s.get("compat", 0))
     d.polygon_mode = polygon_mode
     d.blend_compat = int(blend_compat)
+    d.polygon_rules = int(polygon_rules)
     if scissor is not None:  # list of (x, y, w, h) rectangles; [] = enabled with none (passes all)
         d.scissor_enable = 1
         d.scissor_count = min(len(scissor), 16)
@@ -158,16 +160,21 @@ def color_dtype(fmt):
 
 
 def render(draws, width, height, samples=1, fmt=FMT_RGBA8, clear=True, clear_color=(0, 0, 0, 0),
-           clear_depth=1.0, compat=False, nthreads=1, color=None, depth=None, with_vis=True):
-    """Renders a pass of draws ((Draw, keep) pairs).  Returns dict(color, depth, vis)."""
+           clear_depth=1.0, compat=False, nthreads=1, color=None, depth=None, with_vis=True, rows=None):
+    """Renders a pass of draws ((Draw, keep) pairs).  Returns dict(color, depth, vis).
+    rows=(y0, y1): only that band of the height-row frame is rendered, into buffers of y1 - y0
+    rows."""
     dt, ch = color_dtype(fmt)
+    nrows = height if rows is None else rows[1] - rows[0]
     if color is None:
-        color = np.zeros((height, width, ch) if ch > 1 else (height, width), dt)
+        color = np.zeros((nrows, width, ch) if ch > 1 else (nrows, width), dt)
     if depth is None:
-        depth = np.zeros((height, width, samples), np.float32)
-    vis = np.zeros((height, width, samples), np.int32) if with_vis else None
+        depth = np.zeros((nrows, width, samples), np.float32)
+    vis = np.zeros((nrows, width, samples), np.int32) if with_vis else None
     t = Target()
     t.width, t.height, t.samples, t.format, t.sample_compat = width, height, samples, fmt, int(compat)
+    if rows is not None:
+        t.row0, t.rows = int(rows[0]), int(rows[1] - rows[0])
     t.color = color.ctypes.data_as(ctypes.c_void_p)
     t.depth = _fp(depth)
     t.vis = vis.ctypes.data_as(ctypes.POINTER(ctypes.c_int)) if with_vis else None

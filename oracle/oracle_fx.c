@@ -482,6 +482,7 @@ typedef struct {
 
 typedef struct {
     int W, H, S;
+    int r0, r1;  /* rows held by the target buffers: [r0, r1) of the H-row frame */
     int sx[16], sy[16];
     int smin_x, smax_x, smin_y, smax_y;
     int shade_x, shade_y;
@@ -849,11 +850,12 @@ static void blend(const ofx_draw* d, const float* src, float* dst) {
  * Two phases per chunk of OFX_CHUNK triangles (in submission order): every thread sets up its
  * slice of the chunk once (clip, snap, cull, edge functions), then every thread rasterises the
  * whole chunk's sub-triangles, in submission order, into its own band of rows (depth test and
- * write immediately, as the reference's in-order path).  Passes without blending are shaded
- * deferred, as the reference's tag-buffer path (TileRasterWorker.cpp:1932-2121): each sample
- * remembers the last fragment that passed it, and each (pixel, fragment) pair that survives is
- * shaded once at the end -- the same colour forward shading leaves there, since unblended
- * fragments overwrite.  Passes with blending shade every passing fragment in order. */
+ * write immediately, as the reference's in-order path).  The draws before the first blended one
+ * are shaded deferred, as the reference's tag-buffer path (TileRasterWorker.cpp:1932-2121): each
+ * sample remembers the last fragment that passed it, and each (pixel, fragment) pair that
+ * survives is shaded once when the prefix ends -- the same colour forward shading leaves there,
+ * since unblended fragments overwrite.  From the first blended draw on, every passing fragment
+ * is shaded in order (a blend reads the colour under it). */
 #define OFX_CHUNK 16384
 
 typedef struct {
@@ -901,7 +903,7 @@ static void raster_rec(pass_job* j, const setup_rec* r) {
     for (int py = ya; py <= yb; py++) {
         for (int px = s->px0; px <= s->px1; px++) {
             if (!scissor_pass(d, px, py)) continue;
-            size_t base = ((size_t)py * c->W + px) * S;
+            size_t base = ((size_t)(py - c->r0) * c->W + px) * S;
             unsigned passmask = 0;
             for (int k = 0; k < S; k++) {
                 int32_t sx = px * 256 + c->sx[k], sy = py * 256 + c->sy[k];
@@ -940,7 +942,7 @@ static void shade_band(pass_job* j) {
     int ncached = 0;
     for (int py = j->y0; py < j->y1; py++) {
         for (int px = 0; px < c->W; px++) {
-            size_t base = ((size_t)py * c->W + px) * S;
+            size_t base = ((size_t)(py - c->r0) * c->W + px) * S;
             unsigned done = 0;
             for (int k = 0; k < S; k++) {
                 int64_t f = j->win[base + k];
@@ -969,6 +971,10 @@ static void* run_pass(void* arg) {
     ofx_sub subs[OFX_MAX_SUB];
     for (int di = 0; di < j->ndraws; di++) {
         const ofx_draw* d = &j->draws[di];
+        if (j->win && d->blend_enable) { /* the deferred prefix ends: shade it, then go forward */
+            shade_band(j);
+            j->win = NULL;
+        }
         for (int t0 = 0; t0 < d->num_triangles; t0 += OFX_CHUNK) {
             int t1 = imin_(t0 + OFX_CHUNK, d->num_triangles);
             int a = t0 + (int)((int64_t)(t1 - t0) * j->id / j->nthreads);
@@ -978,6 +984,7 @@ static void* run_pass(void* arg) {
             for (int t = a; t < b; t++) {
                 int ns = triangle_subs(j->c, d, t, subs);
                 for (int si = 0; si < ns; si++) {
+                    if (subs[si].py1 < j->c->r0 || subs[si].py0 >= j->c->r1) continue;
                     out[n].s = subs[si];
                     out[n].draw = di;
                     out[n].tri = t;
@@ -994,6 +1001,191 @@ static void* run_pass(void* arg) {
     }
     if (j->win) shade_band(j);
     return NULL;
+}
+
+/* ---------------------------------------------------------------- reference line / point rules
+ * polygon_rules == 1: the reference CUDA renderer's own line and point pipelines
+ * (TileRasterCoreInvocationCuda.cu:2780-3334), which do not go through triangle coverage:
+ *   points (:2782-2822): every index of the draw is a point: clip = MVP * position; skipped if
+ *     w < 1e-8; NDC x, y, z = clip / w; x, y mapped by v * 0.5 + 0.5 and skipped outside [0, 1];
+ *     pixel (int)(x * (W - 1)), (int)(y * (H - 1)) (truncation);
+ *   lines (:2974-3055, 3062-3115): the three edges (v0 v1), (v1 v2), (v2 v0) of every triangle,
+ *     no culling; an edge with both w < 0 is dropped, one endpoint with w < 0 moves to the point
+ *     where w = 1 (t = (w_other - 1) / (w_other - w), lerp from the other endpoint); the same NDC
+ *     mapping; an edge is dropped when its first endpoint leaves [0, 1]^2 or its second endpoint has
+ *     x < 0 or y < 0 (the second endpoint's upper bounds are not tested, :3010: fragments past the
+ *     frame's right or top edge are dropped here, as they never reach a pixel of the frame there);
+ *     pixels from a Bresenham walk between the truncated endpoints (float error term against 1/2,
+ *     x-major when |dx| > |dy|);
+ *   fragments (:2855-2920, 3167-3280): per pixel, the candidate with the smallest z wins (a point's
+ *     NDC z; a line fragment's z interpolated by the fraction of the pixel along the edge's major
+ *     axis in pixel units, (p - a W) / (b W - a W)); ties go to the earlier point / edge in
+ *     submission order (the reference leaves them to atomic arrival order); the winner is kept if
+ *     its z is below the depth in the buffer (strict, whatever the depth function), and writes
+ *     depth and colour.  Colour: the vertex attribute of a point; for a line fragment the two
+ *     endpoints' attributes interpolated perspective-correctly with the endpoints' w.  The
+ *     interpolation lerp is a + (b - a) t (ShaderOpsCuda.cuh:98-109).
+ *   Single-sample targets only; visibility holds the triangle the point or edge belongs to. */
+typedef struct {
+    uint64_t key;  /* ordered depth bits << 32 | candidate order; ~0 = none */
+} ref_cand;
+
+static inline uint64_t depth_key(float z, uint32_t order) {
+    uint32_t u = f2u(z + 0.0f);
+    u = (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+    return ((uint64_t)u << 32) | order;
+}
+
+static inline float key_depth(uint64_t k) {
+    uint32_t u = (uint32_t)(k >> 32);
+    u = (u & 0x80000000u) ? (u & 0x7fffffffu) : ~u;
+    return u2f(u);
+}
+
+static inline void ref_offer(uint64_t* keys, const pass_ctx* c, int px, int py, float z, uint32_t order) {
+    if (px < 0 || py < c->r0 || px >= c->W || py >= c->r1 || z != z) return;
+    uint64_t k = depth_key(z, order);
+    size_t i = (size_t)(py - c->r0) * c->W + px;
+    if (k < keys[i]) keys[i] = k;
+}
+
+/* The edge from vertex a to vertex b of triangle t after the w < 0 clip and the NDC mapping;
+ * returns 0 when the edge is dropped.  out: x, y in [0, 1] units, z = NDC z, w. */
+static int ref_edge(const ofx_draw* d, int t, int e, float p1[4], float p2[4]) {
+    const int ia = d->indices[3 * t + e], ib = d->indices[3 * t + (e + 1) % 3];
+    if (ia < 0 || ia >= d->num_vertices || ib < 0 || ib >= d->num_vertices) return 0;
+    float v1[4], v2[4];
+    xform(d->mvp, d->vertices + (size_t)ia * d->vertex_stride, v1);
+    xform(d->mvp, d->vertices + (size_t)ib * d->vertex_stride, v2);
+    if (v1[3] < 0.0f && v2[3] < 0.0f) return 0;
+    if (v1[3] < 0.0f) {
+        float t1 = (-1.0f + v2[3]) / (v2[3] - v1[3]);
+        for (int k = 0; k < 4; k++) v1[k] = v2[k] + (v1[k] - v2[k]) * t1;
+    }
+    if (v2[3] < 0.0f) {
+        float t2 = (-1.0f + v1[3]) / (v1[3] - v2[3]);
+        for (int k = 0; k < 4; k++) v2[k] = v1[k] + (v2[k] - v1[k]) * t2;
+    }
+    for (int k = 0; k < 3; k++) { v1[k] = v1[k] / v1[3]; v2[k] = v2[k] / v2[3]; }
+    v1[0] = v1[0] * 0.5f + 0.5f; v1[1] = v1[1] * 0.5f + 0.5f;
+    v2[0] = v2[0] * 0.5f + 0.5f; v2[1] = v2[1] * 0.5f + 0.5f;
+    if (v1[0] < 0.0f || v1[1] < 0.0f || v1[0] > 1.0f || v1[1] > 1.0f) return 0;
+    if (v2[0] < 0.0f || v2[1] < 0.0f) return 0;
+    memcpy(p1, v1, 16);
+    memcpy(p2, v2, 16);
+    return 1;
+}
+
+/* Fraction of pixel (px, py) along the edge, along its major axis in pixel units. */
+static inline float ref_percent(const pass_ctx* c, const float* p1, const float* p2, int px, int py) {
+    float ax = p1[0] * (float)c->W, ay = p1[1] * (float)c->H, bx = p2[0] * (float)c->W, by = p2[1] * (float)c->H;
+    if (fabsf(bx - ax) >= fabsf(by - ay)) return ((float)px - ax) / (bx - ax);
+    return ((float)py - ay) / (by - ay);
+}
+
+static void ref_line_fragments(uint64_t* keys, const pass_ctx* c, const float* p1, const float* p2, uint32_t order) {
+    int x1 = (int)(p1[0] * (float)(c->W - 1)), y1 = (int)(p1[1] * (float)(c->H - 1));
+    int x2 = (int)(p2[0] * (float)(c->W - 1)), y2 = (int)(p2[1] * (float)(c->H - 1));
+    int dx = abs(x1 - x2), dy = abs(y1 - y2);
+    if (dx > dy) {
+        if (x2 < x1) { int q = x1; x1 = x2; x2 = q; q = y1; y1 = y2; y2 = q; }
+        float slope = fabsf(1.0f * (float)(y2 - y1) / (float)(x2 - x1));
+        int step = (y2 - y1) > 0 ? 1 : -1;
+        float err = 0.0f;
+        int cx = x1, cy = y1;
+        for (int i = 0; i <= x2 - x1; i++) {
+            if (cx < c->W && cy < c->H) {
+                float f = ref_percent(c, p1, p2, cx, cy);
+                ref_offer(keys, c, cx, cy, p1[2] + (p2[2] - p1[2]) * f, order);
+            }
+            err = err + slope;
+            if (err > 0.5f) { cy += step; err = err - 1.0f; }
+            cx++;
+        }
+    } else {
+        if (y2 < y1) { int q = x1; x1 = x2; x2 = q; q = y1; y1 = y2; y2 = q; }
+        float slope = fabsf(1.0f * (float)(x2 - x1) / (float)(y2 - y1));
+        int step = (x2 - x1) > 0 ? 1 : -1;
+        float err = 0.0f;
+        int cx = x1, cy = y1;
+        for (int i = 0; i <= y2 - y1; i++) {
+            if (cx < c->W && cy < c->H) {
+                float f = ref_percent(c, p1, p2, cx, cy);
+                ref_offer(keys, c, cx, cy, p1[2] + (p2[2] - p1[2]) * f, order);
+            }
+            err = err + slope;
+            if (err > 0.5f) { cx += step; err = err - 1.0f; }
+            cy++;
+        }
+    }
+}
+
+static void ref_attr(const ofx_draw* d, int vid, float out[4]) {
+    const float* a = d->vertices + (size_t)vid * d->vertex_stride + d->attr_offset;
+    for (int k = 0; k < 4; k++) out[k] = k < d->attr_count ? a[k] : 0.0f;
+}
+
+/* One draw under the reference's line / point rules into the (single-sample) pass state. */
+static int ref_rules_draw(const pass_ctx* c, const ofx_draw* d, ofx_target* tg, float* scol) {
+    size_t npix = (size_t)c->W * (size_t)(c->r1 - c->r0);
+    uint64_t* keys = (uint64_t*)malloc(npix * sizeof(uint64_t));
+    if (!keys) return 3;
+    for (size_t i = 0; i < npix; i++) keys[i] = ~(uint64_t)0;
+    if (d->polygon_mode == 2) {
+        for (int i = 0; i < 3 * d->num_triangles; i++) {
+            int vid = d->indices[i];
+            if (vid < 0 || vid >= d->num_vertices) continue;
+            float v[4];
+            xform(d->mvp, d->vertices + (size_t)vid * d->vertex_stride, v);
+            if (v[3] < 1e-8f) continue;
+            float x = v[0] / v[3], y = v[1] / v[3], z = v[2] / v[3];
+            x = x * 0.5f + 0.5f;
+            y = y * 0.5f + 0.5f;
+            if (x < 0.0f || x > 1.0f || y < 0.0f || y > 1.0f) continue;
+            ref_offer(keys, c, (int)(x * (float)(c->W - 1)), (int)(y * (float)(c->H - 1)), z, (uint32_t)i);
+        }
+    } else {
+        for (int t = 0; t < d->num_triangles; t++)
+            for (int e = 0; e < 3; e++) {
+                float p1[4], p2[4];
+                if (ref_edge(d, t, e, p1, p2)) ref_line_fragments(keys, c, p1, p2, (uint32_t)(3 * t + e));
+            }
+    }
+    for (int py = c->r0; py < c->r1; py++)
+        for (int px = 0; px < c->W; px++) {
+            size_t i = (size_t)(py - c->r0) * c->W + px;
+            uint64_t k = keys[i];
+            if (k == ~(uint64_t)0) continue;
+            float z = key_depth(k);
+            if (!(z < tg->depth[i])) continue;
+            uint32_t order = (uint32_t)k;
+            int t = (int)(order / 3u), e = (int)(order % 3u);
+            float col[4];
+            if (d->shading == OFX_SHADE_PRIMID) {
+                col[0] = (float)(d->prim_base + t); col[1] = (float)e; col[2] = 0.0f; col[3] = 1.0f;
+            } else if (d->polygon_mode == 2) {
+                ref_attr(d, d->indices[order], col);
+                if (d->attr_count < 4) col[3] = 1.0f;
+            } else {
+                float p1[4], p2[4], a1[4], a2[4];
+                ref_edge(d, t, e, p1, p2);
+                float f = ref_percent(c, p1, p2, px, py);
+                float z1 = p1[3], z2 = p2[3];
+                float zt = z1 * z2 / (z2 + f * (z1 - z2));
+                ref_attr(d, d->indices[3 * t + e], a1);
+                ref_attr(d, d->indices[3 * t + (e + 1) % 3], a2);
+                for (int q = 0; q < 4; q++) {
+                    float u1 = a1[q] / z1, u2 = a2[q] / z2;
+                    col[q] = (f * (u2 - u1) + u1) * zt;
+                }
+                if (d->attr_count < 4) col[3] = 1.0f;
+            }
+            tg->depth[i] = z;
+            if (tg->vis) tg->vis[i] = d->prim_base + (d->polygon_mode == 2 ? (int)(order / 3u) : t);
+            memcpy(scol + i * 4, col, 16);
+        }
+    free(keys);
+    return 0;
 }
 
 static void decode_color(const ofx_target* t, size_t pix, float c[4]) {
@@ -1041,6 +1233,9 @@ int ofx_render_pass(const ofx_draw* draws, int ndraws, ofx_target* t, int clear,
     if (t->width <= 0 || t->height <= 0 || t->width > 16384 || t->height > 16384) return 2;
     pass_ctx c;
     c.W = t->width; c.H = t->height; c.S = S;
+    c.r0 = t->rows > 0 ? t->row0 : 0;
+    c.r1 = t->rows > 0 ? t->row0 + t->rows : t->height;
+    if (c.r0 < 0 || c.r1 > c.H || c.r0 >= c.r1) return 4;
     ofx_sample_positions(S, t->sample_compat, c.sx, c.sy);
     c.smin_x = c.smax_x = c.sx[0];
     c.smin_y = c.smax_y = c.sy[0];
@@ -1055,7 +1250,7 @@ int ofx_render_pass(const ofx_draw* draws, int ndraws, ofx_target* t, int clear,
     c.gx = (float)(1.0 + 2.0 * OFX_GUARD_PX / (double)c.W);
     c.gy = (float)(1.0 + 2.0 * OFX_GUARD_PX / (double)c.H);
 
-    size_t npix = (size_t)c.W * c.H;
+    size_t npix = (size_t)c.W * (size_t)(c.r1 - c.r0);
     float* scol = (float*)malloc(npix * S * 4 * sizeof(float));
     if (!scol) return 3;
     for (size_t p = 0; p < npix; p++) {
@@ -1068,12 +1263,17 @@ int ofx_render_pass(const ofx_draw* draws, int ndraws, ofx_target* t, int clear,
             if (t->vis) t->vis[p * S + k] = -1;
         }
     }
-    if (nthreads < 1) nthreads = 1;
-    if (nthreads > c.H) nthreads = c.H;
-    if (nthreads > 256) nthreads = 256;
-    int deferred = 1;
     for (int i = 0; i < ndraws; i++)
-        if (draws[i].blend_enable) deferred = 0;
+        if (draws[i].polygon_rules && draws[i].polygon_mode != 0) {
+            int rc = (ndraws == 1 && S == 1) ? ref_rules_draw(&c, &draws[0], t, scol) : 5;
+            if (rc) { free(scol); return rc; }
+            ndraws = 0;  /* drawn; resolve below */
+        }
+    if (nthreads < 1) nthreads = 1;
+    if (nthreads > c.r1 - c.r0) nthreads = c.r1 - c.r0;
+    if (nthreads > 256) nthreads = 256;
+    /* the draws before the first blended one are shaded deferred */
+    int deferred = ndraws > 0 && !draws[0].blend_enable;
     int64_t* win = NULL;
     if (deferred) {
         win = (int64_t*)malloc(npix * S * sizeof(int64_t));
@@ -1097,8 +1297,8 @@ int ofx_render_pass(const ofx_draw* draws, int ndraws, ofx_target* t, int clear,
             jobs[i].draws = draws; jobs[i].ndraws = ndraws; jobs[i].t = t; jobs[i].c = &c; jobs[i].scol = scol;
             jobs[i].win = win; jobs[i].id = i; jobs[i].nthreads = nthreads; jobs[i].bar = &bar;
             jobs[i].lists = lists; jobs[i].counts = counts;
-            jobs[i].y0 = (int)((int64_t)c.H * i / nthreads);
-            jobs[i].y1 = (int)((int64_t)c.H * (i + 1) / nthreads);
+            jobs[i].y0 = c.r0 + (int)((int64_t)(c.r1 - c.r0) * i / nthreads);
+            jobs[i].y1 = c.r0 + (int)((int64_t)(c.r1 - c.r0) * (i + 1) / nthreads);
         }
         if (nthreads == 1) run_pass(&jobs[0]);
         else {

@@ -75,6 +75,10 @@ typedef struct {
      * reference supports (ZERO, ONE, SRC_ALPHA, ONE_MINUS_SRC_ALPHA, DST_ALPHA,
      * ONE_MINUS_DST_ALPHA).  Pinning only; the GPU path blends by the factors' names. */
     int blend_compat;
+    /* polygon_mode 1 / 2 with polygon_rules = 1: the reference's own line and point pipelines
+     * (Bresenham lines over triangle edges, truncated points per index; see oracle_fx.c) instead
+     * of the fill-rule parts above; only as the single draw of a pass on a 1-sample target. */
+    int polygon_rules;
 } ofx_draw;
 
 typedef struct {
@@ -84,6 +88,8 @@ typedef struct {
     void* color;                /* resolved colour, format-dependent, row-major */
     float* depth;               /* per-sample depth [H][W][S] */
     int* vis;                   /* per-sample visible primitive id [H][W][S], -1 = none */
+    int row0, rows;             /* rows > 0: the buffers hold only rows [row0, row0 + rows) of the
+                                   height-row frame (a horizontal band rendered alone) */
 } ofx_target;
 
 /* Renders one pass of `ndraws` draws into `t`.  clear != 0 clears colour to clear_color

@@ -233,3 +233,19 @@ def test_line_mode_one_pixel_per_column_along_an_x_major_edge():
     # and the lines are there at 4x too, with every pixel they touch holding at least one sample
     vis4 = O.render([d], W, H, 4)["vis"] >= 0
     assert vis4[:10, 5:18].any(axis=2).sum(0).min() >= 1
+
+
+def test_row_band_render_matches_full_frame():
+    """Rendering only rows [y0, y1) of a frame (every triangle set up, only the band rasterised)
+    reproduces those rows of the full render exactly, for a deferred and a blended pass."""
+    from ifrit_gb300 import scenes
+    v, f, mvp = scenes.triangle_soup(20000, 4, 320, 200)
+    opaque = O.make_draw(v, f[:10000], mvp, attr_offset=3, attr_count=2, cull_mode=0, depth_func=3)
+    blended = O.make_draw(v, f[10000:], mvp, attr_offset=3, attr_count=2, cull_mode=0, depth_func=3, depth_write=0,
+                          blend=(6, 7, 1, 7), prim_base=10000)
+    for draws in ([opaque], [opaque, blended]):
+        full = O.render(draws, 320, 200, 4, nthreads=4)
+        for y0, y1 in ((0, 64), (70, 134), (199, 200)):
+            band = O.render(draws, 320, 200, 4, nthreads=3, rows=(y0, y1))
+            for k in ("color", "depth", "vis"):
+                assert np.array_equal(full[k][y0:y1].view(np.uint8), band[k].view(np.uint8)), (k, y0, y1)
