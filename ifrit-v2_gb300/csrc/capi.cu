@@ -422,6 +422,7 @@ int consume_status(IfritGbRenderer* h, PassScratch& s) {
         return rc ? rc : IFTR_ERR_OVERFLOW;
     }
     if (sticky & 2u) return IFTR_ERR_LIMIT;
+    if (sticky & 4u) return IFTR_ERR_CUDA;  // a bulk copy into shared memory did not complete in time
     return IFTR_OK;
 }
 

@@ -156,5 +156,6 @@ extern "C" IFTR_API int iftrDrawNoAlloc(const IfritGbNoAllocPass* p, void* cudaS
     if (cudaMemcpyAsync(status, base + kOffStatus, sizeof(status), cudaMemcpyDeviceToHost, stream) != cudaSuccess ||
         cudaStreamSynchronize(stream) != cudaSuccess)
         return IFTR_ERR_CUDA;
+    if (status[ifr::ST_STICKY] & 4u) return IFTR_ERR_CUDA;  // a bulk copy into shared memory did not complete
     return status[ifr::ST_OVERFLOW] ? IFTR_ERR_OVERFLOW : IFTR_OK;
 }

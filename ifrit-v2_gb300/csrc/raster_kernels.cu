@@ -73,14 +73,15 @@ __device__ __forceinline__ void bin_sub(const PassArgs& a, const ViewArgs& v, co
 // path: fetch, transform, clip and set-up; writes the triangle's record (and vertex attributes)
 // and hands every visible (sub-)triangle to emit(view, draw, sub-triangle, entry).
 template <class Emit>
-__device__ __forceinline__ void front_end(const PassArgs& a, int g, int di, const Emit& emit) {
+__device__ __forceinline__ void front_end(const PassArgs& a, int g, int di, const Emit& emit,
+                                          const StagedInput* st = nullptr) {
     const DrawDev& d = a.draws[di];
     const ViewArgs& v = a.views[d.view];
     int t = g - __ldg(a.draw_start + di);
     CVert poly[3];  // registers: only the rare clipping path below goes through memory
     bool inside, rejected;
     TriRecord* rec = a.records + g;
-    if (!fetch_triangle(v.c, d, t, poly, inside, rejected)) {
+    if (!fetch_triangle(v.c, d, t, poly, inside, rejected, st)) {
         rec->flags = 0;
         return;
     }
@@ -95,7 +96,7 @@ __device__ __forceinline__ void front_end(const PassArgs& a, int g, int di, cons
         r.draw = di;
         if (a.attrs && d.shading != SHADE_PRIMID && d.attr_count > 0) {
             float a0[4], a1[4], a2[4];
-            fetch_attrs(d, t, a0, a1, a2);
+            fetch_attrs_staged(d, st, t, a0, a1, a2);
             float4* dst = a.attrs[g].a;
             dst[0] = make_float4(a0[0], a0[1], a0[2], a0[3]);
             dst[1] = make_float4(a1[0], a1[1], a1[2], a1[3]);
@@ -121,7 +122,7 @@ __device__ __forceinline__ void front_end(const PassArgs& a, int g, int di, cons
         r.draw = di;
         if (a.attrs && d.shading != SHADE_PRIMID && d.attr_count > 0) {
             float a0[4], a1[4], a2[4];
-            fetch_attrs(d, t, a0, a1, a2);
+            fetch_attrs_staged(d, st, t, a0, a1, a2);
             float4* dst = a.attrs[g].a;
             dst[0] = make_float4(a0[0], a0[1], a0[2], a0[3]);
             dst[1] = make_float4(a1[0], a1[1], a1[2], a1[3]);
@@ -228,15 +229,158 @@ __device__ __forceinline__ void warp_tiles(const PassArgs& a, const WarpTiles& w
     }
 }
 
+// ---- bulk copies into shared memory (TMA, cp.async.bulk) with an mbarrier
+__device__ __forceinline__ uint32_t smem_addr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+// Arms the barrier's current phase for `bytes` of bulk-copy data and copies [src, src + bytes)
+// (both 16-byte aligned, bytes a multiple of 16) into shared memory at dst.  One thread.
+__device__ __forceinline__ void bulk_load(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes) : "memory");
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+                 ::"r"(smem_addr(dst)), "l"(src), "r"(bytes), "r"(smem_addr(bar))
+                 : "memory");
+}
+
+// Waits for the barrier phase of the given parity, giving up after kBulkWaitLimit polls.
+constexpr int kBulkWaitLimit = 1 << 20;
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+    for (int i = 0; i < kBulkWaitLimit; i++) {
+        uint32_t ok;
+        asm volatile(
+            "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+            : "=r"(ok)
+            : "r"(smem_addr(bar)), "r"(parity)
+            : "memory");
+        if (ok) return true;
+    }
+    return false;
+}
+
+// Stages [src, src + bytes) (4-byte aligned) so that its byte i lands at the returned address + i
+// inside `buf` (16-byte aligned, at least bytes + 16 long): the 16-byte-aligned inner part by one
+// bulk copy from thread 0 on the barrier's next phase, the unaligned head and tail (under 16
+// bytes each) by plain loads.  All threads call it with the same arguments; `phases` counts the
+// barrier phases used so far.  ok (the same in every thread) is false if the wait gave up, which
+// is also recorded in the pass status.
+__device__ __forceinline__ const unsigned char* stage_bytes(const PassArgs& a, const void* src, uint32_t bytes,
+                                                            unsigned char* buf, uint64_t* bar, uint32_t& phases,
+                                                            bool& ok) {
+    const uintptr_t s0 = (uintptr_t)src, s1 = s0 + bytes;
+    const uintptr_t i0 = (s0 + 15) & ~(uintptr_t)15, i1 = s1 & ~(uintptr_t)15;
+    unsigned char* out = buf + (s0 & 15);
+    const bool bulk = i1 > i0;
+    if (bulk && threadIdx.x == 0) bulk_load(out + (i0 - s0), reinterpret_cast<const void*>(i0), (uint32_t)(i1 - i0), bar);
+    // head and tail words (the whole range when it holds no aligned 16 bytes)
+    const uint32_t* w = static_cast<const uint32_t*>(src);
+    uint32_t* o = reinterpret_cast<uint32_t*>(out);
+    const int nw = (int)(bytes / 4);
+    const int head = bulk ? (int)((i0 - s0) / 4) : nw, tail = bulk ? (int)((i1 - s0) / 4) : nw;
+    for (int k = threadIdx.x; k < head; k += blockDim.x) o[k] = __ldg(w + k);
+    for (int k = tail + threadIdx.x; k < nw; k += blockDim.x) o[k] = __ldg(w + k);
+    bool mine = true;
+    if (bulk) {
+        mine = mbar_wait(bar, phases & 1u);
+        phases++;
+    }
+    ok = __syncthreads_and(mine) != 0;
+    if (!ok && threadIdx.x == 0) atomicOr(a.status + ST_STICKY, 4u);
+    return out;
+}
+
+constexpr int kStageTris = 256;                        // counting-binner CTA size
+constexpr int kStageIdxBytes = kStageTris * 12 + 16;   // the CTA's index slice
+constexpr int kStageVtxBytes = 20 * 1024 + 16;         // vertex window (unshared or local vertices)
+
+// Stages the CTA's index slice, and the vertex rows its triangles reference when they fit, in
+// shared memory; only when all of the CTA's triangles belong to one draw.  `phases`: barrier
+// phases used; all_ok false if a wait gave up (the kernel waits once more before it exits).
+__device__ __forceinline__ void stage_block(const PassArgs& a, StagedInput& st, unsigned char* sidx, unsigned char* svtx,
+                                            uint64_t* bar, int* sh, uint32_t& phases, bool& all_ok) {
+    st.idx = nullptr;
+    st.verts = nullptr;
+    all_ok = true;
+    phases = 0;
+    const int g0 = blockIdx.x * kStageTris;
+    const int n = min(kStageTris, a.total_tris - g0);
+    if (threadIdx.x == 0) {
+        const int d0 = find_draw(a, g0), d1 = find_draw(a, g0 + n - 1);
+        sh[0] = d0 == d1 ? d0 : -1;
+        sh[1] = 0x7fffffff;  // window: smallest and largest vertex index
+        sh[2] = -1;
+        mbar_init(bar, 1);
+    }
+    __syncthreads();
+    const int di = sh[0];
+    if (di < 0) return;
+    const DrawDev& d = a.draws[di];
+    const int t0 = g0 - __ldg(a.draw_start + di);
+    bool ok;
+    const unsigned char* ip = stage_bytes(a, d.indices + 3 * (size_t)t0, 12u * (uint32_t)n, sidx, bar, phases, ok);
+    if (!ok) {
+        all_ok = false;
+        return;
+    }
+    st.idx = reinterpret_cast<const int*>(ip);
+    st.t_first = t0;
+    st.t_end = t0 + n;
+    // the vertex window of the CTA's triangles
+    int lo = 0x7fffffff, hi = -1;
+    for (int k = threadIdx.x; k < 3 * n; k += blockDim.x) {
+        const int vid = st.idx[k];
+        if (vid >= 0 && vid < d.num_vertices) {
+            lo = min(lo, vid);
+            hi = max(hi, vid);
+        }
+    }
+    lo = __reduce_min_sync(0xffffffffu, lo);
+    hi = __reduce_max_sync(0xffffffffu, hi);
+    if ((threadIdx.x & 31) == 0) {
+        atomicMin(sh + 1, lo);
+        atomicMax(sh + 2, hi);
+    }
+    __syncthreads();
+    lo = sh[1];
+    hi = sh[2];
+    if (hi < lo) return;
+    const size_t vbytes = (size_t)(hi - lo + 1) * d.stride * 4;
+    if (vbytes + 16 > (size_t)kStageVtxBytes) return;
+    const unsigned char* vp = stage_bytes(a, d.vertices + (size_t)lo * d.stride, (uint32_t)vbytes, svtx, bar, phases, ok);
+    if (!ok) {
+        all_ok = false;
+        return;
+    }
+    st.verts = reinterpret_cast<const float*>(vp);
+    st.v_first = lo;
+    st.v_end = hi + 1;
+}
+
 // Counting pass: full front end per triangle; unclipped triangles leave a compact record.
-__global__ void __launch_bounds__(256) bin_count_kernel(PassArgs a) {
+// The CTA's index slice and, when it fits, its vertex window come into shared memory by bulk
+// copies (TMA) first.
+__global__ void __launch_bounds__(kStageTris) bin_count_kernel(PassArgs a) {
+    __shared__ __align__(16) unsigned char s_idx[kStageIdxBytes];
+    __shared__ __align__(16) unsigned char s_vtx[kStageVtxBytes];
+    __shared__ __align__(8) uint64_t s_bar;
+    __shared__ int s_info[3];
     const int g = blockIdx.x * blockDim.x + threadIdx.x;
+    StagedInput st;
+    bool staged_ok;
+    uint32_t phases;
+    stage_block(a, st, s_idx, s_vtx, &s_bar, s_info, phases, staged_ok);
     const int di = find_draw_warp(a, min(g, a.total_tris - 1));
     WarpTiles w;
     w.big = w.small = false;
-    if (g < a.total_tris) front_end(a, g, di, CountEmit{a, w});
+    if (g < a.total_tris) front_end(a, g, di, CountEmit{a, w}, &st);
     warp_small_tiles(a, w, false);
     warp_tiles(a, w, g, false);
+    if (!staged_ok && phases > 0)  // a wait gave up: let the copy land before the CTA's shared memory goes
+        mbar_wait(&s_bar, (phases - 1) & 1u);
 }
 
 // Scattering pass: same overlaps as the counting pass, read back from the records (clipped
@@ -1546,6 +1690,9 @@ struct FwdRecords {
     int32_t draw[kFwdThreads];
 };
 
+static_assert(sizeof(FwdRecords) >= kFwdThreads * (sizeof(float4) + sizeof(int2)),
+              "the ordered stage reuses the record arrays as per-warp shading scratch");
+
 constexpr int kFwdFrags = 8;  // fragments a pixel holds before they are shaded
 
 // Shades fragment f = (entry, sample mask) at pixel (px, py) and writes or blends it into the
@@ -1577,6 +1724,151 @@ template <int S>
 __device__ __noinline__ void apply_fragments(const PassArgs& a, const ViewArgs& v, int px, int py, float4* scol,
                                              const int2* frags, int n) {
     for (int i = 0; i < n; i++) apply_fragment<S>(a, v, px, py, scol, frags[i * kFwdThreads + threadIdx.x]);
+}
+
+// The recorded fragments of a warp's 32 pixels, shaded warp-cooperatively and applied in order.
+// Items (pixel, fragment) are numbered pixel-major in fragment order and taken 32 per round, one
+// per lane, whatever pixel it belongs to (the quad derivatives are evaluated analytically at the
+// owner's pixel); each round's anisotropic probes are spread over all lanes and summed per item in
+// probe order (as the shade stage does), then every lane applies the round's items of its own pixel
+// in item order, so each pixel still sees its fragments in submission order.  `wres` (32 float4)
+// and `wmeta` (32 int2) are the warp's shared scratch.
+template <int S>
+__device__ __forceinline__ void shade_fragments_warp(const PassArgs& a, const ViewArgs& v, int tx0, int ty0,
+                                                     float4* scol, const int2* frags, int nfrag, float4* wres,
+                                                     int2* wmeta) {
+    constexpr int NT = kFwdThreads;
+    const int lane = threadIdx.x & 31, wbase = threadIdx.x & ~31;
+    int incl = nfrag;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int q = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += q;
+    }
+    const int pre_f = incl - nfrag;
+    const int total = __shfl_sync(0xffffffffu, incl, 31);
+    for (int r0 = 0; r0 < total; r0 += 32) {
+        const int b = r0 + lane;
+        int owner = 0;  // the last lane whose first item is at or before b
+#pragma unroll
+        for (int step = 16; step > 0; step >>= 1)
+            if (__shfl_sync(0xffffffffu, pre_f, owner + step) <= b) owner += step;
+        const int fi = b - __shfl_sync(0xffffffffu, pre_f, owner);
+        int di = 0, n = 0, mask = 0;
+        float c[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+        TexProbe tp;
+        tp.u = tp.v = tp.du = tp.dv = tp.t = 0.0f;
+        tp.lo = tp.hi = tp.n = 0;
+        tp.two = tp.aniso = false;
+        if (b < total) {
+            const int2 f = frags[fi * NT + wbase + owner];
+            mask = f.y;
+            int olx, oly;
+            tile_pixel<16>(wbase + owner, olx, oly);
+            const int opx = tx0 + olx, opy = ty0 + oly;
+            const int g = f.x >> 3, sub = f.x & 7;
+            const TriRecord* rp = a.records + g;
+            const int4 q1 = __ldg(reinterpret_cast<const int4*>(rp) + 1);  // X2, Y2, flags, draw
+            di = q1.w;
+            const DrawDev& d = a.draws[di];
+            const int t = g - __ldg(a.draw_start + di);
+            const bool from_record = sub == 0 && (q1.z & REC_VALID) && d.polygon_mode == POLY_FILL;
+            ShadeGeom geo;
+            float4 plane;
+            int plane_y;
+            if (from_record) {
+                shade_geom_record(rp, q1, geo, plane, plane_y);
+            } else {
+                ShadeGeom tg;
+                float4 tpl;
+                int tpy;
+                shade_geom_general(v.c, d, a.records, g, t, sub, &tg, &tpl, &tpy);
+                geo = tg;
+            }
+            float a0[4], a1[4], a2[4];
+            if (sub == 0 && (q1.z & REC_VALID) && a.attrs && d.shading != SHADE_PRIMID && d.attr_count > 0) {
+                const float4 p0 = __ldg(&a.attrs[g].a[0]), p1 = __ldg(&a.attrs[g].a[1]), p2 = __ldg(&a.attrs[g].a[2]);
+                a0[0] = p0.x; a0[1] = p0.y; a0[2] = p0.z; a0[3] = p0.w;
+                a1[0] = p1.x; a1[1] = p1.y; a1[2] = p1.z; a1[3] = p1.w;
+                a2[0] = p2.x; a2[1] = p2.y; a2[2] = p2.z; a2[3] = p2.w;
+            } else if (d.shading != SHADE_PRIMID) {
+                fetch_attrs(d, t, a0, a1, a2);
+            } else {
+#pragma unroll
+                for (int k = 0; k < 4; k++) a0[k] = a1[k] = a2[k] = 0.0f;
+            }
+            if (shade_prepare_attrs(v.c, d, geo, t, sub, opx, opy, a0, a1, a2, c, tp)) n = tp.n;
+        }
+        int pincl = n;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int q = __shfl_up_sync(0xffffffffu, pincl, o);
+            if (lane >= o) pincl += q;
+        }
+        const int T = __shfl_sync(0xffffffffu, pincl, 31);
+        if (T > 0) {
+            const int pre = pincl - n;
+            const int packed = tp.lo | (tp.hi << 8) | (tp.n << 16) | (tp.two ? 1 << 24 : 0) | (tp.aniso ? 1 << 25 : 0);
+            float acc[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+            for (int c0 = 0; c0 < T; c0 += 32) {
+                const int j = c0 + lane;
+                int k = 0;  // the item of probe j: the last lane whose first probe is at or before j
+#pragma unroll
+                for (int step = 16; step > 0; step >>= 1)
+                    if (__shfl_sync(0xffffffffu, pre, k + step) <= j) k += step;
+                TexProbe q;
+                q.u = __shfl_sync(0xffffffffu, tp.u, k);
+                q.v = __shfl_sync(0xffffffffu, tp.v, k);
+                q.du = __shfl_sync(0xffffffffu, tp.du, k);
+                q.dv = __shfl_sync(0xffffffffu, tp.dv, k);
+                q.t = __shfl_sync(0xffffffffu, tp.t, k);
+                const int qp = __shfl_sync(0xffffffffu, packed, k);
+                const int qd = __shfl_sync(0xffffffffu, di, k);
+                const int i = j - __shfl_sync(0xffffffffu, pre, k);
+                q.lo = qp & 255;
+                q.hi = (qp >> 8) & 255;
+                q.n = (qp >> 16) & 255;
+                q.two = (qp >> 24) & 1;
+                q.aniso = (qp >> 25) & 1;
+                float r[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+                if (j < T) tex_probe(a.draws[qd], q, i, r);
+                wres[lane] = make_float4(r[0], r[1], r[2], r[3]);
+                __syncwarp();
+                const int qa = max(pre, c0), qb = min(pre + n, c0 + 32);
+                for (int m = qa; m < qb; m++) {
+                    const float4 x = wres[m - c0];
+                    acc[0] = acc[0] + x.x; acc[1] = acc[1] + x.y; acc[2] = acc[2] + x.z; acc[3] = acc[3] + x.w;
+                }
+                __syncwarp();
+            }
+            if (n > 0) tex_finish(tp, acc, c);
+        }
+        wres[lane] = make_float4(c[0], c[1], c[2], c[3]);
+        wmeta[lane] = make_int2(b < total ? owner | (mask << 5) : -1, di);
+        __syncwarp();
+        const int nr = min(32, total - r0);
+        for (int m = 0; m < nr; m++) {
+            const int2 md = wmeta[m];
+            if ((md.x & 31) != lane) continue;
+            const float4 x = wres[m];
+            const float col[4] = {x.x, x.y, x.z, x.w};
+            const DrawDev& d = a.draws[md.y];
+            const unsigned fm = (unsigned)md.x >> 5;
+#pragma unroll
+            for (int k = 0; k < S; k++) {
+                if (!(fm & (1u << k))) continue;
+                float4& sc = scol[k * NT + threadIdx.x];
+                if (d.blend_enable) {
+                    float dst[4] = {sc.x, sc.y, sc.z, sc.w};
+                    blend_into(d, col, dst);
+                    sc = make_float4(dst[0], dst[1], dst[2], dst[3]);
+                } else {
+                    sc = make_float4(col[0], col[1], col[2], col[3]);
+                }
+            }
+        }
+        __syncwarp();
+    }
 }
 
 template <int S>
@@ -1648,25 +1940,36 @@ __device__ __forceinline__ void forward_tile(const PassArgs& a, const ViewArgs& 
         }
         n = 0;
     }
-    // sort them into submission order (bitonic, padded to 2^k)
-    int P = 1;
-    while (P < n) P <<= 1;
-    for (int i = n + tid; i < P; i += NT) list[i] = 0xFFFFFFFFu;
-    __syncthreads();
-    for (int k = 2; k <= P; k <<= 1) {
-        for (int j = k >> 1; j > 0; j >>= 1) {
-            for (int i = tid; i < P; i += NT) {
-                int ixj = i ^ j;
-                if (ixj > i) {
-                    uint32_t x = list[i], y = list[ixj];
-                    bool up = (i & k) == 0;
-                    if ((x > y) == up) {
-                        list[i] = y;
-                        list[ixj] = x;
+    // sort them into submission order: up to one entry per thread by rank (entries are distinct, so
+    // every rank is; two barriers), longer lists bitonically (padded to 2^k)
+    if (n <= NT) {
+        const uint32_t e = tid < n ? list[tid] : 0u;
+        int rank = 0;
+        if (tid < n)
+            for (int j = 0; j < n; j++) rank += list[j] < e;
+        __syncthreads();
+        if (tid < n) list[rank] = e;
+        __syncthreads();
+    } else {
+        int P = 1;
+        while (P < n) P <<= 1;
+        for (int i = n + tid; i < P; i += NT) list[i] = 0xFFFFFFFFu;
+        __syncthreads();
+        for (int k = 2; k <= P; k <<= 1) {
+            for (int j = k >> 1; j > 0; j >>= 1) {
+                for (int i = tid; i < P; i += NT) {
+                    int ixj = i ^ j;
+                    if (ixj > i) {
+                        uint32_t x = list[i], y = list[ixj];
+                        bool up = (i & k) == 0;
+                        if ((x > y) == up) {
+                            list[i] = y;
+                            list[ixj] = x;
+                        }
                     }
                 }
+                __syncthreads();
             }
-            __syncthreads();
         }
     }
 
@@ -1733,11 +2036,13 @@ __device__ __forceinline__ void forward_tile(const PassArgs& a, const ViewArgs& 
         }
         __syncthreads();
     }
-    // shade the recorded fragments with the warp converged on fragment slot i of every lane, and
-    // apply each one in submission order to its samples
-    const int maxn = __reduce_max_sync(0xffffffffu, nfrag);
-    for (int i = 0; i < maxn; i++)
-        if (i < nfrag) apply_fragment<S>(a, v, px, py, scol, frags[i * NT + tid]);
+    // shade the recorded fragments warp-cooperatively and apply each one in submission order to
+    // its samples; the record arrays are free again (every thread passed the batch loop's barrier)
+    {
+        float4* wres = reinterpret_cast<float4*>(&rec) + (tid >> 5) * 32;
+        int2* wmeta = reinterpret_cast<int2*>(reinterpret_cast<float4*>(&rec) + NT) + (tid >> 5) * 32;
+        shade_fragments_warp<S>(a, v, tx * TS, ty * TS, scol, frags, nfrag, wres, wmeta);
+    }
     if (!inpix) return;
     float acc[4];
 #pragma unroll

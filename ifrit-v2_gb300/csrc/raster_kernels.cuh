@@ -15,7 +15,8 @@ constexpr int kMaxViews = 4096;
 
 // Status words of a pass.  Words below ST_PASS_WORDS describe the latest pass and are cleared
 // when it starts; ST_STICKY (bit 0: some pass overflowed its pair list, bit 1: some ordered tile
-// exceeded kOrderedCap) and ST_MAX_PAIRS accumulate until the host reads and clears them.
+// exceeded kOrderedCap, bit 2: a bulk copy into shared memory was not seen complete within the
+// wait limit) and ST_MAX_PAIRS accumulate until the host reads and clears them.
 enum StatusWord {
     ST_OVERFLOW = 0,
     ST_PAIRS = 1,

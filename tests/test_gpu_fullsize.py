@@ -50,15 +50,15 @@ def test_stress_frame_full_size_bands():
 
     chain, levels = O.build_mips(sc["texture"])
     tex = (chain, levels, sc["texture"].shape[1], sc["texture"].shape[0])
-    odraws, blended = [], []
+    odraws, blended, base = [], [], 0  # primitive ids count triangles in pass order
     for d in sc["draws"]:
-        first = d["first"] // 3
-        f = sc["indices"][first:(d["first"] + d["count"]) // 3]
+        f = sc["indices"][d["first"] // 3:(d["first"] + d["count"]) // 3]
         odraws.append(O.make_draw(sc["vertices"], f, d["mvp"], attr_offset=3, attr_count=2, cull_mode=2, depth_func=3,
                                   depth_write=int(not d["blend"]), blend=(6, 7, 1, 7) if d["blend"] else None,
-                                  shading=O.SHADE_TEXTURED, texture=tex, sampler={"max_aniso": 16}, prim_base=first))
+                                  shading=O.SHADE_TEXTURED, texture=tex, sampler={"max_aniso": 16}, prim_base=base))
         if d["blend"]:
-            blended.append((first, first + len(f)))
+            blended.append((base, base + len(f)))
+        base += len(f)
     assert len(blended) == 4
     # three bands centred on where the first three blended instances are visible
     bands = []
