@@ -761,7 +761,8 @@ def run_ours_c5(args):
                        "width": W, "height": H, "samples": 8, "triangles": T, "shaded_samples_per_frame": shaded,
                        "l2": "inputs larger than L2 (no flush)", "parallelism": "replicas" if world > 1 else "single"},
             "tris_per_s": world * T / (m / 1000.0),
-            "stage_ms": {"binning": st[0] + st[1] + st[2], "raster": st[3], "shade": st[4], "ordered": st[5]},
+            "stage_ms": {"binning": st[0] + st[1] + st[2], "raster": st[3], "shade": st[4], "ordered": st[5],
+                         "binning_count_scan_scatter": st[:3]},
             "roofline": {"bound": "hbm", "achieved": B / t_tile / 1e9, "peak": peak, "unit": "GB/s",
                          "frac": B / t_tile / 1e9 / peak, "traffic": profiled_traffic("c5"), "algorithmic_bytes": B,
                          "kernel": "tile stage (raster + shade + ordered kernels)", "peak_source": peak_kind},
@@ -788,7 +789,7 @@ def run_ours_c5(args):
                                                  "pass_roofline_frac", "e2e")}
         line["plain_c2"]["workload"] = workload("c2")["desc"]
         res1 = measure_frame(workload("c1"), 20, 3, 3)
-        line["plain_c1"] = {k: res1[k] for k in ("value", "ms_per_step", "tris_per_s", "e2e")}
+        line["plain_c1"] = {k: res1[k] for k in ("value", "ms_per_step", "tris_per_s", "stage_ms", "e2e")}
         torch.cuda.empty_cache()
         res3 = run_c3(args, 5, 3, 3, with_cpu=False)
         line["batched_c3"] = {k: res3[k] for k in ("value", "ms_per_step", "tris_per_s", "views", "triangles", "tuning",
@@ -853,7 +854,7 @@ def measure_frame(w, steps, warmup, e2e_steps, dist=None, world=1):
         r.finish()
     ev0 = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
     ev1 = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
-    tile_ms, bin_ms, raster_ms, shade_ms = [], [], [], []
+    tile_ms, bin_ms, raster_ms, shade_ms, bin_parts = [], [], [], [], []
     clocks = ClockSampler()
     clocks.start()
     if dist:
@@ -866,6 +867,7 @@ def measure_frame(w, steps, warmup, e2e_steps, dist=None, world=1):
         ev1[i].record(stream)
         r.finish()
         st = r.stage_times()
+        bin_parts.append(st[:3])
         bin_ms.append(st[0] + st[1] + st[2])
         raster_ms.append(st[3])
         shade_ms.append(st[4])
@@ -902,7 +904,8 @@ def measure_frame(w, steps, warmup, e2e_steps, dist=None, world=1):
         "value": world * shaded / (ms / 1000.0), "ms_per_step": ms, "shaded": shaded,
         "tris_per_s": world * len(w["indices"]) / (ms / 1000.0),
         "stage_ms": {"binning": statistics.mean(bin_ms), "raster": statistics.mean(raster_ms),
-                     "shade": statistics.mean(shade_ms)},
+                     "shade": statistics.mean(shade_ms),
+                     "binning_count_scan_scatter": [statistics.mean(x[i] for x in bin_parts) for i in range(3)]},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": profiled_traffic(w["name"]), "algorithmic_bytes": B,
                      "kernel": "tile stage (raster + shade kernels)", "peak_source": peak_kind},

@@ -87,6 +87,20 @@ inline void set_view_depth_state(ViewArgs& v, const DrawDev* draws, int n) {
     int i = 0;
     while (i < n && order_independent(draws[i], draws[0])) v.ordered_prefix += draws[i++].num_triangles;
     if (i < n) v.ordered = 1;
+    // Occlusion culling of ordered entries per tile: depths only ever decrease after a prefix that
+    // writes under LESS / LEQUAL when every later draw either writes nothing or writes under LESS,
+    // LEQUAL, EQUAL or NEVER.
+    v.ordered_cull = 0;
+    if (v.ordered && v.ordered_prefix > 0 && v.depth_write &&
+        (v.depth_func == IF_COMPARE_OP_LESS || v.depth_func == IF_COMPARE_OP_LESS_OR_EQUAL)) {
+        v.ordered_cull = 1;
+        for (int j = i; j < n; j++) {
+            const int f = draws[j].depth_func;
+            if (draws[j].depth_write && f != IF_COMPARE_OP_LESS && f != IF_COMPARE_OP_LESS_OR_EQUAL &&
+                f != IF_COMPARE_OP_EQUAL && f != IF_COMPARE_OP_NEVER)
+                v.ordered_cull = 0;
+        }
+    }
 }
 
 inline bool valid_samples(int S) { return S == 1 || S == 2 || S == 4 || S == 8 || S == 16; }

@@ -177,10 +177,11 @@ struct CountEmit {
     }
 };
 
-// Warp-aggregated list updates of the lanes' small tile ranges: for every tile slot k of the
-// ranges, the lanes naming the same tile (__match_any_sync) make one atomicAdd of their count,
-// issued by the lowest of them; scattering, each lane's list slot is the returned base plus its
-// rank among those lanes.  Lanes of a warp hold consecutive triangles, which in a mesh are
+// Warp-aggregated list slots for the lanes' small tile ranges (the scattering pass, whose atomics
+// return the slot the store waits for; the counting pass needs no result and issues one
+// fire-and-forget reduction per tile instead): for every tile slot k of the ranges, the lanes naming
+// the same tile (__match_any_sync) make one atomicAdd of their count, issued by the lowest of them,
+// and each lane's list slot is the returned base plus its rank among those lanes.  Lanes of a warp hold consecutive triangles, which in a mesh are
 // neighbours and mostly share tiles.  List order within a tile carries no meaning (the
 // order-independent stages key by entry, the ordered stage sorts).
 __device__ __forceinline__ void warp_small_tiles(const PassArgs& a, const WarpTiles& w, bool scatter) {
@@ -377,7 +378,9 @@ __global__ void __launch_bounds__(kStageTris) bin_count_kernel(PassArgs a) {
     WarpTiles w;
     w.big = w.small = false;
     if (g < a.total_tris) front_end(a, g, di, CountEmit{a, w}, &st);
-    warp_small_tiles(a, w, false);
+    if (w.small)  // counts need no result back: one fire-and-forget reduction per tile
+        for (int ty = w.ty0; ty <= w.ty1; ty++)
+            for (int tx = w.tx0; tx <= w.tx1; tx++) atomicAdd(a.tile_count + w.tbase + ty * w.tiles_x + tx, 1u);
     warp_tiles(a, w, g, false);
     if (!staged_ok && phases > 0)  // a wait gave up: let the copy land before the CTA's shared memory goes
         mbar_wait(&s_bar, (phases - 1) & 1u);
@@ -697,6 +700,41 @@ struct RecordPlane {
     float z0, dzdx, dzdy;
     int32_t X0, Y0;
 };
+// The depth a depth-order word stands for (inverse of depth_order).
+__device__ __forceinline__ float order_depth(uint32_t u) {
+    return __uint_as_float((u & 0x80000000u) ? (u & 0x7fffffffu) : ~u);
+}
+
+// Whether ordered entry e may pass its depth test anywhere in a tile whose farthest prefix depth
+// is dmax (its samples' depths only decrease from there: ViewArgs::ordered_cull).  Conservative:
+// true unless the entry is an unclipped filled triangle under LESS / LEQUAL / EQUAL (or NEVER)
+// whose depth plane, over its bounding box clipped to the tile's sample positions, lies beyond
+// dmax by more than the rounding of the per-sample evaluation (2^-20 of the terms' magnitudes).
+__device__ __forceinline__ bool may_pass_tile(const PassArgs& a, const PassConst& c, uint32_t e, int tx0, int ty0,
+                                              int xmax, int ymax, float dmax) {
+    const int g = (int)(e >> 3);
+    if ((e & 7u) != 0u) return true;
+    const TriRecord* rp = a.records + g;
+    const int4 q1 = __ldg(reinterpret_cast<const int4*>(rp) + 1);  // X2, Y2, flags, draw
+    if (!(q1.z & REC_VALID)) return true;
+    const DrawDev& d = a.draws[q1.w];
+    if (d.polygon_mode != POLY_FILL) return true;
+    const int f = d.depth_func;
+    if (f == 0) return false;  // NEVER
+    if (f != 1 && f != 3 && f != 2) return true;
+    const int4 q0 = __ldg(reinterpret_cast<const int4*>(rp));
+    const float4 q2 = __ldg(reinterpret_cast<const float4*>(rp) + 2);  // z0, dz/dx, dz/dy
+    const int32_t sx0 = max(min(q0.x, min(q0.z, q1.x)), tx0 * 256 + c.smin_x);
+    const int32_t sx1 = min(max(q0.x, max(q0.z, q1.x)), xmax * 256 + c.smax_x);
+    const int32_t sy0 = max(min(q0.y, min(q0.w, q1.y)), ty0 * 256 + c.smin_y);
+    const int32_t sy1 = min(max(q0.y, max(q0.w, q1.y)), ymax * 256 + c.smax_y);
+    if (sx0 > sx1 || sy0 > sy1) return false;  // no sample of the tile inside its bounding box
+    const float ax = q2.y * (float)(sx0 - q0.x), bx = q2.y * (float)(sx1 - q0.x);
+    const float ay = q2.z * (float)(sy0 - q0.y), by = q2.z * (float)(sy1 - q0.y);
+    const float zmin = (q2.x + fminf(ax, bx)) + fminf(ay, by);
+    const float margin = (fabsf(q2.x) + fmaxf(fabsf(ax), fabsf(bx)) + fmaxf(fabsf(ay), fabsf(by))) * 0x1p-20f;
+    return !(zmin - margin > dmax);
+}
 
 // ---------------------------------------------------------------------------- atomic visibility
 // Alternative to binning + the tile raster stage for deferred views: the thread of each triangle
@@ -1059,7 +1097,6 @@ __device__ __forceinline__ void raster_tile(const PassArgs& a, const ViewArgs& v
     const uint32_t beg = has_list ? a.tile_offset[gtile] : 0u;
     const uint32_t end = has_list ? a.tile_offset[gtile + 1] : 0u;
     const int xmax = min(v.c.W, tx0 + TS) - 1, ymax = min(v.c.H, ty0 + TS) - 1;
-    uint32_t ordered_left = 0;  // ordered views: entries of the tile left for the ordered stage
 
     for (uint32_t base = beg; base < end;) {
         const int nb = (int)min((uint32_t)NT, end - base);
@@ -1191,7 +1228,6 @@ __device__ __forceinline__ void raster_tile(const PassArgs& a, const ViewArgs& v
         const uint32_t P = Ps + s_total[2];
         const int NSP = (int)(Ns + s_total[3]);
         if (fits) {
-            ordered_left += in_stage ? 0u : 1u;
             const uint32_t first = (large ? incl_l : incl_s) - cnt;
             uint32_t sp = (first >> 17) + (large ? Ns : 0u), p = (first & 0x1ffffu) + (large ? Ps : 0u);
             const uint32_t span_end = sp + (uint32_t)rs.nspan;
@@ -1284,10 +1320,33 @@ __device__ __forceinline__ void raster_tile(const PassArgs& a, const ViewArgs& v
     }
     __syncthreads();
     if (v.ordered) {
-        // tiles without ordered entries are finished by the shade stage; the scatter cursors are
-        // free after binning and carry the per-tile count to the later stages
-        ordered_left = __reduce_add_sync(0xffffffffu, ordered_left);
-        if (lane == 0) warp_sum[wid] = ordered_left;
+        // tiles without ordered entries that may pass the depth test are finished by the shade
+        // stage; the scatter cursors are free after binning and carry the per-tile count to the
+        // later stages
+        float dmax = 0.0f;  // farthest prefix depth of the tile's samples (culling views)
+        if (v.ordered_cull) {
+            uint32_t hmax = 0u;  // depth-order words of the prefix keys (ascending in depth)
+            if (inpix) {
+#pragma unroll
+                for (int k = 0; k < S; k++) hmax = max(hmax, (uint32_t)(skey[k * (TS * TS) + ly * TS + lx] >> 32));
+            }
+            hmax = __reduce_max_sync(0xffffffffu, hmax);
+            if (lane == 0) warp_sum[wid] = hmax;
+            __syncthreads();
+#pragma unroll
+            for (int w = 0; w < NW; w++) hmax = max(hmax, warp_sum[w]);
+            dmax = order_depth(hmax);
+            __syncthreads();
+        }
+        const uint32_t first_ordered = (uint32_t)(v.first_tri + v.ordered_prefix);
+        uint32_t left = 0;
+        for (uint32_t i = beg + tid; i < end; i += NT) {
+            const uint32_t e = __ldg(a.pairs + i);
+            if ((e >> 3) < first_ordered) continue;
+            left += !v.ordered_cull || may_pass_tile(a, v.c, e, tx0, ty0, xmax, ymax, dmax);
+        }
+        left = __reduce_add_sync(0xffffffffu, left);
+        if (lane == 0) warp_sum[wid] = left;
         __syncthreads();
         if (tid == 0) {
             uint32_t sum = 0;
@@ -1690,9 +1749,6 @@ struct FwdRecords {
     int32_t draw[kFwdThreads];
 };
 
-static_assert(sizeof(FwdRecords) >= kFwdThreads * (sizeof(float4) + sizeof(int2)),
-              "the ordered stage reuses the record arrays as per-warp shading scratch");
-
 constexpr int kFwdFrags = 8;  // fragments a pixel holds before they are shaded
 
 // Shades fragment f = (entry, sample mask) at pixel (px, py) and writes or blends it into the
@@ -1726,150 +1782,6 @@ __device__ __noinline__ void apply_fragments(const PassArgs& a, const ViewArgs& 
     for (int i = 0; i < n; i++) apply_fragment<S>(a, v, px, py, scol, frags[i * kFwdThreads + threadIdx.x]);
 }
 
-// The recorded fragments of a warp's 32 pixels, shaded warp-cooperatively and applied in order.
-// Items (pixel, fragment) are numbered pixel-major in fragment order and taken 32 per round, one
-// per lane, whatever pixel it belongs to (the quad derivatives are evaluated analytically at the
-// owner's pixel); each round's anisotropic probes are spread over all lanes and summed per item in
-// probe order (as the shade stage does), then every lane applies the round's items of its own pixel
-// in item order, so each pixel still sees its fragments in submission order.  `wres` (32 float4)
-// and `wmeta` (32 int2) are the warp's shared scratch.
-template <int S>
-__device__ __forceinline__ void shade_fragments_warp(const PassArgs& a, const ViewArgs& v, int tx0, int ty0,
-                                                     float4* scol, const int2* frags, int nfrag, float4* wres,
-                                                     int2* wmeta) {
-    constexpr int NT = kFwdThreads;
-    const int lane = threadIdx.x & 31, wbase = threadIdx.x & ~31;
-    int incl = nfrag;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-        const int q = __shfl_up_sync(0xffffffffu, incl, o);
-        if (lane >= o) incl += q;
-    }
-    const int pre_f = incl - nfrag;
-    const int total = __shfl_sync(0xffffffffu, incl, 31);
-    for (int r0 = 0; r0 < total; r0 += 32) {
-        const int b = r0 + lane;
-        int owner = 0;  // the last lane whose first item is at or before b
-#pragma unroll
-        for (int step = 16; step > 0; step >>= 1)
-            if (__shfl_sync(0xffffffffu, pre_f, owner + step) <= b) owner += step;
-        const int fi = b - __shfl_sync(0xffffffffu, pre_f, owner);
-        int di = 0, n = 0, mask = 0;
-        float c[4] = {0.0f, 0.0f, 0.0f, 0.0f};
-        TexProbe tp;
-        tp.u = tp.v = tp.du = tp.dv = tp.t = 0.0f;
-        tp.lo = tp.hi = tp.n = 0;
-        tp.two = tp.aniso = false;
-        if (b < total) {
-            const int2 f = frags[fi * NT + wbase + owner];
-            mask = f.y;
-            int olx, oly;
-            tile_pixel<16>(wbase + owner, olx, oly);
-            const int opx = tx0 + olx, opy = ty0 + oly;
-            const int g = f.x >> 3, sub = f.x & 7;
-            const TriRecord* rp = a.records + g;
-            const int4 q1 = __ldg(reinterpret_cast<const int4*>(rp) + 1);  // X2, Y2, flags, draw
-            di = q1.w;
-            const DrawDev& d = a.draws[di];
-            const int t = g - __ldg(a.draw_start + di);
-            const bool from_record = sub == 0 && (q1.z & REC_VALID) && d.polygon_mode == POLY_FILL;
-            ShadeGeom geo;
-            float4 plane;
-            int plane_y;
-            if (from_record) {
-                shade_geom_record(rp, q1, geo, plane, plane_y);
-            } else {
-                ShadeGeom tg;
-                float4 tpl;
-                int tpy;
-                shade_geom_general(v.c, d, a.records, g, t, sub, &tg, &tpl, &tpy);
-                geo = tg;
-            }
-            float a0[4], a1[4], a2[4];
-            if (sub == 0 && (q1.z & REC_VALID) && a.attrs && d.shading != SHADE_PRIMID && d.attr_count > 0) {
-                const float4 p0 = __ldg(&a.attrs[g].a[0]), p1 = __ldg(&a.attrs[g].a[1]), p2 = __ldg(&a.attrs[g].a[2]);
-                a0[0] = p0.x; a0[1] = p0.y; a0[2] = p0.z; a0[3] = p0.w;
-                a1[0] = p1.x; a1[1] = p1.y; a1[2] = p1.z; a1[3] = p1.w;
-                a2[0] = p2.x; a2[1] = p2.y; a2[2] = p2.z; a2[3] = p2.w;
-            } else if (d.shading != SHADE_PRIMID) {
-                fetch_attrs(d, t, a0, a1, a2);
-            } else {
-#pragma unroll
-                for (int k = 0; k < 4; k++) a0[k] = a1[k] = a2[k] = 0.0f;
-            }
-            if (shade_prepare_attrs(v.c, d, geo, t, sub, opx, opy, a0, a1, a2, c, tp)) n = tp.n;
-        }
-        int pincl = n;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            const int q = __shfl_up_sync(0xffffffffu, pincl, o);
-            if (lane >= o) pincl += q;
-        }
-        const int T = __shfl_sync(0xffffffffu, pincl, 31);
-        if (T > 0) {
-            const int pre = pincl - n;
-            const int packed = tp.lo | (tp.hi << 8) | (tp.n << 16) | (tp.two ? 1 << 24 : 0) | (tp.aniso ? 1 << 25 : 0);
-            float acc[4] = {0.0f, 0.0f, 0.0f, 0.0f};
-            for (int c0 = 0; c0 < T; c0 += 32) {
-                const int j = c0 + lane;
-                int k = 0;  // the item of probe j: the last lane whose first probe is at or before j
-#pragma unroll
-                for (int step = 16; step > 0; step >>= 1)
-                    if (__shfl_sync(0xffffffffu, pre, k + step) <= j) k += step;
-                TexProbe q;
-                q.u = __shfl_sync(0xffffffffu, tp.u, k);
-                q.v = __shfl_sync(0xffffffffu, tp.v, k);
-                q.du = __shfl_sync(0xffffffffu, tp.du, k);
-                q.dv = __shfl_sync(0xffffffffu, tp.dv, k);
-                q.t = __shfl_sync(0xffffffffu, tp.t, k);
-                const int qp = __shfl_sync(0xffffffffu, packed, k);
-                const int qd = __shfl_sync(0xffffffffu, di, k);
-                const int i = j - __shfl_sync(0xffffffffu, pre, k);
-                q.lo = qp & 255;
-                q.hi = (qp >> 8) & 255;
-                q.n = (qp >> 16) & 255;
-                q.two = (qp >> 24) & 1;
-                q.aniso = (qp >> 25) & 1;
-                float r[4] = {0.0f, 0.0f, 0.0f, 0.0f};
-                if (j < T) tex_probe(a.draws[qd], q, i, r);
-                wres[lane] = make_float4(r[0], r[1], r[2], r[3]);
-                __syncwarp();
-                const int qa = max(pre, c0), qb = min(pre + n, c0 + 32);
-                for (int m = qa; m < qb; m++) {
-                    const float4 x = wres[m - c0];
-                    acc[0] = acc[0] + x.x; acc[1] = acc[1] + x.y; acc[2] = acc[2] + x.z; acc[3] = acc[3] + x.w;
-                }
-                __syncwarp();
-            }
-            if (n > 0) tex_finish(tp, acc, c);
-        }
-        wres[lane] = make_float4(c[0], c[1], c[2], c[3]);
-        wmeta[lane] = make_int2(b < total ? owner | (mask << 5) : -1, di);
-        __syncwarp();
-        const int nr = min(32, total - r0);
-        for (int m = 0; m < nr; m++) {
-            const int2 md = wmeta[m];
-            if ((md.x & 31) != lane) continue;
-            const float4 x = wres[m];
-            const float col[4] = {x.x, x.y, x.z, x.w};
-            const DrawDev& d = a.draws[md.y];
-            const unsigned fm = (unsigned)md.x >> 5;
-#pragma unroll
-            for (int k = 0; k < S; k++) {
-                if (!(fm & (1u << k))) continue;
-                float4& sc = scol[k * NT + threadIdx.x];
-                if (d.blend_enable) {
-                    float dst[4] = {sc.x, sc.y, sc.z, sc.w};
-                    blend_into(d, col, dst);
-                    sc = make_float4(dst[0], dst[1], dst[2], dst[3]);
-                } else {
-                    sc = make_float4(col[0], col[1], col[2], col[3]);
-                }
-            }
-        }
-        __syncwarp();
-    }
-}
 
 template <int S>
 __device__ __forceinline__ void forward_tile(const PassArgs& a, const ViewArgs& v, int gtile, FwdRecords& rec,
@@ -2036,13 +1948,13 @@ __device__ __forceinline__ void forward_tile(const PassArgs& a, const ViewArgs& 
         }
         __syncthreads();
     }
-    // shade the recorded fragments warp-cooperatively and apply each one in submission order to
-    // its samples; the record arrays are free again (every thread passed the batch loop's barrier)
-    {
-        float4* wres = reinterpret_cast<float4*>(&rec) + (tid >> 5) * 32;
-        int2* wmeta = reinterpret_cast<int2*>(reinterpret_cast<float4*>(&rec) + NT) + (tid >> 5) * 32;
-        shade_fragments_warp<S>(a, v, tx * TS, ty * TS, scol, frags, nfrag, wres, wmeta);
-    }
+    // shade the recorded fragments with the warp converged on fragment slot i of every lane, and
+    // apply each one in submission order to its samples (spreading the fragments' anisotropic probes
+    // over the warp's lanes, as the shade stage does, measured slower here: 5.15 vs 4.09 ms on the
+    // stress frame, more instruction-cache stalls at no fewer instructions)
+    const int maxn = __reduce_max_sync(0xffffffffu, nfrag);
+    for (int i = 0; i < maxn; i++)
+        if (i < nfrag) apply_fragment<S>(a, v, px, py, scol, frags[i * NT + tid]);
     if (!inpix) return;
     float acc[4];
 #pragma unroll

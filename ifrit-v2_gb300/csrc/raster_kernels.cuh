@@ -48,6 +48,9 @@ struct ViewArgs {
     int ordered_prefix;      // ordered views: triangles of the leading draws that need no ordering
                              //    (opaque, the first draw's depth state); they go through the
                              //    order-independent raster stage and the rest is applied on top
+    int ordered_cull;        // ordered views: 1 when the prefix writes depth under LESS / LEQUAL and
+                             //    no later draw can raise a depth, so that an ordered entry lying
+                             //    behind a tile's farthest prefix depth cannot pass anywhere there
     unsigned long long* keys;  // atomic visibility path: per-sample 64-bit keys [H][W][S], else nullptr
     float4* sample_colors;   // ordered views: per-sample colour of the order-independent prefix,
                              //    handed from the shade stage to the ordered stage, tile-major
