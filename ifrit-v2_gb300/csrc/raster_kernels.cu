@@ -263,127 +263,108 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
     return false;
 }
 
-// Stages [src, src + bytes) (4-byte aligned) so that its byte i lands at the returned address + i
-// inside `buf` (16-byte aligned, at least bytes + 16 long): the 16-byte-aligned inner part by one
-// bulk copy from thread 0 on the barrier's next phase, the unaligned head and tail (under 16
-// bytes each) by plain loads.  All threads call it with the same arguments; `phases` counts the
-// barrier phases used so far.  ok (the same in every thread) is false if the wait gave up, which
-// is also recorded in the pass status.
-__device__ __forceinline__ const unsigned char* stage_bytes(const PassArgs& a, const void* src, uint32_t bytes,
-                                                            unsigned char* buf, uint64_t* bar, uint32_t& phases,
-                                                            bool& ok) {
-    const uintptr_t s0 = (uintptr_t)src, s1 = s0 + bytes;
-    const uintptr_t i0 = (s0 + 15) & ~(uintptr_t)15, i1 = s1 & ~(uintptr_t)15;
-    unsigned char* out = buf + (s0 & 15);
-    const bool bulk = i1 > i0;
-    if (bulk && threadIdx.x == 0) bulk_load(out + (i0 - s0), reinterpret_cast<const void*>(i0), (uint32_t)(i1 - i0), bar);
-    // head and tail words (the whole range when it holds no aligned 16 bytes)
-    const uint32_t* w = static_cast<const uint32_t*>(src);
-    uint32_t* o = reinterpret_cast<uint32_t*>(out);
-    const int nw = (int)(bytes / 4);
-    const int head = bulk ? (int)((i0 - s0) / 4) : nw, tail = bulk ? (int)((i1 - s0) / 4) : nw;
-    for (int k = threadIdx.x; k < head; k += blockDim.x) o[k] = __ldg(w + k);
-    for (int k = tail + threadIdx.x; k < nw; k += blockDim.x) o[k] = __ldg(w + k);
-    bool mine = true;
-    if (bulk) {
-        mine = mbar_wait(bar, phases & 1u);
-        phases++;
-    }
-    ok = __syncthreads_and(mine) != 0;
-    if (!ok && threadIdx.x == 0) atomicOr(a.status + ST_STICKY, 4u);
-    return out;
-}
+constexpr int kStageTris = 256;                       // triangles per counting-binner block
+constexpr int kStageIdxBytes = kStageTris * 12 + 16;  // one block's index slice (+ alignment slack)
 
-constexpr int kStageTris = 256;                        // counting-binner CTA size
-constexpr int kStageIdxBytes = kStageTris * 12 + 16;   // the CTA's index slice
-constexpr int kStageVtxBytes = 20 * 1024 + 16;         // vertex window (unshared or local vertices)
+// One block's index slice in flight or staged: the 16-byte-aligned inner part of the slice is
+// copied by one bulk copy; the words outside it (under 16 bytes at each end) are read from global
+// memory by the consumer.
+struct IdxStage {
+    int draw;         // the block's draw, or -1 when its triangles span draws (nothing staged)
+    int t_first, n;   // the block's first triangle within the draw, triangle count
+    int w0, w1;       // staged words [w0, w1) of the slice
+    int off;          // byte offset of the slice's word 0 in the stage buffer
+};
 
-// Stages the CTA's index slice, and the vertex rows its triangles reference when they fit, in
-// shared memory; only when all of the CTA's triangles belong to one draw.  `phases`: barrier
-// phases used; all_ok false if a wait gave up (the kernel waits once more before it exits).
-__device__ __forceinline__ void stage_block(const PassArgs& a, StagedInput& st, unsigned char* sidx, unsigned char* svtx,
-                                            uint64_t* bar, int* sh, uint32_t& phases, bool& all_ok) {
-    st.idx = nullptr;
-    st.verts = nullptr;
-    all_ok = true;
-    phases = 0;
-    const int g0 = blockIdx.x * kStageTris;
+// Issues the bulk copy of block `blk`'s index slice into `buf` on `bar` (thread 0 only).
+__device__ __forceinline__ void issue_index_stage(const PassArgs& a, int blk, unsigned char* buf, uint64_t* bar,
+                                                  IdxStage& st) {
+    const int g0 = blk * kStageTris;
     const int n = min(kStageTris, a.total_tris - g0);
-    if (threadIdx.x == 0) {
-        const int d0 = find_draw(a, g0), d1 = find_draw(a, g0 + n - 1);
-        sh[0] = d0 == d1 ? d0 : -1;
-        sh[1] = 0x7fffffff;  // window: smallest and largest vertex index
-        sh[2] = -1;
-        mbar_init(bar, 1);
-    }
-    __syncthreads();
-    const int di = sh[0];
-    if (di < 0) return;
-    const DrawDev& d = a.draws[di];
-    const int t0 = g0 - __ldg(a.draw_start + di);
-    bool ok;
-    const unsigned char* ip = stage_bytes(a, d.indices + 3 * (size_t)t0, 12u * (uint32_t)n, sidx, bar, phases, ok);
-    if (!ok) {
-        all_ok = false;
-        return;
-    }
-    st.idx = reinterpret_cast<const int*>(ip);
-    st.t_first = t0;
-    st.t_end = t0 + n;
-    // the vertex window of the CTA's triangles
-    int lo = 0x7fffffff, hi = -1;
-    for (int k = threadIdx.x; k < 3 * n; k += blockDim.x) {
-        const int vid = st.idx[k];
-        if (vid >= 0 && vid < d.num_vertices) {
-            lo = min(lo, vid);
-            hi = max(hi, vid);
-        }
-    }
-    lo = __reduce_min_sync(0xffffffffu, lo);
-    hi = __reduce_max_sync(0xffffffffu, hi);
-    if ((threadIdx.x & 31) == 0) {
-        atomicMin(sh + 1, lo);
-        atomicMax(sh + 2, hi);
-    }
-    __syncthreads();
-    lo = sh[1];
-    hi = sh[2];
-    if (hi < lo) return;
-    const size_t vbytes = (size_t)(hi - lo + 1) * d.stride * 4;
-    if (vbytes + 16 > (size_t)kStageVtxBytes) return;
-    const unsigned char* vp = stage_bytes(a, d.vertices + (size_t)lo * d.stride, (uint32_t)vbytes, svtx, bar, phases, ok);
-    if (!ok) {
-        all_ok = false;
-        return;
-    }
-    st.verts = reinterpret_cast<const float*>(vp);
-    st.v_first = lo;
-    st.v_end = hi + 1;
+    const int d0 = find_draw(a, g0), d1 = find_draw(a, g0 + n - 1);
+    st.draw = -1;
+    st.w0 = st.w1 = 0;
+    if (d0 != d1) return;
+    const DrawDev& d = a.draws[d0];
+    st.draw = d0;
+    st.t_first = g0 - __ldg(a.draw_start + d0);
+    st.n = n;
+    const uintptr_t s0 = (uintptr_t)(d.indices + 3 * (size_t)st.t_first), s1 = s0 + 12u * (uint32_t)n;
+    const uintptr_t i0 = (s0 + 15) & ~(uintptr_t)15, i1 = s1 & ~(uintptr_t)15;
+    st.off = (int)(s0 & 15);
+    if (i1 <= i0) return;
+    st.w0 = (int)((i0 - s0) / 4);
+    st.w1 = (int)((i1 - s0) / 4);
+    bulk_load(buf + st.off + (i0 - s0), reinterpret_cast<const void*>(i0), (uint32_t)(i1 - i0), bar);
 }
 
 // Counting pass: full front end per triangle; unclipped triangles leave a compact record.
-// The CTA's index slice and, when it fits, its vertex window come into shared memory by bulk
-// copies (TMA) first.
-__global__ void __launch_bounds__(kStageTris) bin_count_kernel(PassArgs a) {
-    __shared__ __align__(16) unsigned char s_idx[kStageIdxBytes];
-    __shared__ __align__(16) unsigned char s_vtx[kStageVtxBytes];
-    __shared__ __align__(8) uint64_t s_bar;
-    __shared__ int s_info[3];
-    const int g = blockIdx.x * blockDim.x + threadIdx.x;
-    StagedInput st;
-    bool staged_ok;
-    uint32_t phases;
-    stage_block(a, st, s_idx, s_vtx, &s_bar, s_info, phases, staged_ok);
-    const int di = find_draw_warp(a, min(g, a.total_tris - 1));
-    WarpTiles w;
-    w.big = w.small = false;
-    if (g < a.total_tris) front_end(a, g, di, CountEmit{a, w}, &st);
-    if (w.small)  // counts need no result back: one fire-and-forget reduction per tile
-        for (int ty = w.ty0; ty <= w.ty1; ty++)
-            for (int tx = w.tx0; tx <= w.tx1; tx++) atomicAdd(a.tile_count + w.tbase + ty * w.tiles_x + tx, 1u);
-    warp_tiles(a, w, g, false);
-    if (!staged_ok && phases > 0)  // a wait gave up: let the copy land before the CTA's shared memory goes
-        mbar_wait(&s_bar, (phases - 1) & 1u);
+// Resident CTAs of the persistent counting binner on the current device (cached per device).
+int bin_count_ctas();
+// Persistent CTAs walk the blocks of 256 triangles in a grid-stride loop; the index slice of the
+// CTA's next block is copied into shared memory by a bulk copy (TMA) while the current block is
+// processed (two stage buffers, one mbarrier each, every wait bounded: a wait that gives up records
+// status bit ST_STICKY & 4, the CTA stops staging and reads global memory, and it waits once more
+// for its copies before it exits).
+__global__ void __launch_bounds__(kStageTris, 5) bin_count_kernel(PassArgs a) {
+    __shared__ __align__(16) unsigned char s_idx[2][kStageIdxBytes];
+    __shared__ __align__(8) uint64_t s_bar[2];
+    __shared__ IdxStage s_st[2];
+    __shared__ int s_fail, s_pend[2];  // a wait gave up; parity + 1 of a copy left pending per buffer
+    const int nblocks = (a.total_tris + kStageTris - 1) / kStageTris;
+    uint32_t uses[2] = {0u, 0u};  // completed phases per buffer (the same in every thread)
+    bool staging = true;
+    if (threadIdx.x == 0) {
+        mbar_init(&s_bar[0], 1);
+        mbar_init(&s_bar[1], 1);
+        s_fail = 0;
+        s_pend[0] = s_pend[1] = 0;
+        if ((int)blockIdx.x < nblocks) issue_index_stage(a, blockIdx.x, s_idx[0], &s_bar[0], s_st[0]);
+    }
+    __syncthreads();
+    int it = 0;
+    for (int blk = blockIdx.x; blk < nblocks; blk += gridDim.x, it++) {
+        const int b = it & 1;
+        const int next = blk + gridDim.x;
+        if (threadIdx.x == 0 && staging && next < nblocks) issue_index_stage(a, next, s_idx[b ^ 1], &s_bar[b ^ 1], s_st[b ^ 1]);
+        const IdxStage st = s_st[b];
+        StagedInput in;
+        in.idx = nullptr;
+        in.verts = nullptr;
+        if (staging && st.w1 > st.w0) {
+            const bool ok = mbar_wait(&s_bar[b], uses[b] & 1u);
+            uses[b]++;
+            if (__syncthreads_and(ok)) {
+                in.idx = reinterpret_cast<const int*>(s_idx[b] + st.off);
+                in.t_first = st.t_first;
+                in.t_end = st.t_first + st.n;
+                in.w0 = st.w0;
+                in.w1 = st.w1;
+            } else {
+                staging = false;
+                if (threadIdx.x == 0) {
+                    s_fail = 1;
+                    atomicOr(a.status + ST_STICKY, 4u);
+                    s_pend[b] = 1 + (int)((uses[b] - 1u) & 1u);  // the phase that did not complete
+                    if (next < nblocks && s_st[b ^ 1].w1 > s_st[b ^ 1].w0) s_pend[b ^ 1] = 1 + (int)(uses[b ^ 1] & 1u);
+                }
+            }
+        }
+        const int g = blk * kStageTris + threadIdx.x;
+        const int di = find_draw_warp(a, min(g, a.total_tris - 1));
+        WarpTiles w;
+        w.big = w.small = false;
+        if (g < a.total_tris) front_end(a, g, di, CountEmit{a, w}, &in);
+        if (w.small)  // counts need no result back: one fire-and-forget reduction per tile
+            for (int ty = w.ty0; ty <= w.ty1; ty++)
+                for (int tx = w.tx0; tx <= w.tx1; tx++) atomicAdd(a.tile_count + w.tbase + ty * w.tiles_x + tx, 1u);
+        warp_tiles(a, w, g, false);
+        __syncthreads();  // buffer b is free for the copy issued two blocks on
+        if (s_fail) staging = false;
+    }
+    if (s_fail && threadIdx.x == 0)  // let copies in flight land before the CTA's shared memory goes
+        for (int q = 0; q < 2; q++)
+            if (s_pend[q]) mbar_wait(&s_bar[q], (uint32_t)(s_pend[q] - 1));
 }
 
 // Scattering pass: same overlaps as the counting pass, read back from the records (clipped
@@ -2444,6 +2425,19 @@ void launch_atomic_front(const PassArgs& a, int npix, cudaStream_t stream, cudaE
     }
 }
 
+int bin_count_ctas() {
+    static int cached[64] = {};
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 1 << 20;
+    if (!cached[dev]) {
+        int sms = 0, occ = 0;
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, bin_count_kernel, kStageTris, 0);
+        cached[dev] = std::max(1, sms * std::max(1, occ));
+    }
+    return cached[dev];
+}
+
 cudaError_t launch_pass(const PassArgs& a, const LaunchPlan& plan, cudaStream_t stream, cudaEvent_t* ev) {
     const int T = a.total_tiles;
     if (ev) cudaEventRecord(ev[0], stream);
@@ -2466,7 +2460,7 @@ cudaError_t launch_pass(const PassArgs& a, const LaunchPlan& plan, cudaStream_t 
     }
     if (a.total_tris > 0) {
         int blocks = (a.total_tris + 255) / 256;
-        bin_count_kernel<<<blocks, 256, 0, stream>>>(a);
+        bin_count_kernel<<<std::min(blocks, bin_count_ctas()), kStageTris, 0, stream>>>(a);
         if (ev) cudaEventRecord(ev[1], stream);
         if (T <= kScanSingle) {
             scan_single_kernel<<<1, kScanThreads, 0, stream>>>(a, T);

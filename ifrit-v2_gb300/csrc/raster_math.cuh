@@ -143,18 +143,22 @@ __device__ __forceinline__ void xform_shared(const float* m, const float* v, flo
     for (int r = 0; r < 4; r++) out[r] = m[4 * r + 0] * x + m[4 * r + 1] * y + m[4 * r + 2] * z + m[4 * r + 3];
 }
 
-// Shared-memory copies of a counting-binner CTA's index slice and vertex window, staged by bulk
-// copies (TMA); a null member, or a triangle / vertex outside the staged range, falls back to
-// global loads.
+// Shared-memory copies of a counting-binner block's index slice (and optionally vertex rows),
+// staged by bulk copies (TMA); a null member, or an index word / vertex outside the staged range,
+// falls back to global loads.
 struct StagedInput {
-    const int* idx;      // indices of triangles [t_first, t_end) of the CTA's draw
+    const int* idx;      // word k of the slice of triangles [t_first, t_end) of the block's draw
     int t_first, t_end;
+    int w0, w1;          // words staged: [w0, w1)
     const float* verts;  // vertex rows [v_first, v_end) of the draw, `stride` floats each
     int v_first, v_end;
 };
 
 __device__ __forceinline__ int staged_index(const DrawDev& d, const StagedInput* st, int t, int i) {
-    if (st && st->idx && t >= st->t_first && t < st->t_end) return st->idx[3 * (t - st->t_first) + i];
+    if (st && st->idx && t >= st->t_first && t < st->t_end) {
+        const int k = 3 * (t - st->t_first) + i;
+        if (k >= st->w0 && k < st->w1) return st->idx[k];
+    }
     return __ldg(d.indices + 3 * (size_t)t + i);
 }
 
