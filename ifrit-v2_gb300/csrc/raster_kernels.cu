@@ -73,15 +73,14 @@ __device__ __forceinline__ void bin_sub(const PassArgs& a, const ViewArgs& v, co
 // path: fetch, transform, clip and set-up; writes the triangle's record (and vertex attributes)
 // and hands every visible (sub-)triangle to emit(view, draw, sub-triangle, entry).
 template <class Emit>
-__device__ __forceinline__ void front_end(const PassArgs& a, int g, int di, const Emit& emit,
-                                          const StagedInput* st = nullptr) {
+__device__ __forceinline__ void front_end(const PassArgs& a, int g, int di, const Emit& emit) {
     const DrawDev& d = a.draws[di];
     const ViewArgs& v = a.views[d.view];
     int t = g - __ldg(a.draw_start + di);
     CVert poly[3];  // registers: only the rare clipping path below goes through memory
     bool inside, rejected;
     TriRecord* rec = a.records + g;
-    if (!fetch_triangle(v.c, d, t, poly, inside, rejected, st)) {
+    if (!fetch_triangle(v.c, d, t, poly, inside, rejected)) {
         rec->flags = 0;
         return;
     }
@@ -96,7 +95,7 @@ __device__ __forceinline__ void front_end(const PassArgs& a, int g, int di, cons
         r.draw = di;
         if (a.attrs && d.shading != SHADE_PRIMID && d.attr_count > 0) {
             float a0[4], a1[4], a2[4];
-            fetch_attrs_staged(d, st, t, a0, a1, a2);
+            fetch_attrs(d, t, a0, a1, a2);
             float4* dst = a.attrs[g].a;
             dst[0] = make_float4(a0[0], a0[1], a0[2], a0[3]);
             dst[1] = make_float4(a1[0], a1[1], a1[2], a1[3]);
@@ -122,7 +121,7 @@ __device__ __forceinline__ void front_end(const PassArgs& a, int g, int di, cons
         r.draw = di;
         if (a.attrs && d.shading != SHADE_PRIMID && d.attr_count > 0) {
             float a0[4], a1[4], a2[4];
-            fetch_attrs_staged(d, st, t, a0, a1, a2);
+            fetch_attrs(d, t, a0, a1, a2);
             float4* dst = a.attrs[g].a;
             dst[0] = make_float4(a0[0], a0[1], a0[2], a0[3]);
             dst[1] = make_float4(a1[0], a1[1], a1[2], a1[3]);
@@ -248,6 +247,14 @@ __device__ __forceinline__ void bulk_load(void* dst, const void* src, uint32_t b
                  : "memory");
 }
 
+// A CTA's bulk-copy barrier: phases used so far (the same in every thread), whether bulk copies
+// are still in use, and whether one was left in flight after a wait gave up.
+struct BulkState {
+    uint64_t* bar;
+    uint32_t phase;
+    bool ok, pending;
+};
+
 // Waits for the barrier phase of the given parity, giving up after kBulkWaitLimit polls.
 constexpr int kBulkWaitLimit = 1 << 20;
 __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
@@ -263,108 +270,19 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
     return false;
 }
 
-constexpr int kStageTris = 256;                       // triangles per counting-binner block
-constexpr int kStageIdxBytes = kStageTris * 12 + 16;  // one block's index slice (+ alignment slack)
-
-// One block's index slice in flight or staged: the 16-byte-aligned inner part of the slice is
-// copied by one bulk copy; the words outside it (under 16 bytes at each end) are read from global
-// memory by the consumer.
-struct IdxStage {
-    int draw;         // the block's draw, or -1 when its triangles span draws (nothing staged)
-    int t_first, n;   // the block's first triangle within the draw, triangle count
-    int w0, w1;       // staged words [w0, w1) of the slice
-    int off;          // byte offset of the slice's word 0 in the stage buffer
-};
-
-// Issues the bulk copy of block `blk`'s index slice into `buf` on `bar` (thread 0 only).
-__device__ __forceinline__ void issue_index_stage(const PassArgs& a, int blk, unsigned char* buf, uint64_t* bar,
-                                                  IdxStage& st) {
-    const int g0 = blk * kStageTris;
-    const int n = min(kStageTris, a.total_tris - g0);
-    const int d0 = find_draw(a, g0), d1 = find_draw(a, g0 + n - 1);
-    st.draw = -1;
-    st.w0 = st.w1 = 0;
-    if (d0 != d1) return;
-    const DrawDev& d = a.draws[d0];
-    st.draw = d0;
-    st.t_first = g0 - __ldg(a.draw_start + d0);
-    st.n = n;
-    const uintptr_t s0 = (uintptr_t)(d.indices + 3 * (size_t)st.t_first), s1 = s0 + 12u * (uint32_t)n;
-    const uintptr_t i0 = (s0 + 15) & ~(uintptr_t)15, i1 = s1 & ~(uintptr_t)15;
-    st.off = (int)(s0 & 15);
-    if (i1 <= i0) return;
-    st.w0 = (int)((i0 - s0) / 4);
-    st.w1 = (int)((i1 - s0) / 4);
-    bulk_load(buf + st.off + (i0 - s0), reinterpret_cast<const void*>(i0), (uint32_t)(i1 - i0), bar);
-}
-
-// Counting pass: full front end per triangle; unclipped triangles leave a compact record.
-// Resident CTAs of the persistent counting binner on the current device (cached per device).
-int bin_count_ctas();
-// Persistent CTAs walk the blocks of 256 triangles in a grid-stride loop; the index slice of the
-// CTA's next block is copied into shared memory by a bulk copy (TMA) while the current block is
-// processed (two stage buffers, one mbarrier each, every wait bounded: a wait that gives up records
-// status bit ST_STICKY & 4, the CTA stops staging and reads global memory, and it waits once more
-// for its copies before it exits).
-__global__ void __launch_bounds__(kStageTris, 5) bin_count_kernel(PassArgs a) {
-    __shared__ __align__(16) unsigned char s_idx[2][kStageIdxBytes];
-    __shared__ __align__(8) uint64_t s_bar[2];
-    __shared__ IdxStage s_st[2];
-    __shared__ int s_fail, s_pend[2];  // a wait gave up; parity + 1 of a copy left pending per buffer
-    const int nblocks = (a.total_tris + kStageTris - 1) / kStageTris;
-    uint32_t uses[2] = {0u, 0u};  // completed phases per buffer (the same in every thread)
-    bool staging = true;
-    if (threadIdx.x == 0) {
-        mbar_init(&s_bar[0], 1);
-        mbar_init(&s_bar[1], 1);
-        s_fail = 0;
-        s_pend[0] = s_pend[1] = 0;
-        if ((int)blockIdx.x < nblocks) issue_index_stage(a, blockIdx.x, s_idx[0], &s_bar[0], s_st[0]);
-    }
-    __syncthreads();
-    int it = 0;
-    for (int blk = blockIdx.x; blk < nblocks; blk += gridDim.x, it++) {
-        const int b = it & 1;
-        const int next = blk + gridDim.x;
-        if (threadIdx.x == 0 && staging && next < nblocks) issue_index_stage(a, next, s_idx[b ^ 1], &s_bar[b ^ 1], s_st[b ^ 1]);
-        const IdxStage st = s_st[b];
-        StagedInput in;
-        in.idx = nullptr;
-        in.verts = nullptr;
-        if (staging && st.w1 > st.w0) {
-            const bool ok = mbar_wait(&s_bar[b], uses[b] & 1u);
-            uses[b]++;
-            if (__syncthreads_and(ok)) {
-                in.idx = reinterpret_cast<const int*>(s_idx[b] + st.off);
-                in.t_first = st.t_first;
-                in.t_end = st.t_first + st.n;
-                in.w0 = st.w0;
-                in.w1 = st.w1;
-            } else {
-                staging = false;
-                if (threadIdx.x == 0) {
-                    s_fail = 1;
-                    atomicOr(a.status + ST_STICKY, 4u);
-                    s_pend[b] = 1 + (int)((uses[b] - 1u) & 1u);  // the phase that did not complete
-                    if (next < nblocks && s_st[b ^ 1].w1 > s_st[b ^ 1].w0) s_pend[b ^ 1] = 1 + (int)(uses[b ^ 1] & 1u);
-                }
-            }
-        }
-        const int g = blk * kStageTris + threadIdx.x;
-        const int di = find_draw_warp(a, min(g, a.total_tris - 1));
-        WarpTiles w;
-        w.big = w.small = false;
-        if (g < a.total_tris) front_end(a, g, di, CountEmit{a, w}, &in);
-        if (w.small)  // counts need no result back: one fire-and-forget reduction per tile
-            for (int ty = w.ty0; ty <= w.ty1; ty++)
-                for (int tx = w.tx0; tx <= w.tx1; tx++) atomicAdd(a.tile_count + w.tbase + ty * w.tiles_x + tx, 1u);
-        warp_tiles(a, w, g, false);
-        __syncthreads();  // buffer b is free for the copy issued two blocks on
-        if (s_fail) staging = false;
-    }
-    if (s_fail && threadIdx.x == 0)  // let copies in flight land before the CTA's shared memory goes
-        for (int q = 0; q < 2; q++)
-            if (s_pend[q]) mbar_wait(&s_bar[q], (uint32_t)(s_pend[q] - 1));
+// Counting pass: full front end per triangle; unclipped triangles leave a compact record.  (Bulk
+// copies of each block's index slice into shared memory measured slower on this HBM-bound pass,
+// whether waited for at once or prefetched a block ahead by persistent CTAs.)
+__global__ void __launch_bounds__(256) bin_count_kernel(PassArgs a) {
+    const int g = blockIdx.x * blockDim.x + threadIdx.x;
+    const int di = find_draw_warp(a, min(g, a.total_tris - 1));
+    WarpTiles w;
+    w.big = w.small = false;
+    if (g < a.total_tris) front_end(a, g, di, CountEmit{a, w});
+    if (w.small)  // counts need no result back: one fire-and-forget reduction per tile
+        for (int ty = w.ty0; ty <= w.ty1; ty++)
+            for (int tx = w.tx0; tx <= w.tx1; tx++) atomicAdd(a.tile_count + w.tbase + ty * w.tiles_x + tx, 1u);
+    warp_tiles(a, w, g, false);
 }
 
 // Scattering pass: same overlaps as the counting pass, read back from the records (clipped
@@ -1766,12 +1684,18 @@ __device__ __noinline__ void apply_fragments(const PassArgs& a, const ViewArgs& 
 
 template <int S>
 __device__ __forceinline__ void forward_tile(const PassArgs& a, const ViewArgs& v, int gtile, FwdRecords& rec,
-                                             float4* scol, uint32_t* list, int2* frags, bool after_raster) {
+                                             float4* scol, uint32_t* list, int2* frags, bool after_raster,
+                                             BulkState& bs) {
     constexpr int TS = 16, NT = kFwdThreads;
     // after the raster and shade stages the shade stage has finished the tiles without ordered
     // entries (uniform over the CTA)
     if (after_raster && a.tile_cursor[gtile] == 0u) return;
     const int ltile = gtile - v.tile_start;
+    // the prefix's per-sample colours of the tile (S x 256 float4, contiguous in the tile-major
+    // hand-off) come in by one bulk copy (TMA) that overlaps the gathering and sorting below
+    const bool bulk = after_raster && bs.ok;
+    if (bulk && threadIdx.x == 0)
+        bulk_load(scol, v.sample_colors + (size_t)ltile * S * NT, (uint32_t)(sizeof(float4) * S * NT), bs.bar);
     const int tx = ltile % v.c.tiles_x, ty = ltile / v.c.tiles_x;
     const int tid = threadIdx.x;
     int lx, ly;
@@ -1795,12 +1719,11 @@ __device__ __forceinline__ void forward_tile(const PassArgs& a, const ViewArgs& 
         for (int k = 0; k < S; k++) {
             if (after_raster) {
                 // the prefix's per-sample state as the shade stage left it: colour in the
-                // per-sample scratch, depth and primitive id in the outputs
+                // per-sample scratch (bulk-copied above), depth and primitive id in the outputs
                 const int ent = inpix ? v.entries[pix * S + k] : -1;
                 dep[k] = inpix ? v.depth[pix * S + k] : 0.0f;
                 vid[k] = ent < 0 ? -1 : (ent >> 3) - v.first_tri;
-                scol[k * NT + tid] = inpix ? v.sample_colors[((size_t)ltile * S + k) * NT + tid]
-                                           : make_float4(bg[0], bg[1], bg[2], bg[3]);
+                if (!bulk) scol[k * NT + tid] = v.sample_colors[((size_t)ltile * S + k) * NT + tid];
             } else {
                 dep[k] = v.clear ? v.clear_depth : (inpix ? v.depth[pix * S + k] : 0.0f);
                 vid[k] = -1;
@@ -1866,6 +1789,18 @@ __device__ __forceinline__ void forward_tile(const PassArgs& a, const ViewArgs& 
         }
     }
 
+    if (bulk) {  // the colours must have landed before the first fragment is applied
+        const bool ok = mbar_wait(bs.bar, bs.phase & 1u);
+        bs.phase++;
+        if (!__syncthreads_and(ok)) {  // gave up: report, and load the colours from memory from now on
+            bs.ok = false;
+            if (threadIdx.x == 0) atomicOr(a.status + ST_STICKY, 4u);
+            bs.pending = true;
+#pragma unroll
+            for (int k = 0; k < S; k++) scol[k * NT + tid] = v.sample_colors[((size_t)ltile * S + k) * NT + tid];
+            __syncthreads();
+        }
+    }
     int nfrag = 0;  // fragments recorded for this thread's pixel, not yet shaded
     for (int base = 0; base < n; base += NT) {
         const int nb = min(NT, n - base);
@@ -1975,9 +1910,20 @@ __global__ void __launch_bounds__(kFwdThreads) forward_kernel(PassArgs a, GroupA
     int2* frags = reinterpret_cast<int2*>(list + kOrderedCap);  // [kFwdFrags][256]
     __shared__ ViewArgs sv;
     __shared__ int s_tile, s_view;
-    if (threadIdx.x == 0) s_view = -1;
+    __shared__ __align__(8) uint64_t s_bar;
+    BulkState bs;
+    bs.bar = &s_bar;
+    bs.phase = 0;
+    bs.ok = true;
+    bs.pending = false;
+    if (threadIdx.x == 0) {
+        s_view = -1;
+        mbar_init(&s_bar, 1);
+    }
+    __syncthreads();
     while (next_tile<kFwdThreads>(a, g, qslot, sv, s_tile, s_view))
-        forward_tile<S>(a, sv, s_tile, rec, scol, list, frags, after_raster != 0);
+        forward_tile<S>(a, sv, s_tile, rec, scol, list, frags, after_raster != 0, bs);
+    if (bs.pending && threadIdx.x == 0) mbar_wait(&s_bar, (bs.phase - 1) & 1u);  // a copy that did not land in time
 }
 
 // ---------------------------------------------------------------------------- reference line / point rules
@@ -2425,19 +2371,6 @@ void launch_atomic_front(const PassArgs& a, int npix, cudaStream_t stream, cudaE
     }
 }
 
-int bin_count_ctas() {
-    static int cached[64] = {};
-    int dev = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 1 << 20;
-    if (!cached[dev]) {
-        int sms = 0, occ = 0;
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, bin_count_kernel, kStageTris, 0);
-        cached[dev] = std::max(1, sms * std::max(1, occ));
-    }
-    return cached[dev];
-}
-
 cudaError_t launch_pass(const PassArgs& a, const LaunchPlan& plan, cudaStream_t stream, cudaEvent_t* ev) {
     const int T = a.total_tiles;
     if (ev) cudaEventRecord(ev[0], stream);
@@ -2460,7 +2393,7 @@ cudaError_t launch_pass(const PassArgs& a, const LaunchPlan& plan, cudaStream_t 
     }
     if (a.total_tris > 0) {
         int blocks = (a.total_tris + 255) / 256;
-        bin_count_kernel<<<std::min(blocks, bin_count_ctas()), kStageTris, 0, stream>>>(a);
+        bin_count_kernel<<<blocks, 256, 0, stream>>>(a);
         if (ev) cudaEventRecord(ev[1], stream);
         if (T <= kScanSingle) {
             scan_single_kernel<<<1, kScanThreads, 0, stream>>>(a, T);

@@ -136,37 +136,6 @@ __device__ __forceinline__ void xform(const float* m, const float* v, float out[
     for (int r = 0; r < 4; r++) out[r] = m[4 * r + 0] * x + m[4 * r + 1] * y + m[4 * r + 2] * z + m[4 * r + 3];
 }
 
-// The same transform of a vertex row staged in shared memory.
-__device__ __forceinline__ void xform_shared(const float* m, const float* v, float out[4]) {
-    float x = v[0], y = v[1], z = v[2];
-#pragma unroll
-    for (int r = 0; r < 4; r++) out[r] = m[4 * r + 0] * x + m[4 * r + 1] * y + m[4 * r + 2] * z + m[4 * r + 3];
-}
-
-// Shared-memory copies of a counting-binner block's index slice (and optionally vertex rows),
-// staged by bulk copies (TMA); a null member, or an index word / vertex outside the staged range,
-// falls back to global loads.
-struct StagedInput {
-    const int* idx;      // word k of the slice of triangles [t_first, t_end) of the block's draw
-    int t_first, t_end;
-    int w0, w1;          // words staged: [w0, w1)
-    const float* verts;  // vertex rows [v_first, v_end) of the draw, `stride` floats each
-    int v_first, v_end;
-};
-
-__device__ __forceinline__ int staged_index(const DrawDev& d, const StagedInput* st, int t, int i) {
-    if (st && st->idx && t >= st->t_first && t < st->t_end) {
-        const int k = 3 * (t - st->t_first) + i;
-        if (k >= st->w0 && k < st->w1) return st->idx[k];
-    }
-    return __ldg(d.indices + 3 * (size_t)t + i);
-}
-
-__device__ __forceinline__ const float* staged_row(const DrawDev& d, const StagedInput* st, int vid) {
-    if (st && st->verts && vid >= st->v_first && vid < st->v_end) return st->verts + (size_t)(vid - st->v_first) * d.stride;
-    return nullptr;
-}
-
 __device__ __forceinline__ float plane_dist(const PassConst& c, int plane, const float* p) {
     switch (plane) {
     case 0: return p[3] - kWEps;
@@ -306,20 +275,17 @@ __device__ __forceinline__ bool setup_sub(const PassConst& c, const DrawDev& d, 
 // Fetch + transform the three vertices of triangle t.  Returns false for invalid indices or
 // non-finite clip coordinates.  Sets `inside` when no clip plane cuts the triangle.
 __device__ __forceinline__ bool fetch_triangle(const PassConst& c, const DrawDev& d, int t, CVert* poly,
-                                               bool& inside, bool& rejected, const StagedInput* st = nullptr) {
+                                               bool& inside, bool& rejected) {
     inside = true;
     rejected = false;
 #pragma unroll
     for (int i = 0; i < 3; i++) {
-        int vid = staged_index(d, st, t, i);
+        int vid = __ldg(d.indices + 3 * (size_t)t + i);
         if (vid < 0 || vid >= d.num_vertices) return false;
         const float* vp = d.vertices + (size_t)vid * d.stride;
-        const float* sp = staged_row(d, st, vid);
         if (d.clip_input) {
 #pragma unroll
-            for (int k = 0; k < 4; k++) poly[i].p[k] = sp ? sp[k] : __ldg(vp + k);
-        } else if (sp) {
-            xform_shared(d.mvp, sp, poly[i].p);
+            for (int k = 0; k < 4; k++) poly[i].p[k] = __ldg(vp + k);
         } else {
             xform(d.mvp, vp, poly[i].p);
         }
@@ -899,23 +865,6 @@ __device__ __forceinline__ void fetch_attrs(const DrawDev& d, int t, float a0[4]
     load_attr(d.vertices + (size_t)__ldg(d.indices + 3 * (size_t)t + 0) * d.stride + d.attr_offset, d.attr_count, a0);
     load_attr(d.vertices + (size_t)__ldg(d.indices + 3 * (size_t)t + 1) * d.stride + d.attr_offset, d.attr_count, a1);
     load_attr(d.vertices + (size_t)__ldg(d.indices + 3 * (size_t)t + 2) * d.stride + d.attr_offset, d.attr_count, a2);
-}
-
-// As fetch_attrs, reading the indices and vertex rows a counting-binner CTA staged when present.
-__device__ __forceinline__ void fetch_attrs_staged(const DrawDev& d, const StagedInput* st, int t, float a0[4],
-                                                   float a1[4], float a2[4]) {
-    float* out[3] = {a0, a1, a2};
-#pragma unroll
-    for (int i = 0; i < 3; i++) {
-        const int vid = staged_index(d, st, t, i);
-        const float* sp = staged_row(d, st, vid);
-        if (sp) {
-#pragma unroll
-            for (int k = 0; k < 4; k++) out[i][k] = k < d.attr_count ? sp[d.attr_offset + k] : 0.0f;
-        } else {
-            load_attr(d.vertices + (size_t)vid * d.stride + d.attr_offset, d.attr_count, out[i]);
-        }
-    }
 }
 
 // Vertex attributes of an unclipped triangle stored by the counting binner next to its set-up
