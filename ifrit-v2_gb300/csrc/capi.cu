@@ -131,8 +131,11 @@ uint64_t g_id_counter = 1;
 // Device scratch and pinned descriptor staging of a pass.  Buffers grow on demand; each growth
 // bumps `generation`, which invalidates CUDA graphs captured with the old addresses.
 struct PassScratch {
-    DevMem tile_count, tile_offset, tile_cursor, block_sums, pairs, records, attrs, status, draws, draw_start, views,
-        view_tiles, queues, entries, sample_colors;
+    DevMem tile_count, tile_offset, tile_cursor, block_sums, pairs, records, attrs, status, desc, queues, entries,
+        sample_colors;
+    // the pass descriptors share one block (one upload per pass): draws | draw starts | views | view
+    // tile starts, each at a 256-byte offset sized for cap_draws / cap_views
+    size_t cap_draws = 0, cap_views = 0, off_draw_start = 0, off_views = 0, off_view_tiles = 0;
     size_t tiles_alloc = 0;
     uint32_t pair_capacity = 0;
     uint64_t generation = 1;
@@ -141,8 +144,8 @@ struct PassScratch {
     cudaEvent_t staged = nullptr;  // recorded after the last descriptor upload
     bool staged_pending = false;
     void release() {
-        for (DevMem* m : {&tile_count, &tile_offset, &tile_cursor, &block_sums, &pairs, &records, &attrs, &status, &draws,
-                          &draw_start, &views, &view_tiles, &queues, &entries, &sample_colors})
+        for (DevMem* m : {&tile_count, &tile_offset, &tile_cursor, &block_sums, &pairs, &records, &attrs, &status, &desc,
+                          &queues, &entries, &sample_colors})
             m->release();
         if (h_status) cudaFreeHost(h_status);
         h_status = nullptr;
@@ -330,10 +333,16 @@ int scratch_reserve(IfritGbRenderer* h, PassScratch& s, size_t tiles, size_t tri
     }
     IFTR_CUDA(h, grow(s.records, std::max<size_t>(1, tris) * sizeof(ifr::TriRecord)));
     IFTR_CUDA(h, grow(s.attrs, std::max<size_t>(1, tris) * sizeof(ifr::TriAttr)));
-    IFTR_CUDA(h, grow(s.draws, std::max<size_t>(1, ndraws) * sizeof(DrawDev)));
-    IFTR_CUDA(h, grow(s.draw_start, (ndraws + 1) * sizeof(int)));
-    IFTR_CUDA(h, grow(s.views, std::max<size_t>(1, nviews) * sizeof(ifr::ViewArgs)));
-    IFTR_CUDA(h, grow(s.view_tiles, (nviews + 1) * sizeof(int)));
+    if (ndraws > s.cap_draws || nviews > s.cap_views || !s.desc.p) {
+        s.cap_draws = std::max(s.cap_draws, std::max<size_t>(1, ndraws + ndraws / 4));
+        s.cap_views = std::max(s.cap_views, std::max<size_t>(1, nviews + nviews / 4));
+        auto a256 = [](size_t x) { return (x + 255) / 256 * 256; };
+        s.off_draw_start = a256(s.cap_draws * sizeof(DrawDev));
+        s.off_views = s.off_draw_start + a256((s.cap_draws + 1) * sizeof(int));
+        s.off_view_tiles = s.off_views + a256(s.cap_views * sizeof(ifr::ViewArgs));
+        s.generation++;
+        IFTR_CUDA(h, s.desc.reserve(s.off_view_tiles + a256((s.cap_views + 1) * sizeof(int))));
+    }
     if (entries) IFTR_CUDA(h, grow(s.entries, entries * sizeof(int)));
     if (s.pair_capacity == 0) {
         rc = ensure_pairs(h, s, std::max<size_t>(1u << 20, tris * 4));
@@ -344,26 +353,25 @@ int scratch_reserve(IfritGbRenderer* h, PassScratch& s, size_t tiles, size_t tri
 }
 
 // Copies the pass descriptors to the device through pinned staging (reused once the previous
-// upload has executed).
+// upload has executed), in one copy: the staging buffer has the device block's layout.
 int upload_descriptors(IfritGbRenderer* h, PassScratch& s, const std::vector<DrawDev>& draws,
                        const std::vector<int>& draw_start, const std::vector<ifr::ViewArgs>& views,
                        const std::vector<int>& view_tiles) {
     const size_t b0 = draws.size() * sizeof(DrawDev), b1 = draw_start.size() * sizeof(int);
     const size_t b2 = views.size() * sizeof(ifr::ViewArgs), b3 = view_tiles.size() * sizeof(int);
+    if (draws.size() > s.cap_draws || views.size() > s.cap_views) return IFTR_ERR_INVALID_ARG;  // reserved first
     if (s.staged_pending) {
         IFTR_CUDA(h, cudaEventSynchronize(s.staged));
         s.staged_pending = false;
     }
-    if (s.staging.size() < b0 + b1 + b2 + b3 && !s.staging.assign(b0 + b1 + b2 + b3)) return IFTR_ERR_CUDA;
+    const size_t total = s.off_view_tiles + b3;
+    if (s.staging.size() < total && !s.staging.assign(total)) return IFTR_ERR_CUDA;
     uint8_t* p = s.staging.data();
     std::memcpy(p, draws.data(), b0);
-    std::memcpy(p + b0, draw_start.data(), b1);
-    std::memcpy(p + b0 + b1, views.data(), b2);
-    std::memcpy(p + b0 + b1 + b2, view_tiles.data(), b3);
-    IFTR_CUDA(h, cudaMemcpyAsync(s.draws.p, p, b0, cudaMemcpyHostToDevice, h->stream));
-    IFTR_CUDA(h, cudaMemcpyAsync(s.draw_start.p, p + b0, b1, cudaMemcpyHostToDevice, h->stream));
-    IFTR_CUDA(h, cudaMemcpyAsync(s.views.p, p + b0 + b1, b2, cudaMemcpyHostToDevice, h->stream));
-    IFTR_CUDA(h, cudaMemcpyAsync(s.view_tiles.p, p + b0 + b1 + b2, b3, cudaMemcpyHostToDevice, h->stream));
+    std::memcpy(p + s.off_draw_start, draw_start.data(), b1);
+    std::memcpy(p + s.off_views, views.data(), b2);
+    std::memcpy(p + s.off_view_tiles, view_tiles.data(), b3);
+    IFTR_CUDA(h, cudaMemcpyAsync(s.desc.p, p, total, cudaMemcpyHostToDevice, h->stream));
     IFTR_CUDA(h, cudaEventRecord(s.staged, h->stream));
     s.staged_pending = true;
     return IFTR_OK;
@@ -372,12 +380,12 @@ int upload_descriptors(IfritGbRenderer* h, PassScratch& s, const std::vector<Dra
 PassArgs make_args(const PassScratch& s, int ndraws, int total_tris, int nviews, int total_tiles) {
     PassArgs a;
     std::memset(&a, 0, sizeof(a));
-    a.draws = s.draws.as<DrawDev>();
-    a.draw_start = s.draw_start.as<int>();
+    a.draws = s.desc.as<DrawDev>();
+    a.draw_start = reinterpret_cast<const int*>(s.desc.as<uint8_t>() + s.off_draw_start);
     a.ndraws = ndraws;
     a.total_tris = total_tris;
-    a.views = s.views.as<ifr::ViewArgs>();
-    a.view_tile_start = s.view_tiles.as<int>();
+    a.views = reinterpret_cast<const ifr::ViewArgs*>(s.desc.as<uint8_t>() + s.off_views);
+    a.view_tile_start = reinterpret_cast<const int*>(s.desc.as<uint8_t>() + s.off_view_tiles);
     a.nviews = nviews;
     a.total_tiles = total_tiles;
     a.tile_count = s.tile_count.as<uint32_t>();
