@@ -56,5 +56,26 @@ def build(force=False, verbose=False):
     return LIB
 
 
+INCLUDE = os.path.join(os.path.dirname(ROOT), "include")
+
+
+def build_extension(sources, out, extra_flags=()):
+    """Compiles CUDA sources written against the device-side extension point
+    (include/ifrit_gb300_ext.cuh: shading functors, mesh-stage functors) into the shared library
+    `out`, for sm_103a with the library's own float flags, linked against libifrit_gb300.so."""
+    build()
+    os.makedirs(os.path.dirname(os.path.abspath(out)), exist_ok=True)
+    tmp = out + ".tmp"
+    flags = ["-std=c++17", "-O3", "-gencode", "arch=compute_103a,code=sm_103a", "-lineinfo", "--fmad=false",
+             "-Xcompiler", "-fPIC"]
+    cmd = ([NVCC] + flags + ["-shared", "-I", INCLUDE] +
+           list(extra_flags) + list(sources) + ["-o", tmp, "-L", PKG, "-lifrit_gb300", "-Xlinker", "-rpath," + PKG])
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("extension build failed:\n" + r.stderr[-6000:])
+    os.replace(tmp, out)
+    return out
+
+
 if __name__ == "__main__":
     build(force=True, verbose=True)

@@ -107,3 +107,15 @@ def test_mesh_outputs_argument_checks(lib):
     assert lib.iftrDrawMeshOutputs(h, 1, None, None, 0, q, q, q, 4, 3, 1) == 1
     assert lib.iftrDrawMeshOutputs(None, 0, None, None, 0, None, None, None, 4, 3, 1) == 1
     assert lib.iftrDestroyInstance(h) == 0
+
+
+@pytest.mark.skipif(not os.path.exists(os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc")), reason="nvcc absent")
+def test_extension_header_builds(lib):
+    """The device-side extension point (include/ifrit_gb300_ext.cuh) compiles for sm_103a with a
+    fragment functor and a mesh-stage functor, links against the library and loads (no calls)."""
+    from ifrit_gb300 import build as ibuild
+    here = os.path.dirname(os.path.abspath(__file__))
+    out = os.path.join(ibuild.BUILD, "ext", "libext_shaders.so")
+    ibuild.build_extension([os.path.join(here, "ext", "ext_shaders.cu")], out)
+    ext = ctypes.CDLL(out)
+    assert ext.ext_shade and ext.ext_draw_grid
