@@ -132,12 +132,14 @@ uint64_t g_id_counter = 1;
 // bumps `generation`, which invalidates CUDA graphs captured with the old addresses.
 struct PassScratch {
     DevMem tile_count, tile_offset, tile_cursor, block_sums, pairs, records, attrs, status, desc, queues, entries,
-        sample_colors;
+        sample_colors, frags, frag_cols, fwd_tiles, fwd_pix_end;
     // the pass descriptors share one block (one upload per pass): draws | draw starts | views | view
     // tile starts, each at a 256-byte offset sized for cap_draws / cap_views
     size_t cap_draws = 0, cap_views = 0, off_draw_start = 0, off_views = 0, off_view_tiles = 0;
     size_t tiles_alloc = 0;
     uint32_t pair_capacity = 0;
+    uint32_t frag_capacity = 0;  // deferred ordered fragments the buffers hold
+    size_t frag_want = 0;        // capacity the next pass with ordered tiles reserves
     uint64_t generation = 1;
     uint32_t* h_status = nullptr;  // pinned copy of the status words, written by each pass
     HostBytes staging;             // pinned descriptors: draws | draw starts | views | view tile starts
@@ -145,7 +147,7 @@ struct PassScratch {
     bool staged_pending = false;
     void release() {
         for (DevMem* m : {&tile_count, &tile_offset, &tile_cursor, &block_sums, &pairs, &records, &attrs, &status, &desc,
-                          &queues, &entries, &sample_colors})
+                          &queues, &entries, &sample_colors, &frags, &frag_cols, &fwd_tiles, &fwd_pix_end})
             m->release();
         if (h_status) cudaFreeHost(h_status);
         h_status = nullptr;
@@ -206,6 +208,7 @@ struct IfritGbRenderer {
     int polygon_mode = 0;  // IF_POLYGON_MODE_*
     int polygon_rules = IFTR_POLYGON_RULES_FILL_PARTS;
     int raster_path = IFTR_RASTER_TILED;
+    long long frag_capacity_setting = -1;  // deferred ordered fragments: -1 automatic, 0 off, n fixed
     bool scissor_enable = false;
     std::vector<float> scissors;  // (x, y, w, h) per rectangle, at most 16
     // device state
@@ -401,6 +404,28 @@ PassArgs make_args(const PassScratch& s, int ndraws, int total_tris, int nviews,
     return a;
 }
 
+// Buffers of the deferred ordered fragments: per-tile bookkeeping for `tiles` tiles and at least
+// `pixels` fragments (more when an earlier pass needed more).
+int reserve_fragments(IfritGbRenderer* h, PassScratch& s, size_t tiles, size_t pixels) {
+    IFTR_CUDA(h, s.fwd_tiles.reserve(std::max<size_t>(1, tiles) * sizeof(uint4)));
+    IFTR_CUDA(h, s.fwd_pix_end.reserve(std::max<size_t>(1, tiles) * 256 * sizeof(uint16_t)));
+    size_t want = h->frag_capacity_setting > 0 ? (size_t)h->frag_capacity_setting
+                                               : std::max(s.frag_want, std::max<size_t>(1u << 20, pixels));
+    want = std::min<size_t>(want, 0xFFFFFFF0u);
+    IFTR_CUDA(h, s.frags.reserve(want * sizeof(uint4)));
+    IFTR_CUDA(h, s.frag_cols.reserve(want * sizeof(float4)));
+    s.frag_capacity = (uint32_t)want;
+    return IFTR_OK;
+}
+
+void set_fragment_args(const PassScratch& s, PassArgs& a) {
+    a.frags = s.frags.as<uint4>();
+    a.frag_cols = s.frag_cols.as<float4>();
+    a.frag_capacity = s.frag_capacity;
+    a.fwd_tiles = s.fwd_tiles.as<uint4>();
+    a.fwd_pix_end = s.fwd_pix_end.as<uint16_t>();
+}
+
 // Stream work of one pass: clear the per-pass status words, run the pipeline, copy the status
 // back to pinned memory.  Contains no host synchronisation (it is also captured into graphs).
 cudaError_t launch_with_status(PassScratch& s, const PassArgs& a, const ifr::LaunchPlan& plan, cudaStream_t st,
@@ -417,13 +442,21 @@ cudaError_t launch_with_status(PassScratch& s, const PassArgs& a, const ifr::Lau
 int consume_status(IfritGbRenderer* h, PassScratch& s) {
     const uint32_t sticky = s.h_status[ifr::ST_STICKY];
     const uint32_t max_pairs = s.h_status[ifr::ST_MAX_PAIRS];
+    const uint32_t max_frags = s.h_status[ifr::ST_MAX_FRAGS];
     h->stats.tile_pairs = s.h_status[ifr::ST_PAIRS];
-    if (sticky || max_pairs) {
+    const uint32_t frag_fail = s.h_status[ifr::ST_FRAG_FAIL];
+    h->stats.deferred_fragments = frag_fail ? 0xFFFFFFFFu - frag_fail : s.h_status[ifr::ST_FRAGS];
+    h->stats.deferred_tiles = (int)s.h_status[ifr::ST_FWD_TILES];
+    if (sticky || max_pairs || max_frags) {
         IFTR_CUDA(h, cudaMemsetAsync(s.status.as<uint32_t>() + ifr::ST_STICKY, 0,
                                      (ifr::ST_WORDS - ifr::ST_STICKY) * sizeof(uint32_t), h->stream));
         s.h_status[ifr::ST_STICKY] = 0;
         s.h_status[ifr::ST_MAX_PAIRS] = 0;
+        s.h_status[ifr::ST_MAX_FRAGS] = 0;
     }
+    // ordered tiles that found the fragment buffer full were finished by the ordered stage itself
+    // (same image); the next pass reserves room for them
+    if (max_frags > s.frag_capacity) s.frag_want = std::max(s.frag_want, (size_t)max_frags + max_frags / 4);
     if (sticky & 1u) {
         size_t want = (size_t)max_pairs + max_pairs / 4 + 1024;
         int rc = ensure_pairs(h, s, want);
@@ -611,6 +644,11 @@ int enqueue_pass(IfritGbRenderer* h, std::vector<DrawDev>& draws, int clear) {
     rc = upload_descriptors(h, h->pass, draws, draw_start, views, view_tiles);
     if (rc) return rc;
     PassArgs a = make_args(h->pass, (int)draws.size(), (int)total, 1, T);
+    if (plan.defer_group >= 0 && h->frag_capacity_setting != 0) {
+        rc = reserve_fragments(h, h->pass, (size_t)T, (size_t)W * H);
+        if (rc) return rc;
+        set_fragment_args(h->pass, a);
+    }
     IFTR_CUDA(h, launch_with_status(h->pass, a, plan, h->stream, h->timing ? h->ev : nullptr));
     h->stats.triangles_in = (uint64_t)total;
     h->pending = 1;
@@ -1302,6 +1340,13 @@ IFTR_API int iftrSetRasterPath(IfritGbRenderer* h, int path) {
 IFTR_API int iftrSetRasterizerPolygonMode(IfritGbRenderer* h, int mode) {
     if (!h || mode < IF_POLYGON_MODE_FILL || mode > IF_POLYGON_MODE_POINT) return IFTR_ERR_INVALID_ARG;
     h->polygon_mode = mode;
+    return IFTR_OK;
+}
+
+IFTR_API int iftrSetOrderedFragmentCapacity(IfritGbRenderer* h, long long fragments) {
+    if (!h || fragments < -1 || fragments > 0xFFFFFFF0LL) return IFTR_ERR_INVALID_ARG;
+    if (h->in_pass) return IFTR_ERR_STATE;
+    h->frag_capacity_setting = fragments;
     return IFTR_OK;
 }
 

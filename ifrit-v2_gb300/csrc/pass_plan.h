@@ -181,6 +181,16 @@ inline bool plan_groups(ViewArgs* v, int n, int* view_tile_start, int sms, int c
     }
     view_tile_start[n] = t;
     total_tiles = t;
+    plan.defer_group = -1;
+    for (int k = 0; k < plan.ngroups; k++)
+        if (plan.ordered[k]) plan.defer_group = plan.defer_group == -1 ? k : -2;
+    if (plan.defer_group >= 0) {
+        const int S = plan.samples[plan.defer_group];
+        plan.ctas_frag_shade = sms * frag_kernel_occupancy(S, 0);
+        plan.ctas_frag_blend = sms * frag_kernel_occupancy(S, 1);
+    } else {
+        plan.defer_group = -1;
+    }
     for (int k = 0; k < plan.ngroups; k++) {
         const int tiles = plan.groups[k].tile_end - plan.groups[k].tile_begin;
         const int S = plan.samples[k], TS = plan.tile_size[k];

@@ -1643,12 +1643,18 @@ struct FwdRecords {
     long long Cb[3][kFwdThreads];
     float z0[kFwdThreads], dzdx[kFwdThreads], dzdy[kFwdThreads];
     int32_t X0[kFwdThreads], Y0[kFwdThreads];
-    int32_t bx[kFwdThreads], by[kFwdThreads];  // px0 | px1 << 16, py0 | py1 << 16
     int32_t key[kFwdThreads];
     int32_t draw[kFwdThreads];
 };
 
-constexpr int kFwdFrags = 8;  // fragments a pixel holds before they are shaded
+constexpr int kFwdFrags = 8;      // fragments a pixel holds before they are shaded
+constexpr int kFwdSmallBox = 24;  // candidate boxes of up to this many pixels are marked by their record's thread
+
+// Lane of pixel (lx, ly) of a TS x TS tile (inverse of tile_pixel).
+template <int TS>
+__device__ __forceinline__ int tile_lane(int lx, int ly) {
+    return ((((ly >> 1) * (TS / 2)) + (lx >> 1)) << 2) | ((ly & 1) << 1) | (lx & 1);
+}
 
 // Shades fragment f = (entry, sample mask) at pixel (px, py) and writes or blends it into the
 // per-sample colours of the calling thread.
@@ -1682,18 +1688,33 @@ __device__ __noinline__ void apply_fragments(const PassArgs& a, const ViewArgs& 
 }
 
 
+// Starting colours of the calling thread's samples: the prefix's per-sample colours handed off by
+// the shade stage, or the background.
 template <int S>
-__device__ __forceinline__ void forward_tile(const PassArgs& a, const ViewArgs& v, int gtile, FwdRecords& rec,
-                                             float4* scol, uint32_t* list, int2* frags, bool after_raster,
-                                             BulkState& bs) {
+__device__ __forceinline__ void start_colours(const ViewArgs& v, float4* scol, int ltile, bool after_raster,
+                                              const float bg[4]) {
+    constexpr int NT = kFwdThreads;
+#pragma unroll
+    for (int k = 0; k < S; k++)
+        scol[k * NT + threadIdx.x] = after_raster ? v.sample_colors[((size_t)ltile * S + k) * NT + threadIdx.x]
+                                                  : make_float4(bg[0], bg[1], bg[2], bg[3]);
+}
+
+template <int S>
+__device__ __forceinline__ void forward_tile(const PassArgs& a, const ViewArgs& v, int vi, int gtile, FwdRecords& rec,
+                                             float4* scol, uint32_t* list, int2* frags, uint32_t* cand,
+                                             bool after_raster, BulkState& bs) {
     constexpr int TS = 16, NT = kFwdThreads;
     // after the raster and shade stages the shade stage has finished the tiles without ordered
     // entries (uniform over the CTA)
     if (after_raster && a.tile_cursor[gtile] == 0u) return;
     const int ltile = gtile - v.tile_start;
-    // the prefix's per-sample colours of the tile (S x 256 float4, contiguous in the tile-major
-    // hand-off) come in by one bulk copy (TMA) that overlaps the gathering and sorting below
-    const bool bulk = after_raster && bs.ok;
+    // With deferred shading (a.frags set) the tile's fragments usually go to the fragment kernels
+    // and the per-sample colours are only loaded where fragments are applied here.  Otherwise the
+    // prefix's per-sample colours of the tile (S x 256 float4, contiguous in the tile-major
+    // hand-off) come in by one bulk copy (TMA) that overlaps the gathering and sorting below.
+    const bool defer = a.frags != nullptr;
+    const bool bulk = after_raster && bs.ok && !defer;
     if (bulk && threadIdx.x == 0)
         bulk_load(scol, v.sample_colors + (size_t)ltile * S * NT, (uint32_t)(sizeof(float4) * S * NT), bs.bar);
     const int tx = ltile % v.c.tiles_x, ty = ltile / v.c.tiles_x;
@@ -1706,31 +1727,33 @@ __device__ __forceinline__ void forward_tile(const PassArgs& a, const ViewArgs& 
 
     float dep[S];
     int vid[S];
-    {
-        float bg[4];
-        if (v.clear) {
-            bg[0] = v.clear_color[0]; bg[1] = v.clear_color[1]; bg[2] = v.clear_color[2]; bg[3] = v.clear_color[3];
-        } else if (inpix) {
-            decode_color(v, pix, bg);
-        } else {
-            bg[0] = bg[1] = bg[2] = bg[3] = 0.0f;
-        }
+    float bg[4];
+    if (v.clear) {
+        bg[0] = v.clear_color[0]; bg[1] = v.clear_color[1]; bg[2] = v.clear_color[2]; bg[3] = v.clear_color[3];
+    } else if (inpix && !after_raster) {
+        decode_color(v, pix, bg);
+    } else {
+        bg[0] = bg[1] = bg[2] = bg[3] = 0.0f;
+    }
 #pragma unroll
-        for (int k = 0; k < S; k++) {
-            if (after_raster) {
-                // the prefix's per-sample state as the shade stage left it: colour in the
-                // per-sample scratch (bulk-copied above), depth and primitive id in the outputs
-                const int ent = inpix ? v.entries[pix * S + k] : -1;
-                dep[k] = inpix ? v.depth[pix * S + k] : 0.0f;
-                vid[k] = ent < 0 ? -1 : (ent >> 3) - v.first_tri;
-                if (!bulk) scol[k * NT + tid] = v.sample_colors[((size_t)ltile * S + k) * NT + tid];
-            } else {
-                dep[k] = v.clear ? v.clear_depth : (inpix ? v.depth[pix * S + k] : 0.0f);
-                vid[k] = -1;
-                scol[k * NT + tid] = make_float4(bg[0], bg[1], bg[2], bg[3]);
-            }
+    for (int k = 0; k < S; k++) {
+        if (after_raster) {
+            // the prefix's per-sample state as the shade stage left it: colour in the per-sample
+            // scratch, depth and primitive id in the outputs
+            const int ent = inpix ? v.entries[pix * S + k] : -1;
+            dep[k] = inpix ? v.depth[pix * S + k] : 0.0f;
+            vid[k] = ent < 0 ? -1 : (ent >> 3) - v.first_tri;
+        } else {
+            dep[k] = v.clear ? v.clear_depth : (inpix ? v.depth[pix * S + k] : 0.0f);
+            vid[k] = -1;
         }
     }
+    bool have_cols = bulk;  // scol holds this thread's starting colours
+    if (!defer && !bulk) {
+        start_colours<S>(v, scol, ltile, after_raster, bg);
+        have_cols = true;
+    }
+    bool flushed = false;  // this pixel applied fragments on the spot
     const bool has_list = a.total_tris > 0 && a.status[ST_OVERFLOW] == 0;
     const uint32_t beg = has_list ? a.tile_offset[gtile] : 0u;
     const uint32_t end = has_list ? a.tile_offset[gtile + 1] : 0u;
@@ -1802,8 +1825,14 @@ __device__ __forceinline__ void forward_tile(const PassArgs& a, const ViewArgs& 
         }
     }
     int nfrag = 0;  // fragments recorded for this thread's pixel, not yet shaded
+    const int lane = tid & 31;
     for (int base = 0; base < n; base += NT) {
         const int nb = min(NT, n - base);
+        // candidate masks of the batch: bit r of cand[r / 32][lane] when record r's pixel box
+        // holds the lane's pixel
+#pragma unroll
+        for (int w = 0; w < NT / 32; w++) cand[w * NT + tid] = 0u;
+        int area = 0, cx0 = 0, cy0 = 0, cw = 1;
         if (tid < nb) {
             uint32_t e = list[base + tid];
             SubTri s;
@@ -1820,49 +1849,139 @@ __device__ __forceinline__ void forward_tile(const PassArgs& a, const ViewArgs& 
                 rec.dzdy[tid] = s.dzdy;
                 rec.X0[tid] = s.X[0];
                 rec.Y0[tid] = s.Y[0];
-                rec.bx[tid] = s.px0 | (s.px1 << 16);
-                rec.by[tid] = s.py0 | (s.py1 << 16);
-            } else {
-                rec.bx[tid] = 1;
-                rec.by[tid] = 1;
+                cx0 = max(s.px0 - tx * TS, 0);
+                cy0 = max(s.py0 - ty * TS, 0);
+                const int cx1 = min(s.px1 - tx * TS, TS - 1), cy1 = min(s.py1 - ty * TS, TS - 1);
+                if (cx1 >= cx0 && cy1 >= cy0) {
+                    cw = cx1 - cx0 + 1;
+                    area = cw * (cy1 - cy0 + 1);
+                }
             }
             rec.key[tid] = (int)e;
             rec.draw[tid] = di;
         }
         __syncthreads();
+        // mark the candidates: small boxes by their record's thread, larger ones by the whole warp
+        uint32_t* crow = cand + (tid >> 5) * NT;
+        if (area > 0 && area <= kFwdSmallBox) {
+            const unsigned bit = 1u << lane;
+            for (int y = cy0, i = 0; i < area; y++)
+                for (int x = cx0; x < cx0 + cw; x++, i++) atomicOr(crow + tile_lane<TS>(x, y), bit);
+        }
+        unsigned big = __ballot_sync(0xffffffffu, area > kFwdSmallBox);
+        while (big) {
+            const int l = __ffs(big) - 1;
+            big &= big - 1;
+            const int na = __shfl_sync(0xffffffffu, area, l), x0 = __shfl_sync(0xffffffffu, cx0, l);
+            const int y0 = __shfl_sync(0xffffffffu, cy0, l), w0 = __shfl_sync(0xffffffffu, cw, l);
+            for (int i = lane; i < na; i += 32) atomicOr(crow + tile_lane<TS>(x0 + i % w0, y0 + i / w0), 1u << l);
+        }
+        __syncthreads();
         if (inpix) {
-            for (int r = 0; r < nb; r++) {
-                const int bx = rec.bx[r], by = rec.by[r];
-                if (px < (bx & 0xffff) || px > (bx >> 16) || py < (by & 0xffff) || py > (by >> 16)) continue;
-                const int32_t A[3] = {rec.A[0][r], rec.A[1][r], rec.A[2][r]};
-                const int32_t B[3] = {rec.B[0][r], rec.B[1][r], rec.B[2][r]};
-                const int64_t Cb[3] = {rec.Cb[0][r], rec.Cb[1][r], rec.Cb[2][r]};
-                const DrawDev& d = a.draws[rec.draw[r]];
-                if (!scissor_pass(d, px, py)) continue;
-                const int func = d.depth_func, write = d.depth_write;
-                const int e = rec.key[r];
-                unsigned mask = 0;
+            // this pixel's candidates in submission order
+            for (int w = 0; w < NT / 32; w++) {
+                uint32_t bits = cand[w * NT + tid];
+                while (bits) {
+                    const int r = w * 32 + __ffs(bits) - 1;
+                    bits &= bits - 1;
+                    const int32_t A[3] = {rec.A[0][r], rec.A[1][r], rec.A[2][r]};
+                    const int32_t B[3] = {rec.B[0][r], rec.B[1][r], rec.B[2][r]};
+                    const int64_t Cb[3] = {rec.Cb[0][r], rec.Cb[1][r], rec.Cb[2][r]};
+                    const DrawDev& d = a.draws[rec.draw[r]];
+                    if (!scissor_pass(d, px, py)) continue;
+                    const int func = d.depth_func, write = d.depth_write;
+                    const int e = rec.key[r];
+                    unsigned mask = 0;
 #pragma unroll
-                for (int k = 0; k < S; k++) {
-                    const int32_t sx = px * 256 + sample_x<S>(k), sy = py * 256 + sample_y<S>(k);
-                    if (!covered(A, B, Cb, sx, sy)) continue;
-                    const float z = sample_depth(rec.z0[r], rec.dzdx[r], rec.dzdy[r], rec.X0[r], rec.Y0[r], sx, sy);
-                    if (!depth_cmp(func, z, dep[k])) continue;
-                    if (write) dep[k] = z;
-                    vid[k] = (e >> 3) - v.first_tri;
-                    mask |= 1u << k;
+                    for (int k = 0; k < S; k++) {
+                        const int32_t sx = px * 256 + sample_x<S>(k), sy = py * 256 + sample_y<S>(k);
+                        if (!covered(A, B, Cb, sx, sy)) continue;
+                        const float z = sample_depth(rec.z0[r], rec.dzdx[r], rec.dzdy[r], rec.X0[r], rec.Y0[r], sx, sy);
+                        if (!depth_cmp(func, z, dep[k])) continue;
+                        if (write) dep[k] = z;
+                        vid[k] = (e >> 3) - v.first_tri;
+                        mask |= 1u << k;
+                    }
+                    if (!mask) continue;
+                    // colours never change depth: record the fragment now, shade it later
+                    if (nfrag == kFwdFrags) {  // a full list is applied on the spot (rare)
+                        if (!have_cols) start_colours<S>(v, scol, ltile, after_raster, bg);
+                        have_cols = true;
+                        apply_fragments<S>(a, v, px, py, scol, frags, nfrag);
+                        nfrag = 0;
+                        flushed = true;
+                    }
+                    frags[nfrag * NT + tid] = make_int2(e, (int)mask);
+                    nfrag++;
                 }
-                if (!mask) continue;
-                // colours never change depth: record the fragment now, shade it later
-                if (nfrag == kFwdFrags) {  // a full list is applied on the spot (rare)
-                    apply_fragments<S>(a, v, px, py, scol, frags, nfrag);
-                    nfrag = 0;
-                }
-                frags[nfrag * NT + tid] = make_int2(e, (int)mask);
-                nfrag++;
             }
         }
         __syncthreads();
+    }
+    if (defer) {
+        // Hand the tile's fragments to the fragment kernels, pixel-major in lane order, unless a
+        // pixel already applied some on the spot or the fragment buffer is full (then the tile is
+        // finished here).  Depth and primitive ids are final now.
+        __shared__ uint32_t s_wsum[NT / 32];
+        __shared__ int s_slot;
+        __shared__ uint32_t s_base;
+        if (!__syncthreads_or(flushed)) {
+            uint32_t incl = (uint32_t)nfrag;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const uint32_t q = __shfl_up_sync(0xffffffffu, incl, o);
+                if (lane >= o) incl += q;
+            }
+            if (lane == 31) s_wsum[tid >> 5] = incl;
+            __syncthreads();
+            uint32_t before = 0, total = 0;
+#pragma unroll
+            for (int w = 0; w < NT / 32; w++) {
+                const uint32_t x = s_wsum[w];
+                before += w < (tid >> 5) ? x : 0u;
+                total += x;
+            }
+            const uint32_t pre = before + incl - (uint32_t)nfrag;
+            if (tid == 0) {
+                int slot = -1;
+                uint32_t fbase = 0;
+                if (total > 0) {
+                    fbase = atomicAdd(a.status + ST_FRAGS, total);
+                    if ((unsigned long long)fbase + total <= a.frag_capacity) {
+                        slot = (int)atomicAdd(a.status + ST_FWD_TILES, 1u);
+                        a.fwd_tiles[slot] = make_uint4((uint32_t)gtile, fbase, (uint32_t)vi, after_raster ? 1u : 0u);
+                    } else {  // later allocations fail too: the fragments below this one are all written
+                        atomicMax(a.status + ST_FRAG_FAIL, 0xFFFFFFFFu - fbase);
+                        const unsigned long long want = (unsigned long long)fbase + total;
+                        atomicMax(a.status + ST_MAX_FRAGS, want > 0xFFFFFFFFull ? 0xFFFFFFFFu : (uint32_t)want);
+                    }
+                }
+                s_slot = slot;
+                s_base = fbase;
+            }
+            __syncthreads();
+            const int slot = s_slot;
+            if (slot >= 0) {
+                uint4* out = a.frags + s_base + pre;
+                for (int i = 0; i < nfrag; i++) {
+                    const int2 f = frags[i * NT + tid];
+                    out[i] = make_uint4((uint32_t)f.x, (uint32_t)px | ((uint32_t)py << 16), (uint32_t)f.y, 0u);
+                }
+                a.fwd_pix_end[(size_t)slot * NT + tid] = (uint16_t)(pre + nfrag);
+                if (inpix) {
+                    float* dp = v.depth + pix * S;
+#pragma unroll
+                    for (int k = 0; k < S; k++) dp[k] = dep[k];
+                    if (v.vis) {
+                        int* vp = v.vis + pix * S;
+#pragma unroll
+                        for (int k = 0; k < S; k++) vp[k] = vid[k];
+                    }
+                }
+                return;
+            }
+        }
+        if (!have_cols) start_colours<S>(v, scol, ltile, after_raster, bg);
     }
     // shade the recorded fragments with the warp converged on fragment slot i of every lane, and
     // apply each one in submission order to its samples (spreading the fragments' anisotropic probes
@@ -1898,7 +2017,7 @@ __device__ __forceinline__ void forward_tile(const PassArgs& a, const ViewArgs& 
 template <int S>
 size_t forward_smem_bytes() {
     return sizeof(FwdRecords) + sizeof(float4) * S * kFwdThreads + sizeof(uint32_t) * kOrderedCap +
-           sizeof(int2) * kFwdFrags * kFwdThreads;
+           sizeof(int2) * kFwdFrags * kFwdThreads + sizeof(uint32_t) * kFwdThreads * (kFwdThreads / 32);
 }
 
 template <int S>
@@ -1908,6 +2027,7 @@ __global__ void __launch_bounds__(kFwdThreads) forward_kernel(PassArgs a, GroupA
     float4* scol = reinterpret_cast<float4*>(smem_raw + sizeof(FwdRecords));  // [S][256]
     uint32_t* list = reinterpret_cast<uint32_t*>(smem_raw + sizeof(FwdRecords) + sizeof(float4) * S * kFwdThreads);
     int2* frags = reinterpret_cast<int2*>(list + kOrderedCap);  // [kFwdFrags][256]
+    uint32_t* cand = reinterpret_cast<uint32_t*>(frags + kFwdFrags * kFwdThreads);  // [8][256]
     __shared__ ViewArgs sv;
     __shared__ int s_tile, s_view;
     __shared__ __align__(8) uint64_t s_bar;
@@ -1922,8 +2042,97 @@ __global__ void __launch_bounds__(kFwdThreads) forward_kernel(PassArgs a, GroupA
     }
     __syncthreads();
     while (next_tile<kFwdThreads>(a, g, qslot, sv, s_tile, s_view))
-        forward_tile<S>(a, sv, s_tile, rec, scol, list, frags, after_raster != 0, bs);
+        forward_tile<S>(a, sv, s_view, s_tile, rec, scol, list, frags, cand, after_raster != 0, bs);
     if (bs.pending && threadIdx.x == 0) mbar_wait(&s_bar, (bs.phase - 1) & 1u);  // a copy that did not land in time
+}
+
+// ---------------------------------------------------------------------------- deferred ordered fragments
+// Fragments of the ordered tiles that the ordered stage handed off: their colours do not depend
+// on the order they are applied in, so they are shaded here with every thread busy (the tile
+// routine would leave most threads of a tile waiting for the pixels with the most fragments),
+// then blended per pixel in submission order.
+
+// Fragments below this count were written by tiles whose allocation fitted.
+__device__ __forceinline__ uint32_t deferred_fragments(const PassArgs& a) {
+    const uint32_t fail = a.status[ST_FRAG_FAIL];
+    const uint32_t n = fail ? 0xFFFFFFFFu - fail : a.status[ST_FRAGS];
+    return min(n, a.frag_capacity);
+}
+
+__global__ void __launch_bounds__(256) frag_shade_kernel(PassArgs a) {
+    const uint32_t n = deferred_fragments(a);
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const uint4 f = a.frags[i];
+        const DrawDev& d = a.draws[record_draw(a, (int)(f.x >> 3))];
+        float c[4];
+        RecordPlane pl;
+        shade_uncached(a, a.views[d.view].c, (int)f.x, (int)(f.y & 0xffffu), (int)(f.y >> 16), c, &pl);
+        a.frag_cols[i] = make_float4(c[0], c[1], c[2], c[3]);
+    }
+}
+
+// One deferred tile per CTA iteration, one pixel per thread: the starting colours (the prefix's
+// hand-off or the background), the pixel's fragments applied in submission order, then the resolve.
+template <int S>
+__global__ void __launch_bounds__(kFwdThreads) frag_blend_kernel(PassArgs a) {
+    constexpr int TS = 16, NT = kFwdThreads;
+    const uint32_t ntiles = a.status[ST_FWD_TILES];
+    const int tid = threadIdx.x;
+    int lx, ly;
+    tile_pixel<TS>(tid, lx, ly);
+    for (uint32_t slot = blockIdx.x; slot < ntiles; slot += gridDim.x) {
+        const uint4 t = a.fwd_tiles[slot];  // global tile, first fragment, view, hand-off flag
+        const ViewArgs& v = a.views[t.z];
+        const int ltile = (int)t.x - v.tile_start;
+        const int tx = ltile % v.c.tiles_x, ty = ltile / v.c.tiles_x;
+        const int px = tx * TS + lx, py = ty * TS + ly;
+        if (px >= v.c.W || py >= v.c.H) continue;
+        const size_t pix = (size_t)py * v.c.W + px;
+        float col[S][4];
+        if (t.w) {
+#pragma unroll
+            for (int k = 0; k < S; k++) {
+                const float4 q = v.sample_colors[((size_t)ltile * S + k) * NT + tid];
+                col[k][0] = q.x; col[k][1] = q.y; col[k][2] = q.z; col[k][3] = q.w;
+            }
+        } else {
+            float bg[4];
+            if (v.clear) {
+                bg[0] = v.clear_color[0]; bg[1] = v.clear_color[1]; bg[2] = v.clear_color[2]; bg[3] = v.clear_color[3];
+            } else {
+                decode_color(v, pix, bg);
+            }
+#pragma unroll
+            for (int k = 0; k < S; k++) {
+                col[k][0] = bg[0]; col[k][1] = bg[1]; col[k][2] = bg[2]; col[k][3] = bg[3];
+            }
+        }
+        const uint16_t* pe = a.fwd_pix_end + (size_t)slot * NT;
+        const uint32_t f0 = t.y + (tid ? pe[tid - 1] : 0u), f1 = t.y + pe[tid];
+        for (uint32_t f = f0; f < f1; f++) {
+            const uint4 r = a.frags[f];
+            const float4 q = a.frag_cols[f];
+            const float c[4] = {q.x, q.y, q.z, q.w};
+            const DrawDev& d = a.draws[record_draw(a, (int)(r.x >> 3))];
+#pragma unroll
+            for (int k = 0; k < S; k++) {
+                if (!(r.z & (1u << k))) continue;
+                if (d.blend_enable) {
+                    blend_into(d, c, col[k]);
+                } else {
+                    col[k][0] = c[0]; col[k][1] = c[1]; col[k][2] = c[2]; col[k][3] = c[3];
+                }
+            }
+        }
+        float acc[4] = {col[0][0], col[0][1], col[0][2], col[0][3]};
+#pragma unroll
+        for (int k = 1; k < S; k++) {
+            acc[0] = acc[0] + col[k][0]; acc[1] = acc[1] + col[k][1]; acc[2] = acc[2] + col[k][2]; acc[3] = acc[3] + col[k][3];
+        }
+        const float invS = 1.0f / (float)S;
+        acc[0] = acc[0] * invS; acc[1] = acc[1] * invS; acc[2] = acc[2] * invS; acc[3] = acc[3] * invS;
+        encode_color(v, pix, acc);
+    }
 }
 
 // ---------------------------------------------------------------------------- reference line / point rules
@@ -2281,6 +2490,24 @@ cudaError_t launch_forward(const PassArgs& a, const GroupArgs& g, int ctas, cuda
     return cudaSuccess;
 }
 
+template <int S>
+cudaError_t launch_frag_kernels(const PassArgs& a, int ctas_shade, int ctas_blend, cudaStream_t stream) {
+    frag_shade_kernel<<<ctas_shade, 256, 0, stream>>>(a);
+    frag_blend_kernel<S><<<ctas_blend, kFwdThreads, 0, stream>>>(a);
+    return cudaSuccess;
+}
+
+cudaError_t launch_group_frags(const PassArgs& a, int S, int ctas_shade, int ctas_blend, cudaStream_t stream) {
+    switch (S) {
+    case 1: return launch_frag_kernels<1>(a, ctas_shade, ctas_blend, stream);
+    case 2: return launch_frag_kernels<2>(a, ctas_shade, ctas_blend, stream);
+    case 4: return launch_frag_kernels<4>(a, ctas_shade, ctas_blend, stream);
+    case 8: return launch_frag_kernels<8>(a, ctas_shade, ctas_blend, stream);
+    case 16: return launch_frag_kernels<16>(a, ctas_shade, ctas_blend, stream);
+    default: return cudaErrorInvalidValue;
+    }
+}
+
 // One tile stage (raster or shade) of a deferred group.
 cudaError_t launch_group_stage(const PassArgs& a, const GroupArgs& g, int S, int TS, int ctas, cudaStream_t stream,
                                bool shade) {
@@ -2334,6 +2561,17 @@ template <int S>
 int forward_occupancy() {
     configure_forward<S>();
     return occupancy_of(forward_kernel<S>, kFwdThreads, forward_smem_bytes<S>());
+}
+
+int frag_kernel_occupancy(int S, int stage) {
+    if (stage == 0) return occupancy_of(frag_shade_kernel, 256, 0);
+    switch (S) {
+    case 1: return occupancy_of(frag_blend_kernel<1>, kFwdThreads, 0);
+    case 2: return occupancy_of(frag_blend_kernel<2>, kFwdThreads, 0);
+    case 4: return occupancy_of(frag_blend_kernel<4>, kFwdThreads, 0);
+    case 8: return occupancy_of(frag_blend_kernel<8>, kFwdThreads, 0);
+    default: return occupancy_of(frag_blend_kernel<16>, kFwdThreads, 0);
+    }
 }
 
 int tile_kernel_occupancy(int S, int TS, int ordered, int stage) {
@@ -2426,6 +2664,8 @@ cudaError_t launch_pass(const PassArgs& a, const LaunchPlan& plan, cudaStream_t 
     if (ev) cudaEventRecord(ev[5], stream);
     for (int i = 0; i < plan.ngroups && err == cudaSuccess; i++)
         if (plan.hybrid[i]) err = launch_group_forward(a, plan.groups[i], plan.samples[i], plan.ctas_fwd[i], stream, true);
+    if (err == cudaSuccess && a.frags && plan.defer_group >= 0)
+        err = launch_group_frags(a, plan.samples[plan.defer_group], plan.ctas_frag_shade, plan.ctas_frag_blend, stream);
     if (ev) cudaEventRecord(ev[6], stream);
     return err != cudaSuccess ? err : cudaGetLastError();
 }

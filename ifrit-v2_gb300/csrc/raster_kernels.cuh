@@ -16,15 +16,19 @@ constexpr int kMaxViews = 4096;
 // Status words of a pass.  Words below ST_PASS_WORDS describe the latest pass and are cleared
 // when it starts; ST_STICKY (bit 0: some pass overflowed its pair list, bit 1: some ordered tile
 // exceeded kOrderedCap, bit 2: a bulk copy into shared memory was not seen complete within the
-// wait limit) and ST_MAX_PAIRS accumulate until the host reads and clears them.
+// wait limit), ST_MAX_PAIRS and ST_MAX_FRAGS accumulate until the host reads and clears them.
 enum StatusWord {
     ST_OVERFLOW = 0,
     ST_PAIRS = 1,
     ST_ORDERED_LIMIT = 2,
-    ST_PASS_WORDS = 4,
-    ST_STICKY = 4,
-    ST_MAX_PAIRS = 5,
-    ST_WORDS = 8
+    ST_FRAGS = 3,       // deferred ordered fragments allocated (may run past the capacity)
+    ST_FRAG_FAIL = 4,   // 0xFFFFFFFF - offset of the first allocation that did not fit; 0: none
+    ST_FWD_TILES = 5,   // ordered tiles whose fragments were deferred
+    ST_PASS_WORDS = 6,
+    ST_STICKY = 6,
+    ST_MAX_PAIRS = 7,
+    ST_MAX_FRAGS = 8,   // largest fragment demand of a pass that did not fit (grows the buffer)
+    ST_WORDS = 12
 };
 constexpr int kOrderedCap = 8192;  // entries per tile an ordered (in-API-order) pass can sort
 
@@ -77,6 +81,12 @@ struct PassArgs {
     uint32_t pair_capacity;
     uint32_t* status;        // StatusWord
     uint32_t* queues;        // persistent tile counters, 3 per launch group (raster, shade, ordered)
+    // deferred shading of ordered fragments (frags == nullptr: the ordered stage shades its own)
+    uint4* frags;            // [frag_capacity] entry, px | py << 16, sample mask, 0
+    float4* frag_cols;       // [frag_capacity] colour of each fragment
+    uint32_t frag_capacity;
+    uint4* fwd_tiles;        // [total_tiles] deferred tiles: global tile, first fragment, view, hand-off flag
+    uint16_t* fwd_pix_end;   // [total_tiles][256] end of each pixel's fragments, from the tile's first
 };
 
 constexpr int kMaxGroups = 16;  // launch groups of a pass: (samples, path, tile size) combinations
@@ -101,6 +111,10 @@ struct LaunchPlan {
     int ctas_fwd[kMaxGroups];   // hybrid groups: persistent CTAs of the ordered stage after shading
     int atomic;                 // one deferred view resolved by the atomic visibility path (no binning)
     int atomic_pixels;          // its W * H
+    int defer_group;            // the only ordered group, whose fragments may be shaded by their own
+                                //    kernels (when PassArgs::frags is set); -1: none
+    int ctas_frag_shade;        // CTAs of the deferred fragment shading and blending kernels
+    int ctas_frag_blend;
 };
 
 }  // namespace ifr
@@ -128,4 +142,6 @@ cudaError_t launch_mesh_compact(const float* pos, const float* attr, const int* 
 // Maximum resident CTAs per SM of a tile kernel for (samples, tile size, ordered); stage 0 is
 // the raster (or ordered) kernel, stage 1 the shade kernel.
 int tile_kernel_occupancy(int samples, int tile_size, int ordered, int stage);
+// Resident CTAs per SM of the deferred fragment shading (stage 0) and blending (stage 1) kernels.
+int frag_kernel_occupancy(int samples, int stage);
 }  // namespace ifr

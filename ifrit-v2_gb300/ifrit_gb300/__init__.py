@@ -48,7 +48,7 @@ EXPORTED = [
     "iftrSetVertexBufferDirty", "ifbufGetBufferRawData", "ifbufSetBufferDirty", "iftrDrawNoAlloc",
     "iftrBeginPass", "iftrPassDraw", "iftrEndPass", "iftrDrawBatch", "iftrSetBatchTuning", "iftrGetBatchTuning",
     "iftrDiffForward", "iftrDiffBackward", "iftrSetScissors", "iftrSetScissorTestEnable",
-    "iftrSetRasterizerPolygonMode", "iftrSetRasterPath", "iftrDrawMeshOutputs", "iftrSetPolygonRules",
+    "iftrSetRasterizerPolygonMode", "iftrSetRasterPath", "iftrDrawMeshOutputs", "iftrSetOrderedFragmentCapacity", "iftrSetPolygonRules",
 ]
 
 
@@ -111,7 +111,8 @@ class DiffPass(ctypes.Structure):
 
 class Stats(ctypes.Structure):
     _fields_ = [("triangles_in", ctypes.c_uint64), ("tile_pairs", ctypes.c_uint64),
-                ("pair_capacity", ctypes.c_uint64), ("retries", ctypes.c_int)]
+                ("pair_capacity", ctypes.c_uint64), ("retries", ctypes.c_int), ("deferred_tiles", ctypes.c_int),
+                ("deferred_fragments", ctypes.c_uint64)]
 
 
 _lib = None
@@ -172,6 +173,7 @@ def load(build_if_missing=True):
         "iftrSetScissors": [vp, fp, ip], "iftrSetScissorTestEnable": [vp, ip],
         "iftrSetRasterizerPolygonMode": [vp, ip], "iftrSetRasterPath": [vp, ip],
         "iftrDrawMeshOutputs": [vp, ip, vp, vp, ip, vp, vp, vp, ip, ip, ip],
+        "iftrSetOrderedFragmentCapacity": [vp, ctypes.c_longlong],
     }
     for name, args in sig.items():
         getattr(lib, name).argtypes = args
@@ -284,6 +286,11 @@ class Renderer:
         check("iftrDrawMeshOutputs", self.lib.iftrDrawMeshOutputs(
             self.h, G, positions.data_ptr(), attributes.data_ptr() if attributes is not None else None, attr_count,
             indices.data_ptr(), num_vertices.data_ptr(), num_indices.data_ptr(), max_v, max_i, int(clear)))
+
+    def set_ordered_fragment_capacity(self, fragments=-1):
+        """-1: automatic deferred shading of ordered fragments; 0: shaded inside the ordered stage;
+        n > 0: a fragment buffer of exactly n (tiles that do not fit are finished in the stage)."""
+        check("iftrSetOrderedFragmentCapacity", self.lib.iftrSetOrderedFragmentCapacity(self.h, int(fragments)))
 
     def set_raster_path(self, path):
         check("iftrSetRasterPath", self.lib.iftrSetRasterPath(self.h, path))

@@ -88,6 +88,8 @@ typedef struct {
     uint64_t tile_pairs;          /* (triangle, tile) overlaps binned in the last pass */
     uint64_t pair_capacity;       /* current scratch capacity in pairs */
     int retries;                  /* overflow re-runs of the last synchronous draw */
+    int deferred_tiles;           /* ordered tiles whose fragments the last pass shaded in the fragment kernels */
+    uint64_t deferred_fragments;  /* those tiles' fragments */
 } IfritGbStats;
 
 typedef struct IfritGbRenderer IfritGbRenderer;
@@ -161,6 +163,14 @@ IFTR_API int iftrSetRasterizerPolygonMode(IfritGbRenderer* h, int mode);
  * belongs to. */
 enum { IFTR_POLYGON_RULES_FILL_PARTS = 0, IFTR_POLYGON_RULES_REFERENCE = 1 };
 IFTR_API int iftrSetPolygonRules(IfritGbRenderer* h, int rules);
+/* Fragments of ordered (blended) draws (no counterpart in the reference): the ordered stage
+ * resolves coverage and depth tile by tile in submission order and hands each tile's passing
+ * fragments to a shading kernel that keeps every thread busy and a blending kernel that applies
+ * them per pixel in order.  The image is the same either way.  fragments = -1 (default): buffer
+ * for one fragment per pixel, grown after a pass that needed more; 0: the ordered stage shades
+ * its fragments itself; n > 0: a buffer of exactly n fragments.  Tiles whose fragments do not fit
+ * (or with more than 8 fragments on one pixel) are finished by the ordered stage. */
+IFTR_API int iftrSetOrderedFragmentCapacity(IfritGbRenderer* h, long long fragments);
 /* Raster path of order-independent passes (no counterpart in the reference).  TILED (default):
  * triangles binned into 16x16 tiles, resolved per tile in shared memory.  ATOMIC: no binning;
  * each triangle's thread resolves its samples into per-sample 64-bit (depth, primitive) keys in

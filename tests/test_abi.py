@@ -119,3 +119,14 @@ def test_extension_header_builds(lib):
     ibuild.build_extension([os.path.join(here, "ext", "ext_shaders.cu")], out)
     ext = ctypes.CDLL(out)
     assert ext.ext_shade and ext.ext_draw_grid
+
+
+def test_ordered_fragment_capacity_argument_checks(lib):
+    h = lib.iftrCreateInstance()
+    assert h
+    assert lib.iftrSetOrderedFragmentCapacity(h, -2) == 1
+    assert lib.iftrSetOrderedFragmentCapacity(h, 1 << 40) == 1
+    for n in (-1, 0, 1000):
+        assert lib.iftrSetOrderedFragmentCapacity(h, n) == 0
+    assert lib.iftrSetOrderedFragmentCapacity(None, 0) == 1
+    assert lib.iftrDestroyInstance(h) == 0
