@@ -418,20 +418,22 @@ int reserve_fragments(IfritGbRenderer* h, PassScratch& s, size_t tiles, size_t p
     return IFTR_OK;
 }
 
-void set_fragment_args(const PassScratch& s, PassArgs& a) {
-    a.frags = s.frags.as<uint4>();
-    a.frag_cols = s.frag_cols.as<float4>();
-    a.frag_capacity = s.frag_capacity;
-    a.fwd_tiles = s.fwd_tiles.as<uint4>();
-    a.fwd_pix_end = s.fwd_pix_end.as<uint16_t>();
+ifr::FragArgs fragment_args(const PassScratch& s) {
+    ifr::FragArgs f;
+    f.frags = s.frags.as<uint4>();
+    f.frag_cols = s.frag_cols.as<float4>();
+    f.frag_capacity = s.frag_capacity;
+    f.fwd_tiles = s.fwd_tiles.as<uint4>();
+    f.fwd_pix_end = s.fwd_pix_end.as<uint16_t>();
+    return f;
 }
 
 // Stream work of one pass: clear the per-pass status words, run the pipeline, copy the status
 // back to pinned memory.  Contains no host synchronisation (it is also captured into graphs).
 cudaError_t launch_with_status(PassScratch& s, const PassArgs& a, const ifr::LaunchPlan& plan, cudaStream_t st,
-                               cudaEvent_t* ev) {
+                               cudaEvent_t* ev, const ifr::FragArgs* fa = nullptr) {
     cudaError_t e = cudaMemsetAsync(s.status.p, 0, ifr::ST_PASS_WORDS * sizeof(uint32_t), st);
-    if (e == cudaSuccess) e = ifr::launch_pass(a, plan, st, ev);
+    if (e == cudaSuccess) e = ifr::launch_pass(a, plan, st, ev, fa);
     if (e == cudaSuccess)
         e = cudaMemcpyAsync(s.h_status, s.status.p, ifr::ST_WORDS * sizeof(uint32_t), cudaMemcpyDeviceToHost, st);
     return e;
@@ -644,12 +646,14 @@ int enqueue_pass(IfritGbRenderer* h, std::vector<DrawDev>& draws, int clear) {
     rc = upload_descriptors(h, h->pass, draws, draw_start, views, view_tiles);
     if (rc) return rc;
     PassArgs a = make_args(h->pass, (int)draws.size(), (int)total, 1, T);
-    if (plan.defer_group >= 0 && h->frag_capacity_setting != 0) {
+    ifr::FragArgs fa;
+    const bool defer = plan.defer_group >= 0 && h->frag_capacity_setting != 0;
+    if (defer) {
         rc = reserve_fragments(h, h->pass, (size_t)T, (size_t)W * H);
         if (rc) return rc;
-        set_fragment_args(h->pass, a);
+        fa = fragment_args(h->pass);
     }
-    IFTR_CUDA(h, launch_with_status(h->pass, a, plan, h->stream, h->timing ? h->ev : nullptr));
+    IFTR_CUDA(h, launch_with_status(h->pass, a, plan, h->stream, h->timing ? h->ev : nullptr, defer ? &fa : nullptr));
     h->stats.triangles_in = (uint64_t)total;
     h->pending = 1;
     return IFTR_OK;

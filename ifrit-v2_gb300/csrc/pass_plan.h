@@ -186,8 +186,10 @@ inline bool plan_groups(ViewArgs* v, int n, int* view_tile_start, int sms, int c
         if (plan.ordered[k]) plan.defer_group = plan.defer_group == -1 ? k : -2;
     if (plan.defer_group >= 0) {
         const int S = plan.samples[plan.defer_group];
+        const GroupArgs& dg = plan.groups[plan.defer_group];
         plan.ctas_frag_shade = sms * frag_kernel_occupancy(S, 0);
         plan.ctas_frag_blend = sms * frag_kernel_occupancy(S, 1);
+        plan.ctas_fwd_defer = std::max(1, std::min(dg.tile_end - dg.tile_begin, sms * frag_kernel_occupancy(S, 2)));
     } else {
         plan.defer_group = -1;
     }

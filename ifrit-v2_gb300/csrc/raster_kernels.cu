@@ -25,6 +25,7 @@
 #include <cuda_fp16.h>
 
 #include <algorithm>
+#include <cstring>
 
 #include "raster_kernels.cuh"
 
@@ -1335,6 +1336,59 @@ static __device__ __noinline__ void shade_geom_general(const PassConst& c, const
     *plane_y = st.Y[0];
 }
 
+// Texture lookups of a warp's items with their probes spread over the lanes (anisotropic lookups
+// take 1 to max_aniso probes each): the calling lane's item has `n` probes described by `tp` for
+// draw `di` (n = 0: no lookup); every item adds its probes' results in probe order and, when it has
+// probes, finishes its colour `c`.  wres: 32 float4 of the warp's shared memory.  Whole warp.
+__device__ __forceinline__ void warp_texture_probes(const DrawDev* draws, int di, const TexProbe& tp, int n, float4* wres,
+                                                    float c[4]) {
+    const int lane = threadIdx.x & 31;
+    int incl = n;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int q = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += q;
+    }
+    const int T = __shfl_sync(0xffffffffu, incl, 31);
+    if (T > 0) {
+        const int pre = incl - n;
+        const int packed = tp.lo | (tp.hi << 8) | (tp.n << 16) | (tp.two ? 1 << 24 : 0) | (tp.aniso ? 1 << 25 : 0);
+        float acc[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+        for (int c0 = 0; c0 < T; c0 += 32) {
+            const int j = c0 + lane;
+            int k = 0;  // the item of probe j: the last lane whose first probe is at or before j
+#pragma unroll
+            for (int step = 16; step > 0; step >>= 1)
+                if (__shfl_sync(0xffffffffu, pre, k + step) <= j) k += step;
+            TexProbe q;
+            q.u = __shfl_sync(0xffffffffu, tp.u, k);
+            q.v = __shfl_sync(0xffffffffu, tp.v, k);
+            q.du = __shfl_sync(0xffffffffu, tp.du, k);
+            q.dv = __shfl_sync(0xffffffffu, tp.dv, k);
+            q.t = __shfl_sync(0xffffffffu, tp.t, k);
+            const int qp = __shfl_sync(0xffffffffu, packed, k);
+            const int qd = __shfl_sync(0xffffffffu, di, k);
+            const int i = j - __shfl_sync(0xffffffffu, pre, k);
+            q.lo = qp & 255;
+            q.hi = (qp >> 8) & 255;
+            q.n = (qp >> 16) & 255;
+            q.two = (qp >> 24) & 1;
+            q.aniso = (qp >> 25) & 1;
+            float r[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+            if (j < T) tex_probe(draws[qd], q, i, r);
+            wres[lane] = make_float4(r[0], r[1], r[2], r[3]);
+            __syncwarp();
+            const int qa = max(pre, c0), qb = min(pre + n, c0 + 32);
+            for (int m = qa; m < qb; m++) {
+                const float4 x = wres[m - c0];
+                acc[0] = acc[0] + x.x; acc[1] = acc[1] + x.y; acc[2] = acc[2] + x.z; acc[3] = acc[3] + x.w;
+            }
+            __syncwarp();
+        }
+        if (n > 0) tex_finish(tp, acc, c);
+    }
+}
+
 // Shade stage CTAs: warps are independent (each pulls its own 32-pixel tasks); a CTA only holds the
 // warps' shared-memory slices.
 constexpr int kShadeThreads = 256;
@@ -1469,52 +1523,7 @@ __device__ __forceinline__ void shade_tile(const PassArgs& a, const ViewArgs& v,
             splane[slot][wbase + owner] = plane;
             splane_y[slot][wbase + owner] = plane_y;
         }
-        // The round's texture probes are spread over the lanes (anisotropic lookups take 1 to
-        // max_aniso probes each); every item then adds its probes' results in probe order.
-        int incl = n;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            const int q = __shfl_up_sync(0xffffffffu, incl, o);
-            if (lane >= o) incl += q;
-        }
-        const int T = __shfl_sync(0xffffffffu, incl, 31);
-        if (T > 0) {
-            const int pre = incl - n;
-            const int packed = tp.lo | (tp.hi << 8) | (tp.n << 16) | (tp.two ? 1 << 24 : 0) | (tp.aniso ? 1 << 25 : 0);
-            float acc[4] = {0.0f, 0.0f, 0.0f, 0.0f};
-            for (int c0 = 0; c0 < T; c0 += 32) {
-                const int j = c0 + lane;
-                int k = 0;  // the item of probe j: the last lane whose first probe is at or before j
-#pragma unroll
-                for (int step = 16; step > 0; step >>= 1)
-                    if (__shfl_sync(0xffffffffu, pre, k + step) <= j) k += step;
-                TexProbe q;
-                q.u = __shfl_sync(0xffffffffu, tp.u, k);
-                q.v = __shfl_sync(0xffffffffu, tp.v, k);
-                q.du = __shfl_sync(0xffffffffu, tp.du, k);
-                q.dv = __shfl_sync(0xffffffffu, tp.dv, k);
-                q.t = __shfl_sync(0xffffffffu, tp.t, k);
-                const int qp = __shfl_sync(0xffffffffu, packed, k);
-                const int qd = __shfl_sync(0xffffffffu, di, k);
-                const int i = j - __shfl_sync(0xffffffffu, pre, k);
-                q.lo = qp & 255;
-                q.hi = (qp >> 8) & 255;
-                q.n = (qp >> 16) & 255;
-                q.two = (qp >> 24) & 1;
-                q.aniso = (qp >> 25) & 1;
-                float r[4] = {0.0f, 0.0f, 0.0f, 0.0f};
-                if (j < T) tex_probe(a.draws[qd], q, i, r);
-                wres[lane] = make_float4(r[0], r[1], r[2], r[3]);
-                __syncwarp();
-                const int qa = max(pre, c0), qb = min(pre + n, c0 + 32);
-                for (int m = qa; m < qb; m++) {
-                    const float4 x = wres[m - c0];
-                    acc[0] = acc[0] + x.x; acc[1] = acc[1] + x.y; acc[2] = acc[2] + x.z; acc[3] = acc[3] + x.w;
-                }
-                __syncwarp();
-            }
-            if (n > 0) tex_finish(tp, acc, c);
-        }
+        warp_texture_probes(a.draws, di, tp, n, wres, c);
         if (b < total) scol[slot][wbase + owner] = make_float4(c[0], c[1], c[2], c[3]);
     }
     __syncwarp();
@@ -1656,8 +1665,8 @@ __device__ __forceinline__ int tile_lane(int lx, int ly) {
     return ((((ly >> 1) * (TS / 2)) + (lx >> 1)) << 2) | ((ly & 1) << 1) | (lx & 1);
 }
 
-// Shades fragment f = (entry, sample mask) at pixel (px, py) and writes or blends it into the
-// per-sample colours of the calling thread.
+// Shades fragment f = (entry, sample mask | draw << 16) at pixel (px, py) and writes or blends it
+// into the per-sample colours of the calling thread.
 template <int S>
 __device__ __forceinline__ void apply_fragment(const PassArgs& a, const ViewArgs& v, int px, int py, float4* scol,
                                                int2 f) {
@@ -1665,8 +1674,8 @@ __device__ __forceinline__ void apply_fragment(const PassArgs& a, const ViewArgs
     float c[4];
     RecordPlane pl;
     shade_uncached(a, v.c, f.x, px, py, c, &pl);
-    const DrawDev& d = a.draws[record_draw(a, f.x >> 3)];
-    const unsigned mask = (unsigned)f.y;
+    const DrawDev& d = a.draws[(unsigned)f.y >> 16];
+    const unsigned mask = (unsigned)f.y & 0xffffu;
 #pragma unroll
     for (int k = 0; k < S; k++) {
         if (!(mask & (1u << k))) continue;
@@ -1688,6 +1697,20 @@ __device__ __noinline__ void apply_fragments(const PassArgs& a, const ViewArgs& 
 }
 
 
+// A pixel's per-sample depths (16-byte stores when S is a multiple of 4: the target is then
+// 16-byte aligned).
+template <int S>
+__device__ __forceinline__ void store_depth(float* dp, const float* dep) {
+    if constexpr (S % 4 == 0) {
+#pragma unroll
+        for (int k = 0; k < S; k += 4)
+            reinterpret_cast<float4*>(dp)[k / 4] = make_float4(dep[k], dep[k + 1], dep[k + 2], dep[k + 3]);
+    } else {
+#pragma unroll
+        for (int k = 0; k < S; k++) dp[k] = dep[k];
+    }
+}
+
 // Starting colours of the calling thread's samples: the prefix's per-sample colours handed off by
 // the shade stage, or the background.
 template <int S>
@@ -1700,20 +1723,23 @@ __device__ __forceinline__ void start_colours(const ViewArgs& v, float4* scol, i
                                                   : make_float4(bg[0], bg[1], bg[2], bg[3]);
 }
 
-template <int S>
-__device__ __forceinline__ void forward_tile(const PassArgs& a, const ViewArgs& v, int vi, int gtile, FwdRecords& rec,
-                                             float4* scol, uint32_t* list, int2* frags, uint32_t* cand,
-                                             bool after_raster, BulkState& bs) {
+// DEFER: the tile's fragments go to the fragment kernels (fa set); the per-sample colours a tile
+// finished here needs live in the tile's rows of the hand-off buffer (exclusive to the tile), not in
+// shared memory.
+template <int S, bool DEFER>
+__device__ __forceinline__ void forward_tile(const PassArgs& a, const FragArgs& fa, const ViewArgs& v, int vi, int gtile,
+                                             FwdRecords& rec, float4* scol_smem, uint32_t* list, int2* frags,
+                                             uint32_t* cand, bool after_raster, BulkState& bs) {
     constexpr int TS = 16, NT = kFwdThreads;
     // after the raster and shade stages the shade stage has finished the tiles without ordered
     // entries (uniform over the CTA)
     if (after_raster && a.tile_cursor[gtile] == 0u) return;
     const int ltile = gtile - v.tile_start;
-    // With deferred shading (a.frags set) the tile's fragments usually go to the fragment kernels
-    // and the per-sample colours are only loaded where fragments are applied here.  Otherwise the
-    // prefix's per-sample colours of the tile (S x 256 float4, contiguous in the tile-major
-    // hand-off) come in by one bulk copy (TMA) that overlaps the gathering and sorting below.
-    const bool defer = a.frags != nullptr;
+    // Without deferral the prefix's per-sample colours of the tile (S x 256 float4, contiguous in
+    // the tile-major hand-off) come in by one bulk copy (TMA) that overlaps the gathering and
+    // sorting below.
+    constexpr bool defer = DEFER;
+    float4* scol = DEFER ? v.sample_colors + (size_t)ltile * S * NT : scol_smem;
     const bool bulk = after_raster && bs.ok && !defer;
     if (bulk && threadIdx.x == 0)
         bulk_load(scol, v.sample_colors + (size_t)ltile * S * NT, (uint32_t)(sizeof(float4) * S * NT), bs.bar);
@@ -1735,20 +1761,41 @@ __device__ __forceinline__ void forward_tile(const PassArgs& a, const ViewArgs& 
     } else {
         bg[0] = bg[1] = bg[2] = bg[3] = 0.0f;
     }
+    if (after_raster) {
+        // the prefix's per-sample state as the shade stage left it: colour in the per-sample
+        // scratch, depth and primitive id in the outputs
+        int ent[S];
+        if (!inpix) {
 #pragma unroll
-    for (int k = 0; k < S; k++) {
-        if (after_raster) {
-            // the prefix's per-sample state as the shade stage left it: colour in the per-sample
-            // scratch, depth and primitive id in the outputs
-            const int ent = inpix ? v.entries[pix * S + k] : -1;
-            dep[k] = inpix ? v.depth[pix * S + k] : 0.0f;
-            vid[k] = ent < 0 ? -1 : (ent >> 3) - v.first_tri;
+            for (int k = 0; k < S; k++) {
+                ent[k] = -1;
+                dep[k] = 0.0f;
+            }
+        } else if constexpr (S % 4 == 0) {
+#pragma unroll
+            for (int k = 0; k < S; k += 4) {
+                const int4 q = reinterpret_cast<const int4*>(v.entries + pix * S)[k / 4];
+                const float4 z = reinterpret_cast<const float4*>(v.depth + pix * S)[k / 4];
+                ent[k] = q.x; ent[k + 1] = q.y; ent[k + 2] = q.z; ent[k + 3] = q.w;
+                dep[k] = z.x; dep[k + 1] = z.y; dep[k + 2] = z.z; dep[k + 3] = z.w;
+            }
         } else {
+#pragma unroll
+            for (int k = 0; k < S; k++) {
+                ent[k] = v.entries[pix * S + k];
+                dep[k] = v.depth[pix * S + k];
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < S; k++) vid[k] = ent[k] < 0 ? -1 : (ent[k] >> 3) - v.first_tri;
+    } else {
+#pragma unroll
+        for (int k = 0; k < S; k++) {
             dep[k] = v.clear ? v.clear_depth : (inpix ? v.depth[pix * S + k] : 0.0f);
             vid[k] = -1;
         }
     }
-    bool have_cols = bulk;  // scol holds this thread's starting colours
+    bool have_cols = bulk || (defer && after_raster);  // scol holds this thread's starting colours
     if (!defer && !bulk) {
         start_colours<S>(v, scol, ltile, after_raster, bg);
         have_cols = true;
@@ -1784,8 +1831,14 @@ __device__ __forceinline__ void forward_tile(const PassArgs& a, const ViewArgs& 
     if (n <= NT) {
         const uint32_t e = tid < n ? list[tid] : 0u;
         int rank = 0;
-        if (tid < n)
-            for (int j = 0; j < n; j++) rank += list[j] < e;
+        if (tid < n) {
+            const uint4* l4 = reinterpret_cast<const uint4*>(list);
+            for (int j = 0; j < (n >> 2); j++) {
+                const uint4 q = l4[j];
+                rank += (int)(q.x < e) + (int)(q.y < e) + (int)(q.z < e) + (int)(q.w < e);
+            }
+            for (int j = n & ~3; j < n; j++) rank += list[j] < e;
+        }
         __syncthreads();
         if (tid < n) list[rank] = e;
         __syncthreads();
@@ -1911,7 +1964,7 @@ __device__ __forceinline__ void forward_tile(const PassArgs& a, const ViewArgs& 
                         nfrag = 0;
                         flushed = true;
                     }
-                    frags[nfrag * NT + tid] = make_int2(e, (int)mask);
+                    frags[nfrag * NT + tid] = make_int2(e, (int)(mask | ((unsigned)rec.draw[r] << 16)));
                     nfrag++;
                 }
             }
@@ -1947,9 +2000,9 @@ __device__ __forceinline__ void forward_tile(const PassArgs& a, const ViewArgs& 
                 uint32_t fbase = 0;
                 if (total > 0) {
                     fbase = atomicAdd(a.status + ST_FRAGS, total);
-                    if ((unsigned long long)fbase + total <= a.frag_capacity) {
+                    if ((unsigned long long)fbase + total <= fa.frag_capacity) {
                         slot = (int)atomicAdd(a.status + ST_FWD_TILES, 1u);
-                        a.fwd_tiles[slot] = make_uint4((uint32_t)gtile, fbase, (uint32_t)vi, after_raster ? 1u : 0u);
+                        fa.fwd_tiles[slot] = make_uint4((uint32_t)gtile, fbase, (uint32_t)vi, after_raster ? 1u : 0u);
                     } else {  // later allocations fail too: the fragments below this one are all written
                         atomicMax(a.status + ST_FRAG_FAIL, 0xFFFFFFFFu - fbase);
                         const unsigned long long want = (unsigned long long)fbase + total;
@@ -1962,16 +2015,15 @@ __device__ __forceinline__ void forward_tile(const PassArgs& a, const ViewArgs& 
             __syncthreads();
             const int slot = s_slot;
             if (slot >= 0) {
-                uint4* out = a.frags + s_base + pre;
+                uint4* out = fa.frags + s_base + pre;
                 for (int i = 0; i < nfrag; i++) {
                     const int2 f = frags[i * NT + tid];
-                    out[i] = make_uint4((uint32_t)f.x, (uint32_t)px | ((uint32_t)py << 16), (uint32_t)f.y, 0u);
+                    out[i] = make_uint4((uint32_t)f.x, (uint32_t)px | ((uint32_t)py << 16), (uint32_t)f.y & 0xffffu,
+                                        (uint32_t)f.y >> 16);
                 }
-                a.fwd_pix_end[(size_t)slot * NT + tid] = (uint16_t)(pre + nfrag);
+                fa.fwd_pix_end[(size_t)slot * NT + tid] = (uint16_t)(pre + nfrag);
                 if (inpix) {
-                    float* dp = v.depth + pix * S;
-#pragma unroll
-                    for (int k = 0; k < S; k++) dp[k] = dep[k];
+                    store_depth<S>(v.depth + pix * S, dep);
                     if (v.vis) {
                         int* vp = v.vis + pix * S;
 #pragma unroll
@@ -2004,9 +2056,7 @@ __device__ __forceinline__ void forward_tile(const PassArgs& a, const ViewArgs& 
     const float invS = 1.0f / (float)S;
     acc[0] = acc[0] * invS; acc[1] = acc[1] * invS; acc[2] = acc[2] * invS; acc[3] = acc[3] * invS;
     encode_color(v, pix, acc);
-    float* dp = v.depth + pix * S;
-#pragma unroll
-    for (int k = 0; k < S; k++) dp[k] = dep[k];
+    store_depth<S>(v.depth + pix * S, dep);
     if (v.vis) {
         int* vp = v.vis + pix * S;
 #pragma unroll
@@ -2014,18 +2064,21 @@ __device__ __forceinline__ void forward_tile(const PassArgs& a, const ViewArgs& 
     }
 }
 
-template <int S>
+template <int S, bool DEFER>
 size_t forward_smem_bytes() {
-    return sizeof(FwdRecords) + sizeof(float4) * S * kFwdThreads + sizeof(uint32_t) * kOrderedCap +
+    return sizeof(FwdRecords) + (DEFER ? 0 : sizeof(float4) * S * kFwdThreads) + sizeof(uint32_t) * kOrderedCap +
            sizeof(int2) * kFwdFrags * kFwdThreads + sizeof(uint32_t) * kFwdThreads * (kFwdThreads / 32);
 }
 
-template <int S>
-__global__ void __launch_bounds__(kFwdThreads) forward_kernel(PassArgs a, GroupArgs g, int qslot, int after_raster) {
+// Two CTAs per SM (128 registers): three, at 80 registers, spilled and measured slower.
+template <int S, bool DEFER>
+__global__ void __launch_bounds__(kFwdThreads, 2) forward_kernel(PassArgs a, FragArgs fa, GroupArgs g,
+                                                                             int qslot, int after_raster) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     FwdRecords& rec = *reinterpret_cast<FwdRecords*>(smem_raw);
-    float4* scol = reinterpret_cast<float4*>(smem_raw + sizeof(FwdRecords));  // [S][256]
-    uint32_t* list = reinterpret_cast<uint32_t*>(smem_raw + sizeof(FwdRecords) + sizeof(float4) * S * kFwdThreads);
+    float4* scol = reinterpret_cast<float4*>(smem_raw + sizeof(FwdRecords));  // [S][256] (not DEFER)
+    uint32_t* list =
+        reinterpret_cast<uint32_t*>(smem_raw + sizeof(FwdRecords) + (DEFER ? 0 : sizeof(float4) * S * kFwdThreads));
     int2* frags = reinterpret_cast<int2*>(list + kOrderedCap);  // [kFwdFrags][256]
     uint32_t* cand = reinterpret_cast<uint32_t*>(frags + kFwdFrags * kFwdThreads);  // [8][256]
     __shared__ ViewArgs sv;
@@ -2042,7 +2095,7 @@ __global__ void __launch_bounds__(kFwdThreads) forward_kernel(PassArgs a, GroupA
     }
     __syncthreads();
     while (next_tile<kFwdThreads>(a, g, qslot, sv, s_tile, s_view))
-        forward_tile<S>(a, sv, s_view, s_tile, rec, scol, list, frags, cand, after_raster != 0, bs);
+        forward_tile<S, DEFER>(a, fa, sv, s_view, s_tile, rec, scol, list, frags, cand, after_raster != 0, bs);
     if (bs.pending && threadIdx.x == 0) mbar_wait(&s_bar, (bs.phase - 1) & 1u);  // a copy that did not land in time
 }
 
@@ -2053,85 +2106,205 @@ __global__ void __launch_bounds__(kFwdThreads) forward_kernel(PassArgs a, GroupA
 // then blended per pixel in submission order.
 
 // Fragments below this count were written by tiles whose allocation fitted.
-__device__ __forceinline__ uint32_t deferred_fragments(const PassArgs& a) {
+__device__ __forceinline__ uint32_t deferred_fragments(const PassArgs& a, const FragArgs& fa) {
     const uint32_t fail = a.status[ST_FRAG_FAIL];
     const uint32_t n = fail ? 0xFFFFFFFFu - fail : a.status[ST_FRAGS];
-    return min(n, a.frag_capacity);
+    return min(n, fa.frag_capacity);
 }
 
-__global__ void __launch_bounds__(256) frag_shade_kernel(PassArgs a) {
-    const uint32_t n = deferred_fragments(a);
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        const uint4 f = a.frags[i];
-        const DrawDev& d = a.draws[record_draw(a, (int)(f.x >> 3))];
-        float c[4];
-        RecordPlane pl;
-        shade_uncached(a, a.views[d.view].c, (int)f.x, (int)(f.y & 0xffffu), (int)(f.y >> 16), c, &pl);
-        a.frag_cols[i] = make_float4(c[0], c[1], c[2], c[3]);
+// Warps take 32 fragments at a time: set-up from the triangle record where there is one, the
+// vertex attributes from the attribute record, then the texture probes of all 32 spread over the
+// lanes (as the shade stage does).
+constexpr int kFragShadeThreads = 256;
+
+__global__ void __launch_bounds__(kFragShadeThreads, 4) frag_shade_kernel(PassArgs a, FragArgs fa) {
+    __shared__ float4 s_res[kFragShadeThreads / 32][32];
+    const uint32_t n = deferred_fragments(a, fa);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const uint32_t stride = gridDim.x * kFragShadeThreads;
+    for (uint32_t base = (blockIdx.x * (kFragShadeThreads / 32) + warp) * 32; base < n; base += stride) {
+        const uint32_t i = base + lane;
+        int di = 0, np = 0;
+        float c[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+        TexProbe tp;
+        tp.u = tp.v = tp.du = tp.dv = tp.t = 0.0f;
+        tp.lo = tp.hi = tp.n = 0;
+        tp.two = tp.aniso = false;
+        if (i < n) {
+            const uint4 f = fa.frags[i];
+            const int g = (int)(f.x >> 3), sub = (int)(f.x & 7u);
+            const int px = (int)(f.y & 0xffffu), py = (int)(f.y >> 16);
+            const TriRecord* rp = a.records + g;
+            const int4 q1 = __ldg(reinterpret_cast<const int4*>(rp) + 1);  // X2, Y2, flags, draw
+            di = q1.w;
+            const DrawDev& d = a.draws[di];
+            const PassConst& pc = a.views[d.view].c;
+            const int t = g - __ldg(a.draw_start + di);
+            const bool from_record = sub == 0 && (q1.z & REC_VALID);
+            ShadeGeom geo;
+            float4 plane;
+            int plane_y;
+            if (from_record && d.polygon_mode == POLY_FILL) {
+                shade_geom_record(rp, q1, geo, plane, plane_y);
+            } else {  // through memory on this rare path only
+                ShadeGeom tg;
+                float4 tpl;
+                int tpy;
+                shade_geom_general(pc, d, a.records, g, t, sub, &tg, &tpl, &tpy);
+                geo = tg;
+            }
+            (void)plane;
+            (void)plane_y;
+            float a0[4], a1[4], a2[4];
+            if (from_record && a.attrs && d.shading != SHADE_PRIMID && d.attr_count > 0) {
+                const float4 r0 = __ldg(&a.attrs[g].a[0]), r1 = __ldg(&a.attrs[g].a[1]), r2 = __ldg(&a.attrs[g].a[2]);
+                a0[0] = r0.x; a0[1] = r0.y; a0[2] = r0.z; a0[3] = r0.w;
+                a1[0] = r1.x; a1[1] = r1.y; a1[2] = r1.z; a1[3] = r1.w;
+                a2[0] = r2.x; a2[1] = r2.y; a2[2] = r2.z; a2[3] = r2.w;
+            } else if (d.shading != SHADE_PRIMID) {
+                fetch_attrs(d, t, a0, a1, a2);
+            } else {
+#pragma unroll
+                for (int k = 0; k < 4; k++) a0[k] = a1[k] = a2[k] = 0.0f;
+            }
+            if (shade_prepare_attrs(pc, d, geo, t, sub, px, py, a0, a1, a2, c, tp)) np = tp.n;
+        }
+        warp_texture_probes(a.draws, di, tp, np, s_res[warp], c);
+        if (i < n) fa.frag_cols[i] = make_float4(c[0], c[1], c[2], c[3]);
     }
 }
 
 // One deferred tile per CTA iteration, one pixel per thread: the starting colours (the prefix's
 // hand-off or the background), the pixel's fragments applied in submission order, then the resolve.
+// The hand-off of the CTA's next tile (S x 256 float4, contiguous) comes into the other half of a
+// double buffer by one bulk copy (TMA) while the current tile is blended; each thread updates its
+// own samples in place.  A wait that gives up reports status bit ST_STICKY & 4 and the CTA reads
+// the hand-off from memory from then on.
 template <int S>
-__global__ void __launch_bounds__(kFwdThreads) frag_blend_kernel(PassArgs a) {
+constexpr int blend_min_blocks() { return S <= 4 ? 4 : S == 8 ? 3 : 1; }
+
+template <int S>
+constexpr size_t blend_smem_bytes() { return 2 * sizeof(float4) * S * kFwdThreads; }
+
+template <int S>
+__global__ void __launch_bounds__(kFwdThreads, blend_min_blocks<S>()) frag_blend_kernel(PassArgs a, FragArgs fa) {
     constexpr int TS = 16, NT = kFwdThreads;
-    const uint32_t ntiles = a.status[ST_FWD_TILES];
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    float4* buf = reinterpret_cast<float4*>(smem_raw);  // [2][S][NT]
+    __shared__ __align__(8) uint64_t s_bar[2];
     const int tid = threadIdx.x;
+    const uint32_t ntiles = a.status[ST_FWD_TILES];
+    if (tid == 0) {
+        mbar_init(&s_bar[0], 1);
+        mbar_init(&s_bar[1], 1);
+    }
+    __syncthreads();
     int lx, ly;
     tile_pixel<TS>(tid, lx, ly);
-    for (uint32_t slot = blockIdx.x; slot < ntiles; slot += gridDim.x) {
-        const uint4 t = a.fwd_tiles[slot];  // global tile, first fragment, view, hand-off flag
+    bool use_bulk = true;          // the same in every thread
+    bool inflight[2] = {false, false};
+    uint32_t parity[2] = {0u, 0u};  // parity of each buffer's next completed phase
+    int stuck = -1;                 // buffer whose copy a wait gave up on
+    uint32_t slot = blockIdx.x;
+    if (slot < ntiles) {
+        const uint4 t = fa.fwd_tiles[slot];
+        if (t.w) {
+            if (tid == 0) {
+                const ViewArgs& v = a.views[t.z];
+                bulk_load(buf, v.sample_colors + (size_t)((int)t.x - v.tile_start) * S * NT,
+                          (uint32_t)(sizeof(float4) * S * NT), &s_bar[0]);
+            }
+            inflight[0] = true;
+        }
+    }
+    for (int b = 0; slot < ntiles; slot += gridDim.x, b ^= 1) {
+        // the next tile's hand-off into the other buffer, free since the barrier that ended the
+        // previous iteration
+        const uint32_t next = slot + gridDim.x;
+        if (next < ntiles && use_bulk) {
+            const uint4 tn = fa.fwd_tiles[next];
+            if (tn.w) {
+                if (tid == 0) {
+                    const ViewArgs& vn = a.views[tn.z];
+                    bulk_load(buf + (b ^ 1) * S * NT, vn.sample_colors + (size_t)((int)tn.x - vn.tile_start) * S * NT,
+                              (uint32_t)(sizeof(float4) * S * NT), &s_bar[b ^ 1]);
+                }
+                inflight[b ^ 1] = true;
+            }
+        }
+        const uint4 t = fa.fwd_tiles[slot];  // global tile, first fragment, view, hand-off flag
         const ViewArgs& v = a.views[t.z];
         const int ltile = (int)t.x - v.tile_start;
         const int tx = ltile % v.c.tiles_x, ty = ltile / v.c.tiles_x;
         const int px = tx * TS + lx, py = ty * TS + ly;
-        if (px >= v.c.W || py >= v.c.H) continue;
+        const bool inpix = px < v.c.W && py < v.c.H;
         const size_t pix = (size_t)py * v.c.W + px;
-        float col[S][4];
-        if (t.w) {
-#pragma unroll
-            for (int k = 0; k < S; k++) {
-                const float4 q = v.sample_colors[((size_t)ltile * S + k) * NT + tid];
-                col[k][0] = q.x; col[k][1] = q.y; col[k][2] = q.z; col[k][3] = q.w;
-            }
-        } else {
-            float bg[4];
-            if (v.clear) {
-                bg[0] = v.clear_color[0]; bg[1] = v.clear_color[1]; bg[2] = v.clear_color[2]; bg[3] = v.clear_color[3];
-            } else {
-                decode_color(v, pix, bg);
-            }
-#pragma unroll
-            for (int k = 0; k < S; k++) {
-                col[k][0] = bg[0]; col[k][1] = bg[1]; col[k][2] = bg[2]; col[k][3] = bg[3];
+        float4* col = buf + b * S * NT + tid;  // this thread's samples, stride NT
+        bool have = false;
+        if (inflight[b]) {
+            const bool ok = mbar_wait(&s_bar[b], parity[b]);
+            parity[b] ^= 1u;
+            inflight[b] = false;
+            if (__syncthreads_and(ok)) {
+                have = true;
+            } else {  // report, and read the hand-off from memory from now on
+                if (tid == 0) atomicOr(a.status + ST_STICKY, 4u);
+                use_bulk = false;
+                stuck = b;
             }
         }
-        const uint16_t* pe = a.fwd_pix_end + (size_t)slot * NT;
-        const uint32_t f0 = t.y + (tid ? pe[tid - 1] : 0u), f1 = t.y + pe[tid];
-        for (uint32_t f = f0; f < f1; f++) {
-            const uint4 r = a.frags[f];
-            const float4 q = a.frag_cols[f];
-            const float c[4] = {q.x, q.y, q.z, q.w};
-            const DrawDev& d = a.draws[record_draw(a, (int)(r.x >> 3))];
+        if (inpix) {
+            if (!have) {
+                if (t.w) {
 #pragma unroll
-            for (int k = 0; k < S; k++) {
-                if (!(r.z & (1u << k))) continue;
-                if (d.blend_enable) {
-                    blend_into(d, c, col[k]);
+                    for (int k = 0; k < S; k++) col[k * NT] = v.sample_colors[((size_t)ltile * S + k) * NT + tid];
                 } else {
-                    col[k][0] = c[0]; col[k][1] = c[1]; col[k][2] = c[2]; col[k][3] = c[3];
+                    float bg[4];
+                    if (v.clear) {
+                        bg[0] = v.clear_color[0]; bg[1] = v.clear_color[1]; bg[2] = v.clear_color[2]; bg[3] = v.clear_color[3];
+                    } else {
+                        decode_color(v, pix, bg);
+                    }
+#pragma unroll
+                    for (int k = 0; k < S; k++) col[k * NT] = make_float4(bg[0], bg[1], bg[2], bg[3]);
                 }
             }
-        }
-        float acc[4] = {col[0][0], col[0][1], col[0][2], col[0][3]};
+            const uint16_t* pe = fa.fwd_pix_end + (size_t)slot * NT;
+            const uint32_t f0 = t.y + (tid ? pe[tid - 1] : 0u), f1 = t.y + pe[tid];
+            for (uint32_t f = f0; f < f1; f++) {
+                const uint4 r = fa.frags[f];  // entry, pixel, sample mask, draw
+                const float4 q = fa.frag_cols[f];
+                const float c[4] = {q.x, q.y, q.z, q.w};
+                const DrawDev& d = a.draws[r.w];
+                for (uint32_t m = r.z; m; m &= m - 1) {  // the covered samples, one copy of the blend code
+                    const int k = __ffs(m) - 1;
+                    if (d.blend_enable) {
+                        const float4 o = col[k * NT];
+                        float dst[4] = {o.x, o.y, o.z, o.w};
+                        blend_into(d, c, dst);
+                        col[k * NT] = make_float4(dst[0], dst[1], dst[2], dst[3]);
+                    } else {
+                        col[k * NT] = q;
+                    }
+                }
+            }
+            float4 q0 = col[0];
+            float acc[4] = {q0.x, q0.y, q0.z, q0.w};
 #pragma unroll
-        for (int k = 1; k < S; k++) {
-            acc[0] = acc[0] + col[k][0]; acc[1] = acc[1] + col[k][1]; acc[2] = acc[2] + col[k][2]; acc[3] = acc[3] + col[k][3];
+            for (int k = 1; k < S; k++) {
+                const float4 q = col[k * NT];
+                acc[0] = acc[0] + q.x; acc[1] = acc[1] + q.y; acc[2] = acc[2] + q.z; acc[3] = acc[3] + q.w;
+            }
+            const float invS = 1.0f / (float)S;
+            acc[0] = acc[0] * invS; acc[1] = acc[1] * invS; acc[2] = acc[2] * invS; acc[3] = acc[3] * invS;
+            encode_color(v, pix, acc);
         }
-        const float invS = 1.0f / (float)S;
-        acc[0] = acc[0] * invS; acc[1] = acc[1] * invS; acc[2] = acc[2] * invS; acc[3] = acc[3] * invS;
-        encode_color(v, pix, acc);
+        __syncthreads();
+    }
+    if (tid == 0) {  // copies left in flight: a prefetch past a failed wait, or the copy given up on
+        for (int b = 0; b < 2; b++)
+            if (inflight[b]) mbar_wait(&s_bar[b], parity[b]);
+        if (stuck >= 0) mbar_wait(&s_bar[stuck], parity[stuck] ^ 1u);
     }
 }
 
@@ -2463,12 +2636,12 @@ cudaError_t configure_deferred() {
     return e;
 }
 
-template <int S>
+template <int S, bool DEFER>
 cudaError_t configure_forward() {
     static bool done = false;
     if (done) return cudaSuccess;
-    cudaError_t e = cudaFuncSetAttribute(forward_kernel<S>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)forward_smem_bytes<S>());
+    cudaError_t e = cudaFuncSetAttribute(forward_kernel<S, DEFER>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)forward_smem_bytes<S, DEFER>());
     if (e == cudaSuccess) done = true;
     return e;
 }
@@ -2482,28 +2655,51 @@ cudaError_t launch_deferred(const PassArgs& a, const GroupArgs& g, int ctas, cud
     return cudaSuccess;
 }
 
-template <int S>
-cudaError_t launch_forward(const PassArgs& a, const GroupArgs& g, int ctas, cudaStream_t stream, int qslot) {
-    cudaError_t e = configure_forward<S>();
+template <int S, bool DEFER>
+cudaError_t launch_forward_form(const PassArgs& a, const FragArgs& fa, const GroupArgs& g, int ctas,
+                                cudaStream_t stream, int qslot) {
+    cudaError_t e = configure_forward<S, DEFER>();
     if (e != cudaSuccess) return e;
-    forward_kernel<S><<<ctas, kFwdThreads, forward_smem_bytes<S>(), stream>>>(a, g, qslot, qslot % 3 == 2);
+    forward_kernel<S, DEFER><<<ctas, kFwdThreads, forward_smem_bytes<S, DEFER>(), stream>>>(a, fa, g, qslot,
+                                                                                           qslot % 3 == 2);
     return cudaSuccess;
 }
 
 template <int S>
-cudaError_t launch_frag_kernels(const PassArgs& a, int ctas_shade, int ctas_blend, cudaStream_t stream) {
-    frag_shade_kernel<<<ctas_shade, 256, 0, stream>>>(a);
-    frag_blend_kernel<S><<<ctas_blend, kFwdThreads, 0, stream>>>(a);
+cudaError_t launch_forward(const PassArgs& a, const FragArgs& fa, const GroupArgs& g, int ctas, cudaStream_t stream,
+                           int qslot) {
+    return fa.frags ? launch_forward_form<S, true>(a, fa, g, ctas, stream, qslot)
+                    : launch_forward_form<S, false>(a, fa, g, ctas, stream, qslot);
+}
+
+template <int S>
+cudaError_t configure_blend() {
+    static bool done = false;
+    if (done) return cudaSuccess;
+    cudaError_t e = cudaFuncSetAttribute(frag_blend_kernel<S>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)blend_smem_bytes<S>());
+    if (e == cudaSuccess) done = true;
+    return e;
+}
+
+template <int S>
+cudaError_t launch_frag_kernels(const PassArgs& a, const FragArgs& fa, int ctas_shade, int ctas_blend,
+                                cudaStream_t stream) {
+    cudaError_t e = configure_blend<S>();
+    if (e != cudaSuccess) return e;
+    frag_shade_kernel<<<ctas_shade, kFragShadeThreads, 0, stream>>>(a, fa);
+    frag_blend_kernel<S><<<ctas_blend, kFwdThreads, blend_smem_bytes<S>(), stream>>>(a, fa);
     return cudaSuccess;
 }
 
-cudaError_t launch_group_frags(const PassArgs& a, int S, int ctas_shade, int ctas_blend, cudaStream_t stream) {
+cudaError_t launch_group_frags(const PassArgs& a, const FragArgs& fa, int S, int ctas_shade, int ctas_blend,
+                               cudaStream_t stream) {
     switch (S) {
-    case 1: return launch_frag_kernels<1>(a, ctas_shade, ctas_blend, stream);
-    case 2: return launch_frag_kernels<2>(a, ctas_shade, ctas_blend, stream);
-    case 4: return launch_frag_kernels<4>(a, ctas_shade, ctas_blend, stream);
-    case 8: return launch_frag_kernels<8>(a, ctas_shade, ctas_blend, stream);
-    case 16: return launch_frag_kernels<16>(a, ctas_shade, ctas_blend, stream);
+    case 1: return launch_frag_kernels<1>(a, fa, ctas_shade, ctas_blend, stream);
+    case 2: return launch_frag_kernels<2>(a, fa, ctas_shade, ctas_blend, stream);
+    case 4: return launch_frag_kernels<4>(a, fa, ctas_shade, ctas_blend, stream);
+    case 8: return launch_frag_kernels<8>(a, fa, ctas_shade, ctas_blend, stream);
+    case 16: return launch_frag_kernels<16>(a, fa, ctas_shade, ctas_blend, stream);
     default: return cudaErrorInvalidValue;
     }
 }
@@ -2530,15 +2726,15 @@ cudaError_t launch_group_stage(const PassArgs& a, const GroupArgs& g, int S, int
 
 // The ordered stage of a group; `second` when it follows the group's raster stage (its queue
 // counter is then the group's second one).
-cudaError_t launch_group_forward(const PassArgs& a, const GroupArgs& g, int S, int ctas, cudaStream_t stream,
-                                 bool second) {
+cudaError_t launch_group_forward(const PassArgs& a, const FragArgs& fa, const GroupArgs& g, int S, int ctas,
+                                 cudaStream_t stream, bool second) {
     const int q = 3 * g.queue + (second ? 2 : 0);
     switch (S) {
-    case 1: return launch_forward<1>(a, g, ctas, stream, q);
-    case 2: return launch_forward<2>(a, g, ctas, stream, q);
-    case 4: return launch_forward<4>(a, g, ctas, stream, q);
-    case 8: return launch_forward<8>(a, g, ctas, stream, q);
-    case 16: return launch_forward<16>(a, g, ctas, stream, q);
+    case 1: return launch_forward<1>(a, fa, g, ctas, stream, q);
+    case 2: return launch_forward<2>(a, fa, g, ctas, stream, q);
+    case 4: return launch_forward<4>(a, fa, g, ctas, stream, q);
+    case 8: return launch_forward<8>(a, fa, g, ctas, stream, q);
+    case 16: return launch_forward<16>(a, fa, g, ctas, stream, q);
     default: return cudaErrorInvalidValue;
     }
 }
@@ -2557,20 +2753,29 @@ int deferred_occupancy(int stage) {
                       : occupancy_of(shade_kernel<S, TS>, kShadeThreads, 0);
 }
 
-template <int S>
+template <int S, bool DEFER = false>
 int forward_occupancy() {
-    configure_forward<S>();
-    return occupancy_of(forward_kernel<S>, kFwdThreads, forward_smem_bytes<S>());
+    configure_forward<S, DEFER>();
+    return occupancy_of(forward_kernel<S, DEFER>, kFwdThreads, forward_smem_bytes<S, DEFER>());
 }
 
 int frag_kernel_occupancy(int S, int stage) {
-    if (stage == 0) return occupancy_of(frag_shade_kernel, 256, 0);
+    if (stage == 0) return occupancy_of(frag_shade_kernel, kFragShadeThreads, 0);
+    if (stage == 2) {
+        switch (S) {
+        case 1: return forward_occupancy<1, true>();
+        case 2: return forward_occupancy<2, true>();
+        case 4: return forward_occupancy<4, true>();
+        case 8: return forward_occupancy<8, true>();
+        default: return forward_occupancy<16, true>();
+        }
+    }
     switch (S) {
-    case 1: return occupancy_of(frag_blend_kernel<1>, kFwdThreads, 0);
-    case 2: return occupancy_of(frag_blend_kernel<2>, kFwdThreads, 0);
-    case 4: return occupancy_of(frag_blend_kernel<4>, kFwdThreads, 0);
-    case 8: return occupancy_of(frag_blend_kernel<8>, kFwdThreads, 0);
-    default: return occupancy_of(frag_blend_kernel<16>, kFwdThreads, 0);
+    case 1: return configure_blend<1>(), occupancy_of(frag_blend_kernel<1>, kFwdThreads, blend_smem_bytes<1>());
+    case 2: return configure_blend<2>(), occupancy_of(frag_blend_kernel<2>, kFwdThreads, blend_smem_bytes<2>());
+    case 4: return configure_blend<4>(), occupancy_of(frag_blend_kernel<4>, kFwdThreads, blend_smem_bytes<4>());
+    case 8: return configure_blend<8>(), occupancy_of(frag_blend_kernel<8>, kFwdThreads, blend_smem_bytes<8>());
+    default: return configure_blend<16>(), occupancy_of(frag_blend_kernel<16>, kFwdThreads, blend_smem_bytes<16>());
     }
 }
 
@@ -2609,8 +2814,13 @@ void launch_atomic_front(const PassArgs& a, int npix, cudaStream_t stream, cudaE
     }
 }
 
-cudaError_t launch_pass(const PassArgs& a, const LaunchPlan& plan, cudaStream_t stream, cudaEvent_t* ev) {
+cudaError_t launch_pass(const PassArgs& a, const LaunchPlan& plan, cudaStream_t stream, cudaEvent_t* ev,
+                        const FragArgs* fa_in) {
     const int T = a.total_tiles;
+    FragArgs fa, nofa;
+    std::memset(&fa, 0, sizeof(fa));
+    std::memset(&nofa, 0, sizeof(nofa));
+    if (fa_in && plan.defer_group >= 0) fa = *fa_in;
     if (ev) cudaEventRecord(ev[0], stream);
     cudaError_t err = cudaMemsetAsync(a.queues, 0, sizeof(uint32_t) * 3 * plan.ngroups, stream);
     if (err != cudaSuccess) return err;
@@ -2653,7 +2863,8 @@ cudaError_t launch_pass(const PassArgs& a, const LaunchPlan& plan, cudaStream_t 
     // second stages (shade; ordered on top of the prefix for hybrid groups)
     for (int i = 0; i < plan.ngroups && err == cudaSuccess; i++) {
         if (plan.ordered[i] && !plan.hybrid[i])
-            err = launch_group_forward(a, plan.groups[i], plan.samples[i], plan.ctas[i], stream, false);
+            err = launch_group_forward(a, i == plan.defer_group ? fa : nofa, plan.groups[i], plan.samples[i],
+                                       i == plan.defer_group && fa.frags ? plan.ctas_fwd_defer : plan.ctas[i], stream, false);
         else
             err = launch_group_stage(a, plan.groups[i], plan.samples[i], plan.tile_size[i], plan.ctas[i], stream, false);
     }
@@ -2663,9 +2874,12 @@ cudaError_t launch_pass(const PassArgs& a, const LaunchPlan& plan, cudaStream_t 
             err = launch_group_stage(a, plan.groups[i], plan.samples[i], plan.tile_size[i], plan.ctas_shade[i], stream, true);
     if (ev) cudaEventRecord(ev[5], stream);
     for (int i = 0; i < plan.ngroups && err == cudaSuccess; i++)
-        if (plan.hybrid[i]) err = launch_group_forward(a, plan.groups[i], plan.samples[i], plan.ctas_fwd[i], stream, true);
-    if (err == cudaSuccess && a.frags && plan.defer_group >= 0)
-        err = launch_group_frags(a, plan.samples[plan.defer_group], plan.ctas_frag_shade, plan.ctas_frag_blend, stream);
+        if (plan.hybrid[i])
+            err = launch_group_forward(a, i == plan.defer_group ? fa : nofa, plan.groups[i], plan.samples[i],
+                                       i == plan.defer_group && fa.frags ? plan.ctas_fwd_defer : plan.ctas_fwd[i], stream,
+                                       true);
+    if (err == cudaSuccess && fa.frags)
+        err = launch_group_frags(a, fa, plan.samples[plan.defer_group], plan.ctas_frag_shade, plan.ctas_frag_blend, stream);
     if (ev) cudaEventRecord(ev[6], stream);
     return err != cudaSuccess ? err : cudaGetLastError();
 }

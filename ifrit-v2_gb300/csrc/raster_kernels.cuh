@@ -81,8 +81,12 @@ struct PassArgs {
     uint32_t pair_capacity;
     uint32_t* status;        // StatusWord
     uint32_t* queues;        // persistent tile counters, 3 per launch group (raster, shade, ordered)
-    // deferred shading of ordered fragments (frags == nullptr: the ordered stage shades its own)
-    uint4* frags;            // [frag_capacity] entry, px | py << 16, sample mask, 0
+};
+
+// Deferred shading of ordered fragments, passed to the ordered stage and the fragment kernels only
+// (frags == nullptr: the ordered stage shades its own fragments).
+struct FragArgs {
+    uint4* frags;            // [frag_capacity] entry, px | py << 16, sample mask, draw
     float4* frag_cols;       // [frag_capacity] colour of each fragment
     uint32_t frag_capacity;
     uint4* fwd_tiles;        // [total_tiles] deferred tiles: global tile, first fragment, view, hand-off flag
@@ -112,9 +116,10 @@ struct LaunchPlan {
     int atomic;                 // one deferred view resolved by the atomic visibility path (no binning)
     int atomic_pixels;          // its W * H
     int defer_group;            // the only ordered group, whose fragments may be shaded by their own
-                                //    kernels (when PassArgs::frags is set); -1: none
+                                //    kernels (when FragArgs::frags is set); -1: none
     int ctas_frag_shade;        // CTAs of the deferred fragment shading and blending kernels
     int ctas_frag_blend;
+    int ctas_fwd_defer;         // CTAs of the defer group's ordered stage in its deferring form
 };
 
 }  // namespace ifr
@@ -127,7 +132,9 @@ constexpr int scan_blocks(int tiles) { return (tiles + 4095) / 4096 + 1; }
 // scan, after scattering, after the raster stage, after the shade stage and after the ordered
 // stage (per-stage timing).
 constexpr int kStageEvents = 7;
-cudaError_t launch_pass(const PassArgs& a, const LaunchPlan& plan, cudaStream_t stream, cudaEvent_t* ev);
+// fa: buffers of the deferred ordered fragments, or nullptr.
+cudaError_t launch_pass(const PassArgs& a, const LaunchPlan& plan, cudaStream_t stream, cudaEvent_t* ev,
+                        const FragArgs* fa = nullptr);
 // Reference line / point rules (iftrSetPolygonRules): one single-sample draw; `keys` holds W*H
 // 64-bit entries of scratch.
 cudaError_t launch_reference_rules(const DrawDev& d, const ViewArgs& v, unsigned long long* keys, cudaStream_t stream);
@@ -142,6 +149,7 @@ cudaError_t launch_mesh_compact(const float* pos, const float* attr, const int* 
 // Maximum resident CTAs per SM of a tile kernel for (samples, tile size, ordered); stage 0 is
 // the raster (or ordered) kernel, stage 1 the shade kernel.
 int tile_kernel_occupancy(int samples, int tile_size, int ordered, int stage);
-// Resident CTAs per SM of the deferred fragment shading (stage 0) and blending (stage 1) kernels.
+// Resident CTAs per SM of the deferred fragment shading (stage 0) and blending (stage 1) kernels
+// and of the ordered stage's deferring form (stage 2).
 int frag_kernel_occupancy(int samples, int stage);
 }  // namespace ifr
