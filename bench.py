@@ -430,6 +430,33 @@ def run_c3(args, steps, warmup, e2e_steps, with_cpu=True, rank=0, world=1, dist=
             r.finish()
         tiny_plain.append((time.perf_counter() - t0) / 3)
         r.close()
+    # the lean plain path: every view's renderer enqueues its pass (iftrDrawAsync) back to back on
+    # one stream and the status is read once per renderer after the last one (no wait per frame)
+    rs = []
+    for v in tiny:
+        r = ig.Renderer(v["width"], v["height"], v["samples"], ig.FORMAT_RGBA8, visibility=False)
+        r.set_stream(stream.cuda_stream)
+        r.set_state(cull=v["cull"], depth_func=ig.LESS_OR_EQUAL, shading=ig.FS_GOURAUD)
+        r.set_mvp(v["mvp"])
+        dv = torch.from_numpy(v["vertices"]).to(dev)
+        di = torch.from_numpy(v["indices"].reshape(-1)).to(dev)
+        stride = v["vertices"].shape[1]
+        r.bind_device_geometry(dv.data_ptr(), stride, len(v["vertices"]), 3, stride - 3, di.data_ptr(), di.numel())
+        r.draw_async()
+        r.finish()
+        rs.append((r, dv, di))
+    lean = []
+    for _ in range(3):
+        t0 = time.perf_counter()
+        for r, _, _ in rs:
+            r.draw_async()
+        for r, _, _ in rs:
+            r.finish()
+        lean.append(time.perf_counter() - t0)
+    for r, _, _ in rs:
+        r.close()
+    del rs
+    tiny_lean = statistics.median(lean)
     views = views_saved
     tiny_batched = sum(tiny_shaded) / (ms_tiny / 1000.0)
     tiny_plain_rate = sum(tiny_shaded) / sum(tiny_plain)
@@ -453,7 +480,13 @@ def run_c3(args, steps, warmup, e2e_steps, with_cpu=True, rank=0, world=1, dist=
         "overhead_bound_small_views": {"views": len(tiny), "size": 128, "triangles_per_view": "900-1100",
                                        "batched": tiny_batched, "plain": tiny_plain_rate,
                                        "ratio": tiny_batched / tiny_plain_rate, "ms_batched": ms_tiny,
-                                       "ms_plain_per_view": 1000.0 * statistics.mean(tiny_plain)},
+                                       "ms_plain_per_view": 1000.0 * statistics.mean(tiny_plain),
+                                       "plain_enqueued": sum(tiny_shaded) / tiny_lean,
+                                       "ratio_to_enqueued": tiny_batched / (sum(tiny_shaded) / tiny_lean),
+                                       "ms_plain_enqueued_per_view": 1000.0 * tiny_lean / len(tiny),
+                                       "how_enqueued": "256 renderers, iftrDrawAsync each back to back on one stream, "
+                                                       "then iftrFinish each (one status read per renderer, no wait "
+                                                       "between frames), host wall time"},
         "roofline": {"bound": "hbm", "achieved": B / (ms / 1000.0) / 1e9, "peak": peak, "unit": "GB/s",
                      "frac": B / (ms / 1000.0) / 1e9 / peak, "traffic": None, "algorithmic_bytes": B,
                      "kernel": "whole batched pass", "peak_source": peak_kind},

@@ -1774,7 +1774,7 @@ __device__ __forceinline__ void forward_tile(const PassArgs& a, const FragArgs& 
         } else if constexpr (S % 4 == 0) {
 #pragma unroll
             for (int k = 0; k < S; k += 4) {
-                const int4 q = reinterpret_cast<const int4*>(v.entries + pix * S)[k / 4];
+                const int4 q = v.vis ? reinterpret_cast<const int4*>(v.entries + pix * S)[k / 4] : make_int4(-1, -1, -1, -1);
                 const float4 z = reinterpret_cast<const float4*>(v.depth + pix * S)[k / 4];
                 ent[k] = q.x; ent[k + 1] = q.y; ent[k + 2] = q.z; ent[k + 3] = q.w;
                 dep[k] = z.x; dep[k + 1] = z.y; dep[k + 2] = z.z; dep[k + 3] = z.w;
@@ -1782,7 +1782,7 @@ __device__ __forceinline__ void forward_tile(const PassArgs& a, const FragArgs& 
         } else {
 #pragma unroll
             for (int k = 0; k < S; k++) {
-                ent[k] = v.entries[pix * S + k];
+                ent[k] = v.vis ? v.entries[pix * S + k] : -1;  // primitive ids are only written with visibility output
                 dep[k] = v.depth[pix * S + k];
             }
         }
@@ -1795,6 +1795,9 @@ __device__ __forceinline__ void forward_tile(const PassArgs& a, const FragArgs& 
             vid[k] = -1;
         }
     }
+    // the depth target already holds dep[] after the raster stage; otherwise (cleared or earlier
+    // content) it is written whatever happens
+    bool dep_changed = !after_raster;
     bool have_cols = bulk || (defer && after_raster);  // scol holds this thread's starting colours
     if (!defer && !bulk) {
         start_colours<S>(v, scol, ltile, after_raster, bg);
@@ -1951,7 +1954,10 @@ __device__ __forceinline__ void forward_tile(const PassArgs& a, const FragArgs& 
                         if (!covered(A, B, Cb, sx, sy)) continue;
                         const float z = sample_depth(rec.z0[r], rec.dzdx[r], rec.dzdy[r], rec.X0[r], rec.Y0[r], sx, sy);
                         if (!depth_cmp(func, z, dep[k])) continue;
-                        if (write) dep[k] = z;
+                        if (write) {
+                            dep_changed |= __float_as_uint(dep[k]) != __float_as_uint(z);
+                            dep[k] = z;
+                        }
                         vid[k] = (e >> 3) - v.first_tri;
                         mask |= 1u << k;
                     }
@@ -2023,7 +2029,7 @@ __device__ __forceinline__ void forward_tile(const PassArgs& a, const FragArgs& 
                 }
                 fa.fwd_pix_end[(size_t)slot * NT + tid] = (uint16_t)(pre + nfrag);
                 if (inpix) {
-                    store_depth<S>(v.depth + pix * S, dep);
+                    if (dep_changed) store_depth<S>(v.depth + pix * S, dep);
                     if (v.vis) {
                         int* vp = v.vis + pix * S;
 #pragma unroll
@@ -2056,7 +2062,7 @@ __device__ __forceinline__ void forward_tile(const PassArgs& a, const FragArgs& 
     const float invS = 1.0f / (float)S;
     acc[0] = acc[0] * invS; acc[1] = acc[1] * invS; acc[2] = acc[2] * invS; acc[3] = acc[3] * invS;
     encode_color(v, pix, acc);
-    store_depth<S>(v.depth + pix * S, dep);
+    if (dep_changed) store_depth<S>(v.depth + pix * S, dep);
     if (v.vis) {
         int* vp = v.vis + pix * S;
 #pragma unroll

@@ -32,8 +32,16 @@
  *   ifrit_ext::draw_mesh_stage(renderer, MyMesh{...}, groups, max_v, max_i, slots, attr_count, clear);
  * launches the functor as the stage kernel (one CTA per work group) on the renderer's stream into
  * the caller's slot arrays and draws them through iftrDrawMeshOutputs (group-order compaction,
- * the current state, clip-space input).  A task stage is the caller's choice of `groups` and of
- * what each group emits.
+ * the current state, clip-space input).
+ *
+ * Task stage (the reference's TaskShader, taskShadingKernel + prefix scan +
+ * taskShadingLaunchSubGroupsKernel):
+ *   struct MyTask { __device__ int mesh_groups(int task) const; };
+ *   struct MyMesh { counts(task, sub, nv, ni); vertex(task, sub, i, clip, attr); index(task, sub, j); };
+ *   ifrit_ext::draw_task_mesh_stage(renderer, MyTask{...}, MyMesh{...}, tasks, max_groups, max_v, max_i,
+ *                                   slots, d_offsets, attr_count, clear, stream);
+ * runs the task functor once per task group, scans the mesh-group counts, runs the mesh functor
+ * once per spawned group (task, sub) and draws the groups in (task, sub) order.
  *
  * Compile with -I<repository>/include; this header includes the library's device arithmetic from
  * ifrit-v2_gb300/csrc (relative to this file).
@@ -42,6 +50,8 @@
 #define IFRIT_GB300_EXT_CUH
 #include <cuda_fp16.h>
 #include <cuda_runtime.h>
+
+#include <climits>
 
 #include "../ifrit-v2_gb300/csrc/pass_plan.h"
 #include "../ifrit-v2_gb300/csrc/raster_math.cuh"
@@ -228,6 +238,84 @@ __global__ void mesh_stage_kernel(Mesh mesh, int max_v, int max_i, float* positi
     for (int j = threadIdx.x; j < ni; j += blockDim.x) indices[(size_t)g * max_i + j] = mesh.index(g, j);
 }
 
+// One thread per task group: the number of mesh groups it spawns (negative counts as zero).
+template <class Task>
+__global__ void task_count_kernel(Task task, int tasks, int* offsets) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < tasks) offsets[t] = max(task.mesh_groups(t), 0);
+}
+
+// Exclusive scan of the counts in place (one CTA); offsets[tasks] receives the total, saturated at
+// INT_MAX.
+__global__ void __launch_bounds__(1024) task_scan_kernel(int* offsets, int tasks) {
+    __shared__ long long s_warp[32];
+    __shared__ long long s_carry;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    if (threadIdx.x == 0) s_carry = 0;
+    __syncthreads();
+    for (int base = 0; base < tasks; base += 1024) {
+        const int i = base + threadIdx.x;
+        const long long x = i < tasks ? offsets[i] : 0;
+        long long incl = x;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const long long q = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += q;
+        }
+        if (lane == 31) s_warp[wid] = incl;
+        __syncthreads();
+        long long before = s_carry;
+        for (int w = 0; w < wid; w++) before += s_warp[w];
+        const long long ex = before + incl - x;
+        if (i < tasks) offsets[i] = (int)min(ex, (long long)INT_MAX);
+        __syncthreads();
+        if (threadIdx.x == 1023) s_carry = before + incl;
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) offsets[tasks] = (int)min(s_carry, (long long)INT_MAX);
+}
+
+// One CTA per mesh slot: slot g runs the mesh functor for (task, sub) with offsets[task] <= g <
+// offsets[task + 1]; slots past the total emit nothing.
+template <class Mesh>
+__global__ void task_mesh_kernel(Mesh mesh, const int* offsets, int tasks, int max_v, int max_i, float* positions,
+                                 float* attributes, int* indices, int* num_vertices, int* num_indices) {
+    const int g = blockIdx.x;
+    __shared__ int s_nv, s_ni, s_task;
+    if (threadIdx.x == 0) {
+        int nv = 0, ni = 0, t = -1;
+        if (g < offsets[tasks]) {
+            int lo = 0, hi = tasks - 1;  // the last task whose first group is at or before g
+            while (lo < hi) {
+                const int mid = (lo + hi + 1) >> 1;
+                if (offsets[mid] <= g) lo = mid; else hi = mid - 1;
+            }
+            t = lo;
+            mesh.counts(t, g - offsets[t], nv, ni);
+        }
+        s_nv = nv;
+        s_ni = ni;
+        s_task = t;
+        num_vertices[g] = nv;
+        num_indices[g] = ni;
+    }
+    __syncthreads();
+    if (s_task < 0) return;
+    const int t = s_task, sub = g - offsets[t];
+    const int nv = min(s_nv, max_v), ni = min(s_ni, max_i);
+    for (int i = threadIdx.x; i < nv; i += blockDim.x) {
+        float clip[4], attr[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+        mesh.vertex(t, sub, i, clip, attr);
+        float* pp = positions + ((size_t)g * max_v + i) * 4;
+        pp[0] = clip[0]; pp[1] = clip[1]; pp[2] = clip[2]; pp[3] = clip[3];
+        if (attributes) {
+            float* ap = attributes + ((size_t)g * max_v + i) * 4;
+            ap[0] = attr[0]; ap[1] = attr[1]; ap[2] = attr[2]; ap[3] = attr[3];
+        }
+    }
+    for (int j = threadIdx.x; j < ni; j += blockDim.x) indices[(size_t)g * max_i + j] = mesh.index(t, sub, j);
+}
+
 }  // namespace detail
 
 // Shades every pixel of a visibility buffer with `shader` into p.color (see the file comment).
@@ -292,6 +380,37 @@ int draw_mesh_stage(IfritGbRenderer* h, const Mesh& mesh, int groups, int max_v,
         if (cudaGetLastError() != cudaSuccess) return IFTR_ERR_CUDA;
     }
     return iftrDrawMeshOutputs(h, groups, slots.positions, attr_count > 0 ? slots.attributes : nullptr, attr_count,
+                               slots.indices, slots.num_vertices, slots.num_indices, max_v, max_i, clear);
+}
+
+// Runs `task` over `tasks` task groups, then `mesh` over the mesh groups they spawn (at most
+// `max_groups`, the slot arrays' group count), and draws them through iftrDrawMeshOutputs in
+// (task, sub) order.  offsets: caller device memory of tasks + 1 ints.  Returns an IFTR_* status;
+// IFTR_ERR_OVERFLOW (nothing drawn) when the tasks spawn more than max_groups groups.
+template <class Task, class Mesh>
+int draw_task_mesh_stage(IfritGbRenderer* h, const Task& task, const Mesh& mesh, int tasks, int max_groups, int max_v,
+                         int max_i, const MeshSlots& slots, int* offsets, int attr_count, int clear,
+                         cudaStream_t stream) {
+    if (!h || tasks < 0 || max_groups < 0 || max_v <= 0 || max_i <= 0 || !offsets || !slots.positions ||
+        !slots.indices || !slots.num_vertices || !slots.num_indices)
+        return IFTR_ERR_INVALID_ARG;
+    int rc = iftrSetStream(h, stream);
+    if (rc) return rc;
+    if (tasks > 0) detail::task_count_kernel<Task><<<(tasks + 255) / 256, 256, 0, stream>>>(task, tasks, offsets);
+    detail::task_scan_kernel<<<1, 1024, 0, stream>>>(offsets, tasks);
+    if (max_groups > 0)
+        detail::task_mesh_kernel<Mesh><<<max_groups, 128, 0, stream>>>(mesh, offsets, tasks, max_v, max_i,
+                                                                       slots.positions,
+                                                                       attr_count > 0 ? slots.attributes : nullptr,
+                                                                       slots.indices, slots.num_vertices,
+                                                                       slots.num_indices);
+    if (cudaGetLastError() != cudaSuccess) return IFTR_ERR_CUDA;
+    int total = 0;
+    if (cudaMemcpyAsync(&total, offsets + tasks, sizeof(int), cudaMemcpyDeviceToHost, stream) != cudaSuccess ||
+        cudaStreamSynchronize(stream) != cudaSuccess)
+        return IFTR_ERR_CUDA;
+    if (total > max_groups) return IFTR_ERR_OVERFLOW;
+    return iftrDrawMeshOutputs(h, max_groups, slots.positions, attr_count > 0 ? slots.attributes : nullptr, attr_count,
                                slots.indices, slots.num_vertices, slots.num_indices, max_v, max_i, clear);
 }
 

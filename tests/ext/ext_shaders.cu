@@ -3,6 +3,7 @@
 //
 //   ext_shade(which, ...)   which 0: ifrit_ext::Gouraud, 1: AttrDerivShader (below)
 //   ext_draw_grid(...)      GridMesh as the mesh stage, drawn through iftrDrawMeshOutputs
+//   ext_draw_task_grid(...) TaskSpawn + TaskGrid as the task and mesh stages
 #include "ifrit_gb300_ext.cuh"
 
 // Uses the attribute, both quad derivatives and the triangle index, so every field of the
@@ -21,6 +22,24 @@ struct AttrDerivShader {
 // exactly representable coordinates transformed by `mvp` with the vertex stage's row order,
 // ((m0 x + m1 y) + m2 z) + m3, so a host-side indexed mesh of the same positions draws the same
 // clip coordinates.
+// Vertex i (0..3) of the quad of grid cell `cell` (nx cells per row).
+__device__ void cell_vertex(const float* mvp, int nx, int cell, int i, float clip[4], float attr[4]) {
+    const int cx = cell % nx, cy = cell / nx;
+    const int vx = cx + (i & 1), vy = cy + (i >> 1);
+    const float p[3] = {(float)vx * 0.125f - 1.0f, (float)vy * 0.125f - 1.0f, -2.0f - (float)((cx * 3 + cy * 5) % 8) * 0.0625f};
+    for (int r = 0; r < 4; r++)
+        clip[r] = ((mvp[4 * r + 0] * p[0] + mvp[4 * r + 1] * p[1]) + mvp[4 * r + 2] * p[2]) + mvp[4 * r + 3];
+    attr[0] = (float)vx * 0.0625f;
+    attr[1] = (float)vy * 0.0625f;
+    attr[2] = (float)((cell * 5) % 9) * 0.125f;
+    attr[3] = 1.0f;
+}
+
+__device__ int quad_index(int j) {
+    const int tri[6] = {0, 1, 2, 2, 1, 3};
+    return tri[j];
+}
+
 struct GridMesh {
     int nx, ny;
     float mvp[16];
@@ -29,21 +48,27 @@ struct GridMesh {
         nv = 4;
         ni = (g % 5 == 1) ? 3 : 6;
     }
-    __device__ void vertex(int g, int i, float clip[4], float attr[4]) const {
-        const int cx = g % nx, cy = g / nx;
-        const int vx = cx + (i & 1), vy = cy + (i >> 1);
-        const float p[3] = {(float)vx * 0.125f - 1.0f, (float)vy * 0.125f - 1.0f, -2.0f - (float)((cx * 3 + cy * 5) % 8) * 0.0625f};
-        for (int r = 0; r < 4; r++)
-            clip[r] = ((mvp[4 * r + 0] * p[0] + mvp[4 * r + 1] * p[1]) + mvp[4 * r + 2] * p[2]) + mvp[4 * r + 3];
-        attr[0] = (float)vx * 0.0625f;
-        attr[1] = (float)vy * 0.0625f;
-        attr[2] = (float)((g * 5) % 9) * 0.125f;
-        attr[3] = 1.0f;
+    __device__ void vertex(int g, int i, float clip[4], float attr[4]) const { cell_vertex(mvp, nx, g, i, clip, attr); }
+    __device__ int index(int g, int j) const { return quad_index(j); }
+};
+
+// Task group t spawns t % 4 mesh groups; mesh group (t, sub) draws cell 3 t + sub (one triangle when
+// (t + sub) % 3 == 1, else two).
+struct TaskSpawn {
+    __device__ int mesh_groups(int t) const { return t % 4; }
+};
+
+struct TaskGrid {
+    int nx;
+    float mvp[16];
+    __device__ void counts(int t, int sub, int& nv, int& ni) const {
+        nv = 4;
+        ni = ((t + sub) % 3 == 1) ? 3 : 6;
     }
-    __device__ int index(int g, int j) const {
-        const int tri[6] = {0, 1, 2, 2, 1, 3};
-        return tri[j];
+    __device__ void vertex(int t, int sub, int i, float clip[4], float attr[4]) const {
+        cell_vertex(mvp, nx, 3 * t + sub, i, clip, attr);
     }
+    __device__ int index(int t, int sub, int j) const { return quad_index(j); }
 };
 
 extern "C" int ext_shade(int which, const float* vertices, int stride, int num_vertices, int attr_offset,
@@ -85,4 +110,15 @@ extern "C" int ext_draw_grid(IfritGbRenderer* h, int nx, int ny, const float* mv
     std::memcpy(m.mvp, mvp, sizeof(m.mvp));
     ifrit_ext::MeshSlots slots{positions, attributes, indices, num_vertices, num_indices};
     return ifrit_ext::draw_mesh_stage(h, m, nx * ny, 4, 6, slots, 4, clear, static_cast<cudaStream_t>(stream));
+}
+
+extern "C" int ext_draw_task_grid(IfritGbRenderer* h, int tasks, int nx, const float* mvp, float* positions,
+                                  float* attributes, int* indices, int* num_vertices, int* num_indices, int* offsets,
+                                  int max_groups, int clear, void* stream) {
+    TaskGrid m;
+    m.nx = nx;
+    std::memcpy(m.mvp, mvp, sizeof(m.mvp));
+    ifrit_ext::MeshSlots slots{positions, attributes, indices, num_vertices, num_indices};
+    return ifrit_ext::draw_task_mesh_stage(h, TaskSpawn{}, m, tasks, max_groups, 4, 6, slots, offsets, 4, clear,
+                                           static_cast<cudaStream_t>(stream));
 }

@@ -11,7 +11,10 @@ linked against libifrit_gb300.so) and called through ctypes:
   numpy restatement over the built-in RGBA32F image bit for bit, and that image matches the oracle
   (so the chain oracle -> built-in -> functor is pinned);
 * a functor-driven mesh stage (a grid, some groups empty or short) drawn through
-  iftrDrawMeshOutputs matches the oracle drawing the same indexed mesh."""
+  iftrDrawMeshOutputs matches the oracle drawing the same indexed mesh;
+* a task functor spawning 0-3 mesh groups per task group, with the mesh functor run per (task, sub),
+  matches the oracle drawing the cells in (task, sub) order, and too many spawned groups return
+  IFTR_ERR_OVERFLOW."""
 import ctypes
 import os
 
@@ -41,6 +44,8 @@ def ext():
     lib.ext_shade.restype = ip
     lib.ext_draw_grid.argtypes = [vp, ip, ip, vp, vp, vp, vp, vp, vp, ip, vp]
     lib.ext_draw_grid.restype = ip
+    lib.ext_draw_task_grid.argtypes = [vp, ip, ip, vp, vp, vp, vp, vp, vp, vp, ip, ip, vp]
+    lib.ext_draw_task_grid.restype = ip
     return lib
 
 
@@ -134,25 +139,39 @@ def test_fragment_fields_match_builtin_and_oracle(ext):
     assert (functor[yy, xy, 1] == ddy * np.float32(64.0)).all()
 
 
+def _cell(verts, tris, nx, cell, one_triangle):
+    """Host restatement of cell_vertex / quad_index (tests/ext/ext_shaders.cu)."""
+    cx, cy = cell % nx, cell // nx
+    base = len(verts)
+    z = np.float32(-2.0) - np.float32((cx * 3 + cy * 5) % 8) * np.float32(0.0625)
+    for i in range(4):
+        vx, vy = cx + (i & 1), cy + (i >> 1)
+        verts.append([np.float32(vx) * np.float32(0.125) - np.float32(1.0),
+                      np.float32(vy) * np.float32(0.125) - np.float32(1.0), z,
+                      np.float32(vx) * np.float32(0.0625), np.float32(vy) * np.float32(0.0625),
+                      np.float32((cell * 5) % 9) * np.float32(0.125), 1.0])
+    tris.append([base, base + 1, base + 2])
+    if not one_triangle:
+        tris.append([base + 2, base + 1, base + 3])
+
+
 def grid_mesh(nx, ny):
-    """Host restatement of GridMesh (tests/ext/ext_shaders.cu): per-group vertices (x, y, z,
-    r, g, b, a) and the triangles of the non-empty groups in group order."""
+    """GridMesh's groups: per-group vertices (x, y, z, r, g, b, a) and the triangles of the
+    non-empty groups in group order."""
     verts, tris = [], []
     for g in range(nx * ny):
         if g % 7 == 3:
             continue
-        cx, cy = g % nx, g // nx
-        base = len(verts)
-        z = np.float32(-2.0) - np.float32((cx * 3 + cy * 5) % 8) * np.float32(0.0625)
-        for i in range(4):
-            vx, vy = cx + (i & 1), cy + (i >> 1)
-            verts.append([np.float32(vx) * np.float32(0.125) - np.float32(1.0),
-                          np.float32(vy) * np.float32(0.125) - np.float32(1.0), z,
-                          np.float32(vx) * np.float32(0.0625), np.float32(vy) * np.float32(0.0625),
-                          np.float32((g * 5) % 9) * np.float32(0.125), 1.0])
-        tris.append([base, base + 1, base + 2])
-        if g % 5 != 1:
-            tris.append([base + 2, base + 1, base + 3])
+        _cell(verts, tris, nx, g, g % 5 == 1)
+    return np.array(verts, np.float32), np.array(tris, np.int32)
+
+
+def task_grid(tasks, nx):
+    """TaskSpawn + TaskGrid: task t spawns t % 4 groups; group (t, sub) draws cell 3 t + sub."""
+    verts, tris = [], []
+    for t in range(tasks):
+        for sub in range(t % 4):
+            _cell(verts, tris, nx, 3 * t + sub, (t + sub) % 3 == 1)
     return np.array(verts, np.float32), np.array(tris, np.int32)
 
 
@@ -182,3 +201,38 @@ def test_functor_mesh_stage_matches_oracle(ext, S):
                    nthreads=os.cpu_count() or 1)
     assert_parity(gpu, ref)
     assert (gpu["vis"] >= 0).sum() > W * H // 4
+
+
+@pytest.mark.parametrize("S", [1, 4])
+def test_functor_task_stage_matches_oracle(ext, S):
+    tasks, nx, W, H = 120, 24, 160, 128
+    mvp = scenes.perspective(60.0, W / H, 0.1, 50.0).astype(np.float32)
+    G = sum(t % 4 for t in range(tasks))
+    dev = torch.device("cuda")
+    pos = torch.full((G, 4, 4), 7.0, dtype=torch.float32, device=dev)
+    att = torch.zeros((G, 4, 4), dtype=torch.float32, device=dev)
+    idx = torch.full((G, 6), -1, dtype=torch.int32, device=dev)
+    nv = torch.zeros(G, dtype=torch.int32, device=dev)
+    ni = torch.zeros(G, dtype=torch.int32, device=dev)
+    offs = torch.zeros(tasks + 1, dtype=torch.int32, device=dev)
+    r = ig.Renderer(W, H, S, ig.FORMAT_RGBA8, visibility=True)
+    r.set_state(cull=ig.CULL_NONE, depth_func=ig.LESS, shading=ig.FS_GOURAUD, clear_color=BG)
+    m = _f32(mvp).reshape(-1)
+    stream = torch.cuda.current_stream().cuda_stream
+    # one group too few: nothing drawn, IFTR_ERR_OVERFLOW
+    rc = ext.ext_draw_task_grid(r.h, tasks, nx, m.ctypes.data, pos.data_ptr(), att.data_ptr(), idx.data_ptr(),
+                                nv.data_ptr(), ni.data_ptr(), offs.data_ptr(), G - 1, 1, stream)
+    assert rc == 4  # IFTR_ERR_OVERFLOW
+    rc = ext.ext_draw_task_grid(r.h, tasks, nx, m.ctypes.data, pos.data_ptr(), att.data_ptr(), idx.data_ptr(),
+                                nv.data_ptr(), ni.data_ptr(), offs.data_ptr(), G, 1, stream)
+    assert rc == 0, "draw_task_mesh_stage returned %d" % rc
+    gpu = {"color": r.color(), "depth": r.depth(), "vis": r.visibility()}
+    r.close()
+    v, f = task_grid(tasks, nx)
+    assert int(ni.sum().item()) == f.size
+    assert offs.cpu().numpy()[-1] == G
+    d = O.make_draw(v, f, mvp, attr_offset=3, attr_count=4, cull_mode=ig.CULL_NONE, depth_func=ig.LESS)
+    ref = O.render([d], W, H, S, FMT_TO_ORACLE[ig.FORMAT_RGBA8], clear=True, clear_color=BG,
+                   nthreads=os.cpu_count() or 1)
+    assert_parity(gpu, ref)
+    assert (gpu["vis"] >= 0).sum() > W * H // 8
