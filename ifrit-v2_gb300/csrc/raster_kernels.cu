@@ -25,6 +25,7 @@
 #include <cuda_fp16.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cstring>
 
 #include "raster_kernels.cuh"
@@ -2765,7 +2766,7 @@ int forward_occupancy() {
     return occupancy_of(forward_kernel<S, DEFER>, kFwdThreads, forward_smem_bytes<S, DEFER>());
 }
 
-int frag_kernel_occupancy(int S, int stage) {
+static int frag_kernel_occupancy_query(int S, int stage) {
     if (stage == 0) return occupancy_of(frag_shade_kernel, kFragShadeThreads, 0);
     if (stage == 2) {
         switch (S) {
@@ -2785,7 +2786,7 @@ int frag_kernel_occupancy(int S, int stage) {
     }
 }
 
-int tile_kernel_occupancy(int S, int TS, int ordered, int stage) {
+static int tile_kernel_occupancy_query(int S, int TS, int ordered, int stage) {
     if (ordered) {
         switch (S) {
         case 1: return forward_occupancy<1>();
@@ -2818,6 +2819,25 @@ void launch_atomic_front(const PassArgs& a, int npix, cudaStream_t stream, cudaE
         cudaEventRecord(ev[3], stream);
         cudaEventRecord(ev[4], stream);
     }
+}
+
+// Occupancy answers do not change for a kernel: asked once per (samples, tile size, form, stage).
+static int sample_slot(int S) { return S == 1 ? 0 : S == 2 ? 1 : S == 4 ? 2 : S == 8 ? 3 : 4; }
+
+int tile_kernel_occupancy(int S, int TS, int ordered, int stage) {
+    static std::atomic<int> cache[5][2][2][2];  // 0: not asked yet (zero-initialised static storage)
+    std::atomic<int>& c = cache[sample_slot(S)][TS == 8][ordered != 0][stage != 0];
+    int n = c.load(std::memory_order_relaxed);
+    if (n == 0) c.store(n = tile_kernel_occupancy_query(S, TS, ordered, stage), std::memory_order_relaxed);
+    return n;
+}
+
+int frag_kernel_occupancy(int S, int stage) {
+    static std::atomic<int> cache[5][3];
+    std::atomic<int>& c = cache[sample_slot(S)][stage < 0 ? 0 : stage > 2 ? 2 : stage];
+    int n = c.load(std::memory_order_relaxed);
+    if (n == 0) c.store(n = frag_kernel_occupancy_query(S, stage), std::memory_order_relaxed);
+    return n;
 }
 
 cudaError_t launch_pass(const PassArgs& a, const LaunchPlan& plan, cudaStream_t stream, cudaEvent_t* ev,

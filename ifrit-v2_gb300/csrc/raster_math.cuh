@@ -559,15 +559,18 @@ __device__ __forceinline__ float log2_series(float x) {
 }
 
 // ------------------------------------------------------------------ textures
-// Byte b -> float(b) exactly via the 2^23 bias trick (one logic op and one add, both full
-// rate), then the same scale the conversion instruction path would use.
-__device__ __forceinline__ float byte_to_float(uint32_t b) { return (float)b; }  // exact for b < 2^24
+// Byte k of t as a float (exact).  Building 2^23 + byte with a byte permute and subtracting 2^23
+// measured the same on the textured frames.
+template <int K>
+__device__ __forceinline__ float byte_to_float(uint32_t t) {
+    return (float)((t >> (8 * K)) & 255u);
+}
 
 __device__ __forceinline__ void unpack_rgba8(uint32_t t, float c[4]) {
-    c[0] = byte_to_float(t & 255u) * kInv255;
-    c[1] = byte_to_float((t >> 8) & 255u) * kInv255;
-    c[2] = byte_to_float((t >> 16) & 255u) * kInv255;
-    c[3] = byte_to_float(t >> 24) * kInv255;
+    c[0] = byte_to_float<0>(t) * kInv255;
+    c[1] = byte_to_float<1>(t) * kInv255;
+    c[2] = byte_to_float<2>(t) * kInv255;
+    c[3] = byte_to_float<3>(t) * kInv255;
 }
 
 __device__ __forceinline__ float lerpf_(float a, float b, float t) { return a + t * (b - a); }
