@@ -1648,14 +1648,23 @@ __global__ void __launch_bounds__(kShadeThreads, kShadeBlocks) shade_kernel(Pass
 // on-chip resolve.  16x16 tiles.
 constexpr int kFwdThreads = 256;
 
+// Set-ups of one batch of ordered entries.  Edge functions are kept relative to the tile origin:
+// a record spanning less than 32 pixels in x and y evaluates them exactly in 32-bit arithmetic (the
+// raster stage's bound, kSmallSpan), larger ones in 64 bits.
 struct FwdRecords {
     int32_t A[3][kFwdThreads], B[3][kFwdThreads];
-    long long Cb[3][kFwdThreads];
+    long long Et[3][kFwdThreads];  // biased edge functions at the tile origin
     float z0[kFwdThreads], dzdx[kFwdThreads], dzdy[kFwdThreads];
     int32_t X0[kFwdThreads], Y0[kFwdThreads];
     int32_t key[kFwdThreads];
     int32_t draw[kFwdThreads];
+    int32_t meta[kFwdThreads];     // kLargeRecord | depth function << 1 | depth write << 4 | scissor test << 5
+    uint32_t box[kFwdThreads];     // pixel box in the tile: column mask | row mask << 16 (0: empty)
 };
+
+// Batches of up to this many records find each pixel's candidates by scanning the records' boxes;
+// larger batches mark them into per-pixel bitmasks from the records' side.
+constexpr int kFwdScanBatch = 64;
 
 constexpr int kFwdFrags = 8;      // fragments a pixel holds before they are shaded
 constexpr int kFwdSmallBox = 24;  // candidate boxes of up to this many pixels are marked by their record's thread
@@ -1887,20 +1896,30 @@ __device__ __forceinline__ void forward_tile(const PassArgs& a, const FragArgs& 
         const int nb = min(NT, n - base);
         // candidate masks of the batch: bit r of cand[r / 32][lane] when record r's pixel box
         // holds the lane's pixel
+        if (nb > kFwdScanBatch) {
 #pragma unroll
-        for (int w = 0; w < NT / 32; w++) cand[w * NT + tid] = 0u;
+            for (int w = 0; w < NT / 32; w++) cand[w * NT + tid] = 0u;
+        }
         int area = 0, cx0 = 0, cy0 = 0, cw = 1;
+        uint32_t box = 0;
         if (tid < nb) {
             uint32_t e = list[base + tid];
             SubTri s;
             int di;
             if (setup_raster_entry(a, v.c, e, &s, &di)) {
+                const int64_t X_t = (int64_t)tx * TS * 256, Y_t = (int64_t)ty * TS * 256;
 #pragma unroll
                 for (int i = 0; i < 3; i++) {
                     rec.A[i][tid] = s.A[i];
                     rec.B[i][tid] = s.B[i];
-                    rec.Cb[i][tid] = s.Cb[i];
+                    rec.Et[i][tid] = s.Cb[i] + (int64_t)s.A[i] * X_t + (int64_t)s.B[i] * Y_t;
                 }
+                const int32_t xmn = min(s.X[0], min(s.X[1], s.X[2])), xmx = max(s.X[0], max(s.X[1], s.X[2]));
+                const int32_t ymn = min(s.Y[0], min(s.Y[1], s.Y[2])), ymx = max(s.Y[0], max(s.Y[1], s.Y[2]));
+                const bool small = xmx - xmn < kSmallSpan && ymx - ymn < kSmallSpan;
+                const DrawDev& d = a.draws[di];
+                rec.meta[tid] = (small ? 0 : kLargeRecord) | (d.depth_func << 1) | ((d.depth_write ? 1 : 0) << 4) |
+                                ((d.scissor_count ? 1 : 0) << 5);
                 rec.z0[tid] = s.z[0];
                 rec.dzdx[tid] = s.dzdx;
                 rec.dzdy[tid] = s.dzdy;
@@ -1912,47 +1931,85 @@ __device__ __forceinline__ void forward_tile(const PassArgs& a, const FragArgs& 
                 if (cx1 >= cx0 && cy1 >= cy0) {
                     cw = cx1 - cx0 + 1;
                     area = cw * (cy1 - cy0 + 1);
+                    box = (((2u << cx1) - 1u) & ~((1u << cx0) - 1u)) | ((((2u << cy1) - 1u) & ~((1u << cy0) - 1u)) << 16);
                 }
             }
             rec.key[tid] = (int)e;
             rec.draw[tid] = di;
+            rec.box[tid] = box;
         }
+        const bool scan = nb <= kFwdScanBatch;  // uniform
         __syncthreads();
-        // mark the candidates: small boxes by their record's thread, larger ones by the whole warp
-        uint32_t* crow = cand + (tid >> 5) * NT;
-        if (area > 0 && area <= kFwdSmallBox) {
-            const unsigned bit = 1u << lane;
-            for (int y = cy0, i = 0; i < area; y++)
-                for (int x = cx0; x < cx0 + cw; x++, i++) atomicOr(crow + tile_lane<TS>(x, y), bit);
+        if (scan) {
+            // this pixel's candidates in submission order: the records whose box holds it
+            uint32_t got0 = 0, got1 = 0;
+            const int n0 = min(nb, 32);
+            for (int r = 0; r < n0; r++) {
+                const uint32_t b = rec.box[r];
+                got0 |= ((b >> lx) & (b >> (16 + ly)) & 1u) << r;
+            }
+            for (int r = 32; r < nb; r++) {
+                const uint32_t b = rec.box[r];
+                got1 |= ((b >> lx) & (b >> (16 + ly)) & 1u) << (r - 32);
+            }
+            cand[tid] = got0;  // the thread's own column: read back below without a barrier
+            cand[NT + tid] = got1;
+        } else {
+            // mark the candidates: small boxes by their record's thread, larger ones by the whole warp
+            uint32_t* crow = cand + (tid >> 5) * NT;
+            if (area > 0 && area <= kFwdSmallBox) {
+                const unsigned bit = 1u << lane;
+                for (int y = cy0, i = 0; i < area; y++)
+                    for (int x = cx0; x < cx0 + cw; x++, i++) atomicOr(crow + tile_lane<TS>(x, y), bit);
+            }
+            unsigned big = __ballot_sync(0xffffffffu, area > kFwdSmallBox);
+            while (big) {
+                const int l = __ffs(big) - 1;
+                big &= big - 1;
+                const int na = __shfl_sync(0xffffffffu, area, l), x0 = __shfl_sync(0xffffffffu, cx0, l);
+                const int y0 = __shfl_sync(0xffffffffu, cy0, l), w0 = __shfl_sync(0xffffffffu, cw, l);
+                for (int i = lane; i < na; i += 32) atomicOr(crow + tile_lane<TS>(x0 + i % w0, y0 + i / w0), 1u << l);
+            }
+            __syncthreads();
         }
-        unsigned big = __ballot_sync(0xffffffffu, area > kFwdSmallBox);
-        while (big) {
-            const int l = __ffs(big) - 1;
-            big &= big - 1;
-            const int na = __shfl_sync(0xffffffffu, area, l), x0 = __shfl_sync(0xffffffffu, cx0, l);
-            const int y0 = __shfl_sync(0xffffffffu, cy0, l), w0 = __shfl_sync(0xffffffffu, cw, l);
-            for (int i = lane; i < na; i += 32) atomicOr(crow + tile_lane<TS>(x0 + i % w0, y0 + i / w0), 1u << l);
-        }
-        __syncthreads();
         if (inpix) {
             // this pixel's candidates in submission order
-            for (int w = 0; w < NT / 32; w++) {
+            const int nw = scan ? kFwdScanBatch / 32 : NT / 32;
+            for (int w = 0; w < nw; w++) {
                 uint32_t bits = cand[w * NT + tid];
                 while (bits) {
                     const int r = w * 32 + __ffs(bits) - 1;
                     bits &= bits - 1;
+                    const int meta = rec.meta[r];
+                    if ((meta & 32) && !scissor_pass(a.draws[rec.draw[r]], px, py)) continue;
+                    const int func = (meta >> 1) & 7, write = (meta >> 4) & 1;
                     const int32_t A[3] = {rec.A[0][r], rec.A[1][r], rec.A[2][r]};
                     const int32_t B[3] = {rec.B[0][r], rec.B[1][r], rec.B[2][r]};
-                    const int64_t Cb[3] = {rec.Cb[0][r], rec.Cb[1][r], rec.Cb[2][r]};
-                    const DrawDev& d = a.draws[rec.draw[r]];
-                    if (!scissor_pass(d, px, py)) continue;
-                    const int func = d.depth_func, write = d.depth_write;
+                    unsigned cov = 0;  // covered samples (tile-relative edge functions)
+                    if (!(meta & kLargeRecord)) {
+                        int32_t e0[3];
+#pragma unroll
+                        for (int i = 0; i < 3; i++) e0[i] = (int32_t)rec.Et[i][r] + A[i] * (lx * 256) + B[i] * (ly * 256);
+#pragma unroll
+                        for (int k = 0; k < S; k++) {
+                            const int32_t c0 = e0[0] + A[0] * sample_x<S>(k) + B[0] * sample_y<S>(k);
+                            const int32_t c1 = e0[1] + A[1] * sample_x<S>(k) + B[1] * sample_y<S>(k);
+                            const int32_t c2 = e0[2] + A[2] * sample_x<S>(k) + B[2] * sample_y<S>(k);
+                            cov |= ((c0 | c1 | c2) >= 0 ? 1u : 0u) << k;
+                        }
+                    } else {
+                        const int64_t Et[3] = {rec.Et[0][r], rec.Et[1][r], rec.Et[2][r]};
+#pragma unroll
+                        for (int k = 0; k < S; k++)
+                            cov |= (covered(A, B, Et, lx * 256 + sample_x<S>(k), ly * 256 + sample_y<S>(k)) ? 1u : 0u) << k;
+                    }
+                    if (!cov) continue;
                     const int e = rec.key[r];
                     unsigned mask = 0;
 #pragma unroll
                     for (int k = 0; k < S; k++) {
                         const int32_t sx = px * 256 + sample_x<S>(k), sy = py * 256 + sample_y<S>(k);
-                        if (!covered(A, B, Cb, sx, sy)) continue;
+                        if (!(cov & (1u << k))) continue;
                         const float z = sample_depth(rec.z0[r], rec.dzdx[r], rec.dzdy[r], rec.X0[r], rec.Y0[r], sx, sy);
                         if (!depth_cmp(func, z, dep[k])) continue;
                         if (write) {
