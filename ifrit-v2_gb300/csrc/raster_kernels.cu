@@ -1808,6 +1808,16 @@ __device__ __forceinline__ void forward_tile(const PassArgs& a, const FragArgs& 
     // the depth target already holds dep[] after the raster stage; otherwise (cleared or earlier
     // content) it is written whatever happens
     bool dep_changed = !after_raster;
+    // Per-pixel occlusion test of candidates (views where depths only decrease, as for the tile
+    // test of the raster stage): a record under LESS / LEQUAL / EQUAL whose depth plane stays beyond
+    // the pixel's farthest depth over the pixel's sample range, by more than the evaluation's
+    // rounding bound, cannot pass at any of its samples.
+    const bool pix_cull = v.ordered_cull && inpix;
+    float dmax_pix = dep[0];
+#pragma unroll
+    for (int k = 1; k < S; k++) dmax_pix = fmaxf(dmax_pix, dep[k]);
+    const int32_t psx0 = px * 256 + v.c.smin_x, psx1 = px * 256 + v.c.smax_x;
+    const int32_t psy0 = py * 256 + v.c.smin_y, psy1 = py * 256 + v.c.smax_y;
     bool have_cols = bulk || (defer && after_raster);  // scol holds this thread's starting colours
     if (!defer && !bulk) {
         start_colours<S>(v, scol, ltile, after_raster, bg);
@@ -1981,8 +1991,16 @@ __device__ __forceinline__ void forward_tile(const PassArgs& a, const FragArgs& 
                     const int r = w * 32 + __ffs(bits) - 1;
                     bits &= bits - 1;
                     const int meta = rec.meta[r];
-                    if ((meta & 32) && !scissor_pass(a.draws[rec.draw[r]], px, py)) continue;
                     const int func = (meta >> 1) & 7, write = (meta >> 4) & 1;
+                    if (pix_cull && func >= 1 && func <= 3) {
+                        const float z0 = rec.z0[r], gx = rec.dzdx[r], gy = rec.dzdy[r];
+                        const float ax = gx * (float)(psx0 - rec.X0[r]), bx = gx * (float)(psx1 - rec.X0[r]);
+                        const float ay = gy * (float)(psy0 - rec.Y0[r]), by = gy * (float)(psy1 - rec.Y0[r]);
+                        const float zmin = (z0 + fminf(ax, bx)) + fminf(ay, by);
+                        const float margin = (fabsf(z0) + fmaxf(fabsf(ax), fabsf(bx)) + fmaxf(fabsf(ay), fabsf(by))) * 0x1p-20f;
+                        if (zmin - margin > dmax_pix) continue;
+                    }
+                    if ((meta & 32) && !scissor_pass(a.draws[rec.draw[r]], px, py)) continue;
                     const int32_t A[3] = {rec.A[0][r], rec.A[1][r], rec.A[2][r]};
                     const int32_t B[3] = {rec.B[0][r], rec.B[1][r], rec.B[2][r]};
                     unsigned cov = 0;  // covered samples (tile-relative edge functions)
