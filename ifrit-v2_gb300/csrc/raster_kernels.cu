@@ -1665,6 +1665,27 @@ struct FwdRecords {
 // Batches of up to this many records find each pixel's candidates by scanning the records' boxes;
 // larger batches mark them into per-pixel bitmasks from the records' side.
 constexpr int kFwdScanBatch = 64;
+// Per-warp buffer of candidate coverage masks (16 bits each) on the scanning path, which leaves the
+// candidate bitmasks unused: the buffers alias them (8 warps x 1 KB).
+constexpr int kFwdWarpCand = 512;
+
+// Position of the n-th (0-based) set bit of x, which has more than n set bits.
+__device__ __forceinline__ int nth_set_bit(uint32_t x, int n) {
+    int pos = 0;
+#pragma unroll
+    for (int w = 16; w >= 1; w >>= 1) {
+        const uint32_t low = x & ((1u << w) - 1u);
+        const int c = __popc(low);
+        if (n >= c) {
+            n -= c;
+            x >>= w;
+            pos += w;
+        } else {
+            x = low;
+        }
+    }
+    return pos;
+}
 
 constexpr int kFwdFrags = 8;      // fragments a pixel holds before they are shaded
 constexpr int kFwdSmallBox = 24;  // candidate boxes of up to this many pixels are marked by their record's thread
@@ -1739,7 +1760,7 @@ __device__ __forceinline__ void start_colours(const ViewArgs& v, float4* scol, i
 template <int S, bool DEFER>
 __device__ __forceinline__ void forward_tile(const PassArgs& a, const FragArgs& fa, const ViewArgs& v, int vi, int gtile,
                                              FwdRecords& rec, float4* scol_smem, uint32_t* list, int2* frags,
-                                             uint32_t* cand, bool after_raster, BulkState& bs) {
+                                             uint32_t* cand, uint16_t* wcov, bool after_raster, BulkState& bs) {
     constexpr int TS = 16, NT = kFwdThreads;
     // after the raster and shade stages the shade stage has finished the tiles without ordered
     // entries (uniform over the CTA)
@@ -1812,12 +1833,9 @@ __device__ __forceinline__ void forward_tile(const PassArgs& a, const FragArgs& 
     // test of the raster stage): a record under LESS / LEQUAL / EQUAL whose depth plane stays beyond
     // the pixel's farthest depth over the pixel's sample range, by more than the evaluation's
     // rounding bound, cannot pass at any of its samples.
-    const bool pix_cull = v.ordered_cull && inpix;
     float dmax_pix = dep[0];
 #pragma unroll
     for (int k = 1; k < S; k++) dmax_pix = fmaxf(dmax_pix, dep[k]);
-    const int32_t psx0 = px * 256 + v.c.smin_x, psx1 = px * 256 + v.c.smax_x;
-    const int32_t psy0 = py * 256 + v.c.smin_y, psy1 = py * 256 + v.c.smax_y;
     bool have_cols = bulk || (defer && after_raster);  // scol holds this thread's starting colours
     if (!defer && !bulk) {
         start_colours<S>(v, scol, ltile, after_raster, bg);
@@ -1950,20 +1968,137 @@ __device__ __forceinline__ void forward_tile(const PassArgs& a, const FragArgs& 
         }
         const bool scan = nb <= kFwdScanBatch;  // uniform
         __syncthreads();
+        // Coverage of record r at tile pixel (qlx, qly) (absolute (qpx, qpy), farthest depth qdmax):
+        // 0 when the per-pixel occlusion test or the scissor test rejects the record there.
+        auto cover = [&](int r, int qlx, int qly, int qpx, int qpy, float qdmax) -> unsigned {
+            const int meta = rec.meta[r];
+            const int func = (meta >> 1) & 7;
+            if (v.ordered_cull && func >= 1 && func <= 3) {
+                const float z0 = rec.z0[r], gx = rec.dzdx[r], gy = rec.dzdy[r];
+                const int32_t qx0 = qpx * 256 + v.c.smin_x, qx1 = qpx * 256 + v.c.smax_x;
+                const int32_t qy0 = qpy * 256 + v.c.smin_y, qy1 = qpy * 256 + v.c.smax_y;
+                const float ax = gx * (float)(qx0 - rec.X0[r]), bx = gx * (float)(qx1 - rec.X0[r]);
+                const float ay = gy * (float)(qy0 - rec.Y0[r]), by = gy * (float)(qy1 - rec.Y0[r]);
+                const float zmin = (z0 + fminf(ax, bx)) + fminf(ay, by);
+                const float margin = (fabsf(z0) + fmaxf(fabsf(ax), fabsf(bx)) + fmaxf(fabsf(ay), fabsf(by))) * 0x1p-20f;
+                if (zmin - margin > qdmax) return 0u;
+            }
+            if ((meta & 32) && !scissor_pass(a.draws[rec.draw[r]], qpx, qpy)) return 0u;
+            const int32_t A[3] = {rec.A[0][r], rec.A[1][r], rec.A[2][r]};
+            const int32_t B[3] = {rec.B[0][r], rec.B[1][r], rec.B[2][r]};
+            unsigned cov = 0;  // tile-relative edge functions
+            if (!(meta & kLargeRecord)) {
+                int32_t e0[3];
+#pragma unroll
+                for (int i = 0; i < 3; i++) e0[i] = (int32_t)rec.Et[i][r] + A[i] * (qlx * 256) + B[i] * (qly * 256);
+#pragma unroll
+                for (int k = 0; k < S; k++) {
+                    const int32_t c0 = e0[0] + A[0] * sample_x<S>(k) + B[0] * sample_y<S>(k);
+                    const int32_t c1 = e0[1] + A[1] * sample_x<S>(k) + B[1] * sample_y<S>(k);
+                    const int32_t c2 = e0[2] + A[2] * sample_x<S>(k) + B[2] * sample_y<S>(k);
+                    cov |= ((c0 | c1 | c2) >= 0 ? 1u : 0u) << k;
+                }
+            } else {
+                const int64_t Et[3] = {rec.Et[0][r], rec.Et[1][r], rec.Et[2][r]};
+#pragma unroll
+                for (int k = 0; k < S; k++)
+                    cov |= (covered(A, B, Et, qlx * 256 + sample_x<S>(k), qly * 256 + sample_y<S>(k)) ? 1u : 0u) << k;
+            }
+            return cov;
+        };
+        // Depth tests of this thread's covered samples of record r, then the fragment record.
+        auto apply = [&](int r, unsigned cov) {
+            const int meta = rec.meta[r];
+            const int func = (meta >> 1) & 7, write = (meta >> 4) & 1;
+            const int e = rec.key[r];
+            unsigned mask = 0;
+#pragma unroll
+            for (int k = 0; k < S; k++) {
+                const int32_t sx = px * 256 + sample_x<S>(k), sy = py * 256 + sample_y<S>(k);
+                if (!(cov & (1u << k))) continue;
+                const float z = sample_depth(rec.z0[r], rec.dzdx[r], rec.dzdy[r], rec.X0[r], rec.Y0[r], sx, sy);
+                if (!depth_cmp(func, z, dep[k])) continue;
+                if (write) {
+                    dep_changed |= __float_as_uint(dep[k]) != __float_as_uint(z);
+                    dep[k] = z;
+                }
+                vid[k] = (e >> 3) - v.first_tri;
+                mask |= 1u << k;
+            }
+            if (!mask) return;
+            // colours never change depth: record the fragment now, shade it later
+            if (nfrag == kFwdFrags) {  // a full list is applied on the spot (rare)
+                if (!have_cols) start_colours<S>(v, scol, ltile, after_raster, bg);
+                have_cols = true;
+                apply_fragments<S>(a, v, px, py, scol, frags, nfrag);
+                nfrag = 0;
+                flushed = true;
+            }
+            frags[nfrag * NT + tid] = make_int2(e, (int)(mask | ((unsigned)rec.draw[r] << 16)));
+            nfrag++;
+        };
         if (scan) {
-            // this pixel's candidates in submission order: the records whose box holds it
+            // this pixel's candidates: the records whose box holds it (bit r of got[r / 32])
             uint32_t got0 = 0, got1 = 0;
-            const int n0 = min(nb, 32);
-            for (int r = 0; r < n0; r++) {
-                const uint32_t b = rec.box[r];
-                got0 |= ((b >> lx) & (b >> (16 + ly)) & 1u) << r;
+            if (inpix) {
+                const int n0 = min(nb, 32);
+                for (int r = 0; r < n0; r++) {
+                    const uint32_t b = rec.box[r];
+                    got0 |= ((b >> lx) & (b >> (16 + ly)) & 1u) << r;
+                }
+                for (int r = 32; r < nb; r++) {
+                    const uint32_t b = rec.box[r];
+                    got1 |= ((b >> lx) & (b >> (16 + ly)) & 1u) << (r - 32);
+                }
             }
-            for (int r = 32; r < nb; r++) {
-                const uint32_t b = rec.box[r];
-                got1 |= ((b >> lx) & (b >> (16 + ly)) & 1u) << (r - 32);
+            // The warp's (pixel, record) candidates in lane-major order; their coverage tests are
+            // spread over all lanes (chunks of kFwdWarpCand), then every lane applies its own in
+            // submission order.
+            const int myc = __popc(got0) + __popc(got1);
+            int incl = myc;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int q = __shfl_up_sync(0xffffffffu, incl, o);
+                if (lane >= o) incl += q;
             }
-            cand[tid] = got0;  // the thread's own column: read back below without a barrier
-            cand[NT + tid] = got1;
+            const int T = __shfl_sync(0xffffffffu, incl, 31), pre = incl - myc;
+            uint16_t* wc = wcov + (tid >> 5) * kFwdWarpCand;
+            uint32_t left0 = got0, left1 = got1;  // this lane's candidates not applied yet
+            for (int c0 = 0; c0 < T; c0 += kFwdWarpCand) {
+                const int cn = min(kFwdWarpCand, T - c0);
+                for (int jb = 0; jb < cn; jb += 32) {
+                    const int j = c0 + jb + lane;
+                    int o = 0;  // owner lane: the last lane whose first candidate is at or before j
+#pragma unroll
+                    for (int step = 16; step > 0; step >>= 1)
+                        if (__shfl_sync(0xffffffffu, pre, o + step) <= j) o += step;
+                    const int opre = __shfl_sync(0xffffffffu, pre, o);
+                    const uint32_t og0 = __shfl_sync(0xffffffffu, got0, o), og1 = __shfl_sync(0xffffffffu, got1, o);
+                    const float odmax = __shfl_sync(0xffffffffu, dmax_pix, o);
+                    if (jb + lane < cn) {
+                        const int idx = j - opre, n0 = __popc(og0);
+                        const int r = idx < n0 ? nth_set_bit(og0, idx) : 32 + nth_set_bit(og1, idx - n0);
+                        int olx, oly;
+                        tile_pixel<TS>((tid & ~31) + o, olx, oly);
+                        wc[jb + lane] = (uint16_t)cover(r, olx, oly, tx * TS + olx, ty * TS + oly, odmax);
+                    }
+                }
+                __syncwarp();
+                const int lo = max(pre, c0), hi = min(pre + myc, c0 + cn);
+                for (int jj = lo; jj < hi; jj++) {
+                    int r;
+                    if (left0) {
+                        r = __ffs(left0) - 1;
+                        left0 &= left0 - 1;
+                    } else {
+                        r = 32 + __ffs(left1) - 1;
+                        left1 &= left1 - 1;
+                    }
+                    const unsigned cov = wc[jj - c0];
+                    if (cov) apply(r, cov);
+                }
+                __syncwarp();
+            }
         } else {
             // mark the candidates: small boxes by their record's thread, larger ones by the whole warp
             uint32_t* crow = cand + (tid >> 5) * NT;
@@ -1981,73 +2116,16 @@ __device__ __forceinline__ void forward_tile(const PassArgs& a, const FragArgs& 
                 for (int i = lane; i < na; i += 32) atomicOr(crow + tile_lane<TS>(x0 + i % w0, y0 + i / w0), 1u << l);
             }
             __syncthreads();
-        }
-        if (inpix) {
-            // this pixel's candidates in submission order
-            const int nw = scan ? kFwdScanBatch / 32 : NT / 32;
-            for (int w = 0; w < nw; w++) {
-                uint32_t bits = cand[w * NT + tid];
-                while (bits) {
-                    const int r = w * 32 + __ffs(bits) - 1;
-                    bits &= bits - 1;
-                    const int meta = rec.meta[r];
-                    const int func = (meta >> 1) & 7, write = (meta >> 4) & 1;
-                    if (pix_cull && func >= 1 && func <= 3) {
-                        const float z0 = rec.z0[r], gx = rec.dzdx[r], gy = rec.dzdy[r];
-                        const float ax = gx * (float)(psx0 - rec.X0[r]), bx = gx * (float)(psx1 - rec.X0[r]);
-                        const float ay = gy * (float)(psy0 - rec.Y0[r]), by = gy * (float)(psy1 - rec.Y0[r]);
-                        const float zmin = (z0 + fminf(ax, bx)) + fminf(ay, by);
-                        const float margin = (fabsf(z0) + fmaxf(fabsf(ax), fabsf(bx)) + fmaxf(fabsf(ay), fabsf(by))) * 0x1p-20f;
-                        if (zmin - margin > dmax_pix) continue;
+            if (inpix) {
+                // this pixel's candidates in submission order
+                for (int w = 0; w < NT / 32; w++) {
+                    uint32_t bits = cand[w * NT + tid];
+                    while (bits) {
+                        const int r = w * 32 + __ffs(bits) - 1;
+                        bits &= bits - 1;
+                        const unsigned cov = cover(r, lx, ly, px, py, dmax_pix);
+                        if (cov) apply(r, cov);
                     }
-                    if ((meta & 32) && !scissor_pass(a.draws[rec.draw[r]], px, py)) continue;
-                    const int32_t A[3] = {rec.A[0][r], rec.A[1][r], rec.A[2][r]};
-                    const int32_t B[3] = {rec.B[0][r], rec.B[1][r], rec.B[2][r]};
-                    unsigned cov = 0;  // covered samples (tile-relative edge functions)
-                    if (!(meta & kLargeRecord)) {
-                        int32_t e0[3];
-#pragma unroll
-                        for (int i = 0; i < 3; i++) e0[i] = (int32_t)rec.Et[i][r] + A[i] * (lx * 256) + B[i] * (ly * 256);
-#pragma unroll
-                        for (int k = 0; k < S; k++) {
-                            const int32_t c0 = e0[0] + A[0] * sample_x<S>(k) + B[0] * sample_y<S>(k);
-                            const int32_t c1 = e0[1] + A[1] * sample_x<S>(k) + B[1] * sample_y<S>(k);
-                            const int32_t c2 = e0[2] + A[2] * sample_x<S>(k) + B[2] * sample_y<S>(k);
-                            cov |= ((c0 | c1 | c2) >= 0 ? 1u : 0u) << k;
-                        }
-                    } else {
-                        const int64_t Et[3] = {rec.Et[0][r], rec.Et[1][r], rec.Et[2][r]};
-#pragma unroll
-                        for (int k = 0; k < S; k++)
-                            cov |= (covered(A, B, Et, lx * 256 + sample_x<S>(k), ly * 256 + sample_y<S>(k)) ? 1u : 0u) << k;
-                    }
-                    if (!cov) continue;
-                    const int e = rec.key[r];
-                    unsigned mask = 0;
-#pragma unroll
-                    for (int k = 0; k < S; k++) {
-                        const int32_t sx = px * 256 + sample_x<S>(k), sy = py * 256 + sample_y<S>(k);
-                        if (!(cov & (1u << k))) continue;
-                        const float z = sample_depth(rec.z0[r], rec.dzdx[r], rec.dzdy[r], rec.X0[r], rec.Y0[r], sx, sy);
-                        if (!depth_cmp(func, z, dep[k])) continue;
-                        if (write) {
-                            dep_changed |= __float_as_uint(dep[k]) != __float_as_uint(z);
-                            dep[k] = z;
-                        }
-                        vid[k] = (e >> 3) - v.first_tri;
-                        mask |= 1u << k;
-                    }
-                    if (!mask) continue;
-                    // colours never change depth: record the fragment now, shade it later
-                    if (nfrag == kFwdFrags) {  // a full list is applied on the spot (rare)
-                        if (!have_cols) start_colours<S>(v, scol, ltile, after_raster, bg);
-                        have_cols = true;
-                        apply_fragments<S>(a, v, px, py, scol, frags, nfrag);
-                        nfrag = 0;
-                        flushed = true;
-                    }
-                    frags[nfrag * NT + tid] = make_int2(e, (int)(mask | ((unsigned)rec.draw[r] << 16)));
-                    nfrag++;
                 }
             }
         }
@@ -2163,6 +2241,9 @@ __global__ void __launch_bounds__(kFwdThreads, 2) forward_kernel(PassArgs a, Fra
         reinterpret_cast<uint32_t*>(smem_raw + sizeof(FwdRecords) + (DEFER ? 0 : sizeof(float4) * S * kFwdThreads));
     int2* frags = reinterpret_cast<int2*>(list + kOrderedCap);  // [kFwdFrags][256]
     uint32_t* cand = reinterpret_cast<uint32_t*>(frags + kFwdFrags * kFwdThreads);  // [8][256]
+    uint16_t* wcov = reinterpret_cast<uint16_t*>(cand);  // [8][kFwdWarpCand], aliases cand
+    static_assert(sizeof(uint16_t) * kFwdWarpCand * (kFwdThreads / 32) <= sizeof(uint32_t) * kFwdThreads * (kFwdThreads / 32),
+                  "coverage buffers fit the candidate masks");
     __shared__ ViewArgs sv;
     __shared__ int s_tile, s_view;
     __shared__ __align__(8) uint64_t s_bar;
@@ -2177,7 +2258,7 @@ __global__ void __launch_bounds__(kFwdThreads, 2) forward_kernel(PassArgs a, Fra
     }
     __syncthreads();
     while (next_tile<kFwdThreads>(a, g, qslot, sv, s_tile, s_view))
-        forward_tile<S, DEFER>(a, fa, sv, s_view, s_tile, rec, scol, list, frags, cand, after_raster != 0, bs);
+        forward_tile<S, DEFER>(a, fa, sv, s_view, s_tile, rec, scol, list, frags, cand, wcov, after_raster != 0, bs);
     if (bs.pending && threadIdx.x == 0) mbar_wait(&s_bar, (bs.phase - 1) & 1u);  // a copy that did not land in time
 }
 
