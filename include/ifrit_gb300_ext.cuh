@@ -22,6 +22,13 @@
  * averaged into the caller's output as the built-in resolve does.  ifrit_ext::Gouraud is the
  * built-in GOURAUD model as a functor (bit-identical to the renderer's own output).
  *
+ * Vertex stage (the reference's VertexShader::execute, Shaders.h:46-56):
+ *   struct MyVertex { __device__ void operator()(int i, float clip[4], float attr[4]) const; };
+ *   ifrit_ext::draw_vertex_stage(renderer, MyVertex{...}, num_vertices, d_indices, num_indices,
+ *                                d_positions, d_attributes, d_counts, attr_count, clear, stream);
+ * runs the functor once per vertex (clip-space position and one float4 varying out) and draws the
+ * caller's triangle list over its outputs (iftrDrawMeshOutputs with one work group).
+ *
  * Mesh / task / geometry stage (the reference's MeshShader / TaskShader / GeometryShader
  * objects, MeshShadingStage / GeneralGeometryStage, TileRasterCoreInvocationCuda.cu:355-561):
  *   struct MyMesh {
@@ -316,6 +323,26 @@ __global__ void task_mesh_kernel(Mesh mesh, const int* offsets, int tasks, int m
     for (int j = threadIdx.x; j < ni; j += blockDim.x) indices[(size_t)g * max_i + j] = mesh.index(t, sub, j);
 }
 
+// One thread per vertex: the vertex functor's outputs; thread 0 also writes the group's counts.
+template <class Vertex>
+__global__ void vertex_stage_kernel(Vertex vs, int num_vertices, int num_indices, float* positions, float* attributes,
+                                    int* counts) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i == 0) {
+        counts[0] = num_vertices;
+        counts[1] = num_indices;
+    }
+    if (i >= num_vertices) return;
+    float clip[4], attr[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+    vs(i, clip, attr);
+    float* pp = positions + (size_t)i * 4;
+    pp[0] = clip[0]; pp[1] = clip[1]; pp[2] = clip[2]; pp[3] = clip[3];
+    if (attributes) {
+        float* ap = attributes + (size_t)i * 4;
+        ap[0] = attr[0]; ap[1] = attr[1]; ap[2] = attr[2]; ap[3] = attr[3];
+    }
+}
+
 }  // namespace detail
 
 // Shades every pixel of a visibility buffer with `shader` into p.color (see the file comment).
@@ -381,6 +408,25 @@ int draw_mesh_stage(IfritGbRenderer* h, const Mesh& mesh, int groups, int max_v,
     }
     return iftrDrawMeshOutputs(h, groups, slots.positions, attr_count > 0 ? slots.attributes : nullptr, attr_count,
                                slots.indices, slots.num_vertices, slots.num_indices, max_v, max_i, clear);
+}
+
+// Runs the vertex functor over `num_vertices` vertices into positions / attributes ([V][4] floats
+// each, caller device memory; attributes may be NULL with attr_count 0) and draws the triangle list
+// indices[num_indices] (device, a multiple of 3) over them with the current state.  counts: caller
+// device memory of 2 ints.  Returns an IFTR_* status.
+template <class Vertex>
+int draw_vertex_stage(IfritGbRenderer* h, const Vertex& vs, int num_vertices, const int* indices, int num_indices,
+                      float* positions, float* attributes, int* counts, int attr_count, int clear, cudaStream_t stream) {
+    if (!h || num_vertices <= 0 || num_indices <= 0 || num_indices % 3 || !indices || !positions || !counts ||
+        (attr_count > 0 && !attributes))
+        return IFTR_ERR_INVALID_ARG;
+    int rc = iftrSetStream(h, stream);
+    if (rc) return rc;
+    detail::vertex_stage_kernel<Vertex><<<(num_vertices + 255) / 256, 256, 0, stream>>>(
+        vs, num_vertices, num_indices, positions, attr_count > 0 ? attributes : nullptr, counts);
+    if (cudaGetLastError() != cudaSuccess) return IFTR_ERR_CUDA;
+    return iftrDrawMeshOutputs(h, 1, positions, attr_count > 0 ? attributes : nullptr, attr_count, indices, counts,
+                               counts + 1, num_vertices, num_indices, clear);
 }
 
 // Runs `task` over `tasks` task groups, then `mesh` over the mesh groups they spawn (at most

@@ -4,6 +4,7 @@
 //   ext_shade(which, ...)   which 0: ifrit_ext::Gouraud, 1: AttrDerivShader (below)
 //   ext_draw_grid(...)      GridMesh as the mesh stage, drawn through iftrDrawMeshOutputs
 //   ext_draw_task_grid(...) TaskSpawn + TaskGrid as the task and mesh stages
+//   ext_draw_vertices(...)  ScaleVertex as the vertex stage over an indexed mesh
 #include "ifrit_gb300_ext.cuh"
 
 // Uses the attribute, both quad derivatives and the triangle index, so every field of the
@@ -121,4 +122,32 @@ extern "C" int ext_draw_task_grid(IfritGbRenderer* h, int tasks, int nx, const f
     ifrit_ext::MeshSlots slots{positions, attributes, indices, num_vertices, num_indices};
     return ifrit_ext::draw_task_mesh_stage(h, TaskSpawn{}, m, tasks, max_groups, 4, 6, slots, offsets, 4, clear,
                                            static_cast<cudaStream_t>(stream));
+}
+
+// Vertex i of an (x y z r g b) AoS array scaled by 1 + (i % 3) / 8 about the origin (exact factors),
+// transformed by `mvp` in the vertex stage's row order; the varying is the colour with alpha 0.5.
+struct ScaleVertex {
+    const float* vertices;
+    float mvp[16];
+    __device__ void operator()(int i, float clip[4], float attr[4]) const {
+        const float* v = vertices + (size_t)i * 6;
+        const float f = 1.0f + (float)(i % 3) * 0.125f;
+        const float p[3] = {v[0] * f, v[1] * f, v[2] * f};
+        for (int r = 0; r < 4; r++)
+            clip[r] = ((mvp[4 * r + 0] * p[0] + mvp[4 * r + 1] * p[1]) + mvp[4 * r + 2] * p[2]) + mvp[4 * r + 3];
+        attr[0] = v[3];
+        attr[1] = v[4];
+        attr[2] = v[5];
+        attr[3] = 0.5f;
+    }
+};
+
+extern "C" int ext_draw_vertices(IfritGbRenderer* h, const float* vertices, int num_vertices, const int* indices,
+                                 int num_indices, const float* mvp, float* positions, float* attributes, int* counts,
+                                 int clear, void* stream) {
+    ScaleVertex vs;
+    vs.vertices = vertices;
+    std::memcpy(vs.mvp, mvp, sizeof(vs.mvp));
+    return ifrit_ext::draw_vertex_stage(h, vs, num_vertices, indices, num_indices, positions, attributes, counts, 4,
+                                        clear, static_cast<cudaStream_t>(stream));
 }

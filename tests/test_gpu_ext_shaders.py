@@ -12,6 +12,7 @@ linked against libifrit_gb300.so) and called through ctypes:
   (so the chain oracle -> built-in -> functor is pinned);
 * a functor-driven mesh stage (a grid, some groups empty or short) drawn through
   iftrDrawMeshOutputs matches the oracle drawing the same indexed mesh;
+* a vertex functor over an indexed mesh matches the oracle drawing the host-transformed mesh;
 * a task functor spawning 0-3 mesh groups per task group, with the mesh functor run per (task, sub),
   matches the oracle drawing the cells in (task, sub) order, and too many spawned groups return
   IFTR_ERR_OVERFLOW."""
@@ -46,6 +47,8 @@ def ext():
     lib.ext_draw_grid.restype = ip
     lib.ext_draw_task_grid.argtypes = [vp, ip, ip, vp, vp, vp, vp, vp, vp, vp, ip, ip, vp]
     lib.ext_draw_task_grid.restype = ip
+    lib.ext_draw_vertices.argtypes = [vp, vp, ip, vp, ip, vp, vp, vp, vp, ip, vp]
+    lib.ext_draw_vertices.restype = ip
     return lib
 
 
@@ -236,3 +239,33 @@ def test_functor_task_stage_matches_oracle(ext, S):
                    nthreads=os.cpu_count() or 1)
     assert_parity(gpu, ref)
     assert (gpu["vis"] >= 0).sum() > W * H // 8
+
+
+@pytest.mark.parametrize("S", [1, 4])
+def test_functor_vertex_stage_matches_oracle(ext, S):
+    v, f, mvp = scenes.c1_scene(9)
+    W, H = 192, 160
+    V = len(v)
+    dev = torch.device("cuda")
+    dv = torch.from_numpy(_f32(v)).to(dev)
+    di = torch.from_numpy(np.ascontiguousarray(f, np.int32).reshape(-1)).to(dev)
+    pos = torch.zeros((V, 4), dtype=torch.float32, device=dev)
+    att = torch.zeros((V, 4), dtype=torch.float32, device=dev)
+    counts = torch.zeros(2, dtype=torch.int32, device=dev)
+    r = ig.Renderer(W, H, S, ig.FORMAT_RGBA32F, visibility=True)
+    r.set_state(cull=ig.CULL_BACK, depth_func=ig.LESS, shading=ig.FS_GOURAUD, clear_color=BG)
+    m = _f32(mvp).reshape(-1)
+    rc = ext.ext_draw_vertices(r.h, dv.data_ptr(), V, di.data_ptr(), f.size, m.ctypes.data, pos.data_ptr(),
+                               att.data_ptr(), counts.data_ptr(), 1, torch.cuda.current_stream().cuda_stream)
+    assert rc == 0, "draw_vertex_stage returned %d" % rc
+    gpu = {"color": r.color(), "depth": r.depth(), "vis": r.visibility()}
+    r.close()
+    # host restatement of ScaleVertex: scaled positions, colour + alpha 0.5 as the varying
+    fac = (np.float32(1.0) + (np.arange(V) % 3).astype(np.float32) * np.float32(0.125)).astype(np.float32)
+    vh = np.concatenate([(v[:, :3] * fac[:, None]).astype(np.float32), v[:, 3:6],
+                         np.full((V, 1), 0.5, np.float32)], 1).astype(np.float32)
+    d = O.make_draw(vh, f, mvp, attr_offset=3, attr_count=4, cull_mode=ig.CULL_BACK, depth_func=ig.LESS)
+    ref = O.render([d], W, H, S, FMT_TO_ORACLE[ig.FORMAT_RGBA32F], clear=True, clear_color=BG,
+                   nthreads=os.cpu_count() or 1)
+    assert_parity(gpu, ref, fmt=ig.FORMAT_RGBA32F)
+    assert (gpu["vis"] >= 0).mean() > 0.2
