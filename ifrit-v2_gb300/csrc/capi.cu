@@ -132,7 +132,7 @@ uint64_t g_id_counter = 1;
 // bumps `generation`, which invalidates CUDA graphs captured with the old addresses.
 struct PassScratch {
     DevMem tile_count, tile_offset, tile_cursor, block_sums, pairs, records, attrs, status, desc, queues, entries,
-        sample_colors, frags, frag_cols, fwd_tiles, fwd_pix_end;
+        sample_colors, frags, frag_cols, fwd_tiles, fwd_pix_end, redo_tiles;
     // the pass descriptors share one block (one upload per pass): draws | draw starts | views | view
     // tile starts, each at a 256-byte offset sized for cap_draws / cap_views
     size_t cap_draws = 0, cap_views = 0, off_draw_start = 0, off_views = 0, off_view_tiles = 0;
@@ -147,7 +147,7 @@ struct PassScratch {
     bool staged_pending = false;
     void release() {
         for (DevMem* m : {&tile_count, &tile_offset, &tile_cursor, &block_sums, &pairs, &records, &attrs, &status, &desc,
-                          &queues, &entries, &sample_colors, &frags, &frag_cols, &fwd_tiles, &fwd_pix_end})
+                          &queues, &entries, &sample_colors, &frags, &frag_cols, &fwd_tiles, &fwd_pix_end, &redo_tiles})
             m->release();
         if (h_status) cudaFreeHost(h_status);
         h_status = nullptr;
@@ -409,6 +409,7 @@ PassArgs make_args(const PassScratch& s, int ndraws, int total_tris, int nviews,
 int reserve_fragments(IfritGbRenderer* h, PassScratch& s, size_t tiles, size_t pixels) {
     IFTR_CUDA(h, s.fwd_tiles.reserve(std::max<size_t>(1, tiles) * sizeof(uint4)));
     IFTR_CUDA(h, s.fwd_pix_end.reserve(std::max<size_t>(1, tiles) * 256 * sizeof(uint16_t)));
+    IFTR_CUDA(h, s.redo_tiles.reserve(std::max<size_t>(1, tiles) * sizeof(uint32_t)));
     size_t want = h->frag_capacity_setting > 0 ? (size_t)h->frag_capacity_setting
                                                : std::max(s.frag_want, std::max<size_t>(1u << 20, pixels));
     want = std::min<size_t>(want, 0xFFFFFFF0u);
@@ -425,6 +426,7 @@ ifr::FragArgs fragment_args(const PassScratch& s) {
     f.frag_capacity = s.frag_capacity;
     f.fwd_tiles = s.fwd_tiles.as<uint4>();
     f.fwd_pix_end = s.fwd_pix_end.as<uint16_t>();
+    f.redo_tiles = s.redo_tiles.as<uint32_t>();
     return f;
 }
 

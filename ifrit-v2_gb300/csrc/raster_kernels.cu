@@ -1687,7 +1687,8 @@ __device__ __forceinline__ int nth_set_bit(uint32_t x, int n) {
     return pos;
 }
 
-constexpr int kFwdFrags = 8;      // fragments a pixel holds before they are shaded
+constexpr int kFwdFrags = 8;      // fragments a pixel holds before they are shaded (in-stage form)
+constexpr int kFwdFragsDefer = 6; // fragments a pixel records in the deferring form (more: the tile is redone)
 constexpr int kFwdSmallBox = 24;  // candidate boxes of up to this many pixels are marked by their record's thread
 
 // Lane of pixel (lx, ly) of a TS x TS tile (inverse of tile_pixel).
@@ -1770,7 +1771,8 @@ __device__ __forceinline__ void forward_tile(const PassArgs& a, const FragArgs& 
     // the tile-major hand-off) come in by one bulk copy (TMA) that overlaps the gathering and
     // sorting below.
     constexpr bool defer = DEFER;
-    float4* scol = DEFER ? v.sample_colors + (size_t)ltile * S * NT : scol_smem;
+    constexpr int kMaxFrags = DEFER ? kFwdFragsDefer : kFwdFrags;
+    float4* scol = scol_smem;  // the in-stage form's per-sample colours (the deferring form uses none)
     const bool bulk = after_raster && bs.ok && !defer;
     if (bulk && threadIdx.x == 0)
         bulk_load(scol, v.sample_colors + (size_t)ltile * S * NT, (uint32_t)(sizeof(float4) * S * NT), bs.bar);
@@ -1829,6 +1831,7 @@ __device__ __forceinline__ void forward_tile(const PassArgs& a, const FragArgs& 
     // the depth target already holds dep[] after the raster stage; otherwise (cleared or earlier
     // content) it is written whatever happens
     bool dep_changed = !after_raster;
+    bool too_many = false;  // deferring form: a pixel passed more than kFwdFragsDefer fragments
     // Per-pixel occlusion test of candidates (views where depths only decrease, as for the tile
     // test of the raster stage): a record under LESS / LEQUAL / EQUAL whose depth plane stays beyond
     // the pixel's farthest depth over the pixel's sample range, by more than the evaluation's
@@ -1836,12 +1839,11 @@ __device__ __forceinline__ void forward_tile(const PassArgs& a, const FragArgs& 
     float dmax_pix = dep[0];
 #pragma unroll
     for (int k = 1; k < S; k++) dmax_pix = fmaxf(dmax_pix, dep[k]);
-    bool have_cols = bulk || (defer && after_raster);  // scol holds this thread's starting colours
+    bool have_cols = bulk;  // scol holds this thread's starting colours (in-stage form)
     if (!defer && !bulk) {
         start_colours<S>(v, scol, ltile, after_raster, bg);
         have_cols = true;
     }
-    bool flushed = false;  // this pixel applied fragments on the spot
     const bool has_list = a.total_tris > 0 && a.status[ST_OVERFLOW] == 0;
     const uint32_t beg = has_list ? a.tile_offset[gtile] : 0u;
     const uint32_t end = has_list ? a.tile_offset[gtile + 1] : 0u;
@@ -2027,12 +2029,16 @@ __device__ __forceinline__ void forward_tile(const PassArgs& a, const FragArgs& 
             }
             if (!mask) return;
             // colours never change depth: record the fragment now, shade it later
-            if (nfrag == kFwdFrags) {  // a full list is applied on the spot (rare)
-                if (!have_cols) start_colours<S>(v, scol, ltile, after_raster, bg);
-                have_cols = true;
-                apply_fragments<S>(a, v, px, py, scol, frags, nfrag);
-                nfrag = 0;
-                flushed = true;
+            if (nfrag == kMaxFrags) {
+                if constexpr (DEFER) {  // the in-stage form redoes this tile
+                    too_many = true;
+                    return;
+                } else {  // a full list is applied on the spot (rare)
+                    if (!have_cols) start_colours<S>(v, scol, ltile, after_raster, bg);
+                    have_cols = true;
+                    apply_fragments<S>(a, v, px, py, scol, frags, nfrag);
+                    nfrag = 0;
+                }
             }
             frags[nfrag * NT + tid] = make_int2(e, (int)(mask | ((unsigned)rec.draw[r] << 16)));
             nfrag++;
@@ -2131,70 +2137,68 @@ __device__ __forceinline__ void forward_tile(const PassArgs& a, const FragArgs& 
         }
         __syncthreads();
     }
-    if (defer) {
-        // Hand the tile's fragments to the fragment kernels, pixel-major in lane order, unless a
-        // pixel already applied some on the spot or the fragment buffer is full (then the tile is
-        // finished here).  Depth and primitive ids are final now.
+    if constexpr (DEFER) {
+        // Hand the tile's fragments to the fragment kernels, pixel-major in lane order.  A tile with a
+        // pixel of more than kFwdFragsDefer fragments, or whose fragments do not fit the buffer, writes
+        // nothing and goes to the redo list: the in-stage form finishes it from the same inputs.
         __shared__ uint32_t s_wsum[NT / 32];
         __shared__ int s_slot;
         __shared__ uint32_t s_base;
-        if (!__syncthreads_or(flushed)) {
-            uint32_t incl = (uint32_t)nfrag;
+        if (__syncthreads_or(too_many)) {
+            if (tid == 0) fa.redo_tiles[atomicAdd(a.status + ST_REDO, 1u)] = (uint32_t)gtile;
+            return;
+        }
+        uint32_t incl = (uint32_t)nfrag;
 #pragma unroll
-            for (int o = 1; o < 32; o <<= 1) {
-                const uint32_t q = __shfl_up_sync(0xffffffffu, incl, o);
-                if (lane >= o) incl += q;
-            }
-            if (lane == 31) s_wsum[tid >> 5] = incl;
-            __syncthreads();
-            uint32_t before = 0, total = 0;
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t q = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += q;
+        }
+        if (lane == 31) s_wsum[tid >> 5] = incl;
+        __syncthreads();
+        uint32_t before = 0, total = 0;
 #pragma unroll
-            for (int w = 0; w < NT / 32; w++) {
-                const uint32_t x = s_wsum[w];
-                before += w < (tid >> 5) ? x : 0u;
-                total += x;
+        for (int w = 0; w < NT / 32; w++) {
+            const uint32_t x = s_wsum[w];
+            before += w < (tid >> 5) ? x : 0u;
+            total += x;
+        }
+        const uint32_t pre = before + incl - (uint32_t)nfrag;
+        if (tid == 0) {
+            int slot = -1;
+            const uint32_t fbase = total ? atomicAdd(a.status + ST_FRAGS, total) : 0u;
+            if ((unsigned long long)fbase + total <= fa.frag_capacity) {
+                slot = (int)atomicAdd(a.status + ST_FWD_TILES, 1u);
+                fa.fwd_tiles[slot] = make_uint4((uint32_t)gtile, fbase, (uint32_t)vi, after_raster ? 1u : 0u);
+            } else {  // later allocations fail too: the fragments below this one are all written
+                atomicMax(a.status + ST_FRAG_FAIL, 0xFFFFFFFFu - fbase);
+                const unsigned long long want = (unsigned long long)fbase + total;
+                atomicMax(a.status + ST_MAX_FRAGS, want > 0xFFFFFFFFull ? 0xFFFFFFFFu : (uint32_t)want);
+                fa.redo_tiles[atomicAdd(a.status + ST_REDO, 1u)] = (uint32_t)gtile;
             }
-            const uint32_t pre = before + incl - (uint32_t)nfrag;
-            if (tid == 0) {
-                int slot = -1;
-                uint32_t fbase = 0;
-                if (total > 0) {
-                    fbase = atomicAdd(a.status + ST_FRAGS, total);
-                    if ((unsigned long long)fbase + total <= fa.frag_capacity) {
-                        slot = (int)atomicAdd(a.status + ST_FWD_TILES, 1u);
-                        fa.fwd_tiles[slot] = make_uint4((uint32_t)gtile, fbase, (uint32_t)vi, after_raster ? 1u : 0u);
-                    } else {  // later allocations fail too: the fragments below this one are all written
-                        atomicMax(a.status + ST_FRAG_FAIL, 0xFFFFFFFFu - fbase);
-                        const unsigned long long want = (unsigned long long)fbase + total;
-                        atomicMax(a.status + ST_MAX_FRAGS, want > 0xFFFFFFFFull ? 0xFFFFFFFFu : (uint32_t)want);
-                    }
-                }
-                s_slot = slot;
-                s_base = fbase;
-            }
-            __syncthreads();
-            const int slot = s_slot;
-            if (slot >= 0) {
-                uint4* out = fa.frags + s_base + pre;
-                for (int i = 0; i < nfrag; i++) {
-                    const int2 f = frags[i * NT + tid];
-                    out[i] = make_uint4((uint32_t)f.x, (uint32_t)px | ((uint32_t)py << 16), (uint32_t)f.y & 0xffffu,
-                                        (uint32_t)f.y >> 16);
-                }
-                fa.fwd_pix_end[(size_t)slot * NT + tid] = (uint16_t)(pre + nfrag);
-                if (inpix) {
-                    if (dep_changed) store_depth<S>(v.depth + pix * S, dep);
-                    if (v.vis) {
-                        int* vp = v.vis + pix * S;
+            s_slot = slot;
+            s_base = fbase;
+        }
+        __syncthreads();
+        const int slot = s_slot;
+        if (slot < 0) return;
+        uint4* out = fa.frags + s_base + pre;
+        for (int i = 0; i < nfrag; i++) {
+            const int2 f = frags[i * NT + tid];
+            out[i] = make_uint4((uint32_t)f.x, (uint32_t)px | ((uint32_t)py << 16), (uint32_t)f.y & 0xffffu,
+                                (uint32_t)f.y >> 16);
+        }
+        fa.fwd_pix_end[(size_t)slot * NT + tid] = (uint16_t)(pre + nfrag);
+        if (inpix) {
+            if (dep_changed) store_depth<S>(v.depth + pix * S, dep);
+            if (v.vis) {
+                int* vp = v.vis + pix * S;
 #pragma unroll
-                        for (int k = 0; k < S; k++) vp[k] = vid[k];
-                    }
-                }
-                return;
+                for (int k = 0; k < S; k++) vp[k] = vid[k];
             }
         }
-        if (!have_cols) start_colours<S>(v, scol, ltile, after_raster, bg);
-    }
+        return;
+    } else {
     // shade the recorded fragments with the warp converged on fragment slot i of every lane, and
     // apply each one in submission order to its samples (spreading the fragments' anisotropic probes
     // over the warp's lanes, as the shade stage does, measured slower here: 5.15 vs 4.09 ms on the
@@ -2222,25 +2226,28 @@ __device__ __forceinline__ void forward_tile(const PassArgs& a, const FragArgs& 
 #pragma unroll
         for (int k = 0; k < S; k++) vp[k] = vid[k];
     }
+    }
 }
 
 template <int S, bool DEFER>
 size_t forward_smem_bytes() {
     return sizeof(FwdRecords) + (DEFER ? 0 : sizeof(float4) * S * kFwdThreads) + sizeof(uint32_t) * kOrderedCap +
-           sizeof(int2) * kFwdFrags * kFwdThreads + sizeof(uint32_t) * kFwdThreads * (kFwdThreads / 32);
+           sizeof(int2) * (DEFER ? kFwdFragsDefer : kFwdFrags) * kFwdThreads +
+           sizeof(uint32_t) * kFwdThreads * (kFwdThreads / 32);
 }
 
-// Two CTAs per SM (128 registers): three, at 80 registers, spilled and measured slower.
+// The in-stage form runs two CTAs per SM (128 registers, its shading code included); the deferring
+// form, which shades nothing, three (80 registers, 73 KB of shared memory).
 template <int S, bool DEFER>
-__global__ void __launch_bounds__(kFwdThreads, 2) forward_kernel(PassArgs a, FragArgs fa, GroupArgs g,
+__global__ void __launch_bounds__(kFwdThreads, DEFER ? 3 : 2) forward_kernel(PassArgs a, FragArgs fa, GroupArgs g,
                                                                              int qslot, int after_raster) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     FwdRecords& rec = *reinterpret_cast<FwdRecords*>(smem_raw);
     float4* scol = reinterpret_cast<float4*>(smem_raw + sizeof(FwdRecords));  // [S][256] (not DEFER)
     uint32_t* list =
         reinterpret_cast<uint32_t*>(smem_raw + sizeof(FwdRecords) + (DEFER ? 0 : sizeof(float4) * S * kFwdThreads));
-    int2* frags = reinterpret_cast<int2*>(list + kOrderedCap);  // [kFwdFrags][256]
-    uint32_t* cand = reinterpret_cast<uint32_t*>(frags + kFwdFrags * kFwdThreads);  // [8][256]
+    int2* frags = reinterpret_cast<int2*>(list + kOrderedCap);  // [fragments per pixel][256]
+    uint32_t* cand = reinterpret_cast<uint32_t*>(frags + (DEFER ? kFwdFragsDefer : kFwdFrags) * kFwdThreads);  // [8][256]
     uint16_t* wcov = reinterpret_cast<uint16_t*>(cand);  // [8][kFwdWarpCand], aliases cand
     static_assert(sizeof(uint16_t) * kFwdWarpCand * (kFwdThreads / 32) <= sizeof(uint32_t) * kFwdThreads * (kFwdThreads / 32),
                   "coverage buffers fit the candidate masks");
@@ -2259,6 +2266,51 @@ __global__ void __launch_bounds__(kFwdThreads, 2) forward_kernel(PassArgs a, Fra
     __syncthreads();
     while (next_tile<kFwdThreads>(a, g, qslot, sv, s_tile, s_view))
         forward_tile<S, DEFER>(a, fa, sv, s_view, s_tile, rec, scol, list, frags, cand, wcov, after_raster != 0, bs);
+    if (bs.pending && threadIdx.x == 0) mbar_wait(&s_bar, (bs.phase - 1) & 1u);  // a copy that did not land in time
+}
+
+// The tiles the deferring form left (redo list), finished by the in-stage form from the same inputs:
+// the deferring form wrote nothing for them.  Tiles are taken in list order, one per CTA iteration.
+template <int S>
+__global__ void __launch_bounds__(kFwdThreads, 2) forward_redo_kernel(PassArgs a, FragArgs fa, GroupArgs g,
+                                                                   int after_raster) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    FwdRecords& rec = *reinterpret_cast<FwdRecords*>(smem_raw);
+    float4* scol = reinterpret_cast<float4*>(smem_raw + sizeof(FwdRecords));  // [S][256]
+    uint32_t* list = reinterpret_cast<uint32_t*>(smem_raw + sizeof(FwdRecords) + sizeof(float4) * S * kFwdThreads);
+    int2* frags = reinterpret_cast<int2*>(list + kOrderedCap);  // [kFwdFrags][256]
+    uint32_t* cand = reinterpret_cast<uint32_t*>(frags + kFwdFrags * kFwdThreads);  // [8][256]
+    uint16_t* wcov = reinterpret_cast<uint16_t*>(cand);
+    __shared__ ViewArgs sv;
+    __shared__ int s_view;
+    __shared__ __align__(8) uint64_t s_bar;
+    BulkState bs;
+    bs.bar = &s_bar;
+    bs.phase = 0;
+    bs.ok = true;
+    bs.pending = false;
+    if (threadIdx.x == 0) mbar_init(&s_bar, 1);
+    const uint32_t n = min(a.status[ST_REDO], (uint32_t)(g.tile_end - g.tile_begin));
+    const FragArgs none{};  // the in-stage form reads no fragment buffers
+    for (uint32_t slot = blockIdx.x; slot < n; slot += gridDim.x) {
+        const int t = (int)fa.redo_tiles[slot];
+        __syncthreads();  // the previous tile's staged data is no longer read
+        if (threadIdx.x == 0) {
+            int lo = g.view_begin, hi = g.view_end - 1;
+            while (lo < hi) {
+                const int mid = (lo + hi + 1) >> 1;
+                if (__ldg(a.view_tile_start + mid) <= t) lo = mid; else hi = mid - 1;
+            }
+            s_view = lo;
+        }
+        __syncthreads();
+        const int* src = reinterpret_cast<const int*>(a.views + s_view);
+        int* dst = reinterpret_cast<int*>(&sv);
+        for (int i = threadIdx.x; i < (int)(sizeof(ViewArgs) / 4); i += kFwdThreads) dst[i] = src[i];
+        __syncthreads();
+        forward_tile<S, false>(a, none, sv, s_view, t, rec, scol, list, frags, cand, wcov, after_raster != 0, bs);
+    }
+    __syncthreads();
     if (bs.pending && threadIdx.x == 0) mbar_wait(&s_bar, (bs.phase - 1) & 1u);  // a copy that did not land in time
 }
 
@@ -2829,10 +2881,30 @@ cudaError_t launch_forward_form(const PassArgs& a, const FragArgs& fa, const Gro
 }
 
 template <int S>
+cudaError_t configure_redo() {
+    static bool done = false;
+    if (done) return cudaSuccess;
+    cudaError_t e = cudaFuncSetAttribute(forward_redo_kernel<S>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)forward_smem_bytes<S, false>());
+    if (e == cudaSuccess) done = true;
+    return e;
+}
+
+// The deferring form, then the in-stage form over the tiles it left (usually none: one CTA per SM
+// reads the count and exits).
+template <int S>
 cudaError_t launch_forward(const PassArgs& a, const FragArgs& fa, const GroupArgs& g, int ctas, cudaStream_t stream,
                            int qslot) {
-    return fa.frags ? launch_forward_form<S, true>(a, fa, g, ctas, stream, qslot)
-                    : launch_forward_form<S, false>(a, fa, g, ctas, stream, qslot);
+    if (!fa.frags) return launch_forward_form<S, false>(a, fa, g, ctas, stream, qslot);
+    cudaError_t e = launch_forward_form<S, true>(a, fa, g, ctas, stream, qslot);
+    if (e == cudaSuccess) e = configure_redo<S>();
+    if (e != cudaSuccess) return e;
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    forward_redo_kernel<S><<<sms > 0 ? sms : 1, kFwdThreads, forward_smem_bytes<S, false>(), stream>>>(a, fa, g,
+                                                                                                     qslot % 3 == 2);
+    return cudaSuccess;
 }
 
 template <int S>

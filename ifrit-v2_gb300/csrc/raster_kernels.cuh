@@ -24,10 +24,11 @@ enum StatusWord {
     ST_FRAGS = 3,       // deferred ordered fragments allocated (may run past the capacity)
     ST_FRAG_FAIL = 4,   // 0xFFFFFFFF - offset of the first allocation that did not fit; 0: none
     ST_FWD_TILES = 5,   // ordered tiles whose fragments were deferred
-    ST_PASS_WORDS = 6,
-    ST_STICKY = 6,
-    ST_MAX_PAIRS = 7,
-    ST_MAX_FRAGS = 8,   // largest fragment demand of a pass that did not fit (grows the buffer)
+    ST_REDO = 6,        // ordered tiles left for the in-stage form (a pixel with too many fragments, buffer full)
+    ST_PASS_WORDS = 7,
+    ST_STICKY = 7,
+    ST_MAX_PAIRS = 8,
+    ST_MAX_FRAGS = 9,   // largest fragment demand of a pass that did not fit (grows the buffer)
     ST_WORDS = 12
 };
 constexpr int kOrderedCap = 8192;  // entries per tile an ordered (in-API-order) pass can sort
@@ -91,6 +92,7 @@ struct FragArgs {
     uint32_t frag_capacity;
     uint4* fwd_tiles;        // [total_tiles] deferred tiles: global tile, first fragment, view, hand-off flag
     uint16_t* fwd_pix_end;   // [total_tiles][256] end of each pixel's fragments, from the tile's first
+    uint32_t* redo_tiles;    // [total_tiles] tiles the deferring stage left to the in-stage form
 };
 
 constexpr int kMaxGroups = 16;  // launch groups of a pass: (samples, path, tile size) combinations

@@ -169,7 +169,7 @@ IFTR_API int iftrSetPolygonRules(IfritGbRenderer* h, int rules);
  * them per pixel in order.  The image is the same either way.  fragments = -1 (default): buffer
  * for one fragment per pixel, grown after a pass that needed more; 0: the ordered stage shades
  * its fragments itself; n > 0: a buffer of exactly n fragments.  Tiles whose fragments do not fit
- * (or with more than 8 fragments on one pixel) are finished by the ordered stage. */
+ * (or with more than 6 fragments on one pixel) are finished by the ordered stage itself. */
 IFTR_API int iftrSetOrderedFragmentCapacity(IfritGbRenderer* h, long long fragments);
 /* Raster path of order-independent passes (no counterpart in the reference).  TILED (default):
  * triangles binned into 16x16 tiles, resolved per tile in shared memory.  ATOMIC: no binning;
