@@ -1,6 +1,6 @@
 """Deferred shading of ordered fragments: the ordered stage hands each tile's passing fragments to a
 shading kernel and a per-pixel blending kernel; tiles that do not fit the fragment buffer, or that
-have a pixel with more than 8 fragments, are finished by the ordered stage itself.  Every route must
+have a pixel with more than 6 fragments, are finished by the ordered stage itself.  Every route must
 give the same image, bit for bit, and match the oracle."""
 import os
 
@@ -61,9 +61,10 @@ def test_deferred_inline_and_partial_capacity_agree():
 
 
 def _layers_pass(capacity, S, first_blended):
-    """Twelve overlapping blended layers of large triangles (a pixel gets up to 12 fragments: the
-    ordered stage applies some of them on the spot) beside small blended triangles; with
-    `first_blended` the pass has no order-independent prefix."""
+    """Twelve overlapping blended layers of large triangles (a pixel gets up to 12 fragments: those
+    tiles go to the redo list and are finished by the in-stage form, which applies some fragments on
+    the spot) beside small blended triangles; with `first_blended` the pass has no order-independent
+    prefix."""
     rng = np.random.default_rng(77)
     W, H = 96, 80
     verts, tris = [], []
