@@ -115,3 +115,58 @@ def test_many_layers_mixed_routes(S, first_blended):
     inline, _ = _layers_pass(0, S, first_blended)
     _same(deferred, inline)
     assert_parity(deferred, ref, fmt=ig.FORMAT_RGBA32F)
+
+
+@pytest.mark.parametrize("S", [1, 4])
+def test_dense_ordered_tiles_marking_and_batches(S):
+    """Hundreds of small blended triangles per 16x16 tile over an opaque prefix: batches of more
+    than 64 records (candidates marked from the records' side) and tiles of more than 256 ordered
+    entries (several batches), through the deferring form, the in-stage form and the oracle."""
+    rng = np.random.default_rng(91)
+    W, H = 48, 40
+    verts, tris = [], []
+    for i in range(20):  # opaque prefix: large triangles behind
+        cx, cy = rng.uniform(-0.5, 0.5, 2)
+        z = rng.uniform(-3.0, -2.5)
+        p = np.array([[cx - 1.5, cy - 1.5, z], [cx + 1.5, cy - 1.2, z], [cx, cy + 1.6, z]], np.float32)
+        c = rng.uniform(0, 1, (3, 4)).astype(np.float32)
+        c[:, 3] = 1.0
+        tris.append([len(verts), len(verts) + 1, len(verts) + 2])
+        verts.extend(np.concatenate([p, c], 1))
+    for i in range(4000):  # blended: ~2-pixel triangles in front
+        cx, cy = rng.uniform(-0.55, 0.55, 2)
+        z = rng.uniform(-1.6, -1.2)
+        p = np.array([[cx, cy, z], [cx + 0.05, cy, z], [cx, cy + 0.05, z]], np.float32)
+        c = rng.uniform(0, 1, (3, 4)).astype(np.float32)
+        tris.append([len(verts), len(verts) + 1, len(verts) + 2])
+        verts.extend(np.concatenate([p, c], 1))
+    v = np.array(verts, np.float32)
+    f = np.array(tris, np.int32)
+    mvp = scenes.perspective(60.0, W / H, 0.1, 50.0).astype(np.float32)
+    outs = []
+    for capacity in (-1, 0):
+        r = ig.Renderer(W, H, S, ig.FORMAT_RGBA32F, visibility=True)
+        r.set_ordered_fragment_capacity(capacity)
+        r.set_geometry(v, f, 4)
+        r.set_mvp(mvp)
+        r.begin_pass(clear=True)
+        odraws, base = [], 0
+        for a, b, blend in ((0, 20, False), (20, len(f), True)):
+            r.set_state(cull=ig.CULL_NONE, depth_func=ig.LESS_OR_EQUAL, depth_write=not blend,
+                        clear_color=(0.1, 0.2, 0.3, 1.0))
+            r.set_blend(blend, 6, 7, 1, 7)
+            r.pass_draw(3 * a, 3 * (b - a))
+            odraws.append(O.make_draw(v, f[a:b], mvp, attr_offset=3, attr_count=4, cull_mode=0, depth_func=3,
+                                      depth_write=int(not blend), blend=(6, 7, 1, 7) if blend else None,
+                                      prim_base=base))
+            base += b - a
+        r.end_pass()
+        outs.append({"color": r.color(), "depth": r.depth(), "vis": r.visibility()})
+        st = r.stats()
+        r.close()
+        if capacity == -1:
+            assert st.tile_pairs > 4000  # up to 1,600 ordered entries in one tile
+    _same(outs[0], outs[1])
+    ref = O.render(odraws, W, H, S, FMT_TO_ORACLE[ig.FORMAT_RGBA32F], clear=True, clear_color=(0.1, 0.2, 0.3, 1.0),
+                   nthreads=os.cpu_count() or 1)
+    assert_parity(outs[0], ref, fmt=ig.FORMAT_RGBA32F)
