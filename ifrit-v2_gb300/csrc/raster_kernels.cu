@@ -1390,19 +1390,38 @@ __device__ __forceinline__ void warp_texture_probes(const DrawDev* draws, int di
     }
 }
 
+// Slot codes of the shade stage's per-sample entries (see shade_tile).
+constexpr int kSlotLate = 4, kSlotNone = 7;
+
+// Sample k's visible entry read again after the shading loop.  The volatile loads keep the compiler
+// from reusing the values read before the loop, which would hold every sample's entry in registers
+// across it.
+template <int S>
+__device__ __forceinline__ int sample_entry_again(const ViewArgs& v, const KeyRule& rule, size_t pix, int k) {
+    if (v.keys) {
+        unsigned long long key;
+        asm volatile("ld.global.u64 %0, [%1];" : "=l"(key) : "l"(v.keys + pix * S + k));
+        return key_entry(rule, key);
+    }
+    int e;
+    asm volatile("ld.global.s32 %0, [%1];" : "=r"(e) : "l"(v.entries + pix * S + k));
+    return e;
+}
+
 // Shade stage CTAs: warps are independent (each pulls its own 32-pixel tasks); a CTA only holds the
 // warps' shared-memory slices.
 constexpr int kShadeThreads = 256;
 constexpr int kShadeBlocks = 4;
 
 // One tile, one thread per pixel.  Each pixel lists its distinct visible entries in sample
-// order; the warp shades list slot i of all its lanes together (set-up straight from the
-// binner's record, quad derivatives, texture filtering), then the samples are resolved on chip
-// and depth, visibility and the resolved colour stored once.
+// order; the warp shades the (pixel, entry) items of all its lanes together (set-up straight
+// from the binner's record, the depths of the pixel's samples on that entry, quad derivatives,
+// texture filtering), then the samples are resolved on chip and depth, visibility and the
+// resolved colour stored once.
 template <int S, int TS>
 __device__ __forceinline__ void shade_tile(const PassArgs& a, const ViewArgs& v, int gtile, int part,
-                                           float4 (*scol)[kShadeThreads], float4 (*splane)[kShadeThreads],
-                                           int (*splane_y)[kShadeThreads], int2* witems, float4* wres,
+                                           float4 (*scol)[kShadeThreads], float (*sdep)[kShadeThreads], int2* witems,
+                                           float4* wres,
                                            bool keep_samples) {
     const int ltile = gtile - v.tile_start;
     const int tx = ltile % v.c.tiles_x, ty = ltile / v.c.tiles_x;
@@ -1413,47 +1432,60 @@ __device__ __forceinline__ void shade_tile(const PassArgs& a, const ViewArgs& v,
     const bool inpix = px < v.c.W && py < v.c.H;
     const size_t pix = (size_t)py * v.c.W + px;
     const KeyRule rule = key_rule(v.depth_func, v.depth_write);
-    int ent[S];
-    if (inpix && v.keys) {  // atomic visibility path
+    // Distinct visible entries of this pixel, in sample order, and each sample's 3-bit slot code:
+    // 0..U-1 its list slot, kSlotLate for entries past the U shaded together (shaded on their own
+    // after the warp's items), kSlotNone for no visible entry.  Only the packed codes stay in
+    // registers across the shading loop: slot entries come back from the warp's item list, late
+    // ones from memory.
+    constexpr int U = S < 4 ? S : 4;  // slots shaded together across the warp
+    using SlotCodes = typename std::conditional<(S > 8), unsigned long long, uint32_t>::type;
+    SlotCodes codes = 0;
+    int uniq[U];
+    int nu = 0;
+    {
+        int ent[S];
+        if (inpix && v.keys) {  // atomic visibility path
 #pragma unroll
-        for (int k = 0; k < S; k++) ent[k] = key_entry(rule, v.keys[pix * S + k]);
-    } else if (inpix) {
-        const int* ep = v.entries + pix * S;
-        if constexpr (S % 4 == 0) {
+            for (int k = 0; k < S; k++) ent[k] = key_entry(rule, v.keys[pix * S + k]);
+        } else if (inpix) {
+            const int* ep = v.entries + pix * S;
+            if constexpr (S % 4 == 0) {
 #pragma unroll
-            for (int k = 0; k < S; k += 4) {
-                int4 q = reinterpret_cast<const int4*>(ep)[k / 4];
-                ent[k] = q.x; ent[k + 1] = q.y; ent[k + 2] = q.z; ent[k + 3] = q.w;
+                for (int k = 0; k < S; k += 4) {
+                    int4 q = reinterpret_cast<const int4*>(ep)[k / 4];
+                    ent[k] = q.x; ent[k + 1] = q.y; ent[k + 2] = q.z; ent[k + 3] = q.w;
+                }
+            } else {
+#pragma unroll
+                for (int k = 0; k < S; k++) ent[k] = ep[k];
             }
         } else {
 #pragma unroll
-            for (int k = 0; k < S; k++) ent[k] = ep[k];
+            for (int k = 0; k < S; k++) ent[k] = -1;
         }
-    } else {
+        int which[S];
 #pragma unroll
-        for (int k = 0; k < S; k++) ent[k] = -1;
-    }
-
-    // distinct visible entries of this pixel, in sample order; sample k uses list slot which[k]
-    constexpr int U = S < 4 ? S : 4;  // slots shaded together across the warp
-    int uniq[U], which[S];
-    int nu = 0;
+        for (int k = 0; k < S; k++) {
+            which[k] = -1;
+            if (ent[k] < 0) continue;
+            int found = -1;
 #pragma unroll
-    for (int k = 0; k < S; k++) {
-        which[k] = -1;
-        if (ent[k] < 0) continue;
-        int found = -1;
+            for (int j = 0; j < k; j++)
+                if (which[j] >= 0 && ent[j] == ent[k]) found = which[j];
+            if (found < 0) {
+                found = nu;
 #pragma unroll
-        for (int j = 0; j < k; j++)
-            if (which[j] >= 0 && ent[j] == ent[k]) found = which[j];
-        if (found < 0) {
-            found = nu;
-#pragma unroll
-            for (int j = 0; j < U; j++)
-                if (j == nu) uniq[j] = ent[k];
-            nu++;
+                for (int j = 0; j < U; j++)
+                    if (j == nu) uniq[j] = ent[k];
+                nu++;
+            }
+            which[k] = found;
         }
-        which[k] = found;
+#pragma unroll
+        for (int k = 0; k < S; k++) {
+            const int code = which[k] < 0 ? kSlotNone : which[k] < U ? which[k] : kSlotLate;
+            codes |= (SlotCodes)code << (3 * k);
+        }
     }
     // The warp's (pixel, entry) shading items, compacted: item i of the warp goes to lane i % 32,
     // whatever pixel it belongs to (quad derivatives are evaluated analytically at the owner's
@@ -1468,22 +1500,23 @@ __device__ __forceinline__ void shade_tile(const PassArgs& a, const ViewArgs& v,
     }
     const int total = __shfl_sync(0xffffffffu, incl, 31);
     int2* items = witems + (tid >> 5) * (32 * U);
+    const int ibase = incl - nc;  // this lane's first item: slot j's entry is items[ibase + j].x
 #pragma unroll
     for (int j = 0; j < U; j++)
-        if (j < nc) items[incl - nc + j] = make_int2(uniq[j], lane | (j << 5));
+        if (j < nc) items[ibase + j] = make_int2(uniq[j], lane | (j << 5));
     __syncwarp();
     for (int r0 = 0; r0 < total; r0 += 32) {
         const int b = r0 + lane;
-        int owner = 0, slot = 0, di = 0, n = 0;  // n: texture probes of this lane's item
+        const int2 it = b < total ? items[b] : make_int2(0, 0);
+        const int owner = it.y & 31, slot = it.y >> 5;
+        const SlotCodes oc = __shfl_sync(0xffffffffu, codes, owner);  // the owner pixel's slot codes
+        int di = 0, n = 0;  // n: texture probes of this lane's item
         float c[4] = {0.0f, 0.0f, 0.0f, 0.0f};
         TexProbe tp;
         tp.u = tp.v = tp.du = tp.dv = tp.t = 0.0f;
         tp.lo = tp.hi = tp.n = 0;
         tp.two = tp.aniso = false;
         if (b < total) {
-            const int2 it = items[b];
-            owner = it.y & 31;
-            slot = it.y >> 5;
             int olx, oly;
             tile_pixel<TS>(part * 32 + owner, olx, oly);
             const int opx = tx * TS + olx, opy = ty * TS + oly;
@@ -1508,6 +1541,12 @@ __device__ __forceinline__ void shade_tile(const PassArgs& a, const ViewArgs& v,
                 plane = tpl;
                 plane_y = tpy;
             }
+            // depths of the owner's samples on this slot, from the item's plane
+#pragma unroll
+            for (int k = 0; k < S; k++)
+                if ((int)(oc >> (3 * k) & 7) == slot)
+                    sdep[k][wbase + owner] = sample_depth(plane.x, plane.y, plane.z, __float_as_int(plane.w), plane_y,
+                                                          opx * 256 + sample_x<S>(k), opy * 256 + sample_y<S>(k));
             float a0[4], a1[4], a2[4];
             if (from_record && a.attrs && d.shading != SHADE_PRIMID && d.attr_count > 0) {
                 const float4 q0 = __ldg(&a.attrs[g].a[0]), q1 = __ldg(&a.attrs[g].a[1]), q2 = __ldg(&a.attrs[g].a[2]);
@@ -1521,8 +1560,6 @@ __device__ __forceinline__ void shade_tile(const PassArgs& a, const ViewArgs& v,
                 for (int k = 0; k < 4; k++) a0[k] = a1[k] = a2[k] = 0.0f;
             }
             if (shade_prepare_attrs(v.c, d, geo, t, sub, opx, opy, a0, a1, a2, c, tp)) n = tp.n;
-            splane[slot][wbase + owner] = plane;
-            splane_y[slot][wbase + owner] = plane_y;
         }
         warp_texture_probes(a.draws, di, tp, n, wres, c);
         if (b < total) scol[slot][wbase + owner] = make_float4(c[0], c[1], c[2], c[3]);
@@ -1530,15 +1567,7 @@ __device__ __forceinline__ void shade_tile(const PassArgs& a, const ViewArgs& v,
     __syncwarp();
     float dep[S];
 #pragma unroll
-    for (int k = 0; k < S; k++) {
-        dep[k] = 0.0f;
-        const int i = which[k];
-        if (i >= 0 && i < U) {
-            const float4 pl = splane[i][tid];
-            dep[k] = sample_depth(pl.x, pl.y, pl.z, __float_as_int(pl.w), splane_y[i][tid], px * 256 + sample_x<S>(k),
-                                  py * 256 + sample_y<S>(k));
-        }
-    }
+    for (int k = 0; k < S; k++) dep[k] = ((int)(codes >> (3 * k)) & 7) < U ? sdep[k][tid] : 0.0f;
     if (!inpix) return;
     float bg[4];
     if (v.clear) {
@@ -1550,18 +1579,19 @@ __device__ __forceinline__ void shade_tile(const PassArgs& a, const ViewArgs& v,
 #pragma unroll
     for (int k = 0; k < S; k++) {
         float c[4];
+        const int code = (int)(codes >> (3 * k)) & 7;
         const float d0v = v.clear ? v.clear_depth : v.depth[pix * S + k];
-        if (which[k] < 0) {
+        if (code == kSlotNone) {
             c[0] = bg[0]; c[1] = bg[1]; c[2] = bg[2]; c[3] = bg[3];
             dep[k] = d0v;
         } else {
-            if (which[k] < U) {
-                float4 q = scol[which[k]][tid];
+            if (code < U) {
+                float4 q = scol[code][tid];
                 c[0] = q.x; c[1] = q.y; c[2] = q.z; c[3] = q.w;
             } else {  // more than U distinct primitives in one pixel: shade this one here
                 RecordPlane pl;
                 float uc[4];  // through memory on this rare path only
-                shade_uncached(a, v.c, ent[k], px, py, uc, &pl);
+                shade_uncached(a, v.c, sample_entry_again<S>(v, rule, pix, k), px, py, uc, &pl);
                 c[0] = uc[0]; c[1] = uc[1]; c[2] = uc[2]; c[3] = uc[3];
                 dep[k] = sample_depth(pl.z0, pl.dzdx, pl.dzdy, pl.X0, pl.Y0, px * 256 + sample_x<S>(k),
                                       py * 256 + sample_y<S>(k));
@@ -1593,7 +1623,11 @@ __device__ __forceinline__ void shade_tile(const PassArgs& a, const ViewArgs& v,
     if (v.vis) {
         int* vp = v.vis + pix * S;
 #pragma unroll
-        for (int k = 0; k < S; k++) vp[k] = ent[k] < 0 ? -1 : (ent[k] >> 3) - v.first_tri;
+        for (int k = 0; k < S; k++) {
+            const int code = (int)(codes >> (3 * k)) & 7;
+            const int e = code == kSlotNone ? -1 : code < U ? items[ibase + code].x : sample_entry_again<S>(v, rule, pix, k);
+            vp[k] = e < 0 ? -1 : (e >> 3) - v.first_tri;
+        }
     }
 }
 
@@ -1605,9 +1639,8 @@ __global__ void __launch_bounds__(kShadeThreads, kShadeBlocks) shade_kernel(Pass
     constexpr int NT = TS * TS, CT = kShadeThreads;
     constexpr int kTasksPerTile = NT / 32;
     constexpr int U = S < 4 ? S : 4;
-    __shared__ float4 scol[4][CT];    // colours of each thread's (up to 4) distinct entries
-    __shared__ float4 splane[4][CT];  // their depth planes: z0, dz/dx, dz/dy, X0 (bits)
-    __shared__ int splane_y[4][CT];   // and Y0
+    __shared__ float4 scol[U][CT];  // colours of each thread's (up to U) distinct entries
+    __shared__ float sdep[S][CT];   // depths of its samples on those entries
     __shared__ int2 witems[CT / 32 * 32 * U];  // per warp: compacted (entry, lane | slot << 5) items
     __shared__ float4 sres[CT];                // per warp: results of one round of texture probes
     const int lane = threadIdx.x & 31;
@@ -1633,8 +1666,8 @@ __global__ void __launch_bounds__(kShadeThreads, kShadeBlocks) shade_kernel(Pass
         // tiles of ordered views with entries left for the ordered stage keep their per-sample
         // colours for it instead of resolving
         const bool keep = a.views[vi].ordered && __ldg(a.tile_cursor + gtile) != 0u;
-        shade_tile<S, TS>(a, a.views[vi], gtile, task % kTasksPerTile, scol, splane, splane_y, witems,
-                          sres + (threadIdx.x & ~31), keep);
+        shade_tile<S, TS>(a, a.views[vi], gtile, task % kTasksPerTile, scol, sdep, witems, sres + (threadIdx.x & ~31),
+                          keep);
     }
 }
 

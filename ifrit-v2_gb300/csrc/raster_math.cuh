@@ -575,6 +575,16 @@ __device__ __forceinline__ void unpack_rgba8(uint32_t t, float c[4]) {
 
 __device__ __forceinline__ float lerpf_(float a, float b, float t) { return a + t * (b - a); }
 
+// Repeat (mode 0) and mirrored-repeat (mode 1) wrapping of coordinates beyond the in-line
+// shortcuts: fmodf, then into [0, n) or [0, 2n).  Out of line so that the filter's four address
+// computations per probe do not each carry a copy of fmodf.
+static __device__ __noinline__ float tex_wrap_far(int mode, float v, float nf) {
+    const float m = mode == 0 ? nf : nf + nf;
+    v = fmodf(v, m);
+    if (v < 0.0f) v = v + m;
+    return v;
+}
+
 // Texel-space wrapping per address mode; returns false outside a clamp-to-border texture.
 // fmodf is exact, and so are the shortcuts on the ranges where they are taken (Sterbenz:
 // v - n is exact for n <= v <= 2n; for |v| < n fmodf returns v itself).
@@ -588,8 +598,7 @@ __device__ __forceinline__ bool tex_address(int mode, float& c, float nf) {
         } else if (v < 0.0f && v > -nf) {
             v = v + nf;
         } else {
-            v = fmodf(v, nf);
-            if (v < 0.0f) v = v + nf;
+            v = tex_wrap_far(0, v, nf);
         }
         break;
     case 1: {
@@ -598,8 +607,7 @@ __device__ __forceinline__ bool tex_address(int mode, float& c, float nf) {
         } else if (v < 0.0f && v > -n2) {
             v = v + n2;
         } else {
-            v = fmodf(v, n2);
-            if (v < 0.0f) v = v + n2;
+            v = tex_wrap_far(1, v, nf);
         }
         v = fminf(v, n2 - v);
         break;
