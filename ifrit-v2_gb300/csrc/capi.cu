@@ -182,6 +182,7 @@ struct IfritGbRenderer {
     bool inited = false;
     cudaStream_t stream = nullptr;
     bool own_stream = false;
+    ifr::SideStream side{};  // created with the first pass that defers ordered fragments
     int sms = 0;
     // bindings
     IfritGbFrameBuffer* fb = nullptr;
@@ -412,7 +413,9 @@ int reserve_fragments(IfritGbRenderer* h, PassScratch& s, size_t tiles, size_t p
     IFTR_CUDA(h, s.redo_tiles.reserve(std::max<size_t>(1, tiles) * sizeof(uint32_t)));
     size_t want = h->frag_capacity_setting > 0 ? (size_t)h->frag_capacity_setting
                                                : std::max(s.frag_want, std::max<size_t>(1u << 20, pixels));
-    want = std::min<size_t>(want, 0xFFFFFFF0u);
+    // below 2^32 with room for the fragment shading kernel's counter, which runs past the count by
+    // up to 32 per warp
+    want = std::min<size_t>(want, 0xFFF00000u);
     IFTR_CUDA(h, s.frags.reserve(want * sizeof(uint4)));
     IFTR_CUDA(h, s.frag_cols.reserve(want * sizeof(float4)));
     s.frag_capacity = (uint32_t)want;
@@ -433,9 +436,10 @@ ifr::FragArgs fragment_args(const PassScratch& s) {
 // Stream work of one pass: clear the per-pass status words, run the pipeline, copy the status
 // back to pinned memory.  Contains no host synchronisation (it is also captured into graphs).
 cudaError_t launch_with_status(PassScratch& s, const PassArgs& a, const ifr::LaunchPlan& plan, cudaStream_t st,
-                               cudaEvent_t* ev, const ifr::FragArgs* fa = nullptr) {
+                               cudaEvent_t* ev, const ifr::FragArgs* fa = nullptr,
+                               const ifr::SideStream* side = nullptr) {
     cudaError_t e = cudaMemsetAsync(s.status.p, 0, ifr::ST_PASS_WORDS * sizeof(uint32_t), st);
-    if (e == cudaSuccess) e = ifr::launch_pass(a, plan, st, ev, fa);
+    if (e == cudaSuccess) e = ifr::launch_pass(a, plan, st, ev, fa, side);
     if (e == cudaSuccess)
         e = cudaMemcpyAsync(s.h_status, s.status.p, ifr::ST_WORDS * sizeof(uint32_t), cudaMemcpyDeviceToHost, st);
     return e;
@@ -654,8 +658,12 @@ int enqueue_pass(IfritGbRenderer* h, std::vector<DrawDev>& draws, int clear) {
         rc = reserve_fragments(h, h->pass, (size_t)T, (size_t)W * H);
         if (rc) return rc;
         fa = fragment_args(h->pass);
+        if (!h->side.fork) IFTR_CUDA(h, cudaEventCreateWithFlags(&h->side.fork, cudaEventDisableTiming));
+        if (!h->side.join) IFTR_CUDA(h, cudaEventCreateWithFlags(&h->side.join, cudaEventDisableTiming));
+        if (!h->side.stream) IFTR_CUDA(h, cudaStreamCreateWithFlags(&h->side.stream, cudaStreamNonBlocking));
     }
-    IFTR_CUDA(h, launch_with_status(h->pass, a, plan, h->stream, h->timing ? h->ev : nullptr, defer ? &fa : nullptr));
+    IFTR_CUDA(h, launch_with_status(h->pass, a, plan, h->stream, h->timing ? h->ev : nullptr, defer ? &fa : nullptr,
+                                    defer ? &h->side : nullptr));
     h->stats.triangles_in = (uint64_t)total;
     h->pending = 1;
     return IFTR_OK;
@@ -1070,6 +1078,12 @@ IFTR_API int iftrDestroyInstance(IfritGbRenderer* h) {
         for (auto& t : h->tex) t.mem.release();
         for (cudaEvent_t e : h->ev)
             if (e) cudaEventDestroy(e);
+        if (h->side.stream) {
+            cudaStreamSynchronize(h->side.stream);
+            cudaStreamDestroy(h->side.stream);
+        }
+        if (h->side.fork) cudaEventDestroy(h->side.fork);
+        if (h->side.join) cudaEventDestroy(h->side.join);
         if (h->own_stream) cudaStreamDestroy(h->stream);
     }
     delete h;

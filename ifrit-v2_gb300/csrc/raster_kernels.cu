@@ -2369,8 +2369,13 @@ __global__ void __launch_bounds__(kFragShadeThreads, 4) frag_shade_kernel(PassAr
     __shared__ float4 s_res[kFragShadeThreads / 32][32];
     const uint32_t n = deferred_fragments(a, fa);
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const uint32_t stride = gridDim.x * kFragShadeThreads;
-    for (uint32_t base = (blockIdx.x * (kFragShadeThreads / 32) + warp) * 32; base < n; base += stride) {
+    for (;;) {
+        // 32 fragments at a time from the pass's counter, so that CTAs which start late (the redo
+        // kernel of the in-stage form may hold part of an SM meanwhile) take less work
+        uint32_t base = 0;
+        if (lane == 0) base = atomicAdd(a.status + ST_FRAG_NEXT, 32u);
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if (base >= n) break;
         const uint32_t i = base + lane;
         int di = 0, np = 0;
         float c[4] = {0.0f, 0.0f, 0.0f, 0.0f};
@@ -2923,21 +2928,40 @@ cudaError_t configure_redo() {
     return e;
 }
 
-// The deferring form, then the in-stage form over the tiles it left (usually none: one CTA per SM
-// reads the count and exits).
+// The deferring form when there are fragment buffers (its redo list is finished by launch_redo),
+// else the in-stage form.
 template <int S>
 cudaError_t launch_forward(const PassArgs& a, const FragArgs& fa, const GroupArgs& g, int ctas, cudaStream_t stream,
                            int qslot) {
     if (!fa.frags) return launch_forward_form<S, false>(a, fa, g, ctas, stream, qslot);
-    cudaError_t e = launch_forward_form<S, true>(a, fa, g, ctas, stream, qslot);
-    if (e == cudaSuccess) e = configure_redo<S>();
+    return launch_forward_form<S, true>(a, fa, g, ctas, stream, qslot);
+}
+
+// The in-stage form over the tiles the deferring form left (usually none or a few: one CTA per SM
+// reads the count, those without a tile exit).
+template <int S>
+cudaError_t launch_redo(const PassArgs& a, const FragArgs& fa, const GroupArgs& g, bool after_raster,
+                        cudaStream_t stream) {
+    cudaError_t e = configure_redo<S>();
     if (e != cudaSuccess) return e;
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     forward_redo_kernel<S><<<sms > 0 ? sms : 1, kFwdThreads, forward_smem_bytes<S, false>(), stream>>>(a, fa, g,
-                                                                                                     qslot % 3 == 2);
+                                                                                                     after_raster);
     return cudaSuccess;
+}
+
+cudaError_t launch_group_redo(const PassArgs& a, const FragArgs& fa, const GroupArgs& g, int S, bool after_raster,
+                              cudaStream_t stream) {
+    switch (S) {
+    case 1: return launch_redo<1>(a, fa, g, after_raster, stream);
+    case 2: return launch_redo<2>(a, fa, g, after_raster, stream);
+    case 4: return launch_redo<4>(a, fa, g, after_raster, stream);
+    case 8: return launch_redo<8>(a, fa, g, after_raster, stream);
+    case 16: return launch_redo<16>(a, fa, g, after_raster, stream);
+    default: return cudaErrorInvalidValue;
+    }
 }
 
 template <int S>
@@ -3102,7 +3126,7 @@ int frag_kernel_occupancy(int S, int stage) {
 }
 
 cudaError_t launch_pass(const PassArgs& a, const LaunchPlan& plan, cudaStream_t stream, cudaEvent_t* ev,
-                        const FragArgs* fa_in) {
+                        const FragArgs* fa_in, const SideStream* side) {
     const int T = a.total_tiles;
     FragArgs fa, nofa;
     std::memset(&fa, 0, sizeof(fa));
@@ -3165,8 +3189,26 @@ cudaError_t launch_pass(const PassArgs& a, const LaunchPlan& plan, cudaStream_t 
             err = launch_group_forward(a, i == plan.defer_group ? fa : nofa, plan.groups[i], plan.samples[i],
                                        i == plan.defer_group && fa.frags ? plan.ctas_fwd_defer : plan.ctas_fwd[i], stream,
                                        true);
-    if (err == cudaSuccess && fa.frags)
-        err = launch_group_frags(a, fa, plan.samples[plan.defer_group], plan.ctas_frag_shade, plan.ctas_frag_blend, stream);
+    if (err == cudaSuccess && fa.frags) {
+        // the redo list's tiles and the deferred fragments' tiles are disjoint: with a side stream
+        // the in-stage form runs beside the fragment kernels (which take their work from a counter,
+        // so the SM share it holds costs them nothing but that share)
+        const int dg = plan.defer_group;
+        cudaStream_t rs = stream;
+        if (side) {
+            err = cudaEventRecord(side->fork, stream);
+            if (err == cudaSuccess) err = cudaStreamWaitEvent(side->stream, side->fork, 0);
+            rs = side->stream;
+        }
+        if (err == cudaSuccess) err = launch_group_redo(a, fa, plan.groups[dg], plan.samples[dg], plan.hybrid[dg] != 0, rs);
+        if (err == cudaSuccess)
+            err = launch_group_frags(a, fa, plan.samples[dg], plan.ctas_frag_shade, plan.ctas_frag_blend, stream);
+        if (side) {  // joined even after an error, so that the side stream holds no work of this pass
+            const cudaError_t j = cudaEventRecord(side->join, side->stream);
+            const cudaError_t w = j == cudaSuccess ? cudaStreamWaitEvent(stream, side->join, 0) : j;
+            if (err == cudaSuccess) err = w;
+        }
+    }
     if (ev) cudaEventRecord(ev[6], stream);
     return err != cudaSuccess ? err : cudaGetLastError();
 }

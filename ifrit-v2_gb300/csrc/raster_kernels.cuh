@@ -25,10 +25,11 @@ enum StatusWord {
     ST_FRAG_FAIL = 4,   // 0xFFFFFFFF - offset of the first allocation that did not fit; 0: none
     ST_FWD_TILES = 5,   // ordered tiles whose fragments were deferred
     ST_REDO = 6,        // ordered tiles left for the in-stage form (a pixel with too many fragments, buffer full)
-    ST_PASS_WORDS = 7,
-    ST_STICKY = 7,
-    ST_MAX_PAIRS = 8,
-    ST_MAX_FRAGS = 9,   // largest fragment demand of a pass that did not fit (grows the buffer)
+    ST_FRAG_NEXT = 7,   // next deferred fragment the fragment shading kernel hands out
+    ST_PASS_WORDS = 8,
+    ST_STICKY = 8,
+    ST_MAX_PAIRS = 9,
+    ST_MAX_FRAGS = 10,  // largest fragment demand of a pass that did not fit (grows the buffer)
     ST_WORDS = 12
 };
 constexpr int kOrderedCap = 8192;  // entries per tile an ordered (in-API-order) pass can sort
@@ -134,9 +135,17 @@ constexpr int scan_blocks(int tiles) { return (tiles + 4095) / 4096 + 1; }
 // scan, after scattering, after the raster stage, after the shade stage and after the ordered
 // stage (per-stage timing).
 constexpr int kStageEvents = 7;
-// fa: buffers of the deferred ordered fragments, or nullptr.
+// A second stream and two events on which the ordered stage's in-stage form finishes the tiles
+// the deferring form left (the redo list) while the deferred fragments are shaded and blended on
+// the pass's stream: the two touch disjoint tiles.
+struct SideStream {
+    cudaStream_t stream;
+    cudaEvent_t fork, join;
+};
+// fa: buffers of the deferred ordered fragments, or nullptr; side: optional, without it the redo
+// kernel runs in stream order before the fragment kernels.
 cudaError_t launch_pass(const PassArgs& a, const LaunchPlan& plan, cudaStream_t stream, cudaEvent_t* ev,
-                        const FragArgs* fa = nullptr);
+                        const FragArgs* fa = nullptr, const SideStream* side = nullptr);
 // Reference line / point rules (iftrSetPolygonRules): one single-sample draw; `keys` holds W*H
 // 64-bit entries of scratch.
 cudaError_t launch_reference_rules(const DrawDev& d, const ViewArgs& v, unsigned long long* keys, cudaStream_t stream);
