@@ -1420,7 +1420,7 @@ constexpr int kShadeBlocks = 4;
 // resolved colour stored once.
 template <int S, int TS>
 __device__ __forceinline__ void shade_tile(const PassArgs& a, const ViewArgs& v, int gtile, int part,
-                                           float4 (*scol)[kShadeThreads], float (*sdep)[kShadeThreads], int2* witems,
+                                           float4 (*scol)[kShadeThreads], float (*sdep)[kShadeThreads],
                                            float4* wres,
                                            bool keep_samples) {
     const int ltile = gtile - v.tile_start;
@@ -1441,6 +1441,8 @@ __device__ __forceinline__ void shade_tile(const PassArgs& a, const ViewArgs& v,
     using SlotCodes = typename std::conditional<(S > 8), unsigned long long, uint32_t>::type;
     SlotCodes codes = 0;
     int uniq[U];
+#pragma unroll
+    for (int j = 0; j < U; j++) uniq[j] = 0;
     int nu = 0;
     {
         int ent[S];
@@ -1499,16 +1501,20 @@ __device__ __forceinline__ void shade_tile(const PassArgs& a, const ViewArgs& v,
         if (lane >= o) incl += q;
     }
     const int total = __shfl_sync(0xffffffffu, incl, 31);
-    int2* items = witems + (tid >> 5) * (32 * U);
-    const int ibase = incl - nc;  // this lane's first item: slot j's entry is items[ibase + j].x
-#pragma unroll
-    for (int j = 0; j < U; j++)
-        if (j < nc) items[ibase + j] = make_int2(uniq[j], lane | (j << 5));
-    __syncwarp();
+    const int ibase = incl - nc;  // this lane's first item in the warp's compacted order
     for (int r0 = 0; r0 < total; r0 += 32) {
         const int b = r0 + lane;
-        const int2 it = b < total ? items[b] : make_int2(0, 0);
-        const int owner = it.y & 31, slot = it.y >> 5;
+        int owner = 0;  // the lane of item b: the last lane whose first item is at or before b
+#pragma unroll
+        for (int step = 16; step > 0; step >>= 1)
+            if (__shfl_sync(0xffffffffu, ibase, owner + step) <= b) owner += step;
+        const int slot = b - __shfl_sync(0xffffffffu, ibase, owner);
+        int item = __shfl_sync(0xffffffffu, uniq[0], owner);  // the item's entry
+#pragma unroll
+        for (int j = 1; j < U; j++) {
+            const int ej = __shfl_sync(0xffffffffu, uniq[j], owner);
+            if (slot == j) item = ej;
+        }
         const SlotCodes oc = __shfl_sync(0xffffffffu, codes, owner);  // the owner pixel's slot codes
         int di = 0, n = 0;  // n: texture probes of this lane's item
         float c[4] = {0.0f, 0.0f, 0.0f, 0.0f};
@@ -1520,7 +1526,7 @@ __device__ __forceinline__ void shade_tile(const PassArgs& a, const ViewArgs& v,
             int olx, oly;
             tile_pixel<TS>(part * 32 + owner, olx, oly);
             const int opx = tx * TS + olx, opy = ty * TS + oly;
-            const int g = it.x >> 3, sub = it.x & 7;
+            const int g = item >> 3, sub = item & 7;
             const TriRecord* rp = a.records + g;
             const int4 q1 = __ldg(reinterpret_cast<const int4*>(rp) + 1);  // X2, Y2, flags, draw
             di = q1.w;
@@ -1625,7 +1631,12 @@ __device__ __forceinline__ void shade_tile(const PassArgs& a, const ViewArgs& v,
 #pragma unroll
         for (int k = 0; k < S; k++) {
             const int code = (int)(codes >> (3 * k)) & 7;
-            const int e = code == kSlotNone ? -1 : code < U ? items[ibase + code].x : sample_entry_again<S>(v, rule, pix, k);
+            int e = uniq[0];
+#pragma unroll
+            for (int j = 1; j < U; j++)
+                if (code == j) e = uniq[j];
+            if (code == kSlotNone) e = -1;
+            else if (code >= U) e = sample_entry_again<S>(v, rule, pix, k);
             vp[k] = e < 0 ? -1 : (e >> 3) - v.first_tri;
         }
     }
@@ -1641,7 +1652,6 @@ __global__ void __launch_bounds__(kShadeThreads, kShadeBlocks) shade_kernel(Pass
     constexpr int U = S < 4 ? S : 4;
     __shared__ float4 scol[U][CT];  // colours of each thread's (up to U) distinct entries
     __shared__ float sdep[S][CT];   // depths of its samples on those entries
-    __shared__ int2 witems[CT / 32 * 32 * U];  // per warp: compacted (entry, lane | slot << 5) items
     __shared__ float4 sres[CT];                // per warp: results of one round of texture probes
     const int lane = threadIdx.x & 31;
     const int ntasks = (g.tile_end - g.tile_begin) * kTasksPerTile;
@@ -1666,8 +1676,7 @@ __global__ void __launch_bounds__(kShadeThreads, kShadeBlocks) shade_kernel(Pass
         // tiles of ordered views with entries left for the ordered stage keep their per-sample
         // colours for it instead of resolving
         const bool keep = a.views[vi].ordered && __ldg(a.tile_cursor + gtile) != 0u;
-        shade_tile<S, TS>(a, a.views[vi], gtile, task % kTasksPerTile, scol, sdep, witems, sres + (threadIdx.x & ~31),
-                          keep);
+        shade_tile<S, TS>(a, a.views[vi], gtile, task % kTasksPerTile, scol, sdep, sres + (threadIdx.x & ~31), keep);
     }
 }
 
@@ -1721,6 +1730,7 @@ __device__ __forceinline__ int nth_set_bit(uint32_t x, int n) {
 }
 
 constexpr int kFwdFrags = 8;      // fragments a pixel holds before they are shaded (in-stage form)
+constexpr int kFwdListDefer = 2048;  // ordered entries of a tile the deferring form sorts (more: the tile is redone)
 constexpr int kFwdFragsDefer = 6; // fragments a pixel records in the deferring form (more: the tile is redone)
 constexpr int kFwdSmallBox = 24;  // candidate boxes of up to this many pixels are marked by their record's thread
 
@@ -1890,11 +1900,15 @@ __device__ __forceinline__ void forward_tile(const PassArgs& a, const FragArgs& 
         const uint32_t e = __ldg(a.pairs + beg + i);
         if ((e >> 3) >= first_ordered) {
             const int at = atomicAdd(&s_count, 1);
-            if (at < kOrderedCap) list[at] = e;
+            if (at < (DEFER ? kFwdListDefer : kOrderedCap)) list[at] = e;
         }
     }
     __syncthreads();
     int n = s_count;
+    if (DEFER && n > kFwdListDefer) {  // nothing written yet: the in-stage form sorts up to kOrderedCap
+        if (tid == 0) fa.redo_tiles[atomicAdd(a.status + ST_REDO, 1u)] = (uint32_t)gtile;
+        return;
+    }
     if (n > kOrderedCap) {  // cannot order this tile on chip: report and leave it as the prefix left it
         if (tid == 0) {
             atomicOr(a.status + ST_ORDERED_LIMIT, 1u);
@@ -2264,13 +2278,15 @@ __device__ __forceinline__ void forward_tile(const PassArgs& a, const FragArgs& 
 
 template <int S, bool DEFER>
 size_t forward_smem_bytes() {
-    return sizeof(FwdRecords) + (DEFER ? 0 : sizeof(float4) * S * kFwdThreads) + sizeof(uint32_t) * kOrderedCap +
+    return sizeof(FwdRecords) + (DEFER ? 0 : sizeof(float4) * S * kFwdThreads) +
+           sizeof(uint32_t) * (DEFER ? kFwdListDefer : kOrderedCap) +
            sizeof(int2) * (DEFER ? kFwdFragsDefer : kFwdFrags) * kFwdThreads +
            sizeof(uint32_t) * kFwdThreads * (kFwdThreads / 32);
 }
 
 // The in-stage form runs two CTAs per SM (128 registers, its shading code included); the deferring
-// form, which shades nothing, three (80 registers, 73 KB of shared memory).
+// form, which shades nothing and sorts up to kFwdListDefer entries, three (80 registers, 49 KB of
+// shared memory, which leaves the rest of the SM's 256 KB to L1).
 template <int S, bool DEFER>
 __global__ void __launch_bounds__(kFwdThreads, DEFER ? 3 : 2) forward_kernel(PassArgs a, FragArgs fa, GroupArgs g,
                                                                              int qslot, int after_raster) {
@@ -2279,7 +2295,7 @@ __global__ void __launch_bounds__(kFwdThreads, DEFER ? 3 : 2) forward_kernel(Pas
     float4* scol = reinterpret_cast<float4*>(smem_raw + sizeof(FwdRecords));  // [S][256] (not DEFER)
     uint32_t* list =
         reinterpret_cast<uint32_t*>(smem_raw + sizeof(FwdRecords) + (DEFER ? 0 : sizeof(float4) * S * kFwdThreads));
-    int2* frags = reinterpret_cast<int2*>(list + kOrderedCap);  // [fragments per pixel][256]
+    int2* frags = reinterpret_cast<int2*>(list + (DEFER ? kFwdListDefer : kOrderedCap));  // [fragments per pixel][256]
     uint32_t* cand = reinterpret_cast<uint32_t*>(frags + (DEFER ? kFwdFragsDefer : kFwdFrags) * kFwdThreads);  // [8][256]
     uint16_t* wcov = reinterpret_cast<uint16_t*>(cand);  // [8][kFwdWarpCand], aliases cand
     static_assert(sizeof(uint16_t) * kFwdWarpCand * (kFwdThreads / 32) <= sizeof(uint32_t) * kFwdThreads * (kFwdThreads / 32),

@@ -117,11 +117,13 @@ def test_many_layers_mixed_routes(S, first_blended):
     assert_parity(deferred, ref, fmt=ig.FORMAT_RGBA32F)
 
 
-@pytest.mark.parametrize("S", [1, 4])
-def test_dense_ordered_tiles_marking_and_batches(S):
+@pytest.mark.parametrize("S,blended", [(1, 4000), (4, 4000), (4, 10000)])
+def test_dense_ordered_tiles_marking_and_batches(S, blended):
     """Hundreds of small blended triangles per 16x16 tile over an opaque prefix: batches of more
     than 64 records (candidates marked from the records' side) and tiles of more than 256 ordered
-    entries (several batches), through the deferring form, the in-stage form and the oracle."""
+    entries (several batches), through the deferring form, the in-stage form and the oracle.  With
+    10,000 blended triangles the busiest tiles hold more than the 2,048 ordered entries the deferring
+    form sorts and go to the redo list whole."""
     rng = np.random.default_rng(91)
     W, H = 48, 40
     verts, tris = [], []
@@ -133,7 +135,7 @@ def test_dense_ordered_tiles_marking_and_batches(S):
         c[:, 3] = 1.0
         tris.append([len(verts), len(verts) + 1, len(verts) + 2])
         verts.extend(np.concatenate([p, c], 1))
-    for i in range(4000):  # blended: ~2-pixel triangles in front
+    for i in range(blended):  # blended: ~2-pixel triangles in front
         cx, cy = rng.uniform(-0.55, 0.55, 2)
         z = rng.uniform(-1.6, -1.2)
         p = np.array([[cx, cy, z], [cx + 0.05, cy, z], [cx, cy + 0.05, z]], np.float32)
@@ -165,7 +167,7 @@ def test_dense_ordered_tiles_marking_and_batches(S):
         st = r.stats()
         r.close()
         if capacity == -1:
-            assert st.tile_pairs > 4000  # up to 1,600 ordered entries in one tile
+            assert st.tile_pairs > blended  # 4,000 blended: up to 1,600 ordered entries in one tile
     _same(outs[0], outs[1])
     ref = O.render(odraws, W, H, S, FMT_TO_ORACLE[ig.FORMAT_RGBA32F], clear=True, clear_color=(0.1, 0.2, 0.3, 1.0),
                    nthreads=os.cpu_count() or 1)
