@@ -1413,6 +1413,94 @@ __device__ __forceinline__ int sample_entry_again(const ViewArgs& v, const KeyRu
 constexpr int kShadeThreads = 256;
 constexpr int kShadeBlocks = 4;
 
+// Per-sample slot codes of a pixel, 3 bits per sample (see shade_tile).
+template <int S>
+using SlotCodesOf = typename std::conditional<(S > 8), unsigned long long, uint32_t>::type;
+
+// The shade stage's per-pixel tail: each sample's colour from its slot (or the background), the
+// resolve (or the per-sample hand-off to the ordered stage), depth and visibility.  `uq` holds the
+// entries of slots 0..3; LATE adds samples past the U shaded slots, shaded here one by one.
+template <int S, int TS, bool LATE>
+__device__ __forceinline__ void resolve_pixel(const PassArgs& a, const ViewArgs& v, const KeyRule& rule,
+                                              SlotCodesOf<S> codes, float4 (*scol)[kShadeThreads],
+                                              float (*sdep)[kShadeThreads], int4 uq, size_t pix, int px, int py,
+                                              int ltile, int part, bool keep_samples) {
+    constexpr int U = S < 4 ? S : 4;
+    const int tid = threadIdx.x;
+    float dep[S];
+#pragma unroll
+    for (int k = 0; k < S; k++) dep[k] = ((int)(codes >> (3 * k)) & 7) < U ? sdep[k][tid] : 0.0f;
+    float bg[4];
+    if (v.clear) {
+        bg[0] = v.clear_color[0]; bg[1] = v.clear_color[1]; bg[2] = v.clear_color[2]; bg[3] = v.clear_color[3];
+    } else {
+        decode_color(v, pix, bg);
+    }
+    float acc[4];
+#pragma unroll
+    for (int k = 0; k < S; k++) {
+        float c[4];
+        const int code = (int)(codes >> (3 * k)) & 7;
+        const float d0v = v.clear ? v.clear_depth : v.depth[pix * S + k];
+        if (code == kSlotNone) {
+            c[0] = bg[0]; c[1] = bg[1]; c[2] = bg[2]; c[3] = bg[3];
+            dep[k] = d0v;
+        } else {
+            if (!LATE || code < U) {
+                float4 q = scol[code & 3][tid];
+                c[0] = q.x; c[1] = q.y; c[2] = q.z; c[3] = q.w;
+            } else {  // past the U shaded slots: shade this sample's primitive here
+                RecordPlane pl;
+                float uc[4];
+                shade_uncached(a, v.c, sample_entry_again<S>(v, rule, pix, k), px, py, uc, &pl);
+                c[0] = uc[0]; c[1] = uc[1]; c[2] = uc[2]; c[3] = uc[3];
+                dep[k] = sample_depth(pl.z0, pl.dzdx, pl.dzdy, pl.X0, pl.Y0, px * 256 + sample_x<S>(k),
+                                      py * 256 + sample_y<S>(k));
+            }
+            if (!rule.write) dep[k] = d0v;
+        }
+        if (keep_samples)  // tile-major hand-off: [tile][sample][lane], coalesced on both sides
+            v.sample_colors[((size_t)ltile * S + k) * (TS * TS) + part * 32 + (tid & 31)] = make_float4(c[0], c[1], c[2], c[3]);
+        if (k == 0) {
+            acc[0] = c[0]; acc[1] = c[1]; acc[2] = c[2]; acc[3] = c[3];
+        } else {
+            acc[0] = acc[0] + c[0]; acc[1] = acc[1] + c[1]; acc[2] = acc[2] + c[2]; acc[3] = acc[3] + c[3];
+        }
+    }
+    if (!keep_samples) {  // a tile with ordered entries is resolved by the ordered stage
+        const float invS = 1.0f / (float)S;
+        acc[0] = acc[0] * invS; acc[1] = acc[1] * invS; acc[2] = acc[2] * invS; acc[3] = acc[3] * invS;
+        encode_color(v, pix, acc);
+    }
+
+    float* dp = v.depth + pix * S;
+    if constexpr (S % 4 == 0) {
+#pragma unroll
+        for (int k = 0; k < S; k += 4) reinterpret_cast<float4*>(dp)[k / 4] = make_float4(dep[k], dep[k + 1], dep[k + 2], dep[k + 3]);
+    } else {
+#pragma unroll
+        for (int k = 0; k < S; k++) dp[k] = dep[k];
+    }
+    if (v.vis) {
+        int* vp = v.vis + pix * S;
+#pragma unroll
+        for (int k = 0; k < S; k++) {
+            const int code = (int)(codes >> (3 * k)) & 7;
+            int e = code == 0 ? uq.x : code == 1 ? uq.y : code == 2 ? uq.z : uq.w;
+            if (code == kSlotNone) e = -1;
+            else if (LATE && code >= U) e = sample_entry_again<S>(v, rule, pix, k);
+            vp[k] = e < 0 ? -1 : (e >> 3) - v.first_tri;
+        }
+    }
+}
+
+template <int S, int TS>
+__device__ __noinline__ void resolve_pixel_late(const PassArgs& a, const ViewArgs& v, KeyRule rule, SlotCodesOf<S> codes,
+                                                float4 (*scol)[kShadeThreads], float (*sdep)[kShadeThreads], int4 uq,
+                                                size_t pix, int px, int py, int ltile, int part, bool keep_samples) {
+    resolve_pixel<S, TS, true>(a, v, rule, codes, scol, sdep, uq, pix, px, py, ltile, part, keep_samples);
+}
+
 // One tile, one thread per pixel.  Each pixel lists its distinct visible entries in sample
 // order; the warp shades the (pixel, entry) items of all its lanes together (set-up straight
 // from the binner's record, the depths of the pixel's samples on that entry, quad derivatives,
@@ -1438,7 +1526,7 @@ __device__ __forceinline__ void shade_tile(const PassArgs& a, const ViewArgs& v,
     // registers across the shading loop: slot entries come back from the warp's item list, late
     // ones from memory.
     constexpr int U = S < 4 ? S : 4;  // slots shaded together across the warp
-    using SlotCodes = typename std::conditional<(S > 8), unsigned long long, uint32_t>::type;
+    using SlotCodes = SlotCodesOf<S>;
     SlotCodes codes = 0;
     int uniq[U];
 #pragma unroll
@@ -1571,75 +1659,13 @@ __device__ __forceinline__ void shade_tile(const PassArgs& a, const ViewArgs& v,
         if (b < total) scol[slot][wbase + owner] = make_float4(c[0], c[1], c[2], c[3]);
     }
     __syncwarp();
-    float dep[S];
-#pragma unroll
-    for (int k = 0; k < S; k++) dep[k] = ((int)(codes >> (3 * k)) & 7) < U ? sdep[k][tid] : 0.0f;
     if (!inpix) return;
-    float bg[4];
-    if (v.clear) {
-        bg[0] = v.clear_color[0]; bg[1] = v.clear_color[1]; bg[2] = v.clear_color[2]; bg[3] = v.clear_color[3];
-    } else {
-        decode_color(v, pix, bg);
-    }
-    float acc[4];
-#pragma unroll
-    for (int k = 0; k < S; k++) {
-        float c[4];
-        const int code = (int)(codes >> (3 * k)) & 7;
-        const float d0v = v.clear ? v.clear_depth : v.depth[pix * S + k];
-        if (code == kSlotNone) {
-            c[0] = bg[0]; c[1] = bg[1]; c[2] = bg[2]; c[3] = bg[3];
-            dep[k] = d0v;
-        } else {
-            if (code < U) {
-                float4 q = scol[code][tid];
-                c[0] = q.x; c[1] = q.y; c[2] = q.z; c[3] = q.w;
-            } else {  // more than U distinct primitives in one pixel: shade this one here
-                RecordPlane pl;
-                float uc[4];  // through memory on this rare path only
-                shade_uncached(a, v.c, sample_entry_again<S>(v, rule, pix, k), px, py, uc, &pl);
-                c[0] = uc[0]; c[1] = uc[1]; c[2] = uc[2]; c[3] = uc[3];
-                dep[k] = sample_depth(pl.z0, pl.dzdx, pl.dzdy, pl.X0, pl.Y0, px * 256 + sample_x<S>(k),
-                                      py * 256 + sample_y<S>(k));
-            }
-            if (!rule.write) dep[k] = d0v;
-        }
-        if (keep_samples)  // tile-major hand-off: [tile][sample][lane], coalesced on both sides
-            v.sample_colors[((size_t)ltile * S + k) * (TS * TS) + part * 32 + (tid & 31)] = make_float4(c[0], c[1], c[2], c[3]);
-        if (k == 0) {
-            acc[0] = c[0]; acc[1] = c[1]; acc[2] = c[2]; acc[3] = c[3];
-        } else {
-            acc[0] = acc[0] + c[0]; acc[1] = acc[1] + c[1]; acc[2] = acc[2] + c[2]; acc[3] = acc[3] + c[3];
-        }
-    }
-    if (!keep_samples) {  // a tile with ordered entries is resolved by the ordered stage
-        const float invS = 1.0f / (float)S;
-        acc[0] = acc[0] * invS; acc[1] = acc[1] * invS; acc[2] = acc[2] * invS; acc[3] = acc[3] * invS;
-        encode_color(v, pix, acc);
-    }
-
-    float* dp = v.depth + pix * S;
-    if constexpr (S % 4 == 0) {
-#pragma unroll
-        for (int k = 0; k < S; k += 4) reinterpret_cast<float4*>(dp)[k / 4] = make_float4(dep[k], dep[k + 1], dep[k + 2], dep[k + 3]);
-    } else {
-#pragma unroll
-        for (int k = 0; k < S; k++) dp[k] = dep[k];
-    }
-    if (v.vis) {
-        int* vp = v.vis + pix * S;
-#pragma unroll
-        for (int k = 0; k < S; k++) {
-            const int code = (int)(codes >> (3 * k)) & 7;
-            int e = uniq[0];
-#pragma unroll
-            for (int j = 1; j < U; j++)
-                if (code == j) e = uniq[j];
-            if (code == kSlotNone) e = -1;
-            else if (code >= U) e = sample_entry_again<S>(v, rule, pix, k);
-            vp[k] = e < 0 ? -1 : (e >> 3) - v.first_tri;
-        }
-    }
+    const int4 uq = make_int4(uniq[0], U > 1 ? uniq[U > 1 ? 1 : 0] : 0, U > 2 ? uniq[U > 2 ? 2 : 0] : 0,
+                              U > 3 ? uniq[U > 3 ? 3 : 0] : 0);
+    if (nu > U)  // more than U distinct primitives in the pixel (rare): out of line
+        resolve_pixel_late<S, TS>(a, v, rule, codes, scol, sdep, uq, pix, px, py, ltile, part, keep_samples);
+    else
+        resolve_pixel<S, TS, false>(a, v, rule, codes, scol, sdep, uq, pix, px, py, ltile, part, keep_samples);
 }
 
 // Persistent warps: each warp pulls 32-pixel tasks (8 quads of one tile) from the group's

@@ -109,6 +109,47 @@ def test_textured_trilinear_anisotropic(aniso, address):
     assert_parity(gpu, ref)
 
 
+def _pinwheels(W, H, wedges=16, radius=2.7, seed=41):
+    """Fans of `wedges` thin triangles around a centre inside a pixel, one every 6 pixels, at
+    random sub-pixel offsets, depths and rotations (NDC positions, identity transform): the centre
+    pixel's samples fall in up to min(S, wedges) different triangles."""
+    rng = np.random.default_rng(seed)
+    verts, tris = [], []
+    for cy in range(3, H - 3, 6):
+        for cx in range(3, W - 3, 6):
+            ox, oy = rng.uniform(0.3, 0.7, 2)
+            z = rng.uniform(-0.5, 0.5)
+            rot = rng.uniform(0.0, 2.0 * np.pi)
+            c = np.array([(cx + ox) / W * 2.0 - 1.0, (cy + oy) / H * 2.0 - 1.0, z])
+            base = len(verts)
+            verts.append(np.concatenate([c, rng.uniform(0, 1, 3)]))
+            for i in range(wedges):
+                a = rot + 2.0 * np.pi * i / wedges
+                q = c + np.array([radius * np.cos(a) * 2.0 / W, radius * np.sin(a) * 2.0 / H, 0.0])
+                verts.append(np.concatenate([q, rng.uniform(0, 1, 3)]))
+            for i in range(wedges):
+                tris.append([base, base + 1 + i, base + 1 + (i + 1) % wedges])
+    return np.array(verts, np.float32), np.array(tris, np.int32), np.eye(4, dtype=np.float32)
+
+
+@pytest.mark.parametrize("S", [8, 16])
+@pytest.mark.parametrize("textured", [False, True])
+def test_pixels_with_more_than_four_primitives(S, textured):
+    """Pixels whose samples see more than the four primitives the shade stage shades together:
+    the others are shaded per sample on the stage's out-of-line path."""
+    W, H = 72, 54
+    v, f, mvp = _pinwheels(W, H)
+    kw = {}
+    if textured:
+        v = np.concatenate([v[:, :3], (v[:, :2] + 1.0) * 3.0], 1)
+        kw = dict(attr=2, shading=ig.FS_TEXTURED, texture=scenes.value_noise_texture(128, 7), max_aniso=8)
+    gpu, ref, _ = render_both(v, f, mvp, W, H, S=S, cull=ig.CULL_NONE, depth_func=ig.LESS, **kw)
+    assert_parity(gpu, ref)
+    vis = gpu["vis"].reshape(-1, S)
+    distinct = np.array([len(set(r[r >= 0].tolist())) for r in vis])
+    assert (distinct > 4).sum() >= 50
+
+
 @pytest.mark.parametrize("aniso", [1, 8])
 def test_textured_clipped_triangles(aniso):
     """Camera inside a textured sphere: the triangles crossing the near plane (95 of 1,280) are
