@@ -585,22 +585,11 @@ static __device__ __noinline__ float tex_wrap_far(int mode, float v, float nf) {
     return v;
 }
 
-// Texel-space wrapping per address mode; returns false outside a clamp-to-border texture.
-// fmodf is exact, and so are the shortcuts on the ranges where they are taken (Sterbenz:
-// v - n is exact for n <= v <= 2n; for |v| < n fmodf returns v itself).
-__device__ __forceinline__ bool tex_address(int mode, float& c, float nf) {
-    float v = c;
+// Texel-space wrapping for the address modes other than repeat (mirrored repeat, clamp to
+// border, mirror once, clamp to edge); -1 outside a clamp-to-border texture.  Out of line: the
+// filter's four address computations per probe inline only the repeat mode.
+static __device__ __noinline__ float tex_address_other(int mode, float v, float nf) {
     switch (mode) {
-    case 0:
-        if (v >= 0.0f && v < nf) {
-        } else if (v >= nf && v < nf + nf) {
-            v = v - nf;
-        } else if (v < 0.0f && v > -nf) {
-            v = v + nf;
-        } else {
-            v = tex_wrap_far(0, v, nf);
-        }
-        break;
     case 1: {
         float n2 = nf + nf;
         if (v >= 0.0f && v < n2) {
@@ -613,7 +602,7 @@ __device__ __forceinline__ bool tex_address(int mode, float& c, float nf) {
         break;
     }
     case 3:
-        if (v < 0.0f || v >= nf) return false;
+        if (v < 0.0f || v >= nf) return -1.0f;
         break;
     case 4:
         v = fabsf(v);
@@ -623,6 +612,29 @@ __device__ __forceinline__ bool tex_address(int mode, float& c, float nf) {
         v = fmaxf(v, 0.0f);
         v = fminf(v, nf - 1.0f);
         break;
+    }
+    if (!(v >= 0.0f)) v = 0.0f;
+    return v;
+}
+
+// Texel-space wrapping per address mode; returns false outside a clamp-to-border texture.
+// fmodf is exact, and so are the shortcuts on the ranges where they are taken (Sterbenz:
+// v - n is exact for n <= v <= 2n; for |v| < n fmodf returns v itself).
+__device__ __forceinline__ bool tex_address(int mode, float& c, float nf) {
+    float v = c;
+    if (mode != 0) {
+        v = tex_address_other(mode, v, nf);
+        if (v < 0.0f) return false;
+        c = v;
+        return true;
+    }
+    if (v >= 0.0f && v < nf) {
+    } else if (v >= nf && v < nf + nf) {
+        v = v - nf;
+    } else if (v < 0.0f && v > -nf) {
+        v = v + nf;
+    } else {
+        v = tex_wrap_far(0, v, nf);
     }
     if (!(v >= 0.0f)) v = 0.0f;
     c = v;
@@ -758,10 +770,8 @@ __device__ __forceinline__ void tex_prepare(const DrawDev& d, float u, float v, 
     float lx2 = xu * xu + xv * xv;
     float ly2 = yu * yu + yv * yv;
     const bool aniso = d.sampler.max_aniso > 1;
-    float lam;
-    if (!aniso) {
-        lam = 0.5f * log2_series(fmaxf(lx2, ly2)) + d.sampler.lod_bias;
-    } else {
+    float lx = fmaxf(lx2, ly2);  // isotropic: lambda = log2(max(|d/dx|^2, |d/dy|^2)) / 2
+    if (aniso) {                 // anisotropic: lambda = log2(major axis / probes)
         float px = sqrtf(lx2), py = sqrtf(ly2);
         bool major_x = px >= py;
         float pmax = major_x ? px : py, pmin = major_x ? py : px;
@@ -772,10 +782,12 @@ __device__ __forceinline__ void tex_prepare(const DrawDev& d, float u, float v, 
         if (n < 1) n = 1;
         p.n = n;
         p.aniso = true;
-        lam = log2_series(pmax / (float)n) + d.sampler.lod_bias;
+        lx = pmax / (float)n;
         p.du = major_x ? dudx : dudy;
         p.dv = major_x ? dvdx : dvdy;
     }
+    const float l2 = log2_series(lx);  // one copy of the series for both cases
+    const float lam = (aniso ? l2 : 0.5f * l2) + d.sampler.lod_bias;
     const LodPick lp = pick_lod(d, lam);
     p.lo = lp.lo;
     p.hi = lp.hi;
