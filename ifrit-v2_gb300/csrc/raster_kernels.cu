@@ -1340,7 +1340,9 @@ static __device__ __noinline__ void shade_geom_general(const PassConst& c, const
 // Texture lookups of a warp's items with their probes spread over the lanes (anisotropic lookups
 // take 1 to max_aniso probes each): the calling lane's item has `n` probes described by `tp` for
 // draw `di` (n = 0: no lookup); every item adds its probes' results in probe order and, when it has
-// probes, finishes its colour `c`.  wres: 32 float4 of the warp's shared memory.  Whole warp.
+// probes, finishes its colour `c`.  wres: 32 float4 of the warp's shared memory.  ROLLED: see
+// tex_probe.  Whole warp.
+template <bool ROLLED = false>
 __device__ __forceinline__ void warp_texture_probes(const DrawDev* draws, int di, const TexProbe& tp, int n, float4* wres,
                                                     float c[4]) {
     const int lane = threadIdx.x & 31;
@@ -1376,7 +1378,7 @@ __device__ __forceinline__ void warp_texture_probes(const DrawDev* draws, int di
             q.two = (qp >> 24) & 1;
             q.aniso = (qp >> 25) & 1;
             float r[4] = {0.0f, 0.0f, 0.0f, 0.0f};
-            if (j < T) tex_probe(draws[qd], q, i, r);
+            if (j < T) tex_probe<ROLLED>(draws[qd], q, i, r);
             wres[lane] = make_float4(r[0], r[1], r[2], r[3]);
             __syncwarp();
             const int qa = max(pre, c0), qb = min(pre + n, c0 + 32);
@@ -1655,7 +1657,7 @@ __device__ __forceinline__ void shade_tile(const PassArgs& a, const ViewArgs& v,
             }
             if (shade_prepare_attrs(v.c, d, geo, t, sub, opx, opy, a0, a1, a2, c, tp)) n = tp.n;
         }
-        warp_texture_probes(a.draws, di, tp, n, wres, c);
+        warp_texture_probes<(S >= 8)>(a.draws, di, tp, n, wres, c);
         if (b < total) scol[slot][wbase + owner] = make_float4(c[0], c[1], c[2], c[3]);
     }
     __syncwarp();

@@ -795,17 +795,30 @@ __device__ __forceinline__ void tex_prepare(const DrawDev& d, float u, float v, 
     p.two = !(lp.hi == lp.lo || lp.t == 0.0f);
 }
 
-// Probe i of a prepared lookup.
+// Probe i of a prepared lookup.  ROLLED runs the two levels of the trilinear fetch through one
+// copy of the bilinear code (the same operations: level lo, then level hi lerped in), for kernels
+// bound by instruction fetch.
+template <bool ROLLED = false>
 __device__ __forceinline__ void tex_probe(const DrawDev& d, const TexProbe& p, int i, float out[4]) {
     const TexState st = tex_state(d);
-    const TexLevel L0 = tex_level(d, p.lo), L1 = tex_level(d, p.hi);
     float u = p.u, v = p.v;
     if (p.aniso) {
         const float t = (float)(i + 1) / (float)(p.n + 1) - 0.5f;
         u = u + p.du * t;
         v = v + p.dv * t;
     }
-    tex_trilinear2(L0, L1, st, p.two, p.t, u, v, out);
+    if constexpr (ROLLED) {
+        const int nl = p.two ? 2 : 1;
+#pragma unroll 1
+        for (int l = 0; l < nl; l++) {
+            float b[4];
+            tex_bilinear(tex_level(d, l == 0 ? p.lo : p.hi), st, u, v, b);
+#pragma unroll
+            for (int k = 0; k < 4; k++) out[k] = l == 0 ? b[k] : lerpf_(out[k], b[k], p.t);
+        }
+    } else {
+        tex_trilinear2(tex_level(d, p.lo), tex_level(d, p.hi), st, p.two, p.t, u, v, out);
+    }
 }
 
 // The lookup's result from its probes' in-order sum (isotropic: the single fetch).
