@@ -1419,6 +1419,29 @@ constexpr int kShadeBlocks = 4;
 template <int S>
 using SlotCodesOf = typename std::conditional<(S > 8), unsigned long long, uint32_t>::type;
 
+// The lowest bit of each of the S 3-bit slot-code fields.
+template <int S>
+__device__ __forceinline__ constexpr SlotCodesOf<S> slot_field_lows() {
+    SlotCodesOf<S> r = 0;
+    for (int k = 0; k < S; k++) r |= (SlotCodesOf<S>)1 << (3 * k);
+    return r;
+}
+
+// Sample k's offset on `axis` at run time: every position of the 8- and 16-sample patterns is a
+// multiple of 16 (1/256 pixel), so the pattern packs into 4 bits per sample and axis.
+template <int S>
+__host__ __device__ constexpr unsigned long long packed_sample_axis(int axis) {
+    unsigned long long r = 0;
+    for (int k = 0; k < S; k++) r |= (unsigned long long)(sample_pos(S, k, axis) / 16) << (4 * k);
+    return r;
+}
+template <int S>
+__device__ __forceinline__ int sample_at(int k, int axis) {
+    static_assert(S == 8 || S == 16, "packed patterns of 16 samples at most");
+    constexpr unsigned long long px = packed_sample_axis<S>(0), py = packed_sample_axis<S>(1);
+    return (int)(((axis ? py : px) >> (4 * k)) & 15u) * 16;
+}
+
 // The shade stage's per-pixel tail: each sample's colour from its slot (or the background), the
 // resolve (or the per-sample hand-off to the ordered stage), depth and visibility.  `uq` holds the
 // entries of slots 0..3; LATE adds samples past the U shaded slots, shaded here one by one.
@@ -1638,11 +1661,24 @@ __device__ __forceinline__ void shade_tile(const PassArgs& a, const ViewArgs& v,
                 plane_y = tpy;
             }
             // depths of the owner's samples on this slot, from the item's plane
+            if constexpr (S >= 8) {  // one copy of the loop body: the samples whose code is `slot`
+                const SlotCodes rep = slot_field_lows<S>();
+                const SlotCodes x = oc ^ (rep * (SlotCodes)slot);  // 0 in the fields equal to slot
+                SlotCodes m = ~(x | (x >> 1) | (x >> 2)) & rep;
+                while (m) {
+                    const int k = (S > 8 ? __ffsll((long long)m) : __ffs((int)m)) - 1;
+                    m &= m - 1;
+                    const int q = k / 3;
+                    sdep[q][wbase + owner] = sample_depth(plane.x, plane.y, plane.z, __float_as_int(plane.w), plane_y,
+                                                          opx * 256 + sample_at<S>(q, 0), opy * 256 + sample_at<S>(q, 1));
+                }
+            } else {
 #pragma unroll
-            for (int k = 0; k < S; k++)
-                if ((int)(oc >> (3 * k) & 7) == slot)
-                    sdep[k][wbase + owner] = sample_depth(plane.x, plane.y, plane.z, __float_as_int(plane.w), plane_y,
-                                                          opx * 256 + sample_x<S>(k), opy * 256 + sample_y<S>(k));
+                for (int k = 0; k < S; k++)
+                    if ((int)(oc >> (3 * k) & 7) == slot)
+                        sdep[k][wbase + owner] = sample_depth(plane.x, plane.y, plane.z, __float_as_int(plane.w), plane_y,
+                                                              opx * 256 + sample_x<S>(k), opy * 256 + sample_y<S>(k));
+            }
             float a0[4], a1[4], a2[4];
             if (from_record && a.attrs && d.shading != SHADE_PRIMID && d.attr_count > 0) {
                 const float4 q0 = __ldg(&a.attrs[g].a[0]), q1 = __ldg(&a.attrs[g].a[1]), q2 = __ldg(&a.attrs[g].a[2]);

@@ -71,7 +71,7 @@ __device__ __forceinline__ bool scissor_pass(const DrawDev& d, int x, int y) {
 // Standard sample positions in 1/256 pixel (the D3D 1/2/4/8/16x patterns): (x, y) of sample k
 // of an S-sample pixel.  With S and k compile-time constants (templated sample counts, unrolled
 // sample loops) these fold to immediates.
-__host__ __device__ __forceinline__ int sample_pos(int S, int k, int axis) {
+__host__ __device__ constexpr int sample_pos(int S, int k, int axis) {
     const int p1[2] = {128, 128};
     const int p2[4] = {192, 192, 64, 64};
     const int p4[8] = {96, 32, 224, 96, 32, 160, 160, 224};
