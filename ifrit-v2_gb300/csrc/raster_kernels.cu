@@ -1557,7 +1557,42 @@ __device__ __forceinline__ void shade_tile(const PassArgs& a, const ViewArgs& v,
 #pragma unroll
     for (int j = 0; j < U; j++) uniq[j] = 0;
     int nu = 0;
-    {
+    if constexpr (S >= 8) {
+        // one copy of the per-sample body: each sample's entry against the (at most U) entries found
+        // so far; entries past the U shaded slots are late (the same codes as the pairwise form)
+        int4 q[S / 4];
+#pragma unroll
+        for (int i = 0; i < S / 4; i++) q[i] = make_int4(-1, -1, -1, -1);
+        if (inpix && !v.keys) {
+            const int4* ep = reinterpret_cast<const int4*>(v.entries + pix * S);
+#pragma unroll
+            for (int i = 0; i < S / 4; i++) q[i] = ep[i];
+        }
+#pragma unroll 1
+        for (int k = 0; k < S; k++) {
+            int4 w = q[0];
+#pragma unroll
+            for (int i = 1; i < S / 4; i++)
+                if ((k >> 2) == i) w = q[i];
+            int e = (k & 3) == 0 ? w.x : (k & 3) == 1 ? w.y : (k & 3) == 2 ? w.z : w.w;
+            if (inpix && v.keys) e = key_entry(rule, v.keys[pix * S + k]);  // atomic visibility path
+            int code = kSlotNone;
+            if (e >= 0) {
+                code = -1;
+#pragma unroll
+                for (int j = 0; j < U; j++)
+                    if (j < nu && uniq[j] == e) code = j;
+                if (code < 0) {
+                    code = nu < U ? nu : kSlotLate;
+#pragma unroll
+                    for (int j = 0; j < U; j++)
+                        if (j == nu) uniq[j] = e;
+                    nu++;
+                }
+            }
+            codes |= (SlotCodes)code << (3 * k);
+        }
+    } else {
         int ent[S];
         if (inpix && v.keys) {  // atomic visibility path
 #pragma unroll
