@@ -1442,6 +1442,79 @@ __device__ __forceinline__ int sample_at(int k, int axis) {
     return (int)(((axis ? py : px) >> (4 * k)) & 15u) * 16;
 }
 
+// Depths of the owner pixel's samples on slot `slot` from the item's depth plane, into column `col`
+// of the per-sample depth array.
+template <int S>
+__device__ __forceinline__ void item_sample_depths(SlotCodesOf<S> oc, int slot, const float4& plane, int plane_y, int opx,
+                                                   int opy, float (*sdep)[kShadeThreads], int col) {
+    using SlotCodes = SlotCodesOf<S>;
+    if constexpr (S >= 8) {  // one copy of the loop body: the samples whose code is `slot`
+        const SlotCodes rep = slot_field_lows<S>();
+        const SlotCodes x = oc ^ (rep * (SlotCodes)slot);  // 0 in the fields equal to slot
+        SlotCodes m = ~(x | (x >> 1) | (x >> 2)) & rep;
+        while (m) {
+            const int k = (S > 8 ? __ffsll((long long)m) : __ffs((int)m)) - 1;
+            m &= m - 1;
+            const int q = k / 3;
+            sdep[q][col] = sample_depth(plane.x, plane.y, plane.z, __float_as_int(plane.w), plane_y,
+                                        opx * 256 + sample_at<S>(q, 0), opy * 256 + sample_at<S>(q, 1));
+        }
+    } else {
+#pragma unroll
+        for (int k = 0; k < S; k++)
+            if ((int)(oc >> (3 * k) & 7) == slot)
+                sdep[k][col] = sample_depth(plane.x, plane.y, plane.z, __float_as_int(plane.w), plane_y,
+                                            opx * 256 + sample_x<S>(k), opy * 256 + sample_y<S>(k));
+    }
+}
+
+// A shading item off the hot path (clipped fan triangles, LINE / POINT parts, draws without an
+// attribute record or with primitive-id shading): the general set-up and attribute fetch, out of
+// line so that the shading loop carries only the record path.  DEPTHS: also the depths of the
+// owner's samples on the item's slot (shade stage).
+struct ItemShade {
+    float c[4];
+    TexProbe tp;
+    int n;
+};
+
+template <int S, bool DEPTHS = true>
+static __device__ __noinline__ ItemShade shade_item_general(const PassArgs& a, const PassConst& pc, int di, int g, int t,
+                                                           int sub, bool from_record, int opx, int opy,
+                                                           SlotCodesOf<S> oc, int slot, float (*sdep)[kShadeThreads],
+                                                           int col) {
+    const DrawDev& d = a.draws[di];
+    ShadeGeom geo;
+    float4 plane;
+    int plane_y;
+    if (from_record && d.polygon_mode == POLY_FILL) {
+        const TriRecord* rp = a.records + g;
+        shade_geom_record(rp, __ldg(reinterpret_cast<const int4*>(rp) + 1), geo, plane, plane_y);
+    } else {
+        shade_geom_general(pc, d, a.records, g, t, sub, &geo, &plane, &plane_y);
+    }
+    if constexpr (DEPTHS) item_sample_depths<S>(oc, slot, plane, plane_y, opx, opy, sdep, col);
+    float a0[4], a1[4], a2[4];
+    if (from_record && a.attrs && d.shading != SHADE_PRIMID && d.attr_count > 0) {
+        const float4 q0 = __ldg(&a.attrs[g].a[0]), q1 = __ldg(&a.attrs[g].a[1]), q2 = __ldg(&a.attrs[g].a[2]);
+        a0[0] = q0.x; a0[1] = q0.y; a0[2] = q0.z; a0[3] = q0.w;
+        a1[0] = q1.x; a1[1] = q1.y; a1[2] = q1.z; a1[3] = q1.w;
+        a2[0] = q2.x; a2[1] = q2.y; a2[2] = q2.z; a2[3] = q2.w;
+    } else if (d.shading != SHADE_PRIMID) {
+        fetch_attrs(d, t, a0, a1, a2);
+    } else {
+#pragma unroll
+        for (int k = 0; k < 4; k++) a0[k] = a1[k] = a2[k] = 0.0f;
+    }
+    ItemShade r;
+    r.c[0] = r.c[1] = r.c[2] = r.c[3] = 0.0f;
+    r.tp.u = r.tp.v = r.tp.du = r.tp.dv = r.tp.t = 0.0f;
+    r.tp.lo = r.tp.hi = r.tp.n = 0;
+    r.tp.two = r.tp.aniso = false;
+    r.n = shade_prepare_attrs(pc, d, geo, t, sub, opx, opy, a0, a1, a2, r.c, r.tp) ? r.tp.n : 0;
+    return r;
+}
+
 // The shade stage's per-pixel tail: each sample's colour from its slot (or the background), the
 // resolve (or the per-sample hand-off to the ordered stage), depth and visibility.  `uq` holds the
 // entries of slots 0..3; LATE adds samples past the U shaded slots, shaded here one by one.
@@ -1681,52 +1754,26 @@ __device__ __forceinline__ void shade_tile(const PassArgs& a, const ViewArgs& v,
             const DrawDev& d = a.draws[di];
             const int t = g - __ldg(a.draw_start + di);
             const bool from_record = sub == 0 && (q1.z & REC_VALID);
-            ShadeGeom geo;
-            float4 plane;
-            int plane_y;
-            if (from_record && d.polygon_mode == POLY_FILL) {
+            if (from_record && d.polygon_mode == POLY_FILL && a.attrs && d.shading != SHADE_PRIMID && d.attr_count > 0) {
+                // the hot path: set-up and vertex attributes straight from the binner's records
+                ShadeGeom geo;
+                float4 plane;
+                int plane_y;
                 shade_geom_record(rp, q1, geo, plane, plane_y);
-            } else {  // through memory on this rare path only
-                ShadeGeom tg;
-                float4 tpl;
-                int tpy;
-                shade_geom_general(v.c, d, a.records, g, t, sub, &tg, &tpl, &tpy);
-                geo = tg;
-                plane = tpl;
-                plane_y = tpy;
-            }
-            // depths of the owner's samples on this slot, from the item's plane
-            if constexpr (S >= 8) {  // one copy of the loop body: the samples whose code is `slot`
-                const SlotCodes rep = slot_field_lows<S>();
-                const SlotCodes x = oc ^ (rep * (SlotCodes)slot);  // 0 in the fields equal to slot
-                SlotCodes m = ~(x | (x >> 1) | (x >> 2)) & rep;
-                while (m) {
-                    const int k = (S > 8 ? __ffsll((long long)m) : __ffs((int)m)) - 1;
-                    m &= m - 1;
-                    const int q = k / 3;
-                    sdep[q][wbase + owner] = sample_depth(plane.x, plane.y, plane.z, __float_as_int(plane.w), plane_y,
-                                                          opx * 256 + sample_at<S>(q, 0), opy * 256 + sample_at<S>(q, 1));
-                }
+                item_sample_depths<S>(oc, slot, plane, plane_y, opx, opy, sdep, wbase + owner);
+                float a0[4], a1[4], a2[4];
+                const float4 r0 = __ldg(&a.attrs[g].a[0]), r1 = __ldg(&a.attrs[g].a[1]), r2 = __ldg(&a.attrs[g].a[2]);
+                a0[0] = r0.x; a0[1] = r0.y; a0[2] = r0.z; a0[3] = r0.w;
+                a1[0] = r1.x; a1[1] = r1.y; a1[2] = r1.z; a1[3] = r1.w;
+                a2[0] = r2.x; a2[1] = r2.y; a2[2] = r2.z; a2[3] = r2.w;
+                if (shade_prepare_attrs(v.c, d, geo, t, sub, opx, opy, a0, a1, a2, c, tp)) n = tp.n;
             } else {
-#pragma unroll
-                for (int k = 0; k < S; k++)
-                    if ((int)(oc >> (3 * k) & 7) == slot)
-                        sdep[k][wbase + owner] = sample_depth(plane.x, plane.y, plane.z, __float_as_int(plane.w), plane_y,
-                                                              opx * 256 + sample_x<S>(k), opy * 256 + sample_y<S>(k));
+                const ItemShade r = shade_item_general<S>(a, v.c, di, g, t, sub, from_record, opx, opy, oc, slot, sdep,
+                                                          wbase + owner);
+                c[0] = r.c[0]; c[1] = r.c[1]; c[2] = r.c[2]; c[3] = r.c[3];
+                tp = r.tp;
+                n = r.n;
             }
-            float a0[4], a1[4], a2[4];
-            if (from_record && a.attrs && d.shading != SHADE_PRIMID && d.attr_count > 0) {
-                const float4 q0 = __ldg(&a.attrs[g].a[0]), q1 = __ldg(&a.attrs[g].a[1]), q2 = __ldg(&a.attrs[g].a[2]);
-                a0[0] = q0.x; a0[1] = q0.y; a0[2] = q0.z; a0[3] = q0.w;
-                a1[0] = q1.x; a1[1] = q1.y; a1[2] = q1.z; a1[3] = q1.w;
-                a2[0] = q2.x; a2[1] = q2.y; a2[2] = q2.z; a2[3] = q2.w;
-            } else if (d.shading != SHADE_PRIMID) {
-                fetch_attrs(d, t, a0, a1, a2);
-            } else {
-#pragma unroll
-                for (int k = 0; k < 4; k++) a0[k] = a1[k] = a2[k] = 0.0f;
-            }
-            if (shade_prepare_attrs(v.c, d, geo, t, sub, opx, opy, a0, a1, a2, c, tp)) n = tp.n;
         }
         warp_texture_probes<(S >= 8)>(a.draws, di, tp, n, wres, c);
         if (b < total) scol[slot][wbase + owner] = make_float4(c[0], c[1], c[2], c[3]);
@@ -2509,33 +2556,23 @@ __global__ void __launch_bounds__(kFragShadeThreads, 4) frag_shade_kernel(PassAr
             const PassConst& pc = a.views[d.view].c;
             const int t = g - __ldg(a.draw_start + di);
             const bool from_record = sub == 0 && (q1.z & REC_VALID);
-            ShadeGeom geo;
-            float4 plane;
-            int plane_y;
-            if (from_record && d.polygon_mode == POLY_FILL) {
+            if (from_record && d.polygon_mode == POLY_FILL && a.attrs && d.shading != SHADE_PRIMID && d.attr_count > 0) {
+                ShadeGeom geo;
+                float4 plane;
+                int plane_y;
                 shade_geom_record(rp, q1, geo, plane, plane_y);
-            } else {  // through memory on this rare path only
-                ShadeGeom tg;
-                float4 tpl;
-                int tpy;
-                shade_geom_general(pc, d, a.records, g, t, sub, &tg, &tpl, &tpy);
-                geo = tg;
-            }
-            (void)plane;
-            (void)plane_y;
-            float a0[4], a1[4], a2[4];
-            if (from_record && a.attrs && d.shading != SHADE_PRIMID && d.attr_count > 0) {
+                float a0[4], a1[4], a2[4];
                 const float4 r0 = __ldg(&a.attrs[g].a[0]), r1 = __ldg(&a.attrs[g].a[1]), r2 = __ldg(&a.attrs[g].a[2]);
                 a0[0] = r0.x; a0[1] = r0.y; a0[2] = r0.z; a0[3] = r0.w;
                 a1[0] = r1.x; a1[1] = r1.y; a1[2] = r1.z; a1[3] = r1.w;
                 a2[0] = r2.x; a2[1] = r2.y; a2[2] = r2.z; a2[3] = r2.w;
-            } else if (d.shading != SHADE_PRIMID) {
-                fetch_attrs(d, t, a0, a1, a2);
+                if (shade_prepare_attrs(pc, d, geo, t, sub, px, py, a0, a1, a2, c, tp)) np = tp.n;
             } else {
-#pragma unroll
-                for (int k = 0; k < 4; k++) a0[k] = a1[k] = a2[k] = 0.0f;
+                const ItemShade r = shade_item_general<1, false>(a, pc, di, g, t, sub, from_record, px, py, 0u, 0, nullptr, 0);
+                c[0] = r.c[0]; c[1] = r.c[1]; c[2] = r.c[2]; c[3] = r.c[3];
+                tp = r.tp;
+                np = r.n;
             }
-            if (shade_prepare_attrs(pc, d, geo, t, sub, px, py, a0, a1, a2, c, tp)) np = tp.n;
         }
         warp_texture_probes(a.draws, di, tp, np, s_res[warp], c);
         if (i < n) fa.frag_cols[i] = make_float4(c[0], c[1], c[2], c[3]);
