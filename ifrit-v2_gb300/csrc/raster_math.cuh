@@ -980,20 +980,13 @@ __device__ __forceinline__ bool shade_prepare_attrs(const PassConst& c, const Dr
     return false;
 }
 
+// Blend factor f of channel ch (0 zero, 1 one, 2 / 3 source colour, 4 / 5 destination colour, 6 / 7
+// source alpha, 8 / 9 destination alpha, the odd ones as one minus it; anything else zero), by
+// selects rather than a branch per factor.
 __device__ __forceinline__ float blend_factor(int f, int ch, const float* src, const float* dst) {
-    switch (f) {
-    case 0: return 0.0f;
-    case 1: return 1.0f;
-    case 2: return src[ch];
-    case 3: return 1.0f - src[ch];
-    case 4: return dst[ch];
-    case 5: return 1.0f - dst[ch];
-    case 6: return src[3];
-    case 7: return 1.0f - src[3];
-    case 8: return dst[3];
-    case 9: return 1.0f - dst[3];
-    default: return 0.0f;
-    }
+    const float x = f <= 3 ? src[ch] : f <= 5 ? dst[ch] : f <= 7 ? src[3] : dst[3];
+    const float v = (f & 1) ? 1.0f - x : x;
+    return (unsigned)f > 9u || f == 0 ? 0.0f : f == 1 ? 1.0f : v;
 }
 
 __device__ __forceinline__ void blend_into(const DrawDev& d, const float* src, float* dst) {
