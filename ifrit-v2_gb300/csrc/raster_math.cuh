@@ -517,17 +517,13 @@ __device__ __forceinline__ float sample_depth(float z0, float dzdx, float dzdy, 
     return (z0 + dzdx * (float)(x - X0)) + dzdy * (float)(y - Y0);
 }
 
+// Depth test by compare op (0 never, 1 less, 2 equal, 3 less or equal, 4 greater, 5 not equal,
+// 6 greater or equal, anything else always): bit 0 passes on less, bit 1 on equal, bit 2 on greater;
+// unordered operands (NaN) pass only "not equal" and "always".  Selects, no branch per op.
 __device__ __forceinline__ bool depth_cmp(int func, float z, float dd) {
-    switch (func) {
-    case 0: return false;
-    case 1: return z < dd;
-    case 2: return z == dd;
-    case 3: return z <= dd;
-    case 4: return z > dd;
-    case 5: return z != dd;
-    case 6: return z >= dd;
-    default: return true;
-    }
+    const bool lt = z < dd, eq = z == dd, gt = z > dd;
+    const bool pass = ((func & 1) && lt) || ((func & 2) && eq) || ((func & 4) && gt);
+    return (unsigned)func >= 7u || pass || (func == 5 && !(lt || eq || gt));
 }
 
 // ------------------------------------------------------------------ log2 (own atanh series)
