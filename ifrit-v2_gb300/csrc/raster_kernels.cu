@@ -949,19 +949,21 @@ __device__ __forceinline__ void raster_depth(const ViewArgs& v, const KeyRule& r
     // (float)(sx - X0) == fbx + sample offset exactly: every term is an integer below
     // 2^24 in magnitude (guard-band bound), so no conversion per sample is needed.
     const float fbx = (float)(gx * 256 - X0), fby = (float)(gy * 256 - Y0);
+    if (rule.explicit_) {  // pass decided by a compare against the initial depth (rare): depth word 0
+#pragma unroll 1
+        for (unsigned m = cov; m; m &= m - 1) {
+            const int k = __ffs((int)m) - 1;
+            const float z = (z0 + gzx * (fbx + (float)sample_at<S>(k, 0))) + gzy * (fby + (float)sample_at<S>(k, 1));
+            if (depth_cmp(rule.func, z, d0_of(v, gx, gy, k))) atomicMin(kp + k * (TS * TS), (unsigned long long)lo_word);
+        }
+        return;
+    }
 #pragma unroll
     for (int k = 0; k < S; k++) {
         if (!(cov & (1u << k))) continue;
         const float z = (z0 + gzx * (fbx + (float)sample_x<S>(k))) + gzy * (fby + (float)sample_y<S>(k));
-        uint32_t hi_word;
-        if (rule.explicit_) {
-            if (!depth_cmp(rule.func, z, d0_of(v, gx, gy, k))) continue;
-            hi_word = 0u;
-        } else {
-            hi_word = rule.invert ? ~depth_order(z) : depth_order(z);
-        }
-        const unsigned long long kv = ((unsigned long long)hi_word << 32) | lo_word;
-        atomicMin(kp + k * (TS * TS), kv);
+        const uint32_t hi_word = rule.invert ? ~depth_order(z) : depth_order(z);
+        atomicMin(kp + k * (TS * TS), ((unsigned long long)hi_word << 32) | lo_word);
     }
 }
 
@@ -1425,21 +1427,6 @@ __device__ __forceinline__ constexpr SlotCodesOf<S> slot_field_lows() {
     SlotCodesOf<S> r = 0;
     for (int k = 0; k < S; k++) r |= (SlotCodesOf<S>)1 << (3 * k);
     return r;
-}
-
-// Sample k's offset on `axis` at run time: every position of the 8- and 16-sample patterns is a
-// multiple of 16 (1/256 pixel), so the pattern packs into 4 bits per sample and axis.
-template <int S>
-__host__ __device__ constexpr unsigned long long packed_sample_axis(int axis) {
-    unsigned long long r = 0;
-    for (int k = 0; k < S; k++) r |= (unsigned long long)(sample_pos(S, k, axis) / 16) << (4 * k);
-    return r;
-}
-template <int S>
-__device__ __forceinline__ int sample_at(int k, int axis) {
-    static_assert(S == 8 || S == 16, "packed patterns of 16 samples at most");
-    constexpr unsigned long long px = packed_sample_axis<S>(0), py = packed_sample_axis<S>(1);
-    return (int)(((axis ? py : px) >> (4 * k)) & 15u) * 16;
 }
 
 // Depths of the owner pixel's samples on slot `slot` from the item's depth plane, into column `col`

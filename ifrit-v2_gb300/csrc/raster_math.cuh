@@ -86,6 +86,30 @@ __device__ __forceinline__ int sample_x(int k) { return sample_pos(S, k, 0); }
 template <int S>
 __device__ __forceinline__ int sample_y(int k) { return sample_pos(S, k, 1); }
 
+// Sample k's offset on `axis` at run time: every position of the sample patterns is a multiple of 16
+// (1/256 pixel), so a pattern packs into 4 bits per sample and axis.
+__host__ __device__ constexpr bool sample_patterns_pack() {
+    for (int S = 1; S <= 16; S *= 2)
+        for (int k = 0; k < S; k++)
+            for (int axis = 0; axis < 2; axis++)
+                if (sample_pos(S, k, axis) % 16 != 0) return false;
+    return true;
+}
+static_assert(sample_patterns_pack(), "every sample position is a multiple of 1/16 pixel");
+
+template <int S>
+__host__ __device__ constexpr unsigned long long packed_sample_axis(int axis) {
+    unsigned long long r = 0;
+    for (int k = 0; k < S; k++) r |= (unsigned long long)(sample_pos(S, k, axis) / 16) << (4 * k);
+    return r;
+}
+template <int S>
+__device__ __forceinline__ int sample_at(int k, int axis) {
+    static_assert(S <= 16, "packed patterns of 16 samples at most");
+    constexpr unsigned long long px = packed_sample_axis<S>(0), py = packed_sample_axis<S>(1);
+    return (int)(((axis ? py : px) >> (4 * k)) & 15u) * 16;
+}
+
 // Attributes are evaluated at the pixel centre (1/256-pixel units).
 constexpr int kShadeOffset = 128;
 
