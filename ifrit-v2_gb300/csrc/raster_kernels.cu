@@ -2418,10 +2418,11 @@ size_t forward_smem_bytes() {
 }
 
 // The in-stage form runs two CTAs per SM (128 registers, its shading code included); the deferring
-// form, which shades nothing and sorts up to kFwdListDefer entries, three (80 registers, 49 KB of
-// shared memory, which leaves the rest of the SM's 256 KB to L1).
+// form, which shades nothing and sorts up to kFwdListDefer entries, four up to 8 samples (64 registers,
+// 49 KB of shared memory each; measured faster than three at 80 registers despite the spills) and three
+// at 16 (whose spills at 64 registers would be larger).
 template <int S, bool DEFER>
-__global__ void __launch_bounds__(kFwdThreads, DEFER ? 3 : 2) forward_kernel(PassArgs a, FragArgs fa, GroupArgs g,
+__global__ void __launch_bounds__(kFwdThreads, DEFER ? (S <= 8 ? 4 : 3) : 2) forward_kernel(PassArgs a, FragArgs fa, GroupArgs g,
                                                                              int qslot, int after_raster) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     FwdRecords& rec = *reinterpret_cast<FwdRecords*>(smem_raw);
