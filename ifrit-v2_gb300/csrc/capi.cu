@@ -335,7 +335,8 @@ int scratch_reserve(IfritGbRenderer* h, PassScratch& s, size_t tiles, size_t tri
         s.tiles_alloc = n;
         s.generation++;
     }
-    IFTR_CUDA(h, grow(s.records, std::max<size_t>(1, tris) * sizeof(ifr::TriRecord)));
+    // the records, then one 8-byte bin word per triangle (written by the counting pass)
+    IFTR_CUDA(h, grow(s.records, std::max<size_t>(1, tris) * (sizeof(ifr::TriRecord) + sizeof(uint2))));
     IFTR_CUDA(h, grow(s.attrs, std::max<size_t>(1, tris) * sizeof(ifr::TriAttr)));
     if (ndraws > s.cap_draws || nviews > s.cap_views || !s.desc.p) {
         s.cap_draws = std::max(s.cap_draws, std::max<size_t>(1, ndraws + ndraws / 4));

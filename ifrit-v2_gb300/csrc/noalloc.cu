@@ -35,7 +35,8 @@ constexpr size_t kOffTileCursor = kOffTileOffset + align256((size_t)(IFTR_NOALLO
 constexpr size_t kOffBlockSums = kOffTileCursor + align256((size_t)IFTR_NOALLOC_MAX_TILES * 4);
 constexpr size_t kOffPairs = kOffBlockSums + align256((size_t)ifr::scan_blocks(IFTR_NOALLOC_MAX_TILES) * 4);
 constexpr size_t kOffRecords = kOffPairs + align256((size_t)IFTR_NOALLOC_MAX_TILE_PAIRS * 4);
-constexpr size_t kOffEntries = kOffRecords + align256((size_t)IFTR_NOALLOC_MAX_TRIANGLES * sizeof(ifr::TriRecord));
+constexpr size_t kOffEntries =
+    kOffRecords + align256((size_t)IFTR_NOALLOC_MAX_TRIANGLES * (sizeof(ifr::TriRecord) + sizeof(uint2)));  // + bin words
 constexpr size_t kScratchEnd = kOffEntries + align256((size_t)IFTR_NOALLOC_MAX_SAMPLES * 4);
 static_assert(kScratchEnd <= IFTR_NOALLOC_SCRATCH_BYTES, "scratch layout exceeds IFTR_NOALLOC_SCRATCH_BYTES");
 

@@ -74,6 +74,9 @@ __device__ __forceinline__ void bin_sub(const PassArgs& a, const ViewArgs& v, co
 // Front end of triangle g (draw di), shared by the counting binner and the atomic visibility
 // path: fetch, transform, clip and set-up; writes the triangle's record (and vertex attributes)
 // and hands every visible (sub-)triangle to emit(view, draw, sub-triangle, entry).
+// What the counting pass leaves the scattering pass for a triangle (see bin_words).
+enum BinKind { BIN_NONE = 0, BIN_RANGE = 1, BIN_CLIPPED = 2, BIN_MODE = 3 };
+
 template <class Emit>
 __device__ __forceinline__ void front_end(const PassArgs& a, int g, int di, const Emit& emit) {
     const DrawDev& d = a.draws[di];
@@ -82,16 +85,12 @@ __device__ __forceinline__ void front_end(const PassArgs& a, int g, int di, cons
     CVert poly[3];  // registers: only the rare clipping path below goes through memory
     bool inside, rejected;
     TriRecord* rec = a.records + g;
-    if (!fetch_triangle(v.c, d, t, poly, inside, rejected)) {
-        rec->flags = 0;
-        return;
-    }
+    // culled triangles leave their record untouched: only binned entries' records are read
+    if (!fetch_triangle(v.c, d, t, poly, inside, rejected)) return;
     if (d.polygon_mode != POLY_FILL) {  // LINE / POINT: record the projected triangle, emit its parts
         SubTri tri;
-        if (!inside || !project_oriented(v.c, d, poly, tri)) {
-            rec->flags = 0;
-            return;
-        }
+        if (!inside || !project_oriented(v.c, d, poly, tri)) return;
+        emit.mark(BIN_MODE);
         TriRecord r;
         mode_record_from_tri(tri, r);
         r.draw = di;
@@ -114,10 +113,7 @@ __device__ __forceinline__ void front_end(const PassArgs& a, int g, int di, cons
     }
     if (inside) {
         SubTri s;
-        if (!setup_sub(v.c, d, poly[0], poly[1], poly[2], s)) {
-            rec->flags = 0;
-            return;
-        }
+        if (!setup_sub(v.c, d, poly[0], poly[1], poly[2], s)) return;
         TriRecord r;
         record_from_sub(s, r);
         r.draw = di;
@@ -135,6 +131,7 @@ __device__ __forceinline__ void front_end(const PassArgs& a, int g, int di, cons
         emit(v, d, s, (uint32_t)g << 3);
         return;
     }
+    emit.mark(BIN_CLIPPED);
     rec->flags = REC_CLIPPED;
     rec->draw = di;
     CVert clip[kMaxPoly];
@@ -153,13 +150,20 @@ __device__ __forceinline__ void front_end(const PassArgs& a, int g, int di, cons
 constexpr int kWarpTiles = 4;
 struct WarpTiles {
     bool big, small;
+    int kind;  // BIN_MODE / BIN_CLIPPED: the scattering pass re-emits the triangle's parts itself
     int tx0, tx1, ty0, ty1, tbase, tiles_x;
     uint32_t entry;  // list entry of a small range
 };
 
+// Bin word of every triangle of the pass (8 bytes, after the records in the same allocation), written
+// by the counting pass so that the scattering pass need not read the records back:
+//   x = tx0 | tx1 << 16, y = ty0 | ty1 << 14 | kind << 28 (the tile range, for BIN_RANGE).
+__device__ __forceinline__ uint2* bin_words(const PassArgs& a) { return reinterpret_cast<uint2*>(a.records + a.total_tris); }
+
 struct CountEmit {
     const PassArgs& a;
     WarpTiles& w;
+    __device__ void mark(int kind) const { w.kind = kind; }
     __device__ void operator()(const ViewArgs& v, const DrawDev& d, const SubTri& s, uint32_t entry) const {
         SubTri c = s;
         if (w.big || w.small) {  // a second fan triangle of a clipped triangle (rare): direct atomics
@@ -280,29 +284,46 @@ __global__ void __launch_bounds__(256) bin_count_kernel(PassArgs a) {
     const int di = find_draw_warp(a, min(g, a.total_tris - 1));
     WarpTiles w;
     w.big = w.small = false;
-    if (g < a.total_tris) front_end(a, g, di, CountEmit{a, w});
+    w.kind = BIN_NONE;
+    if (g < a.total_tris) {
+        front_end(a, g, di, CountEmit{a, w});
+        uint2 b = make_uint2(0u, (uint32_t)w.kind << 28);
+        if (w.kind == BIN_NONE && (w.small || w.big))
+            b = make_uint2((uint32_t)w.tx0 | ((uint32_t)w.tx1 << 16),
+                           (uint32_t)w.ty0 | ((uint32_t)w.ty1 << 14) | ((uint32_t)BIN_RANGE << 28));
+        bin_words(a)[g] = b;
+    }
     if (w.small)  // counts need no result back: one fire-and-forget reduction per tile
         for (int ty = w.ty0; ty <= w.ty1; ty++)
             for (int tx = w.tx0; tx <= w.tx1; tx++) atomicAdd(a.tile_count + w.tbase + ty * w.tiles_x + tx, 1u);
     warp_tiles(a, w, g, false);
 }
 
-// Scattering pass: same overlaps as the counting pass, read back from the records (clipped
-// triangles run the front end again).  Every list slot comes from an atomicAdd whose result the
+// Scattering pass: same overlaps as the counting pass, from its bin words (clipped triangles run the
+// front end again, LINE / POINT parts come from their records).  Every list slot comes from an atomicAdd whose result the
 // store waits for, so a triangle over many tiles would serialise hundreds of round trips in one
 // thread: the tile ranges of unclipped triangles over more than kWarpTiles tiles are walked by the
 // whole warp instead, and the smaller ones take their slots through warp-aggregated atomics.
 __global__ void __launch_bounds__(256) bin_scatter_kernel(PassArgs a) {
     const int g = blockIdx.x * blockDim.x + threadIdx.x;
+    const int di = find_draw_warp(a, min(g, a.total_tris - 1));
     WarpTiles w;
     w.big = w.small = false;
     if (g < a.total_tris && !a.status[ST_OVERFLOW]) {
-        const int flags = __ldg(&a.records[g].flags);
-        if (flags & (REC_VALID | REC_CLIPPED)) {
-            const int di = record_draw(a, g);
+        const uint2 b = bin_words(a)[g];
+        const int kind = (int)(b.y >> 28);
+        if (kind != BIN_NONE) {
             const DrawDev& d = a.draws[di];
             const ViewArgs& v = a.views[d.view];
-            if (d.polygon_mode != POLY_FILL) {
+            if (kind == BIN_RANGE) {  // the counting pass's tile range
+                w.tx0 = (int)(b.x & 0xffffu); w.tx1 = (int)(b.x >> 16);
+                w.ty0 = (int)(b.y & 0x3fffu); w.ty1 = (int)((b.y >> 14) & 0x3fffu);
+                w.tbase = v.tile_start;
+                w.tiles_x = v.c.tiles_x;
+                w.entry = (uint32_t)g << 3;
+                w.big = (w.tx1 - w.tx0 + 1) * (w.ty1 - w.ty0 + 1) > kWarpTiles;
+                w.small = !w.big;
+            } else if (kind == BIN_MODE) {
                 SubTri tri;
                 tri_from_mode_record(a.records + g, tri);
                 for (int sub = 0; sub < 6; sub++) {
@@ -310,19 +331,7 @@ __global__ void __launch_bounds__(256) bin_scatter_kernel(PassArgs a) {
                     if (mode_sub(v.c, d.polygon_mode, tri, sub, s))
                         bin_sub(a, v, d, s, ((uint32_t)g << 3) | (uint32_t)sub, true);
                 }
-            } else if (flags & REC_VALID) {
-                SubTri s;
-                if (sub_from_record(v.c, a.records + g, s) && scissor_clamp(d, s)) {
-                    const int sh = v.c.tile_shift;
-                    w.tx0 = s.px0 >> sh; w.tx1 = s.px1 >> sh;
-                    w.ty0 = s.py0 >> sh; w.ty1 = s.py1 >> sh;
-                    w.tbase = v.tile_start;
-                    w.tiles_x = v.c.tiles_x;
-                    w.entry = (uint32_t)g << 3;
-                    w.big = (w.tx1 - w.tx0 + 1) * (w.ty1 - w.ty0 + 1) > kWarpTiles;
-                    w.small = !w.big;
-                }
-            } else {
+            } else {  // clipped: the front end again
                 const int t = g - __ldg(a.draw_start + di);
                 CVert poly[kMaxPoly];
                 bool inside, rejected;
@@ -657,6 +666,7 @@ __global__ void __launch_bounds__(256) init_keys_kernel(PassArgs a, int npix) {
 
 template <int S>
 struct GlobalRasterEmit {
+    __device__ void mark(int) const {}
     __device__ void operator()(const ViewArgs& v, const DrawDev& d, SubTri s, uint32_t entry) const {
         if (!scissor_clamp(d, s)) return;
         const KeyRule rule = key_rule(v.depth_func, v.depth_write);
