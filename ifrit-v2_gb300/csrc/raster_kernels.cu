@@ -2679,6 +2679,22 @@ __global__ void __launch_bounds__(kFwdThreads, blend_min_blocks<S>()) frag_blend
                 const float4 q = fa.frag_cols[f];
                 const float c[4] = {q.x, q.y, q.z, q.w};
                 const DrawDev& d = a.draws[r.w];
+                if (d.blend_enable && !blend_reads_dst(d)) {
+                    // factors of the source only (alpha blending): once per fragment
+                    float fs[4], fd[4];
+#pragma unroll
+                    for (int ch = 0; ch < 4; ch++) {
+                        fs[ch] = blend_factor(ch < 3 ? d.blend_src_color : d.blend_src_alpha, ch, c, c);
+                        fd[ch] = blend_factor(ch < 3 ? d.blend_dst_color : d.blend_dst_alpha, ch, c, c);
+                    }
+                    for (uint32_t m = r.z; m; m &= m - 1) {
+                        const int k = __ffs(m) - 1;
+                        const float4 o = col[k * NT];
+                        col[k * NT] = make_float4(o.x * fd[0] + c[0] * fs[0], o.y * fd[1] + c[1] * fs[1],
+                                                  o.z * fd[2] + c[2] * fs[2], o.w * fd[3] + c[3] * fs[3]);
+                    }
+                    continue;
+                }
                 for (uint32_t m = r.z; m; m &= m - 1) {  // the covered samples, one copy of the blend code
                     const int k = __ffs(m) - 1;
                     if (d.blend_enable) {

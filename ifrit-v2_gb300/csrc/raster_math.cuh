@@ -1009,6 +1009,12 @@ __device__ __forceinline__ float blend_factor(int f, int ch, const float* src, c
     return (unsigned)f > 9u || f == 0 ? 0.0f : f == 1 ? 1.0f : v;
 }
 
+// Whether any of the draw's four blend factors reads the destination colour (codes 4, 5, 8, 9).
+__device__ __forceinline__ bool blend_reads_dst(const DrawDev& d) {
+    auto reads = [](int f) { return f == 4 || f == 5 || f == 8 || f == 9; };
+    return reads(d.blend_src_color) || reads(d.blend_dst_color) || reads(d.blend_src_alpha) || reads(d.blend_dst_alpha);
+}
+
 __device__ __forceinline__ void blend_into(const DrawDev& d, const float* src, float* dst) {
     float out[4];
 #pragma unroll
