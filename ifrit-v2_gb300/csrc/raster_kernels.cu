@@ -1894,6 +1894,22 @@ __device__ __forceinline__ void apply_fragment(const PassArgs& a, const ViewArgs
     shade_uncached(a, v.c, f.x, px, py, c, &pl);
     const DrawDev& d = a.draws[(unsigned)f.y >> 16];
     const unsigned mask = (unsigned)f.y & 0xffffu;
+    if (d.blend_enable && !blend_reads_dst(d)) {  // factors of the source only: once per fragment
+        float fs[4], fd[4];
+#pragma unroll
+        for (int ch = 0; ch < 4; ch++) {
+            fs[ch] = blend_factor(ch < 3 ? d.blend_src_color : d.blend_src_alpha, ch, c, c);
+            fd[ch] = blend_factor(ch < 3 ? d.blend_dst_color : d.blend_dst_alpha, ch, c, c);
+        }
+#pragma unroll
+        for (int k = 0; k < S; k++) {
+            if (!(mask & (1u << k))) continue;
+            float4& sc = scol[k * NT + threadIdx.x];
+            sc = make_float4(sc.x * fd[0] + c[0] * fs[0], sc.y * fd[1] + c[1] * fs[1], sc.z * fd[2] + c[2] * fs[2],
+                             sc.w * fd[3] + c[3] * fs[3]);
+        }
+        return;
+    }
 #pragma unroll
     for (int k = 0; k < S; k++) {
         if (!(mask & (1u << k))) continue;
