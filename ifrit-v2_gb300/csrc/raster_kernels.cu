@@ -2220,11 +2220,13 @@ __device__ __forceinline__ void forward_tile(const PassArgs& a, const FragArgs& 
             const int func = (meta >> 1) & 7, write = (meta >> 4) & 1;
             const int e = rec.key[r];
             unsigned mask = 0;
+            // (float)(sx - X0) == fbx + sample offset exactly (integers below 2^24), as in raster_depth
+            const float z0 = rec.z0[r], gzx = rec.dzdx[r], gzy = rec.dzdy[r];
+            const float fbx = (float)(px * 256 - rec.X0[r]), fby = (float)(py * 256 - rec.Y0[r]);
 #pragma unroll
             for (int k = 0; k < S; k++) {
-                const int32_t sx = px * 256 + sample_x<S>(k), sy = py * 256 + sample_y<S>(k);
                 if (!(cov & (1u << k))) continue;
-                const float z = sample_depth(rec.z0[r], rec.dzdx[r], rec.dzdy[r], rec.X0[r], rec.Y0[r], sx, sy);
+                const float z = (z0 + gzx * (fbx + (float)sample_x<S>(k))) + gzy * (fby + (float)sample_y<S>(k));
                 if (!depth_cmp(func, z, dep[k])) continue;
                 if (write) {
                     dep_changed |= __float_as_uint(dep[k]) != __float_as_uint(z);
