@@ -304,7 +304,8 @@ __global__ void __launch_bounds__(256) bin_count_kernel(PassArgs a) {
 // store waits for, so a triangle over many tiles would serialise hundreds of round trips in one
 // thread: the tile ranges of unclipped triangles over more than kWarpTiles tiles are walked by the
 // whole warp instead, and the smaller ones take their slots through warp-aggregated atomics.
-__global__ void __launch_bounds__(256) bin_scatter_kernel(PassArgs a) {
+// Eight CTAs per SM (32 registers): the kernel waits on its slot atomics, and more warps hide them.
+__global__ void __launch_bounds__(256, 8) bin_scatter_kernel(PassArgs a) {
     const int g = blockIdx.x * blockDim.x + threadIdx.x;
     const int di = find_draw_warp(a, min(g, a.total_tris - 1));
     WarpTiles w;
