@@ -300,11 +300,12 @@ __global__ void __launch_bounds__(256) bin_count_kernel(PassArgs a) {
 }
 
 // Scattering pass: same overlaps as the counting pass, from its bin words (clipped triangles run the
-// front end again, LINE / POINT parts come from their records).  Every list slot comes from an atomicAdd whose result the
-// store waits for, so a triangle over many tiles would serialise hundreds of round trips in one
-// thread: the tile ranges of unclipped triangles over more than kWarpTiles tiles are walked by the
-// whole warp instead, and the smaller ones take their slots through warp-aggregated atomics.
-// Eight CTAs per SM (32 registers): the kernel waits on its slot atomics, and more warps hide them.
+// front end again, LINE / POINT parts come from their records).  Every list slot comes from an
+// atomicAdd whose result the store waits for, so a triangle over many tiles would serialise hundreds of
+// round trips in one thread: the tile ranges of unclipped triangles over more than kWarpTiles tiles are
+// walked by the whole warp instead, and the smaller ones take their slots through warp-aggregated
+// atomics.  Eight CTAs per SM (32 registers): the kernel waits on its slot atomics, and more warps hide
+// them.
 __global__ void __launch_bounds__(256, 8) bin_scatter_kernel(PassArgs a) {
     const int g = blockIdx.x * blockDim.x + threadIdx.x;
     const int di = find_draw_warp(a, min(g, a.total_tris - 1));
@@ -1618,9 +1619,9 @@ __device__ __forceinline__ void shade_tile(const PassArgs& a, const ViewArgs& v,
     const KeyRule rule = key_rule(v.depth_func, v.depth_write);
     // Distinct visible entries of this pixel, in sample order, and each sample's 3-bit slot code:
     // 0..U-1 its list slot, kSlotLate for entries past the U shaded together (shaded on their own
-    // after the warp's items), kSlotNone for no visible entry.  Only the packed codes stay in
-    // registers across the shading loop: slot entries come back from the warp's item list, late
-    // ones from memory.
+    // after the warp's items), kSlotNone for no visible entry.  Per-sample entries do not stay in
+    // registers across the shading loop: the slots' entries (uniq) reach the item lanes by shuffles,
+    // late ones are read again from memory.
     constexpr int U = S < 4 ? S : 4;  // slots shaded together across the warp
     using SlotCodes = SlotCodesOf<S>;
     SlotCodes codes = 0;
