@@ -157,7 +157,8 @@ struct WarpTiles {
 
 // Bin word of every triangle of the pass (8 bytes, after the records in the same allocation), written
 // by the counting pass so that the scattering pass need not read the records back:
-//   x = tx0 | tx1 << 16, y = ty0 | ty1 << 14 | kind << 28 (the tile range, for BIN_RANGE).
+//   x = tx0 | tx1 << 16, y = ty0 | ty1 << 14 | kind << 28 (the tile range, for BIN_RANGE); tile
+//   coordinates stay below 2^11 (targets of at most 16384 pixels, tiles of at least 8).
 __device__ __forceinline__ uint2* bin_words(const PassArgs& a) { return reinterpret_cast<uint2*>(a.records + a.total_tris); }
 
 struct CountEmit {
