@@ -123,6 +123,19 @@ def profiled_traffic(name):
     return None
 
 
+def profiled_issue(name):
+    """Fraction of issue slots each dominant tile kernel used (ncu sm__issue_active) in the committed
+    summary, if present: the bound of these instruction-issue-bound kernels beside the DRAM roofline."""
+    path = os.path.join(ROOT, "profiles", "tile_kernel_%s.txt" % name)
+    try:
+        for line in open(path):
+            if line.startswith("issue_active_per_kernel:"):
+                return {k: float(v) for k, v in (kv.split("=") for kv in line.split(":", 1)[1].split())}
+    except (OSError, ValueError):
+        pass
+    return None
+
+
 class ClockSampler:
     FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
@@ -807,7 +820,8 @@ def run_ours_c5(args):
                          "binning_count_scan_scatter": st[:3]},
             "roofline": {"bound": "hbm", "achieved": B / t_tile / 1e9, "peak": peak, "unit": "GB/s",
                          "frac": B / t_tile / 1e9 / peak, "traffic": profiled_traffic("c5"), "algorithmic_bytes": B,
-                         "kernel": "tile stage (raster + shade + ordered kernels)", "peak_source": peak_kind},
+                         "kernel": "tile stage (raster + shade + ordered kernels)", "peak_source": peak_kind,
+                         "issue_active": profiled_issue("c5")},
             "pass_roofline_frac": B / (m / 1000.0) / 1e9 / peak,
             "e2e": {"value": world * shaded / e2e_s, "unit": "samples/s",
                     "h2d_bytes_per_step": int(sc["vertices"].nbytes + sc["indices"].nbytes),
@@ -963,7 +977,8 @@ def measure_frame(w, steps, warmup, e2e_steps, dist=None, world=1, separate_brea
                      "binning_count_scan_scatter": [statistics.mean(x[i] for x in bin_parts) for i in range(3)]},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": profiled_traffic(w["name"]), "algorithmic_bytes": B,
-                     "kernel": "tile stage (raster + shade kernels)", "peak_source": peak_kind},
+                     "kernel": "tile stage (raster + shade kernels)", "peak_source": peak_kind,
+                     "issue_active": profiled_issue(w["name"])},
         "pass_roofline_frac": B / (ms / 1000.0) / 1e9 / peak,
         "e2e": {"value": world * shaded / e2e_s, "unit": "samples/s",
                 "h2d_bytes_per_step": int(w["vertices"].nbytes + w["indices"].nbytes),
